@@ -1,0 +1,152 @@
+/*
+ * smoke_gb300.h -- C ABI of libsmoke_gb300, a GB300-native (sm_103a) implementation of the
+ * semi-Lagrangian smoke step of RasmusAlmryd/smoke-simulation on a staggered MAC grid.
+ *
+ * The reference exposes one implicit simulation through ten C++ free functions
+ * (project/smokeSimulation.cuh:4-17).  This ABI keeps the same operations but with an explicit
+ * handle, status codes instead of exit(-1), and stream-ordered steps.  The reference's own
+ * C++ signatures are also exported by the library (include/smokeSimulation_gb300.cuh).
+ *
+ * Conventions
+ *   - Every function returns SMK_OK (0) or an SMK_ERR_* code; smk_last_error() gives detail.
+ *   - Host arrays use the reference's layout (smokeSimulation.cu:127-147): cells
+ *     nx*ny*nz floats, faces (nx+1)*(ny+1)*(nz+1) floats per component, x fastest.
+ *   - Mask bytes: nonzero = fluid, 0 = solid (the reference's dev_s, :24, :200-207, :306-309).
+ *   - `stream` arguments are cudaStream_t passed as void* (NULL = the legacy default stream).
+ *   - A handle is not thread-safe; distinct handles are independent.
+ */
+#ifndef SMOKE_GB300_H
+#define SMOKE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SMK_OK 0
+#define SMK_ERR_INVALID 1     /* bad argument (null pointer, size, id) */
+#define SMK_ERR_CUDA 2        /* a CUDA runtime call failed */
+#define SMK_ERR_OOM 3         /* device memory allocation failed */
+#define SMK_ERR_STATE 4       /* call not valid in the current state */
+#define SMK_ERR_TIMEOUT 5     /* a bounded device wait gave up */
+
+/* Projection schemes. */
+#define SMK_PROJECT_REFERENCE 0 /* in-place velocity red-black SOR, bit-exact with the reference */
+#define SMK_PROJECT_PRESSURE 1  /* pressure red-black SOR, gradient subtract fused at the end */
+
+/* Velocity clamp modes. */
+#define SMK_CLAMP_REFERENCE 0 /* if |u|^2*dt > c^2 scale by c^2/(|u|^2*dt) (smokeSimulation.cu:343-349) */
+#define SMK_CLAMP_MAGNITUDE 1 /* |u| <= c */
+#define SMK_CLAMP_NONE 2
+
+/* Storage precision of the advected fields (u, v, w, density). */
+#define SMK_STORAGE_F32 0
+#define SMK_STORAGE_BF16 1
+
+typedef struct smk_sim smk_sim;
+
+typedef struct smk_params {
+    float gravity;      /* reference: -9.82 (smokeSimulation.cu:28) */
+    float buoyancy;     /* reference: 2.0   (:29) */
+    float clamp_const;  /* reference: MAX_VELOCITY_PER_STEP 3.0 (:39) */
+    int clamp_mode;     /* SMK_CLAMP_* */
+    int projection;     /* SMK_PROJECT_* */
+    int max_sweeps;     /* red+black sweeps; reference: num_iterations 30 (:797) */
+    double omega;       /* over-relaxation; reference: OVER_RELAXATION 1.9 (:38) */
+    float tol;          /* PRESSURE only: stop on max|residual| <= tol (0: fixed sweeps) */
+    int check_every;    /* PRESSURE only: residual check cadence in sweeps */
+    int warm_start;     /* PRESSURE only: keep the pressure across steps */
+    int report_div;     /* measure max|div u| after the projection every step */
+    int storage;        /* SMK_STORAGE_* (F32 only for PROJECT_REFERENCE) */
+} smk_params;
+
+typedef struct smk_stats {
+    int sweeps;         /* sweeps performed by the last step's projection */
+    int converged;      /* tolerance reached (PRESSURE with tol > 0) */
+    float resid_max;    /* max |residual| at the last residual check */
+    float div_max;      /* max |div u| after projection (report_div), else -1 */
+    int step_index;     /* steps taken since creation */
+} smk_stats;
+
+/* Host copy of the full state in the reference's layout (both ping-pong buffers). */
+typedef struct smk_host_state {
+    float* rho[2];
+    float* u[2];
+    float* v[2];
+    float* w[2];
+    uint8_t* s;
+    int index_now;      /* the reference's indexNow (smokeSimulation.cu:707); 1 after init */
+} smk_host_state;
+
+/* The reference's constants (smokeSimulation.cu:28-39, :797), PROJECT_REFERENCE, F32. */
+void smk_default_params(smk_params* p);
+
+/* Status text for a code, and the last error message of the calling thread. */
+const char* smk_error_string(int code);
+const char* smk_last_error(void);
+
+/* Allocate a simulation of nx*ny*nz cells on the current device.  The state matches the
+ * reference's initializeVolume (smokeSimulation.cu:124-238): density zero, velocities zero,
+ * mask fluid except the y = 0 floor.  Replaces initializeVolume's allocation part. */
+int smk_create(int nx, int ny, int nz, const smk_params* params, smk_sim** out);
+/* Free everything (replaces deleteVolume, :240-248). */
+int smk_destroy(smk_sim* sim);
+
+int smk_set_params(smk_sim* sim, const smk_params* params);
+int smk_get_params(const smk_sim* sim, smk_params* params);
+int smk_get_dims(const smk_sim* sim, int* nx, int* ny, int* nz);
+
+/* Upload density into buffer [0] (initializeVolume's H2D copy, :138). */
+int smk_set_density(smk_sim* sim, const float* host_rho);
+/* Replace the solid mask (nx*ny*nz bytes, nonzero = fluid). Registered obstacles still
+ * overwrite interior cells every step, as fillObstacle does (:289-313). */
+int smk_set_solid_mask(smk_sim* sim, const uint8_t* host_s);
+
+/* Object registry (addObstacle :88-95, addSmokeSource :97-104, updateObjectPos :106-109).
+ * Ids are sequential across kinds, as in the reference.  No cap on the object count. */
+int smk_add_obstacle(smk_sim* sim, float x, float y, float z, float vx, float vy, float vz, float r,
+                     int* id);
+int smk_add_smoke_source(smk_sim* sim, float x, float y, float z, float r, int* id);
+/* Box emitter over cells [x0,x1)x[y0,y1)x[z0,z1): density into both buffers each step (the
+ * reference's documented emulation of a box source); when set_vy, v-faces below and above each
+ * box cell are set to vy before forcing. */
+int smk_add_box_emitter(smk_sim* sim, int x0, int y0, int z0, int x1, int y1, int z1,
+                        float density, float vy, int set_vy, int* id);
+int smk_update_object_pos(smk_sim* sim, int id, float x, float y, float z);
+int smk_clear_objects(smk_sim* sim);
+
+/* One step, stream-ordered (no host synchronisation): the stage sequence of simulate()
+ * (:774-811) without its D2H copy. */
+int smk_step(smk_sim* sim, float dt, void* stream);
+/* simulate(float*, dt) (:774-819): one step, then a blocking copy of the new density into
+ * host_out (nx*ny*nz floats). */
+int smk_simulate(smk_sim* sim, float* host_out, float dt);
+/* Copy the current density (the buffer the last step wrote) to host or device memory,
+ * stream-ordered; call smk_sync (or synchronise the stream) before reading a host copy. */
+int smk_read_density(smk_sim* sim, float* dst, int dst_on_device, void* stream);
+int smk_sync(smk_sim* sim, void* stream);
+
+/* Full state in the reference layout (checkpoint / resume, parity checks).  Blocking. */
+int smk_read_state(smk_sim* sim, const smk_host_state* st);
+int smk_write_state(smk_sim* sim, const smk_host_state* st);
+/* The projected velocities of the last step (buffer "now" after projection) are not kept
+ * separately; smk_read_state returns both buffers as the reference holds them. */
+
+/* Statistics of the last step (blocking). */
+int smk_get_stats(smk_sim* sim, smk_stats* out);
+
+/* Per-stage device times of the last step, measured with CUDA events on the step's stream
+ * when timing is enabled.  Stages: 0 objects+emitters, 1 forcing, 2 projection,
+ * 3 advection, 4 whole step.  Blocking. */
+int smk_set_timing(smk_sim* sim, int enable);
+int smk_get_stage_times(smk_sim* sim, float* ms, int count);
+/* Number of kernel launches the library issued since creation. */
+long long smk_launch_count(const smk_sim* sim);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SMOKE_GB300_H */

@@ -1,0 +1,129 @@
+"""Build recipe for the oracles (test infrastructure only).
+
+1. The restatement (oracle/smoke_oracle.cpp) -> oracle/_build/libsmoke_oracle.so.
+2. The reference's own step built for the host ("oracle B"):
+   a. when the reference checkout is present, project/smokeSimulation.cu is rewritten into
+      oracle/_ref/ref_step_host.cpp by the text rules below (launch syntax -> host_launch,
+      the three solver literals -> variables with the same default values, glm includes
+      dropped: glm is unused by the simulation) and the harness oracle/ref_harness_tail.inc is
+      appended;
+   b. whenever oracle/_ref/ref_step_host.cpp exists, it is compiled with g++/OpenMP against the
+      host shim in oracle/ref_shim/ into oracle/_ref/libsmoke_ref_host.so.
+   Step 2a only runs where the reference sources are; the generated file is a build
+   intermediate under oracle/_ref/ (git-ignored), so a machine without the reference can still
+   run step 2b.
+
+Both libraries are compiled without FMA contraction (-ffp-contract=off): the restatement's
+float instantiation is then bit-identical to the reference's own arithmetic.
+"""
+from __future__ import annotations
+
+import os
+import re
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+REF_OUT = os.path.join(HERE, "_ref")
+REFERENCE_SRC = os.environ.get(
+    "SMOKE_REFERENCE_SRC", "/root/reference/project/smokeSimulation.cu")
+
+ORACLE_SO = os.path.join(BUILD, "libsmoke_oracle.so")
+REF_CPP = os.path.join(REF_OUT, "ref_step_host.cpp")
+REF_SO = os.path.join(REF_OUT, "libsmoke_ref_host.so")
+
+CXXFLAGS = ["-O3", "-fopenmp", "-ffp-contract=off", "-fno-fast-math", "-fPIC", "-shared",
+            "-std=c++17"]
+
+
+def _run(cmd: list[str]) -> None:
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("command failed: %s\n%s\n%s" % (" ".join(cmd), r.stdout, r.stderr))
+
+
+def _stale(out: str, *srcs: str) -> bool:
+    if not os.path.exists(out):
+        return True
+    t = os.path.getmtime(out)
+    return any(os.path.getmtime(s) > t for s in srcs if os.path.exists(s))
+
+
+def build_restatement(force: bool = False) -> str:
+    os.makedirs(BUILD, exist_ok=True)
+    src = os.path.join(HERE, "smoke_oracle.cpp")
+    if force or _stale(ORACLE_SO, src):
+        _run(["g++", *CXXFLAGS, src, "-o", ORACLE_SO])
+    return ORACLE_SO
+
+
+_LAUNCH = re.compile(r"([A-Za-z_][A-Za-z0-9_]*)\s*<<\s*<([^>]*)>>\s*>\s*\(")
+
+
+def rewrite_reference(text: str, header: str | None) -> str:
+    """Text rules applied to project/smokeSimulation.cu (never edited in place); the module's
+    header project/smokeSimulation.cuh is inlined where the source includes it."""
+    out = []
+    for line in text.splitlines():
+        s = line.strip()
+        if s.startswith("#include <glm/") or s == "using namespace glm;":
+            out.append("// (glm include dropped: unused by the simulation)")
+            continue
+        if s.startswith("#define OVER_RELAXATION"):
+            out.append("#define OVER_RELAXATION ref_over_relaxation")
+            continue
+        if s.startswith("#define MAX_VELOCITY_PER_STEP"):
+            out.append("#define MAX_VELOCITY_PER_STEP ref_max_velocity")
+            continue
+        if s == '#include "smokeSimulation.cuh"' and header is not None:
+            out.append("// ---- project/smokeSimulation.cuh (inlined) ----")
+            out.extend(header.splitlines())
+            continue
+        line = line.replace("int num_iterations = 30;", "int num_iterations = ref_num_iterations;")
+        line = _LAUNCH.sub(lambda m: "host_launch(%s, %s, " % (m.group(2).strip(), m.group(1)), line)
+        out.append(line)
+    out.append('#include "ref_harness_tail.inc"')
+    return "\n".join(out) + "\n"
+
+
+def generate_reference_tu() -> bool:
+    if not os.path.exists(REFERENCE_SRC):
+        return False
+    os.makedirs(REF_OUT, exist_ok=True)
+    with open(REFERENCE_SRC, "r", encoding="utf-8", errors="replace") as f:
+        text = f.read()
+    hdr_path = os.path.join(os.path.dirname(REFERENCE_SRC), "smokeSimulation.cuh")
+    with open(hdr_path, "r", encoding="utf-8", errors="replace") as f:
+        header = f.read()
+    new = rewrite_reference(text, header)
+    if "<<<" in new.replace(" ", "") or "<< <" in new:
+        raise RuntimeError("a kernel launch was left unrewritten")
+    old = None
+    if os.path.exists(REF_CPP):
+        with open(REF_CPP) as f:
+            old = f.read()
+    if old != new:
+        with open(REF_CPP, "w") as f:
+            f.write(new)
+    return True
+
+
+def build_reference(force: bool = False) -> str | None:
+    generate_reference_tu()
+    if not os.path.exists(REF_CPP):
+        return None
+    deps = [REF_CPP, os.path.join(HERE, "ref_harness_tail.inc"),
+            os.path.join(HERE, "ref_shim", "cuda_runtime.h")]
+    if force or _stale(REF_SO, *deps):
+        _run(["g++", *CXXFLAGS, "-Wno-narrowing", "-w", "-I", os.path.join(HERE, "ref_shim"),
+              "-I", HERE, REF_CPP, "-o", REF_SO])
+    return REF_SO
+
+
+def build(force: bool = False) -> dict:
+    return {"restatement": build_restatement(force), "reference": build_reference(force)}
+
+
+if __name__ == "__main__":
+    print(build(force="--force" in sys.argv))

@@ -1,0 +1,295 @@
+"""smoke_simulation_gb300 -- GB300-native semi-Lagrangian smoke step (Python front end).
+
+The simulation runs in libsmoke_gb300.so (hand-written sm_103a CUDA kernels behind the C ABI
+in include/smoke_gb300.h).  This module is a thin ctypes binding of that ABI for tests,
+benchmarks and Python callers; it adds no compute of its own and has no CPU fallback: if the
+library is missing, importing `lib()` raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libsmoke_gb300.so")
+
+SMK_OK = 0
+PROJECT_REFERENCE = 0
+PROJECT_PRESSURE = 1
+CLAMP_REFERENCE, CLAMP_MAGNITUDE, CLAMP_NONE = 0, 1, 2
+STORAGE_F32, STORAGE_BF16 = 0, 1
+
+
+class SmokeError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__("smoke_gb300 error %d: %s" % (code, msg))
+        self.code = code
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("gravity", C.c_float), ("buoyancy", C.c_float), ("clamp_const", C.c_float),
+        ("clamp_mode", C.c_int), ("projection", C.c_int), ("max_sweeps", C.c_int),
+        ("omega", C.c_double), ("tol", C.c_float), ("check_every", C.c_int),
+        ("warm_start", C.c_int), ("report_div", C.c_int), ("storage", C.c_int),
+    ]
+
+
+class Stats(C.Structure):
+    _fields_ = [("sweeps", C.c_int), ("converged", C.c_int), ("resid_max", C.c_float),
+                ("div_max", C.c_float), ("step_index", C.c_int)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class HostState(C.Structure):
+    _fields_ = [("rho", C.c_void_p * 2), ("u", C.c_void_p * 2), ("v", C.c_void_p * 2),
+                ("w", C.c_void_p * 2), ("s", C.c_void_p), ("index_now", C.c_int)]
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Load the in-tree CUDA library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError("libsmoke_gb300.so is not built; run smoke_simulation_gb300.build.build()")
+    L = C.CDLL(LIB_PATH)
+    vp, i, f = C.c_void_p, C.c_int, C.c_float
+    sig = {
+        "smk_default_params": (None, [C.POINTER(Params)]),
+        "smk_error_string": (C.c_char_p, [i]),
+        "smk_last_error": (C.c_char_p, []),
+        "smk_create": (i, [i, i, i, C.POINTER(Params), C.POINTER(vp)]),
+        "smk_destroy": (i, [vp]),
+        "smk_set_params": (i, [vp, C.POINTER(Params)]),
+        "smk_get_params": (i, [vp, C.POINTER(Params)]),
+        "smk_set_density": (i, [vp, vp]),
+        "smk_set_solid_mask": (i, [vp, vp]),
+        "smk_add_obstacle": (i, [vp, f, f, f, f, f, f, f, C.POINTER(i)]),
+        "smk_add_smoke_source": (i, [vp, f, f, f, f, C.POINTER(i)]),
+        "smk_add_box_emitter": (i, [vp, i, i, i, i, i, i, f, f, i, C.POINTER(i)]),
+        "smk_update_object_pos": (i, [vp, i, f, f, f]),
+        "smk_clear_objects": (i, [vp]),
+        "smk_step": (i, [vp, f, vp]),
+        "smk_simulate": (i, [vp, vp, f]),
+        "smk_read_density": (i, [vp, vp, i, vp]),
+        "smk_sync": (i, [vp, vp]),
+        "smk_read_state": (i, [vp, C.POINTER(HostState)]),
+        "smk_write_state": (i, [vp, C.POINTER(HostState)]),
+        "smk_get_stats": (i, [vp, C.POINTER(Stats)]),
+        "smk_set_timing": (i, [vp, i]),
+        "smk_get_stage_times": (i, [vp, C.POINTER(C.c_float), i]),
+        "smk_launch_count": (C.c_longlong, [vp]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def _check(rc: int):
+    if rc != SMK_OK:
+        L = lib()
+        raise SmokeError(rc, "%s: %s" % (L.smk_error_string(rc).decode(),
+                                         L.smk_last_error().decode()))
+
+
+def default_params(**kw) -> Params:
+    p = Params()
+    lib().smk_default_params(C.byref(p))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+def _ptr(a: np.ndarray) -> int:
+    assert a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data
+
+
+class Simulation:
+    """One resident grid: the reference's implicit module state as an object."""
+
+    def __init__(self, nx: int, ny: int, nz: int, params: Optional[Params] = None):
+        self.nx, self.ny, self.nz = nx, ny, nz
+        self.h = C.c_void_p()
+        _check(lib().smk_create(nx, ny, nz, C.byref(params) if params is not None else None,
+                                C.byref(self.h)))
+
+    # -- lifecycle ---------------------------------------------------------------------------
+    def close(self):
+        if self.h:
+            lib().smk_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def cell_shape(self):
+        return (self.nz, self.ny, self.nx)
+
+    @property
+    def face_shape(self):
+        return (self.nz + 1, self.ny + 1, self.nx + 1)
+
+    # -- configuration -----------------------------------------------------------------------
+    def params(self) -> Params:
+        p = Params()
+        _check(lib().smk_get_params(self.h, C.byref(p)))
+        return p
+
+    def set_params(self, p: Params = None, **kw):
+        p = p or self.params()
+        for k, v in kw.items():
+            setattr(p, k, v)
+        _check(lib().smk_set_params(self.h, C.byref(p)))
+
+    def set_density(self, rho: np.ndarray):
+        a = np.ascontiguousarray(rho, np.float32)
+        assert a.size == self.nx * self.ny * self.nz
+        _check(lib().smk_set_density(self.h, _ptr(a)))
+
+    def set_mask(self, s: np.ndarray):
+        a = np.ascontiguousarray(s, np.uint8)
+        assert a.size == self.nx * self.ny * self.nz
+        _check(lib().smk_set_solid_mask(self.h, _ptr(a)))
+
+    def add_obstacle(self, x, y, z, vx=0.0, vy=0.0, vz=0.0, r=1.0) -> int:
+        i = C.c_int()
+        _check(lib().smk_add_obstacle(self.h, x, y, z, vx, vy, vz, r, C.byref(i)))
+        return i.value
+
+    def add_smoke_source(self, x, y, z, r) -> int:
+        i = C.c_int()
+        _check(lib().smk_add_smoke_source(self.h, x, y, z, r, C.byref(i)))
+        return i.value
+
+    def add_box_emitter(self, x0, y0, z0, x1, y1, z1, density=1.0, vy=0.0, set_vy=False) -> int:
+        i = C.c_int()
+        _check(lib().smk_add_box_emitter(self.h, int(x0), int(y0), int(z0), int(x1), int(y1),
+                                         int(z1), density, vy, int(bool(set_vy)), C.byref(i)))
+        return i.value
+
+    def update_object_pos(self, oid: int, x, y, z):
+        _check(lib().smk_update_object_pos(self.h, oid, x, y, z))
+
+    def clear_objects(self):
+        _check(lib().smk_clear_objects(self.h))
+
+    # -- stepping ----------------------------------------------------------------------------
+    def step(self, dt: float, stream: int = 0):
+        _check(lib().smk_step(self.h, dt, stream))
+
+    def simulate(self, out: np.ndarray, dt: float):
+        assert out.dtype == np.float32 and out.flags["C_CONTIGUOUS"]
+        _check(lib().smk_simulate(self.h, _ptr(out), dt))
+        return out
+
+    def read_density(self, out: Optional[np.ndarray] = None) -> np.ndarray:
+        out = np.empty(self.cell_shape, np.float32) if out is None else out
+        _check(lib().smk_read_density(self.h, _ptr(out), 0, None))
+        _check(lib().smk_sync(self.h, None))
+        return out
+
+    def read_density_device(self, dev_ptr: int, stream: int = 0):
+        _check(lib().smk_read_density(self.h, dev_ptr, 1, stream))
+
+    def sync(self, stream: int = 0):
+        _check(lib().smk_sync(self.h, stream))
+
+    def read_state(self) -> dict:
+        cs, fs = self.cell_shape, self.face_shape
+        st = {"rho": [np.zeros(cs, np.float32) for _ in range(2)],
+              "u": [np.zeros(fs, np.float32) for _ in range(2)],
+              "v": [np.zeros(fs, np.float32) for _ in range(2)],
+              "w": [np.zeros(fs, np.float32) for _ in range(2)],
+              "s": np.zeros(cs, np.uint8)}
+        hs = HostState()
+        for k in ("rho", "u", "v", "w"):
+            arr = getattr(hs, k)
+            for j in range(2):
+                arr[j] = _ptr(st[k][j])
+        hs.s = _ptr(st["s"])
+        _check(lib().smk_read_state(self.h, C.byref(hs)))
+        st["index_now"] = hs.index_now
+        return st
+
+    def write_state(self, st: dict):
+        keep = []
+        hs = HostState()
+        for k in ("rho", "u", "v", "w"):
+            arr = getattr(hs, k)
+            for j in range(2):
+                if st.get(k) is None or st[k][j] is None:
+                    arr[j] = None
+                    continue
+                a = np.ascontiguousarray(st[k][j], np.float32)
+                keep.append(a)
+                arr[j] = _ptr(a)
+        if st.get("s") is not None:
+            s = np.ascontiguousarray(st["s"], np.uint8)
+            keep.append(s)
+            hs.s = _ptr(s)
+        hs.index_now = int(st.get("index_now", 1))
+        _check(lib().smk_write_state(self.h, C.byref(hs)))
+
+    def stats(self) -> Stats:
+        s = Stats()
+        _check(lib().smk_get_stats(self.h, C.byref(s)))
+        return s
+
+    def set_timing(self, on: bool = True):
+        _check(lib().smk_set_timing(self.h, int(on)))
+
+    def stage_times(self) -> np.ndarray:
+        t = (C.c_float * 5)()
+        _check(lib().smk_get_stage_times(self.h, t, 5))
+        return np.array(t[:], np.float64)
+
+    def launch_count(self) -> int:
+        return int(lib().smk_launch_count(self.h))
+
+
+def params_for_scene(scene, **overrides) -> Params:
+    p = default_params()
+    p.gravity, p.buoyancy = scene.gravity, scene.buoyancy
+    p.clamp_const, p.clamp_mode = scene.clamp_const, scene.clamp_mode
+    p.projection, p.max_sweeps, p.omega = scene.scheme, scene.iterations, scene.omega
+    p.tol, p.check_every, p.warm_start = scene.tol, scene.check_every, scene.warm_start
+    for k, v in overrides.items():
+        setattr(p, k, v)
+    return p
+
+
+def from_scene(scene, **overrides) -> Simulation:
+    """A Simulation holding `scene`'s initial state and objects (buffer [0] = initial fields,
+    buffer [1] = 0, as after the reference's initializeVolume plus the scene's writes)."""
+    sim = Simulation(scene.nx, scene.ny, scene.nz, params_for_scene(scene, **overrides))
+    sim.set_density(scene.initial_density())
+    if scene.mask is not None:
+        sim.set_mask(scene.mask)
+    if scene.u0 is not None or scene.v0 is not None or scene.w0 is not None:
+        sim.write_state({"u": [scene.initial_velocity("u"), None],
+                         "v": [scene.initial_velocity("v"), None],
+                         "w": [scene.initial_velocity("w"), None], "index_now": 1})
+    for bx in scene.boxes:
+        sim.add_box_emitter(*bx[:6], density=bx[6], vy=bx[7], set_vy=bool(bx[8]))
+    for (x, y, z, r) in scene.spheres:
+        sim.add_smoke_source(x, y, z, r)
+    for ob in scene.obstacles:
+        sim.add_obstacle(*ob)
+    return sim

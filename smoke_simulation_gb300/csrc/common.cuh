@@ -1,0 +1,109 @@
+// Shared device definitions for libsmoke_gb300.
+//
+// HBM layout.  Every field of one simulation -- density (cells), u, v, w (faces), pressure and
+// right-hand side (cells), the solid mask and the neighbour-flag byte (cells) -- uses ONE
+// index function  i = x + X*y + XY*z  with X = round_up(nx+1, 8) (32-byte rows) and
+// XY = X*(ny+1).  Faces use x <= nx, y <= ny, z <= nz; cells use x < nx, y < ny, z < nz and
+// leave the last row/plane unused.  One index therefore addresses a cell and its three
+// "lower" faces (u at x, v at y, w at z), exactly like the reference's shared staggered index
+// (project/smokeSimulation.cu:146-147, :337), while rows stay aligned for vector access.
+//
+// The whole library is compiled with -fmad=false so that every float expression rounds
+// exactly as written (no contraction); fused multiply-adds appear only as explicit fmaf().
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace smk {
+
+struct Grid {
+    int nx, ny, nz;
+    int X;   // row pitch in elements
+    int XY;  // plane pitch in elements
+    __host__ __device__ __forceinline__ int idx(int x, int y, int z) const { return x + X * y + XY * z; }
+};
+
+// Neighbour-flag byte per cell, derived from the mask whenever it changes.
+enum : uint8_t {
+    F_SELF = 1u << 0,  // s(x,y,z)
+    F_XM = 1u << 1,    // s(x-1,y,z)
+    F_XP = 1u << 2,    // s(x+1,y,z)
+    F_YM = 1u << 3,    // s(x,y-1,z)
+    F_YP = 1u << 4,    // s(x,y+1,z)
+    F_ZM = 1u << 5,    // s(x,y,z-1)
+    F_ZP = 1u << 6,    // s(x,y,z+1)
+    F_PROJ = 1u << 7,  // updated by the projection: interior, fluid, >= 1 fluid neighbour
+    F_NBRS = 0x7E,
+};
+
+// Device-side per-step status written by the solver kernels.
+struct StepStatus {
+    unsigned div_bits;   // max |div u| after projection, as float bits (non-negative)
+    int done;            // tolerance reached: later sweep groups are skipped
+    int done_group;      // check group that set `done`
+    int pad;
+    unsigned rmax_bits[1];  // max |residual| per check group (flexible; sized at allocation)
+};
+
+// Object records (the reference's packing, smokeSimulation.cu:719-725, :750-758).
+struct SphereObj { float x, y, z, r; };
+struct ObstacleObj { float x, y, z, vx, vy, vz, r; };
+struct BoxObj { int x0, y0, z0, x1, y1, z1; float density, vy; int set_vy; };
+
+__device__ __forceinline__ void atomic_max_bits(unsigned* p, float nonneg) {
+    atomicMax(p, __float_as_uint(nonneg));
+}
+
+// ---- reference-exact helpers ---------------------------------------------------------------
+
+// avgU/avgV/avgW (smokeSimulation.cu:409-447): 8-point sums in the reference's order, / 8.
+__device__ __forceinline__ float avgU(const float* __restrict__ f, const Grid& g, int i) {
+    const int X = g.X, XY = g.XY;
+    float s = f[i - XY] + f[i + 1 - XY] + f[i - X - XY] + f[i + 1 - X - XY] + f[i] + f[i + 1] +
+              f[i - X] + f[i + 1 - X];
+    return s / 8.0f;
+}
+__device__ __forceinline__ float avgV(const float* __restrict__ f, const Grid& g, int i) {
+    const int X = g.X, XY = g.XY;
+    float s = f[i - XY] + f[i - 1 - XY] + f[i + X - XY] + f[i - 1 + X - XY] + f[i] + f[i - 1] +
+              f[i + X] + f[i - 1 + X];
+    return s / 8.0f;
+}
+__device__ __forceinline__ float avgW(const float* __restrict__ f, const Grid& g, int i) {
+    const int X = g.X, XY = g.XY;
+    float s = f[i] + f[i - 1] + f[i - X] + f[i - 1 - X] + f[i - XY] + f[i - 1 - XY] + f[i - X - XY] +
+              f[i - 1 - X - XY];
+    return s / 8.0f;
+}
+
+// sampleSmoke (smokeSimulation.cu:451-484): clamp the position to [1, n-1] with the CELL
+// dims, trilinear weights from (c - delta) - i0, eight terms summed in the reference order.
+__device__ __forceinline__ float sample_ref(const float* __restrict__ f, const Grid& g, float px,
+                                           float py, float pz, float dx, float dy, float dz) {
+    const float mx = (float)(unsigned)(g.nx - 1), my = (float)(unsigned)(g.ny - 1),
+                mz = (float)(unsigned)(g.nz - 1);
+    float x = fmaxf(fminf(px, mx), 1.0f);
+    float y = fmaxf(fminf(py, my), 1.0f);
+    float z = fmaxf(fminf(pz, mz), 1.0f);
+    int x0 = (int)fminf(floorf(x - dx), mx);
+    float xw1 = (x - dx) - (float)x0;
+    float xw0 = 1.0f - xw1;
+    int x1 = (int)fminf((float)(x0 + 1), mx);
+    int y0 = (int)fminf(floorf(y - dy), my);
+    float yw1 = (y - dy) - (float)y0;
+    float yw0 = 1.0f - yw1;
+    int y1 = (int)fminf((float)(y0 + 1), my);
+    int z0 = (int)fminf(floorf(z - dz), mz);
+    float zw1 = (z - dz) - (float)z0;
+    float zw0 = 1.0f - zw1;
+    int z1 = (int)fminf((float)(z0 + 1), mz);
+    const int X = g.X, XY = g.XY;
+    const int r00 = y0 * X + z0 * XY, r10 = y1 * X + z0 * XY, r01 = y0 * X + z1 * XY,
+              r11 = y1 * X + z1 * XY;
+    return xw0 * yw0 * zw0 * f[x0 + r00] + xw1 * yw0 * zw0 * f[x1 + r00] +
+           xw0 * yw1 * zw0 * f[x0 + r10] + xw1 * yw1 * zw0 * f[x1 + r10] +
+           xw0 * yw0 * zw1 * f[x0 + r01] + xw1 * yw0 * zw1 * f[x1 + r01] +
+           xw0 * yw1 * zw1 * f[x0 + r11] + xw1 * yw1 * zw1 * f[x1 + r11];
+}
+
+}  // namespace smk

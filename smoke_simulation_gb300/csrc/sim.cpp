@@ -1,0 +1,547 @@
+// libsmoke_gb300: handle management and the step driver behind the C ABI (smoke_gb300.h).
+//
+// Replaces the reference's module globals and host orchestration
+// (project/smokeSimulation.cu:16-248, :707-819) with an explicit handle.  A step issues the
+// reference's stage sequence (simulate, :774-811) on one CUDA stream without host
+// synchronisation; only smk_simulate (the reference's simulate with its blocking D2H, :814)
+// and the explicit read/stat calls synchronise.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/smoke_gb300.h"
+#include "kernels.h"
+#include "sim_internal.h"
+
+using namespace smk;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+#define SMK_CUDA(call)                                                                   \
+    do {                                                                                 \
+        cudaError_t e_ = (call);                                                         \
+        if (e_ != cudaSuccess) {                                                         \
+            return fail(e_ == cudaErrorMemoryAllocation ? SMK_ERR_OOM : SMK_ERR_CUDA,    \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));             \
+        }                                                                                \
+    } while (0)
+
+struct DeviceGuard {
+    int prev = -1;
+    bool changed = false;
+    explicit DeviceGuard(int dev) {
+        if (cudaGetDevice(&prev) == cudaSuccess && prev != dev) {
+            changed = cudaSetDevice(dev) == cudaSuccess;
+        }
+    }
+    ~DeviceGuard() {
+        if (changed) cudaSetDevice(prev);
+    }
+};
+
+int check_params(const smk_params* p) {
+    if (!p) return fail(SMK_ERR_INVALID, "params is null");
+    if (p->projection != SMK_PROJECT_REFERENCE && p->projection != SMK_PROJECT_PRESSURE)
+        return fail(SMK_ERR_INVALID, "unknown projection scheme");
+    if (p->clamp_mode < 0 || p->clamp_mode > 2) return fail(SMK_ERR_INVALID, "unknown clamp mode");
+    if (p->max_sweeps < 0 || p->max_sweeps > 1000000) return fail(SMK_ERR_INVALID, "max_sweeps out of range");
+    if (p->projection == SMK_PROJECT_PRESSURE && p->tol > 0 && p->check_every <= 0)
+        return fail(SMK_ERR_INVALID, "check_every must be positive when tol > 0");
+    if (p->storage != SMK_STORAGE_F32 && p->storage != SMK_STORAGE_BF16)
+        return fail(SMK_ERR_INVALID, "unknown storage precision");
+    if (p->storage == SMK_STORAGE_BF16 && p->projection == SMK_PROJECT_REFERENCE)
+        return fail(SMK_ERR_INVALID, "BF16 storage needs the pressure projection");
+    if (p->projection == SMK_PROJECT_PRESSURE && p->tol > 0 &&
+        (p->max_sweeps + p->check_every - 1) / p->check_every > 4000)
+        return fail(SMK_ERR_INVALID, "too many residual checks per step (max_sweeps/check_every > 4000)");
+    return SMK_OK;
+}
+
+cudaMemcpy3DParms copy3d(void* dst, size_t dpitch, size_t dy, const void* src, size_t spitch,
+                         size_t sy, size_t width_bytes, size_t h, size_t d, cudaMemcpyKind kind) {
+    cudaMemcpy3DParms m;
+    memset(&m, 0, sizeof(m));
+    m.srcPtr = make_cudaPitchedPtr(const_cast<void*>(src), spitch, width_bytes, sy);
+    m.dstPtr = make_cudaPitchedPtr(dst, dpitch, width_bytes, dy);
+    m.extent = make_cudaExtent(width_bytes, h, d);
+    m.kind = kind;
+    return m;
+}
+
+}  // namespace
+
+// ---- smk_sim --------------------------------------------------------------------------------
+
+int smk_sim::alloc() {
+    const size_t n = elems();
+    float** fl[] = {&rho[0], &rho[1], &u[0], &u[1], &v[0], &v[1], &w[0], &w[1], &P, &b};
+    for (float** f : fl) {
+        SMK_CUDA(cudaMalloc((void**)f, n * sizeof(float)));
+        SMK_CUDA(cudaMemset(*f, 0, n * sizeof(float)));
+    }
+    SMK_CUDA(cudaMalloc((void**)&s, n));
+    SMK_CUDA(cudaMalloc((void**)&flags, n));
+    SMK_CUDA(cudaMemset(flags, 0, n));
+    status_groups = 4096;
+    SMK_CUDA(cudaMalloc((void**)&status, sizeof(StepStatus) + sizeof(unsigned) * status_groups));
+    SMK_CUDA(cudaMemset(status, 0, sizeof(StepStatus) + sizeof(unsigned) * status_groups));
+    for (auto& e : ev) SMK_CUDA(cudaEventCreate(&e));
+    // initializeVolume's mask: fluid except the y = 0 floor (smokeSimulation.cu:200-207)
+    std::vector<uint8_t> host((size_t)g.nx * g.ny * g.nz, 1);
+    for (int z = 0; z < g.nz; ++z)
+        for (int x = 0; x < g.nx; ++x) host[(size_t)x + (size_t)z * g.nx * g.ny] = 0;
+    return upload_mask(host.data());
+}
+
+void smk_sim::release() {
+    float* fl[] = {rho[0], rho[1], u[0], u[1], v[0], v[1], w[0], w[1], P, b};
+    for (float* f : fl)
+        if (f) cudaFree(f);
+    if (s) cudaFree(s);
+    if (flags) cudaFree(flags);
+    if (status) cudaFree(status);
+    for (auto& e : ev)
+        if (e) cudaEventDestroy(e);
+}
+
+int smk_sim::upload_mask(const uint8_t* host) {
+    std::vector<uint8_t> norm((size_t)g.nx * g.ny * g.nz);
+    for (size_t i = 0; i < norm.size(); ++i) norm[i] = host[i] ? 1 : 0;
+    auto m = copy3d(s, g.X, g.ny + 1, norm.data(), g.nx, g.ny, g.nx, g.ny, g.nz, cudaMemcpyHostToDevice);
+    SMK_CUDA(cudaMemcpy3D(&m));
+    mask_dirty = true;
+    return SMK_OK;
+}
+
+int smk_sim::step(float dt, cudaStream_t st) {
+    const int past = index_now;
+    const int now = index_now ^ 1;
+    index_now = now;
+    const bool timed = timing;
+    if (timed) SMK_CUDA(cudaEventRecord(ev[0], st));
+
+    // a4: objects (drawObjects, smokeSimulation.cu:714-771)
+    std::vector<BoxObj> boxes;
+    std::vector<SphereObj> spheres;
+    std::vector<ObstacleObj> obstacles;
+    for (const auto& o : objects) {
+        if (o.kind == OBJ_BOX) boxes.push_back(o.box);
+        else if (o.kind == OBJ_SPHERE) spheres.push_back(o.sphere);
+        else obstacles.push_back(o.obstacle);
+    }
+    if (!boxes.empty()) {
+        launch_emit_boxes(g, rho[0], rho[1], v[now], boxes.data(), (int)boxes.size(), st);
+        ++launches;
+    }
+    if (!spheres.empty()) {
+        launch_fill_smoke(g, rho[0], rho[1], spheres.data(), (int)spheres.size(), st);
+        ++launches;
+    }
+    if (!obstacles.empty() && (obstacles_dirty || mask_dirty)) {
+        launch_fill_obstacles(g, s, obstacles.data(), (int)obstacles.size(), st);
+        ++launches;
+        mask_dirty = true;
+    }
+    obstacles_dirty = false;
+    if (mask_dirty) {
+        launch_build_flags(g, s, flags, P, st);
+        ++launches;
+        mask_dirty = false;
+    }
+    if (timed) SMK_CUDA(cudaEventRecord(ev[1], st));
+
+    // b: integrate + velocityConfinement (:789-791)
+    launch_forcing(g, u[now], v[now], w[now], rho[now], flags, dt, p.gravity, p.buoyancy,
+                   p.clamp_const, p.clamp_mode, st);
+    ++launches;
+    if (timed) SMK_CUDA(cudaEventRecord(ev[2], st));
+
+    // c/d: projection (:795-801)
+    const size_t status_bytes = sizeof(StepStatus) + sizeof(unsigned) * status_groups;
+    SMK_CUDA(cudaMemsetAsync(status, 0, status_bytes, st));
+    last_groups = 0;
+    if (p.projection == SMK_PROJECT_REFERENCE) {
+        for (int it = 0; it < p.max_sweeps; ++it) {
+            launch_project_velocity(g, u[now], v[now], w[now], flags, 0, p.omega, st);
+            launch_project_velocity(g, u[now], v[now], w[now], flags, 1, p.omega, st);
+            launches += 2;
+        }
+    } else {
+        float wacc[7];
+        wacc[0] = 0.0f;
+        for (int a = 1; a <= 6; ++a) wacc[a] = (float)p.omega / (float)a;
+        launch_rhs(g, u[now], v[now], w[now], flags, b, P, p.warm_start, st);
+        ++launches;
+        const bool use_tol = p.tol > 0.0f;
+        const int G = use_tol ? p.check_every : (p.max_sweeps > 0 ? p.max_sweeps : 1);
+        int sweep = 0, group = 0;
+        while (sweep < p.max_sweeps) {
+            if (use_tol) {
+                launch_resid_check(g, P, b, flags, status, group, p.tol, st);
+                ++launches;
+            }
+            int end = sweep + G < p.max_sweeps ? sweep + G : p.max_sweeps;
+            for (; sweep < end; ++sweep) {
+                launch_sweep(g, P, b, flags, 0, wacc, use_tol ? status : nullptr, st);
+                launch_sweep(g, P, b, flags, 1, wacc, use_tol ? status : nullptr, st);
+                launches += 2;
+            }
+            ++group;
+        }
+        last_groups = group;
+        launch_gradient_subtract(g, u[now], v[now], w[now], P, flags, st);
+        ++launches;
+    }
+    if (p.report_div) {
+        launch_div_max(g, u[now], v[now], w[now], flags, status, st);
+        ++launches;
+    }
+    if (timed) SMK_CUDA(cudaEventRecord(ev[3], st));
+
+    // a: advection (:805-810)
+    launch_advect_velocity(g, u[now], v[now], w[now], u[past], v[past], w[past], flags, dt, st);
+    launch_advect_density(g, rho[now], rho[past], u[past], v[past], w[past], flags, dt, st);
+    launches += 2;
+    if (timed) SMK_CUDA(cudaEventRecord(ev[4], st));
+    SMK_CUDA(cudaGetLastError());
+    ++steps;
+    last_projection = p.projection;
+    last_tol = p.tol;
+    last_max_sweeps = p.max_sweeps;
+    last_check_every = p.check_every;
+    return SMK_OK;
+}
+
+// ---- C ABI ----------------------------------------------------------------------------------
+
+extern "C" {
+
+void smk_default_params(smk_params* p) {
+    if (!p) return;
+    memset(p, 0, sizeof(*p));
+    p->gravity = -9.82f;
+    p->buoyancy = 2.0f;
+    p->clamp_const = 3.0f;
+    p->clamp_mode = SMK_CLAMP_REFERENCE;
+    p->projection = SMK_PROJECT_REFERENCE;
+    p->max_sweeps = 30;
+    p->omega = 1.9;
+    p->tol = 0.0f;
+    p->check_every = 10;
+    p->warm_start = 0;
+    p->report_div = 0;
+    p->storage = SMK_STORAGE_F32;
+}
+
+const char* smk_error_string(int code) {
+    switch (code) {
+        case SMK_OK: return "ok";
+        case SMK_ERR_INVALID: return "invalid argument";
+        case SMK_ERR_CUDA: return "CUDA error";
+        case SMK_ERR_OOM: return "out of device memory";
+        case SMK_ERR_STATE: return "invalid state";
+        case SMK_ERR_TIMEOUT: return "device wait timed out";
+        default: return "unknown error";
+    }
+}
+
+const char* smk_last_error(void) { return g_last_error.c_str(); }
+
+int smk_create(int nx, int ny, int nz, const smk_params* params, smk_sim** out) {
+    if (!out) return fail(SMK_ERR_INVALID, "out is null");
+    *out = nullptr;
+    if (nx < 1 || ny < 1 || nz < 1) return fail(SMK_ERR_INVALID, "grid dimensions must be >= 1");
+    smk_params p;
+    if (params) p = *params; else smk_default_params(&p);
+    int rc = check_params(&p);
+    if (rc) return rc;
+    long long X = ((long long)nx + 1 + 7) / 8 * 8;
+    long long total = X * (ny + 1) * (long long)(nz + 1);
+    if (total >= (1LL << 31)) return fail(SMK_ERR_INVALID, "grid too large for 32-bit indexing");
+    smk_sim* sim = new smk_sim();
+    sim->g.nx = nx;
+    sim->g.ny = ny;
+    sim->g.nz = nz;
+    sim->g.X = (int)X;
+    sim->g.XY = (int)(X * (ny + 1));
+    sim->p = p;
+    cudaGetDevice(&sim->device);
+    rc = sim->alloc();
+    if (rc) {
+        sim->release();
+        delete sim;
+        return rc;
+    }
+    *out = sim;
+    return SMK_OK;
+}
+
+int smk_destroy(smk_sim* sim) {
+    if (!sim) return fail(SMK_ERR_INVALID, "sim is null");
+    DeviceGuard dg(sim->device);
+    cudaDeviceSynchronize();
+    sim->release();
+    delete sim;
+    return SMK_OK;
+}
+
+int smk_set_params(smk_sim* sim, const smk_params* params) {
+    if (!sim) return fail(SMK_ERR_INVALID, "sim is null");
+    int rc = check_params(params);
+    if (rc) return rc;
+    sim->p = *params;
+    return SMK_OK;
+}
+
+int smk_get_params(const smk_sim* sim, smk_params* params) {
+    if (!sim || !params) return fail(SMK_ERR_INVALID, "null argument");
+    *params = sim->p;
+    return SMK_OK;
+}
+
+int smk_get_dims(const smk_sim* sim, int* nx, int* ny, int* nz) {
+    if (!sim) return fail(SMK_ERR_INVALID, "sim is null");
+    if (nx) *nx = sim->g.nx;
+    if (ny) *ny = sim->g.ny;
+    if (nz) *nz = sim->g.nz;
+    return SMK_OK;
+}
+
+int smk_set_density(smk_sim* sim, const float* host_rho) {
+    if (!sim || !host_rho) return fail(SMK_ERR_INVALID, "null argument");
+    DeviceGuard dg(sim->device);
+    const Grid& g = sim->g;
+    auto m = copy3d(sim->rho[0], (size_t)g.X * 4, g.ny + 1, host_rho, (size_t)g.nx * 4, g.ny,
+                    (size_t)g.nx * 4, g.ny, g.nz, cudaMemcpyHostToDevice);
+    SMK_CUDA(cudaMemcpy3D(&m));
+    return SMK_OK;
+}
+
+int smk_set_solid_mask(smk_sim* sim, const uint8_t* host_s) {
+    if (!sim || !host_s) return fail(SMK_ERR_INVALID, "null argument");
+    DeviceGuard dg(sim->device);
+    return sim->upload_mask(host_s);
+}
+
+static int add_object(smk_sim* sim, const smk_sim::Object& o, int* id) {
+    sim->objects.push_back(o);
+    if (id) *id = (int)sim->objects.size() - 1;
+    return SMK_OK;
+}
+
+int smk_add_obstacle(smk_sim* sim, float x, float y, float z, float vx, float vy, float vz, float r,
+                     int* id) {
+    if (!sim) return fail(SMK_ERR_INVALID, "sim is null");
+    smk_sim::Object o{};
+    o.kind = smk_sim::OBJ_OBSTACLE;
+    o.obstacle = ObstacleObj{x, y, z, vx, vy, vz, r};
+    sim->obstacles_dirty = true;
+    return add_object(sim, o, id);
+}
+
+int smk_add_smoke_source(smk_sim* sim, float x, float y, float z, float r, int* id) {
+    if (!sim) return fail(SMK_ERR_INVALID, "sim is null");
+    smk_sim::Object o{};
+    o.kind = smk_sim::OBJ_SPHERE;
+    o.sphere = SphereObj{x, y, z, r};
+    return add_object(sim, o, id);
+}
+
+int smk_add_box_emitter(smk_sim* sim, int x0, int y0, int z0, int x1, int y1, int z1, float density,
+                        float vy, int set_vy, int* id) {
+    if (!sim) return fail(SMK_ERR_INVALID, "sim is null");
+    smk_sim::Object o{};
+    o.kind = smk_sim::OBJ_BOX;
+    o.box = BoxObj{x0, y0, z0, x1, y1, z1, density, vy, set_vy ? 1 : 0};
+    return add_object(sim, o, id);
+}
+
+int smk_update_object_pos(smk_sim* sim, int id, float x, float y, float z) {
+    if (!sim) return fail(SMK_ERR_INVALID, "sim is null");
+    if (id < 0 || id >= (int)sim->objects.size()) return fail(SMK_ERR_INVALID, "object id out of range");
+    auto& o = sim->objects[id];
+    if (o.kind == smk_sim::OBJ_SPHERE) {
+        o.sphere.x = x; o.sphere.y = y; o.sphere.z = z;
+    } else if (o.kind == smk_sim::OBJ_OBSTACLE) {
+        o.obstacle.x = x; o.obstacle.y = y; o.obstacle.z = z;
+        sim->obstacles_dirty = true;
+    } else {
+        int dx = (int)x - o.box.x0, dy = (int)y - o.box.y0, dz = (int)z - o.box.z0;
+        o.box.x0 += dx; o.box.x1 += dx; o.box.y0 += dy; o.box.y1 += dy; o.box.z0 += dz; o.box.z1 += dz;
+    }
+    return SMK_OK;
+}
+
+int smk_clear_objects(smk_sim* sim) {
+    if (!sim) return fail(SMK_ERR_INVALID, "sim is null");
+    sim->objects.clear();
+    sim->obstacles_dirty = true;
+    return SMK_OK;
+}
+
+int smk_step(smk_sim* sim, float dt, void* stream) {
+    if (!sim) return fail(SMK_ERR_INVALID, "sim is null");
+    DeviceGuard dg(sim->device);
+    return sim->step(dt, (cudaStream_t)stream);
+}
+
+int smk_read_density(smk_sim* sim, float* dst, int dst_on_device, void* stream) {
+    if (!sim || !dst) return fail(SMK_ERR_INVALID, "null argument");
+    DeviceGuard dg(sim->device);
+    const Grid& g = sim->g;
+    const float* src = sim->rho[sim->index_now ^ 1];
+    auto m = copy3d(dst, (size_t)g.nx * 4, g.ny, src, (size_t)g.X * 4, g.ny + 1, (size_t)g.nx * 4, g.ny,
+                    g.nz, dst_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost);
+    SMK_CUDA(cudaMemcpy3DAsync(&m, (cudaStream_t)stream));
+    return SMK_OK;
+}
+
+int smk_sync(smk_sim* sim, void* stream) {
+    if (!sim) return fail(SMK_ERR_INVALID, "sim is null");
+    DeviceGuard dg(sim->device);
+    SMK_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+    return SMK_OK;
+}
+
+int smk_simulate(smk_sim* sim, float* host_out, float dt) {
+    if (!sim || !host_out) return fail(SMK_ERR_INVALID, "null argument");
+    DeviceGuard dg(sim->device);
+    int rc = sim->step(dt, (cudaStream_t)0);
+    if (rc) return rc;
+    rc = smk_read_density(sim, host_out, 0, nullptr);
+    if (rc) return rc;
+    SMK_CUDA(cudaStreamSynchronize((cudaStream_t)0));
+    return SMK_OK;
+}
+
+static int state_copy(smk_sim* sim, const smk_host_state* st, bool to_device) {
+    if (!sim || !st) return fail(SMK_ERR_INVALID, "null argument");
+    DeviceGuard dg(sim->device);
+    const Grid& g = sim->g;
+    SMK_CUDA(cudaDeviceSynchronize());
+    for (int k = 0; k < 2; ++k) {
+        float* dev_c[1] = {sim->rho[k]};
+        float* host_c[1] = {st->rho[k]};
+        float* dev_f[3] = {sim->u[k], sim->v[k], sim->w[k]};
+        float* host_f[3] = {st->u[k], st->v[k], st->w[k]};
+        for (int j = 0; j < 1; ++j) {
+            if (!host_c[j]) continue;
+            cudaMemcpy3DParms m =
+                to_device ? copy3d(dev_c[j], (size_t)g.X * 4, g.ny + 1, host_c[j], (size_t)g.nx * 4, g.ny,
+                                   (size_t)g.nx * 4, g.ny, g.nz, cudaMemcpyHostToDevice)
+                          : copy3d(host_c[j], (size_t)g.nx * 4, g.ny, dev_c[j], (size_t)g.X * 4, g.ny + 1,
+                                   (size_t)g.nx * 4, g.ny, g.nz, cudaMemcpyDeviceToHost);
+            SMK_CUDA(cudaMemcpy3D(&m));
+        }
+        for (int j = 0; j < 3; ++j) {
+            if (!host_f[j]) continue;
+            size_t wb = (size_t)(g.nx + 1) * 4;
+            cudaMemcpy3DParms m =
+                to_device ? copy3d(dev_f[j], (size_t)g.X * 4, g.ny + 1, host_f[j], wb, g.ny + 1, wb,
+                                   g.ny + 1, g.nz + 1, cudaMemcpyHostToDevice)
+                          : copy3d(host_f[j], wb, g.ny + 1, dev_f[j], (size_t)g.X * 4, g.ny + 1, wb,
+                                   g.ny + 1, g.nz + 1, cudaMemcpyDeviceToHost);
+            SMK_CUDA(cudaMemcpy3D(&m));
+        }
+    }
+    if (st->s) {
+        if (to_device) {
+            int rc = sim->upload_mask(st->s);
+            if (rc) return rc;
+        } else {
+            auto m = copy3d(st->s, g.nx, g.ny, sim->s, g.X, g.ny + 1, g.nx, g.ny, g.nz,
+                            cudaMemcpyDeviceToHost);
+            SMK_CUDA(cudaMemcpy3D(&m));
+        }
+    }
+    return SMK_OK;
+}
+
+int smk_read_state(smk_sim* sim, const smk_host_state* st) {
+    int rc = state_copy(sim, st, false);
+    if (rc == SMK_OK) const_cast<smk_host_state*>(st)->index_now = sim->index_now;
+    return rc;
+}
+
+int smk_write_state(smk_sim* sim, const smk_host_state* st) {
+    if (st && st->index_now != 0 && st->index_now != 1)
+        return fail(SMK_ERR_INVALID, "index_now must be 0 or 1");
+    int rc = state_copy(sim, st, true);
+    if (rc == SMK_OK) sim->index_now = st->index_now;
+    return rc;
+}
+
+int smk_get_stats(smk_sim* sim, smk_stats* out) {
+    if (!sim || !out) return fail(SMK_ERR_INVALID, "null argument");
+    DeviceGuard dg(sim->device);
+    memset(out, 0, sizeof(*out));
+    out->step_index = sim->steps;
+    out->div_max = -1.0f;
+    if (sim->steps == 0) return SMK_OK;
+    std::vector<unsigned> host(4 + sim->status_groups);
+    SMK_CUDA(cudaDeviceSynchronize());
+    SMK_CUDA(cudaMemcpy(host.data(), sim->status, sizeof(StepStatus) + sizeof(unsigned) * sim->status_groups,
+                        cudaMemcpyDeviceToHost));
+    StepStatus hs;
+    memcpy(&hs, host.data(), sizeof(StepStatus) - sizeof(unsigned));
+    const unsigned* rmax = host.data() + 4;
+    if (sim->p.report_div) {
+        float d;
+        memcpy(&d, &hs.div_bits, 4);
+        out->div_max = d;
+    }
+    if (sim->last_projection == SMK_PROJECT_REFERENCE) {
+        out->sweeps = sim->last_max_sweeps;
+    } else if (sim->last_tol > 0) {
+        int ng = sim->last_groups;
+        int G = sim->last_check_every;
+        if (hs.done) {
+            out->sweeps = hs.done_group * G;
+            out->converged = 1;
+            memcpy(&out->resid_max, &rmax[hs.done_group - 1], 4);
+        } else {
+            out->sweeps = sim->last_max_sweeps;
+            float r = 0;
+            if (ng > 0) memcpy(&r, &rmax[ng - 1], 4);
+            out->resid_max = r;
+            out->converged = (ng > 0 && r <= sim->last_tol) ? 1 : 0;
+        }
+    } else {
+        out->sweeps = sim->last_max_sweeps;
+    }
+    return SMK_OK;
+}
+
+int smk_set_timing(smk_sim* sim, int enable) {
+    if (!sim) return fail(SMK_ERR_INVALID, "sim is null");
+    sim->timing = enable != 0;
+    return SMK_OK;
+}
+
+int smk_get_stage_times(smk_sim* sim, float* ms, int count) {
+    if (!sim || !ms) return fail(SMK_ERR_INVALID, "null argument");
+    if (!sim->timing || sim->steps == 0) return fail(SMK_ERR_STATE, "timing not enabled or no step taken");
+    DeviceGuard dg(sim->device);
+    SMK_CUDA(cudaEventSynchronize(sim->ev[4]));
+    float t[5];
+    for (int k = 0; k < 4; ++k) SMK_CUDA(cudaEventElapsedTime(&t[k], sim->ev[k], sim->ev[k + 1]));
+    SMK_CUDA(cudaEventElapsedTime(&t[4], sim->ev[0], sim->ev[4]));
+    for (int k = 0; k < count && k < 5; ++k) ms[k] = t[k];
+    return SMK_OK;
+}
+
+long long smk_launch_count(const smk_sim* sim) { return sim ? sim->launches : 0; }
+
+}  // extern "C"

@@ -1,0 +1,59 @@
+// The simulation handle behind smk_sim* (host side).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <vector>
+
+#include "../../include/smoke_gb300.h"
+#include "common.cuh"
+
+struct smk_sim {
+    enum Kind { OBJ_OBSTACLE = 0, OBJ_SPHERE = 1, OBJ_BOX = 2 };
+    struct Object {
+        int kind;
+        smk::SphereObj sphere;
+        smk::ObstacleObj obstacle;
+        smk::BoxObj box;
+    };
+
+    smk::Grid g{};
+    smk_params p{};
+    int device = 0;
+
+    // Ping-pong fields (the reference's dev_smoke/u/v/w[2], smokeSimulation.cu:20-23), the
+    // pressure-scheme P and b, the mask (dev_s, :24) and its derived neighbour flags.
+    float* rho[2] = {nullptr, nullptr};
+    float* u[2] = {nullptr, nullptr};
+    float* v[2] = {nullptr, nullptr};
+    float* w[2] = {nullptr, nullptr};
+    float* P = nullptr;
+    float* b = nullptr;
+    uint8_t* s = nullptr;
+    uint8_t* flags = nullptr;
+    smk::StepStatus* status = nullptr;
+    int status_groups = 0;
+
+    int index_now = 1;  // indexNow (:707)
+    std::vector<Object> objects;
+    bool mask_dirty = true;
+    bool obstacles_dirty = false;
+
+    bool timing = false;
+    cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    long long launches = 0;
+    int steps = 0;
+
+    // what the last step ran (for smk_get_stats)
+    int last_projection = 0;
+    float last_tol = 0.0f;
+    int last_max_sweeps = 0;
+    int last_check_every = 1;
+    int last_groups = 0;
+
+    size_t elems() const { return (size_t)g.XY * (size_t)(g.nz + 1); }
+    int alloc();
+    void release();
+    int upload_mask(const uint8_t* host);
+    int step(float dt, cudaStream_t st);
+};

@@ -1,0 +1,207 @@
+"""GPU parity tests through the C ABI.
+
+REFERENCE scheme: bit-exact with the reference's own step (golden vectors generated from its
+host build) and with the oracle restatement, on every field of both ping-pong buffers.
+PRESSURE scheme: bit-exact with the oracle's pressure-form restatement (same operation order),
+and within the stated tolerances (tests/helpers.py) of the reference form and of FP64.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import smoke_simulation_gb300 as smk
+from oracle import oracle as O
+from smoke_simulation_gb300 import scenes as S
+from tests import helpers as H
+
+pytestmark = pytest.mark.gpu
+
+
+def _run_gpu(sc, steps=None, **over):
+    sim = smk.from_scene(sc, **over)
+    for _ in range(sc.steps if steps is None else steps):
+        sim.step(sc.dt)
+    return sim
+
+
+@pytest.mark.parametrize("name,scene", [
+    ("tiny", lambda: S.small_scene(12, 10, 11, steps=5, seed=3)),
+    ("small_a", lambda: S.small_scene()),
+    ("small_b", lambda: S.small_scene(17, 23, 19, seed=5, obstacles=2, sources=3)),
+])
+def test_reference_scheme_matches_golden_small(gpu, name, scene):
+    g = H.golden()["scenes"][name]
+    sim = _run_gpu(scene())
+    st = sim.read_state()
+    if H.state_hashes(st) != g["final"]:
+        o = O.OracleSim(scene()).run()
+        pytest.fail(H.first_mismatch(st, H.oracle_state(o)))
+    assert H.sha(sim.read_density()) == g["density_out"]
+    sim.close()
+
+
+def test_reference_scheme_matches_golden_ref80(gpu):
+    g = H.golden()["scenes"]["ref80"]
+    sc = S.config_ref80(steps=100)
+    sim = smk.from_scene(sc)
+    out = np.zeros(sc.cell_shape, np.float32)
+    for k in range(100):
+        sim.simulate(out, sc.dt)
+        if (k + 1) % 20 == 0:
+            assert H.sha(out) == g["density_every_20"][str(k + 1)], k + 1
+    assert H.state_hashes(sim.read_state()) == g["final"]
+    sim.close()
+
+
+@pytest.mark.parametrize("dims,seed,kw", [
+    ((9, 8, 7), 21, {}),
+    ((16, 16, 16), 22, {"obstacles": 3, "sources": 3}),
+    ((31, 12, 20), 23, {"noise": 4.0}),
+    ((5, 5, 5), 24, {"boxes": 0, "obstacles": 0}),
+    ((3, 40, 4), 25, {}),
+    ((67, 33, 45), 26, {"obstacles": 2, "sources": 2}),
+])
+def test_reference_scheme_equals_oracle_stepwise(gpu, dims, seed, kw):
+    sc = S.small_scene(*dims, steps=4, seed=seed, **kw)
+    o = O.OracleSim(sc)
+    sim = smk.from_scene(sc)
+    for k in range(sc.steps):
+        o.step()
+        sim.step(sc.dt)
+        msg = H.first_mismatch(sim.read_state(), H.oracle_state(o))
+        assert msg == "", "step %d: %s" % (k, msg)
+    sim.close()
+
+
+def test_reference_api_symbols_match_golden_app80(gpu):
+    """The reference's own C++ entry points (mangled names, exactly as main.cpp calls them)."""
+    L = smk.lib()
+    f = C.c_float
+    init = L["_Z16initializeVolumePfjjj"]
+    init.argtypes = [C.c_void_p, C.c_uint, C.c_uint, C.c_uint]
+    add_src = L["_Z14addSmokeSourceffff"]
+    add_src.argtypes = [f] * 4
+    add_src.restype = C.c_int
+    add_obs = L["_Z11addObstaclefffffff"]
+    add_obs.argtypes = [f] * 7
+    add_obs.restype = C.c_int
+    upd = L["_Z15updateObjectPosifff"]
+    upd.argtypes = [C.c_int, f, f, f]
+    simulate = L["_Z8simulatePff"]
+    simulate.argtypes = [C.c_void_p, f]
+    grav = L["_Z10getGravityv"]
+    grav.restype = C.POINTER(f)
+    buoy = L["_Z11getBuoyancyv"]
+    buoy.restype = C.POINTER(f)
+    delete = L["_Z12deleteVolumev"]
+
+    g = H.golden()["scenes"]["app80"]
+    grid = np.zeros((80, 80, 80), np.float32)
+    init(grid.ctypes.data, 80, 80, 80)
+    sid = add_src(40.0, 40.0, 40.0, 5.0)
+    add_obs(60.0, 10.0, 60.0, 0.0, 0.0, 0.0, 13.0)
+    grav()[0], buoy()[0] = -9.82, 2.0
+    simulate(grid.ctypes.data, 0.01)
+    for k in range(20):
+        if k == 10:
+            grav()[0], buoy()[0] = -5.0, 6.0
+        upd(sid, *H.app80_path(k))
+        simulate(grid.ctypes.data, 0.05)
+        assert H.sha(grid) == g["density_each_step"][str(k + 1)], k + 1
+    delete()
+
+
+@pytest.mark.parametrize("dims,seed", [((20, 16, 18), 11), ((33, 17, 29), 41), ((64, 64, 64), 42)])
+@pytest.mark.parametrize("tol", [0.0, 1e-3])
+def test_pressure_scheme_equals_oracle(gpu, dims, seed, tol):
+    sc = S.small_scene(*dims, steps=5, seed=seed, scheme=1, iterations=40, tol=tol,
+                       check_every=4, obstacles=2)
+    o = O.OracleSim(sc)
+    sim = smk.from_scene(sc, report_div=1)
+    for k in range(sc.steps):
+        ost = o.step()
+        sim.step(sc.dt)
+        st = sim.stats()
+        assert st.sweeps == ost.sweeps, (k, st.sweeps, ost.sweeps)
+        assert st.converged == ost.converged
+        if tol > 0:
+            assert st.resid_max == ost.resid_max
+        assert st.div_max == ost.div_max
+        msg = H.first_mismatch(sim.read_state(), H.oracle_state(o))
+        assert msg == "", "step %d: %s" % (k, msg)
+    sim.close()
+
+
+def test_pressure_scheme_within_tolerance_of_reference_and_fp64(gpu):
+    sc = S.config_ref80(steps=40)
+    sim = _run_gpu(sc, projection=1)
+    rho = sim.read_density()
+    ref = O.OracleSim(sc, np.float32, 0).run()
+    f64 = O.OracleSim(sc, np.float64, 0).run()
+    assert H.max_abs(rho, ref.density()) <= H.DENSITY_MAX_ABS
+    assert H.rel_l2(rho, ref.density()) <= H.DENSITY_REL_L2
+    assert H.max_abs(rho, f64.density()) <= H.DENSITY_MAX_ABS
+    assert H.rel_l2(rho, f64.density()) <= H.DENSITY_REL_L2
+    sim.close()
+
+
+def test_large_grid_properties(gpu):
+    """256^3 workload, two steps: finite fields, mask kept bit-exact, tolerance rule honoured,
+    and the post-projection divergence within the tolerance when converged."""
+    sc = S.config_large(n=256, steps=2)
+    sim = smk.from_scene(sc, report_div=1)
+    for _ in range(2):
+        sim.step(sc.dt)
+        st = sim.stats()
+        assert st.sweeps <= sc.iterations and (st.sweeps % sc.check_every == 0
+                                                or st.sweeps == sc.iterations)
+        if st.converged:
+            assert st.resid_max <= sc.tol
+        assert np.isfinite(st.div_max)
+    s = sim.read_state()
+    assert np.array_equal(s["s"], sc.mask)
+    for k in ("rho", "u", "v", "w"):
+        for j in range(2):
+            assert np.isfinite(s[k][j]).all()
+    assert s["rho"][s["index_now"] ^ 1].max() == 1.0
+    sim.close()
+
+
+def test_state_roundtrip_and_resume(gpu):
+    """read_state / write_state reproduce a run exactly (checkpoint / resume)."""
+    sc = S.small_scene(24, 20, 22, steps=6, seed=9, scheme=1, iterations=20)
+    a = _run_gpu(sc, steps=3)
+    ck = a.read_state()
+    b = smk.from_scene(sc)
+    b.write_state(ck)
+    for _ in range(3):
+        a.step(sc.dt)
+        b.step(sc.dt)
+    assert H.first_mismatch(a.read_state(), b.read_state()) == ""
+    a.close()
+    b.close()
+
+
+def test_density_to_device_buffer(gpu):
+    import torch
+    sc = S.small_scene(16, 12, 14, steps=2, seed=4)
+    sim = _run_gpu(sc)
+    dev = torch.empty(sc.cell_shape, dtype=torch.float32, device=gpu)
+    stream = torch.cuda.current_stream().cuda_stream
+    sim.read_density_device(dev.data_ptr(), stream)
+    torch.cuda.synchronize()
+    assert H.bits_equal(dev.cpu().numpy(), sim.read_density())
+    sim.close()
+
+
+def test_stage_timing_and_launch_count(gpu):
+    sc = S.small_scene(32, 32, 32, steps=2, seed=5, scheme=1, iterations=10)
+    sim = smk.from_scene(sc)
+    sim.set_timing(True)
+    n0 = sim.launch_count()
+    sim.step(sc.dt)
+    t = sim.stage_times()
+    assert (t >= 0).all() and t[4] >= t[:4].sum() * 0.99
+    assert sim.launch_count() > n0
+    sim.close()
