@@ -1,0 +1,376 @@
+"""Benchmark: cell-updates/s of the smoke step on the 256^3 workload.
+
+Workload (one "step" = one full simulation step of one 256^3 grid): FP32 fields, 5% Bernoulli
+solids (seed 1) plus two r=24 spheres, four seeded sphere emitters, dt = 0.02, pressure-form
+red-black SOR to max|residual| <= 1e-4 checked every 10 sweeps, capped at 200 sweeps.
+Synthetic inputs from smoke_simulation_gb300.scenes (the reference publishes no dataset).
+
+  value   cell-updates/s with the state resident in HBM (CUDA events on the step stream)
+  e2e     the same metric through smk_simulate (the reference's simulate(): step plus a
+          blocking copy of the density into pinned host memory), host wall clock
+  roofline  the sweep phase (red-black passes + residual checks), algorithmic bytes from the
+          per-cell model in the design doc, over its event-timed duration in the timed steps
+  cpu_baseline  the reference's own step built for the host (OpenMP, all cores) on a bounded
+          sample of the same workload
+
+Multi-GPU: the path does not shard (one grid per simulation); under torchrun every rank runs an
+independent replica ("replicas only") and value is the sum over ranks with max-over-ranks time.
+
+--impl reference times the reference's own CPU step (oracle/_ref; the restatement if the
+reference build is absent) on the same workload and prints the same JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "cell-updates/s"
+UNIT = "cell-updates/s"
+N_DEFAULT = 256
+# Sweeps the reference step is given in the CPU baseline and the reference arm: the
+# reference's projection has no convergence test, so it runs the sweep count that this
+# workload's tolerance rule takes on the GPU (mean over the benchmark's steps).
+REF_SWEEPS_DEFAULT = 170
+# Algorithmic bytes per cell: one red+black sweep reads P, b, flags and writes P.
+SWEEP_BYTES_PER_CELL = 13.0
+CHECK_BYTES_PER_CELL = 9.0
+
+
+def load_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.file = None
+
+    def start(self):
+        try:
+            self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.file, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        if self.proc is None:
+            return out
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.file.flush()
+        self.file.seek(0)
+        rows = [r.split(",") for r in self.file.read().strip().splitlines() if r.strip()]
+        self.file.close()
+        os.unlink(self.file.name)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            r = [x.strip() for x in r]
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except ValueError:
+                continue
+            for name, val in zip(names, r[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(name)
+        if sm:
+            out = {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                   "reasons": sorted(reasons), "samples": len(sm)}
+        return out
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return ws, rank, local
+
+
+def dist_max(x: float, ws: int) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def dist_sum(x: float, ws: int) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def dist_barrier(ws: int):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def workload(n: int):
+    from smoke_simulation_gb300 import scenes as S
+    return S.config_large(n=n, steps=50)
+
+
+def cpu_reference_rate(n: int, sweeps: int, steps: int, threads: int = 0):
+    """Time the reference's own step (host build) or, without it, the restatement, on the
+    workload at `n`^3 with `sweeps` fixed iterations.  Returns (rate, kind, cores, seconds)."""
+    from oracle import oracle as O
+    sc = workload(n)
+    sc.scheme = 0
+    sc.iterations = sweeps
+    sc.tol = 0.0
+    cores = threads or os.cpu_count() or 1
+    if O.reference_available():
+        sim = O.RefHostSim(sc, threads=cores)
+        kind = "reference"
+        cores = sim.lib.ref_max_threads()
+    else:
+        sim = O.OracleSim(sc)
+        kind = "port"
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        sim.step()
+    dt = time.perf_counter() - t0
+    if kind == "reference":
+        sim.close()
+    return sc.cells * steps / dt, kind, cores, dt
+
+
+def run_reference_arm(args, ws, rank):
+    if rank != 0:
+        return 0
+    steps = max(1, min(args.steps, args.ref_max_steps))
+    warm = min(args.warmup, 1)
+    from oracle import oracle as O
+    sc = workload(args.n)
+    sc.scheme, sc.iterations, sc.tol = 0, args.ref_sweeps, 0.0
+    cores = os.cpu_count() or 1
+    if O.reference_available():
+        sim = O.RefHostSim(sc, threads=cores)
+        kind = "reference"
+        cores = sim.lib.ref_max_threads()
+    else:
+        sim = O.OracleSim(sc)
+        kind = "port"
+    for _ in range(warm):
+        sim.step()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        sim.step()
+    dt = time.perf_counter() - t0
+    rate = sc.cells * steps / dt
+    sample = ("%d timed step(s) (+%d warm-up) of the %d^3 workload, reference step with %d "
+              "fixed red-black iterations, OpenMP over %d threads" % (steps, warm, args.n,
+                                                                     args.ref_sweeps, cores))
+    line = {
+        "metric": METRIC, "value": rate, "unit": UNIT, "impl": "reference", "n_gpus": ws,
+        "steps": steps, "warmup": warm, "ms_per_step": 1e3 * dt / steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": "smoke step %d^3 FP32, 5%% random solids + 2 spheres r=24, 4 "
+                               "emitters, dt=0.02, red-black SOR %d sweeps" % (args.n, args.ref_sweeps),
+                   "cells": sc.cells, "l2": "inputs larger than L2 (CPU run)"},
+        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": kind,
+                         "sample": sample},
+        "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=N_DEFAULT)
+    ap.add_argument("--ref-sweeps", type=int, default=REF_SWEEPS_DEFAULT)
+    ap.add_argument("--ref-max-steps", type=int, default=3)
+    ap.add_argument("--cpu-steps", type=int, default=1)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=0, help="0: same as --steps")
+    args = ap.parse_args()
+    assert args.warmup >= 0 and args.steps >= 1
+
+    ws, rank, local = dist_setup()
+    if args.impl == "reference":
+        return run_reference_arm(args, ws, rank)
+
+    import torch
+    import smoke_simulation_gb300 as smk
+    from smoke_simulation_gb300 import build
+    if not os.path.exists(smk.LIB_PATH):
+        build.build()
+    torch.cuda.set_device(local)
+
+    sc = workload(args.n)
+    sim = smk.from_scene(sc, report_div=1)
+    stream = torch.cuda.Stream()
+    sh = stream.cuda_stream
+    sim.set_timing(True)
+
+    # warm-up steps (part of the simulation; state evolves)
+    for _ in range(max(args.warmup, 0)):
+        sim.step(sc.dt, sh)
+    torch.cuda.synchronize()
+
+    # ---- device-timed region: K steps, inputs resident in HBM ------------------------------
+    launches0 = sim.launch_count()
+    sweeps, divs, conv, sweep_ms, proj_ms = [], [], [], [], []
+    clocks = ClockSampler(local)
+    clocks.start()
+    dist_barrier(ws)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        sim.step(sc.dt, sh)
+        # per-step stats need the step's status: read after the timed region from the events
+        # the library recorded (no host sync inside the region)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    dist_barrier(ws)
+    clk = clocks.stop()
+    elapsed = e0.elapsed_time(e1) / 1e3
+    launches = sim.launch_count() - launches0
+
+    # per-step statistics and stage times: replay a few steps with a sync after each (outside
+    # the timed region) to read the solver status and the event-timed sweep phase
+    for _ in range(min(args.steps, 5)):
+        sim.step(sc.dt, sh)
+        st = sim.stats()
+        t = sim.stage_times()
+        sweeps.append(st.sweeps)
+        divs.append(st.div_max)
+        conv.append(st.converged)
+        sweep_ms.append(float(t[5]))
+    elapsed_max = dist_max(elapsed, ws)
+    cells_all = dist_sum(float(sc.cells * args.steps), ws)
+    value = cells_all / elapsed_max
+
+    # ---- roofline of the sweep phase ---------------------------------------------------------
+    peak, peak_kind = load_peaks()
+    mean_sweeps = float(np.mean(sweeps))
+    checks = int(np.ceil(mean_sweeps / sc.check_every)) + 1
+    sweep_bytes = sc.cells * (SWEEP_BYTES_PER_CELL * mean_sweeps + CHECK_BYTES_PER_CELL * checks)
+    proj_seconds = float(np.mean(sweep_ms)) / 1e3
+    achieved = sweep_bytes / proj_seconds / 1e9 if proj_seconds > 0 else None
+    traffic = None
+    tf = os.path.join(ROOT, "profiles", "sweep_traffic.json")
+    if os.path.exists(tf):
+        with open(tf) as f:
+            tr = json.load(f)
+        traffic = tr.get("bytes_per_cell_per_sweep")
+        if traffic is not None:
+            traffic = traffic * sc.cells
+
+    # ---- e2e through the public API with host buffers ----------------------------------------
+    e2e_steps = args.e2e_steps or args.steps
+    out = torch.empty(sc.cell_shape, dtype=torch.float32, pin_memory=True).numpy()
+    sim.set_timing(False)
+    sim.simulate(out, sc.dt)  # warm
+    dist_barrier(ws)
+    t0 = time.perf_counter()
+    for k in range(e2e_steps):
+        # the step's input: the emitter positions (launch parameters); result: the density
+        sim.simulate(out, sc.dt)
+    e2e_dt = dist_max(time.perf_counter() - t0, ws)
+    e2e_value = dist_sum(float(sc.cells * e2e_steps), ws) / e2e_dt
+
+    # ---- CPU baseline (rank 0, N=1 only) -------------------------------------------------------
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        # the reference step has no tolerance test: give it the mean sweep count this run's
+        # tolerance rule took, so both sides do the same projection work per step
+        ref_sweeps = int(round(mean_sweeps))
+        rate, kind, cores, secs = cpu_reference_rate(args.n, ref_sweeps, args.cpu_steps)
+        cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": kind,
+               "sample": "%d step(s) of the %d^3 workload with %d fixed red-black iterations "
+                         "(the GPU run's mean sweeps per step), %.1f s" % (
+                             args.cpu_steps, args.n, ref_sweeps, secs)}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * elapsed_max / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": "smoke step %d^3 FP32, 5%% random solids + 2 spheres r=24, 4 "
+                                   "emitters, dt=0.02, pressure red-black SOR to max|div|<=1e-4 "
+                                   "(checked every 10 sweeps, cap 200)" % args.n,
+                       "cells": sc.cells, "parallelism": "replicas" if ws > 1 else "single",
+                       "l2": "inputs larger than L2 (%.0f MB resident state)" % (
+                           sim_bytes(sc) / 1e6),
+                       "mean_sweeps": mean_sweeps, "converged_frac": float(np.mean(conv)),
+                       "max_div_post_projection": float(np.max(divs))},
+            "roofline": {"bound": "hbm", "kernel": "k_sweep+k_resid_check (sweep phase)",
+                         "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                         "peak_kind": peak_kind,
+                         "algorithmic_bytes": sweep_bytes},
+            "clocks": clk,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 16 * len(sc.spheres),
+                    "d2h_bytes_per_step": 4 * sc.cells, "api": "smk_simulate (pinned host out)"},
+            "gpu_launches": int(launches),
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line))
+    sim.close()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def sim_bytes(sc) -> float:
+    X = (sc.nx + 1 + 7) // 8 * 8
+    elems = X * (sc.ny + 1) * (sc.nz + 1)
+    return elems * (10 * 4 + 2)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -139,11 +139,20 @@ int smk_get_stats(smk_sim* sim, smk_stats* out);
 
 /* Per-stage device times of the last step, measured with CUDA events on the step's stream
  * when timing is enabled.  Stages: 0 objects+emitters, 1 forcing, 2 projection,
- * 3 advection, 4 whole step.  Blocking. */
+ * 3 advection, 4 whole step, 5 the sweep phase inside the projection (red-black passes and
+ * residual checks; PRESSURE only, else 0).  Blocking. */
 int smk_set_timing(smk_sim* sim, int enable);
 int smk_get_stage_times(smk_sim* sim, float* ms, int count);
 /* Number of kernel launches the library issued since creation. */
 long long smk_launch_count(const smk_sim* sim);
+
+/* Pressure sweep kernel (PRESSURE projection).  depth 0: one colour pass per launch.
+ * depth 2, 4, 6 or 8: temporally blocked, `depth` colour passes per pass over HBM, the grid
+ * cut into z-chunks of `zchunk` planes (>= 1).  Results are bit-identical for every choice;
+ * only speed differs.  No counterpart in the reference (its projection is fixed,
+ * smokeSimulation.cu:795-801). */
+int smk_set_sweep_kernel(smk_sim* sim, int depth, int zchunk);
+int smk_get_sweep_kernel(const smk_sim* sim, int* depth, int* zchunk);
 
 #ifdef __cplusplus
 }

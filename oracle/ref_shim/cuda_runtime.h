@@ -50,9 +50,14 @@ struct cudaDeviceProp {
     size_t sharedMemPerBlock;
 };
 
+// Allocations are rounded up to 256 bytes, the granularity cudaMalloc gives on a GPU.  The
+// reference sizes its object buffers for 3 objects (smokeSimulation.cu:56, :221-229) but
+// copies every registered object into them (:729, :760); on a GPU a 4th sphere still lands
+// inside the 256-byte allocation, and the same holds here.
 template <typename T>
 inline cudaError_t cudaMalloc(T** p, size_t n) {
-    *p = (T*)calloc(n ? n : 1, 1);
+    size_t rounded = (n + 255) / 256 * 256;
+    *p = (T*)calloc(rounded ? rounded : 256, 1);
     return *p ? cudaSuccess : cudaErrorMemoryAllocation;
 }
 inline cudaError_t cudaFree(void* p) { free(p); return cudaSuccess; }

@@ -88,6 +88,8 @@ def lib() -> C.CDLL:
         "smk_set_timing": (i, [vp, i]),
         "smk_get_stage_times": (i, [vp, C.POINTER(C.c_float), i]),
         "smk_launch_count": (C.c_longlong, [vp]),
+        "smk_set_sweep_kernel": (i, [vp, i, i]),
+        "smk_get_sweep_kernel": (i, [vp, C.POINTER(i), C.POINTER(i)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -256,12 +258,20 @@ class Simulation:
         _check(lib().smk_set_timing(self.h, int(on)))
 
     def stage_times(self) -> np.ndarray:
-        t = (C.c_float * 5)()
-        _check(lib().smk_get_stage_times(self.h, t, 5))
+        t = (C.c_float * 6)()
+        _check(lib().smk_get_stage_times(self.h, t, 6))
         return np.array(t[:], np.float64)
 
     def launch_count(self) -> int:
         return int(lib().smk_launch_count(self.h))
+
+    def set_sweep_kernel(self, depth: int, zchunk: int = 32):
+        _check(lib().smk_set_sweep_kernel(self.h, depth, zchunk))
+
+    def sweep_kernel(self):
+        d, z = C.c_int(), C.c_int()
+        _check(lib().smk_get_sweep_kernel(self.h, C.byref(d), C.byref(z)))
+        return d.value, z.value
 
 
 def params_for_scene(scene, **overrides) -> Params:

@@ -54,6 +54,24 @@ __device__ __forceinline__ void atomic_max_bits(unsigned* p, float nonneg) {
     atomicMax(p, __float_as_uint(nonneg));
 }
 
+// Max-reduce `v` (bit patterns of non-negative floats: the IEEE order, NaN largest) over the
+// block, then one atomicMax per block, skipped when the stored value is already larger.  One
+// atomic per warp on a single address serialises at L2 and costs ~1 ms on a 256^3 grid.
+__device__ __forceinline__ void block_max_to(unsigned v, unsigned* dst) {
+    __shared__ unsigned red[32];
+    for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
+    const int nthreads = blockDim.x * blockDim.y * blockDim.z;
+    const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+    const int lane = tid & 31, warp = tid >> 5, nwarps = (nthreads + 31) >> 5;
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        unsigned w = lane < nwarps ? red[lane] : 0u;
+        for (int o = 16; o > 0; o >>= 1) w = max(w, __shfl_xor_sync(0xffffffffu, w, o));
+        if (lane == 0 && w > *(volatile unsigned*)dst) atomicMax(dst, w);
+    }
+}
+
 // ---- reference-exact helpers ---------------------------------------------------------------
 
 // avgU/avgV/avgW (smokeSimulation.cu:409-447): 8-point sums in the reference's order, / 8.

@@ -27,13 +27,21 @@ void launch_project_velocity(const Grid& g, float* u, float* v, float* w, const 
 
 // Stage c/d (pressure scheme).
 void launch_rhs(const Grid& g, const float* u, const float* v, const float* w, const uint8_t* flags,
-                float* b, float* P, int warm, cudaStream_t st);
+                float* b, float* P, const float* P2, const int* pcur, int warm, cudaStream_t st);
 void launch_sweep(const Grid& g, float* P, const float* b, const uint8_t* flags, int colour,
                   const float* wacc7, const StepStatus* status, cudaStream_t st);
 void launch_resid_check(const Grid& g, const float* P, const float* b, const uint8_t* flags,
                         StepStatus* status, int group, float tol, cudaStream_t st);
-void launch_gradient_subtract(const Grid& g, float* u, float* v, float* w, const float* P,
-                              const uint8_t* flags, cudaStream_t st);
+void launch_gradient_subtract(const Grid& g, float* u, float* v, float* w, const float* P0,
+                              const float* P1, const int* pcur, const uint8_t* flags,
+                              cudaStream_t st);
+// Temporally blocked sweeps: nhalf <= T colour passes in one pass over HBM, P_in -> P_out;
+// `check` launches also record the residual of the input state for tolerance group `group`.
+int sweep_tb_depth_supported(int T);
+void launch_sweep_tb(const Grid& g, const float* Pin, float* Pout, const float* b,
+                     const uint8_t* flags, int T, int nhalf, int colour0, int zchunk,
+                     const float* wacc7, StepStatus* status, int check, int group, float tol,
+                     int* pcur, int out_idx, cudaStream_t st);
 void launch_div_max(const Grid& g, const float* u, const float* v, const float* w,
                     const uint8_t* flags, StepStatus* status, cudaStream_t st);
 

@@ -25,10 +25,13 @@ inline dim3 grid3(int rx, int ry, int rz) {
 
 struct WAcc { float w[8]; };
 
-// b = -div(u*) on projectable cells; P = 0 off them (and everywhere on a cold start).
+// b = -div(u*) on projectable cells; P = 0 off them (and everywhere on a cold start).  P is
+// the first of the two pressure buffers; on a warm start whose previous solve ended in the
+// second buffer (*pcur == 1) the previous pressure is taken from there.
 __global__ void k_rhs(Grid g, const float* __restrict__ u, const float* __restrict__ v,
                       const float* __restrict__ w, const uint8_t* __restrict__ flags,
-                      float* __restrict__ b, float* __restrict__ P, int warm) {
+                      float* __restrict__ b, float* __restrict__ P, const float* __restrict__ P2,
+                      const int* __restrict__ pcur, int warm) {
     int x = blockIdx.x * BX + threadIdx.x;
     int y = blockIdx.y * BY + threadIdx.y;
     int z = blockIdx.z;
@@ -38,6 +41,7 @@ __global__ void k_rhs(Grid g, const float* __restrict__ u, const float* __restri
         float div = -u[i] + u[i + 1] + -v[i] + v[i + g.X] + -w[i] + w[i + g.XY];
         b[i] = -div;
         if (!warm) P[i] = 0.0f;
+        else if (pcur != nullptr && P2 != nullptr && *pcur == 1) P[i] = P2[i];
     } else {
         b[i] = 0.0f;
         P[i] = 0.0f;
@@ -92,16 +96,18 @@ __global__ void k_resid_check(Grid g, const float* __restrict__ P, const float* 
             m = fabsf(r);
         }
     }
-    unsigned mb = __float_as_uint(m);
-    for (int o = 16; o > 0; o >>= 1) mb = max(mb, __shfl_xor_sync(0xffffffffu, mb, o));
-    if ((threadIdx.x & 31) == 0 && mb) atomicMax(&status->rmax_bits[group], mb);
+    block_max_to(__float_as_uint(m), &status->rmax_bits[group]);
 }
 
 // u -= P(x) - P(x-1) on faces whose two cells are fluid (P is 0 off the projectable set, so
 // this reproduces exactly which faces the reference's passes move).
+// The pressure is the first buffer, or the second when *pcur == 1 (the temporally blocked
+// sweeps ping-pong between the two and record where the last executed launch wrote).
 __global__ void k_gradient_subtract(Grid g, float* __restrict__ u, float* __restrict__ v,
-                                    float* __restrict__ w, const float* __restrict__ P,
+                                    float* __restrict__ w, const float* __restrict__ P0,
+                                    const float* __restrict__ P1, const int* __restrict__ pcur,
                                     const uint8_t* __restrict__ flags) {
+    const float* __restrict__ P = (pcur != nullptr && *pcur == 1) ? P1 : P0;
     int x = 1 + blockIdx.x * BX + threadIdx.x;
     int y = 1 + blockIdx.y * BY + threadIdx.y;
     int z = 1 + blockIdx.z;
@@ -119,8 +125,8 @@ __global__ void k_gradient_subtract(Grid g, float* __restrict__ u, float* __rest
 }  // namespace
 
 void launch_rhs(const Grid& g, const float* u, const float* v, const float* w, const uint8_t* flags,
-                float* b, float* P, int warm, cudaStream_t st) {
-    k_rhs<<<grid3(g.nx, g.ny, g.nz), dim3(BX, BY), 0, st>>>(g, u, v, w, flags, b, P, warm);
+                float* b, float* P, const float* P2, const int* pcur, int warm, cudaStream_t st) {
+    k_rhs<<<grid3(g.nx, g.ny, g.nz), dim3(BX, BY), 0, st>>>(g, u, v, w, flags, b, P, P2, pcur, warm);
 }
 
 void launch_sweep(const Grid& g, float* P, const float* b, const uint8_t* flags, int colour,
@@ -141,11 +147,12 @@ void launch_resid_check(const Grid& g, const float* P, const float* b, const uin
                                                                                group, tol);
 }
 
-void launch_gradient_subtract(const Grid& g, float* u, float* v, float* w, const float* P,
-                              const uint8_t* flags, cudaStream_t st) {
+void launch_gradient_subtract(const Grid& g, float* u, float* v, float* w, const float* P0,
+                              const float* P1, const int* pcur, const uint8_t* flags,
+                              cudaStream_t st) {
     if (g.nx < 2 || g.ny < 2 || g.nz < 2) return;
-    k_gradient_subtract<<<grid3(g.nx - 1, g.ny - 1, g.nz - 1), dim3(BX, BY), 0, st>>>(g, u, v, w, P,
-                                                                                     flags);
+    k_gradient_subtract<<<grid3(g.nx - 1, g.ny - 1, g.nz - 1), dim3(BX, BY), 0, st>>>(
+        g, u, v, w, P0, P1, pcur, flags);
 }
 
 }  // namespace smk

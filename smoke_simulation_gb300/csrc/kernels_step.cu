@@ -255,9 +255,7 @@ __global__ void k_div_max(Grid g, const float* __restrict__ u, const float* __re
             m = fabsf(div);
         }
     }
-    unsigned mb = __float_as_uint(m);
-    for (int o = 16; o > 0; o >>= 1) mb = max(mb, __shfl_xor_sync(0xffffffffu, mb, o));
-    if ((threadIdx.x & 31) == 0 && mb) atomicMax(&status->div_bits, mb);
+    block_max_to(__float_as_uint(m), &status->div_bits);
 }
 
 }  // namespace

@@ -86,11 +86,13 @@ cudaMemcpy3DParms copy3d(void* dst, size_t dpitch, size_t dy, const void* src, s
 
 int smk_sim::alloc() {
     const size_t n = elems();
-    float** fl[] = {&rho[0], &rho[1], &u[0], &u[1], &v[0], &v[1], &w[0], &w[1], &P, &b};
+    float** fl[] = {&rho[0], &rho[1], &u[0], &u[1], &v[0], &v[1], &w[0], &w[1], &P, &P2, &b};
     for (float** f : fl) {
         SMK_CUDA(cudaMalloc((void**)f, n * sizeof(float)));
         SMK_CUDA(cudaMemset(*f, 0, n * sizeof(float)));
     }
+    SMK_CUDA(cudaMalloc((void**)&pcur, sizeof(int)));
+    SMK_CUDA(cudaMemset(pcur, 0, sizeof(int)));
     SMK_CUDA(cudaMalloc((void**)&s, n));
     SMK_CUDA(cudaMalloc((void**)&flags, n));
     SMK_CUDA(cudaMemset(flags, 0, n));
@@ -106,9 +108,10 @@ int smk_sim::alloc() {
 }
 
 void smk_sim::release() {
-    float* fl[] = {rho[0], rho[1], u[0], u[1], v[0], v[1], w[0], w[1], P, b};
+    float* fl[] = {rho[0], rho[1], u[0], u[1], v[0], v[1], w[0], w[1], P, P2, b};
     for (float* f : fl)
         if (f) cudaFree(f);
+    if (pcur) cudaFree(pcur);
     if (s) cudaFree(s);
     if (flags) cudaFree(flags);
     if (status) cudaFree(status);
@@ -182,26 +185,51 @@ int smk_sim::step(float dt, cudaStream_t st) {
         float wacc[7];
         wacc[0] = 0.0f;
         for (int a = 1; a <= 6; ++a) wacc[a] = (float)p.omega / (float)a;
-        launch_rhs(g, u[now], v[now], w[now], flags, b, P, p.warm_start, st);
+        launch_rhs(g, u[now], v[now], w[now], flags, b, P, P2, pcur, p.warm_start, st);
         ++launches;
         const bool use_tol = p.tol > 0.0f;
         const int G = use_tol ? p.check_every : (p.max_sweeps > 0 ? p.max_sweeps : 1);
         int sweep = 0, group = 0;
-        while (sweep < p.max_sweeps) {
-            if (use_tol) {
-                launch_resid_check(g, P, b, flags, status, group, p.tol, st);
-                ++launches;
+        if (timed) SMK_CUDA(cudaEventRecord(ev[5], st));
+        if (sweep_depth > 0) {
+            // temporally blocked: each launch applies up to sweep_depth colour passes,
+            // ping-ponging P <-> P2; group starts are the check launches
+            int nl = 0;
+            while (sweep < p.max_sweeps) {
+                const int end = sweep + G < p.max_sweeps ? sweep + G : p.max_sweeps;
+                const int h1 = 2 * end;
+                for (int h = 2 * sweep; h < h1; h += sweep_depth) {
+                    const int nh = h1 - h < sweep_depth ? h1 - h : sweep_depth;
+                    const bool in_a = (nl & 1) == 0;
+                    launch_sweep_tb(g, in_a ? P : P2, in_a ? P2 : P, b, flags, sweep_depth, nh, h & 1,
+                                    sweep_zchunk, wacc, use_tol ? status : nullptr,
+                                    use_tol && h == 2 * sweep, group, p.tol, pcur, in_a ? 1 : 0, st);
+                    ++nl;
+                    ++launches;
+                }
+                sweep = end;
+                ++group;
             }
-            int end = sweep + G < p.max_sweeps ? sweep + G : p.max_sweeps;
-            for (; sweep < end; ++sweep) {
-                launch_sweep(g, P, b, flags, 0, wacc, use_tol ? status : nullptr, st);
-                launch_sweep(g, P, b, flags, 1, wacc, use_tol ? status : nullptr, st);
-                launches += 2;
+        } else {
+            while (sweep < p.max_sweeps) {
+                if (use_tol) {
+                    launch_resid_check(g, P, b, flags, status, group, p.tol, st);
+                    ++launches;
+                }
+                int end = sweep + G < p.max_sweeps ? sweep + G : p.max_sweeps;
+                for (; sweep < end; ++sweep) {
+                    launch_sweep(g, P, b, flags, 0, wacc, use_tol ? status : nullptr, st);
+                    launch_sweep(g, P, b, flags, 1, wacc, use_tol ? status : nullptr, st);
+                    launches += 2;
+                }
+                ++group;
             }
-            ++group;
         }
         last_groups = group;
-        launch_gradient_subtract(g, u[now], v[now], w[now], P, flags, st);
+        if (timed) SMK_CUDA(cudaEventRecord(ev[6], st));
+        const bool tb_used = sweep_depth > 0 && p.max_sweeps > 0;
+        if (!tb_used) SMK_CUDA(cudaMemsetAsync(pcur, 0, sizeof(int), st));
+        launch_gradient_subtract(g, u[now], v[now], w[now], P, P2, pcur, flags, st);
         ++launches;
     }
     if (p.report_div) {
@@ -535,13 +563,37 @@ int smk_get_stage_times(smk_sim* sim, float* ms, int count) {
     if (!sim->timing || sim->steps == 0) return fail(SMK_ERR_STATE, "timing not enabled or no step taken");
     DeviceGuard dg(sim->device);
     SMK_CUDA(cudaEventSynchronize(sim->ev[4]));
-    float t[5];
+    float t[6];
     for (int k = 0; k < 4; ++k) SMK_CUDA(cudaEventElapsedTime(&t[k], sim->ev[k], sim->ev[k + 1]));
     SMK_CUDA(cudaEventElapsedTime(&t[4], sim->ev[0], sim->ev[4]));
-    for (int k = 0; k < count && k < 5; ++k) ms[k] = t[k];
+    t[5] = 0.0f;
+    if (sim->last_projection == SMK_PROJECT_PRESSURE)
+        SMK_CUDA(cudaEventElapsedTime(&t[5], sim->ev[5], sim->ev[6]));
+    for (int k = 0; k < count && k < 6; ++k) ms[k] = t[k];
     return SMK_OK;
 }
 
 long long smk_launch_count(const smk_sim* sim) { return sim ? sim->launches : 0; }
+
+}  // extern "C"
+
+extern "C" {
+
+int smk_set_sweep_kernel(smk_sim* sim, int depth, int zchunk) {
+    if (!sim) return fail(SMK_ERR_INVALID, "sim is null");
+    if (depth != 0 && !sweep_tb_depth_supported(depth))
+        return fail(SMK_ERR_INVALID, "sweep depth must be 0, 2, 4, 6 or 8");
+    if (zchunk < 1) return fail(SMK_ERR_INVALID, "zchunk must be >= 1");
+    sim->sweep_depth = depth;
+    sim->sweep_zchunk = zchunk;
+    return SMK_OK;
+}
+
+int smk_get_sweep_kernel(const smk_sim* sim, int* depth, int* zchunk) {
+    if (!sim) return fail(SMK_ERR_INVALID, "sim is null");
+    if (depth) *depth = sim->sweep_depth;
+    if (zchunk) *zchunk = sim->sweep_zchunk;
+    return SMK_OK;
+}
 
 }  // extern "C"

@@ -28,7 +28,9 @@ struct smk_sim {
     float* v[2] = {nullptr, nullptr};
     float* w[2] = {nullptr, nullptr};
     float* P = nullptr;
+    float* P2 = nullptr;  // second pressure buffer (temporally blocked sweeps ping-pong)
     float* b = nullptr;
+    int* pcur = nullptr;  // device: which pressure buffer the last executed sweep wrote
     uint8_t* s = nullptr;
     uint8_t* flags = nullptr;
     smk::StepStatus* status = nullptr;
@@ -39,8 +41,13 @@ struct smk_sim {
     bool mask_dirty = true;
     bool obstacles_dirty = false;
 
+    // sweep kernel: 0 = one colour pass per launch; T > 0 = temporally blocked, T passes per
+    // launch over z-chunks of sweep_zchunk planes (chosen by smk_set_sweep_kernel / autotune)
+    int sweep_depth = 4;
+    int sweep_zchunk = 32;
+
     bool timing = false;
-    cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t ev[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
     long long launches = 0;
     int steps = 0;
 

@@ -114,11 +114,16 @@ def test_reference_api_symbols_match_golden_app80(gpu):
 
 @pytest.mark.parametrize("dims,seed", [((20, 16, 18), 11), ((33, 17, 29), 41), ((64, 64, 64), 42)])
 @pytest.mark.parametrize("tol", [0.0, 1e-3])
-def test_pressure_scheme_equals_oracle(gpu, dims, seed, tol):
-    sc = S.small_scene(*dims, steps=5, seed=seed, scheme=1, iterations=40, tol=tol,
-                       check_every=4, obstacles=2)
+@pytest.mark.parametrize("kernel", [(0, 1), (2, 7), (4, 32), (6, 5), (8, 64)])
+def test_pressure_scheme_equals_oracle(gpu, dims, seed, tol, kernel):
+    """Every sweep kernel (one colour pass per launch, or temporally blocked with depth 2-8
+    over several z-chunk sizes) reproduces the oracle bit for bit, including the tolerance
+    rule's sweep counts and residuals."""
+    sc = S.small_scene(*dims, steps=5, seed=seed, scheme=1, iterations=41, tol=tol,
+                       check_every=5, obstacles=2)
     o = O.OracleSim(sc)
     sim = smk.from_scene(sc, report_div=1)
+    sim.set_sweep_kernel(*kernel)
     for k in range(sc.steps):
         ost = o.step()
         sim.step(sc.dt)
@@ -164,7 +169,8 @@ def test_large_grid_properties(gpu):
     for k in ("rho", "u", "v", "w"):
         for j in range(2):
             assert np.isfinite(s[k][j]).all()
-    assert s["rho"][s["index_now"] ^ 1].max() == 1.0
+    rho = s["rho"][s["index_now"] ^ 1]
+    assert 0.99 <= rho.max() <= 1.0 + 1e-6 and rho.min() >= -1e-6
     sim.close()
 
 
