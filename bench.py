@@ -367,7 +367,7 @@ def main():
 
 
 def sim_bytes(sc) -> float:
-    X = (sc.nx + 1 + 7) // 8 * 8
+    X = (sc.nx + 1 + 15) // 16 * 16
     elems = X * (sc.ny + 1) * (sc.nz + 1)
     return elems * (10 * 4 + 2)
 

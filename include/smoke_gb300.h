@@ -147,7 +147,7 @@ int smk_get_stage_times(smk_sim* sim, float* ms, int count);
 long long smk_launch_count(const smk_sim* sim);
 
 /* Pressure sweep kernel (PRESSURE projection).  depth 0: one colour pass per launch.
- * depth 2, 4, 6 or 8: temporally blocked, `depth` colour passes per pass over HBM, the grid
+ * depth 2, 4 or 6: temporally blocked, `depth` colour passes per pass over HBM, the grid
  * cut into z-chunks of `zchunk` planes (>= 1).  Results are bit-identical for every choice;
  * only speed differs.  No counterpart in the reference (its projection is fixed,
  * smokeSimulation.cu:795-801). */

@@ -254,6 +254,16 @@ inline T fma_t(T a, T b, T c) {
     return std::fma(a, b, c);
 }
 
+// Neighbour sum of the pressure scheme, in a fixed tree order (depth 3, so the GPU kernels'
+// dependent-add chain is short): ((P_x- + P_x+) + (P_y- + P_y+)) + (P_z- + P_z+).
+template <typename T>
+inline T nbr_sum(const Dims& d, const T* P, int x, int y, int z) {
+    const T sx = P[d.c(x - 1, y, z)] + P[d.c(x + 1, y, z)];
+    const T sy = P[d.c(x, y - 1, z)] + P[d.c(x, y + 1, z)];
+    const T sz = P[d.c(x, y, z - 1)] + P[d.c(x, y, z + 1)];
+    return (sx + sy) + sz;
+}
+
 // max |r| as the GPU reduces it: the largest IEEE bit pattern of |r| (so NaN wins).
 template <typename T>
 inline void max_abs_bits(T val, T& m) {
@@ -277,8 +287,7 @@ T residual_max(const Dims& d, const T* P, const T* b, const uint8_t* s) {
             for (int x = 1; x < d.nx - 1; ++x) {
                 if (!projectable(d, s, x, y, z)) continue;
                 int acc = fluid_nbrs(d, s, x, y, z);
-                T sum = P[d.c(x - 1, y, z)] + P[d.c(x + 1, y, z)] + P[d.c(x, y - 1, z)] +
-                        P[d.c(x, y + 1, z)] + P[d.c(x, y, z - 1)] + P[d.c(x, y, z + 1)];
+                T sum = nbr_sum(d, P, x, y, z);
                 T r = fma_t<T>(-(T)acc, P[d.c(x, y, z)], b[d.c(x, y, z)] + sum);
                 max_abs_bits(r, m);
             }
@@ -288,7 +297,7 @@ T residual_max(const Dims& d, const T* P, const T* b, const uint8_t* s) {
 // Pressure-form red-black SOR.  rhs b = -div(u*) on projectable cells (fluid, interior, at
 // least one fluid neighbour -- exactly the cells the reference updates), 0 elsewhere; P stays 0
 // on every other cell, so neighbour sums need no mask.  One sweep = colour 0 then colour 1.
-//   r      = fma(-acc, P_c, b_c + sum_nbr P)
+//   r      = fma(-acc, P_c, b_c + nbr_sum)
 //   P_c   <- fma(omega/acc, r, P_c)           (omega/acc rounded to T once per acc value)
 // Tolerance rule (tol > 0): at every check point j = k*check_every the residual max of the
 // current state is computed; the sweeps of that group run regardless, and if the residual was
@@ -340,8 +349,7 @@ int project_pressure(const Dims& d, T* u, T* v, T* w, T* P, T* b, const uint8_t*
                             if (!projectable(d, s, x, y, z)) continue;
                             int acc = fluid_nbrs(d, s, x, y, z);
                             long long c = d.c(x, y, z);
-                            T sum = P[d.c(x - 1, y, z)] + P[d.c(x + 1, y, z)] + P[d.c(x, y - 1, z)] +
-                                    P[d.c(x, y + 1, z)] + P[d.c(x, y, z - 1)] + P[d.c(x, y, z + 1)];
+                            T sum = nbr_sum(d, P, x, y, z);
                             T r = fma_t<T>(-(T)acc, P[c], b[c] + sum);
                             P[c] = fma_t<T>(wacc[acc], r, P[c]);
                         }

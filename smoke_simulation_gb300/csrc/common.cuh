@@ -2,7 +2,8 @@
 //
 // HBM layout.  Every field of one simulation -- density (cells), u, v, w (faces), pressure and
 // right-hand side (cells), the solid mask and the neighbour-flag byte (cells) -- uses ONE
-// index function  i = x + X*y + XY*z  with X = round_up(nx+1, 8) (32-byte rows) and
+// index function  i = x + X*y + XY*z  with X = round_up(nx+1, 16) (64-byte float rows and
+// 16-byte flag rows, as TMA tensor maps require) and
 // XY = X*(ny+1).  Faces use x <= nx, y <= ny, z <= nz; cells use x < nx, y < ny, z < nz and
 // leave the last row/plane unused.  One index therefore addresses a cell and its three
 // "lower" faces (u at x, v at y, w at z), exactly like the reference's shared staggered index
@@ -41,7 +42,7 @@ struct StepStatus {
     unsigned div_bits;   // max |div u| after projection, as float bits (non-negative)
     int done;            // tolerance reached: later sweep groups are skipped
     int done_group;      // check group that set `done`
-    int pad;
+    int error;           // a bounded device wait gave up (the kernel returned early)
     unsigned rmax_bits[1];  // max |residual| per check group (flexible; sized at allocation)
 };
 

@@ -37,11 +37,15 @@ void launch_gradient_subtract(const Grid& g, float* u, float* v, float* w, const
                               cudaStream_t st);
 // Temporally blocked sweeps: nhalf <= T colour passes in one pass over HBM, P_in -> P_out;
 // `check` launches also record the residual of the input state for tolerance group `group`.
+// The pressure buffers are read through TMA tensor maps built once per simulation.
 int sweep_tb_depth_supported(int T);
-void launch_sweep_tb(const Grid& g, const float* Pin, float* Pout, const float* b,
-                     const uint8_t* flags, int T, int nhalf, int colour0, int zchunk,
-                     const float* wacc7, StepStatus* status, int check, int group, float tol,
-                     int* pcur, int out_idx, cudaStream_t st);
+struct SweepMaps;
+SweepMaps* create_sweep_maps(const Grid& g, const float* Pa, const float* Pb, const float* b,
+                             const uint8_t* flags);
+void destroy_sweep_maps(SweepMaps* m);
+int launch_sweep_tb(const SweepMaps* m, const Grid& g, bool in_is_a, float* Pout, int T, int nhalf,
+                    int colour0, int zchunk, const float* wacc7, StepStatus* status, int check,
+                    int group, float tol, int* pcur, int out_idx, int* kerr, cudaStream_t st);
 void launch_div_max(const Grid& g, const float* u, const float* v, const float* w,
                     const uint8_t* flags, StepStatus* status, cudaStream_t st);
 

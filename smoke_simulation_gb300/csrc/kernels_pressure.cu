@@ -48,7 +48,8 @@ __global__ void k_rhs(Grid g, const float* __restrict__ u, const float* __restri
     }
 }
 
-// One colour pass:  r = fma(-acc, P_c, b_c + sum P_nbr);  P_c = fma(omega/acc, r, P_c).
+// One colour pass:  r = fma(-acc, P_c, b_c + (((P_x-+P_x+)+(P_y-+P_y+))+(P_z-+P_z+)));
+// P_c = fma(omega/acc, r, P_c).
 __global__ void k_sweep(Grid g, float* __restrict__ P, const float* __restrict__ b,
                         const uint8_t* __restrict__ flags, int colour, WAcc wa,
                         const StepStatus* __restrict__ status) {
@@ -61,7 +62,7 @@ __global__ void k_sweep(Grid g, float* __restrict__ P, const float* __restrict__
     uint8_t f = flags[i];
     if (!(f & F_PROJ)) return;
     int acc = __popc((unsigned)(f & F_NBRS));
-    float sum = P[i - 1] + P[i + 1] + P[i - g.X] + P[i + g.X] + P[i - g.XY] + P[i + g.XY];
+    float sum = ((P[i - 1] + P[i + 1]) + (P[i - g.X] + P[i + g.X])) + (P[i - g.XY] + P[i + g.XY]);
     float pc = P[i];
     float r = fmaf(-(float)acc, pc, b[i] + sum);
     P[i] = fmaf(wa.w[acc], r, pc);
@@ -91,7 +92,7 @@ __global__ void k_resid_check(Grid g, const float* __restrict__ P, const float* 
         uint8_t f = flags[i];
         if (f & F_PROJ) {
             int acc = __popc((unsigned)(f & F_NBRS));
-            float sum = P[i - 1] + P[i + 1] + P[i - g.X] + P[i + g.X] + P[i - g.XY] + P[i + g.XY];
+            float sum = ((P[i - 1] + P[i + 1]) + (P[i - g.X] + P[i + g.X])) + (P[i - g.XY] + P[i + g.XY]);
             float r = fmaf(-(float)acc, P[i], b[i] + sum);
             m = fabsf(r);
         }

@@ -2,27 +2,42 @@
 //
 // One launch applies `nhalf` <= T half-sweeps (colour passes) to P in a single pass over HBM:
 // read P_in, b and the flag byte once, write P_out once -- 13 bytes per cell for T/2 sweeps,
-// where one colour pass per launch would move ~9-11 bytes per pass.
+// where one colour pass per launch moves ~9-11 bytes per pass.
 //
-// Decomposition.  A CTA owns an x-y tile of 64 x 32 columns (T-cell halo on each side, so the
-// interior is (64-2T) x (32-2T)) and a z-range [za, zb) of output planes.  It marches z as a
-// wavefront: at iteration q it loads plane q, computes the residual of plane q-1 (time 0, for
-// the tolerance check) and brings plane q-1-t from time t-1 to time t for t = 1..T, so plane
-// q-1-T leaves the pipeline finished.  Colour-t cells of a plane read only opposite-colour
-// neighbours, whose values at time t-1 are what the neighbouring planes hold at that moment,
-// so one copy of each plane suffices.  Halo cells are recomputed redundantly; cells within
-// T - t of the interior are exact after half-sweep t, which is all the interior needs.
+// Decomposition.  A CTA of 32 x TY threads owns an x-y tile of 64 x 2TY cells (a T-cell halo
+// on each side; the interior is (64-2T) x (2TY-2T)) and a z-range [za, zb) of output planes.
+// It marches z as a wavefront: at iteration q it takes plane q, computes the residual of plane
+// q-1 at time 0 (tolerance-check launches) and brings plane q-1-t from time t-1 to time t for
+// t = 1..T, so plane q-1-T leaves the pipeline finished.  A colour-t cell reads only
+// opposite-colour neighbours, whose time t-1 values are exactly what the neighbouring planes
+// hold at that moment, so one copy of each plane suffices.  Halo cells are recomputed
+// redundantly; cells within T - t of the interior are exact after half-sweep t.
 //
-// Storage per thread (2 x-adjacent columns): the z-ring of P, b and flags in registers.
-// Neighbours: z from registers, x from the thread's own pair or a warp shuffle (a tile row is
-// one warp), y from a shared-memory copy of the plane published once per iteration
-// (double-buffered, one barrier per iteration).
+// Loads.  Planes arrive through TMA: thread 0 issues cp.async.bulk.tensor copies of the
+// tile's P, b and flag boxes for plane q+S into an S-stage shared-memory ring (S = (T+4)/2,
+// half the register ring, so stage and phase are fixed per unrolled iteration) while plane q is
+// being computed; an mbarrier per stage counts the bytes.  Boxes outside the grid (halo, first
+// and last planes) are zero-filled by the TMA unit, which is what the solver needs there (P = 0,
+// not projectable).  Waits are bounded: on timeout the kernel records an error, waits (bounded)
+// for its own copies still in flight and returns.
 //
-// Every update is  r = fma(-acc, P_c, b_c + (((((P_x- + P_x+) + P_y-) + P_y+) + P_z-) + P_z+));
-// P_c = fma(omega/acc, r, P_c), the oracle's order, so results equal the one-pass-per-colour
-// kernel bit for bit.
+// Per thread: a 2 x 2 patch (x0, x0+1) x (y0, y0+1) with x0, y0 even, so a cell's colour is
+// the parity of z alone and the two cells updated per stage are (A, row 0) + (B, row 1) or
+// (B, row 0) + (A, row 1), uniformly over the CTA.  The z-rings of P, b and flags live in
+// registers; the loop over z is unrolled by the ring length so every slot is a fixed register.
+// x-neighbours come from the patch or a warp shuffle (a tile row of 32 threads is one warp),
+// y-neighbours from the patch or a shared-memory copy of each in-flight plane, published once
+// per iteration (double-buffered: one barrier per iteration).
+//
+// Every update is  r = fma(-acc, P_c, b_c + (((P_x- + P_x+) + (P_y- + P_y+)) + (P_z- + P_z+)));
+// P_c = fma(omega/acc, r, P_c), the oracle's order, so every launch shape gives the same bits
+// as one colour pass per launch.  (-acc, omega/acc) come from a 128-entry table indexed by the
+// flag byte (six neighbour bits + "projectable").
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
+
+#include <cstring>
 
 #include "common.cuh"
 #include "kernels.h"
@@ -31,22 +46,113 @@ namespace smk {
 
 namespace {
 
-constexpr int TB_TX = 32;            // threads per tile row (one warp)
-constexpr int TB_TY = 32;            // tile rows
-constexpr int TB_CX = 2 * TB_TX;     // columns per tile row (2 per thread)
+constexpr int TB_TX = 32;      // threads per tile row (one warp) = 64 cells
+constexpr int TB_TY = 16;      // tile rows of threads = 32 cell rows
+constexpr int BOX_F = 68;      // float box width: 64 cells + up to 2 alignment cells, 16-B multiple
+constexpr int BOX_U8 = 80;     // flag box width in bytes: 64 + up to 15 alignment bytes
+constexpr int ROWS = 2 * TB_TY;
+constexpr int STAGE_P = ROWS * BOX_F * 4;     // bytes
+constexpr int STAGE_F = ROWS * BOX_U8;        // bytes
+constexpr int STAGE_BYTES = 2 * STAGE_P + STAGE_F;
+constexpr unsigned WAIT_LIMIT = 1u << 20;
 
 struct WAcc8 { float w[8]; };
 
-__device__ __forceinline__ float2 ld2(const float* p) { return __ldg(reinterpret_cast<const float2*>(p)); }
+struct TBMaps {
+    CUtensorMap pin;  // P_in
+    CUtensorMap b;
+    CUtensorMap f;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait on an mbarrier phase.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+    for (unsigned i = 0; i < WAIT_LIMIT; ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, int x, int y, int z,
+                                            uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(dst),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(bar)
+        : "memory");
+}
+
+// Issue the three boxes of plane z into stage `st` (thread 0 only).
+__device__ __forceinline__ void issue_plane(const TBMaps& m, unsigned char* stage, uint32_t bar,
+                                            int xf, int xb, int y, int z) {
+    mbar_expect_tx(bar, (uint32_t)STAGE_BYTES);
+    tma_load_3d(smem_u32(stage), &m.pin, xf, y, z, bar);
+    tma_load_3d(smem_u32(stage + STAGE_P), &m.b, xf, y, z, bar);
+    tma_load_3d(smem_u32(stage + 2 * STAGE_P), &m.f, xb, y, z, bar);
+}
+
+// One cell update in the oracle's operation order; `c` = {-acc, omega/acc} from the flag
+// table, `proj` = the cell is projectable (else it keeps its value, 0).
+__device__ __forceinline__ float relax(float pc, float bc, float2 c, bool proj, float xm, float xp,
+                                       float ym, float yp, float zm, float zp) {
+    const float sum = ((xm + xp) + (ym + yp)) + (zm + zp);
+    const float r = fmaf(c.x, pc, bc + sum);
+    const float pn = fmaf(c.y, r, pc);
+    return proj ? pn : pc;
+}
+
+__device__ __forceinline__ unsigned resid_bits(float pc, float bc, float2 c, bool proj, float xm,
+                                               float xp, float ym, float yp, float zm, float zp) {
+    const float sum = ((xm + xp) + (ym + yp)) + (zm + zp);
+    const float r = fmaf(c.x, pc, bc + sum);
+    return proj ? __float_as_uint(fabsf(r)) : 0u;
+}
+
+// flag byte of cell k (0..3 = A0, B0, A1, B1) of a packed patch word -> table index:
+// bits 0-5 the six fluid-neighbour bits, bit 6 "projectable"
+__device__ __forceinline__ unsigned fidx(unsigned f, int k) { return (f >> (8 * k + 1)) & 0x7fu; }
 
 template <int T>
 __global__ void __launch_bounds__(TB_TX * TB_TY, 1)
-k_sweep_tb(Grid g, const float* __restrict__ Pin, float* __restrict__ Pout,
-           const float* __restrict__ B, const uint8_t* __restrict__ F, int nhalf, int colour0,
-           int zchunk, WAcc8 wa, StepStatus* status, int check, int group, float tol,
-           int* __restrict__ pcur, int out_idx) {
-    extern __shared__ float2 smem_tb[];
-    __shared__ float wacc[8];
+k_sweep_tb(const __grid_constant__ TBMaps maps, Grid g, float* __restrict__ Pout, int nhalf,
+           int colour0, int zchunk, WAcc8 wa, StepStatus* status, int check, int group, float tol,
+           int* __restrict__ pcur, int out_idx, int* __restrict__ kerr) {
+    constexpr int R = T + 4;                 // register ring length (even, >= T + 3)
+    constexpr int TB_S = R / 2;              // TMA stages (planes in flight)
+    constexpr int IX = 2 * TB_TX - 2 * T;    // interior columns
+    constexpr int IY = ROWS - 2 * T;         // interior rows
+    constexpr int PROW = (TB_TY + 2) * TB_TX;  // float2 per published row set (zero row above/below)
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    // TMA destinations must be 128-byte aligned: align the dynamic base explicitly (the launch
+    // requests 128 spare bytes)
+    unsigned char* stages = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);  // [S][STAGE_BYTES]
+    // published planes: [2 buffers][T+1 planes][2 rows][TY+2][32] pairs (A, B)
+    float2* pub = reinterpret_cast<float2*>(stages + TB_S * STAGE_BYTES);
+    __shared__ __align__(8) uint64_t mbar[TB_S];
+    __shared__ float2 coef[128];
 
     if (status != nullptr) {
         if (*(volatile int*)&status->done) return;
@@ -60,172 +166,287 @@ k_sweep_tb(Grid g, const float* __restrict__ Pin, float* __restrict__ Pout,
         }
     }
     const int tx = threadIdx.x, ty = threadIdx.y;
-    if (ty == 0 && tx < 8) wacc[tx] = wa.w[tx];
-    if (pcur != nullptr && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && tx == 0 && ty == 0)
+    const int tid = ty * TB_TX + tx;
+    const bool leader = tid == 0;
+    if (tid < 128) {
+        const int acc = __popc(tid & 0x3f);
+        coef[tid] = make_float2(-(float)acc, (tid & 0x40) ? wa.w[acc] : 0.0f);
+    }
+    // zero the padding rows of every published plane (never written afterwards)
+    for (int i = tid; i < 2 * (T + 1) * 2 * 2 * TB_TX; i += TB_TX * TB_TY) {
+        const int lane = i % TB_TX, edge = (i / TB_TX) % 2, set = i / (2 * TB_TX);
+        pub[set * PROW + (edge ? (TB_TY + 1) * TB_TX : 0) + lane] = make_float2(0.f, 0.f);
+    }
+    if (pcur != nullptr && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && leader)
         *pcur = out_idx;
 
-    constexpr int IX = TB_CX - 2 * T, IY = TB_TY - 2 * T;
-    const int xA = (int)blockIdx.x * IX - T + 2 * tx;  // even
-    const int y = (int)blockIdx.y * IY - T + ty;
+    const int X0 = (int)blockIdx.x * IX - T;  // even; first tile column
+    const int Y0 = (int)blockIdx.y * IY - T;  // even; first tile row
+    const int xf = X0 - (X0 & 3);             // 16-byte aligned float box start
+    const int xb = X0 - (X0 & 15);            // 16-byte aligned flag box start
+    const int of = X0 - xf + 2 * tx;          // this thread's column in the float box
+    const int ob = X0 - xb + 2 * tx;          // ... in the flag box
+    const int x0 = X0 + 2 * tx;
+    const int y0 = Y0 + 2 * ty;
     const int za = (int)blockIdx.z * zchunk;
     const int zb = min(za + zchunk, g.nz);
-    const bool colok = xA >= 0 && xA < g.X && y >= 0 && y <= g.ny;
-    const bool interior = (2 * tx >= T) && (2 * tx < T + IX) && (ty >= T) && (ty < T + IY) &&
-                          xA < g.nx && y < g.ny && y >= 0 && xA >= 0;
-    const int rowoff = xA + g.X * y;
+    const bool inx = (2 * tx >= T) && (2 * tx < T + IX) && x0 < g.nx;
+    const bool in0 = inx && (2 * ty >= T) && (2 * ty < T + IY) && y0 >= 0 && y0 < g.ny;
+    const bool in1 = in0 && y0 + 1 < g.ny;
+    const int off0 = x0 + g.X * y0;
+    const int off1 = off0 + g.X;
 
-    // z-rings: index j holds plane q - j
-    float2 p[T + 3];
-    float2 bb[T + 2];
-    unsigned ff[T + 2];
+    const int qbeg = za - T;
+    const int qend = zb + T;
+    const int nouter = (qend - qbeg + R) / R;
+    const int qfinal = qbeg + nouter * R - 1;  // last iteration executed
+
+    if (leader) {
+        for (int s = 0; s < TB_S; ++s) mbar_init(smem_u32(&mbar[s]), 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        for (int s = 0; s < TB_S; ++s)
+            issue_plane(maps, stages + s * STAGE_BYTES, smem_u32(&mbar[s]), xf, xb, Y0, qbeg + s);
+    }
+
+    float2 p0[R], p1[R], b0[R], b1[R];  // P and b, rows 0 and 1, slot = plane mod R
+    unsigned ff[R];                     // flags: bytes A0, B0, A1, B1
 #pragma unroll
-    for (int j = 0; j < T + 3; ++j) p[j] = make_float2(0.f, 0.f);
-#pragma unroll
-    for (int j = 0; j < T + 2; ++j) { bb[j] = make_float2(0.f, 0.f); ff[j] = 0u; }
+    for (int j = 0; j < R; ++j) {
+        p0[j] = p1[j] = b0[j] = b1[j] = make_float2(0.f, 0.f);
+        ff[j] = 0u;
+    }
 
     unsigned rmax = 0u;
-    int par = 0;
-    const int qbeg = za - T;
-    const int qlast_load = min(zb - 1 + T, g.nz);
-    const int qend = zb + T;
+    const int p_par = (qbeg + colour0) & 1;  // stage colour parity of the first iteration
+    int par = 0;                             // publish-buffer parity
+    const int me0 = (ty + 1) * TB_TX + tx;   // my slot in a padded published row set
+    __syncthreads();                         // barriers, table and padding visible
 
-    // prefetch registers for the next plane
-    float2 np_ = make_float2(0.f, 0.f), nb_ = make_float2(0.f, 0.f);
-    unsigned nf_ = 0u;
-    if (colok && qbeg >= 0 && qbeg <= qlast_load) {
-        const int i = rowoff + g.XY * qbeg;
-        np_ = ld2(Pin + i);
-        nb_ = ld2(B + i);
-        nf_ = __ldg(reinterpret_cast<const unsigned short*>(F + i));
-    }
-    __syncthreads();  // wacc visible
-
-    for (int q = qbeg; q <= qend; ++q) {
+    for (int base = qbeg; base <= qend; base += R) {
 #pragma unroll
-        for (int j = T + 2; j > 0; --j) p[j] = p[j - 1];
+        for (int k = 0; k < R; ++k) {
+            const int q = base + k;
+            const int st = k % TB_S;
+            const uint32_t phase = (uint32_t)((k / TB_S) & 1);
+            // ---- plane q: wait for its TMA stage, take this thread's patch into slot k
+            const bool ok = mbar_wait(smem_u32(&mbar[st]), phase);
+            {
+                const unsigned char* S_ = stages + st * STAGE_BYTES;
+                const float* sp = reinterpret_cast<const float*>(S_);
+                const float* sb = reinterpret_cast<const float*>(S_ + STAGE_P);
+                const unsigned char* sf = S_ + 2 * STAGE_P;
+                const int r0 = (2 * ty) * BOX_F + of, r1 = r0 + BOX_F;
+                p0[k] = *reinterpret_cast<const float2*>(sp + r0);
+                p1[k] = *reinterpret_cast<const float2*>(sp + r1);
+                b0[k] = *reinterpret_cast<const float2*>(sb + r0);
+                b1[k] = *reinterpret_cast<const float2*>(sb + r1);
+                const unsigned f0 = *reinterpret_cast<const unsigned short*>(sf + (2 * ty) * BOX_U8 + ob);
+                const unsigned f1 = *reinterpret_cast<const unsigned short*>(sf + (2 * ty + 1) * BOX_U8 + ob);
+                ff[k] = f0 | (f1 << 16);
+            }
+            // ---- publish planes q-1-s (slot (k-1-s) mod R) for the y-neighbours; the residual
+            // plane (s = 0) only in check launches
+            float2* pb = pub + par * (T + 1) * 2 * PROW;
 #pragma unroll
-        for (int j = T + 1; j > 0; --j) { bb[j] = bb[j - 1]; ff[j] = ff[j - 1]; }
-        p[0] = np_;
-        bb[0] = nb_;
-        ff[0] = nf_;
-        // issue the next plane's loads now; they complete while this plane computes
-        np_ = make_float2(0.f, 0.f);
-        nb_ = make_float2(0.f, 0.f);
-        nf_ = 0u;
-        const int qn = q + 1;
-        if (colok && qn >= 0 && qn <= qlast_load) {
-            const int i = rowoff + g.XY * qn;
-            np_ = ld2(Pin + i);
-            nb_ = ld2(B + i);
-            nf_ = __ldg(reinterpret_cast<const unsigned short*>(F + i));
-        }
-
-        // publish planes q-1-s (s = 0..T) at their current time for the y-neighbours
-        float2* buf = smem_tb + par * (T + 1) * TB_TY * TB_TX;
-#pragma unroll
-        for (int s = 0; s <= T; ++s) buf[(s * TB_TY + ty) * TB_TX + tx] = p[1 + s];
-        __syncthreads();
-
-        // stage 0: residual of plane q-1 at time 0 (tolerance check launches only)
-        if (check) {
-            const int zp = q - 1;
-            const float2 cur = p[1];
-            const float left = __shfl_up_sync(0xffffffffu, cur.y, 1);
-            const float right = __shfl_down_sync(0xffffffffu, cur.x, 1);
-            if (interior && zp >= za && zp < zb) {
-                const float2 ym = buf[(0 * TB_TY + ty - 1) * TB_TX + tx];
-                const float2 yp = buf[(0 * TB_TY + ty + 1) * TB_TX + tx];
-                const float2 up = p[0], dn = p[2];
-                const unsigned f2 = ff[1];
-                const unsigned fa = f2 & 0xffu, fb = (f2 >> 8) & 0xffu;
-                if (fa & F_PROJ) {
-                    const int acc = __popc(fa & F_NBRS);
-                    const float sum = left + cur.y + ym.x + yp.x + dn.x + up.x;
-                    const float r = fmaf(-(float)acc, cur.x, bb[1].x + sum);
-                    rmax = max(rmax, __float_as_uint(fabsf(r)));
-                }
-                if (fb & F_PROJ) {
-                    const int acc = __popc(fb & F_NBRS);
-                    const float sum = cur.x + right + ym.y + yp.y + dn.y + up.y;
-                    const float r = fmaf(-(float)acc, cur.y, bb[1].y + sum);
-                    rmax = max(rmax, __float_as_uint(fabsf(r)));
+            for (int s = 0; s <= T; ++s) {
+                if (s > 0 || check) {
+                    const int j = (k - 1 - s + 2 * R) % R;
+                    pb[(2 * s) * PROW + me0] = p0[j];
+                    pb[(2 * s + 1) * PROW + me0] = p1[j];
                 }
             }
-        }
+            if (__syncthreads_or(!ok)) {
+                // a TMA stage never completed: record it, drain what is in flight, stop
+                if (leader) {
+                    atomicExch(kerr, 1);
+                    const int last = min(q + TB_S - 1, qfinal);
+                    for (int pq = q; pq <= last; ++pq) {
+                        const int d = pq - qbeg;
+                        mbar_wait(smem_u32(&mbar[d % TB_S]), (uint32_t)((d / TB_S) & 1));
+                    }
+                }
+                __syncthreads();
+                return;
+            }
+            // every thread has read stage st: refill it with plane q + S
+            if (leader && q + TB_S <= qfinal)
+                issue_plane(maps, stages + st * STAGE_BYTES, smem_u32(&mbar[st]), xf, xb, Y0, q + TB_S);
 
-        // stages 1..T: plane q-1-t from time t-1 to t (colour c_t cells)
-#pragma unroll
-        for (int t = 1; t <= T; ++t) {
-            if (t <= nhalf) {
-                const int zp = q - 1 - t;
-                const int ct = colour0 ^ ((t - 1) & 1);
-                const bool updA = ((y + zp) & 1) == ct;  // cell A (even x) has colour (y+zp)&1
-                const float2 cur = p[1 + t];
-                const float left = __shfl_up_sync(0xffffffffu, cur.y, 1);
-                const float right = __shfl_down_sync(0xffffffffu, cur.x, 1);
-                const float2 ym = ty > 0 ? buf[(t * TB_TY + ty - 1) * TB_TX + tx] : make_float2(0.f, 0.f);
-                const float2 yp = ty < TB_TY - 1 ? buf[(t * TB_TY + ty + 1) * TB_TX + tx]
-                                                 : make_float2(0.f, 0.f);
-                const float2 up = p[t], dn = p[2 + t];
-                const unsigned f = updA ? (ff[1 + t] & 0xffu) : ((ff[1 + t] >> 8) & 0xffu);
-                if (f & F_PROJ) {
-                    const int acc = __popc(f & F_NBRS);
-                    const float pc = updA ? cur.x : cur.y;
-                    const float xm = updA ? left : cur.x;
-                    const float xp = updA ? cur.y : right;
-                    const float sum = xm + xp + (updA ? ym.x : ym.y) + (updA ? yp.x : yp.y) +
-                                      (updA ? dn.x : dn.y) + (updA ? up.x : up.y);
-                    const float bc = updA ? bb[1 + t].x : bb[1 + t].y;
-                    const float r = fmaf(-(float)acc, pc, bc + sum);
-                    const float pn = fmaf(wacc[acc], r, pc);
-                    if (updA) p[1 + t].x = pn; else p[1 + t].y = pn;
+            // ---- stage 0: residual of plane q-1 at time 0
+            if (check) {
+                const int j = (k - 1 + R) % R, ju = k, jd = (k - 2 + R) % R;
+                const float lB0 = __shfl_up_sync(0xffffffffu, p0[j].y, 1);
+                const float lB1 = __shfl_up_sync(0xffffffffu, p1[j].y, 1);
+                const float rA0 = __shfl_down_sync(0xffffffffu, p0[j].x, 1);
+                const float rA1 = __shfl_down_sync(0xffffffffu, p1[j].x, 1);
+                const int zp = q - 1;
+                if (zp >= za && zp < zb && in0) {
+                    const float2 up = pb[PROW + me0 - TB_TX];  // row y0-1 (thread above, row 1)
+                    const float2 dn = pb[me0 + TB_TX];         // row y0+2 (thread below, row 0)
+                    const unsigned f = ff[j];
+                    const unsigned i0 = fidx(f, 0), i1 = fidx(f, 1), i2 = fidx(f, 2), i3 = fidx(f, 3);
+                    rmax = max(rmax, resid_bits(p0[j].x, b0[j].x, coef[i0], i0 & 0x40u, lB0, p0[j].y,
+                                                up.x, p1[j].x, p0[jd].x, p0[ju].x));
+                    rmax = max(rmax, resid_bits(p0[j].y, b0[j].y, coef[i1], i1 & 0x40u, p0[j].x, rA0,
+                                                up.y, p1[j].y, p0[jd].y, p0[ju].y));
+                    if (in1) {
+                        rmax = max(rmax, resid_bits(p1[j].x, b1[j].x, coef[i2], i2 & 0x40u, lB1, p1[j].y,
+                                                    p0[j].x, dn.x, p1[jd].x, p1[ju].x));
+                        rmax = max(rmax, resid_bits(p1[j].y, b1[j].y, coef[i3], i3 & 0x40u, p1[j].x, rA1,
+                                                    p0[j].y, dn.y, p1[jd].y, p1[ju].y));
+                    }
                 }
             }
-        }
 
-        // plane q-1-T is finished
-        const int zo = q - 1 - T;
-        if (interior && zo >= za && zo < zb)
-            *reinterpret_cast<float2*>(Pout + rowoff + g.XY * zo) = p[1 + T];
-        par ^= 1;
+            // ---- stages 1..T: plane q-1-t (slot k-1-t) from time t-1 to t
+            const bool sA = ((k + p_par) & 1) == 0;  // update (A0, B1), else (B0, A1)
+#pragma unroll
+            for (int t = 1; t <= T; ++t) {
+                if (t <= nhalf) {
+                    const int j = (k - 1 - t + 2 * R) % R;
+                    const int ju = (k - t + 2 * R) % R;
+                    const int jd = (k - 2 - t + 2 * R) % R;
+                    const float2* ps = pb + (2 * t) * PROW;
+                    const unsigned f = ff[j];
+                    if (sA) {
+                        const float lB0 = __shfl_up_sync(0xffffffffu, p0[j].y, 1);
+                        const float rA1 = __shfl_down_sync(0xffffffffu, p1[j].x, 1);
+                        const float ymA = ps[PROW + me0 - TB_TX].x;  // row y0-1, column A
+                        const float ypB = ps[me0 + TB_TX].y;         // row y0+2, column B
+                        const unsigned ia = fidx(f, 0), ib = fidx(f, 3);
+                        const float nA0 = relax(p0[j].x, b0[j].x, coef[ia], ia & 0x40u, lB0, p0[j].y,
+                                                ymA, p1[j].x, p0[jd].x, p0[ju].x);
+                        const float nB1 = relax(p1[j].y, b1[j].y, coef[ib], ib & 0x40u, p1[j].x, rA1,
+                                                p0[j].y, ypB, p1[jd].y, p1[ju].y);
+                        p0[j].x = nA0;
+                        p1[j].y = nB1;
+                    } else {
+                        const float rA0 = __shfl_down_sync(0xffffffffu, p0[j].x, 1);
+                        const float lB1 = __shfl_up_sync(0xffffffffu, p1[j].y, 1);
+                        const float ymB = ps[PROW + me0 - TB_TX].y;  // row y0-1, column B
+                        const float ypA = ps[me0 + TB_TX].x;         // row y0+2, column A
+                        const unsigned ia = fidx(f, 1), ib = fidx(f, 2);
+                        const float nB0 = relax(p0[j].y, b0[j].y, coef[ia], ia & 0x40u, p0[j].x, rA0,
+                                                ymB, p1[j].y, p0[jd].y, p0[ju].y);
+                        const float nA1 = relax(p1[j].x, b1[j].x, coef[ib], ib & 0x40u, lB1, p1[j].y,
+                                                p0[j].x, ypA, p1[jd].x, p1[ju].x);
+                        p0[j].y = nB0;
+                        p1[j].x = nA1;
+                    }
+                }
+            }
+
+            // ---- plane q-1-T is finished (slot k-1-T)
+            const int zo = q - 1 - T;
+            if (zo >= za && zo < zb) {
+                const int j = (k - 1 - T + 2 * R) % R;
+                if (in0) *reinterpret_cast<float2*>(Pout + off0 + g.XY * zo) = p0[j];
+                if (in1) *reinterpret_cast<float2*>(Pout + off1 + g.XY * zo) = p1[j];
+            }
+            par ^= 1;
+        }
     }
 
     if (check) block_max_to(rmax, &status->rmax_bits[group]);
 }
 
+
+// ---- host side --------------------------------------------------------------------------------
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*,
+                                  CUtensorMapInterleave, CUtensorMapSwizzle, CUtensorMapL2promotion,
+                                  CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+    static EncodeTiledFn fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+    }
+    return fn;
+}
+
+bool encode_3d(CUtensorMap* m, const void* base, bool is_u8, const Grid& g) {
+    EncodeTiledFn fn = encode_fn();
+    if (!fn || base == nullptr || (reinterpret_cast<uintptr_t>(base) & 15u) != 0) return false;
+    const size_t es = is_u8 ? 1 : 4;
+    cuuint64_t dims[3] = {(cuuint64_t)g.X, (cuuint64_t)(g.ny + 1), (cuuint64_t)(g.nz + 1)};
+    cuuint64_t strides[2] = {(cuuint64_t)g.X * es, (cuuint64_t)g.XY * es};
+    cuuint32_t box[3] = {(cuuint32_t)(is_u8 ? BOX_U8 : BOX_F), (cuuint32_t)ROWS, 1u};
+    cuuint32_t estr[3] = {1u, 1u, 1u};
+    CUresult r = fn(m, is_u8 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
+                    const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                    CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+
 template <int T>
-void launch_tb(const Grid& g, const float* Pin, float* Pout, const float* b, const uint8_t* flags,
-               int nhalf, int colour0, int zchunk, const float* wacc7, StepStatus* status, int check,
-               int group, float tol, int* pcur, int out_idx, cudaStream_t st) {
+int launch_tb(const TBMaps& maps, const Grid& g, float* Pout, int nhalf, int colour0, int zchunk,
+              const float* wacc7, StepStatus* status, int check, int group, float tol, int* pcur,
+              int out_idx, int* kerr, cudaStream_t st) {
     static bool configured = false;
-    const size_t smem = sizeof(float2) * 2 * (T + 1) * TB_TY * TB_TX;
+    constexpr int TB_S = (T + 4) / 2;
+    const size_t smem =
+        128 + (size_t)TB_S * STAGE_BYTES + sizeof(float2) * 2 * (T + 1) * 2 * (TB_TY + 2) * TB_TX;
     if (!configured) {
-        cudaFuncSetAttribute(k_sweep_tb<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (cudaFuncSetAttribute(k_sweep_tb<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+            cudaSuccess)
+            return -1;
         configured = true;
     }
     WAcc8 wa;
     for (int k = 0; k < 7; ++k) wa.w[k] = wacc7[k];
     wa.w[7] = 0.0f;
-    constexpr int IX = TB_CX - 2 * T, IY = TB_TY - 2 * T;
+    constexpr int IX = 2 * TB_TX - 2 * T, IY = ROWS - 2 * T;
     dim3 grid((unsigned)((g.nx + IX - 1) / IX), (unsigned)((g.ny + IY - 1) / IY),
               (unsigned)((g.nz + zchunk - 1) / zchunk));
-    k_sweep_tb<T><<<grid, dim3(TB_TX, TB_TY), smem, st>>>(g, Pin, Pout, b, flags, nhalf, colour0, zchunk,
-                                                         wa, status, check, group, tol, pcur, out_idx);
+    k_sweep_tb<T><<<grid, dim3(TB_TX, TB_TY), smem, st>>>(maps, g, Pout, nhalf, colour0, zchunk, wa, status,
+                                                         check, group, tol, pcur, out_idx, kerr);
+    return 0;
 }
 
 }  // namespace
 
-int sweep_tb_depth_supported(int T) { return T == 2 || T == 4 || T == 6 || T == 8; }
+int sweep_tb_depth_supported(int T) { return T == 2 || T == 4 || T == 6; }
 
-void launch_sweep_tb(const Grid& g, const float* Pin, float* Pout, const float* b,
-                     const uint8_t* flags, int T, int nhalf, int colour0, int zchunk,
-                     const float* wacc7, StepStatus* status, int check, int group, float tol,
-                     int* pcur, int out_idx, cudaStream_t st) {
+// Tensor maps for the sweep's TMA loads: P_a, P_b, b (float) and flags (u8).
+struct SweepMaps {
+    CUtensorMap pa, pb, b, f;
+};
+
+SweepMaps* create_sweep_maps(const Grid& g, const float* Pa, const float* Pb, const float* b,
+                             const uint8_t* flags) {
+    SweepMaps* m = new SweepMaps();
+    if (!encode_3d(&m->pa, Pa, false, g) || !encode_3d(&m->pb, Pb, false, g) ||
+        !encode_3d(&m->b, b, false, g) || !encode_3d(&m->f, flags, true, g)) {
+        delete m;
+        return nullptr;
+    }
+    return m;
+}
+
+void destroy_sweep_maps(SweepMaps* m) { delete m; }
+
+int launch_sweep_tb(const SweepMaps* m, const Grid& g, bool in_is_a, float* Pout, int T, int nhalf,
+                    int colour0, int zchunk, const float* wacc7, StepStatus* status, int check,
+                    int group, float tol, int* pcur, int out_idx, int* kerr, cudaStream_t st) {
+    TBMaps maps;
+    maps.pin = in_is_a ? m->pa : m->pb;
+    maps.b = m->b;
+    maps.f = m->f;
     switch (T) {
-        case 2: launch_tb<2>(g, Pin, Pout, b, flags, nhalf, colour0, zchunk, wacc7, status, check, group, tol, pcur, out_idx, st); break;
-        case 4: launch_tb<4>(g, Pin, Pout, b, flags, nhalf, colour0, zchunk, wacc7, status, check, group, tol, pcur, out_idx, st); break;
-        case 6: launch_tb<6>(g, Pin, Pout, b, flags, nhalf, colour0, zchunk, wacc7, status, check, group, tol, pcur, out_idx, st); break;
-        default: launch_tb<8>(g, Pin, Pout, b, flags, nhalf, colour0, zchunk, wacc7, status, check, group, tol, pcur, out_idx, st); break;
+        case 2: return launch_tb<2>(maps, g, Pout, nhalf, colour0, zchunk, wacc7, status, check, group, tol, pcur, out_idx, kerr, st);
+        case 4: return launch_tb<4>(maps, g, Pout, nhalf, colour0, zchunk, wacc7, status, check, group, tol, pcur, out_idx, kerr, st);
+        default: return launch_tb<6>(maps, g, Pout, nhalf, colour0, zchunk, wacc7, status, check, group, tol, pcur, out_idx, kerr, st);
     }
 }
 

@@ -91,11 +91,15 @@ int smk_sim::alloc() {
         SMK_CUDA(cudaMalloc((void**)f, n * sizeof(float)));
         SMK_CUDA(cudaMemset(*f, 0, n * sizeof(float)));
     }
-    SMK_CUDA(cudaMalloc((void**)&pcur, sizeof(int)));
-    SMK_CUDA(cudaMemset(pcur, 0, sizeof(int)));
+    SMK_CUDA(cudaMalloc((void**)&pcur, 2 * sizeof(int)));
+    SMK_CUDA(cudaMemset(pcur, 0, 2 * sizeof(int)));
+    kerr = pcur + 1;
     SMK_CUDA(cudaMalloc((void**)&s, n));
     SMK_CUDA(cudaMalloc((void**)&flags, n));
     SMK_CUDA(cudaMemset(flags, 0, n));
+    // the tensor maps capture the buffer addresses: every buffer must exist first
+    maps = create_sweep_maps(g, P, P2, b, flags);
+    if (!maps) return fail(SMK_ERR_CUDA, "could not encode the TMA tensor maps of the sweep kernel");
     status_groups = 4096;
     SMK_CUDA(cudaMalloc((void**)&status, sizeof(StepStatus) + sizeof(unsigned) * status_groups));
     SMK_CUDA(cudaMemset(status, 0, sizeof(StepStatus) + sizeof(unsigned) * status_groups));
@@ -112,6 +116,7 @@ void smk_sim::release() {
     for (float* f : fl)
         if (f) cudaFree(f);
     if (pcur) cudaFree(pcur);
+    if (maps) destroy_sweep_maps(maps);
     if (s) cudaFree(s);
     if (flags) cudaFree(flags);
     if (status) cudaFree(status);
@@ -201,9 +206,11 @@ int smk_sim::step(float dt, cudaStream_t st) {
                 for (int h = 2 * sweep; h < h1; h += sweep_depth) {
                     const int nh = h1 - h < sweep_depth ? h1 - h : sweep_depth;
                     const bool in_a = (nl & 1) == 0;
-                    launch_sweep_tb(g, in_a ? P : P2, in_a ? P2 : P, b, flags, sweep_depth, nh, h & 1,
-                                    sweep_zchunk, wacc, use_tol ? status : nullptr,
-                                    use_tol && h == 2 * sweep, group, p.tol, pcur, in_a ? 1 : 0, st);
+                    if (launch_sweep_tb(maps, g, in_a, in_a ? P2 : P, sweep_depth, nh, h & 1,
+                                        sweep_zchunk, wacc, use_tol ? status : nullptr,
+                                        use_tol && h == 2 * sweep, group, p.tol, pcur, in_a ? 1 : 0,
+                                        kerr, st) != 0)
+                        return fail(SMK_ERR_CUDA, "sweep kernel configuration failed");
                     ++nl;
                     ++launches;
                 }
@@ -295,7 +302,7 @@ int smk_create(int nx, int ny, int nz, const smk_params* params, smk_sim** out) 
     if (params) p = *params; else smk_default_params(&p);
     int rc = check_params(&p);
     if (rc) return rc;
-    long long X = ((long long)nx + 1 + 7) / 8 * 8;
+    long long X = ((long long)nx + 1 + 15) / 16 * 16;  // 16-element rows: TMA strides
     long long total = X * (ny + 1) * (long long)(nz + 1);
     if (total >= (1LL << 31)) return fail(SMK_ERR_INVALID, "grid too large for 32-bit indexing");
     smk_sim* sim = new smk_sim();
@@ -436,11 +443,23 @@ int smk_read_density(smk_sim* sim, float* dst, int dst_on_device, void* stream) 
     return SMK_OK;
 }
 
+// After a synchronisation: report (and clear) a bounded device wait that gave up.
+static int check_kernel_error(smk_sim* sim) {
+    int e = 0;
+    SMK_CUDA(cudaMemcpy(&e, sim->kerr, sizeof(int), cudaMemcpyDeviceToHost));
+    if (e) {
+        SMK_CUDA(cudaMemset(sim->kerr, 0, sizeof(int)));
+        return fail(SMK_ERR_TIMEOUT, "a sweep kernel's bounded wait for its TMA loads gave up; "
+                                     "the step's projection is incomplete");
+    }
+    return SMK_OK;
+}
+
 int smk_sync(smk_sim* sim, void* stream) {
     if (!sim) return fail(SMK_ERR_INVALID, "sim is null");
     DeviceGuard dg(sim->device);
     SMK_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
-    return SMK_OK;
+    return check_kernel_error(sim);
 }
 
 int smk_simulate(smk_sim* sim, float* host_out, float dt) {
@@ -451,7 +470,7 @@ int smk_simulate(smk_sim* sim, float* host_out, float dt) {
     rc = smk_read_density(sim, host_out, 0, nullptr);
     if (rc) return rc;
     SMK_CUDA(cudaStreamSynchronize((cudaStream_t)0));
-    return SMK_OK;
+    return check_kernel_error(sim);
 }
 
 static int state_copy(smk_sim* sim, const smk_host_state* st, bool to_device) {
@@ -520,6 +539,8 @@ int smk_get_stats(smk_sim* sim, smk_stats* out) {
     if (sim->steps == 0) return SMK_OK;
     std::vector<unsigned> host(4 + sim->status_groups);
     SMK_CUDA(cudaDeviceSynchronize());
+    int krc = check_kernel_error(sim);
+    if (krc) return krc;
     SMK_CUDA(cudaMemcpy(host.data(), sim->status, sizeof(StepStatus) + sizeof(unsigned) * sim->status_groups,
                         cudaMemcpyDeviceToHost));
     StepStatus hs;
@@ -582,7 +603,7 @@ extern "C" {
 int smk_set_sweep_kernel(smk_sim* sim, int depth, int zchunk) {
     if (!sim) return fail(SMK_ERR_INVALID, "sim is null");
     if (depth != 0 && !sweep_tb_depth_supported(depth))
-        return fail(SMK_ERR_INVALID, "sweep depth must be 0, 2, 4, 6 or 8");
+        return fail(SMK_ERR_INVALID, "sweep depth must be 0, 2, 4 or 6");
     if (zchunk < 1) return fail(SMK_ERR_INVALID, "zchunk must be >= 1");
     sim->sweep_depth = depth;
     sim->sweep_zchunk = zchunk;

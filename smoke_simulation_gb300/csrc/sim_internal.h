@@ -8,6 +8,8 @@
 #include "../../include/smoke_gb300.h"
 #include "common.cuh"
 
+namespace smk { struct SweepMaps; }
+
 struct smk_sim {
     enum Kind { OBJ_OBSTACLE = 0, OBJ_SPHERE = 1, OBJ_BOX = 2 };
     struct Object {
@@ -31,6 +33,8 @@ struct smk_sim {
     float* P2 = nullptr;  // second pressure buffer (temporally blocked sweeps ping-pong)
     float* b = nullptr;
     int* pcur = nullptr;  // device: which pressure buffer the last executed sweep wrote
+    int* kerr = nullptr;  // device: a bounded wait in a kernel gave up (sticky until read)
+    smk::SweepMaps* maps = nullptr;  // TMA tensor maps of P, P2, b, flags
     uint8_t* s = nullptr;
     uint8_t* flags = nullptr;
     smk::StepStatus* status = nullptr;
@@ -44,7 +48,7 @@ struct smk_sim {
     // sweep kernel: 0 = one colour pass per launch; T > 0 = temporally blocked, T passes per
     // launch over z-chunks of sweep_zchunk planes (chosen by smk_set_sweep_kernel / autotune)
     int sweep_depth = 4;
-    int sweep_zchunk = 32;
+    int sweep_zchunk = 47;
 
     bool timing = false;
     cudaEvent_t ev[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};

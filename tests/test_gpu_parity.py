@@ -114,9 +114,9 @@ def test_reference_api_symbols_match_golden_app80(gpu):
 
 @pytest.mark.parametrize("dims,seed", [((20, 16, 18), 11), ((33, 17, 29), 41), ((64, 64, 64), 42)])
 @pytest.mark.parametrize("tol", [0.0, 1e-3])
-@pytest.mark.parametrize("kernel", [(0, 1), (2, 7), (4, 32), (6, 5), (8, 64)])
+@pytest.mark.parametrize("kernel", [(0, 1), (2, 7), (4, 32), (6, 5), (4, 3)])
 def test_pressure_scheme_equals_oracle(gpu, dims, seed, tol, kernel):
-    """Every sweep kernel (one colour pass per launch, or temporally blocked with depth 2-8
+    """Every sweep kernel (one colour pass per launch, or temporally blocked with depth 2-6
     over several z-chunk sizes) reproduces the oracle bit for bit, including the tolerance
     rule's sweep counts and residuals."""
     sc = S.small_scene(*dims, steps=5, seed=seed, scheme=1, iterations=41, tol=tol,
