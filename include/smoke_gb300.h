@@ -154,6 +154,25 @@ long long smk_launch_count(const smk_sim* sim);
 int smk_set_sweep_kernel(smk_sim* sim, int depth, int zchunk);
 int smk_get_sweep_kernel(const smk_sim* sim, int* depth, int* zchunk);
 
+/* Pressure projection of a caller-owned velocity field that allocates no device memory.
+ * No counterpart in the reference: it is for callers that cannot call cudaMalloc when they need
+ * the projection (inside a stream capture, under a fixed-budget or framework-owned memory
+ * pool, in a hook where a synchronising allocation is not allowed).  u, v, w: device arrays in
+ * the reference's face layout ((nx+1)(ny+1)(nz+1) floats, x fastest), projected in place;
+ * mask: device array of nx*ny*nz bytes, nonzero = fluid.  Uses params->max_sweeps, omega, tol
+ * and check_every with the PRESSURE scheme's arithmetic (results equal smk_step's projection).
+ * Scratch comes from one fixed device array inside the library (about 19 MB, held by every GPU
+ * that loads the library until exit): grids with (nx+1)(ny+1)(nz+1) > 2,097,152 are rejected
+ * with SMK_ERR_INVALID.  All calls share that array: calls that overlap on the GPU race; order
+ * them on one stream.  The first call on a device looks up the array's address
+ * (cudaGetSymbolAddress): make it before any stream capture.  stats may be NULL (stream-ordered
+ * call); when given, the call synchronises `stream` and fills sweeps/converged/resid/div. */
+int smk_project_noalloc(float* u, float* v, float* w, const uint8_t* mask, int nx, int ny, int nz,
+                        const smk_params* params, smk_stats* stats, void* stream);
+/* The size limit above, and the message of the last failed smk_project_noalloc call. */
+long long smk_project_noalloc_max_elems(void);
+const char* smk_project_noalloc_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif

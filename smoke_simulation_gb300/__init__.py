@@ -90,6 +90,10 @@ def lib() -> C.CDLL:
         "smk_launch_count": (C.c_longlong, [vp]),
         "smk_set_sweep_kernel": (i, [vp, i, i]),
         "smk_get_sweep_kernel": (i, [vp, C.POINTER(i), C.POINTER(i)]),
+        "smk_project_noalloc": (i, [vp, vp, vp, vp, i, i, i, C.POINTER(Params),
+                                    C.POINTER(Stats), vp]),
+        "smk_project_noalloc_max_elems": (C.c_longlong, []),
+        "smk_project_noalloc_last_error": (C.c_char_p, []),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
