@@ -2,7 +2,7 @@
 
 Workload (one "step" = one full simulation step of one 256^3 grid): FP32 fields, 5% Bernoulli
 solids (seed 1) plus two r=24 spheres, four seeded sphere emitters, dt = 0.02, pressure-form
-red-black SOR to max|residual| <= 1e-4 checked every 10 sweeps, capped at 200 sweeps.
+red-black SOR to max|residual| <= 1e-4 checked every 6 sweeps, capped at 200 sweeps.
 Synthetic inputs from smoke_simulation_gb300.scenes (the reference publishes no dataset).
 
   value   cell-updates/s with the state resident in HBM (CUDA events on the step stream)
@@ -250,9 +250,9 @@ def main():
     sim = smk.from_scene(sc, report_div=1)
     stream = torch.cuda.Stream()
     sh = stream.cuda_stream
-    sim.set_timing(True)
+    depth, zchunk, tuned_us = sim.autotune()
 
-    # warm-up steps (part of the simulation; state evolves)
+    # warm-up steps (part of the simulation; state evolves; steady steps replay a CUDA graph)
     for _ in range(max(args.warmup, 0)):
         sim.step(sc.dt, sh)
     torch.cuda.synchronize()
@@ -269,8 +269,6 @@ def main():
     e0.record(stream)
     for _ in range(args.steps):
         sim.step(sc.dt, sh)
-        # per-step stats need the step's status: read after the timed region from the events
-        # the library recorded (no host sync inside the region)
     e1.record(stream)
     torch.cuda.synchronize()
     dist_barrier(ws)
@@ -278,8 +276,10 @@ def main():
     elapsed = e0.elapsed_time(e1) / 1e3
     launches = sim.launch_count() - launches0
 
-    # per-step statistics and stage times: replay a few steps with a sync after each (outside
-    # the timed region) to read the solver status and the event-timed sweep phase
+    # per-step statistics and stage times: the next few steps of the same simulation, with a
+    # sync after each (outside the timed region) to read the solver status and the sweep phase
+    # timed by CUDA events on the step stream (these steps launch directly, not as a graph)
+    sim.set_timing(True)
     for _ in range(min(args.steps, 5)):
         sim.step(sc.dt, sh)
         st = sim.stats()
@@ -292,21 +292,25 @@ def main():
     cells_all = dist_sum(float(sc.cells * args.steps), ws)
     value = cells_all / elapsed_max
 
-    # ---- roofline of the sweep phase ---------------------------------------------------------
+    # ---- roofline of the dominant kernel (the blocked sweep, per launch) ---------------------
+    # algorithmic bytes per launch = cells x 13 B x (depth/2 sweeps); the launch duration is the
+    # event-timed sweep phase of the measured steps divided by the launches that ran in it
+    # (the residual check is fused into the first launch of each group: no extra bytes)
     peak, peak_kind = load_peaks()
     mean_sweeps = float(np.mean(sweeps))
-    checks = int(np.ceil(mean_sweeps / sc.check_every)) + 1
-    sweep_bytes = sc.cells * (SWEEP_BYTES_PER_CELL * mean_sweeps + CHECK_BYTES_PER_CELL * checks)
-    proj_seconds = float(np.mean(sweep_ms)) / 1e3
-    achieved = sweep_bytes / proj_seconds / 1e9 if proj_seconds > 0 else None
+    sweeps_per_launch = depth / 2.0 if depth > 0 else 0.5
+    launches_run = mean_sweeps / sweeps_per_launch
+    bytes_per_launch = sc.cells * SWEEP_BYTES_PER_CELL * sweeps_per_launch
+    launch_seconds = float(np.mean(sweep_ms)) / 1e3 / launches_run
+    achieved = bytes_per_launch / launch_seconds / 1e9 if launch_seconds > 0 else None
+    sweep_bytes = bytes_per_launch * launches_run
     traffic = None
     tf = os.path.join(ROOT, "profiles", "sweep_traffic.json")
-    if os.path.exists(tf):
+    if os.path.exists(tf) and depth > 0:
         with open(tf) as f:
             tr = json.load(f)
-        traffic = tr.get("bytes_per_cell_per_sweep")
-        if traffic is not None:
-            traffic = traffic * sc.cells
+        if tr.get("kernel") == "k_sweep_tb<%d>" % depth:
+            traffic = tr["bytes_per_cell_per_sweep"] * sweeps_per_launch * sc.cells
 
     # ---- e2e through the public API with host buffers ----------------------------------------
     e2e_steps = args.e2e_steps or args.steps
@@ -341,17 +345,21 @@ def main():
             "data": "synthetic",
             "config": {"workload": "smoke step %d^3 FP32, 5%% random solids + 2 spheres r=24, 4 "
                                    "emitters, dt=0.02, pressure red-black SOR to max|div|<=1e-4 "
-                                   "(checked every 10 sweeps, cap 200)" % args.n,
+                                   "(checked every 6 sweeps, cap 200)" % args.n,
                        "cells": sc.cells, "parallelism": "replicas" if ws > 1 else "single",
                        "l2": "inputs larger than L2 (%.0f MB resident state)" % (
                            sim_bytes(sc) / 1e6),
                        "mean_sweeps": mean_sweeps, "converged_frac": float(np.mean(conv)),
+                       "sweep_kernel": {"depth": depth, "zchunk": zchunk, "tuned_us_per_sweep": tuned_us},
                        "max_div_post_projection": float(np.max(divs))},
-            "roofline": {"bound": "hbm", "kernel": "k_sweep+k_resid_check (sweep phase)",
+            "roofline": {"bound": "hbm", "kernel": "k_sweep_tb<%d> (z-chunk %d)" % (depth, zchunk),
                          "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": (achieved / peak) if achieved else None, "traffic": traffic,
-                         "peak_kind": peak_kind,
-                         "algorithmic_bytes": sweep_bytes},
+                         "peak_kind": peak_kind, "bytes_per_launch": bytes_per_launch,
+                         "launch_us": launch_seconds * 1e6,
+                         "note": "achieved = algorithmic bytes per launch / mean launch duration; "
+                                 "temporal blocking applies depth/2 sweeps per HBM pass, so "
+                                 "achieved can exceed the single-pass roofline"},
             "clocks": clk,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 16 * len(sc.spheres),
                     "d2h_bytes_per_step": 4 * sc.cells, "api": "smk_simulate (pinned host out)"},

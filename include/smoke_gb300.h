@@ -153,6 +153,15 @@ long long smk_launch_count(const smk_sim* sim);
  * smokeSimulation.cu:795-801). */
 int smk_set_sweep_kernel(smk_sim* sim, int depth, int zchunk);
 int smk_get_sweep_kernel(const smk_sim* sim, int* depth, int* zchunk);
+/* Replay steady-state steps as a captured CUDA graph (default on).  A graph is re-captured
+ * when dt, the parameters, the objects or the sweep kernel change; steps after a mask or
+ * obstacle change run directly.  Results are identical either way. */
+int smk_set_graphs(smk_sim* sim, int enable);
+/* Time the blocked sweep kernel's depths and z-chunk sizes on this simulation's buffers and
+ * keep the fastest (cached per grid shape and device for the process).  Synchronises; does not
+ * change the simulation's results.  Outputs may be NULL; us_per_sweep is -1 on a cache hit.
+ * No counterpart in the reference. */
+int smk_autotune(smk_sim* sim, int* depth, int* zchunk, float* us_per_sweep);
 
 /* Pressure projection of a caller-owned velocity field that allocates no device memory.
  * No counterpart in the reference: it is for callers that cannot call cudaMalloc when they need

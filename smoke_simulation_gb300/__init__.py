@@ -93,6 +93,8 @@ def lib() -> C.CDLL:
         "smk_project_noalloc": (i, [vp, vp, vp, vp, i, i, i, C.POINTER(Params),
                                     C.POINTER(Stats), vp]),
         "smk_project_noalloc_max_elems": (C.c_longlong, []),
+        "smk_autotune": (i, [vp, C.POINTER(i), C.POINTER(i), C.POINTER(f)]),
+        "smk_set_graphs": (i, [vp, i]),
         "smk_project_noalloc_last_error": (C.c_char_p, []),
     }
     for name, (res, args) in sig.items():
@@ -271,6 +273,15 @@ class Simulation:
 
     def set_sweep_kernel(self, depth: int, zchunk: int = 32):
         _check(lib().smk_set_sweep_kernel(self.h, depth, zchunk))
+
+    def autotune(self):
+        """Pick the fastest sweep kernel shape for this grid; returns (depth, zchunk, us/sweep)."""
+        d, z, t = C.c_int(), C.c_int(), C.c_float()
+        _check(lib().smk_autotune(self.h, C.byref(d), C.byref(z), C.byref(t)))
+        return d.value, z.value, t.value
+
+    def set_graphs(self, on: bool = True):
+        _check(lib().smk_set_graphs(self.h, int(on)))
 
     def sweep_kernel(self):
         d, z = C.c_int(), C.c_int()

@@ -39,6 +39,8 @@ void launch_gradient_subtract(const Grid& g, float* u, float* v, float* w, const
 // `check` launches also record the residual of the input state for tolerance group `group`.
 // The pressure buffers are read through TMA tensor maps built once per simulation.
 int sweep_tb_depth_supported(int T);
+// Set the kernels' shared-memory attributes once (outside any stream capture).
+int prepare_sweep_kernels();
 struct SweepMaps;
 SweepMaps* create_sweep_maps(const Grid& g, const float* Pa, const float* Pb, const float* b,
                              const uint8_t* flags);

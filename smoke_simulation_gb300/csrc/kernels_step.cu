@@ -219,8 +219,12 @@ __global__ void k_advect_velocity(Grid g, const float* __restrict__ u0, const fl
 }
 
 // ---- a: advectSmoke (smokeSimulation.cu:617-638) --------------------------------------------
-// Uses the NEW velocities; the backtrace x + 0.5 - u*dt is evaluated in double as in the
-// reference (int + double literal), then rounded to float.
+// Uses the NEW velocities.  The reference evaluates the backtrace x + 0.5 - u*dt in double
+// (int + double literal) and rounds to float.  With a = x + 0.5 (exact, lowest bit 2^-1) and
+// b = u*dt (a float), the exact a - b needs at most max(e_a - e_b, 0) + 24 bits, so it is exact
+// in double unless |b| < a*2^-29; then a - b lies strictly inside a's float rounding interval,
+// in double too.  Either way float(double(a) - double(b)) equals the single-rounded float
+// subtraction, which avoids GB300's slow FP64 pipe (the golden-vector tests pin this).
 __global__ void k_advect_density(Grid g, const float* __restrict__ r0, float* __restrict__ r1,
                                  const float* __restrict__ u, const float* __restrict__ v,
                                  const float* __restrict__ w, const uint8_t* __restrict__ flags,
@@ -234,9 +238,9 @@ __global__ void k_advect_density(Grid g, const float* __restrict__ r0, float* __
     float ut = (u[i] + u[i + 1]) / 2.0f;
     float vt = (v[i] + v[i + g.X]) / 2.0f;
     float wt = (w[i] + w[i + g.XY]) / 2.0f;
-    float xt = __double2float_rn(((double)x + 0.5) - (double)(ut * dt));
-    float yt = __double2float_rn(((double)y + 0.5) - (double)(vt * dt));
-    float zt = __double2float_rn(((double)z + 0.5) - (double)(wt * dt));
+    float xt = __fsub_rn((float)x + 0.5f, ut * dt);
+    float yt = __fsub_rn((float)y + 0.5f, vt * dt);
+    float zt = __fsub_rn((float)z + 0.5f, wt * dt);
     r1[i] = sample_ref(r0, g, xt, yt, zt, 0.5f, 0.5f, 0.5f);
 }
 

@@ -390,19 +390,21 @@ bool encode_3d(CUtensorMap* m, const void* base, bool is_u8, const Grid& g) {
 }
 
 template <int T>
+constexpr size_t tb_smem_bytes() {
+    return 128 + (size_t)((T + 4) / 2) * STAGE_BYTES + sizeof(float2) * 2 * (T + 1) * 2 * (TB_TY + 2) * TB_TX;
+}
+
+template <int T>
+int configure_tb() {
+    return cudaFuncSetAttribute(k_sweep_tb<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)tb_smem_bytes<T>()) == cudaSuccess ? 0 : -1;
+}
+
+template <int T>
 int launch_tb(const TBMaps& maps, const Grid& g, float* Pout, int nhalf, int colour0, int zchunk,
               const float* wacc7, StepStatus* status, int check, int group, float tol, int* pcur,
               int out_idx, int* kerr, cudaStream_t st) {
-    static bool configured = false;
-    constexpr int TB_S = (T + 4) / 2;
-    const size_t smem =
-        128 + (size_t)TB_S * STAGE_BYTES + sizeof(float2) * 2 * (T + 1) * 2 * (TB_TY + 2) * TB_TX;
-    if (!configured) {
-        if (cudaFuncSetAttribute(k_sweep_tb<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-            cudaSuccess)
-            return -1;
-        configured = true;
-    }
+    const size_t smem = tb_smem_bytes<T>();
     WAcc8 wa;
     for (int k = 0; k < 7; ++k) wa.w[k] = wacc7[k];
     wa.w[7] = 0.0f;
@@ -417,6 +419,8 @@ int launch_tb(const TBMaps& maps, const Grid& g, float* Pout, int nhalf, int col
 }  // namespace
 
 int sweep_tb_depth_supported(int T) { return T == 2 || T == 4 || T == 6; }
+
+int prepare_sweep_kernels() { return configure_tb<2>() | configure_tb<4>() | configure_tb<6>(); }
 
 // Tensor maps for the sweep's TMA loads: P_a, P_b, b (float) and flags (u8).
 struct SweepMaps {

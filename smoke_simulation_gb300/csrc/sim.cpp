@@ -103,7 +103,10 @@ int smk_sim::alloc() {
     status_groups = 4096;
     SMK_CUDA(cudaMalloc((void**)&status, sizeof(StepStatus) + sizeof(unsigned) * status_groups));
     SMK_CUDA(cudaMemset(status, 0, sizeof(StepStatus) + sizeof(unsigned) * status_groups));
+    SMK_CUDA(cudaMalloc((void**)&tune_status, sizeof(StepStatus) + sizeof(unsigned)));
     for (auto& e : ev) SMK_CUDA(cudaEventCreate(&e));
+    SMK_CUDA(cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking));
+    if (prepare_sweep_kernels() != 0) return fail(SMK_ERR_CUDA, "sweep kernel configuration failed");
     // initializeVolume's mask: fluid except the y = 0 floor (smokeSimulation.cu:200-207)
     std::vector<uint8_t> host((size_t)g.nx * g.ny * g.nz, 1);
     for (int z = 0; z < g.nz; ++z)
@@ -120,8 +123,12 @@ void smk_sim::release() {
     if (s) cudaFree(s);
     if (flags) cudaFree(flags);
     if (status) cudaFree(status);
+    if (tune_status) cudaFree(tune_status);
     for (auto& e : ev)
         if (e) cudaEventDestroy(e);
+    for (auto& gs : graphs)
+        if (gs.exec) cudaGraphExecDestroy(gs.exec);
+    if (cap_stream) cudaStreamDestroy(cap_stream);
 }
 
 int smk_sim::upload_mask(const uint8_t* host) {
@@ -133,7 +140,7 @@ int smk_sim::upload_mask(const uint8_t* host) {
     return SMK_OK;
 }
 
-int smk_sim::step(float dt, cudaStream_t st) {
+int smk_sim::enqueue(float dt, cudaStream_t st) {
     const int past = index_now;
     const int now = index_now ^ 1;
     index_now = now;
@@ -252,6 +259,69 @@ int smk_sim::step(float dt, cudaStream_t st) {
     if (timed) SMK_CUDA(cudaEventRecord(ev[4], st));
     SMK_CUDA(cudaGetLastError());
     ++steps;
+    last_projection = p.projection;
+    last_tol = p.tol;
+    last_max_sweeps = p.max_sweeps;
+    last_check_every = p.check_every;
+    return SMK_OK;
+}
+
+// Everything the step's kernels bake in as launch parameters: a captured graph is reused only
+// while all of it is unchanged.
+std::string smk_sim::graph_signature(float dt) const {
+    std::string sig;
+    auto put = [&sig](const void* p, size_t n) { sig.append(static_cast<const char*>(p), n); };
+    put(&dt, sizeof(dt));
+    put(&p, sizeof(p));
+    put(&sweep_depth, sizeof(sweep_depth));
+    put(&sweep_zchunk, sizeof(sweep_zchunk));
+    const char t = timing ? 1 : 0;
+    put(&t, 1);
+    for (const Object& o : objects) put(&o, sizeof(o));
+    return sig;
+}
+
+// One step.  Steady state replays a CUDA graph of the whole step (captured on an internal
+// stream, launched on the caller's): one launch call instead of ~100 for a 256^3 step with the
+// tolerance-driven solve, and the GPU runs the kernels back to back.  A step whose mask or
+// obstacles changed runs directly (it includes the one-off mask kernels), and so does a step
+// with stage timing on (events recorded inside a capture cannot be queried afterwards).
+int smk_sim::step(float dt, cudaStream_t st) {
+    if (!use_graphs || timing || mask_dirty || obstacles_dirty) return enqueue(dt, st);
+    GraphSlot& gs = graphs[index_now];
+    std::string sig = graph_signature(dt);
+    if (gs.exec == nullptr || gs.sig != sig) {
+        const int idx0 = index_now, steps0 = steps;
+        const long long l0 = launches;
+        SMK_CUDA(cudaStreamBeginCapture(cap_stream, cudaStreamCaptureModeThreadLocal));
+        const int rc = enqueue(dt, cap_stream);
+        cudaGraph_t graph = nullptr;
+        const cudaError_t ce = cudaStreamEndCapture(cap_stream, &graph);
+        if (rc != SMK_OK) {
+            if (graph) cudaGraphDestroy(graph);
+            index_now = idx0;
+            steps = steps0;
+            launches = l0;
+            return rc;
+        }
+        if (ce != cudaSuccess) return fail(SMK_ERR_CUDA, std::string("step capture: ") + cudaGetErrorString(ce));
+        gs.launches = launches - l0;
+        gs.groups = last_groups;
+        index_now = idx0;
+        steps = steps0;
+        launches = l0;
+        if (gs.exec) cudaGraphExecDestroy(gs.exec);
+        gs.exec = nullptr;
+        const cudaError_t ie = cudaGraphInstantiate(&gs.exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ie != cudaSuccess) return fail(SMK_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ie));
+        gs.sig.swap(sig);
+    }
+    SMK_CUDA(cudaGraphLaunch(gs.exec, st));
+    index_now ^= 1;
+    launches += gs.launches;
+    ++steps;
+    last_groups = gs.groups;
     last_projection = p.projection;
     last_tol = p.tol;
     last_max_sweeps = p.max_sweeps;
@@ -610,10 +680,138 @@ int smk_set_sweep_kernel(smk_sim* sim, int depth, int zchunk) {
     return SMK_OK;
 }
 
+int smk_set_graphs(smk_sim* sim, int enable) {
+    if (!sim) return fail(SMK_ERR_INVALID, "sim is null");
+    sim->use_graphs = enable != 0;
+    return SMK_OK;
+}
+
 int smk_get_sweep_kernel(const smk_sim* sim, int* depth, int* zchunk) {
     if (!sim) return fail(SMK_ERR_INVALID, "sim is null");
     if (depth) *depth = sim->sweep_depth;
     if (zchunk) *zchunk = sim->sweep_zchunk;
+    return SMK_OK;
+}
+
+}  // extern "C"
+
+// ---- autotuner ------------------------------------------------------------------------------
+//
+// The blocked sweep kernel has two free parameters: the depth T (colour passes per HBM pass)
+// and the z-chunk (planes per CTA).  Larger T moves fewer bytes per sweep but recomputes a
+// wider halo; the z-chunk trades the pipeline's start-up planes against wave quantisation on
+// the SM count.  Candidates are chunks with no unroll padding ((chunk + 2T + 1) a multiple of
+// the ring length T + 4); each is timed on the simulation's own buffers with CUDA events and
+// the fastest is kept.  Results are cached per grid shape for the process.  Tuning reads P, b
+// and the flags and writes only the second pressure buffer, after moving a live pressure out
+// of it, so the simulation's results do not depend on whether or when tuning ran.
+
+#include <map>
+#include <mutex>
+#include <tuple>
+
+namespace {
+std::mutex g_tune_mutex;
+// key: device, grid shape, tolerance group size (0 = no tolerance)
+std::map<std::tuple<int, int, int, int, int>, std::pair<int, int>> g_tune_cache;
+}  // namespace
+
+extern "C" {
+
+int smk_autotune(smk_sim* sim, int* depth_out, int* zchunk_out, float* us_per_sweep_out) {
+    if (!sim) return fail(SMK_ERR_INVALID, "sim is null");
+    DeviceGuard dg(sim->device);
+    const Grid& g = sim->g;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const int gkey = sim->p.tol > 0.0f ? sim->p.check_every : -std::max(1, std::min(sim->p.max_sweeps, 20));
+    const auto key = std::make_tuple(dev, g.nx, g.ny, g.nz, gkey);
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mutex);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) {
+            sim->sweep_depth = it->second.first;
+            sim->sweep_zchunk = it->second.second;
+            if (depth_out) *depth_out = sim->sweep_depth;
+            if (zchunk_out) *zchunk_out = sim->sweep_zchunk;
+            if (us_per_sweep_out) *us_per_sweep_out = -1.0f;
+            return SMK_OK;
+        }
+    }
+    SMK_CUDA(cudaDeviceSynchronize());
+    // a live pressure in the second buffer (warm start) moves to the first
+    int pc = 0;
+    SMK_CUDA(cudaMemcpy(&pc, sim->pcur, sizeof(int), cudaMemcpyDeviceToHost));
+    if (pc == 1) {
+        SMK_CUDA(cudaMemcpy(sim->P, sim->P2, sim->elems() * sizeof(float), cudaMemcpyDeviceToDevice));
+        SMK_CUDA(cudaMemset(sim->pcur, 0, sizeof(int)));
+    }
+    float wacc[7];
+    wacc[0] = 0.0f;
+    for (int a = 1; a <= 6; ++a) wacc[a] = (float)sim->p.omega / (float)a;
+    cudaStream_t st = nullptr;
+    SMK_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    cudaEvent_t e0, e1;
+    SMK_CUDA(cudaEventCreate(&e0));
+    SMK_CUDA(cudaEventCreate(&e1));
+    int best_d = sim->sweep_depth, best_z = sim->sweep_zchunk;
+    float best = 1e30f;
+    const int depths[3] = {2, 4, 6};
+    // time one tolerance group exactly as a step issues it: 2G colour passes in launches of
+    // `d` (the last one partial when d does not divide 2G), the first with the fused residual
+    const bool use_tol = sim->p.tol > 0.0f;
+    const int G = use_tol ? sim->p.check_every : std::max(1, std::min(sim->p.max_sweeps, 20));
+    auto run_group = [&](int d, int zc) -> int {
+        if (use_tol) SMK_CUDA(cudaMemsetAsync(sim->tune_status, 0, sizeof(StepStatus) + sizeof(unsigned), st));
+        for (int h = 0; h < 2 * G; h += d) {
+            const int nh = 2 * G - h < d ? 2 * G - h : d;
+            if (launch_sweep_tb(sim->maps, g, true, sim->P2, d, nh, h & 1, zc, wacc,
+                                use_tol ? sim->tune_status : nullptr, use_tol && h == 0, 0, sim->p.tol,
+                                nullptr, 0, sim->kerr, st) != 0)
+                return fail(SMK_ERR_CUDA, "sweep kernel configuration failed");
+        }
+        return SMK_OK;
+    };
+    for (int d : depths) {
+        const int R = d + 4;
+        for (int m = 2; m <= 16; ++m) {
+            const int zc = R * m - 2 * d - 1;
+            if (zc < 8) continue;
+            if (zc > g.nz + R) break;
+            const int reps = 2;
+            int rc = run_group(d, zc);  // warm
+            if (rc) return rc;
+            SMK_CUDA(cudaEventRecord(e0, st));
+            for (int r = 0; r < reps && rc == SMK_OK; ++r) rc = run_group(d, zc);
+            if (rc) return rc;
+            SMK_CUDA(cudaEventRecord(e1, st));
+            SMK_CUDA(cudaEventSynchronize(e1));
+            float ms = 0.0f;
+            SMK_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            const float us_per_sweep = 1e3f * ms / (reps * G);
+            if (us_per_sweep < best) {
+                best = us_per_sweep;
+                best_d = d;
+                best_z = zc;
+            }
+            if (zc > g.nz) break;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaStreamDestroy(st);
+    SMK_CUDA(cudaGetLastError());
+    int krc = check_kernel_error(sim);
+    if (krc) return krc;
+    sim->sweep_depth = best_d;
+    sim->sweep_zchunk = best_z;
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mutex);
+        g_tune_cache[key] = std::make_pair(best_d, best_z);
+    }
+    if (depth_out) *depth_out = best_d;
+    if (zchunk_out) *zchunk_out = best_z;
+    if (us_per_sweep_out) *us_per_sweep_out = best;
     return SMK_OK;
 }
 

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
 #include <vector>
 
 #include "../../include/smoke_gb300.h"
@@ -38,6 +39,7 @@ struct smk_sim {
     uint8_t* s = nullptr;
     uint8_t* flags = nullptr;
     smk::StepStatus* status = nullptr;
+    smk::StepStatus* tune_status = nullptr;  // status of the autotuner's timing launches
     int status_groups = 0;
 
     int index_now = 1;  // indexNow (:707)
@@ -66,5 +68,18 @@ struct smk_sim {
     int alloc();
     void release();
     int upload_mask(const uint8_t* host);
+    // CUDA graph replay of steady-state steps, one graph per ping-pong parity
+    struct GraphSlot {
+        cudaGraphExec_t exec = nullptr;
+        std::string sig;
+        long long launches = 0;
+        int groups = 0;
+    };
+    bool use_graphs = true;
+    GraphSlot graphs[2];
+    cudaStream_t cap_stream = nullptr;
+
     int step(float dt, cudaStream_t st);
+    int enqueue(float dt, cudaStream_t st);
+    std::string graph_signature(float dt) const;
 };

@@ -185,9 +185,10 @@ def _seeded_spheres(rng: SplitMix64, count: int, n: Tuple[int, int, int], r: int
 def config_large(n: int = 256, steps: int = 50, max_sweeps: int = 200, tol: float = 1e-4) -> Scene:
     """Single large grid: Bernoulli(0.05) solids (seed 1) plus two r=24 spheres, four seeded
     sphere emitters (r=6, lower half), dt=0.02, pressure red-black SOR to max|div| <= tol capped
-    at max_sweeps sweeps."""
+    at max_sweeps sweeps, residual checked every 6 sweeps (a group of 12 colour passes splits
+    evenly into launches of 2, 4 or 6 passes)."""
     sc = Scene("large%d" % n, n, n, n, dt=0.02, steps=steps, scheme=1, iterations=max_sweeps,
-               tol=tol, check_every=10)
+               tol=tol, check_every=6)
     rng = SplitMix64(1, lane=3)
     r_obs = max(2, (24 * n) // 256)
     solids = _seeded_spheres(rng, 2, (n, n, n), r_obs)
