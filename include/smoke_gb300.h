@@ -163,6 +163,17 @@ int smk_set_graphs(smk_sim* sim, int enable);
  * No counterpart in the reference. */
 int smk_autotune(smk_sim* sim, int* depth, int* zchunk, float* us_per_sweep);
 
+/* Batches: many independent grids stepped together.  A batch step is one CUDA graph launch in
+ * which every member grid's full step is a concurrent branch (re-captured when a member's dt,
+ * parameters, objects, sweep kernel or ping-pong parity changes).  Members keep their own state
+ * and results (identical to stepping them alone); the batch does not own them.  No counterpart
+ * in the reference (one implicit grid, smokeSimulation.cu:16-24). */
+typedef struct smk_batch smk_batch;
+int smk_batch_create(int count, smk_sim* const* sims, smk_batch** out);
+/* dts: one dt per member, or NULL to use dt_all for every member.  Stream-ordered. */
+int smk_batch_step(smk_batch* batch, const float* dts, float dt_all, void* stream);
+int smk_batch_destroy(smk_batch* batch);
+
 /* Pressure projection of a caller-owned velocity field that allocates no device memory.
  * No counterpart in the reference: it is for callers that cannot call cudaMalloc when they need
  * the projection (inside a stream capture, under a fixed-budget or framework-owned memory

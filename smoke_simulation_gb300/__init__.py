@@ -95,6 +95,9 @@ def lib() -> C.CDLL:
         "smk_project_noalloc_max_elems": (C.c_longlong, []),
         "smk_autotune": (i, [vp, C.POINTER(i), C.POINTER(i), C.POINTER(f)]),
         "smk_set_graphs": (i, [vp, i]),
+        "smk_batch_create": (i, [i, C.POINTER(vp), C.POINTER(vp)]),
+        "smk_batch_step": (i, [vp, C.POINTER(f), f, vp]),
+        "smk_batch_destroy": (i, [vp]),
         "smk_project_noalloc_last_error": (C.c_char_p, []),
     }
     for name, (res, args) in sig.items():
@@ -287,6 +290,36 @@ class Simulation:
         d, z = C.c_int(), C.c_int()
         _check(lib().smk_get_sweep_kernel(self.h, C.byref(d), C.byref(z)))
         return d.value, z.value
+
+
+class Batch:
+    """Many independent grids stepped as one CUDA graph launch (smk_batch_*).  The batch does
+    not own its members; keep the Simulation objects alive while the batch is in use."""
+
+    def __init__(self, sims):
+        self.sims = list(sims)
+        arr = (C.c_void_p * len(self.sims))(*[s.h.value for s in self.sims])
+        self.h = C.c_void_p()
+        _check(lib().smk_batch_create(len(self.sims), arr, C.byref(self.h)))
+
+    def step(self, dt, stream: int = 0):
+        """dt: one float for every member, or a sequence with one dt per member."""
+        if isinstance(dt, (list, tuple, np.ndarray)):
+            dts = (C.c_float * len(self.sims))(*[float(x) for x in dt])
+            _check(lib().smk_batch_step(self.h, dts, 0.0, stream))
+        else:
+            _check(lib().smk_batch_step(self.h, None, float(dt), stream))
+
+    def close(self):
+        if self.h:
+            lib().smk_batch_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def params_for_scene(scene, **overrides) -> Params:

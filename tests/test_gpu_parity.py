@@ -138,6 +138,24 @@ def test_pressure_scheme_equals_oracle(gpu, dims, seed, tol, kernel):
     sim.close()
 
 
+@pytest.mark.parametrize("kernel", [(0, 1), (4, 11), (6, 25)])
+def test_warm_start_equals_oracle(gpu, kernel):
+    """Warm start (the pressure carried across steps, including through the blocked kernel's
+    second buffer) follows the oracle bit for bit, and stays within the tolerance."""
+    sc = S.small_scene(36, 30, 40, steps=6, seed=55, scheme=1, iterations=60, tol=1e-3,
+                       check_every=6, obstacles=1, warm_start=1)
+    o = O.OracleSim(sc)
+    sim = smk.from_scene(sc, report_div=1)
+    sim.set_sweep_kernel(*kernel)
+    for k in range(sc.steps):
+        ost = o.step()
+        sim.step(sc.dt)
+        st = sim.stats()
+        assert st.sweeps == ost.sweeps and st.div_max == ost.div_max
+        assert H.first_mismatch(sim.read_state(), H.oracle_state(o)) == "", k
+    sim.close()
+
+
 def test_pressure_scheme_within_tolerance_of_reference_and_fp64(gpu):
     sc = S.config_ref80(steps=40)
     sim = _run_gpu(sc, projection=1)
