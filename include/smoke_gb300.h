@@ -174,6 +174,49 @@ int smk_batch_create(int count, smk_sim* const* sims, smk_batch** out);
 int smk_batch_step(smk_batch* batch, const float* dts, float dt_all, void* stream);
 int smk_batch_destroy(smk_batch* batch);
 
+/* Serving: many simulation requests kept resident on one GPU with continuous admission.  No
+ * counterpart in the reference (one simulation stepped from the render loop, main.cpp:889-896).
+ * smk_server_tick retires requests whose last step completed (their density goes to
+ * out_density), admits queued requests in arrival order while the device-memory budget and
+ * the slot limit allow, and issues one step per active request on its own stream (work of
+ * different requests overlaps).  Per-step latency = device time of a request's step, measured
+ * with events on its stream.  Each request is an independent simulation: its results are the
+ * same alone and in the mix. */
+#define SMK_REQ_QUEUED 0
+#define SMK_REQ_ACTIVE 1
+#define SMK_REQ_DONE 2
+#define SMK_REQ_FAILED 3
+typedef struct smk_server smk_server;
+typedef struct smk_request_desc {
+    int nx, ny, nz;            /* grid cells */
+    int steps;                 /* steps to run */
+    float dt;
+    const smk_params* params;  /* NULL: smk_default_params */
+    const uint8_t* mask;       /* host, nx*ny*nz bytes (1 = fluid); NULL: reference initial mask */
+    const float* spheres;      /* sphere sources, 4 floats each (x, y, z, r) */
+    int n_spheres;
+    const float* boxes;        /* box emitters, 9 floats each (x0,y0,z0,x1,y1,z1,density,vy,set_vy) */
+    int n_boxes;
+    const float* obstacles;    /* obstacles, 7 floats each (x,y,z,vx,vy,vz,r) */
+    int n_obstacles;
+    float* out_density;        /* host, nx*ny*nz floats, written at completion (may be NULL) */
+} smk_request_desc;
+typedef struct smk_server_stats {
+    long long steps_completed;
+    int requests_completed;
+    int active, queued;
+    double cell_updates;
+    size_t bytes_in_use;
+    float p50_step_ms, p99_step_ms, max_step_ms;
+} smk_server_stats;
+int smk_server_create(size_t budget_bytes, int max_active, smk_server** out);
+int smk_server_submit(smk_server* server, const smk_request_desc* request, int* id);
+int smk_server_tick(smk_server* server, int* n_active, int* n_queued);
+int smk_server_request_status(smk_server* server, int id, int* state, int* steps_done, int* error);
+int smk_server_get_stats(smk_server* server, smk_server_stats* out);
+int smk_server_destroy(smk_server* server);
+const char* smk_server_last_error(void);
+
 /* Pressure projection of a caller-owned velocity field that allocates no device memory.
  * No counterpart in the reference: it is for callers that cannot call cudaMalloc when they need
  * the projection (inside a stream capture, under a fixed-budget or framework-owned memory

@@ -3,18 +3,20 @@
 // Each kernel restates one stage of the reference step (project/smokeSimulation.cu) with the
 // reference's exact floating-point expression order, on the library's pitched layout
 // (common.cuh) and with x-contiguous, coalesced thread mapping (one thread per x, a warp per
-// row segment) instead of the reference's 8x8x8 cubes.
+// row segment) instead of the reference's 8x8x8 cubes.  The per-step stage bodies live in
+// stage_bodies.cuh, shared with the grouped (batch) kernels.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
 #include "common.cuh"
 #include "kernels.h"
+#include "stage_bodies.cuh"
 
 namespace smk {
 
 namespace {
 
-constexpr int BX = 64, BY = 4;
+constexpr int BX = SB_BX, BY = SB_BY;
 
 inline dim3 grid3(int rx, int ry, int rz) {
     return dim3((unsigned)((rx + BX - 1) / BX), (unsigned)((ry + BY - 1) / BY), (unsigned)rz);
@@ -25,51 +27,22 @@ struct SphereList { int n; SphereObj s[MAX_OBJ_PER_LAUNCH]; };
 struct ObstacleList { int n; ObstacleObj o[MAX_OBJ_PER_LAUNCH]; };
 struct BoxList { int n; BoxObj b[MAX_OBJ_PER_LAUNCH]; };
 
-// ---- a4: emitters ---------------------------------------------------------------------------
+// ---- a4: emitters and obstacles ---------------------------------------------------------------
 
-// Box emitters over the union box [lo, hi): density into both buffers, optional v-faces.
 __global__ void k_emit_boxes(Grid g, float* __restrict__ rho0, float* __restrict__ rho1,
-                             float* __restrict__ v_now, BoxList L, int x0, int y0, int z0, int x1,
-                             int y1) {
-    int x = x0 + blockIdx.x * BX + threadIdx.x;
-    int y = y0 + blockIdx.y * BY + threadIdx.y;
-    int z = z0 + blockIdx.z;
-    if (x >= x1 || y >= y1) return;
-    for (int k = 0; k < L.n; ++k) {
-        const BoxObj& b = L.b[k];
-        if (x >= b.x0 && x < b.x1 && y >= b.y0 && y < b.y1 && z >= b.z0 && z < b.z1) {
-            int i = g.idx(x, y, z);
-            rho0[i] = b.density;
-            rho1[i] = b.density;
-            if (b.set_vy) {
-                v_now[i] = b.vy;
-                v_now[i + g.X] = b.vy;
-            }
-        }
-    }
+                             float* __restrict__ v_now, const __grid_constant__ BoxList L, int x0,
+                             int y0, int z0, int x1, int y1, int z1) {
+    body_emit_boxes(g, rho0, rho1, v_now, L.b, L.n, x0, y0, z0, x1, y1, z1, blockIdx);
 }
 
-// fillSmoke (smokeSimulation.cu:251-273): interior cells, float squared distance from the
-// integer corner, strict test, density 1 in both buffers.
-__global__ void k_fill_smoke(Grid g, float* __restrict__ rho0, float* __restrict__ rho1, SphereList L,
-                             int x0, int y0, int z0, int x1, int y1) {
-    int x = x0 + blockIdx.x * BX + threadIdx.x;
-    int y = y0 + blockIdx.y * BY + threadIdx.y;
-    int z = z0 + blockIdx.z;
-    if (x >= x1 || y >= y1) return;
-    for (int k = 0; k < L.n; ++k) {
-        float dx = (float)x - L.s[k].x, dy = (float)y - L.s[k].y, dz = (float)z - L.s[k].z;
-        float dist = dx * dx + dy * dy + dz * dz;
-        if (dist < L.s[k].r * L.s[k].r) {
-            int i = g.idx(x, y, z);
-            rho0[i] = 1.0f;
-            rho1[i] = 1.0f;
-        }
-    }
+__global__ void k_fill_smoke(Grid g, float* __restrict__ rho0, float* __restrict__ rho1,
+                             const __grid_constant__ SphereList L, int x0, int y0, int z0, int x1,
+                             int y1, int z1) {
+    body_fill_smoke(g, rho0, rho1, L.s, L.n, x0, y0, z0, x1, y1, z1, blockIdx);
 }
 
 // fillObstacle (smokeSimulation.cu:289-313): interior cells; each obstacle overwrites the
-// cell, so the last one decides.  `first` marks the first chunk of obstacles.
+// cell, so the last one decides.
 __global__ void k_fill_obstacles(Grid g, uint8_t* __restrict__ s, ObstacleList L) {
     int x = 1 + blockIdx.x * BX + threadIdx.x;
     int y = 1 + blockIdx.y * BY + threadIdx.y;
@@ -105,41 +78,10 @@ __global__ void k_build_flags(Grid g, const uint8_t* __restrict__ s, uint8_t* __
 }
 
 // ---- b: integrate (smokeSimulation.cu:315-329) + velocityConfinement (:331-352) ------------
-// Both are pointwise on the shared staggered index, so one pass applies integrate then clamp.
 __global__ void k_forcing(Grid g, float* __restrict__ u, float* __restrict__ v, float* __restrict__ w,
                           const float* __restrict__ rho, const uint8_t* __restrict__ flags, float dt,
                           float gravity, float alpha, float lim_sq, float lim, int clamp_mode) {
-    int x = blockIdx.x * BX + threadIdx.x;
-    int y = 1 + blockIdx.y * BY + threadIdx.y;
-    int z = blockIdx.z;
-    if (x >= g.nx || y >= g.ny) return;
-    int i = g.idx(x, y, z);
-    uint8_t f = flags[i];
-    float vt = v[i];
-    if ((f & F_SELF) && (f & F_YM)) {
-        float r = rho[i];
-        float buoy = alpha * (r - 0.0f);
-        vt = vt + (r * gravity * dt + buoy * dt);
-        if (!(x >= 1 && z >= 1 && clamp_mode != 2)) v[i] = vt;
-    }
-    if (x >= 1 && z >= 1 && clamp_mode != 2) {
-        float ut = u[i], wt = w[i];
-        float len = ut * ut + vt * vt + wt * wt;
-        if (clamp_mode == 0) {
-            if (len * dt > lim_sq) {
-                float s = lim_sq / (len * dt);
-                u[i] = ut * s;
-                vt = vt * s;
-                w[i] = wt * s;
-            }
-        } else if (len > lim * lim) {
-            float s = lim / sqrtf(len);
-            u[i] = ut * s;
-            vt = vt * s;
-            w[i] = wt * s;
-        }
-        v[i] = vt;
-    }
+    body_forcing(g, u, v, w, rho, flags, dt, gravity, alpha, lim_sq, lim, clamp_mode, blockIdx);
 }
 
 // ---- d (reference scheme): divergence kernel (smokeSimulation.cu:356-394) ------------------
@@ -172,94 +114,26 @@ __global__ void k_project_velocity(Grid g, float* __restrict__ u, float* __restr
     w[iz] = w[iz] + pt * (float)sz1;
 }
 
-// ---- a: velocityAdvectionU/V/W (smokeSimulation.cu:527-615), fused -------------------------
-// One thread per staggered index computes whichever of the three face updates apply there.
+// ---- a: velocityAdvectionU/V/W (:527-615) and advectSmoke (:617-638) ------------------------
 __global__ void k_advect_velocity(Grid g, const float* __restrict__ u0, const float* __restrict__ v0,
                                   const float* __restrict__ w0, float* __restrict__ u1,
                                   float* __restrict__ v1, float* __restrict__ w1,
                                   const uint8_t* __restrict__ flags, float dt) {
-    int x = 1 + blockIdx.x * BX + threadIdx.x;
-    int y = 1 + blockIdx.y * BY + threadIdx.y;
-    int z = 1 + blockIdx.z;
-    if (x >= g.nx || y >= g.ny) return;
-    const int i = g.idx(x, y, z);
-    const uint8_t f = flags[i];
-    if (!(f & F_SELF)) return;
-    const bool inx = x <= g.nx - 2, iny = y <= g.ny - 2, inz = z <= g.nz - 2;
-    if (iny && inz && (f & F_XM)) {
-        float xt = (float)x, yt = (float)y + 0.5f, zt = (float)z + 0.5f;
-        float uu = u0[i];
-        float vv = avgV(v0, g, i);
-        float ww = avgW(w0, g, i);
-        xt = xt - dt * uu;
-        yt = yt - dt * vv;
-        zt = zt - dt * ww;
-        u1[i] = sample_ref(u0, g, xt, yt, zt, 0.0f, 0.5f, 0.5f);
-    }
-    if (inx && inz && (f & F_YM)) {
-        float xt = (float)x + 0.5f, yt = (float)y, zt = (float)z + 0.5f;
-        float uu = avgU(u0, g, i);
-        float vv = v0[i];
-        float ww = avgW(w0, g, i);
-        xt = xt - dt * uu;
-        yt = yt - dt * vv;
-        zt = zt - dt * ww;
-        v1[i] = sample_ref(v0, g, xt, yt, zt, 0.5f, 0.0f, 0.5f);
-    }
-    if (inx && iny && (f & F_ZM)) {
-        float xt = (float)x + 0.5f, yt = (float)y + 0.5f, zt = (float)z;
-        float uu = avgU(u0, g, i);
-        float vv = avgV(v0, g, i);
-        float ww = w0[i];
-        xt = xt - dt * uu;
-        yt = yt - dt * vv;
-        zt = zt - dt * ww;
-        w1[i] = sample_ref(w0, g, xt, yt, zt, 0.5f, 0.5f, 0.0f);
-    }
+    body_advect_velocity(g, u0, v0, w0, u1, v1, w1, flags, dt, blockIdx);
 }
 
-// ---- a: advectSmoke (smokeSimulation.cu:617-638) --------------------------------------------
-// Uses the NEW velocities.  The reference evaluates the backtrace x + 0.5 - u*dt in double
-// (int + double literal) and rounds to float.  With a = x + 0.5 (exact, lowest bit 2^-1) and
-// b = u*dt (a float), the exact a - b needs at most max(e_a - e_b, 0) + 24 bits, so it is exact
-// in double unless |b| < a*2^-29; then a - b lies strictly inside a's float rounding interval,
-// in double too.  Either way float(double(a) - double(b)) equals the single-rounded float
-// subtraction, which avoids GB300's slow FP64 pipe (the golden-vector tests pin this).
 __global__ void k_advect_density(Grid g, const float* __restrict__ r0, float* __restrict__ r1,
                                  const float* __restrict__ u, const float* __restrict__ v,
                                  const float* __restrict__ w, const uint8_t* __restrict__ flags,
                                  float dt) {
-    int x = 1 + blockIdx.x * BX + threadIdx.x;
-    int y = 1 + blockIdx.y * BY + threadIdx.y;
-    int z = 1 + blockIdx.z;
-    if (x > g.nx - 2 || y > g.ny - 2) return;
-    const int i = g.idx(x, y, z);
-    if (!(flags[i] & F_SELF)) return;
-    float ut = (u[i] + u[i + 1]) / 2.0f;
-    float vt = (v[i] + v[i + g.X]) / 2.0f;
-    float wt = (w[i] + w[i + g.XY]) / 2.0f;
-    float xt = __fsub_rn((float)x + 0.5f, ut * dt);
-    float yt = __fsub_rn((float)y + 0.5f, vt * dt);
-    float zt = __fsub_rn((float)z + 0.5f, wt * dt);
-    r1[i] = sample_ref(r0, g, xt, yt, zt, 0.5f, 0.5f, 0.5f);
+    body_advect_density(g, r0, r1, u, v, w, flags, dt, blockIdx);
 }
 
 // max |div u| over projectable cells (post-projection diagnostic).
 __global__ void k_div_max(Grid g, const float* __restrict__ u, const float* __restrict__ v,
                           const float* __restrict__ w, const uint8_t* __restrict__ flags,
                           StepStatus* status) {
-    int x = 1 + blockIdx.x * BX + threadIdx.x;
-    int y = 1 + blockIdx.y * BY + threadIdx.y;
-    int z = 1 + blockIdx.z;
-    float m = 0.0f;
-    if (x <= g.nx - 2 && y <= g.ny - 2) {
-        int i = g.idx(x, y, z);
-        if (flags[i] & F_PROJ) {
-            float div = -u[i] + u[i + 1] + -v[i] + v[i + g.X] + -w[i] + w[i + g.XY];
-            m = fabsf(div);
-        }
-    }
-    block_max_to(__float_as_uint(m), &status->div_bits);
+    body_div_max(g, u, v, w, flags, status, blockIdx);
 }
 
 }  // namespace
@@ -285,8 +159,31 @@ void launch_emit_boxes(const Grid& g, float* rho0, float* rho1, float* v_now, co
         }
         if (x0 >= x1 || y0 >= y1 || z0 >= z1) continue;
         k_emit_boxes<<<grid3(x1 - x0, y1 - y0, z1 - z0), dim3(BX, BY), 0, st>>>(g, rho0, rho1, v_now,
-                                                                                L, x0, y0, z0, x1, y1);
+                                                                                L, x0, y0, z0, x1, y1, z1);
     }
+}
+
+// Union bounding box (one cell of margin) of a list of spheres, clipped to the interior
+// [1, n-2]; returns false when empty.
+bool sphere_bounds(const Grid& g, const SphereObj* sp, int ns, int a0[3], int a1[3]) {
+    double lo[3] = {1e30, 1e30, 1e30}, hi[3] = {-1e30, -1e30, -1e30};
+    for (int k = 0; k < ns; ++k) {
+        double c[3] = {sp[k].x, sp[k].y, sp[k].z};
+        double r = sp[k].r < 0 ? -sp[k].r : sp[k].r;
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = c[a] - r - 1 < lo[a] ? c[a] - r - 1 : lo[a];
+            hi[a] = c[a] + r + 1 > hi[a] ? c[a] + r + 1 : hi[a];
+        }
+    }
+    int n3[3] = {g.nx, g.ny, g.nz};
+    for (int a = 0; a < 3; ++a) {
+        double l = lo[a] < 1 ? 1 : lo[a];
+        double h = hi[a] > n3[a] - 2 ? n3[a] - 2 : hi[a];
+        if (!(l <= h)) return false;
+        a0[a] = (int)l;
+        a1[a] = (int)h + 1;
+    }
+    return true;
 }
 
 void launch_fill_smoke(const Grid& g, float* rho0, float* rho1, const SphereObj* sp, int ns,
@@ -294,30 +191,11 @@ void launch_fill_smoke(const Grid& g, float* rho0, float* rho1, const SphereObj*
     for (int base = 0; base < ns; base += MAX_OBJ_PER_LAUNCH) {
         SphereList L;
         L.n = ns - base < MAX_OBJ_PER_LAUNCH ? ns - base : MAX_OBJ_PER_LAUNCH;
-        // union bounding box (one cell of margin), clipped to the interior [1, n-2]
-        double lo[3] = {1e30, 1e30, 1e30}, hi[3] = {-1e30, -1e30, -1e30};
-        for (int k = 0; k < L.n; ++k) {
-            L.s[k] = sp[base + k];
-            double c[3] = {L.s[k].x, L.s[k].y, L.s[k].z};
-            double r = L.s[k].r < 0 ? -L.s[k].r : L.s[k].r;
-            for (int a = 0; a < 3; ++a) {
-                lo[a] = c[a] - r - 1 < lo[a] ? c[a] - r - 1 : lo[a];
-                hi[a] = c[a] + r + 1 > hi[a] ? c[a] + r + 1 : hi[a];
-            }
-        }
-        int n3[3] = {g.nx, g.ny, g.nz};
+        for (int k = 0; k < L.n; ++k) L.s[k] = sp[base + k];
         int a0[3], a1[3];
-        bool empty = false;
-        for (int a = 0; a < 3; ++a) {
-            double l = lo[a] < 1 ? 1 : lo[a];
-            double h = hi[a] > n3[a] - 2 ? n3[a] - 2 : hi[a];
-            if (!(l <= h)) { empty = true; break; }
-            a0[a] = (int)l;
-            a1[a] = (int)h + 1;
-        }
-        if (empty) continue;
+        if (!sphere_bounds(g, L.s, L.n, a0, a1)) continue;
         k_fill_smoke<<<grid3(a1[0] - a0[0], a1[1] - a0[1], a1[2] - a0[2]), dim3(BX, BY), 0, st>>>(
-            g, rho0, rho1, L, a0[0], a0[1], a0[2], a1[0], a1[1]);
+            g, rho0, rho1, L, a0[0], a0[1], a0[2], a1[0], a1[1], a1[2]);
     }
 }
 

@@ -1,0 +1,300 @@
+// Bodies of the per-step stage kernels, shared by the single-grid kernels (one launch per grid
+// and stage) and the grouped kernels (one launch per stage over every grid of a batch).
+//
+// A body receives its block coordinates explicitly (`bid`), checks every axis against its own
+// range, and evaluates the reference's expressions in the reference's order (see the single-
+// grid kernels in kernels_step.cu / kernels_pressure.cu for the reference lines each restates).
+// Blocks are 64 x 4 threads over x and y, one z plane per block.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "common.cuh"
+
+namespace smk {
+
+constexpr int SB_BX = 64, SB_BY = 4;
+
+struct WAcc { float w[8]; };
+
+// ---- emitters ---------------------------------------------------------------------------------
+
+// Box emitters restricted to [x0,x1)x[y0,..)x[z0,..): density into both buffers, optional v.
+__device__ __forceinline__ void body_emit_boxes(const Grid& g, float* __restrict__ rho0,
+                                                float* __restrict__ rho1, float* __restrict__ v_now,
+                                                const BoxObj* boxes, int nb, int x0, int y0, int z0,
+                                                int x1, int y1, int z1, uint3 bid) {
+    const int x = x0 + (int)bid.x * SB_BX + (int)threadIdx.x;
+    const int y = y0 + (int)bid.y * SB_BY + (int)threadIdx.y;
+    const int z = z0 + (int)bid.z;
+    if (x >= x1 || y >= y1 || z >= z1) return;
+    for (int k = 0; k < nb; ++k) {
+        const BoxObj& b = boxes[k];
+        if (x >= b.x0 && x < b.x1 && y >= b.y0 && y < b.y1 && z >= b.z0 && z < b.z1) {
+            const int i = g.idx(x, y, z);
+            rho0[i] = b.density;
+            rho1[i] = b.density;
+            if (b.set_vy) {
+                v_now[i] = b.vy;
+                v_now[i + g.X] = b.vy;
+            }
+        }
+    }
+}
+
+// fillSmoke (smokeSimulation.cu:251-273) over the box [x0,x1)x[y0,y1)x[z0,z1) (within the
+// interior): float squared distance from the integer corner, strict test, both buffers = 1.
+__device__ __forceinline__ void body_fill_smoke(const Grid& g, float* __restrict__ rho0,
+                                                float* __restrict__ rho1, const SphereObj* sp, int ns,
+                                                int x0, int y0, int z0, int x1, int y1, int z1,
+                                                uint3 bid) {
+    const int x = x0 + (int)bid.x * SB_BX + (int)threadIdx.x;
+    const int y = y0 + (int)bid.y * SB_BY + (int)threadIdx.y;
+    const int z = z0 + (int)bid.z;
+    if (x >= x1 || y >= y1 || z >= z1) return;
+    for (int k = 0; k < ns; ++k) {
+        const float dx = (float)x - sp[k].x, dy = (float)y - sp[k].y, dz = (float)z - sp[k].z;
+        const float dist = dx * dx + dy * dy + dz * dz;
+        if (dist < sp[k].r * sp[k].r) {
+            const int i = g.idx(x, y, z);
+            rho0[i] = 1.0f;
+            rho1[i] = 1.0f;
+        }
+    }
+}
+
+// ---- forcing: integrate (smokeSimulation.cu:315-329) + velocityConfinement (:331-352) -------
+__device__ __forceinline__ void body_forcing(const Grid& g, float* __restrict__ u, float* __restrict__ v,
+                                             float* __restrict__ w, const float* __restrict__ rho,
+                                             const uint8_t* __restrict__ flags, float dt, float gravity,
+                                             float alpha, float lim_sq, float lim, int clamp_mode,
+                                             uint3 bid) {
+    const int x = (int)bid.x * SB_BX + (int)threadIdx.x;
+    const int y = 1 + (int)bid.y * SB_BY + (int)threadIdx.y;
+    const int z = (int)bid.z;
+    if (x >= g.nx || y >= g.ny || z >= g.nz) return;
+    const int i = g.idx(x, y, z);
+    const uint8_t f = flags[i];
+    float vt = v[i];
+    if ((f & F_SELF) && (f & F_YM)) {
+        const float r = rho[i];
+        const float buoy = alpha * (r - 0.0f);
+        vt = vt + (r * gravity * dt + buoy * dt);
+        if (!(x >= 1 && z >= 1 && clamp_mode != 2)) v[i] = vt;
+    }
+    if (x >= 1 && z >= 1 && clamp_mode != 2) {
+        const float ut = u[i], wt = w[i];
+        const float len = ut * ut + vt * vt + wt * wt;
+        if (clamp_mode == 0) {
+            if (len * dt > lim_sq) {
+                const float s = lim_sq / (len * dt);
+                u[i] = ut * s;
+                vt = vt * s;
+                w[i] = wt * s;
+            }
+        } else if (len > lim * lim) {
+            const float s = lim / sqrtf(len);
+            u[i] = ut * s;
+            vt = vt * s;
+            w[i] = wt * s;
+        }
+        v[i] = vt;
+    }
+}
+
+// ---- pressure scheme ------------------------------------------------------------------------
+
+// b = -div(u*) on projectable cells; P = 0 off them (and everywhere on a cold start); on a warm
+// start whose previous solve ended in the second buffer (*pcur == 1) P is taken from there.
+__device__ __forceinline__ void body_rhs(const Grid& g, const float* __restrict__ u,
+                                         const float* __restrict__ v, const float* __restrict__ w,
+                                         const uint8_t* __restrict__ flags, float* __restrict__ b,
+                                         float* __restrict__ P, const float* __restrict__ P2,
+                                         const int* __restrict__ pcur, int warm, uint3 bid) {
+    const int x = (int)bid.x * SB_BX + (int)threadIdx.x;
+    const int y = (int)bid.y * SB_BY + (int)threadIdx.y;
+    const int z = (int)bid.z;
+    if (x >= g.nx || y >= g.ny || z >= g.nz) return;
+    const int i = g.idx(x, y, z);
+    if (flags[i] & F_PROJ) {
+        const float div = -u[i] + u[i + 1] + -v[i] + v[i + g.X] + -w[i] + w[i + g.XY];
+        b[i] = -div;
+        if (!warm) P[i] = 0.0f;
+        else if (pcur != nullptr && P2 != nullptr && *pcur == 1) P[i] = P2[i];
+    } else {
+        b[i] = 0.0f;
+        P[i] = 0.0f;
+    }
+}
+
+// One colour pass:  r = fma(-acc, P_c, b_c + (((P_x-+P_x+)+(P_y-+P_y+))+(P_z-+P_z+)));
+// P_c = fma(omega/acc, r, P_c).  bid.x counts same-colour cells of a row.
+__device__ __forceinline__ void body_sweep(const Grid& g, float* __restrict__ P, const float* __restrict__ b,
+                                           const uint8_t* __restrict__ flags, int colour, const WAcc& wa,
+                                           const StepStatus* __restrict__ status, uint3 bid) {
+    if (status && *(volatile const int*)&status->done) return;
+    const int y = 1 + (int)bid.y * SB_BY + (int)threadIdx.y;
+    const int z = 1 + (int)bid.z;
+    const int x = 1 + ((1 + y + z + colour) & 1) + 2 * ((int)bid.x * SB_BX + (int)threadIdx.x);
+    if (x > g.nx - 2 || y > g.ny - 2 || z > g.nz - 2) return;
+    const int i = g.idx(x, y, z);
+    const uint8_t f = flags[i];
+    if (!(f & F_PROJ)) return;
+    const int acc = __popc((unsigned)(f & F_NBRS));
+    const float sum = ((P[i - 1] + P[i + 1]) + (P[i - g.X] + P[i + g.X])) + (P[i - g.XY] + P[i + g.XY]);
+    const float pc = P[i];
+    const float r = fmaf(-(float)acc, pc, b[i] + sum);
+    P[i] = fmaf(wa.w[acc], r, pc);
+}
+
+// Residual check at the start of sweep group `group`: if the previous group's residual was
+// within tolerance the solve is over (set `done`); otherwise record max |r| for this group.
+// Contains a block barrier: every thread of the block must call it.
+__device__ __forceinline__ void body_resid_check(const Grid& g, const float* __restrict__ P,
+                                                 const float* __restrict__ b,
+                                                 const uint8_t* __restrict__ flags, StepStatus* status,
+                                                 int group, float tol, uint3 bid) {
+    if (*(volatile int*)&status->done) return;
+    if (group > 0 && __uint_as_float(status->rmax_bits[group - 1]) <= tol) {
+        if (bid.x == 0 && bid.y == 0 && bid.z == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
+            status->done = 1;
+            status->done_group = group;
+        }
+        return;
+    }
+    const int x = 1 + (int)bid.x * SB_BX + (int)threadIdx.x;
+    const int y = 1 + (int)bid.y * SB_BY + (int)threadIdx.y;
+    const int z = 1 + (int)bid.z;
+    float m = 0.0f;
+    if (x <= g.nx - 2 && y <= g.ny - 2 && z <= g.nz - 2) {
+        const int i = g.idx(x, y, z);
+        const uint8_t f = flags[i];
+        if (f & F_PROJ) {
+            const int acc = __popc((unsigned)(f & F_NBRS));
+            const float sum = ((P[i - 1] + P[i + 1]) + (P[i - g.X] + P[i + g.X])) + (P[i - g.XY] + P[i + g.XY]);
+            const float r = fmaf(-(float)acc, P[i], b[i] + sum);
+            m = fabsf(r);
+        }
+    }
+    block_max_to(__float_as_uint(m), &status->rmax_bits[group]);
+}
+
+// u -= P(x) - P(x-1) on faces whose two cells are fluid (P is 0 off the projectable set).  The
+// pressure is the first buffer, or the second when *pcur == 1.
+__device__ __forceinline__ void body_gradient_subtract(const Grid& g, float* __restrict__ u,
+                                                       float* __restrict__ v, float* __restrict__ w,
+                                                       const float* __restrict__ P0,
+                                                       const float* __restrict__ P1,
+                                                       const int* __restrict__ pcur,
+                                                       const uint8_t* __restrict__ flags, uint3 bid) {
+    const float* __restrict__ P = (pcur != nullptr && *pcur == 1) ? P1 : P0;
+    const int x = 1 + (int)bid.x * SB_BX + (int)threadIdx.x;
+    const int y = 1 + (int)bid.y * SB_BY + (int)threadIdx.y;
+    const int z = 1 + (int)bid.z;
+    if (x >= g.nx || y >= g.ny || z >= g.nz) return;
+    const int i = g.idx(x, y, z);
+    const uint8_t f = flags[i];
+    if (!(f & F_SELF)) return;
+    const bool inx = x <= g.nx - 2, iny = y <= g.ny - 2, inz = z <= g.nz - 2;
+    const float pc = P[i];
+    if (iny && inz && (f & F_XM)) u[i] = u[i] - (pc - P[i - 1]);
+    if (inx && inz && (f & F_YM)) v[i] = v[i] - (pc - P[i - g.X]);
+    if (inx && iny && (f & F_ZM)) w[i] = w[i] - (pc - P[i - g.XY]);
+}
+
+// max |div u| over projectable cells.  Contains a block barrier.
+__device__ __forceinline__ void body_div_max(const Grid& g, const float* __restrict__ u,
+                                             const float* __restrict__ v, const float* __restrict__ w,
+                                             const uint8_t* __restrict__ flags, StepStatus* status,
+                                             uint3 bid) {
+    const int x = 1 + (int)bid.x * SB_BX + (int)threadIdx.x;
+    const int y = 1 + (int)bid.y * SB_BY + (int)threadIdx.y;
+    const int z = 1 + (int)bid.z;
+    float m = 0.0f;
+    if (x <= g.nx - 2 && y <= g.ny - 2 && z <= g.nz - 2) {
+        const int i = g.idx(x, y, z);
+        if (flags[i] & F_PROJ) {
+            const float div = -u[i] + u[i + 1] + -v[i] + v[i + g.X] + -w[i] + w[i + g.XY];
+            m = fabsf(div);
+        }
+    }
+    block_max_to(__float_as_uint(m), &status->div_bits);
+}
+
+// ---- advection --------------------------------------------------------------------------------
+
+// velocityAdvectionU/V/W (smokeSimulation.cu:527-615), the three fused per staggered index.
+__device__ __forceinline__ void body_advect_velocity(const Grid& g, const float* __restrict__ u0,
+                                                     const float* __restrict__ v0,
+                                                     const float* __restrict__ w0, float* __restrict__ u1,
+                                                     float* __restrict__ v1, float* __restrict__ w1,
+                                                     const uint8_t* __restrict__ flags, float dt,
+                                                     uint3 bid) {
+    const int x = 1 + (int)bid.x * SB_BX + (int)threadIdx.x;
+    const int y = 1 + (int)bid.y * SB_BY + (int)threadIdx.y;
+    const int z = 1 + (int)bid.z;
+    if (x >= g.nx || y >= g.ny || z >= g.nz) return;
+    const int i = g.idx(x, y, z);
+    const uint8_t f = flags[i];
+    if (!(f & F_SELF)) return;
+    const bool inx = x <= g.nx - 2, iny = y <= g.ny - 2, inz = z <= g.nz - 2;
+    if (iny && inz && (f & F_XM)) {
+        float xt = (float)x, yt = (float)y + 0.5f, zt = (float)z + 0.5f;
+        const float uu = u0[i];
+        const float vv = avgV(v0, g, i);
+        const float ww = avgW(w0, g, i);
+        xt = xt - dt * uu;
+        yt = yt - dt * vv;
+        zt = zt - dt * ww;
+        u1[i] = sample_ref(u0, g, xt, yt, zt, 0.0f, 0.5f, 0.5f);
+    }
+    if (inx && inz && (f & F_YM)) {
+        float xt = (float)x + 0.5f, yt = (float)y, zt = (float)z + 0.5f;
+        const float uu = avgU(u0, g, i);
+        const float vv = v0[i];
+        const float ww = avgW(w0, g, i);
+        xt = xt - dt * uu;
+        yt = yt - dt * vv;
+        zt = zt - dt * ww;
+        v1[i] = sample_ref(v0, g, xt, yt, zt, 0.5f, 0.0f, 0.5f);
+    }
+    if (inx && iny && (f & F_ZM)) {
+        float xt = (float)x + 0.5f, yt = (float)y + 0.5f, zt = (float)z;
+        const float uu = avgU(u0, g, i);
+        const float vv = avgV(v0, g, i);
+        const float ww = w0[i];
+        xt = xt - dt * uu;
+        yt = yt - dt * vv;
+        zt = zt - dt * ww;
+        w1[i] = sample_ref(w0, g, xt, yt, zt, 0.5f, 0.5f, 0.0f);
+    }
+}
+
+// advectSmoke (smokeSimulation.cu:617-638) with the NEW velocities.  The reference evaluates
+// the backtrace x + 0.5 - u*dt in double and rounds to float.  With a = x + 0.5 (exact, lowest
+// bit 2^-1) and b = u*dt (a float), the exact a - b needs at most max(e_a - e_b, 0) + 24 bits,
+// so it is exact in double unless |b| < a*2^-29; then a - b lies strictly inside a's float
+// rounding interval, in double too.  Either way float(double(a) - double(b)) equals the single-
+// rounded float subtraction, which avoids GB300's slow FP64 pipe (golden-vector tests pin it).
+__device__ __forceinline__ void body_advect_density(const Grid& g, const float* __restrict__ r0,
+                                                    float* __restrict__ r1, const float* __restrict__ u,
+                                                    const float* __restrict__ v,
+                                                    const float* __restrict__ w,
+                                                    const uint8_t* __restrict__ flags, float dt,
+                                                    uint3 bid) {
+    const int x = 1 + (int)bid.x * SB_BX + (int)threadIdx.x;
+    const int y = 1 + (int)bid.y * SB_BY + (int)threadIdx.y;
+    const int z = 1 + (int)bid.z;
+    if (x > g.nx - 2 || y > g.ny - 2 || z > g.nz - 2) return;
+    const int i = g.idx(x, y, z);
+    if (!(flags[i] & F_SELF)) return;
+    const float ut = (u[i] + u[i + 1]) / 2.0f;
+    const float vt = (v[i] + v[i + g.X]) / 2.0f;
+    const float wt = (w[i] + w[i + g.XY]) / 2.0f;
+    const float xt = __fsub_rn((float)x + 0.5f, ut * dt);
+    const float yt = __fsub_rn((float)y + 0.5f, vt * dt);
+    const float zt = __fsub_rn((float)z + 0.5f, wt * dt);
+    r1[i] = sample_ref(r0, g, xt, yt, zt, 0.5f, 0.5f, 0.5f);
+}
+
+}  // namespace smk
