@@ -34,7 +34,7 @@ extern "C" {
 
 /* Projection schemes. */
 #define SMK_PROJECT_REFERENCE 0 /* in-place velocity red-black SOR, bit-exact with the reference */
-#define SMK_PROJECT_PRESSURE 1  /* pressure red-black SOR, gradient subtract fused at the end */
+#define SMK_PROJECT_PRESSURE 1  /* pressure red-black SOR on P, then one pass subtracting grad P */
 
 /* Velocity clamp modes. */
 #define SMK_CLAMP_REFERENCE 0 /* if |u|^2*dt > c^2 scale by c^2/(|u|^2*dt) (smokeSimulation.cu:343-349) */
@@ -43,7 +43,8 @@ extern "C" {
 
 /* Storage precision of the advected fields (u, v, w, density). */
 #define SMK_STORAGE_F32 0
-#define SMK_STORAGE_BF16 1
+#define SMK_STORAGE_BF16 1     /* density and u, v, w in BF16 (FP32 arithmetic, FP32 pressure) */
+#define SMK_STORAGE_BF16_VEL 2 /* u, v, w in BF16, density in FP32 */
 
 typedef struct smk_sim smk_sim;
 

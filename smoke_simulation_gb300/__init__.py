@@ -20,7 +20,7 @@ SMK_OK = 0
 PROJECT_REFERENCE = 0
 PROJECT_PRESSURE = 1
 CLAMP_REFERENCE, CLAMP_MAGNITUDE, CLAMP_NONE = 0, 1, 2
-STORAGE_F32, STORAGE_BF16 = 0, 1
+STORAGE_F32, STORAGE_BF16, STORAGE_BF16_VEL = 0, 1, 2
 
 
 class SmokeError(RuntimeError):

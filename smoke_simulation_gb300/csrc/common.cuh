@@ -12,6 +12,7 @@
 // The whole library is compiled with -fmad=false so that every float expression rounds
 // exactly as written (no contraction); fused multiply-adds appear only as explicit fmaf().
 #pragma once
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -73,31 +74,43 @@ __device__ __forceinline__ void block_max_to(unsigned v, unsigned* dst) {
     }
 }
 
+// ---- storage types ----------------------------------------------------------------------------
+// Fields are stored as float (FP32 form) or bf16 (BF16 storage form); arithmetic is FP32 in
+// both.  ldv/stv are the only places a stored value is converted.
+__device__ __forceinline__ float ldv(const float* __restrict__ p, int i) { return p[i]; }
+__device__ __forceinline__ float ldv(const __nv_bfloat16* __restrict__ p, int i) { return __bfloat162float(p[i]); }
+__device__ __forceinline__ void stv(float* __restrict__ p, int i, float v) { p[i] = v; }
+__device__ __forceinline__ void stv(__nv_bfloat16* __restrict__ p, int i, float v) { p[i] = __float2bfloat16_rn(v); }
+
 // ---- reference-exact helpers ---------------------------------------------------------------
 
 // avgU/avgV/avgW (smokeSimulation.cu:409-447): 8-point sums in the reference's order, / 8.
-__device__ __forceinline__ float avgU(const float* __restrict__ f, const Grid& g, int i) {
+template <typename T>
+__device__ __forceinline__ float avgU(const T* __restrict__ f, const Grid& g, int i) {
     const int X = g.X, XY = g.XY;
-    float s = f[i - XY] + f[i + 1 - XY] + f[i - X - XY] + f[i + 1 - X - XY] + f[i] + f[i + 1] +
-              f[i - X] + f[i + 1 - X];
+    float s = ldv(f, i - XY) + ldv(f, i + 1 - XY) + ldv(f, i - X - XY) + ldv(f, i + 1 - X - XY) + ldv(f, i) +
+              ldv(f, i + 1) + ldv(f, i - X) + ldv(f, i + 1 - X);
     return s / 8.0f;
 }
-__device__ __forceinline__ float avgV(const float* __restrict__ f, const Grid& g, int i) {
+template <typename T>
+__device__ __forceinline__ float avgV(const T* __restrict__ f, const Grid& g, int i) {
     const int X = g.X, XY = g.XY;
-    float s = f[i - XY] + f[i - 1 - XY] + f[i + X - XY] + f[i - 1 + X - XY] + f[i] + f[i - 1] +
-              f[i + X] + f[i - 1 + X];
+    float s = ldv(f, i - XY) + ldv(f, i - 1 - XY) + ldv(f, i + X - XY) + ldv(f, i - 1 + X - XY) + ldv(f, i) +
+              ldv(f, i - 1) + ldv(f, i + X) + ldv(f, i - 1 + X);
     return s / 8.0f;
 }
-__device__ __forceinline__ float avgW(const float* __restrict__ f, const Grid& g, int i) {
+template <typename T>
+__device__ __forceinline__ float avgW(const T* __restrict__ f, const Grid& g, int i) {
     const int X = g.X, XY = g.XY;
-    float s = f[i] + f[i - 1] + f[i - X] + f[i - 1 - X] + f[i - XY] + f[i - 1 - XY] + f[i - X - XY] +
-              f[i - 1 - X - XY];
+    float s = ldv(f, i) + ldv(f, i - 1) + ldv(f, i - X) + ldv(f, i - 1 - X) + ldv(f, i - XY) + ldv(f, i - 1 - XY) +
+              ldv(f, i - X - XY) + ldv(f, i - 1 - X - XY);
     return s / 8.0f;
 }
 
 // sampleSmoke (smokeSimulation.cu:451-484): clamp the position to [1, n-1] with the CELL
 // dims, trilinear weights from (c - delta) - i0, eight terms summed in the reference order.
-__device__ __forceinline__ float sample_ref(const float* __restrict__ f, const Grid& g, float px,
+template <typename T>
+__device__ __forceinline__ float sample_ref(const T* __restrict__ f, const Grid& g, float px,
                                            float py, float pz, float dx, float dy, float dz) {
     const float mx = (float)(unsigned)(g.nx - 1), my = (float)(unsigned)(g.ny - 1),
                 mz = (float)(unsigned)(g.nz - 1);
@@ -119,10 +132,10 @@ __device__ __forceinline__ float sample_ref(const float* __restrict__ f, const G
     const int X = g.X, XY = g.XY;
     const int r00 = y0 * X + z0 * XY, r10 = y1 * X + z0 * XY, r01 = y0 * X + z1 * XY,
               r11 = y1 * X + z1 * XY;
-    return xw0 * yw0 * zw0 * f[x0 + r00] + xw1 * yw0 * zw0 * f[x1 + r00] +
-           xw0 * yw1 * zw0 * f[x0 + r10] + xw1 * yw1 * zw0 * f[x1 + r10] +
-           xw0 * yw0 * zw1 * f[x0 + r01] + xw1 * yw0 * zw1 * f[x1 + r01] +
-           xw0 * yw1 * zw1 * f[x0 + r11] + xw1 * yw1 * zw1 * f[x1 + r11];
+    return xw0 * yw0 * zw0 * ldv(f, x0 + r00) + xw1 * yw0 * zw0 * ldv(f, x1 + r00) +
+           xw0 * yw1 * zw0 * ldv(f, x0 + r10) + xw1 * yw1 * zw0 * ldv(f, x1 + r10) +
+           xw0 * yw0 * zw1 * ldv(f, x0 + r01) + xw1 * yw0 * zw1 * ldv(f, x1 + r01) +
+           xw0 * yw1 * zw1 * ldv(f, x0 + r11) + xw1 * yw1 * zw1 * ldv(f, x1 + r11);
 }
 
 }  // namespace smk

@@ -8,16 +8,20 @@
 namespace smk {
 
 // Stage a4: emitters and obstacles.
-void launch_emit_boxes(const Grid& g, float* rho0, float* rho1, float* v_now, const BoxObj* boxes,
-                       int nb, cudaStream_t st);
-void launch_fill_smoke(const Grid& g, float* rho0, float* rho1, const SphereObj* sp, int ns,
+// Storage-typed launchers are instantiated for float (FP32 form) and __nv_bfloat16 (BF16
+// storage form); arithmetic is FP32 in both.
+template <typename T, typename Tv>
+void launch_emit_boxes(const Grid& g, T* rho0, T* rho1, Tv* v_now, const BoxObj* boxes, int nb,
                        cudaStream_t st);
+template <typename T>
+void launch_fill_smoke(const Grid& g, T* rho0, T* rho1, const SphereObj* sp, int ns, cudaStream_t st);
 void launch_fill_obstacles(const Grid& g, uint8_t* s, const ObstacleObj* ob, int no, cudaStream_t st);
 // Neighbour flags from the mask; zeroes the pressure where a cell is not projectable.
 void launch_build_flags(const Grid& g, const uint8_t* s, uint8_t* flags, float* P, cudaStream_t st);
 
 // Stage b: integrate (forcing) + velocityConfinement (clamp), fused.
-void launch_forcing(const Grid& g, float* u, float* v, float* w, const float* rho,
+template <typename Tv, typename T>
+void launch_forcing(const Grid& g, Tv* u, Tv* v, Tv* w, const T* rho,
                     const uint8_t* flags, float dt, float gravity, float buoyancy, float clamp_const,
                     int clamp_mode, cudaStream_t st);
 
@@ -26,7 +30,8 @@ void launch_project_velocity(const Grid& g, float* u, float* v, float* w, const 
                              int colour, double omega, cudaStream_t st);
 
 // Stage c/d (pressure scheme).
-void launch_rhs(const Grid& g, const float* u, const float* v, const float* w, const uint8_t* flags,
+template <typename T>
+void launch_rhs(const Grid& g, const T* u, const T* v, const T* w, const uint8_t* flags,
                 float* b, float* P, const float* P2, const int* pcur, int warm, cudaStream_t st);
 void launch_sweep(const Grid& g, float* P, const float* b, const uint8_t* flags, int colour,
                   const float* wacc7, const StepStatus* status, cudaStream_t st);
@@ -52,11 +57,17 @@ void launch_div_max(const Grid& g, const float* u, const float* v, const float* 
                     const uint8_t* flags, StepStatus* status, cudaStream_t st);
 
 // Stage a: advection.
-void launch_advect_velocity(const Grid& g, const float* u0, const float* v0, const float* w0,
-                            float* u1, float* v1, float* w1, const uint8_t* flags, float dt,
-                            cudaStream_t st);
-void launch_advect_density(const Grid& g, const float* r0, float* r1, const float* u1,
-                           const float* v1, const float* w1, const uint8_t* flags, float dt,
-                           cudaStream_t st);
+template <typename Ti, typename To>
+void launch_advect_velocity(const Grid& g, const Ti* u0, const Ti* v0, const Ti* w0, To* u1, To* v1,
+                            To* w1, const uint8_t* flags, float dt, cudaStream_t st);
+template <typename T, typename Tv>
+void launch_advect_density(const Grid& g, const T* r0, T* r1, const Tv* u1, const Tv* v1, const Tv* w1,
+                           const uint8_t* flags, float dt, cudaStream_t st);
+// BF16 storage form: the projection written in FP32 over every face, and rounded into the state.
+void launch_project_bf16(const Grid& g, __nv_bfloat16* u, __nv_bfloat16* v, __nv_bfloat16* w,
+                         const float* P0, const float* P1, const int* pcur, const uint8_t* flags,
+                         float* pu, float* pv, float* pw, cudaStream_t st);
+void launch_convert(const __nv_bfloat16* src, float* dst, size_t n, cudaStream_t st);
+void launch_convert(const float* src, __nv_bfloat16* dst, size_t n, cudaStream_t st);
 
 }  // namespace smk

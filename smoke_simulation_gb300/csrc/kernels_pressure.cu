@@ -25,8 +25,9 @@ inline dim3 grid3(int rx, int ry, int rz) {
     return dim3((unsigned)((rx + BX - 1) / BX), (unsigned)((ry + BY - 1) / BY), (unsigned)rz);
 }
 
-__global__ void k_rhs(Grid g, const float* __restrict__ u, const float* __restrict__ v,
-                      const float* __restrict__ w, const uint8_t* __restrict__ flags,
+template <typename T>
+__global__ void k_rhs(Grid g, const T* __restrict__ u, const T* __restrict__ v,
+                      const T* __restrict__ w, const uint8_t* __restrict__ flags,
                       float* __restrict__ b, float* __restrict__ P, const float* __restrict__ P2,
                       const int* __restrict__ pcur, int warm) {
     body_rhs(g, u, v, w, flags, b, P, P2, pcur, warm, blockIdx);
@@ -53,10 +54,16 @@ __global__ void k_gradient_subtract(Grid g, float* __restrict__ u, float* __rest
 
 }  // namespace
 
-void launch_rhs(const Grid& g, const float* u, const float* v, const float* w, const uint8_t* flags,
+template <typename T>
+void launch_rhs(const Grid& g, const T* u, const T* v, const T* w, const uint8_t* flags,
                 float* b, float* P, const float* P2, const int* pcur, int warm, cudaStream_t st) {
     k_rhs<<<grid3(g.nx, g.ny, g.nz), dim3(BX, BY), 0, st>>>(g, u, v, w, flags, b, P, P2, pcur, warm);
 }
+template void launch_rhs<float>(const Grid&, const float*, const float*, const float*, const uint8_t*, float*,
+                                float*, const float*, const int*, int, cudaStream_t);
+template void launch_rhs<__nv_bfloat16>(const Grid&, const __nv_bfloat16*, const __nv_bfloat16*,
+                                        const __nv_bfloat16*, const uint8_t*, float*, float*, const float*,
+                                        const int*, int, cudaStream_t);
 
 void launch_sweep(const Grid& g, float* P, const float* b, const uint8_t* flags, int colour,
                   const float* wacc7, const StepStatus* status, cudaStream_t st) {

@@ -29,13 +29,15 @@ struct BoxList { int n; BoxObj b[MAX_OBJ_PER_LAUNCH]; };
 
 // ---- a4: emitters and obstacles ---------------------------------------------------------------
 
-__global__ void k_emit_boxes(Grid g, float* __restrict__ rho0, float* __restrict__ rho1,
-                             float* __restrict__ v_now, const __grid_constant__ BoxList L, int x0,
+template <typename T, typename Tv>
+__global__ void k_emit_boxes(Grid g, T* __restrict__ rho0, T* __restrict__ rho1,
+                             Tv* __restrict__ v_now, const __grid_constant__ BoxList L, int x0,
                              int y0, int z0, int x1, int y1, int z1) {
     body_emit_boxes(g, rho0, rho1, v_now, L.b, L.n, x0, y0, z0, x1, y1, z1, blockIdx);
 }
 
-__global__ void k_fill_smoke(Grid g, float* __restrict__ rho0, float* __restrict__ rho1,
+template <typename T>
+__global__ void k_fill_smoke(Grid g, T* __restrict__ rho0, T* __restrict__ rho1,
                              const __grid_constant__ SphereList L, int x0, int y0, int z0, int x1,
                              int y1, int z1) {
     body_fill_smoke(g, rho0, rho1, L.s, L.n, x0, y0, z0, x1, y1, z1, blockIdx);
@@ -78,8 +80,9 @@ __global__ void k_build_flags(Grid g, const uint8_t* __restrict__ s, uint8_t* __
 }
 
 // ---- b: integrate (smokeSimulation.cu:315-329) + velocityConfinement (:331-352) ------------
-__global__ void k_forcing(Grid g, float* __restrict__ u, float* __restrict__ v, float* __restrict__ w,
-                          const float* __restrict__ rho, const uint8_t* __restrict__ flags, float dt,
+template <typename Tv, typename T>
+__global__ void k_forcing(Grid g, Tv* __restrict__ u, Tv* __restrict__ v, Tv* __restrict__ w,
+                          const T* __restrict__ rho, const uint8_t* __restrict__ flags, float dt,
                           float gravity, float alpha, float lim_sq, float lim, int clamp_mode) {
     body_forcing(g, u, v, w, rho, flags, dt, gravity, alpha, lim_sq, lim, clamp_mode, blockIdx);
 }
@@ -115,18 +118,38 @@ __global__ void k_project_velocity(Grid g, float* __restrict__ u, float* __restr
 }
 
 // ---- a: velocityAdvectionU/V/W (:527-615) and advectSmoke (:617-638) ------------------------
-__global__ void k_advect_velocity(Grid g, const float* __restrict__ u0, const float* __restrict__ v0,
-                                  const float* __restrict__ w0, float* __restrict__ u1,
-                                  float* __restrict__ v1, float* __restrict__ w1,
+template <typename Ti, typename To>
+__global__ void k_advect_velocity(Grid g, const Ti* __restrict__ u0, const Ti* __restrict__ v0,
+                                  const Ti* __restrict__ w0, To* __restrict__ u1,
+                                  To* __restrict__ v1, To* __restrict__ w1,
                                   const uint8_t* __restrict__ flags, float dt) {
     body_advect_velocity(g, u0, v0, w0, u1, v1, w1, flags, dt, blockIdx);
 }
 
-__global__ void k_advect_density(Grid g, const float* __restrict__ r0, float* __restrict__ r1,
-                                 const float* __restrict__ u, const float* __restrict__ v,
-                                 const float* __restrict__ w, const uint8_t* __restrict__ flags,
+template <typename T, typename Tv>
+__global__ void k_advect_density(Grid g, const T* __restrict__ r0, T* __restrict__ r1,
+                                 const Tv* __restrict__ u, const Tv* __restrict__ v,
+                                 const Tv* __restrict__ w, const uint8_t* __restrict__ flags,
                                  float dt) {
     body_advect_density(g, r0, r1, u, v, w, flags, dt, blockIdx);
+}
+
+__global__ void k_project_bf16(Grid g, __nv_bfloat16* __restrict__ u, __nv_bfloat16* __restrict__ v,
+                               __nv_bfloat16* __restrict__ w, const float* __restrict__ P0,
+                               const float* __restrict__ P1, const int* __restrict__ pcur,
+                               const uint8_t* __restrict__ flags, float* __restrict__ pu,
+                               float* __restrict__ pv, float* __restrict__ pw) {
+    body_project_bf16(g, u, v, w, P0, P1, pcur, flags, pu, pv, pw, blockIdx);
+}
+
+__global__ void k_bf16_to_f32(const __nv_bfloat16* __restrict__ a, float* __restrict__ b, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        b[i] = __bfloat162float(a[i]);
+}
+
+__global__ void k_f32_to_bf16(const float* __restrict__ a, __nv_bfloat16* __restrict__ b, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        b[i] = __float2bfloat16_rn(a[i]);
 }
 
 // max |div u| over projectable cells (post-projection diagnostic).
@@ -140,7 +163,8 @@ __global__ void k_div_max(Grid g, const float* __restrict__ u, const float* __re
 
 // ---- launchers ------------------------------------------------------------------------------
 
-void launch_emit_boxes(const Grid& g, float* rho0, float* rho1, float* v_now, const BoxObj* boxes,
+template <typename T, typename Tv>
+void launch_emit_boxes(const Grid& g, T* rho0, T* rho1, Tv* v_now, const BoxObj* boxes,
                        int nb, cudaStream_t st) {
     for (int base = 0; base < nb; base += MAX_OBJ_PER_LAUNCH) {
         BoxList L;
@@ -186,7 +210,8 @@ bool sphere_bounds(const Grid& g, const SphereObj* sp, int ns, int a0[3], int a1
     return true;
 }
 
-void launch_fill_smoke(const Grid& g, float* rho0, float* rho1, const SphereObj* sp, int ns,
+template <typename T>
+void launch_fill_smoke(const Grid& g, T* rho0, T* rho1, const SphereObj* sp, int ns,
                        cudaStream_t st) {
     for (int base = 0; base < ns; base += MAX_OBJ_PER_LAUNCH) {
         SphereList L;
@@ -212,7 +237,8 @@ void launch_build_flags(const Grid& g, const uint8_t* s, uint8_t* flags, float* 
     k_build_flags<<<grid3(g.nx, g.ny, g.nz), dim3(BX, BY), 0, st>>>(g, s, flags, P);
 }
 
-void launch_forcing(const Grid& g, float* u, float* v, float* w, const float* rho,
+template <typename Tv, typename T>
+void launch_forcing(const Grid& g, Tv* u, Tv* v, Tv* w, const T* rho,
                     const uint8_t* flags, float dt, float gravity, float buoyancy, float clamp_const,
                     int clamp_mode, cudaStream_t st) {
     if (g.ny < 2) return;
@@ -229,16 +255,18 @@ void launch_project_velocity(const Grid& g, float* u, float* v, float* w, const 
                                                                                  colour, omega);
 }
 
-void launch_advect_velocity(const Grid& g, const float* u0, const float* v0, const float* w0,
-                            float* u1, float* v1, float* w1, const uint8_t* flags, float dt,
+template <typename Ti, typename To>
+void launch_advect_velocity(const Grid& g, const Ti* u0, const Ti* v0, const Ti* w0,
+                            To* u1, To* v1, To* w1, const uint8_t* flags, float dt,
                             cudaStream_t st) {
     if (g.nx < 2 || g.ny < 2 || g.nz < 2) return;
     k_advect_velocity<<<grid3(g.nx - 1, g.ny - 1, g.nz - 1), dim3(BX, BY), 0, st>>>(
         g, u0, v0, w0, u1, v1, w1, flags, dt);
 }
 
-void launch_advect_density(const Grid& g, const float* r0, float* r1, const float* u1,
-                           const float* v1, const float* w1, const uint8_t* flags, float dt,
+template <typename T, typename Tv>
+void launch_advect_density(const Grid& g, const T* r0, T* r1, const Tv* u1,
+                           const Tv* v1, const Tv* w1, const uint8_t* flags, float dt,
                            cudaStream_t st) {
     if (g.nx < 3 || g.ny < 3 || g.nz < 3) return;
     k_advect_density<<<grid3(g.nx - 2, g.ny - 2, g.nz - 2), dim3(BX, BY), 0, st>>>(g, r0, r1, u1, v1,
@@ -250,5 +278,55 @@ void launch_div_max(const Grid& g, const float* u, const float* v, const float* 
     if (g.nx < 3 || g.ny < 3 || g.nz < 3) return;
     k_div_max<<<grid3(g.nx - 2, g.ny - 2, g.nz - 2), dim3(BX, BY), 0, st>>>(g, u, v, w, flags, status);
 }
+
+void launch_project_bf16(const Grid& g, __nv_bfloat16* u, __nv_bfloat16* v, __nv_bfloat16* w,
+                         const float* P0, const float* P1, const int* pcur, const uint8_t* flags,
+                         float* pu, float* pv, float* pw, cudaStream_t st) {
+    k_project_bf16<<<grid3(g.nx + 1, g.ny + 1, g.nz + 1), dim3(BX, BY), 0, st>>>(g, u, v, w, P0, P1, pcur,
+                                                                               flags, pu, pv, pw);
+}
+
+void launch_convert(const __nv_bfloat16* src, float* dst, size_t n, cudaStream_t st) {
+    k_bf16_to_f32<<<(unsigned)((n + 255) / 256 < 65536 ? (n + 255) / 256 : 65536), 256, 0, st>>>(src, dst, n);
+}
+
+void launch_convert(const float* src, __nv_bfloat16* dst, size_t n, cudaStream_t st) {
+    k_f32_to_bf16<<<(unsigned)((n + 255) / 256 < 65536 ? (n + 255) / 256 : 65536), 256, 0, st>>>(src, dst, n);
+}
+
+// explicit instantiations: FP32 storage and BF16 storage
+template void launch_emit_boxes<float, float>(const Grid&, float*, float*, float*, const BoxObj*, int,
+                                              cudaStream_t);
+template void launch_emit_boxes<__nv_bfloat16, __nv_bfloat16>(const Grid&, __nv_bfloat16*, __nv_bfloat16*,
+                                                              __nv_bfloat16*, const BoxObj*, int, cudaStream_t);
+template void launch_emit_boxes<float, __nv_bfloat16>(const Grid&, float*, float*, __nv_bfloat16*,
+                                                      const BoxObj*, int, cudaStream_t);
+template void launch_fill_smoke<float>(const Grid&, float*, float*, const SphereObj*, int, cudaStream_t);
+template void launch_fill_smoke<__nv_bfloat16>(const Grid&, __nv_bfloat16*, __nv_bfloat16*, const SphereObj*,
+                                               int, cudaStream_t);
+template void launch_forcing<float, float>(const Grid&, float*, float*, float*, const float*, const uint8_t*,
+                                           float, float, float, float, int, cudaStream_t);
+template void launch_forcing<__nv_bfloat16, __nv_bfloat16>(const Grid&, __nv_bfloat16*, __nv_bfloat16*,
+                                                           __nv_bfloat16*, const __nv_bfloat16*, const uint8_t*,
+                                                           float, float, float, float, int, cudaStream_t);
+template void launch_forcing<__nv_bfloat16, float>(const Grid&, __nv_bfloat16*, __nv_bfloat16*, __nv_bfloat16*,
+                                                   const float*, const uint8_t*, float, float, float, float, int,
+                                                   cudaStream_t);
+template void launch_advect_velocity<float, float>(const Grid&, const float*, const float*, const float*,
+                                                   float*, float*, float*, const uint8_t*, float, cudaStream_t);
+template void launch_advect_velocity<float, __nv_bfloat16>(const Grid&, const float*, const float*,
+                                                           const float*, __nv_bfloat16*, __nv_bfloat16*,
+                                                           __nv_bfloat16*, const uint8_t*, float, cudaStream_t);
+template void launch_advect_density<float, float>(const Grid&, const float*, float*, const float*,
+                                                  const float*, const float*, const uint8_t*, float,
+                                                  cudaStream_t);
+template void launch_advect_density<float, __nv_bfloat16>(const Grid&, const float*, float*,
+                                                          const __nv_bfloat16*, const __nv_bfloat16*,
+                                                          const __nv_bfloat16*, const uint8_t*, float,
+                                                          cudaStream_t);
+template void launch_advect_density<__nv_bfloat16, __nv_bfloat16>(const Grid&, const __nv_bfloat16*,
+                                                                  __nv_bfloat16*, const __nv_bfloat16*,
+                                                                  const __nv_bfloat16*, const __nv_bfloat16*,
+                                                                  const uint8_t*, float, cudaStream_t);
 
 }  // namespace smk

@@ -24,6 +24,9 @@ namespace {
 
 thread_local std::string g_last_error;
 
+// A stored field as BF16 (the allocation is 2 bytes per element in the BF16 storage form).
+inline __nv_bfloat16* bf(float* p) { return reinterpret_cast<__nv_bfloat16*>(p); }
+
 int fail(int code, const std::string& msg) {
     g_last_error = msg;
     return code;
@@ -59,9 +62,9 @@ int check_params(const smk_params* p) {
     if (p->max_sweeps < 0 || p->max_sweeps > 1000000) return fail(SMK_ERR_INVALID, "max_sweeps out of range");
     if (p->projection == SMK_PROJECT_PRESSURE && p->tol > 0 && p->check_every <= 0)
         return fail(SMK_ERR_INVALID, "check_every must be positive when tol > 0");
-    if (p->storage != SMK_STORAGE_F32 && p->storage != SMK_STORAGE_BF16)
+    if (p->storage != SMK_STORAGE_F32 && p->storage != SMK_STORAGE_BF16 && p->storage != SMK_STORAGE_BF16_VEL)
         return fail(SMK_ERR_INVALID, "unknown storage precision");
-    if (p->storage == SMK_STORAGE_BF16 && p->projection == SMK_PROJECT_REFERENCE)
+    if (p->storage != SMK_STORAGE_F32 && p->projection == SMK_PROJECT_REFERENCE)
         return fail(SMK_ERR_INVALID, "BF16 storage needs the pressure projection");
     if (p->projection == SMK_PROJECT_PRESSURE && p->tol > 0 &&
         (p->max_sweeps + p->check_every - 1) / p->check_every > 4000)
@@ -86,10 +89,32 @@ cudaMemcpy3DParms copy3d(void* dst, size_t dpitch, size_t dy, const void* src, s
 
 int smk_sim::alloc() {
     const size_t n = elems();
-    float** fl[] = {&rho[0], &rho[1], &u[0], &u[1], &v[0], &v[1], &w[0], &w[1], &P, &P2, &b};
+    bf16 = p.storage == SMK_STORAGE_BF16 || p.storage == SMK_STORAGE_BF16_VEL;
+    rho_bf16 = p.storage == SMK_STORAGE_BF16;
+    // advected fields: 4 bytes (FP32) or 2 bytes (BF16 storage) per element; the solver's
+    // pressure and right-hand side are FP32 in every form
+    float** vfields[] = {&u[0], &u[1], &v[0], &v[1], &w[0], &w[1]};
+    for (float** f : vfields) {
+        SMK_CUDA(cudaMalloc((void**)f, n * (bf16 ? 2 : 4)));
+        SMK_CUDA(cudaMemset(*f, 0, n * (bf16 ? 2 : 4)));
+    }
+    float** rfields[] = {&rho[0], &rho[1]};
+    for (float** f : rfields) {
+        SMK_CUDA(cudaMalloc((void**)f, n * (rho_bf16 ? 2 : 4)));
+        SMK_CUDA(cudaMemset(*f, 0, n * (rho_bf16 ? 2 : 4)));
+    }
+    float** fl[] = {&P, &P2, &b};
     for (float** f : fl) {
         SMK_CUDA(cudaMalloc((void**)f, n * sizeof(float)));
         SMK_CUDA(cudaMemset(*f, 0, n * sizeof(float)));
+    }
+    if (bf16) {
+        // FP32 projected velocity (what advection consumes); scratch for conversions between steps
+        float** pr[] = {&proj[0], &proj[1], &proj[2]};
+        for (float** f : pr) {
+            SMK_CUDA(cudaMalloc((void**)f, n * sizeof(float)));
+            SMK_CUDA(cudaMemset(*f, 0, n * sizeof(float)));
+        }
     }
     SMK_CUDA(cudaMalloc((void**)&pcur, 2 * sizeof(int)));
     SMK_CUDA(cudaMemset(pcur, 0, 2 * sizeof(int)));
@@ -115,7 +140,7 @@ int smk_sim::alloc() {
 }
 
 void smk_sim::release() {
-    float* fl[] = {rho[0], rho[1], u[0], u[1], v[0], v[1], w[0], w[1], P, P2, b};
+    float* fl[] = {rho[0], rho[1], u[0], u[1], v[0], v[1], w[0], w[1], P, P2, b, proj[0], proj[1], proj[2]};
     for (float* f : fl)
         if (f) cudaFree(f);
     if (pcur) cudaFree(pcur);
@@ -157,11 +182,14 @@ int smk_sim::enqueue(float dt, cudaStream_t st) {
         else obstacles.push_back(o.obstacle);
     }
     if (!boxes.empty()) {
-        launch_emit_boxes(g, rho[0], rho[1], v[now], boxes.data(), (int)boxes.size(), st);
+        if (rho_bf16) launch_emit_boxes(g, bf(rho[0]), bf(rho[1]), bf(v[now]), boxes.data(), (int)boxes.size(), st);
+        else if (bf16) launch_emit_boxes(g, rho[0], rho[1], bf(v[now]), boxes.data(), (int)boxes.size(), st);
+        else launch_emit_boxes(g, rho[0], rho[1], v[now], boxes.data(), (int)boxes.size(), st);
         ++launches;
     }
     if (!spheres.empty()) {
-        launch_fill_smoke(g, rho[0], rho[1], spheres.data(), (int)spheres.size(), st);
+        if (rho_bf16) launch_fill_smoke(g, bf(rho[0]), bf(rho[1]), spheres.data(), (int)spheres.size(), st);
+        else launch_fill_smoke(g, rho[0], rho[1], spheres.data(), (int)spheres.size(), st);
         ++launches;
     }
     if (!obstacles.empty() && (obstacles_dirty || mask_dirty)) {
@@ -178,8 +206,15 @@ int smk_sim::enqueue(float dt, cudaStream_t st) {
     if (timed) SMK_CUDA(cudaEventRecord(ev[1], st));
 
     // b: integrate + velocityConfinement (:789-791)
-    launch_forcing(g, u[now], v[now], w[now], rho[now], flags, dt, p.gravity, p.buoyancy,
-                   p.clamp_const, p.clamp_mode, st);
+    if (rho_bf16)
+        launch_forcing(g, bf(u[now]), bf(v[now]), bf(w[now]), (const __nv_bfloat16*)bf(rho[now]), flags, dt,
+                       p.gravity, p.buoyancy, p.clamp_const, p.clamp_mode, st);
+    else if (bf16)
+        launch_forcing(g, bf(u[now]), bf(v[now]), bf(w[now]), (const float*)rho[now], flags, dt, p.gravity,
+                       p.buoyancy, p.clamp_const, p.clamp_mode, st);
+    else
+        launch_forcing(g, u[now], v[now], w[now], (const float*)rho[now], flags, dt, p.gravity, p.buoyancy,
+                       p.clamp_const, p.clamp_mode, st);
     ++launches;
     if (timed) SMK_CUDA(cudaEventRecord(ev[2], st));
 
@@ -197,7 +232,12 @@ int smk_sim::enqueue(float dt, cudaStream_t st) {
         float wacc[7];
         wacc[0] = 0.0f;
         for (int a = 1; a <= 6; ++a) wacc[a] = (float)p.omega / (float)a;
-        launch_rhs(g, u[now], v[now], w[now], flags, b, P, P2, pcur, p.warm_start, st);
+        if (bf16)
+            launch_rhs(g, (const __nv_bfloat16*)bf(u[now]), (const __nv_bfloat16*)bf(v[now]),
+                       (const __nv_bfloat16*)bf(w[now]), flags, b, P, P2, pcur, p.warm_start, st);
+        else
+            launch_rhs(g, (const float*)u[now], (const float*)v[now], (const float*)w[now], flags, b, P, P2,
+                       pcur, p.warm_start, st);
         ++launches;
         const bool use_tol = p.tol > 0.0f;
         const int G = use_tol ? p.check_every : (p.max_sweeps > 0 ? p.max_sweeps : 1);
@@ -243,18 +283,39 @@ int smk_sim::enqueue(float dt, cudaStream_t st) {
         if (timed) SMK_CUDA(cudaEventRecord(ev[6], st));
         const bool tb_used = sweep_depth > 0 && p.max_sweeps > 0;
         if (!tb_used) SMK_CUDA(cudaMemsetAsync(pcur, 0, sizeof(int), st));
-        launch_gradient_subtract(g, u[now], v[now], w[now], P, P2, pcur, flags, st);
+        if (bf16)
+            launch_project_bf16(g, bf(u[now]), bf(v[now]), bf(w[now]), P, P2, pcur, flags, proj[0], proj[1],
+                                proj[2], st);
+        else
+            launch_gradient_subtract(g, u[now], v[now], w[now], P, P2, pcur, flags, st);
         ++launches;
     }
+    // the projected velocity advection consumes: the state itself (FP32) or its FP32 copy
+    const float* pu = bf16 ? proj[0] : u[now];
+    const float* pv = bf16 ? proj[1] : v[now];
+    const float* pw = bf16 ? proj[2] : w[now];
     if (p.report_div) {
-        launch_div_max(g, u[now], v[now], w[now], flags, status, st);
+        launch_div_max(g, pu, pv, pw, flags, status, st);
         ++launches;
     }
     if (timed) SMK_CUDA(cudaEventRecord(ev[3], st));
 
     // a: advection (:805-810)
-    launch_advect_velocity(g, u[now], v[now], w[now], u[past], v[past], w[past], flags, dt, st);
-    launch_advect_density(g, rho[now], rho[past], u[past], v[past], w[past], flags, dt, st);
+    if (bf16) {
+        launch_advect_velocity(g, pu, pv, pw, bf(u[past]), bf(v[past]), bf(w[past]), flags, dt, st);
+        if (rho_bf16)
+            launch_advect_density(g, (const __nv_bfloat16*)bf(rho[now]), bf(rho[past]),
+                                  (const __nv_bfloat16*)bf(u[past]), (const __nv_bfloat16*)bf(v[past]),
+                                  (const __nv_bfloat16*)bf(w[past]), flags, dt, st);
+        else
+            launch_advect_density(g, (const float*)rho[now], rho[past], (const __nv_bfloat16*)bf(u[past]),
+                                  (const __nv_bfloat16*)bf(v[past]), (const __nv_bfloat16*)bf(w[past]),
+                                  flags, dt, st);
+    } else {
+        launch_advect_velocity(g, pu, pv, pw, u[past], v[past], w[past], flags, dt, st);
+        launch_advect_density(g, (const float*)rho[now], rho[past], (const float*)u[past],
+                              (const float*)v[past], (const float*)w[past], flags, dt, st);
+    }
     launches += 2;
     if (timed) SMK_CUDA(cudaEventRecord(ev[4], st));
     SMK_CUDA(cudaGetLastError());
@@ -406,8 +467,24 @@ int smk_set_params(smk_sim* sim, const smk_params* params) {
     if (!sim) return fail(SMK_ERR_INVALID, "sim is null");
     int rc = check_params(params);
     if (rc) return rc;
+    if (params->storage != sim->p.storage)
+        return fail(SMK_ERR_INVALID, "the storage precision is fixed when the simulation is created");
     sim->p = *params;
     return SMK_OK;
+}
+
+// FP32 view of a stored field for a device-to-host/device copy: the field itself, or (BF16
+// storage) its conversion into the projection scratch buffer, stream-ordered on `st`.
+static const float* fp32_source(smk_sim* sim, const float* field, bool is_bf16, cudaStream_t st) {
+    if (!is_bf16) return field;
+    launch_convert(reinterpret_cast<const __nv_bfloat16*>(field), sim->proj[0], sim->elems(), st);
+    return sim->proj[0];
+}
+// Where a host-to-device copy of a field lands (the field, or the scratch for BF16), and the
+// conversion that completes it.
+static float* fp32_target(smk_sim* sim, float* field, bool is_bf16) { return is_bf16 ? sim->proj[0] : field; }
+static void fp32_commit(smk_sim* sim, float* field, bool is_bf16, cudaStream_t st) {
+    if (is_bf16) launch_convert(sim->proj[0], reinterpret_cast<__nv_bfloat16*>(field), sim->elems(), st);
 }
 
 int smk_get_params(const smk_sim* sim, smk_params* params) {
@@ -428,9 +505,12 @@ int smk_set_density(smk_sim* sim, const float* host_rho) {
     if (!sim || !host_rho) return fail(SMK_ERR_INVALID, "null argument");
     DeviceGuard dg(sim->device);
     const Grid& g = sim->g;
-    auto m = copy3d(sim->rho[0], (size_t)g.X * 4, g.ny + 1, host_rho, (size_t)g.nx * 4, g.ny,
+    if (sim->rho_bf16) SMK_CUDA(cudaMemset(sim->proj[0], 0, sim->elems() * sizeof(float)));
+    auto m = copy3d(fp32_target(sim, sim->rho[0], sim->rho_bf16), (size_t)g.X * 4, g.ny + 1, host_rho, (size_t)g.nx * 4, g.ny,
                     (size_t)g.nx * 4, g.ny, g.nz, cudaMemcpyHostToDevice);
     SMK_CUDA(cudaMemcpy3D(&m));
+    fp32_commit(sim, sim->rho[0], sim->rho_bf16, nullptr);
+    SMK_CUDA(cudaDeviceSynchronize());
     return SMK_OK;
 }
 
@@ -506,7 +586,7 @@ int smk_read_density(smk_sim* sim, float* dst, int dst_on_device, void* stream) 
     if (!sim || !dst) return fail(SMK_ERR_INVALID, "null argument");
     DeviceGuard dg(sim->device);
     const Grid& g = sim->g;
-    const float* src = sim->rho[sim->index_now ^ 1];
+    const float* src = fp32_source(sim, sim->rho[sim->index_now ^ 1], sim->rho_bf16, (cudaStream_t)stream);
     auto m = copy3d(dst, (size_t)g.nx * 4, g.ny, src, (size_t)g.X * 4, g.ny + 1, (size_t)g.nx * 4, g.ny,
                     g.nz, dst_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost);
     SMK_CUDA(cudaMemcpy3DAsync(&m, (cudaStream_t)stream));
@@ -555,23 +635,31 @@ static int state_copy(smk_sim* sim, const smk_host_state* st, bool to_device) {
         float* host_f[3] = {st->u[k], st->v[k], st->w[k]};
         for (int j = 0; j < 1; ++j) {
             if (!host_c[j]) continue;
+            if (to_device && sim->rho_bf16) SMK_CUDA(cudaMemset(sim->proj[0], 0, sim->elems() * sizeof(float)));
             cudaMemcpy3DParms m =
-                to_device ? copy3d(dev_c[j], (size_t)g.X * 4, g.ny + 1, host_c[j], (size_t)g.nx * 4, g.ny,
-                                   (size_t)g.nx * 4, g.ny, g.nz, cudaMemcpyHostToDevice)
-                          : copy3d(host_c[j], (size_t)g.nx * 4, g.ny, dev_c[j], (size_t)g.X * 4, g.ny + 1,
-                                   (size_t)g.nx * 4, g.ny, g.nz, cudaMemcpyDeviceToHost);
+                to_device ? copy3d(fp32_target(sim, dev_c[j], sim->rho_bf16), (size_t)g.X * 4, g.ny + 1,
+                                   host_c[j], (size_t)g.nx * 4, g.ny, (size_t)g.nx * 4, g.ny, g.nz,
+                                   cudaMemcpyHostToDevice)
+                          : copy3d(host_c[j], (size_t)g.nx * 4, g.ny,
+                                   fp32_source(sim, dev_c[j], sim->rho_bf16, nullptr),
+                                   (size_t)g.X * 4, g.ny + 1, (size_t)g.nx * 4, g.ny, g.nz,
+                                   cudaMemcpyDeviceToHost);
             SMK_CUDA(cudaMemcpy3D(&m));
+            if (to_device) fp32_commit(sim, dev_c[j], sim->rho_bf16, nullptr);
         }
         for (int j = 0; j < 3; ++j) {
             if (!host_f[j]) continue;
             size_t wb = (size_t)(g.nx + 1) * 4;
+            if (to_device && sim->bf16) SMK_CUDA(cudaMemset(sim->proj[0], 0, sim->elems() * sizeof(float)));
             cudaMemcpy3DParms m =
-                to_device ? copy3d(dev_f[j], (size_t)g.X * 4, g.ny + 1, host_f[j], wb, g.ny + 1, wb,
-                                   g.ny + 1, g.nz + 1, cudaMemcpyHostToDevice)
-                          : copy3d(host_f[j], wb, g.ny + 1, dev_f[j], (size_t)g.X * 4, g.ny + 1, wb,
-                                   g.ny + 1, g.nz + 1, cudaMemcpyDeviceToHost);
+                to_device ? copy3d(fp32_target(sim, dev_f[j], sim->bf16), (size_t)g.X * 4, g.ny + 1, host_f[j],
+                                   wb, g.ny + 1, wb, g.ny + 1, g.nz + 1, cudaMemcpyHostToDevice)
+                          : copy3d(host_f[j], wb, g.ny + 1, fp32_source(sim, dev_f[j], sim->bf16, nullptr),
+                                   (size_t)g.X * 4, g.ny + 1, wb, g.ny + 1, g.nz + 1, cudaMemcpyDeviceToHost);
             SMK_CUDA(cudaMemcpy3D(&m));
+            if (to_device) fp32_commit(sim, dev_f[j], sim->bf16, nullptr);
         }
+        SMK_CUDA(cudaDeviceSynchronize());
     }
     if (st->s) {
         if (to_device) {

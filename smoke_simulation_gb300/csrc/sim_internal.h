@@ -30,6 +30,11 @@ struct smk_sim {
     float* u[2] = {nullptr, nullptr};
     float* v[2] = {nullptr, nullptr};
     float* w[2] = {nullptr, nullptr};
+    // With BF16 storage (bf16 == true) rho/u/v/w point to __nv_bfloat16 arrays, and proj[]
+    // holds the FP32 projected velocity advection consumes (scratch between steps).
+    bool bf16 = false;      // u, v, w stored in BF16 (both BF16 storage forms)
+    bool rho_bf16 = false;  // density stored in BF16 (SMK_STORAGE_BF16)
+    float* proj[3] = {nullptr, nullptr, nullptr};
     float* P = nullptr;
     float* P2 = nullptr;  // second pressure buffer (temporally blocked sweeps ping-pong)
     float* b = nullptr;

@@ -20,8 +20,9 @@ struct WAcc { float w[8]; };
 // ---- emitters ---------------------------------------------------------------------------------
 
 // Box emitters restricted to [x0,x1)x[y0,..)x[z0,..): density into both buffers, optional v.
-__device__ __forceinline__ void body_emit_boxes(const Grid& g, float* __restrict__ rho0,
-                                                float* __restrict__ rho1, float* __restrict__ v_now,
+template <typename T, typename Tv>
+__device__ __forceinline__ void body_emit_boxes(const Grid& g, T* __restrict__ rho0,
+                                                T* __restrict__ rho1, Tv* __restrict__ v_now,
                                                 const BoxObj* boxes, int nb, int x0, int y0, int z0,
                                                 int x1, int y1, int z1, uint3 bid) {
     const int x = x0 + (int)bid.x * SB_BX + (int)threadIdx.x;
@@ -32,11 +33,11 @@ __device__ __forceinline__ void body_emit_boxes(const Grid& g, float* __restrict
         const BoxObj& b = boxes[k];
         if (x >= b.x0 && x < b.x1 && y >= b.y0 && y < b.y1 && z >= b.z0 && z < b.z1) {
             const int i = g.idx(x, y, z);
-            rho0[i] = b.density;
-            rho1[i] = b.density;
+            stv(rho0, i, b.density);
+            stv(rho1, i, b.density);
             if (b.set_vy) {
-                v_now[i] = b.vy;
-                v_now[i + g.X] = b.vy;
+                stv(v_now, i, b.vy);
+                stv(v_now, i + g.X, b.vy);
             }
         }
     }
@@ -44,8 +45,9 @@ __device__ __forceinline__ void body_emit_boxes(const Grid& g, float* __restrict
 
 // fillSmoke (smokeSimulation.cu:251-273) over the box [x0,x1)x[y0,y1)x[z0,z1) (within the
 // interior): float squared distance from the integer corner, strict test, both buffers = 1.
-__device__ __forceinline__ void body_fill_smoke(const Grid& g, float* __restrict__ rho0,
-                                                float* __restrict__ rho1, const SphereObj* sp, int ns,
+template <typename T>
+__device__ __forceinline__ void body_fill_smoke(const Grid& g, T* __restrict__ rho0,
+                                                T* __restrict__ rho1, const SphereObj* sp, int ns,
                                                 int x0, int y0, int z0, int x1, int y1, int z1,
                                                 uint3 bid) {
     const int x = x0 + (int)bid.x * SB_BX + (int)threadIdx.x;
@@ -57,15 +59,16 @@ __device__ __forceinline__ void body_fill_smoke(const Grid& g, float* __restrict
         const float dist = dx * dx + dy * dy + dz * dz;
         if (dist < sp[k].r * sp[k].r) {
             const int i = g.idx(x, y, z);
-            rho0[i] = 1.0f;
-            rho1[i] = 1.0f;
+            stv(rho0, i, 1.0f);
+            stv(rho1, i, 1.0f);
         }
     }
 }
 
 // ---- forcing: integrate (smokeSimulation.cu:315-329) + velocityConfinement (:331-352) -------
-__device__ __forceinline__ void body_forcing(const Grid& g, float* __restrict__ u, float* __restrict__ v,
-                                             float* __restrict__ w, const float* __restrict__ rho,
+template <typename Tv, typename T>
+__device__ __forceinline__ void body_forcing(const Grid& g, Tv* __restrict__ u, Tv* __restrict__ v,
+                                             Tv* __restrict__ w, const T* __restrict__ rho,
                                              const uint8_t* __restrict__ flags, float dt, float gravity,
                                              float alpha, float lim_sq, float lim, int clamp_mode,
                                              uint3 bid) {
@@ -75,30 +78,30 @@ __device__ __forceinline__ void body_forcing(const Grid& g, float* __restrict__ 
     if (x >= g.nx || y >= g.ny || z >= g.nz) return;
     const int i = g.idx(x, y, z);
     const uint8_t f = flags[i];
-    float vt = v[i];
+    float vt = ldv(v, i);
     if ((f & F_SELF) && (f & F_YM)) {
-        const float r = rho[i];
+        const float r = ldv(rho, i);
         const float buoy = alpha * (r - 0.0f);
         vt = vt + (r * gravity * dt + buoy * dt);
-        if (!(x >= 1 && z >= 1 && clamp_mode != 2)) v[i] = vt;
+        if (!(x >= 1 && z >= 1 && clamp_mode != 2)) stv(v, i, vt);
     }
     if (x >= 1 && z >= 1 && clamp_mode != 2) {
-        const float ut = u[i], wt = w[i];
+        const float ut = ldv(u, i), wt = ldv(w, i);
         const float len = ut * ut + vt * vt + wt * wt;
         if (clamp_mode == 0) {
             if (len * dt > lim_sq) {
                 const float s = lim_sq / (len * dt);
-                u[i] = ut * s;
+                stv(u, i, ut * s);
                 vt = vt * s;
-                w[i] = wt * s;
+                stv(w, i, wt * s);
             }
         } else if (len > lim * lim) {
             const float s = lim / sqrtf(len);
-            u[i] = ut * s;
+            stv(u, i, ut * s);
             vt = vt * s;
-            w[i] = wt * s;
+            stv(w, i, wt * s);
         }
-        v[i] = vt;
+        stv(v, i, vt);
     }
 }
 
@@ -106,8 +109,9 @@ __device__ __forceinline__ void body_forcing(const Grid& g, float* __restrict__ 
 
 // b = -div(u*) on projectable cells; P = 0 off them (and everywhere on a cold start); on a warm
 // start whose previous solve ended in the second buffer (*pcur == 1) P is taken from there.
-__device__ __forceinline__ void body_rhs(const Grid& g, const float* __restrict__ u,
-                                         const float* __restrict__ v, const float* __restrict__ w,
+template <typename T>
+__device__ __forceinline__ void body_rhs(const Grid& g, const T* __restrict__ u,
+                                         const T* __restrict__ v, const T* __restrict__ w,
                                          const uint8_t* __restrict__ flags, float* __restrict__ b,
                                          float* __restrict__ P, const float* __restrict__ P2,
                                          const int* __restrict__ pcur, int warm, uint3 bid) {
@@ -117,7 +121,8 @@ __device__ __forceinline__ void body_rhs(const Grid& g, const float* __restrict_
     if (x >= g.nx || y >= g.ny || z >= g.nz) return;
     const int i = g.idx(x, y, z);
     if (flags[i] & F_PROJ) {
-        const float div = -u[i] + u[i + 1] + -v[i] + v[i + g.X] + -w[i] + w[i + g.XY];
+        const float div = -ldv(u, i) + ldv(u, i + 1) + -ldv(v, i) + ldv(v, i + g.X) + -ldv(w, i) +
+                          ldv(w, i + g.XY);
         b[i] = -div;
         if (!warm) P[i] = 0.0f;
         else if (pcur != nullptr && P2 != nullptr && *pcur == 1) P[i] = P2[i];
@@ -221,13 +226,48 @@ __device__ __forceinline__ void body_div_max(const Grid& g, const float* __restr
     block_max_to(__float_as_uint(m), &status->div_bits);
 }
 
+// BF16 storage form: the projected velocity is written in FP32 to (pu, pv, pw) over every face
+// (advection reads it there, and max|div u| is measured there), and rounded into the BF16
+// state where the gradient changed it, so the state holds the projected velocity as in the
+// FP32 form.  Storing only the rounded value would leave a divergence of order 1e-2 |u|.
+__device__ __forceinline__ void body_project_bf16(const Grid& g, __nv_bfloat16* __restrict__ u,
+                                                  __nv_bfloat16* __restrict__ v,
+                                                  __nv_bfloat16* __restrict__ w,
+                                                  const float* __restrict__ P0, const float* __restrict__ P1,
+                                                  const int* __restrict__ pcur,
+                                                  const uint8_t* __restrict__ flags, float* __restrict__ pu,
+                                                  float* __restrict__ pv, float* __restrict__ pw, uint3 bid) {
+    const float* __restrict__ P = (pcur != nullptr && *pcur == 1) ? P1 : P0;
+    const int x = (int)bid.x * SB_BX + (int)threadIdx.x;
+    const int y = (int)bid.y * SB_BY + (int)threadIdx.y;
+    const int z = (int)bid.z;
+    if (x > g.nx || y > g.ny || z > g.nz) return;
+    const int i = g.idx(x, y, z);
+    float uu = ldv(u, i), vv = ldv(v, i), ww = ldv(w, i);
+    const bool cell = x < g.nx && y < g.ny && z < g.nz && x >= 1 && y >= 1 && z >= 1;
+    if (cell) {
+        const uint8_t f = flags[i];
+        if (f & F_SELF) {
+            const bool inx = x <= g.nx - 2, iny = y <= g.ny - 2, inz = z <= g.nz - 2;
+            const float pc = P[i];
+            if (iny && inz && (f & F_XM)) { uu = uu - (pc - P[i - 1]); stv(u, i, uu); }
+            if (inx && inz && (f & F_YM)) { vv = vv - (pc - P[i - g.X]); stv(v, i, vv); }
+            if (inx && iny && (f & F_ZM)) { ww = ww - (pc - P[i - g.XY]); stv(w, i, ww); }
+        }
+    }
+    pu[i] = uu;
+    pv[i] = vv;
+    pw[i] = ww;
+}
+
 // ---- advection --------------------------------------------------------------------------------
 
 // velocityAdvectionU/V/W (smokeSimulation.cu:527-615), the three fused per staggered index.
-__device__ __forceinline__ void body_advect_velocity(const Grid& g, const float* __restrict__ u0,
-                                                     const float* __restrict__ v0,
-                                                     const float* __restrict__ w0, float* __restrict__ u1,
-                                                     float* __restrict__ v1, float* __restrict__ w1,
+template <typename Ti, typename To>
+__device__ __forceinline__ void body_advect_velocity(const Grid& g, const Ti* __restrict__ u0,
+                                                     const Ti* __restrict__ v0,
+                                                     const Ti* __restrict__ w0, To* __restrict__ u1,
+                                                     To* __restrict__ v1, To* __restrict__ w1,
                                                      const uint8_t* __restrict__ flags, float dt,
                                                      uint3 bid) {
     const int x = 1 + (int)bid.x * SB_BX + (int)threadIdx.x;
@@ -240,33 +280,33 @@ __device__ __forceinline__ void body_advect_velocity(const Grid& g, const float*
     const bool inx = x <= g.nx - 2, iny = y <= g.ny - 2, inz = z <= g.nz - 2;
     if (iny && inz && (f & F_XM)) {
         float xt = (float)x, yt = (float)y + 0.5f, zt = (float)z + 0.5f;
-        const float uu = u0[i];
+        const float uu = ldv(u0, i);
         const float vv = avgV(v0, g, i);
         const float ww = avgW(w0, g, i);
         xt = xt - dt * uu;
         yt = yt - dt * vv;
         zt = zt - dt * ww;
-        u1[i] = sample_ref(u0, g, xt, yt, zt, 0.0f, 0.5f, 0.5f);
+        stv(u1, i, sample_ref(u0, g, xt, yt, zt, 0.0f, 0.5f, 0.5f));
     }
     if (inx && inz && (f & F_YM)) {
         float xt = (float)x + 0.5f, yt = (float)y, zt = (float)z + 0.5f;
         const float uu = avgU(u0, g, i);
-        const float vv = v0[i];
+        const float vv = ldv(v0, i);
         const float ww = avgW(w0, g, i);
         xt = xt - dt * uu;
         yt = yt - dt * vv;
         zt = zt - dt * ww;
-        v1[i] = sample_ref(v0, g, xt, yt, zt, 0.5f, 0.0f, 0.5f);
+        stv(v1, i, sample_ref(v0, g, xt, yt, zt, 0.5f, 0.0f, 0.5f));
     }
     if (inx && iny && (f & F_ZM)) {
         float xt = (float)x + 0.5f, yt = (float)y + 0.5f, zt = (float)z;
         const float uu = avgU(u0, g, i);
         const float vv = avgV(v0, g, i);
-        const float ww = w0[i];
+        const float ww = ldv(w0, i);
         xt = xt - dt * uu;
         yt = yt - dt * vv;
         zt = zt - dt * ww;
-        w1[i] = sample_ref(w0, g, xt, yt, zt, 0.5f, 0.5f, 0.0f);
+        stv(w1, i, sample_ref(w0, g, xt, yt, zt, 0.5f, 0.5f, 0.0f));
     }
 }
 
@@ -276,10 +316,11 @@ __device__ __forceinline__ void body_advect_velocity(const Grid& g, const float*
 // so it is exact in double unless |b| < a*2^-29; then a - b lies strictly inside a's float
 // rounding interval, in double too.  Either way float(double(a) - double(b)) equals the single-
 // rounded float subtraction, which avoids GB300's slow FP64 pipe (golden-vector tests pin it).
-__device__ __forceinline__ void body_advect_density(const Grid& g, const float* __restrict__ r0,
-                                                    float* __restrict__ r1, const float* __restrict__ u,
-                                                    const float* __restrict__ v,
-                                                    const float* __restrict__ w,
+template <typename T, typename Tv>
+__device__ __forceinline__ void body_advect_density(const Grid& g, const T* __restrict__ r0,
+                                                    T* __restrict__ r1, const Tv* __restrict__ u,
+                                                    const Tv* __restrict__ v,
+                                                    const Tv* __restrict__ w,
                                                     const uint8_t* __restrict__ flags, float dt,
                                                     uint3 bid) {
     const int x = 1 + (int)bid.x * SB_BX + (int)threadIdx.x;
@@ -288,13 +329,13 @@ __device__ __forceinline__ void body_advect_density(const Grid& g, const float* 
     if (x > g.nx - 2 || y > g.ny - 2 || z > g.nz - 2) return;
     const int i = g.idx(x, y, z);
     if (!(flags[i] & F_SELF)) return;
-    const float ut = (u[i] + u[i + 1]) / 2.0f;
-    const float vt = (v[i] + v[i + g.X]) / 2.0f;
-    const float wt = (w[i] + w[i + g.XY]) / 2.0f;
+    const float ut = (ldv(u, i) + ldv(u, i + 1)) / 2.0f;
+    const float vt = (ldv(v, i) + ldv(v, i + g.X)) / 2.0f;
+    const float wt = (ldv(w, i) + ldv(w, i + g.XY)) / 2.0f;
     const float xt = __fsub_rn((float)x + 0.5f, ut * dt);
     const float yt = __fsub_rn((float)y + 0.5f, vt * dt);
     const float zt = __fsub_rn((float)z + 0.5f, wt * dt);
-    r1[i] = sample_ref(r0, g, xt, yt, zt, 0.5f, 0.5f, 0.5f);
+    stv(r1, i, sample_ref(r0, g, xt, yt, zt, 0.5f, 0.5f, 0.5f));
 }
 
 }  // namespace smk
