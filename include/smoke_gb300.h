@@ -164,16 +164,41 @@ int smk_set_graphs(smk_sim* sim, int enable);
  * No counterpart in the reference. */
 int smk_autotune(smk_sim* sim, int* depth, int* zchunk, float* us_per_sweep);
 
-/* Batches: many independent grids stepped together.  A batch step is one CUDA graph launch in
- * which every member grid's full step is a concurrent branch (re-captured when a member's dt,
- * parameters, objects, sweep kernel or ping-pong parity changes).  Members keep their own state
- * and results (identical to stepping them alone); the batch does not own them.  No counterpart
- * in the reference (one implicit grid, smokeSimulation.cu:16-24). */
+/* Batches: many independent grids of any sizes stepped together.  Members keep their own state
+ * and results (identical to stepping them alone); the batch does not own them.  Two forms:
+ *   GROUPED   one persistent launch per stage over every member (emitters, forcing, the whole
+ *             projection as one cooperative kernel, velocity advection, density advection:
+ *             five launches per batch step whatever the number of grids), replayed as a
+ *             captured CUDA graph; needs the PRESSURE projection in every member;
+ *   BRANCHES  one CUDA graph whose concurrent branches are the members' own single-grid steps.
+ * AUTO (the default) takes GROUPED when every member allows it.  Graphs are re-captured when a
+ * member's dt, parameters, objects, sweep kernel or ping-pong parity changes; a step in which a
+ * member has a pending mask change or stage timing runs as BRANCHES without a graph.  No
+ * counterpart in the reference (one implicit grid, smokeSimulation.cu:16-24). */
+#define SMK_BATCH_AUTO 0
+#define SMK_BATCH_GROUPED 1
+#define SMK_BATCH_BRANCHES 2
 typedef struct smk_batch smk_batch;
 int smk_batch_create(int count, smk_sim* const* sims, smk_batch** out);
 /* dts: one dt per member, or NULL to use dt_all for every member.  Stream-ordered. */
 int smk_batch_step(smk_batch* batch, const float* dts, float dt_all, void* stream);
 int smk_batch_destroy(smk_batch* batch);
+int smk_batch_set_mode(smk_batch* batch, int mode);
+/* Replay batch steps as captured graphs (default on); off: direct launches. */
+int smk_batch_set_graphs(smk_batch* batch, int enable);
+/* The form the last step ran (SMK_BATCH_GROUPED or SMK_BATCH_BRANCHES; 0 before the first
+ * step) and the kernels the batch has launched so far (either pointer may be NULL). */
+int smk_batch_get_info(const smk_batch* batch, int* last_mode, long long* launches);
+/* Time the grouped projection kernel's schedules (CTAs per SM, z planes per tile, solve-wave
+ * budget) on the members' scratch pressure buffers and keep the fastest.  Synchronises; does
+ * not change any member's results.  Outputs may be NULL. */
+int smk_batch_autotune(smk_batch* batch, int* ctas_per_sm, float* us_per_sweep);
+/* The grouped projection's schedule: cooperative CTAs per SM (0: all resident), z planes per
+ * sweep tile, and the solve-wave budget in bytes of pressure + rhs + flags (0: one wave; else
+ * members are packed into waves solved one after another so a wave's passes stay in L2).
+ * Results do not depend on it. */
+int smk_batch_get_schedule(const smk_batch* batch, int* ctas_per_sm, int* zslab, long long* wave_bytes);
+int smk_batch_set_schedule(smk_batch* batch, int ctas_per_sm, int zslab, long long wave_bytes);
 
 /* Serving: many simulation requests kept resident on one GPU with continuous admission.  No
  * counterpart in the reference (one simulation stepped from the render loop, main.cpp:889-896).

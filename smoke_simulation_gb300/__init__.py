@@ -98,6 +98,12 @@ def lib() -> C.CDLL:
         "smk_batch_create": (i, [i, C.POINTER(vp), C.POINTER(vp)]),
         "smk_batch_step": (i, [vp, C.POINTER(f), f, vp]),
         "smk_batch_destroy": (i, [vp]),
+        "smk_batch_set_mode": (i, [vp, i]),
+        "smk_batch_set_graphs": (i, [vp, i]),
+        "smk_batch_get_info": (i, [vp, C.POINTER(i), C.POINTER(C.c_longlong)]),
+        "smk_batch_autotune": (i, [vp, C.POINTER(i), C.POINTER(f)]),
+        "smk_batch_get_schedule": (i, [vp, C.POINTER(i), C.POINTER(i), C.POINTER(C.c_longlong)]),
+        "smk_batch_set_schedule": (i, [vp, i, i, C.c_longlong]),
         "smk_project_noalloc_last_error": (C.c_char_p, []),
     }
     for name, (res, args) in sig.items():
@@ -292,15 +298,49 @@ class Simulation:
         return d.value, z.value
 
 
-class Batch:
-    """Many independent grids stepped as one CUDA graph launch (smk_batch_*).  The batch does
-    not own its members; keep the Simulation objects alive while the batch is in use."""
+BATCH_AUTO, BATCH_GROUPED, BATCH_BRANCHES = 0, 1, 2
 
-    def __init__(self, sims):
+
+class Batch:
+    """Many independent grids of any sizes stepped together (smk_batch_*): GROUPED runs one
+    persistent launch per stage over every member, BRANCHES one graph branch per member; AUTO
+    takes GROUPED when every member uses the PRESSURE projection.  The batch does not own its
+    members; keep the Simulation objects alive while the batch is in use."""
+
+    def __init__(self, sims, mode: int = BATCH_AUTO):
         self.sims = list(sims)
         arr = (C.c_void_p * len(self.sims))(*[s.h.value for s in self.sims])
         self.h = C.c_void_p()
         _check(lib().smk_batch_create(len(self.sims), arr, C.byref(self.h)))
+        if mode != BATCH_AUTO:
+            self.set_mode(mode)
+
+    def set_mode(self, mode: int):
+        _check(lib().smk_batch_set_mode(self.h, int(mode)))
+
+    def set_graphs(self, enable: bool):
+        _check(lib().smk_batch_set_graphs(self.h, 1 if enable else 0))
+
+    def info(self) -> tuple[int, int]:
+        """(form of the last step: BATCH_GROUPED / BATCH_BRANCHES, kernels launched so far)."""
+        m, n = C.c_int(), C.c_longlong()
+        _check(lib().smk_batch_get_info(self.h, C.byref(m), C.byref(n)))
+        return m.value, n.value
+
+    def autotune(self) -> tuple[int, float]:
+        """Tune the grouped projection's schedule; returns (ctas_per_sm, us_per_sweep)."""
+        c, us = C.c_int(), C.c_float()
+        _check(lib().smk_batch_autotune(self.h, C.byref(c), C.byref(us)))
+        return c.value, us.value
+
+    def schedule(self) -> tuple[int, int, int]:
+        """(cooperative CTAs per SM (0 = all resident), z planes per tile, solve-wave bytes)."""
+        c, z, w = C.c_int(), C.c_int(), C.c_longlong()
+        _check(lib().smk_batch_get_schedule(self.h, C.byref(c), C.byref(z), C.byref(w)))
+        return c.value, z.value, w.value
+
+    def set_schedule(self, ctas_per_sm: int, zslab: int, wave_bytes: int):
+        _check(lib().smk_batch_set_schedule(self.h, int(ctas_per_sm), int(zslab), int(wave_bytes)))
 
     def step(self, dt, stream: int = 0):
         """dt: one float for every member, or a sequence with one dt per member."""

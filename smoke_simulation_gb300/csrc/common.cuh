@@ -59,6 +59,8 @@ __device__ __forceinline__ void atomic_max_bits(unsigned* p, float nonneg) {
 // Max-reduce `v` (bit patterns of non-negative floats: the IEEE order, NaN largest) over the
 // block, then one atomicMax per block, skipped when the stored value is already larger.  One
 // atomic per warp on a single address serialises at L2 and costs ~1 ms on a 256^3 grid.
+// Every thread of the block must call it; it ends with a block barrier, so a persistent loop
+// may call it again without racing on the shared scratch.
 __device__ __forceinline__ void block_max_to(unsigned v, unsigned* dst) {
     __shared__ unsigned red[32];
     for (int o = 16; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(0xffffffffu, v, o));
@@ -72,6 +74,7 @@ __device__ __forceinline__ void block_max_to(unsigned v, unsigned* dst) {
         for (int o = 16; o > 0; o >>= 1) w = max(w, __shfl_xor_sync(0xffffffffu, w, o));
         if (lane == 0 && w > *(volatile unsigned*)dst) atomicMax(dst, w);
     }
+    __syncthreads();
 }
 
 // ---- storage types ----------------------------------------------------------------------------

@@ -15,6 +15,9 @@ void launch_emit_boxes(const Grid& g, T* rho0, T* rho1, Tv* v_now, const BoxObj*
                        cudaStream_t st);
 template <typename T>
 void launch_fill_smoke(const Grid& g, T* rho0, T* rho1, const SphereObj* sp, int ns, cudaStream_t st);
+// Union bounding box (one cell of margin) of spheres, clipped to the interior [1, n-2]:
+// [a0, a1) per axis; false when empty.
+bool sphere_bounds(const Grid& g, const SphereObj* sp, int ns, int a0[3], int a1[3]);
 void launch_fill_obstacles(const Grid& g, uint8_t* s, const ObstacleObj* ob, int no, cudaStream_t st);
 // Neighbour flags from the mask; zeroes the pressure where a cell is not projectable.
 void launch_build_flags(const Grid& g, const uint8_t* s, uint8_t* flags, float* P, cudaStream_t st);

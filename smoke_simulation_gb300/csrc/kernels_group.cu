@@ -1,0 +1,471 @@
+// Grouped kernels of a batch step: one persistent launch per stage over every grid (group.h).
+//
+//   k_group_objects     emitters (boxes, then spheres) of every grid
+//   k_group_forcing     integrate + clamp
+//   k_group_project     the whole projection as ONE cooperative kernel: b and the pressure
+//                       start, every red-black colour pass of every grid with the per-grid
+//                       tolerance rule, the gradient subtract (or the BF16 projection), and
+//                       max |div u|; phases are separated by a bounded grid barrier
+//   k_group_adv_vel     velocity advection
+//   k_group_adv_rho     density advection
+// The grid-stride kernels are sized to the resident CTAs of the device; every tile runs the
+// stage body of the single-grid kernel, so a grid's results are the same alone and batched.
+//
+// Tolerance rule (the single-grid sweep loop's): at the start of check group k (sweep k*G) a
+// grid whose residual recorded at the start of group k-1 is within tolerance is done; any other
+// grid records max |r| of its current pressure for group k and runs the group's passes.  Every
+// CTA makes the same decision from the same recorded residuals (written before a barrier), so
+// all CTAs agree on the set of active grids without further communication.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "common.cuh"
+#include "group.h"
+#include "stage_bodies.cuh"
+
+namespace smk {
+
+namespace {
+
+constexpr unsigned long long GROUP_WAIT_NS = 2000000000ull;  // a barrier wait gives up after 2 s
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ int tid256() { return (int)threadIdx.x + SB_BX * (int)threadIdx.y; }
+
+// Block index of tile `local` of a 64 x 4 block launch over an rx x ry x rz range.
+__device__ __forceinline__ uint3 tile_bid(int local, int rx, int ry) {
+    const int nbx = group_div_up(rx, SB_BX), nby = group_div_up(ry, SB_BY);
+    uint3 b;
+    b.x = (unsigned)(local % nbx);
+    b.y = (unsigned)((local / nbx) % nby);
+    b.z = (unsigned)(local / (nbx * nby));
+    return b;
+}
+
+// f(j, local) for every tile of `stage` this CTA owns (grid-stride over the batch's tiles).
+// With `mask` (shared memory, one byte per grid), grids whose byte has none of the bits
+// `need` are skipped as a whole.  j is uniform over the CTA, so f may contain block barriers.
+template <class F>
+__device__ __forceinline__ void for_tiles(const GroupArgs& a, int stage, const uint8_t* mask, int need, F&& f) {
+    const int* st = a.starts + stage * (a.n + 1);
+    const int total = st[a.n];
+    const int step = (int)gridDim.x;
+    int j = 0;
+    for (int t = (int)blockIdx.x; t < total; t += step) {
+        while (st[j + 1] <= t) ++j;
+        if (mask != nullptr && !(mask[j] & need)) {
+            const int end = st[j + 1];
+            t += ((end - t + step - 1) / step - 1) * step;  // the loop's += lands on the first t >= end
+            continue;
+        }
+        f(j, t - st[j]);
+    }
+}
+
+// ---- grid-stride stages ---------------------------------------------------------------------
+
+template <typename T, typename Tv>
+__device__ __forceinline__ void objects_cell(const GroupGrid& d, const GroupArgs& a, int x, int y, int z) {
+    if (x >= d.bx0 && x < d.bx1 && y >= d.by0 && y < d.by1 && z >= d.bz0 && z < d.bz1)
+        cell_emit_boxes(d.g, (T*)d.rho0, (T*)d.rho1, (Tv*)d.v_now, a.boxes + d.box0, d.nbox, x, y, z);
+    if (x >= d.sx0 && x < d.sx1 && y >= d.sy0 && y < d.sy1 && z >= d.sz0 && z < d.sz1)
+        cell_fill_smoke(d.g, (T*)d.rho0, (T*)d.rho1, a.spheres + d.sph0, d.nsph, x, y, z);
+}
+
+__global__ void __launch_bounds__(GROUP_TILE) k_group_objects(const GroupArgs a) {
+    for_tiles(a, GS_OBJECTS, nullptr, 0, [&](int j, int local) {
+        const GroupGrid& d = a.grids[j];
+        const uint3 bid = tile_bid(local, d.ox1 - d.ox0, d.oy1 - d.oy0);
+        const int x = d.ox0 + (int)bid.x * SB_BX + (int)threadIdx.x;
+        const int y = d.oy0 + (int)bid.y * SB_BY + (int)threadIdx.y;
+        const int z = d.oz0 + (int)bid.z;
+        if (x >= d.ox1 || y >= d.oy1 || z >= d.oz1) return;
+        if (d.kind == GK_BF16) objects_cell<__nv_bfloat16, __nv_bfloat16>(d, a, x, y, z);
+        else if (d.kind == GK_BF16_VEL) objects_cell<float, __nv_bfloat16>(d, a, x, y, z);
+        else objects_cell<float, float>(d, a, x, y, z);
+    });
+}
+
+__global__ void __launch_bounds__(GROUP_TILE) k_group_forcing(const GroupArgs a) {
+    for_tiles(a, GS_FORCE, nullptr, 0, [&](int j, int local) {
+        const GroupGrid& d = a.grids[j];
+        const uint3 bid = tile_bid(local, d.g.nx, d.g.ny - 1);
+        typedef __nv_bfloat16 h;
+        if (d.kind == GK_BF16)
+            body_forcing<h, h>(d.g, (h*)d.u_now, (h*)d.v_now, (h*)d.w_now, (const h*)d.rho_now, d.flags, d.dt,
+                               d.gravity, d.alpha, d.lim_sq, d.lim, d.clamp_mode, bid);
+        else if (d.kind == GK_BF16_VEL)
+            body_forcing<h, float>(d.g, (h*)d.u_now, (h*)d.v_now, (h*)d.w_now, (const float*)d.rho_now, d.flags,
+                                   d.dt, d.gravity, d.alpha, d.lim_sq, d.lim, d.clamp_mode, bid);
+        else
+            body_forcing<float, float>(d.g, (float*)d.u_now, (float*)d.v_now, (float*)d.w_now,
+                                       (const float*)d.rho_now, d.flags, d.dt, d.gravity, d.alpha, d.lim_sq,
+                                       d.lim, d.clamp_mode, bid);
+    });
+}
+
+__global__ void __launch_bounds__(GROUP_TILE) k_group_adv_vel(const GroupArgs a) {
+    for_tiles(a, GS_ADV_VEL, nullptr, 0, [&](int j, int local) {
+        const GroupGrid& d = a.grids[j];
+        const uint3 bid = tile_bid(local, d.g.nx - 1, d.g.ny - 1);
+        typedef __nv_bfloat16 h;
+        if (d.kind == GK_F32)
+            body_advect_velocity<float, float>(d.g, d.pu, d.pv, d.pw, (float*)d.u_past, (float*)d.v_past,
+                                               (float*)d.w_past, d.flags, d.dt, bid);
+        else
+            body_advect_velocity<float, h>(d.g, d.pu, d.pv, d.pw, (h*)d.u_past, (h*)d.v_past, (h*)d.w_past,
+                                           d.flags, d.dt, bid);
+    });
+}
+
+__global__ void __launch_bounds__(GROUP_TILE) k_group_adv_rho(const GroupArgs a) {
+    for_tiles(a, GS_ADV_RHO, nullptr, 0, [&](int j, int local) {
+        const GroupGrid& d = a.grids[j];
+        const uint3 bid = tile_bid(local, d.g.nx - 2, d.g.ny - 2);
+        typedef __nv_bfloat16 h;
+        if (d.kind == GK_BF16)
+            body_advect_density<h, h>(d.g, (const h*)d.rho_now, (h*)d.rho_past, (const h*)d.u_past,
+                                      (const h*)d.v_past, (const h*)d.w_past, d.flags, d.dt, bid);
+        else if (d.kind == GK_BF16_VEL)
+            body_advect_density<float, h>(d.g, (const float*)d.rho_now, (float*)d.rho_past, (const h*)d.u_past,
+                                          (const h*)d.v_past, (const h*)d.w_past, d.flags, d.dt, bid);
+        else
+            body_advect_density<float, float>(d.g, (const float*)d.rho_now, (float*)d.rho_past,
+                                              (const float*)d.u_past, (const float*)d.v_past,
+                                              (const float*)d.w_past, d.flags, d.dt, bid);
+    });
+}
+
+// ---- cooperative projection -----------------------------------------------------------------
+
+// Grid barrier over the cooperative launch (all CTAs co-resident).  Arrivals count up in one
+// 64-bit counter that is zeroed before the launch; a CTA waits for `target` = its barrier
+// number x gridDim.x.  The wait is bounded: after 2 s it raises `abort`, and a CTA that sees
+// `abort` leaves too.  Returns false when the kernel must stop.
+__device__ bool group_barrier(const GroupArgs& a, unsigned long long& target) {
+    __shared__ int ok_s;
+    __syncthreads();
+    target += gridDim.x;
+    if (tid256() == 0) {
+        __threadfence();
+        atomicAdd(&a.sync->count, 1ull);
+        int ok = 1;
+        const unsigned long long t0 = global_ns();
+        while (*(volatile unsigned long long*)&a.sync->count < target) {
+            if (*(volatile int*)&a.sync->abort) {
+                ok = 0;
+                break;
+            }
+            if (global_ns() - t0 > GROUP_WAIT_NS) {
+                atomicExch(&a.sync->abort, 1);
+                ok = 0;
+                break;
+            }
+            __nanosleep(32);
+        }
+        __threadfence();
+        ok_s = ok;
+    }
+    __syncthreads();
+    return ok_s != 0;
+}
+
+// A barrier gave up: flag every grid of the batch (the host reports it at the next sync).
+__device__ void group_abort(const GroupArgs& a) {
+    for (int j = tid256(); j < a.n; j += GROUP_TILE) atomicExch(a.grids[j].kerr, 1);
+}
+
+// Up to ZB cells of one same-colour (k, y) column of a colour pass: every load first, then the
+// updates.  Nothing a colour pass reads is written during the pass (it writes only cells of
+// its colour and reads the other colour's cells and the cell itself), so the loads of the ZB
+// cells are independent of the stores and can all be in flight at once.  Cell q sits in plane
+// z0 + q at x = xa + (par ^ (q & 1)); `count` cells are valid.  The arithmetic is cell_sweep's.
+constexpr int ZB = 4;
+__device__ __forceinline__ void sweep_column(const Grid& g, float* P, const float* b,
+                                             const uint8_t* __restrict__ flags, const float* wacc, int base,
+                                             int par, int xa, int count) {
+    float c[ZB], sum[ZB], bb[ZB];
+    int idx[ZB];
+    uint8_t f[ZB];
+#pragma unroll
+    for (int q = 0; q < ZB; ++q) {
+        const int pq = par ^ (q & 1);
+        idx[q] = base + q * g.XY + pq;
+        f[q] = 0;
+        if (q < count && xa + pq <= g.nx - 2) {
+            const int i = idx[q];
+            f[q] = flags[i];
+            sum[q] = ((P[i - 1] + P[i + 1]) + (P[i - g.X] + P[i + g.X])) + (P[i - g.XY] + P[i + g.XY]);
+            c[q] = P[i];
+            bb[q] = b[i];
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < ZB; ++q) {
+        if (f[q] & F_PROJ) {
+            const int acc = __popc((unsigned)(f[q] & F_NBRS));
+            const float r = fmaf(-(float)acc, c[q], bb[q] + sum[q]);
+            P[idx[q]] = fmaf(wacc[acc], r, c[q]);
+        }
+    }
+}
+
+// max |residual| bits over up to ZB cells of an interior column (cell_resid's expression).
+__device__ __forceinline__ unsigned resid_column(const Grid& g, const float* P, const float* b,
+                                                 const uint8_t* __restrict__ flags, int i0, int count) {
+    unsigned m = 0u;
+    float v[ZB];
+#pragma unroll
+    for (int q = 0; q < ZB; ++q) v[q] = q < count ? cell_resid(g, P, b, flags, i0 + q * g.XY) : 0.0f;
+#pragma unroll
+    for (int q = 0; q < ZB; ++q) m = max(m, __float_as_uint(v[q]));
+    return m;
+}
+
+// Per-grid byte of the active set (dynamic shared memory).
+enum : uint8_t { GA_DONE = 1, GA_SWEEP = 2, GA_CHECK = 4 };
+
+__global__ void __launch_bounds__(GROUP_TILE) k_group_project(const GroupArgs a) {
+    extern __shared__ uint8_t gst[];
+    const int tid = tid256();
+    unsigned long long target = 0;
+    for (int j = tid; j < a.n; j += GROUP_TILE) gst[j] = 0;
+
+    if (!a.sweeps_only) {
+        // this step's status words (zeroed by one CTA per grid), then b and the pressure start
+        for (int j = (int)blockIdx.x; j < a.n; j += (int)gridDim.x) {
+            unsigned* w = reinterpret_cast<unsigned*>(a.grids[j].status);
+            for (int k = tid; k < a.grids[j].status_words; k += GROUP_TILE) w[k] = 0u;
+        }
+        for_tiles(a, GS_RHS, nullptr, 0, [&](int j, int local) {
+            const GroupGrid& d = a.grids[j];
+            const uint3 bid = tile_bid(local, d.g.nx, d.g.ny);
+            if (d.kind == GK_F32)
+                body_rhs<float>(d.g, (const float*)d.u_now, (const float*)d.v_now, (const float*)d.w_now, d.flags,
+                                d.b, d.P, d.P2, d.pcur, d.warm, bid);
+            else
+                body_rhs<__nv_bfloat16>(d.g, (const __nv_bfloat16*)d.u_now, (const __nv_bfloat16*)d.v_now,
+                                        (const __nv_bfloat16*)d.w_now, d.flags, d.b, d.P, d.P2, d.pcur, d.warm,
+                                        bid);
+        });
+        if (!group_barrier(a, target)) {
+            group_abort(a);
+            return;
+        }
+        // the solve runs in place in P: the next step's warm start reads it there
+        if (blockIdx.x == 0)
+            for (int j = tid; j < a.n; j += GROUP_TILE) *a.grids[j].pcur = 0;
+    }
+
+    // the solve waves run one after another; inside a wave every grid runs its own colour
+    // passes and tolerance rule, pass by pass in lockstep with the wave's other grids
+    for (int wave = 0; wave < a.nwaves; ++wave)
+    for (int s = 0;; ++s) {
+        // which grids sweep now, and which record a residual first (group starts)
+        int act = 0, chk = 0;
+        for (int j = tid; j < a.n; j += GROUP_TILE) {
+            const GroupGrid& d = a.grids[j];
+            uint8_t m = gst[j] & GA_DONE;
+            if (!m && d.wave == wave && s < d.max_sweeps) {
+                bool check = false;
+                if (!a.sweeps_only && d.tol > 0.0f && s % d.check_every == 0) {
+                    const int k = s / d.check_every;
+                    if (k > 0 && __uint_as_float(*(volatile unsigned*)&d.status->rmax_bits[k - 1]) <= d.tol) {
+                        m = GA_DONE;
+                        if (blockIdx.x == 0) {
+                            d.status->done = 1;
+                            d.status->done_group = k;
+                        }
+                    } else {
+                        check = true;
+                    }
+                }
+                if (!m) m = check ? (GA_SWEEP | GA_CHECK) : GA_SWEEP;
+            }
+            gst[j] = m;
+            act |= m & GA_SWEEP;
+            chk |= m & GA_CHECK;
+        }
+        act = __syncthreads_or(act);
+        chk = __syncthreads_or(chk);
+        if (!act) break;
+
+        if (chk) {
+            int cur = -1;
+            unsigned mb = 0u;
+            auto flush = [&]() {
+                const GroupGrid& d = a.grids[cur];
+                block_max_to(mb, &d.status->rmax_bits[s / d.check_every]);
+            };
+            for_tiles(a, GS_RESID, gst, GA_CHECK, [&](int j, int local) {
+                if (j != cur) {
+                    if (cur >= 0) flush();
+                    cur = j;
+                    mb = 0u;
+                }
+                const GroupGrid& d = a.grids[j];
+                const Grid& g = d.g;
+                const int tpp = group_interior_tpp(g);
+                const int z0 = 1 + (local / tpp) * a.zslab;
+                const int z1 = min(z0 + a.zslab, g.nz - 1);
+                const int f = (local % tpp) * GROUP_TILE + tid;
+                const int L = g.nx - 2;
+                if (f < L * (g.ny - 2)) {
+                    int i = g.idx(1 + f % L, 1 + f / L, z0);
+                    for (int z = z0; z < z1; z += ZB, i += ZB * g.XY)
+                        mb = max(mb, resid_column(g, d.P, d.b, d.flags, i, z1 - z));
+                }
+            });
+            if (cur >= 0) flush();
+            if (!group_barrier(a, target)) {
+                group_abort(a);
+                return;
+            }
+        }
+
+        for (int colour = 0; colour < 2; ++colour) {
+            for_tiles(a, GS_SWEEP, gst, GA_SWEEP, [&](int j, int local) {
+                const GroupGrid& d = a.grids[j];
+                const Grid& g = d.g;
+                const int tpp = group_sweep_tpp(g);
+                const int z0 = 1 + (local / tpp) * a.zslab;
+                const int z1 = min(z0 + a.zslab, g.nz - 1);
+                const int f = (local % tpp) * GROUP_TILE + tid;
+                const int H = (g.nx - 1) / 2;  // same-colour cells per row (rounded up)
+                if (f < H * (g.ny - 2)) {
+                    const int y = 1 + f / H;
+                    // the colour's cell of this (k, y) column alternates between x and x +- 1 in z
+                    const int xa = 1 + 2 * (f % H);
+                    const int par = (1 + y + z0 + colour) & 1;  // ZB is even: same at every chunk start
+                    int base = g.idx(xa, y, z0);
+                    for (int z = z0; z < z1; z += ZB, base += ZB * g.XY)
+                        sweep_column(g, d.P, d.b, d.flags, d.wacc, base, par, xa, z1 - z);
+                }
+            });
+            if (!group_barrier(a, target)) {
+                group_abort(a);
+                return;
+            }
+        }
+    }
+    if (a.sweeps_only) return;
+
+    for_tiles(a, GS_PROJECT, nullptr, 0, [&](int j, int local) {
+        const GroupGrid& d = a.grids[j];
+        int rx, ry, rz;
+        group_extent(GS_PROJECT, d, rx, ry, rz);
+        const uint3 bid = tile_bid(local, rx, ry);
+        if (d.kind == GK_F32)
+            body_gradient_subtract(d.g, (float*)d.u_now, (float*)d.v_now, (float*)d.w_now, d.P, nullptr, nullptr,
+                                   d.flags, bid);
+        else
+            body_project_bf16(d.g, (__nv_bfloat16*)d.u_now, (__nv_bfloat16*)d.v_now, (__nv_bfloat16*)d.w_now,
+                              d.P, nullptr, nullptr, d.flags, d.pu, d.pv, d.pw, bid);
+    });
+
+    if (a.starts[GS_DIV * (a.n + 1) + a.n] > 0) {
+        if (!group_barrier(a, target)) {
+            group_abort(a);
+            return;
+        }
+        int cur = -1;
+        unsigned mb = 0u;
+        for_tiles(a, GS_DIV, nullptr, 0, [&](int j, int local) {
+            if (j != cur) {
+                if (cur >= 0) block_max_to(mb, &a.grids[cur].status->div_bits);
+                cur = j;
+                mb = 0u;
+            }
+            const GroupGrid& d = a.grids[j];
+            const Grid& g = d.g;
+            const int tpp = group_interior_tpp(g);
+            const int z0 = 1 + (local / tpp) * a.zslab;
+            const int z1 = min(z0 + a.zslab, g.nz - 1);
+            const int f = (local % tpp) * GROUP_TILE + tid;
+            const int L = g.nx - 2;
+            if (f < L * (g.ny - 2)) {
+                int i = g.idx(1 + f % L, 1 + f / L, z0);
+                for (int z = z0; z < z1; ++z, i += g.XY)
+                    mb = max(mb, __float_as_uint(cell_div(g, d.pu, d.pv, d.pw, d.flags, i)));
+            }
+        });
+        if (cur >= 0) block_max_to(mb, &a.grids[cur].status->div_bits);
+    }
+}
+
+int g_sms = 0;
+int g_occ[6] = {0, 0, 0, 0, 0, 0};  // resident CTAs per SM: project, objects, forcing, adv_vel, adv_rho
+
+int ensure_occupancy() {
+    if (g_sms > 0) return 0;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
+    const void* ks[5] = {(const void*)k_group_project, (const void*)k_group_objects, (const void*)k_group_forcing,
+                         (const void*)k_group_adv_vel, (const void*)k_group_adv_rho};
+    for (int k = 0; k < 5 && e == cudaSuccess; ++k)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&g_occ[k], ks[k], GROUP_TILE, k == 0 ? 16384 : 0);
+    if (e != cudaSuccess) {
+        g_sms = 0;
+        return (int)e;
+    }
+    return 0;
+}
+
+int launch_grid_stride(const void* kernel, int total, int occ, const GroupArgs& a, cudaStream_t st) {
+    if (total <= 0) return 0;
+    const int cap = occ * g_sms;
+    const int ctas = total < cap ? total : cap;
+    void* args[] = {(void*)&a};
+    return (int)cudaLaunchKernel(kernel, dim3((unsigned)ctas), dim3(SB_BX, SB_BY), args, 0, st);
+}
+
+int launch_project(const GroupArgs& a, const GroupLaunch& L, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(a.sync, 0, sizeof(GroupSync), st);
+    if (e != cudaSuccess) return (int)e;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)L.coop_ctas);
+    cfg.blockDim = dim3(SB_BX, SB_BY);
+    cfg.dynamicSmemBytes = (size_t)a.n;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return (int)cudaLaunchKernelEx(&cfg, k_group_project, a);
+}
+
+}  // namespace
+
+int group_occupancy(int* coop_per_sm, int* stage_per_sm, int* sms) {
+    const int rc = ensure_occupancy();
+    if (rc) return rc;
+    if (coop_per_sm) *coop_per_sm = g_occ[0];
+    if (stage_per_sm) *stage_per_sm = g_occ[2];
+    if (sms) *sms = g_sms;
+    return 0;
+}
+
+int launch_group_step(const GroupArgs& a, const GroupLaunch& L, cudaStream_t st) {
+    int rc = ensure_occupancy();
+    if (!rc) rc = launch_grid_stride((const void*)k_group_objects, L.total[GS_OBJECTS], g_occ[1], a, st);
+    if (!rc) rc = launch_grid_stride((const void*)k_group_forcing, L.total[GS_FORCE], g_occ[2], a, st);
+    if (!rc) rc = launch_project(a, L, st);
+    if (!rc) rc = launch_grid_stride((const void*)k_group_adv_vel, L.total[GS_ADV_VEL], g_occ[3], a, st);
+    if (!rc) rc = launch_grid_stride((const void*)k_group_adv_rho, L.total[GS_ADV_RHO], g_occ[4], a, st);
+    return rc;
+}
+
+int launch_group_sweeps_only(const GroupArgs& a, const GroupLaunch& L, cudaStream_t st) {
+    int rc = ensure_occupancy();
+    if (!rc) rc = launch_project(a, L, st);
+    return rc;
+}
+
+}  // namespace smk

@@ -32,28 +32,6 @@ int fail(int code, const std::string& msg) {
     return code;
 }
 
-#define SMK_CUDA(call)                                                                   \
-    do {                                                                                 \
-        cudaError_t e_ = (call);                                                         \
-        if (e_ != cudaSuccess) {                                                         \
-            return fail(e_ == cudaErrorMemoryAllocation ? SMK_ERR_OOM : SMK_ERR_CUDA,    \
-                        std::string(#call) + ": " + cudaGetErrorString(e_));             \
-        }                                                                                \
-    } while (0)
-
-struct DeviceGuard {
-    int prev = -1;
-    bool changed = false;
-    explicit DeviceGuard(int dev) {
-        if (cudaGetDevice(&prev) == cudaSuccess && prev != dev) {
-            changed = cudaSetDevice(dev) == cudaSuccess;
-        }
-    }
-    ~DeviceGuard() {
-        if (changed) cudaSetDevice(prev);
-    }
-};
-
 int check_params(const smk_params* p) {
     if (!p) return fail(SMK_ERR_INVALID, "params is null");
     if (p->projection != SMK_PROJECT_REFERENCE && p->projection != SMK_PROJECT_PRESSURE)
@@ -84,6 +62,8 @@ cudaMemcpy3DParms copy3d(void* dst, size_t dpitch, size_t dy, const void* src, s
 }
 
 }  // namespace
+
+int smk_fail(int code, const std::string& msg) { return fail(code, msg); }
 
 // ---- smk_sim --------------------------------------------------------------------------------
 
@@ -599,7 +579,7 @@ static int check_kernel_error(smk_sim* sim) {
     SMK_CUDA(cudaMemcpy(&e, sim->kerr, sizeof(int), cudaMemcpyDeviceToHost));
     if (e) {
         SMK_CUDA(cudaMemset(sim->kerr, 0, sizeof(int)));
-        return fail(SMK_ERR_TIMEOUT, "a sweep kernel's bounded wait for its TMA loads gave up; "
+        return fail(SMK_ERR_TIMEOUT, "a bounded device wait (TMA loads or a grid barrier) gave up; "
                                      "the step's projection is incomplete");
     }
     return SMK_OK;
@@ -900,172 +880,6 @@ int smk_autotune(smk_sim* sim, int* depth_out, int* zchunk_out, float* us_per_sw
     if (depth_out) *depth_out = best_d;
     if (zchunk_out) *zchunk_out = best_z;
     if (us_per_sweep_out) *us_per_sweep_out = best;
-    return SMK_OK;
-}
-
-}  // extern "C"
-
-// ---- batches: many independent grids stepped as one CUDA graph -----------------------------
-//
-// A batch step captures every grid's full step as its own branch of one graph (fork/join with
-// events from an origin stream), so the small kernels of many uneven grids run concurrently and
-// the host issues one cudaGraphLaunch per batch step.  A grid keeps its own buffers, parameters
-// and tuned sweep kernel, so its results are the same alone and in the batch.  The graph is
-// re-captured when any grid's signature (dt, parameters, objects, kernel) or ping-pong parity
-// changes; a step in which any grid has a pending mask change or stage timing runs directly,
-// still on the per-grid branch streams.
-
-struct smk_batch {
-    std::vector<smk_sim*> sims;
-    std::vector<cudaStream_t> branch;
-    std::vector<cudaEvent_t> join;
-    cudaStream_t origin = nullptr;
-    cudaEvent_t fork = nullptr;
-    cudaGraphExec_t exec = nullptr;
-    std::string sig;
-    std::vector<long long> launches;
-    std::vector<int> groups;
-    int device = 0;
-};
-
-extern "C" {
-
-int smk_batch_create(int count, smk_sim* const* sims, smk_batch** out) {
-    if (!out || count <= 0 || !sims) return fail(SMK_ERR_INVALID, "need at least one simulation");
-    *out = nullptr;
-    smk_batch* b = new smk_batch();
-    cudaGetDevice(&b->device);
-    for (int i = 0; i < count; ++i) {
-        if (!sims[i] || sims[i]->device != b->device) {
-            delete b;
-            return fail(SMK_ERR_INVALID, "batch members must be valid simulations on the current device");
-        }
-        b->sims.push_back(sims[i]);
-    }
-    auto cleanup = [b]() {
-        for (auto s : b->branch) if (s) cudaStreamDestroy(s);
-        for (auto e : b->join) if (e) cudaEventDestroy(e);
-        if (b->origin) cudaStreamDestroy(b->origin);
-        if (b->fork) cudaEventDestroy(b->fork);
-        delete b;
-    };
-    if (cudaStreamCreateWithFlags(&b->origin, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess) {
-        cleanup();
-        return fail(SMK_ERR_CUDA, "batch stream/event creation failed");
-    }
-    b->branch.assign(count, nullptr);
-    b->join.assign(count, nullptr);
-    for (int i = 0; i < count; ++i) {
-        if (cudaStreamCreateWithFlags(&b->branch[i], cudaStreamNonBlocking) != cudaSuccess ||
-            cudaEventCreateWithFlags(&b->join[i], cudaEventDisableTiming) != cudaSuccess) {
-            cleanup();
-            return fail(SMK_ERR_CUDA, "batch stream/event creation failed");
-        }
-    }
-    b->launches.assign(count, 0);
-    b->groups.assign(count, 0);
-    *out = b;
-    return SMK_OK;
-}
-
-int smk_batch_destroy(smk_batch* b) {
-    if (!b) return fail(SMK_ERR_INVALID, "batch is null");
-    DeviceGuard dg(b->device);
-    cudaStreamSynchronize(b->origin);
-    for (auto s : b->branch) cudaStreamSynchronize(s);
-    if (b->exec) cudaGraphExecDestroy(b->exec);
-    for (auto s : b->branch) cudaStreamDestroy(s);
-    for (auto e : b->join) cudaEventDestroy(e);
-    cudaStreamDestroy(b->origin);
-    cudaEventDestroy(b->fork);
-    delete b;
-    return SMK_OK;
-}
-
-// dts: one dt per grid (NULL: every grid uses dt_all).  Stream-ordered on `stream`.
-int smk_batch_step(smk_batch* b, const float* dts, float dt_all, void* stream) {
-    if (!b) return fail(SMK_ERR_INVALID, "batch is null");
-    DeviceGuard dg(b->device);
-    cudaStream_t st = (cudaStream_t)stream;
-    const int n = (int)b->sims.size();
-    bool direct = false;
-    std::string sig;
-    for (int i = 0; i < n; ++i) {
-        smk_sim* s = b->sims[i];
-        if (s->timing || s->mask_dirty || s->obstacles_dirty || !s->use_graphs) direct = true;
-        const float dt = dts ? dts[i] : dt_all;
-        std::string gs = s->graph_signature(dt);
-        const int len = (int)gs.size();
-        sig.append(reinterpret_cast<const char*>(&len), sizeof(len));
-        sig += gs;
-        sig.push_back((char)s->index_now);
-    }
-    if (direct) {
-        // direct launches on the branch streams, ordered after `st`
-        SMK_CUDA(cudaEventRecord(b->fork, st));
-        for (int i = 0; i < n; ++i) {
-            SMK_CUDA(cudaStreamWaitEvent(b->branch[i], b->fork, 0));
-            const int rc = b->sims[i]->step(dts ? dts[i] : dt_all, b->branch[i]);
-            if (rc) return rc;
-            SMK_CUDA(cudaEventRecord(b->join[i], b->branch[i]));
-            SMK_CUDA(cudaStreamWaitEvent(st, b->join[i], 0));
-        }
-        return SMK_OK;
-    }
-    if (b->exec == nullptr || sig != b->sig) {
-        std::vector<int> idx0(n), steps0(n);
-        std::vector<long long> l0(n);
-        for (int i = 0; i < n; ++i) {
-            idx0[i] = b->sims[i]->index_now;
-            steps0[i] = b->sims[i]->steps;
-            l0[i] = b->sims[i]->launches;
-        }
-        SMK_CUDA(cudaStreamBeginCapture(b->origin, cudaStreamCaptureModeThreadLocal));
-        int rc = SMK_OK;
-        cudaError_t ce = cudaEventRecord(b->fork, b->origin);
-        for (int i = 0; i < n && rc == SMK_OK && ce == cudaSuccess; ++i) {
-            ce = cudaStreamWaitEvent(b->branch[i], b->fork, 0);
-            if (ce != cudaSuccess) break;
-            rc = b->sims[i]->enqueue(dts ? dts[i] : dt_all, b->branch[i]);
-            if (rc == SMK_OK) ce = cudaEventRecord(b->join[i], b->branch[i]);
-            if (rc == SMK_OK && ce == cudaSuccess) ce = cudaStreamWaitEvent(b->origin, b->join[i], 0);
-        }
-        cudaGraph_t graph = nullptr;
-        const cudaError_t ee = cudaStreamEndCapture(b->origin, &graph);
-        for (int i = 0; i < n; ++i) {
-            smk_sim* s = b->sims[i];
-            b->launches[i] = s->launches - l0[i];
-            b->groups[i] = s->last_groups;
-            s->index_now = idx0[i];
-            s->steps = steps0[i];
-            s->launches = l0[i];
-        }
-        if (rc != SMK_OK || ce != cudaSuccess || ee != cudaSuccess) {
-            if (graph) cudaGraphDestroy(graph);
-            if (rc) return rc;
-            return fail(SMK_ERR_CUDA, std::string("batch capture: ") +
-                                          cudaGetErrorString(ce != cudaSuccess ? ce : ee));
-        }
-        if (b->exec) cudaGraphExecDestroy(b->exec);
-        b->exec = nullptr;
-        const cudaError_t ie = cudaGraphInstantiate(&b->exec, graph, 0);
-        cudaGraphDestroy(graph);
-        if (ie != cudaSuccess) return fail(SMK_ERR_CUDA, std::string("batch instantiate: ") + cudaGetErrorString(ie));
-        b->sig.swap(sig);
-    }
-    SMK_CUDA(cudaGraphLaunch(b->exec, st));
-    for (int i = 0; i < n; ++i) {
-        smk_sim* s = b->sims[i];
-        s->index_now ^= 1;
-        s->launches += b->launches[i];
-        ++s->steps;
-        s->last_groups = b->groups[i];
-        s->last_projection = s->p.projection;
-        s->last_tol = s->p.tol;
-        s->last_max_sweeps = s->p.max_sweeps;
-        s->last_check_every = s->p.check_every;
-    }
     return SMK_OK;
 }
 

@@ -11,6 +11,32 @@
 
 namespace smk { struct SweepMaps; }
 
+// Records `msg` as smk_last_error's text and returns `code` (sim.cpp).
+int smk_fail(int code, const std::string& msg);
+
+#define SMK_CUDA(call)                                                                   \
+    do {                                                                                 \
+        cudaError_t e_ = (call);                                                         \
+        if (e_ != cudaSuccess) {                                                         \
+            return smk_fail(e_ == cudaErrorMemoryAllocation ? SMK_ERR_OOM : SMK_ERR_CUDA, \
+                            std::string(#call) + ": " + cudaGetErrorString(e_));         \
+        }                                                                                \
+    } while (0)
+
+// Makes `dev` the current device for the scope.
+struct DeviceGuard {
+    int prev = -1;
+    bool changed = false;
+    explicit DeviceGuard(int dev) {
+        if (cudaGetDevice(&prev) == cudaSuccess && prev != dev) {
+            changed = cudaSetDevice(dev) == cudaSuccess;
+        }
+    }
+    ~DeviceGuard() {
+        if (changed) cudaSetDevice(prev);
+    }
+};
+
 struct smk_sim {
     enum Kind { OBJ_OBSTACLE = 0, OBJ_SPHERE = 1, OBJ_BOX = 2 };
     struct Object {

@@ -19,16 +19,12 @@ struct WAcc { float w[8]; };
 
 // ---- emitters ---------------------------------------------------------------------------------
 
-// Box emitters restricted to [x0,x1)x[y0,..)x[z0,..): density into both buffers, optional v.
+// One cell of the box emitters (in list order, so the last box containing the cell decides):
+// density into both buffers, and the box's upward velocity on the cell's two v faces.
 template <typename T, typename Tv>
-__device__ __forceinline__ void body_emit_boxes(const Grid& g, T* __restrict__ rho0,
-                                                T* __restrict__ rho1, Tv* __restrict__ v_now,
-                                                const BoxObj* boxes, int nb, int x0, int y0, int z0,
-                                                int x1, int y1, int z1, uint3 bid) {
-    const int x = x0 + (int)bid.x * SB_BX + (int)threadIdx.x;
-    const int y = y0 + (int)bid.y * SB_BY + (int)threadIdx.y;
-    const int z = z0 + (int)bid.z;
-    if (x >= x1 || y >= y1 || z >= z1) return;
+__device__ __forceinline__ void cell_emit_boxes(const Grid& g, T* __restrict__ rho0, T* __restrict__ rho1,
+                                                Tv* __restrict__ v_now, const BoxObj* boxes, int nb,
+                                                int x, int y, int z) {
     for (int k = 0; k < nb; ++k) {
         const BoxObj& b = boxes[k];
         if (x >= b.x0 && x < b.x1 && y >= b.y0 && y < b.y1 && z >= b.z0 && z < b.z1) {
@@ -43,17 +39,24 @@ __device__ __forceinline__ void body_emit_boxes(const Grid& g, T* __restrict__ r
     }
 }
 
-// fillSmoke (smokeSimulation.cu:251-273) over the box [x0,x1)x[y0,y1)x[z0,z1) (within the
-// interior): float squared distance from the integer corner, strict test, both buffers = 1.
-template <typename T>
-__device__ __forceinline__ void body_fill_smoke(const Grid& g, T* __restrict__ rho0,
-                                                T* __restrict__ rho1, const SphereObj* sp, int ns,
-                                                int x0, int y0, int z0, int x1, int y1, int z1,
-                                                uint3 bid) {
+// Box emitters restricted to [x0,x1)x[y0,..)x[z0,..): density into both buffers, optional v.
+template <typename T, typename Tv>
+__device__ __forceinline__ void body_emit_boxes(const Grid& g, T* __restrict__ rho0,
+                                                T* __restrict__ rho1, Tv* __restrict__ v_now,
+                                                const BoxObj* boxes, int nb, int x0, int y0, int z0,
+                                                int x1, int y1, int z1, uint3 bid) {
     const int x = x0 + (int)bid.x * SB_BX + (int)threadIdx.x;
     const int y = y0 + (int)bid.y * SB_BY + (int)threadIdx.y;
     const int z = z0 + (int)bid.z;
     if (x >= x1 || y >= y1 || z >= z1) return;
+    cell_emit_boxes(g, rho0, rho1, v_now, boxes, nb, x, y, z);
+}
+
+// One cell of fillSmoke (smokeSimulation.cu:251-273): float squared distance from the integer
+// corner, strict test, both buffers = 1.
+template <typename T>
+__device__ __forceinline__ void cell_fill_smoke(const Grid& g, T* __restrict__ rho0, T* __restrict__ rho1,
+                                                const SphereObj* sp, int ns, int x, int y, int z) {
     for (int k = 0; k < ns; ++k) {
         const float dx = (float)x - sp[k].x, dy = (float)y - sp[k].y, dz = (float)z - sp[k].z;
         const float dist = dx * dx + dy * dy + dz * dz;
@@ -63,6 +66,19 @@ __device__ __forceinline__ void body_fill_smoke(const Grid& g, T* __restrict__ r
             stv(rho1, i, 1.0f);
         }
     }
+}
+
+// fillSmoke over the box [x0,x1)x[y0,y1)x[z0,z1) (within the interior).
+template <typename T>
+__device__ __forceinline__ void body_fill_smoke(const Grid& g, T* __restrict__ rho0,
+                                                T* __restrict__ rho1, const SphereObj* sp, int ns,
+                                                int x0, int y0, int z0, int x1, int y1, int z1,
+                                                uint3 bid) {
+    const int x = x0 + (int)bid.x * SB_BX + (int)threadIdx.x;
+    const int y = y0 + (int)bid.y * SB_BY + (int)threadIdx.y;
+    const int z = z0 + (int)bid.z;
+    if (x >= x1 || y >= y1 || z >= z1) return;
+    cell_fill_smoke(g, rho0, rho1, sp, ns, x, y, z);
 }
 
 // ---- forcing: integrate (smokeSimulation.cu:315-329) + velocityConfinement (:331-352) -------
@@ -106,15 +122,18 @@ __device__ __forceinline__ void body_forcing(const Grid& g, Tv* __restrict__ u, 
 }
 
 // ---- pressure scheme ------------------------------------------------------------------------
+//
+// The projection bodies take plain (not __restrict__) pointers: the grouped projection runs
+// them as phases of one cooperative launch, where a phase reads what other CTAs wrote in an
+// earlier phase (after a grid barrier), so no load of P, b or the velocities may go through
+// the non-coherent read-only path.
 
 // b = -div(u*) on projectable cells; P = 0 off them (and everywhere on a cold start); on a warm
 // start whose previous solve ended in the second buffer (*pcur == 1) P is taken from there.
 template <typename T>
-__device__ __forceinline__ void body_rhs(const Grid& g, const T* __restrict__ u,
-                                         const T* __restrict__ v, const T* __restrict__ w,
-                                         const uint8_t* __restrict__ flags, float* __restrict__ b,
-                                         float* __restrict__ P, const float* __restrict__ P2,
-                                         const int* __restrict__ pcur, int warm, uint3 bid) {
+__device__ __forceinline__ void body_rhs(const Grid& g, const T* u, const T* v, const T* w,
+                                         const uint8_t* __restrict__ flags, float* b, float* P,
+                                         const float* P2, const int* pcur, int warm, uint3 bid) {
     const int x = (int)bid.x * SB_BX + (int)threadIdx.x;
     const int y = (int)bid.y * SB_BY + (int)threadIdx.y;
     const int z = (int)bid.z;
@@ -132,9 +151,40 @@ __device__ __forceinline__ void body_rhs(const Grid& g, const T* __restrict__ u,
     }
 }
 
-// One colour pass:  r = fma(-acc, P_c, b_c + (((P_x-+P_x+)+(P_y-+P_y+))+(P_z-+P_z+)));
-// P_c = fma(omega/acc, r, P_c).  bid.x counts same-colour cells of a row.
-__device__ __forceinline__ void body_sweep(const Grid& g, float* __restrict__ P, const float* __restrict__ b,
+// One cell of a colour pass:  r = fma(-acc, P_c, b_c + (((P_x-+P_x+)+(P_y-+P_y+))+(P_z-+P_z+)));
+// P_c = fma(omega/acc, r, P_c).
+__device__ __forceinline__ void cell_sweep(const Grid& g, float* P, const float* b,
+                                           const uint8_t* __restrict__ flags, int i, const float* wacc) {
+    const uint8_t f = flags[i];
+    if (!(f & F_PROJ)) return;
+    const int acc = __popc((unsigned)(f & F_NBRS));
+    const float sum = ((P[i - 1] + P[i + 1]) + (P[i - g.X] + P[i + g.X])) + (P[i - g.XY] + P[i + g.XY]);
+    const float pc = P[i];
+    const float r = fmaf(-(float)acc, pc, b[i] + sum);
+    P[i] = fmaf(wacc[acc], r, pc);
+}
+
+// |residual| of one cell (0 off the projectable set), the expression of cell_sweep.
+__device__ __forceinline__ float cell_resid(const Grid& g, const float* P, const float* b,
+                                            const uint8_t* __restrict__ flags, int i) {
+    const uint8_t f = flags[i];
+    if (!(f & F_PROJ)) return 0.0f;
+    const int acc = __popc((unsigned)(f & F_NBRS));
+    const float sum = ((P[i - 1] + P[i + 1]) + (P[i - g.X] + P[i + g.X])) + (P[i - g.XY] + P[i + g.XY]);
+    const float r = fmaf(-(float)acc, P[i], b[i] + sum);
+    return fabsf(r);
+}
+
+// |div u| of one cell (0 off the projectable set).
+__device__ __forceinline__ float cell_div(const Grid& g, const float* u, const float* v, const float* w,
+                                          const uint8_t* __restrict__ flags, int i) {
+    if (!(flags[i] & F_PROJ)) return 0.0f;
+    const float div = -u[i] + u[i + 1] + -v[i] + v[i + g.X] + -w[i] + w[i + g.XY];
+    return fabsf(div);
+}
+
+// One colour pass.  bid.x counts same-colour cells of a row.
+__device__ __forceinline__ void body_sweep(const Grid& g, float* P, const float* b,
                                            const uint8_t* __restrict__ flags, int colour, const WAcc& wa,
                                            const StepStatus* __restrict__ status, uint3 bid) {
     if (status && *(volatile const int*)&status->done) return;
@@ -142,21 +192,13 @@ __device__ __forceinline__ void body_sweep(const Grid& g, float* __restrict__ P,
     const int z = 1 + (int)bid.z;
     const int x = 1 + ((1 + y + z + colour) & 1) + 2 * ((int)bid.x * SB_BX + (int)threadIdx.x);
     if (x > g.nx - 2 || y > g.ny - 2 || z > g.nz - 2) return;
-    const int i = g.idx(x, y, z);
-    const uint8_t f = flags[i];
-    if (!(f & F_PROJ)) return;
-    const int acc = __popc((unsigned)(f & F_NBRS));
-    const float sum = ((P[i - 1] + P[i + 1]) + (P[i - g.X] + P[i + g.X])) + (P[i - g.XY] + P[i + g.XY]);
-    const float pc = P[i];
-    const float r = fmaf(-(float)acc, pc, b[i] + sum);
-    P[i] = fmaf(wa.w[acc], r, pc);
+    cell_sweep(g, P, b, flags, g.idx(x, y, z), wa.w);
 }
 
 // Residual check at the start of sweep group `group`: if the previous group's residual was
 // within tolerance the solve is over (set `done`); otherwise record max |r| for this group.
 // Contains a block barrier: every thread of the block must call it.
-__device__ __forceinline__ void body_resid_check(const Grid& g, const float* __restrict__ P,
-                                                 const float* __restrict__ b,
+__device__ __forceinline__ void body_resid_check(const Grid& g, const float* P, const float* b,
                                                  const uint8_t* __restrict__ flags, StepStatus* status,
                                                  int group, float tol, uint3 bid) {
     if (*(volatile int*)&status->done) return;
@@ -171,28 +213,16 @@ __device__ __forceinline__ void body_resid_check(const Grid& g, const float* __r
     const int y = 1 + (int)bid.y * SB_BY + (int)threadIdx.y;
     const int z = 1 + (int)bid.z;
     float m = 0.0f;
-    if (x <= g.nx - 2 && y <= g.ny - 2 && z <= g.nz - 2) {
-        const int i = g.idx(x, y, z);
-        const uint8_t f = flags[i];
-        if (f & F_PROJ) {
-            const int acc = __popc((unsigned)(f & F_NBRS));
-            const float sum = ((P[i - 1] + P[i + 1]) + (P[i - g.X] + P[i + g.X])) + (P[i - g.XY] + P[i + g.XY]);
-            const float r = fmaf(-(float)acc, P[i], b[i] + sum);
-            m = fabsf(r);
-        }
-    }
+    if (x <= g.nx - 2 && y <= g.ny - 2 && z <= g.nz - 2) m = cell_resid(g, P, b, flags, g.idx(x, y, z));
     block_max_to(__float_as_uint(m), &status->rmax_bits[group]);
 }
 
 // u -= P(x) - P(x-1) on faces whose two cells are fluid (P is 0 off the projectable set).  The
 // pressure is the first buffer, or the second when *pcur == 1.
-__device__ __forceinline__ void body_gradient_subtract(const Grid& g, float* __restrict__ u,
-                                                       float* __restrict__ v, float* __restrict__ w,
-                                                       const float* __restrict__ P0,
-                                                       const float* __restrict__ P1,
-                                                       const int* __restrict__ pcur,
+__device__ __forceinline__ void body_gradient_subtract(const Grid& g, float* u, float* v, float* w,
+                                                       const float* P0, const float* P1, const int* pcur,
                                                        const uint8_t* __restrict__ flags, uint3 bid) {
-    const float* __restrict__ P = (pcur != nullptr && *pcur == 1) ? P1 : P0;
+    const float* P = (pcur != nullptr && *pcur == 1) ? P1 : P0;
     const int x = 1 + (int)bid.x * SB_BX + (int)threadIdx.x;
     const int y = 1 + (int)bid.y * SB_BY + (int)threadIdx.y;
     const int z = 1 + (int)bid.z;
@@ -208,21 +238,14 @@ __device__ __forceinline__ void body_gradient_subtract(const Grid& g, float* __r
 }
 
 // max |div u| over projectable cells.  Contains a block barrier.
-__device__ __forceinline__ void body_div_max(const Grid& g, const float* __restrict__ u,
-                                             const float* __restrict__ v, const float* __restrict__ w,
-                                             const uint8_t* __restrict__ flags, StepStatus* status,
-                                             uint3 bid) {
+__device__ __forceinline__ void body_div_max(const Grid& g, const float* u, const float* v,
+                                             const float* w, const uint8_t* __restrict__ flags,
+                                             StepStatus* status, uint3 bid) {
     const int x = 1 + (int)bid.x * SB_BX + (int)threadIdx.x;
     const int y = 1 + (int)bid.y * SB_BY + (int)threadIdx.y;
     const int z = 1 + (int)bid.z;
     float m = 0.0f;
-    if (x <= g.nx - 2 && y <= g.ny - 2 && z <= g.nz - 2) {
-        const int i = g.idx(x, y, z);
-        if (flags[i] & F_PROJ) {
-            const float div = -u[i] + u[i + 1] + -v[i] + v[i + g.X] + -w[i] + w[i + g.XY];
-            m = fabsf(div);
-        }
-    }
+    if (x <= g.nx - 2 && y <= g.ny - 2 && z <= g.nz - 2) m = cell_div(g, u, v, w, flags, g.idx(x, y, z));
     block_max_to(__float_as_uint(m), &status->div_bits);
 }
 
@@ -230,14 +253,11 @@ __device__ __forceinline__ void body_div_max(const Grid& g, const float* __restr
 // (advection reads it there, and max|div u| is measured there), and rounded into the BF16
 // state where the gradient changed it, so the state holds the projected velocity as in the
 // FP32 form.  Storing only the rounded value would leave a divergence of order 1e-2 |u|.
-__device__ __forceinline__ void body_project_bf16(const Grid& g, __nv_bfloat16* __restrict__ u,
-                                                  __nv_bfloat16* __restrict__ v,
-                                                  __nv_bfloat16* __restrict__ w,
-                                                  const float* __restrict__ P0, const float* __restrict__ P1,
-                                                  const int* __restrict__ pcur,
-                                                  const uint8_t* __restrict__ flags, float* __restrict__ pu,
-                                                  float* __restrict__ pv, float* __restrict__ pw, uint3 bid) {
-    const float* __restrict__ P = (pcur != nullptr && *pcur == 1) ? P1 : P0;
+__device__ __forceinline__ void body_project_bf16(const Grid& g, __nv_bfloat16* u, __nv_bfloat16* v,
+                                                  __nv_bfloat16* w, const float* P0, const float* P1,
+                                                  const int* pcur, const uint8_t* __restrict__ flags,
+                                                  float* pu, float* pv, float* pw, uint3 bid) {
+    const float* P = (pcur != nullptr && *pcur == 1) ? P1 : P0;
     const int x = (int)bid.x * SB_BX + (int)threadIdx.x;
     const int y = (int)bid.y * SB_BY + (int)threadIdx.y;
     const int z = (int)bid.z;

@@ -60,3 +60,154 @@ def test_batch_rejects_empty(gpu):
     import ctypes as C
     h = C.c_void_p()
     assert smk.lib().smk_batch_create(0, None, C.byref(h)) == 1
+
+
+def _grouped_scenes(count=7, seed=11):
+    scs = S.config_batched(count=count, steps=6, seed=seed, lo=8, hi=44, scheme=1, iterations=30)
+    for i, sc in enumerate(scs):
+        sc.u0, sc.v0, sc.w0 = S.noise_velocity(sc.face_shape, 0.3, seed=200 + i)
+        # a mix of tolerance rules, group sizes and pressure starts across the members
+        sc.tol = (1e-3, 0.0, 1e-4, 5e-4)[i % 4]
+        sc.check_every = (4, 1, 6, 3)[i % 4]
+        sc.warm_start = i % 2
+    scs[1].iterations = 0  # a member without sweeps
+    return scs
+
+
+def _step_all(batch, alone, oracles, dts, steps, mask_step=None, scs=None, batch_sims=None):
+    for k in range(steps):
+        if k == mask_step:
+            m = scs[1].initial_mask().copy()
+            m[2:4, 2:4, 2:4] = 0
+            batch_sims[1].set_mask(m)
+            alone[1].set_mask(m)
+            if oracles:
+                oracles[1].s[...] = m
+        batch.step(dts)
+        for s, dt in zip(alone, dts):
+            s.step(dt)
+        for o, dt in zip(oracles or [], dts):
+            o.step(dt)
+
+
+def test_grouped_equals_alone_and_oracle(gpu):
+    """One persistent launch per stage over 7 uneven grids (8..44 cells per side, per-member dt,
+    tolerance, group size and pressure start) is bit-identical to each grid stepped alone and
+    to the oracle, including a step with a mask change (run per member) in between."""
+    scs = _grouped_scenes()
+    dts = [sc.dt * (1.0 + 0.05 * i) for i, sc in enumerate(scs)]
+    batch_sims = [smk.from_scene(sc, report_div=1) for sc in scs]
+    alone = [smk.from_scene(sc, report_div=1) for sc in scs]
+    for s in alone:
+        s.set_graphs(False)
+        s.autotune()
+    oracles = [O.OracleSim(sc) for sc in scs]
+    batch = smk.Batch(batch_sims, mode=smk.BATCH_GROUPED)
+    _step_all(batch, alone, oracles, dts, 6, mask_step=3, scs=scs, batch_sims=batch_sims)
+    mode, launches = batch.info()
+    assert mode == smk.BATCH_GROUPED
+    for i in range(len(scs)):
+        a = batch_sims[i].read_state()
+        assert H.first_mismatch(a, alone[i].read_state()) == "", i
+        assert H.first_mismatch(a, H.oracle_state(oracles[i])) == "", i
+        sa, sb = batch_sims[i].stats(), alone[i].stats()
+        assert (sa.sweeps, sa.converged, sa.div_max, sa.resid_max) == (sb.sweeps, sb.converged, sb.div_max,
+                                                                       sb.resid_max), i
+    batch.close()
+    for s in batch_sims + alone:
+        s.close()
+
+
+def test_grouped_launches_per_step_do_not_grow_with_members(gpu):
+    scs = _grouped_scenes(count=12, seed=5)
+    sims = [smk.from_scene(sc) for sc in scs]
+    batch = smk.Batch(sims, mode=smk.BATCH_GROUPED)
+    batch.step(0.05)  # first step: mask upload, per member
+    _, l0 = batch.info()
+    for _ in range(4):
+        batch.step(0.05)
+    mode, l1 = batch.info()
+    assert mode == smk.BATCH_GROUPED
+    assert (l1 - l0) == 4 * 5  # emitters, forcing, projection, two advections
+    batch.close()
+    for s in sims:
+        s.close()
+
+
+@pytest.mark.parametrize("storage", [smk.STORAGE_BF16, smk.STORAGE_BF16_VEL])
+def test_grouped_bf16_members_equal_alone(gpu, storage):
+    scs = _grouped_scenes(count=5, seed=13)
+    batch_sims = [smk.from_scene(sc, report_div=1, storage=storage) for sc in scs]
+    alone = [smk.from_scene(sc, report_div=1, storage=storage) for sc in scs]
+    batch = smk.Batch(batch_sims, mode=smk.BATCH_GROUPED)
+    _step_all(batch, alone, None, [0.05] * len(scs), 5)
+    assert batch.info()[0] == smk.BATCH_GROUPED
+    for i in range(len(scs)):
+        assert H.first_mismatch(batch_sims[i].read_state(), alone[i].read_state()) == "", i
+        assert batch_sims[i].stats().div_max == alone[i].stats().div_max
+    batch.close()
+    for s in batch_sims + alone:
+        s.close()
+
+
+def test_grouped_graphs_autotune_and_parity_changes_do_not_change_results(gpu):
+    """Graph replay on/off, a tuned CTA count, and a member stepped on its own between batch
+    steps (its ping-pong parity then differs from the others') leave the results unchanged."""
+    scs = _grouped_scenes(count=6, seed=17)
+    runs = []
+    for variant in ("graphs", "direct", "tuned"):
+        sims = [smk.from_scene(sc, report_div=1) for sc in scs]
+        batch = smk.Batch(sims, mode=smk.BATCH_GROUPED)
+        if variant == "direct":
+            batch.set_graphs(False)
+        for k in range(6):
+            if k == 2 and variant == "tuned":
+                c, us = batch.autotune()
+                assert c >= 1 and us > 0
+            if k == 3:
+                sims[0].step(0.05)  # member 0 alone: parities now differ across the batch
+            batch.step(0.05)
+        assert batch.info()[0] == smk.BATCH_GROUPED
+        runs.append([s.read_state() for s in sims])
+        batch.close()
+        for s in sims:
+            s.close()
+    for i in range(len(scs)):
+        assert H.first_mismatch(runs[0][i], runs[1][i]) == "", i
+        assert H.first_mismatch(runs[0][i], runs[2][i]) == "", i
+
+
+def test_grouped_mode_rejects_reference_scheme(gpu):
+    scs = _scenes()
+    sims = [smk.from_scene(sc) for sc in scs]
+    batch = smk.Batch(sims)
+    with pytest.raises(smk.SmokeError):
+        batch.set_mode(smk.BATCH_GROUPED)
+    batch.step(0.05)
+    batch.step(0.05)
+    assert batch.info()[0] == smk.BATCH_BRANCHES
+    batch.close()
+    for s in sims:
+        s.close()
+
+
+@pytest.mark.parametrize("sched", [(1, 1, 1 << 20), (0, 4, 0), (2, 16, 300_000), (3, 7, 1 << 30)])
+def test_grouped_schedules_do_not_change_results(gpu, sched):
+    """CTAs per SM, z planes per tile and solve waves (1 MB, 300 kB: nearly one wave per grid)
+    change only the speed."""
+    scs = _grouped_scenes(count=6, seed=23)
+    ref = [smk.from_scene(sc, report_div=1) for sc in scs]
+    sims = [smk.from_scene(sc, report_div=1) for sc in scs]
+    batch = smk.Batch(sims, mode=smk.BATCH_GROUPED)
+    batch.set_schedule(*sched)
+    assert batch.schedule() == sched
+    for _ in range(4):
+        batch.step(0.05)
+        for s in ref:
+            s.step(0.05)
+    for i in range(len(scs)):
+        assert H.first_mismatch(sims[i].read_state(), ref[i].read_state()) == "", i
+        assert sims[i].stats().sweeps == ref[i].stats().sweeps
+    batch.close()
+    for s in sims + ref:
+        s.close()
