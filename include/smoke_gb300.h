@@ -204,10 +204,10 @@ int smk_batch_set_schedule(smk_batch* batch, int ctas_per_sm, int zslab, long lo
  * counterpart in the reference (one simulation stepped from the render loop, main.cpp:889-896).
  * smk_server_tick retires requests whose last step completed (their density goes to
  * out_density), admits queued requests in arrival order while the device-memory budget and
- * the slot limit allow, and issues one step per active request on its own stream (work of
- * different requests overlaps).  Per-step latency = device time of a request's step, measured
- * with events on its stream.  Each request is an independent simulation: its results are the
- * same alone and in the mix. */
+ * the slot limit allow, and issues the next step of every active request (work of different
+ * requests overlaps: concurrent streams, or one grouped step, see smk_server_set_mode).
+ * Per-step latency = device time of a request's step, measured with events.  Each request is
+ * an independent simulation: its results are the same alone and in the mix. */
 #define SMK_REQ_QUEUED 0
 #define SMK_REQ_ACTIVE 1
 #define SMK_REQ_DONE 2
@@ -236,6 +236,12 @@ typedef struct smk_server_stats {
     float p50_step_ms, p99_step_ms, max_step_ms;
 } smk_server_stats;
 int smk_server_create(size_t budget_bytes, int max_active, smk_server** out);
+/* Serving form, before the first request runs: STREAMS (default) steps every request with its
+ * own single-grid kernels on its own stream; GROUPED issues one grouped step (the batch's
+ * GROUPED kernels) over all active requests per tick.  Results are the same in both. */
+#define SMK_SERVE_STREAMS 0
+#define SMK_SERVE_GROUPED 1
+int smk_server_set_mode(smk_server* server, int mode);
 int smk_server_submit(smk_server* server, const smk_request_desc* request, int* id);
 int smk_server_tick(smk_server* server, int* n_active, int* n_queued);
 int smk_server_request_status(smk_server* server, int id, int* state, int* steps_done, int* error);

@@ -62,7 +62,7 @@ struct smk_batch {
     Slot slots[2];
     unsigned long long clock = 0;
     // schedule of the grouped projection; ctas_per_sm 0 = all resident CTAs
-    GroupSchedule sched{0, 8, 0};
+    GroupSchedule sched{0, 4, 0};
 };
 
 namespace {
@@ -193,12 +193,12 @@ void fill_record(smk_sim* s, float dt, TableImage& t, GroupGrid& d) {
     }
 }
 
-int build_table(smk_batch* b, const float* dts, float dt_all, const GroupSchedule& sch, TableImage& t) {
-    const int n = (int)b->sims.size();
+int build_table(smk_sim* const* sims, int n, const float* dts, float dt_all, const GroupSchedule& sch,
+                TableImage& t) {
     t.grids.resize(n);
     t.boxes.clear();
     t.spheres.clear();
-    for (int i = 0; i < n; ++i) fill_record(b->sims[i], dts ? dts[i] : dt_all, t, t.grids[i]);
+    for (int i = 0; i < n; ++i) fill_record(sims[i], dts ? dts[i] : dt_all, t, t.grids[i]);
     t.zslab = std::max(1, sch.zslab);
     t.nwaves = assign_waves(t.grids, sch.wave_bytes);
     t.starts.assign((size_t)GS_COUNT * (n + 1), 0);
@@ -224,15 +224,17 @@ int build_table(smk_batch* b, const float* dts, float dt_all, const GroupSchedul
     return SMK_OK;
 }
 
-// Copy a table image into `dev` (synchronous; callers hold no graph that reads it in flight).
-int upload_table(const TableImage& t, void* dev, GroupArgs& a, int n) {
-    std::vector<char> blob(t.bytes, 0);
-    memcpy(blob.data() + t.off_grids, t.grids.data(), sizeof(GroupGrid) * n);
-    memcpy(blob.data() + t.off_starts, t.starts.data(), sizeof(int) * t.starts.size());
-    if (!t.boxes.empty()) memcpy(blob.data() + t.off_boxes, t.boxes.data(), sizeof(BoxObj) * t.boxes.size());
-    if (!t.spheres.empty())
-        memcpy(blob.data() + t.off_spheres, t.spheres.data(), sizeof(SphereObj) * t.spheres.size());
-    SMK_CUDA(cudaMemcpy(dev, blob.data(), t.bytes, cudaMemcpyHostToDevice));
+// Lay a table image out in `blob` (t.bytes bytes) as the device copy will hold it.
+void pack_table(const TableImage& t, char* blob) {
+    memset(blob, 0, t.bytes);
+    memcpy(blob + t.off_grids, t.grids.data(), sizeof(GroupGrid) * t.grids.size());
+    memcpy(blob + t.off_starts, t.starts.data(), sizeof(int) * t.starts.size());
+    if (!t.boxes.empty()) memcpy(blob + t.off_boxes, t.boxes.data(), sizeof(BoxObj) * t.boxes.size());
+    if (!t.spheres.empty()) memcpy(blob + t.off_spheres, t.spheres.data(), sizeof(SphereObj) * t.spheres.size());
+}
+
+// Kernel arguments for a table whose device copy starts at `dev`.
+void table_args(const TableImage& t, void* dev, GroupArgs& a, int n) {
     char* base = static_cast<char*>(dev);
     a.sync = reinterpret_cast<GroupSync*>(base);
     a.grids = reinterpret_cast<const GroupGrid*>(base + t.off_grids);
@@ -243,10 +245,18 @@ int upload_table(const TableImage& t, void* dev, GroupArgs& a, int n) {
     a.zslab = t.zslab;
     a.nwaves = t.nwaves;
     a.sweeps_only = 0;
+}
+
+// Copy a table image into `dev` (synchronous; callers hold no step that reads it in flight).
+int upload_table(const TableImage& t, void* dev, GroupArgs& a, int n) {
+    std::vector<char> blob(t.bytes);
+    pack_table(t, blob.data());
+    SMK_CUDA(cudaMemcpy(dev, blob.data(), t.bytes, cudaMemcpyHostToDevice));
+    table_args(t, dev, a, n);
     return SMK_OK;
 }
 
-int launch_config(smk_batch* b, const TableImage& t, GroupLaunch& L, int& kernels) {
+int launch_config(const GroupSchedule& sched, const TableImage& t, GroupLaunch& L, int& kernels) {
     int coop = 0, stage = 0, sms = 0;
     const int rc = group_occupancy(&coop, &stage, &sms);
     if (rc) return smk_fail(SMK_ERR_CUDA, std::string("grouped kernels: ") + cudaGetErrorString((cudaError_t)rc));
@@ -259,17 +269,19 @@ int launch_config(smk_batch* b, const TableImage& t, GroupLaunch& L, int& kernel
     }
     const int launched[4] = {GS_OBJECTS, GS_FORCE, GS_ADV_VEL, GS_ADV_RHO};
     for (int s : launched) kernels += L.total[s] > 0 ? 1 : 0;
-    const int per_sm = b->sched.ctas_per_sm > 0 ? std::min(b->sched.ctas_per_sm, coop) : coop;
+    const int per_sm = sched.ctas_per_sm > 0 ? std::min(sched.ctas_per_sm, coop) : coop;
     L.coop_ctas = per_sm * sms;
     return SMK_OK;
 }
 
-bool grouped_eligible(const smk_batch* b) {
-    if ((int)b->sims.size() > MAX_GROUPED) return false;
-    for (const smk_sim* s : b->sims)
-        if (s->p.projection != SMK_PROJECT_PRESSURE) return false;
+bool grouped_eligible(smk_sim* const* sims, int n) {
+    if (n > MAX_GROUPED) return false;
+    for (int i = 0; i < n; ++i)
+        if (sims[i]->p.projection != SMK_PROJECT_PRESSURE) return false;
     return true;
 }
+
+bool grouped_eligible(const smk_batch* b) { return grouped_eligible(b->sims.data(), (int)b->sims.size()); }
 
 void after_step(smk_sim* s) {
     s->index_now ^= 1;
@@ -285,6 +297,9 @@ void after_step(smk_sim* s) {
 
 int grouped_step(smk_batch* b, const float* dts, float dt_all, cudaStream_t st) {
     const int n = (int)b->sims.size();
+    // one-off mask / obstacle kernels of members with a pending change, ahead of the step
+    for (smk_sim* s : b->sims)
+        if (s->mask_dirty || s->obstacles_dirty) b->launches += s->prepare_mask(st);
     std::string sig;
     for (int i = 0; i < n; ++i) {
         smk_sim* s = b->sims[i];
@@ -301,7 +316,7 @@ int grouped_step(smk_batch* b, const float* dts, float dt_all, cudaStream_t st) 
     if (!slot) {
         slot = b->slots[0].used <= b->slots[1].used ? &b->slots[0] : &b->slots[1];
         TableImage t;
-        int rc = build_table(b, dts, dt_all, b->sched, t);
+        int rc = build_table(b->sims.data(), n, dts, dt_all, b->sched, t);
         if (rc) return rc;
         // the slot being replaced may still be read by a step in flight
         SMK_CUDA(cudaDeviceSynchronize());
@@ -319,7 +334,7 @@ int grouped_step(smk_batch* b, const float* dts, float dt_all, cudaStream_t st) 
         }
         rc = upload_table(t, slot->dev, slot->args, n);
         if (rc) return rc;
-        rc = launch_config(b, t, slot->L, slot->kernels);
+        rc = launch_config(b->sched, t, slot->L, slot->kernels);
         if (rc) return rc;
         if (b->use_graphs && b->graphs_ok) {
             cudaGraph_t graph = nullptr;
@@ -447,6 +462,87 @@ void release_slots(smk_batch* b) {
 
 }  // namespace
 
+// ---- grouped steps over a changing set of simulations (the serving loop) ----------------------
+
+struct GroupRunner {
+    struct Slot {
+        void* dev = nullptr;
+        char* host = nullptr;  // pinned staging of the table copy
+        size_t cap = 0;
+        cudaEvent_t done = nullptr;
+        bool used = false;
+    };
+    static constexpr int RING = 4;
+    Slot ring[RING];
+    int next = 0;
+};
+
+GroupRunner* group_runner_create() {
+    GroupRunner* r = new GroupRunner();
+    for (auto& sl : r->ring) {
+        if (cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming) != cudaSuccess) {
+            group_runner_destroy(r);
+            return nullptr;
+        }
+    }
+    return r;
+}
+
+void group_runner_destroy(GroupRunner* r) {
+    if (!r) return;
+    for (auto& sl : r->ring) {
+        if (sl.done) {
+            if (sl.used) cudaEventSynchronize(sl.done);
+            cudaEventDestroy(sl.done);
+        }
+        if (sl.dev) cudaFree(sl.dev);
+        if (sl.host) cudaFreeHost(sl.host);
+    }
+    delete r;
+}
+
+int group_runner_step(GroupRunner* r, smk_sim* const* sims, const float* dts, int n,
+                      const GroupSchedule& sched, cudaStream_t st, int* kernels) {
+    if (kernels) *kernels = 0;
+    if (!r || n <= 0) return SMK_OK;
+    if (!grouped_eligible(sims, n))
+        return smk_fail(SMK_ERR_INVALID, "a grouped step needs the PRESSURE projection in every member");
+    int k = 0;
+    for (int i = 0; i < n; ++i)
+        if (sims[i]->mask_dirty || sims[i]->obstacles_dirty) k += sims[i]->prepare_mask(st);
+    TableImage t;
+    int rc = build_table(sims, n, dts, 0.0f, sched, t);
+    if (rc) return rc;
+    GroupRunner::Slot& sl = r->ring[r->next];
+    r->next = (r->next + 1) % GroupRunner::RING;
+    if (sl.used) SMK_CUDA(cudaEventSynchronize(sl.done));  // the step that last read it is done
+    if (sl.cap < t.bytes) {
+        if (sl.dev) cudaFree(sl.dev);
+        if (sl.host) cudaFreeHost(sl.host);
+        sl.dev = nullptr;
+        sl.host = nullptr;
+        sl.cap = 0;
+        SMK_CUDA(cudaMalloc(&sl.dev, t.bytes));
+        SMK_CUDA(cudaMallocHost((void**)&sl.host, t.bytes));
+        sl.cap = t.bytes;
+    }
+    pack_table(t, sl.host);
+    SMK_CUDA(cudaMemcpyAsync(sl.dev, sl.host, t.bytes, cudaMemcpyHostToDevice, st));
+    GroupArgs a{};
+    table_args(t, sl.dev, a, n);
+    GroupLaunch L{};
+    int nk = 0;
+    rc = launch_config(sched, t, L, nk);
+    if (rc) return rc;
+    const int lrc = launch_group_step(a, L, st);
+    if (lrc) return smk_fail(SMK_ERR_CUDA, std::string("grouped step: ") + cudaGetErrorString((cudaError_t)lrc));
+    SMK_CUDA(cudaEventRecord(sl.done, st));
+    sl.used = true;
+    for (int i = 0; i < n; ++i) after_step(sims[i]);
+    if (kernels) *kernels = k + nk;
+    return SMK_OK;
+}
+
 extern "C" {
 
 int smk_batch_create(int count, smk_sim* const* sims, smk_batch** out) {
@@ -532,9 +628,9 @@ int smk_batch_step(smk_batch* b, const float* dts, float dt_all, void* stream) {
     DeviceGuard dg(b->device);
     cudaStream_t st = (cudaStream_t)stream;
     bool grouped = b->mode != SMK_BATCH_BRANCHES && grouped_eligible(b);
-    // a pending mask or obstacle change (one-off kernels) or stage timing: per-member steps
+    // stage timing is per member: per-member steps
     for (const smk_sim* s : b->sims)
-        if (s->timing || s->mask_dirty || s->obstacles_dirty) grouped = false;
+        if (s->timing) grouped = false;
     if (grouped) return grouped_step(b, dts, dt_all, st);
     return branches_step(b, dts, dt_all, st);
 }
@@ -580,7 +676,7 @@ int smk_batch_autotune(smk_batch* b, int* ctas_per_sm, float* us_per_sweep) {
         for (long long wb : waves) {
             if (rc) break;
             TableImage t;
-            rc = build_table(b, nullptr, 0.0f, GroupSchedule{0, zs, wb}, t);
+            rc = build_table(b->sims.data(), n, nullptr, 0.0f, GroupSchedule{0, zs, wb}, t);
             if (rc) break;
             if (wb > 0 && t.nwaves == 1) continue;  // same schedule as one wave
             for (GroupGrid& d : t.grids) {

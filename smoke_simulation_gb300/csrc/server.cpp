@@ -4,17 +4,22 @@
 // (project/main.cpp:93, :889-896).  A server instead keeps many simulations resident on one GPU
 // and admits new ones while others run:
 //   - submit() queues a request (grid size, step count, scene, parameters);
-//   - tick() (1) retires requests whose last step has completed: their density is copied to the
-//     caller's host buffer and their device memory is freed; (2) admits queued requests in
-//     arrival order while the device-memory budget and the slot limit allow; (3) issues one step
-//     for every active request, each on its own stream, so the work of different requests
-//     overlaps on the device;
-//   - every issued step is bracketed by CUDA events on its stream; its latency (device time from
-//     the step's first kernel being ready to its last kernel finishing, including time shared
-//     with other requests) is collected for p50/p99.
-// Each request is an independent simulation with its own buffers, so its results do not depend
-// on what else is resident (tested: alone vs in the mix).  Host-side failures (a request that
-// does not fit the budget at all, allocation failure, invalid input) are reported per request.
+//   - tick() (1) collects the steps that completed and retires requests whose last step has
+//     completed: their density is copied to the caller's host buffer and their device memory is
+//     freed; (2) admits queued requests in arrival order while the device-memory budget and the
+//     slot limit allow; (3) issues the next step of every active request, in one of two forms:
+//       STREAMS (default): each request's own step (its captured graph of single-grid kernels,
+//         with the blocked sweep kernel) on its own stream, so the requests' kernels overlap;
+//         latency = device time of the request's step, events on its stream;
+//       GROUPED: ONE grouped step over every active request (one persistent launch per stage
+//         over all the requests' grids, kernels_group.cu), so the requests share every launch;
+//         latency = device time of that step, for every member;
+//     a request admitted now joins the next step.  Up to two steps per request (STREAMS) or per
+//     server (GROUPED) are in flight, so the host prepares the next step while the device runs.
+// Each request is an independent simulation with its own buffers, and the grouped kernels give
+// every grid the results it gets alone (tested: alone vs in the mix).  Host-side failures (a
+// request that does not fit the budget at all, allocation failure, invalid input) are reported
+// per request.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -24,6 +29,7 @@
 #include <vector>
 
 #include "../../include/smoke_gb300.h"
+#include "group.h"
 #include "sim_internal.h"
 
 namespace {
@@ -49,11 +55,18 @@ struct Request {
     int error = SMK_OK;
     size_t bytes = 0;
     smk_sim* sim = nullptr;
+    // STREAMS form: the request's own stream and two step slots (issue / collect)
     cudaStream_t stream = nullptr;
     cudaEvent_t ev_start[2] = {nullptr, nullptr};
     cudaEvent_t ev_end[2] = {nullptr, nullptr};
     bool pending[2] = {false, false};
-    double admit_time = 0.0;
+};
+
+// One issued server step: its events and the requests it advanced.
+struct TickRec {
+    cudaEvent_t start = nullptr, end = nullptr;
+    std::vector<Request*> members;
+    bool pending = false;
 };
 
 size_t footprint(int nx, int ny, int nz) {
@@ -77,20 +90,60 @@ struct smk_server {
     double cell_updates = 0.0;
     long long steps_completed = 0;
     int requests_completed = 0;
+    int mode = SMK_SERVE_STREAMS;
+    bool started = false;  // the form is fixed once a request was admitted
+    cudaStream_t stream = nullptr;
+    GroupRunner* runner = nullptr;
+    smk::GroupSchedule sched{0, 4, 0};
+    TickRec ticks[2];
+    int tick_next = 0;
 };
 
 extern "C" {
 
 const char* smk_server_last_error(void) { return g_srv_err.c_str(); }
 
+static void destroy_server(smk_server* s) {
+    if (s->stream) cudaStreamSynchronize(s->stream);
+    for (Request* r : s->all) {
+        if (r->sim) smk_destroy(r->sim);
+        for (int k = 0; k < 2; ++k) {
+            if (r->ev_start[k]) cudaEventDestroy(r->ev_start[k]);
+            if (r->ev_end[k]) cudaEventDestroy(r->ev_end[k]);
+        }
+        if (r->stream) cudaStreamDestroy(r->stream);
+        delete r;
+    }
+    for (TickRec& t : s->ticks) {
+        if (t.start) cudaEventDestroy(t.start);
+        if (t.end) cudaEventDestroy(t.end);
+    }
+    if (s->runner) group_runner_destroy(s->runner);
+    if (s->stream) cudaStreamDestroy(s->stream);
+    delete s;
+}
+
 int smk_server_create(size_t budget_bytes, int max_active, smk_server** out) {
     if (!out || budget_bytes == 0 || max_active < 1) return sfail(SMK_ERR_INVALID, "bad server limits");
+    *out = nullptr;
     smk_server* s = new smk_server();
     s->budget = budget_bytes;
     s->max_active = max_active;
     cudaGetDevice(&s->device);
     *out = s;
     return SMK_OK;
+}
+
+// The server's stream, step events and grouped-step runner, created with the first step.
+static int ensure_device_state(smk_server* s) {
+    if (s->runner) return SMK_OK;
+    bool ok = s->stream || cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) == cudaSuccess;
+    for (TickRec& t : s->ticks) {
+        ok = ok && (t.start || cudaEventCreate(&t.start) == cudaSuccess);
+        ok = ok && (t.end || cudaEventCreate(&t.end) == cudaSuccess);
+    }
+    if (ok) s->runner = group_runner_create();
+    return ok && s->runner ? SMK_OK : sfail(SMK_ERR_CUDA, "server stream/event creation failed");
 }
 
 static void release_request(smk_server* s, Request* r) {
@@ -108,14 +161,17 @@ static void release_request(smk_server* s, Request* r) {
     r->stream = nullptr;
 }
 
+int smk_server_set_mode(smk_server* s, int mode) {
+    if (!s) return sfail(SMK_ERR_INVALID, "server is null");
+    if (mode != SMK_SERVE_STREAMS && mode != SMK_SERVE_GROUPED) return sfail(SMK_ERR_INVALID, "unknown serving form");
+    if (s->started && mode != s->mode) return sfail(SMK_ERR_INVALID, "the serving form is fixed once requests run");
+    s->mode = mode;
+    return SMK_OK;
+}
+
 int smk_server_destroy(smk_server* s) {
     if (!s) return sfail(SMK_ERR_INVALID, "server is null");
-    cudaDeviceSynchronize();
-    for (Request* r : s->all) {
-        release_request(s, r);
-        delete r;
-    }
-    delete s;
+    destroy_server(s);
     return SMK_OK;
 }
 
@@ -150,15 +206,19 @@ int smk_server_submit(smk_server* s, const smk_request_desc* d, int* id) {
     return SMK_OK;
 }
 
-// Collect the latency of a finished step (slot k) of request r.
-static void collect(smk_server* s, Request* r, int k) {
-    if (!r->pending[k]) return;
+// A completed server step: its device time is each member's step latency.
+static void collect(smk_server* s, TickRec& t) {
+    if (!t.pending) return;
     float ms = 0.0f;
-    if (cudaEventElapsedTime(&ms, r->ev_start[k], r->ev_end[k]) == cudaSuccess) s->latencies_ms.push_back(ms);
-    r->pending[k] = false;
-    r->steps_done++;
-    s->steps_completed++;
-    s->cell_updates += (double)r->nx * r->ny * r->nz;
+    const bool timed = cudaEventElapsedTime(&ms, t.start, t.end) == cudaSuccess;
+    for (Request* r : t.members) {
+        if (timed) s->latencies_ms.push_back(ms);
+        r->steps_done++;
+        s->steps_completed++;
+        s->cell_updates += (double)r->nx * r->ny * r->nz;
+    }
+    t.members.clear();
+    t.pending = false;
 }
 
 static int admit(smk_server* s, Request* r) {
@@ -177,11 +237,11 @@ static int admit(smk_server* s, Request* r) {
         const float* o = &r->obstacles[7 * k];
         rc = smk_add_obstacle(r->sim, o[0], o[1], o[2], o[3], o[4], o[5], o[6], nullptr);
     }
-    if (rc == SMK_OK && cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking) != cudaSuccess)
-        rc = SMK_ERR_CUDA;
-    for (int k = 0; rc == SMK_OK && k < 2; ++k) {
-        if (cudaEventCreate(&r->ev_start[k]) != cudaSuccess || cudaEventCreate(&r->ev_end[k]) != cudaSuccess)
-            rc = SMK_ERR_CUDA;
+    if (rc == SMK_OK && s->mode == SMK_SERVE_STREAMS) {
+        if (cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking) != cudaSuccess) rc = SMK_ERR_CUDA;
+        for (int k = 0; rc == SMK_OK && k < 2; ++k)
+            if (cudaEventCreate(&r->ev_start[k]) != cudaSuccess || cudaEventCreate(&r->ev_end[k]) != cudaSuccess)
+                rc = SMK_ERR_CUDA;
     }
     if (rc == SMK_OK) s->used += r->bytes;
     if (rc != SMK_OK) {
@@ -198,8 +258,20 @@ static int admit(smk_server* s, Request* r) {
     return SMK_OK;
 }
 
-int smk_server_tick(smk_server* s, int* n_active, int* n_queued) {
-    if (!s) return sfail(SMK_ERR_INVALID, "server is null");
+// ---- STREAMS form: every request's own step on its own stream ------------------------------
+
+// Collect the latency of a finished step (slot k) of request r.
+static void collect_req(smk_server* s, Request* r, int k) {
+    if (!r->pending[k]) return;
+    float ms = 0.0f;
+    if (cudaEventElapsedTime(&ms, r->ev_start[k], r->ev_end[k]) == cudaSuccess) s->latencies_ms.push_back(ms);
+    r->pending[k] = false;
+    r->steps_done++;
+    s->steps_completed++;
+    s->cell_updates += (double)r->nx * r->ny * r->nz;
+}
+
+static int tick_streams(smk_server* s) {
     // (1) collect finished steps and retire finished requests.  A request keeps at most one
     // step in flight while the next is issued: the step issued two ticks ago is waited for,
     // the one issued last tick is collected if it has already finished.
@@ -209,13 +281,13 @@ int smk_server_tick(smk_server* s, int* n_active, int* n_queued) {
         const int k_old = (r->steps_issued - 2) & 1;
         if (r->steps_issued >= 2 && r->pending[k_old]) {
             if (cudaEventSynchronize(r->ev_end[k_old]) != cudaSuccess) failed = true;
-            else collect(s, r, k_old);
+            else collect_req(s, r, k_old);
         }
         const int k_new = (r->steps_issued - 1) & 1;
         if (!failed && r->steps_issued >= 1 && r->pending[k_new]) {
             const bool last = r->steps_issued >= r->steps;
             const cudaError_t q = last ? cudaEventSynchronize(r->ev_end[k_new]) : cudaEventQuery(r->ev_end[k_new]);
-            if (q == cudaSuccess) collect(s, r, k_new);
+            if (q == cudaSuccess) collect_req(s, r, k_new);
             else if (q != cudaErrorNotReady) failed = true;
         }
         if (failed) {
@@ -256,7 +328,7 @@ int smk_server_tick(smk_server* s, int* n_active, int* n_queued) {
                 r->state = SMK_REQ_FAILED;
                 continue;
             }
-            collect(s, r, k);
+            collect_req(s, r, k);
         }
         cudaEventRecord(r->ev_start[k], r->stream);
         int rc = smk_step(r->sim, r->dt, r->stream);
@@ -276,9 +348,117 @@ int smk_server_tick(smk_server* s, int* n_active, int* n_queued) {
         else ok.push_back(r);
     }
     s->active.swap(ok);
+    return SMK_OK;
+}
+
+// ---- GROUPED form: one grouped step over every active request --------------------------------
+
+static int tick_grouped(smk_server* s) {
+    // (1) collect completed steps (oldest first); with both slots in flight and nothing else to
+    // do, wait for the older one instead of returning to a host that would spin on tick()
+    const int older = s->tick_next, newer = s->tick_next ^ 1;
+    for (int k : {older, newer}) {
+        TickRec& t = s->ticks[k];
+        if (!t.pending) continue;
+        const cudaError_t q = cudaEventQuery(t.end);
+        if (q == cudaSuccess) collect(s, t);
+        else if (q != cudaErrorNotReady) return sfail(SMK_ERR_CUDA, std::string("server step: ") + cudaGetErrorString(q));
+    }
+    bool work = false;
+    for (Request* r : s->active) work = work || r->steps_issued < r->steps;
+    if (!work && s->queue.empty()) {
+        for (int k : {older, newer}) {
+            TickRec& t = s->ticks[k];
+            if (!t.pending) continue;
+            if (cudaEventSynchronize(t.end) != cudaSuccess) return sfail(SMK_ERR_CUDA, "server step failed");
+            collect(s, t);
+        }
+    }
+    // retire requests whose last step completed
+    std::vector<Request*> still;
+    for (Request* r : s->active) {
+        if (r->steps_done >= r->steps) {
+            int rc = SMK_OK;
+            if (r->out) {
+                rc = smk_read_density(r->sim, r->out, 0, s->stream);
+                if (rc == SMK_OK) rc = smk_sync(r->sim, s->stream);
+            }
+            r->error = rc;
+            r->state = rc == SMK_OK ? SMK_REQ_DONE : SMK_REQ_FAILED;
+            s->requests_completed++;
+            release_request(s, r);
+        } else {
+            still.push_back(r);
+        }
+    }
+    s->active.swap(still);
+    // (2) admit in arrival order while memory and slots allow
+    while (!s->queue.empty() && (int)s->active.size() < s->max_active &&
+           s->used + s->queue.front()->bytes <= s->budget) {
+        Request* r = s->queue.front();
+        s->queue.pop_front();
+        if (admit(s, r) == SMK_OK) s->active.push_back(r);
+    }
+    // (3) one grouped step over every active request with steps left (requests on the
+    // reference projection, which the grouped kernels do not run, step on their own)
+    std::vector<smk_sim*> grouped;
+    std::vector<float> dts;
+    std::vector<Request*> members, single;
+    for (Request* r : s->active) {
+        if (r->steps_issued >= r->steps) continue;
+        members.push_back(r);
+        if (r->params.projection == SMK_PROJECT_PRESSURE) {
+            grouped.push_back(r->sim);
+            dts.push_back(r->dt);
+        } else {
+            single.push_back(r);
+        }
+    }
+    if (!members.empty()) {
+        const int drc = ensure_device_state(s);
+        if (drc) return drc;
+        TickRec& t = s->ticks[s->tick_next];
+        if (t.pending) {  // both slots in flight: the older step must finish first
+            if (cudaEventSynchronize(t.end) != cudaSuccess) return sfail(SMK_ERR_CUDA, "server step failed");
+            collect(s, t);
+        }
+        cudaEventRecord(t.start, s->stream);
+        int rc = group_runner_step(s->runner, grouped.data(), dts.data(), (int)grouped.size(), s->sched,
+                                   s->stream, nullptr);
+        for (size_t k = 0; rc == SMK_OK && k < single.size(); ++k) rc = smk_step(single[k]->sim, single[k]->dt, s->stream);
+        cudaEventRecord(t.end, s->stream);
+        if (rc != SMK_OK) {
+            // the step's members cannot continue: report and release them
+            cudaStreamSynchronize(s->stream);
+            std::vector<Request*> ok;
+            for (Request* r : s->active) {
+                if (std::find(members.begin(), members.end(), r) != members.end()) {
+                    r->error = rc;
+                    r->state = SMK_REQ_FAILED;
+                    release_request(s, r);
+                } else {
+                    ok.push_back(r);
+                }
+            }
+            s->active.swap(ok);
+        } else {
+            for (Request* r : members) r->steps_issued++;
+            t.members = members;
+            t.pending = true;
+            s->tick_next ^= 1;
+        }
+    }
+    return SMK_OK;
+}
+
+int smk_server_tick(smk_server* s, int* n_active, int* n_queued) {
+    if (!s) return sfail(SMK_ERR_INVALID, "server is null");
+    DeviceGuard dg(s->device);
+    if (!s->queue.empty()) s->started = true;
+    const int rc = s->mode == SMK_SERVE_GROUPED ? tick_grouped(s) : tick_streams(s);
     if (n_active) *n_active = (int)s->active.size();
     if (n_queued) *n_queued = (int)s->queue.size();
-    return SMK_OK;
+    return rc;
 }
 
 int smk_server_request_status(smk_server* s, int id, int* state, int* steps_done, int* error) {

@@ -307,6 +307,26 @@ int smk_sim::enqueue(float dt, cudaStream_t st) {
     return SMK_OK;
 }
 
+int smk_sim::prepare_mask(cudaStream_t st) {
+    int n = 0;
+    std::vector<ObstacleObj> obstacles;
+    for (const auto& o : objects)
+        if (o.kind == OBJ_OBSTACLE) obstacles.push_back(o.obstacle);
+    if (!obstacles.empty() && (obstacles_dirty || mask_dirty)) {
+        launch_fill_obstacles(g, s, obstacles.data(), (int)obstacles.size(), st);
+        ++n;
+        mask_dirty = true;
+    }
+    obstacles_dirty = false;
+    if (mask_dirty) {
+        launch_build_flags(g, s, flags, P, st);
+        ++n;
+        mask_dirty = false;
+    }
+    launches += n;
+    return n;
+}
+
 // Everything the step's kernels bake in as launch parameters: a captured graph is reused only
 // while all of it is unchanged.
 std::string smk_sim::graph_signature(float dt) const {

@@ -113,4 +113,18 @@ struct smk_sim {
     int step(float dt, cudaStream_t st);
     int enqueue(float dt, cudaStream_t st);
     std::string graph_signature(float dt) const;
+    // The one-off part of a step after a mask or obstacle change (fillObstacle, neighbour
+    // flags), as enqueue issues it; used before a grouped step.  Returns the kernels launched.
+    int prepare_mask(cudaStream_t st);
 };
+
+// ---- grouped steps over many simulations (batch.cpp) -----------------------------------------
+namespace smk { struct GroupSchedule; }
+struct GroupRunner;
+GroupRunner* group_runner_create();
+void group_runner_destroy(GroupRunner* r);
+// One grouped step of `n` simulations (dts[i] each) on `st` with direct launches; the
+// per-step tables come from a ring of device buffers recycled once their step completed.
+// Members must use the PRESSURE projection.  *kernels (may be NULL) receives the launches.
+int group_runner_step(GroupRunner* r, smk_sim* const* sims, const float* dts, int n,
+                      const smk::GroupSchedule& sched, cudaStream_t st, int* kernels);

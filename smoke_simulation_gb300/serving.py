@@ -56,6 +56,7 @@ def _bind():
             ("smk_server_request_status", i, [vp, i, C.POINTER(i), C.POINTER(i), C.POINTER(i)]),
             ("smk_server_get_stats", i, [vp, C.POINTER(ServerStats)]),
             ("smk_server_destroy", i, [vp]),
+            ("smk_server_set_mode", i, [vp, i]),
             ("smk_server_last_error", C.c_char_p, [])):
         fn = getattr(L, name)
         fn.restype = res
@@ -70,13 +71,19 @@ def _srv_check(rc: int):
         raise SmokeError(rc, _bind().smk_server_last_error().decode())
 
 
-class Server:
-    """Resident simulations with continuous admission (see smk_server_tick)."""
+SERVE_STREAMS, SERVE_GROUPED = 0, 1
 
-    def __init__(self, budget_bytes: int = 120 * 10**9, max_active: int = 64):
+
+class Server:
+    """Resident simulations with continuous admission (see smk_server_tick).  mode: STREAMS
+    (each request's own kernels on its own stream) or GROUPED (one grouped step per tick)."""
+
+    def __init__(self, budget_bytes: int = 120 * 10**9, max_active: int = 64, mode: int = SERVE_STREAMS):
         L = _bind()
         self.h = C.c_void_p()
         _srv_check(L.smk_server_create(budget_bytes, max_active, C.byref(self.h)))
+        if mode != SERVE_STREAMS:
+            _srv_check(L.smk_server_set_mode(self.h, int(mode)))
         self._keep = {}
         self.outputs = {}
 

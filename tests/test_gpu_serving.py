@@ -1,5 +1,6 @@
-"""GPU tests of the serving loop: continuous admission, overlap on the device, and each
-request's result identical alone and in the mix."""
+"""GPU tests of the serving loop in both forms (per-request streams, one grouped step per tick):
+continuous admission, overlap on the device, and each request's result identical alone and in
+the mix."""
 import numpy as np
 import pytest
 
@@ -25,9 +26,10 @@ def _alone(sc, steps):
     return rho
 
 
-def test_results_same_alone_and_in_the_mix(gpu):
+@pytest.mark.parametrize("mode", [SV.SERVE_STREAMS, SV.SERVE_GROUPED])
+def test_results_same_alone_and_in_the_mix(gpu, mode):
     reqs = _requests()
-    srv = SV.Server(budget_bytes=10**10, max_active=3)  # 3 slots: later requests queue
+    srv = SV.Server(budget_bytes=10**10, max_active=3, mode=mode)  # 3 slots: later requests queue
     ids = [srv.submit(sc, steps) for sc, steps in reqs]
     seen_queue = False
     for _ in range(10000):
@@ -48,11 +50,12 @@ def test_results_same_alone_and_in_the_mix(gpu):
     srv.close()
 
 
-def test_memory_budget_admission(gpu):
+@pytest.mark.parametrize("mode", [SV.SERVE_STREAMS, SV.SERVE_GROUPED])
+def test_memory_budget_admission(gpu, mode):
     reqs = _requests()[:3]
     big = max(sc.nx for sc, _ in reqs)
     one = int(1.5 * ((big + 1 + 15) // 16 * 16) * (big + 1) ** 2 * 46) + (1 << 20)
-    srv = SV.Server(budget_bytes=one, max_active=8)  # memory for about one request at a time
+    srv = SV.Server(budget_bytes=one, max_active=8, mode=mode)  # memory for about one request at a time
     ids = [srv.submit(sc, steps) for sc, steps in reqs]
     max_active = 0
     for _ in range(10000):
