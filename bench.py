@@ -12,6 +12,10 @@ Synthetic inputs from smoke_simulation_gb300.scenes (the reference publishes no 
           per-cell model in the design doc, over its event-timed duration in the timed steps
   cpu_baseline  the reference's own step built for the host (OpenMP, all cores) on a bounded
           sample of the same workload
+  forms   the chosen forms beside the plain step: 64 uneven grids in the grouped batch form
+          (FP32 and BF16 velocities), the 512^3 mixed-precision step, and the Poisson serving
+          stream with p50/p99 step latency, each against the plain FP32 form (one grid at a
+          time, pressure restarted from zero every step) on the same grids
 
 Multi-GPU: the path does not shard (one grid per simulation); under torchrun every rank runs an
 independent replica ("replicas only") and value is the sum over ranks with max-over-ranks time.
@@ -73,7 +77,7 @@ class ClockSampler:
             self.file = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=self.file, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
@@ -227,7 +231,7 @@ def run_reference_arm(args, ws, rank):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=300)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=N_DEFAULT)
@@ -238,6 +242,14 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=0, help="0: same as --steps")
     ap.add_argument("--cold-steps", type=int, default=10,
                     help="timed steps of the zero-pressure-start form (0: skip)")
+    ap.add_argument("--forms-steps", type=int, default=10, help="timed steps of the batched/mixed forms")
+    ap.add_argument("--mixed-n", type=int, default=512, help="mixed-precision grid side (0: skip)")
+    ap.add_argument("--serve-requests", type=int, default=16, help="serving stream length (0: skip)")
+    ap.add_argument("--no-forms", action="store_true", help="skip the batched/mixed/serving forms")
+    ap.add_argument("--sweep-kernel", default="", help="D,Z: blocked sweep depth and z-chunk instead "
+                    "of the autotuner's choice (to profile the configuration a timed run chose)")
+    ap.add_argument("--batch-schedule", default="", help="C,Z,W: grouped projection schedule instead of "
+                    "the autotuner's choice")
     args = ap.parse_args()
     assert args.warmup >= 0 and args.steps >= 1
 
@@ -256,7 +268,12 @@ def main():
     sim = smk.from_scene(sc, report_div=1)
     stream = torch.cuda.Stream()
     sh = stream.cuda_stream
-    depth, zchunk, tuned_us = sim.autotune()
+    if args.sweep_kernel:
+        depth, zchunk = (int(x) for x in args.sweep_kernel.split(","))
+        sim.set_sweep_kernel(depth, zchunk)
+        tuned_us = None
+    else:
+        depth, zchunk, tuned_us = sim.autotune()
 
     # warm-up steps (part of the simulation; state evolves; steady steps replay a CUDA graph)
     for _ in range(max(args.warmup, 0)):
@@ -315,7 +332,7 @@ def main():
     if os.path.exists(tf) and depth > 0:
         with open(tf) as f:
             tr = json.load(f)
-        if tr.get("kernel") == "k_sweep_tb<%d>" % depth:
+        if tr.get("kernel") == "k_sweep_tb<%d>" % depth and tr.get("zchunk") == zchunk:
             traffic = tr["bytes_per_cell_per_sweep"] * sweeps_per_launch * sc.cells
 
     # ---- e2e through the public API with host buffers ----------------------------------------
@@ -370,6 +387,12 @@ def main():
                          "on the GPU in this run), %.1f s" % (args.cpu_steps, args.n, ref_sweeps,
                                                              secs)}
 
+    forms = None
+    if rank == 0 and ws == 1 and not args.no_forms:
+        sim.close()
+        sim = None
+        forms = run_forms(args, smk, torch)
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
@@ -401,13 +424,154 @@ def main():
                     "d2h_bytes_per_step": 4 * sc.cells, "api": "smk_simulate (pinned host out)"},
             "gpu_launches": int(launches),
             "cpu_baseline": cpu,
+            "forms": forms,
         }
         print(json.dumps(line))
-    sim.close()
+    if sim is not None:
+        sim.close()
     if ws > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
     return 0
+
+
+def _timed_steps(step, stream, steps, torch):
+    """CUDA-event time (s) of `steps` calls of step() on `stream`."""
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / 1e3
+
+
+def _rel_l2(a, b) -> float:
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def run_forms(args, smk, torch):
+    """The chosen forms next to the plain one (rank 0, one GPU): a batch of 64 uneven grids in the
+    grouped form, the 512^3 mixed-precision step, and the Poisson serving stream.  "Plain" is
+    the FP32 step of one grid at a time with the pressure restarted from zero every step (the
+    reference's projection), on the same grids; every form solves to max|div u| <= 1e-4."""
+    from smoke_simulation_gb300 import scenes as S
+    from smoke_simulation_gb300 import serving as SV
+    stream = torch.cuda.Stream()
+    sh = stream.cuda_stream
+    forms = {}
+
+    # ---- batched: 64 grids, side log-uniform 32..128 (seed 2) --------------------------------
+    scs = S.config_batched(count=64, steps=args.forms_steps)
+    for sc in scs:
+        sc.tol, sc.check_every, sc.iterations, sc.warm_start = 1e-4, 6, 200, 1
+    cells = float(sum(sc.cells for sc in scs))
+    batched = {}
+    dens = {}
+    for name, storage in (("f32", smk.STORAGE_F32), ("bf16", smk.STORAGE_BF16_VEL)):
+        sims = [smk.from_scene(sc, report_div=1, storage=storage) for sc in scs]
+        b = smk.Batch(sims, mode=smk.BATCH_GROUPED)
+        b.step(scs[0].dt, sh)
+        torch.cuda.synchronize()
+        if args.batch_schedule:
+            b.set_schedule(*(int(x) for x in args.batch_schedule.split(",")))
+            sched_us = None
+        else:
+            sched_us = b.autotune()[1]
+        for _ in range(args.warmup):
+            b.step(scs[0].dt, sh)
+        _, l0 = b.info()
+        secs = _timed_steps(lambda: b.step(scs[0].dt, sh), stream, args.forms_steps, torch)
+        _, l1 = b.info()
+        st = [s.stats() for s in sims]
+        batched[name] = {"value": cells * args.forms_steps / secs, "ms_per_step": 1e3 * secs / args.forms_steps,
+                         "mean_sweeps": float(np.mean([x.sweeps for x in st])),
+                         "max_div_post_projection": float(max(x.div_max for x in st)),
+                         "launches_per_step": (l1 - l0) / args.forms_steps,
+                         "schedule": {"ctas_per_sm_zslab_wavebytes": b.schedule(),
+                                      "tuned_us_per_sweep": sched_us}}
+        dens[name] = [s.read_density() for s in sims]
+        b.close()
+        for s in sims:
+            s.close()
+    batched["bf16"]["density_rel_l2_vs_f32_max"] = max(_rel_l2(a, r) for a, r in zip(dens["bf16"], dens["f32"]))
+    # plain: the same grids one at a time, FP32, pressure from zero each step
+    sims = [smk.from_scene(sc, warm_start=0) for sc in scs]
+    for s in sims:
+        s.autotune()
+    for _ in range(args.warmup):
+        for s, sc in zip(sims, scs):
+            s.step(sc.dt, sh)
+    secs = _timed_steps(lambda: [s.step(sc.dt, sh) for s, sc in zip(sims, scs)], stream, args.forms_steps, torch)
+    plain = {"value": cells * args.forms_steps / secs, "ms_per_step": 1e3 * secs / args.forms_steps,
+             "mean_sweeps": float(np.mean([s.stats().sweeps for s in sims]))}
+    for s in sims:
+        s.close()
+    forms["batched"] = {"workload": "64 grids, cube side log-uniform 32..128 (seed 2), sphere solid + box "
+                                    "emitter each, dt=0.05, warm-started pressure to max|div|<=1e-4; "
+                                    "one persistent launch per stage over all grids (grouped form), "
+                                    "CUDA-graph replay, schedule from the autotuner",
+                        "cells": cells, "steps": args.forms_steps, "grouped": batched, "plain": plain,
+                        "grouped_bf16_vs_plain": batched["bf16"]["value"] / plain["value"],
+                        "grouped_f32_vs_plain": batched["f32"]["value"] / plain["value"]}
+
+    # ---- mixed precision at 512^3 -------------------------------------------------------------
+    if args.mixed_n > 0:
+        sc = S.config_mixed(args.mixed_n, steps=args.forms_steps)
+        sc.warm_start = 1
+        mixed = {}
+        rho = {}
+        for name, storage in (("f32", smk.STORAGE_F32), ("bf16_vel", smk.STORAGE_BF16_VEL),
+                              ("bf16_all", smk.STORAGE_BF16)):
+            sim = smk.from_scene(sc, report_div=1, storage=storage)
+            sim.autotune()
+            sim.step(sc.dt, sh)  # mask upload step (direct launches)
+            secs = _timed_steps(lambda: sim.step(sc.dt, sh), stream, args.forms_steps - 1, torch)
+            st = sim.stats()
+            mixed[name] = {"value": float(sc.cells) * (args.forms_steps - 1) / secs,
+                           "ms_per_step": 1e3 * secs / (args.forms_steps - 1), "sweeps_last": st.sweeps,
+                           "max_div_post_projection": st.div_max}
+            rho[name] = sim.read_density()
+            sim.close()
+        for name in ("bf16_vel", "bf16_all"):
+            mixed[name]["density_rel_l2_vs_f32"] = _rel_l2(rho[name], rho["f32"])
+        forms["mixed"] = {"workload": "%d^3, 2%% random solids (seed 3), one 32x8x32 emitter, dt=0.02, "
+                                      "warm-started FP32 pressure red-black SOR to max|div|<=1e-4 (checked every "
+                                      "10 sweeps), %d steps; bf16_vel = u,v,w in BF16 + density FP32, bf16_all = "
+                                      "density too; errors vs the FP64 oracle are tested at 80^3"
+                                      % (args.mixed_n, args.forms_steps),
+                          "cells": float(sc.cells), **mixed}
+
+    # ---- serving: Poisson stream, continuous admission ----------------------------------------
+    if args.serve_requests > 0:
+        arr = SV.poisson_stream(args.serve_requests)
+        srv = SV.Server(budget_bytes=120 * 10**9, max_active=64)
+        wall, _ = SV.drive(srv, arr, storage=smk.STORAGE_BF16_VEL)
+        st = srv.stats()
+        serve = {"value": st.cell_updates / wall, "wall_s": wall, "p50_step_ms": st.p50_step_ms,
+                 "p99_step_ms": st.p99_step_ms, "max_step_ms": st.max_step_ms,
+                 "requests": st.requests_completed, "steps": st.steps_completed}
+        srv.close()
+        srv = SV.Server(budget_bytes=120 * 10**9, max_active=1)
+        wall1, _ = SV.drive(srv, arr, warm_start=0)
+        st1 = srv.stats()
+        plain1 = {"value": st1.cell_updates / wall1, "wall_s": wall1, "p50_step_ms": st1.p50_step_ms,
+                  "p99_step_ms": st1.p99_step_ms}
+        srv.close()
+        forms["serving"] = {"workload": "%d requests, Poisson 200/s (seed 4), cube side log-uniform 48..192, "
+                                        "50..500 steps, sphere solid + box emitter, tol 1e-4; served with "
+                                        "u,v,w in BF16 (density FP32), warm-started pressure, up to 64 "
+                                        "resident (120 GB budget), each request's step on its own stream; "
+                                        "plain = the same stream one request at a time, FP32, pressure "
+                                        "from zero each step; cell-updates/s over host wall time"
+                                        % args.serve_requests,
+                            "served": serve, "plain_one_at_a_time": plain1,
+                            "served_vs_plain": serve["value"] / plain1["value"]}
+    return forms
 
 
 def sim_bytes(sc) -> float:
