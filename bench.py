@@ -2,8 +2,11 @@
 
 Workload (one "step" = one full simulation step of one 256^3 grid): FP32 fields, 5% Bernoulli
 solids (seed 1) plus two r=24 spheres, four seeded sphere emitters, dt = 0.02, pressure-form
-red-black SOR to max|residual| <= 1e-4 checked every 6 sweeps, capped at 200 sweeps.
-Synthetic inputs from smoke_simulation_gb300.scenes (the reference publishes no dataset).
+red-black SOR to max|residual| <= 1e-4 checked every 6 sweeps, capped at 200 sweeps, 50 steps.
+Synthetic inputs from smoke_simulation_gb300.scenes (the reference publishes no dataset).  The
+K timed steps are the 50-step workload run from its initial fields K/50 times (the fields are
+written back between runs, outside the timed events), so every timed step is a step of the
+configured workload rather than of an ever longer simulation.
 
   value   cell-updates/s with the state resident in HBM (CUDA events on the step stream)
   e2e     the same metric through smk_simulate (the reference's simulate(): step plus a
@@ -231,7 +234,7 @@ def run_reference_arm(args, ws, rank):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=N_DEFAULT)
@@ -240,7 +243,7 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=0, help="0: same as --steps")
-    ap.add_argument("--cold-steps", type=int, default=10,
+    ap.add_argument("--cold-steps", type=int, default=50,
                     help="timed steps of the zero-pressure-start form (0: skip)")
     ap.add_argument("--forms-steps", type=int, default=10, help="timed steps of the batched/mixed forms")
     ap.add_argument("--mixed-n", type=int, default=512, help="mixed-precision grid side (0: skip)")
@@ -266,6 +269,8 @@ def main():
 
     sc = workload(args.n)
     sim = smk.from_scene(sc, report_div=1)
+    initial = sim.read_state()  # the workload's initial fields; every timed segment starts here
+    seg = sc.steps              # the workload is sc.steps (50) steps long
     stream = torch.cuda.Stream()
     sh = stream.cuda_stream
     if args.sweep_kernel:
@@ -275,35 +280,43 @@ def main():
     else:
         depth, zchunk, tuned_us = sim.autotune()
 
-    # warm-up steps (part of the simulation; state evolves; steady steps replay a CUDA graph)
+    # warm-up steps (graph capture, caches); the timed segments restart from the initial state
     for _ in range(max(args.warmup, 0)):
         sim.step(sc.dt, sh)
     torch.cuda.synchronize()
 
-    # ---- device-timed region: K steps, inputs resident in HBM ------------------------------
-    launches0 = sim.launch_count()
-    sweeps, divs, conv, sweep_ms, proj_ms = [], [], [], [], []
+    def segments(total):
+        """Lengths of the timed segments: the workload's steps from its initial state, repeated."""
+        out = []
+        while total > 0:
+            out.append(min(seg, total))
+            total -= out[-1]
+        return out
+
+    # ---- device-timed region: K steps (segments of the 50-step workload), state in HBM --------
+    # before each segment the initial fields are written back (outside the timed events; this
+    # also restarts the pressure history, as a new simulation has none)
+    launches = 0
+    elapsed = 0.0
     clocks = ClockSampler(local)
     clocks.start()
-    dist_barrier(ws)
-    torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        sim.step(sc.dt, sh)
-    e1.record(stream)
-    torch.cuda.synchronize()
+    for n in segments(args.steps):
+        sim.write_state(initial)
+        launches0 = sim.launch_count()
+        dist_barrier(ws)
+        torch.cuda.synchronize()
+        elapsed += _timed_steps(lambda: sim.step(sc.dt, sh), stream, n, torch)
+        launches += sim.launch_count() - launches0
     dist_barrier(ws)
     clk = clocks.stop()
-    elapsed = e0.elapsed_time(e1) / 1e3
-    launches = sim.launch_count() - launches0
 
-    # per-step statistics and stage times: the next few steps of the same simulation, with a
-    # sync after each (outside the timed region) to read the solver status and the sweep phase
-    # timed by CUDA events on the step stream (these steps launch directly, not as a graph)
+    # per-step statistics and stage times: one more pass over the workload's steps with a sync
+    # after each (outside the timed region) to read the solver status and the sweep phase timed
+    # by CUDA events on the step stream (these steps launch directly, not as a graph)
+    sweeps, divs, conv, sweep_ms = [], [], [], []
+    sim.write_state(initial)
     sim.set_timing(True)
-    for _ in range(min(args.steps, 5)):
+    for _ in range(seg):
         sim.step(sc.dt, sh)
         st = sim.stats()
         t = sim.stage_times()
@@ -311,6 +324,7 @@ def main():
         divs.append(st.div_max)
         conv.append(st.converged)
         sweep_ms.append(float(t[5]))
+    sim.set_timing(False)
     elapsed_max = dist_max(elapsed, ws)
     cells_all = dist_sum(float(sc.cells * args.steps), ws)
     value = cells_all / elapsed_max
@@ -326,7 +340,6 @@ def main():
     bytes_per_launch = sc.cells * SWEEP_BYTES_PER_CELL * sweeps_per_launch
     launch_seconds = float(np.mean(sweep_ms)) / 1e3 / launches_run
     achieved = bytes_per_launch / launch_seconds / 1e9 if launch_seconds > 0 else None
-    sweep_bytes = bytes_per_launch * launches_run
     traffic = None
     tf = os.path.join(ROOT, "profiles", "sweep_traffic.json")
     if os.path.exists(tf) and depth > 0:
@@ -338,41 +351,39 @@ def main():
     # ---- e2e through the public API with host buffers ----------------------------------------
     e2e_steps = args.e2e_steps or args.steps
     out = torch.empty(sc.cell_shape, dtype=torch.float32, pin_memory=True).numpy()
-    sim.set_timing(False)
-    sim.simulate(out, sc.dt)  # warm
-    dist_barrier(ws)
-    t0 = time.perf_counter()
-    for k in range(e2e_steps):
-        # the step's input: the emitter positions (launch parameters); result: the density
-        sim.simulate(out, sc.dt)
-    e2e_dt = dist_max(time.perf_counter() - t0, ws)
+    e2e_dt = 0.0
+    for n in segments(e2e_steps):
+        sim.write_state(initial)
+        dist_barrier(ws)
+        t0 = time.perf_counter()
+        for _ in range(n):
+            # the step's input: the emitter positions (launch parameters); result: the density
+            sim.simulate(out, sc.dt)
+        e2e_dt += time.perf_counter() - t0
+    e2e_dt = dist_max(e2e_dt, ws)
     e2e_value = dist_sum(float(sc.cells * e2e_steps), ws) / e2e_dt
 
     # ---- the same solve from a zero pressure every step (the reference's iteration) ---------
-    # continues the same simulation with warm start off: 2 steps to settle, then timed steps
     cold = None
     if args.cold_steps > 0:
         sim.set_params(warm_start=0)
-        for _ in range(2):
+        cold_s = 0.0
+        for n in segments(args.cold_steps):
+            sim.write_state(initial)
+            cold_s += _timed_steps(lambda: sim.step(sc.dt, sh), stream, n, torch)
+        sim.write_state(initial)
+        cold_sweeps, cold_conv = [], []
+        for _ in range(min(seg, args.cold_steps)):
             sim.step(sc.dt, sh)
-        torch.cuda.synchronize()
-        c0 = torch.cuda.Event(enable_timing=True)
-        c1 = torch.cuda.Event(enable_timing=True)
-        c0.record(stream)
-        for _ in range(args.cold_steps):
-            sim.step(sc.dt, sh)
-        c1.record(stream)
-        torch.cuda.synchronize()
-        cold_s = c0.elapsed_time(c1) / 1e3
-        cold_sweeps = []
-        for _ in range(2):
-            sim.step(sc.dt, sh)
-            cold_sweeps.append(sim.stats().sweeps)
+            st = sim.stats()
+            cold_sweeps.append(st.sweeps)
+            cold_conv.append(st.converged)
         cold = {"value": dist_sum(float(sc.cells * args.cold_steps), ws) / dist_max(cold_s, ws),
                 "ms_per_step": 1e3 * cold_s / args.cold_steps,
-                "mean_sweeps": float(np.mean(cold_sweeps)), "steps": args.cold_steps,
+                "mean_sweeps": float(np.mean(cold_sweeps)), "converged_frac": float(np.mean(cold_conv)),
+                "steps": args.cold_steps,
                 "note": "pressure restarted from zero every step, as the reference's projection "
-                        "does; same tolerance rule"}
+                        "does; same tolerance rule; the first steps of the workload"}
 
     # ---- CPU baseline (rank 0, N=1 only) -------------------------------------------------------
     cpu = None
@@ -404,6 +415,9 @@ def main():
                                    "max|div|<=1e-4 "
                                    "(checked every 6 sweeps, cap 200)" % args.n,
                        "cells": sc.cells, "parallelism": "replicas" if ws > 1 else "single",
+                       "timed_steps": "%d steps: the %d-step workload from its initial fields, "
+                                      "%d time(s) (fields written back between segments, outside "
+                                      "the timed events)" % (args.steps, seg, len(segments(args.steps))),
                        "l2": "inputs larger than L2 (%.0f MB resident state)" % (
                            sim_bytes(sc) / 1e6),
                        "mean_sweeps": mean_sweeps, "converged_frac": float(np.mean(conv)),

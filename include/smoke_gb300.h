@@ -129,7 +129,10 @@ int smk_simulate(smk_sim* sim, float* host_out, float dt);
 int smk_read_density(smk_sim* sim, float* dst, int dst_on_device, void* stream);
 int smk_sync(smk_sim* sim, void* stream);
 
-/* Full state in the reference layout (checkpoint / resume, parity checks).  Blocking. */
+/* Full state in the reference layout (checkpoint / resume, parity checks).  Blocking.  The
+ * state is the reference's (fields, mask, ping-pong index); writing one also restarts the
+ * PRESSURE projection's warm-start history, so the next step starts from zero pressure as the
+ * first step of a new simulation does. */
 int smk_read_state(smk_sim* sim, const smk_host_state* st);
 int smk_write_state(smk_sim* sim, const smk_host_state* st);
 /* The projected velocities of the last step (buffer "now" after projection) are not kept
@@ -158,6 +161,10 @@ int smk_get_sweep_kernel(const smk_sim* sim, int* depth, int* zchunk);
  * when dt, the parameters, the objects or the sweep kernel change; steps after a mask or
  * obstacle change run directly.  Results are identical either way. */
 int smk_set_graphs(smk_sim* sim, int enable);
+/* In a captured step, run the tolerance groups of the blocked solve as a device-side WHILE loop
+ * (a graph conditional node: no launches after the solve has converged; default on) or as the
+ * unrolled launches up to max_sweeps (later ones exit at entry).  Results are identical. */
+int smk_set_graph_loops(smk_sim* sim, int enable);
 /* Time the blocked sweep kernel's depths and z-chunk sizes on this simulation's buffers and
  * keep the fastest (cached per grid shape and device for the process).  Synchronises; does not
  * change the simulation's results.  Outputs may be NULL; us_per_sweep is -1 on a cache hit.

@@ -95,6 +95,7 @@ def lib() -> C.CDLL:
         "smk_project_noalloc_max_elems": (C.c_longlong, []),
         "smk_autotune": (i, [vp, C.POINTER(i), C.POINTER(i), C.POINTER(f)]),
         "smk_set_graphs": (i, [vp, i]),
+        "smk_set_graph_loops": (i, [vp, i]),
         "smk_batch_create": (i, [i, C.POINTER(vp), C.POINTER(vp)]),
         "smk_batch_step": (i, [vp, C.POINTER(f), f, vp]),
         "smk_batch_destroy": (i, [vp]),
@@ -279,6 +280,9 @@ class Simulation:
 
     def launch_count(self) -> int:
         return int(lib().smk_launch_count(self.h))
+
+    def set_graph_loops(self, enable: bool):
+        _check(lib().smk_set_graph_loops(self.h, 1 if enable else 0))
 
     def set_sweep_kernel(self, depth: int, zchunk: int = 32):
         _check(lib().smk_set_sweep_kernel(self.h, depth, zchunk))

@@ -53,9 +53,17 @@ struct SweepMaps;
 SweepMaps* create_sweep_maps(const Grid& g, const float* Pa, const float* Pb, const float* b,
                              const uint8_t* flags);
 void destroy_sweep_maps(SweepMaps* m);
+// group_base (device, may be NULL): the launch's group index is group + *group_base (a graph's
+// device-side group loop).
 int launch_sweep_tb(const SweepMaps* m, const Grid& g, bool in_is_a, float* Pout, int T, int nhalf,
                     int colour0, int zchunk, const float* wacc7, StepStatus* status, int check,
-                    int group, float tol, int* pcur, int out_idx, int* kerr, cudaStream_t st);
+                    int group, float tol, int* pcur, int out_idx, int* kerr, const int* group_base,
+                    cudaStream_t st);
+// Last node of a device-side group loop's body: counter += step; loop again while the solve is
+// not done and counter < limit; *launches += launches_per_iter.
+void launch_group_loop_next(const StepStatus* status, int* counter, int step, int limit,
+                            unsigned long long* launches, int launches_per_iter,
+                            cudaGraphConditionalHandle handle, cudaStream_t st);
 void launch_div_max(const Grid& g, const float* u, const float* v, const float* w,
                     const uint8_t* flags, StepStatus* status, cudaStream_t st);
 

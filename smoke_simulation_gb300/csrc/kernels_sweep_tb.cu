@@ -27,7 +27,9 @@
 // registers; the loop over z is unrolled by the ring length so every slot is a fixed register.
 // x-neighbours come from the patch or a warp shuffle (a tile row of 32 threads is one warp),
 // y-neighbours from the patch or a shared-memory copy of each in-flight plane, published once
-// per iteration (double-buffered: one barrier per iteration).
+// per iteration (double-buffered: one barrier per iteration).  The published copy keeps the
+// patch's two columns (A = x0, B = x0+1) in separate float planes, so a warp's y-neighbour read
+// (one column) is 32 consecutive floats: one shared-memory wavefront, not two.
 //
 // Every update is  r = fma(-acc, P_c, b_c + (((P_x- + P_x+) + (P_y- + P_y+)) + (P_z- + P_z+)));
 // P_c = fma(omega/acc, r, P_c), the oracle's order, so every launch shape gives the same bits
@@ -139,21 +141,23 @@ template <int T>
 __global__ void __launch_bounds__(TB_TX * TB_TY, 1)
 k_sweep_tb(const __grid_constant__ TBMaps maps, Grid g, float* __restrict__ Pout, int nhalf,
            int colour0, int zchunk, WAcc8 wa, StepStatus* status, int check, int group, float tol,
-           int* __restrict__ pcur, int out_idx, int* __restrict__ kerr) {
+           int* __restrict__ pcur, int out_idx, int* __restrict__ kerr, const int* __restrict__ group_base) {
     constexpr int R = T + 4;                 // register ring length (even, >= T + 3)
     constexpr int TB_S = R / 2;              // TMA stages (planes in flight)
     constexpr int IX = 2 * TB_TX - 2 * T;    // interior columns
     constexpr int IY = ROWS - 2 * T;         // interior rows
-    constexpr int PROW = (TB_TY + 2) * TB_TX;  // float2 per published row set (zero row above/below)
+    constexpr int PROW = (TB_TY + 2) * TB_TX;  // floats per published column plane (zero row above/below)
     extern __shared__ __align__(128) unsigned char smem_raw[];
     // TMA destinations must be 128-byte aligned: align the dynamic base explicitly (the launch
     // requests 128 spare bytes)
     unsigned char* stages = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);  // [S][STAGE_BYTES]
-    // published planes: [2 buffers][T+1 planes][2 rows][TY+2][32] pairs (A, B)
-    float2* pub = reinterpret_cast<float2*>(stages + TB_S * STAGE_BYTES);
+    // published planes: [2 buffers][T+1 planes][2 rows][2 columns A, B][TY+2][32] floats
+    float* pub = reinterpret_cast<float*>(stages + TB_S * STAGE_BYTES);
     __shared__ __align__(8) uint64_t mbar[TB_S];
     __shared__ float2 coef[128];
 
+    // inside a graph's device-side group loop the group index is relative to the loop counter
+    if (group_base != nullptr) group += *group_base;
     if (status != nullptr) {
         if (*(volatile int*)&status->done) return;
         if (check && group > 0 && __uint_as_float(status->rmax_bits[group - 1]) <= tol) {
@@ -173,9 +177,9 @@ k_sweep_tb(const __grid_constant__ TBMaps maps, Grid g, float* __restrict__ Pout
         coef[tid] = make_float2(-(float)acc, (tid & 0x40) ? wa.w[acc] : 0.0f);
     }
     // zero the padding rows of every published plane (never written afterwards)
-    for (int i = tid; i < 2 * (T + 1) * 2 * 2 * TB_TX; i += TB_TX * TB_TY) {
+    for (int i = tid; i < 2 * (T + 1) * 2 * 2 * 2 * TB_TX; i += TB_TX * TB_TY) {
         const int lane = i % TB_TX, edge = (i / TB_TX) % 2, set = i / (2 * TB_TX);
-        pub[set * PROW + (edge ? (TB_TY + 1) * TB_TX : 0) + lane] = make_float2(0.f, 0.f);
+        pub[set * PROW + (edge ? (TB_TY + 1) * TB_TX : 0) + lane] = 0.0f;
     }
     if (pcur != nullptr && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && leader)
         *pcur = out_idx;
@@ -247,13 +251,16 @@ k_sweep_tb(const __grid_constant__ TBMaps maps, Grid g, float* __restrict__ Pout
             }
             // ---- publish planes q-1-s (slot (k-1-s) mod R) for the y-neighbours; the residual
             // plane (s = 0) only in check launches
-            float2* pb = pub + par * (T + 1) * 2 * PROW;
+            // column plane of published plane s, row r (0 = y0, 1 = y0+1), column c (0 = A, 1 = B)
+            float* pb = pub + par * (T + 1) * 4 * PROW;
 #pragma unroll
             for (int s = 0; s <= T; ++s) {
                 if (s > 0 || check) {
                     const int j = (k - 1 - s + 2 * R) % R;
-                    pb[(2 * s) * PROW + me0] = p0[j];
-                    pb[(2 * s + 1) * PROW + me0] = p1[j];
+                    pb[(4 * s + 0) * PROW + me0] = p0[j].x;
+                    pb[(4 * s + 1) * PROW + me0] = p0[j].y;
+                    pb[(4 * s + 2) * PROW + me0] = p1[j].x;
+                    pb[(4 * s + 3) * PROW + me0] = p1[j].y;
                 }
             }
             if (__syncthreads_or(!ok)) {
@@ -282,8 +289,9 @@ k_sweep_tb(const __grid_constant__ TBMaps maps, Grid g, float* __restrict__ Pout
                 const float rA1 = __shfl_down_sync(0xffffffffu, p1[j].x, 1);
                 const int zp = q - 1;
                 if (zp >= za && zp < zb && in0) {
-                    const float2 up = pb[PROW + me0 - TB_TX];  // row y0-1 (thread above, row 1)
-                    const float2 dn = pb[me0 + TB_TX];         // row y0+2 (thread below, row 0)
+                    // row y0-1 (thread above, row 1) and row y0+2 (thread below, row 0)
+                    const float2 up = make_float2(pb[2 * PROW + me0 - TB_TX], pb[3 * PROW + me0 - TB_TX]);
+                    const float2 dn = make_float2(pb[me0 + TB_TX], pb[PROW + me0 + TB_TX]);
                     const unsigned f = ff[j];
                     const unsigned i0 = fidx(f, 0), i1 = fidx(f, 1), i2 = fidx(f, 2), i3 = fidx(f, 3);
                     rmax = max(rmax, resid_bits(p0[j].x, b0[j].x, coef[i0], i0 & 0x40u, lB0, p0[j].y,
@@ -307,13 +315,13 @@ k_sweep_tb(const __grid_constant__ TBMaps maps, Grid g, float* __restrict__ Pout
                     const int j = (k - 1 - t + 2 * R) % R;
                     const int ju = (k - t + 2 * R) % R;
                     const int jd = (k - 2 - t + 2 * R) % R;
-                    const float2* ps = pb + (2 * t) * PROW;
+                    const float* ps = pb + (4 * t) * PROW;
                     const unsigned f = ff[j];
                     if (sA) {
                         const float lB0 = __shfl_up_sync(0xffffffffu, p0[j].y, 1);
                         const float rA1 = __shfl_down_sync(0xffffffffu, p1[j].x, 1);
-                        const float ymA = ps[PROW + me0 - TB_TX].x;  // row y0-1, column A
-                        const float ypB = ps[me0 + TB_TX].y;         // row y0+2, column B
+                        const float ymA = ps[2 * PROW + me0 - TB_TX];  // row y0-1, column A
+                        const float ypB = ps[PROW + me0 + TB_TX];      // row y0+2, column B
                         const unsigned ia = fidx(f, 0), ib = fidx(f, 3);
                         const float nA0 = relax(p0[j].x, b0[j].x, coef[ia], ia & 0x40u, lB0, p0[j].y,
                                                 ymA, p1[j].x, p0[jd].x, p0[ju].x);
@@ -324,8 +332,8 @@ k_sweep_tb(const __grid_constant__ TBMaps maps, Grid g, float* __restrict__ Pout
                     } else {
                         const float rA0 = __shfl_down_sync(0xffffffffu, p0[j].x, 1);
                         const float lB1 = __shfl_up_sync(0xffffffffu, p1[j].y, 1);
-                        const float ymB = ps[PROW + me0 - TB_TX].y;  // row y0-1, column B
-                        const float ypA = ps[me0 + TB_TX].x;         // row y0+2, column A
+                        const float ymB = ps[3 * PROW + me0 - TB_TX];  // row y0-1, column B
+                        const float ypA = ps[me0 + TB_TX];             // row y0+2, column A
                         const unsigned ia = fidx(f, 1), ib = fidx(f, 2);
                         const float nB0 = relax(p0[j].y, b0[j].y, coef[ia], ia & 0x40u, p0[j].x, rA0,
                                                 ymB, p1[j].y, p0[jd].y, p0[ju].y);
@@ -403,7 +411,7 @@ int configure_tb() {
 template <int T>
 int launch_tb(const TBMaps& maps, const Grid& g, float* Pout, int nhalf, int colour0, int zchunk,
               const float* wacc7, StepStatus* status, int check, int group, float tol, int* pcur,
-              int out_idx, int* kerr, cudaStream_t st) {
+              int out_idx, int* kerr, const int* group_base, cudaStream_t st) {
     const size_t smem = tb_smem_bytes<T>();
     WAcc8 wa;
     for (int k = 0; k < 7; ++k) wa.w[k] = wacc7[k];
@@ -412,8 +420,20 @@ int launch_tb(const TBMaps& maps, const Grid& g, float* Pout, int nhalf, int col
     dim3 grid((unsigned)((g.nx + IX - 1) / IX), (unsigned)((g.ny + IY - 1) / IY),
               (unsigned)((g.nz + zchunk - 1) / zchunk));
     k_sweep_tb<T><<<grid, dim3(TB_TX, TB_TY), smem, st>>>(maps, g, Pout, nhalf, colour0, zchunk, wa, status,
-                                                         check, group, tol, pcur, out_idx, kerr);
+                                                         check, group, tol, pcur, out_idx, kerr, group_base);
     return 0;
+}
+
+// End of one iteration of a graph's device-side loop over tolerance groups: advance the group
+// counter and keep looping while the solve is not done and full groups remain.  One thread.
+__global__ void k_group_loop_next(const StepStatus* status, int* counter, int step, int limit,
+                                  unsigned long long* launches, int launches_per_iter,
+                                  cudaGraphConditionalHandle handle) {
+    const int c = *counter + step;
+    *counter = c;
+    *launches += (unsigned long long)launches_per_iter;
+    const bool more = *(volatile const int*)&status->done == 0 && c < limit;
+    cudaGraphSetConditional(handle, more ? 1u : 0u);
 }
 
 }  // namespace
@@ -442,16 +462,23 @@ void destroy_sweep_maps(SweepMaps* m) { delete m; }
 
 int launch_sweep_tb(const SweepMaps* m, const Grid& g, bool in_is_a, float* Pout, int T, int nhalf,
                     int colour0, int zchunk, const float* wacc7, StepStatus* status, int check,
-                    int group, float tol, int* pcur, int out_idx, int* kerr, cudaStream_t st) {
+                    int group, float tol, int* pcur, int out_idx, int* kerr, const int* group_base,
+                    cudaStream_t st) {
     TBMaps maps;
     maps.pin = in_is_a ? m->pa : m->pb;
     maps.b = m->b;
     maps.f = m->f;
     switch (T) {
-        case 2: return launch_tb<2>(maps, g, Pout, nhalf, colour0, zchunk, wacc7, status, check, group, tol, pcur, out_idx, kerr, st);
-        case 4: return launch_tb<4>(maps, g, Pout, nhalf, colour0, zchunk, wacc7, status, check, group, tol, pcur, out_idx, kerr, st);
-        default: return launch_tb<6>(maps, g, Pout, nhalf, colour0, zchunk, wacc7, status, check, group, tol, pcur, out_idx, kerr, st);
+        case 2: return launch_tb<2>(maps, g, Pout, nhalf, colour0, zchunk, wacc7, status, check, group, tol, pcur, out_idx, kerr, group_base, st);
+        case 4: return launch_tb<4>(maps, g, Pout, nhalf, colour0, zchunk, wacc7, status, check, group, tol, pcur, out_idx, kerr, group_base, st);
+        default: return launch_tb<6>(maps, g, Pout, nhalf, colour0, zchunk, wacc7, status, check, group, tol, pcur, out_idx, kerr, group_base, st);
     }
+}
+
+void launch_group_loop_next(const StepStatus* status, int* counter, int step, int limit,
+                            unsigned long long* launches, int launches_per_iter,
+                            cudaGraphConditionalHandle handle, cudaStream_t st) {
+    k_group_loop_next<<<1, 1, 0, st>>>(status, counter, step, limit, launches, launches_per_iter, handle);
 }
 
 }  // namespace smk

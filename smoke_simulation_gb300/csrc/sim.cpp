@@ -96,9 +96,12 @@ int smk_sim::alloc() {
             SMK_CUDA(cudaMemset(*f, 0, n * sizeof(float)));
         }
     }
-    SMK_CUDA(cudaMalloc((void**)&pcur, 2 * sizeof(int)));
-    SMK_CUDA(cudaMemset(pcur, 0, 2 * sizeof(int)));
+    SMK_CUDA(cudaMalloc((void**)&pcur, 4 * sizeof(int)));
+    SMK_CUDA(cudaMemset(pcur, 0, 4 * sizeof(int)));
     kerr = pcur + 1;
+    gcount = pcur + 2;
+    SMK_CUDA(cudaMalloc((void**)&loop_launches, sizeof(unsigned long long)));
+    SMK_CUDA(cudaMemset(loop_launches, 0, sizeof(unsigned long long)));
     SMK_CUDA(cudaMalloc((void**)&s, n));
     SMK_CUDA(cudaMalloc((void**)&flags, n));
     SMK_CUDA(cudaMemset(flags, 0, n));
@@ -111,6 +114,7 @@ int smk_sim::alloc() {
     SMK_CUDA(cudaMalloc((void**)&tune_status, sizeof(StepStatus) + sizeof(unsigned)));
     for (auto& e : ev) SMK_CUDA(cudaEventCreate(&e));
     SMK_CUDA(cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking));
+    SMK_CUDA(cudaStreamCreateWithFlags(&body_stream, cudaStreamNonBlocking));
     if (prepare_sweep_kernels() != 0) return fail(SMK_ERR_CUDA, "sweep kernel configuration failed");
     // initializeVolume's mask: fluid except the y = 0 floor (smokeSimulation.cu:200-207)
     std::vector<uint8_t> host((size_t)g.nx * g.ny * g.nz, 1);
@@ -124,6 +128,7 @@ void smk_sim::release() {
     for (float* f : fl)
         if (f) cudaFree(f);
     if (pcur) cudaFree(pcur);
+    if (loop_launches) cudaFree(loop_launches);
     if (maps) destroy_sweep_maps(maps);
     if (s) cudaFree(s);
     if (flags) cudaFree(flags);
@@ -134,6 +139,7 @@ void smk_sim::release() {
     for (auto& gs : graphs)
         if (gs.exec) cudaGraphExecDestroy(gs.exec);
     if (cap_stream) cudaStreamDestroy(cap_stream);
+    if (body_stream) cudaStreamDestroy(body_stream);
 }
 
 int smk_sim::upload_mask(const uint8_t* host) {
@@ -150,7 +156,14 @@ int smk_sim::enqueue(float dt, cudaStream_t st) {
     const int now = index_now ^ 1;
     index_now = now;
     const bool timed = timing;
-    if (timed) SMK_CUDA(cudaEventRecord(ev[0], st));
+    cudaStreamCaptureStatus cap_status = cudaStreamCaptureStatusNone;
+    SMK_CUDA(cudaStreamIsCapturing(st, &cap_status));
+    const bool capturing = cap_status == cudaStreamCaptureStatusActive;
+    // stage-timing events; inside a capture they become event-record nodes of the graph
+    auto rec = [&](cudaEvent_t e) {
+        return cudaEventRecordWithFlags(e, st, capturing ? cudaEventRecordExternal : cudaEventRecordDefault);
+    };
+    if (timed) SMK_CUDA(rec(ev[0]));
 
     // a4: objects (drawObjects, smokeSimulation.cu:714-771)
     std::vector<BoxObj> boxes;
@@ -183,7 +196,7 @@ int smk_sim::enqueue(float dt, cudaStream_t st) {
         ++launches;
         mask_dirty = false;
     }
-    if (timed) SMK_CUDA(cudaEventRecord(ev[1], st));
+    if (timed) SMK_CUDA(rec(ev[1]));
 
     // b: integrate + velocityConfinement (:789-791)
     if (rho_bf16)
@@ -196,7 +209,7 @@ int smk_sim::enqueue(float dt, cudaStream_t st) {
         launch_forcing(g, u[now], v[now], w[now], (const float*)rho[now], flags, dt, p.gravity, p.buoyancy,
                        p.clamp_const, p.clamp_mode, st);
     ++launches;
-    if (timed) SMK_CUDA(cudaEventRecord(ev[2], st));
+    if (timed) SMK_CUDA(rec(ev[2]));
 
     // c/d: projection (:795-801)
     const size_t status_bytes = sizeof(StepStatus) + sizeof(unsigned) * status_groups;
@@ -222,25 +235,78 @@ int smk_sim::enqueue(float dt, cudaStream_t st) {
         const bool use_tol = p.tol > 0.0f;
         const int G = use_tol ? p.check_every : (p.max_sweeps > 0 ? p.max_sweeps : 1);
         int sweep = 0, group = 0;
-        if (timed) SMK_CUDA(cudaEventRecord(ev[5], st));
+        if (timed) SMK_CUDA(rec(ev[5]));
         if (sweep_depth > 0) {
             // temporally blocked: each launch applies up to sweep_depth colour passes,
             // ping-ponging P <-> P2; group starts are the check launches
             int nl = 0;
-            while (sweep < p.max_sweeps) {
-                const int end = sweep + G < p.max_sweeps ? sweep + G : p.max_sweeps;
-                const int h1 = 2 * end;
-                for (int h = 2 * sweep; h < h1; h += sweep_depth) {
+            // the launches of one group [s0, s1) in sweeps; `grp` is the group index, relative to
+            // *gbase when gbase is set (device-side loop)
+            auto issue_group = [&](int grp, int s0, int s1, const int* gbase, cudaStream_t s) -> int {
+                const int h1 = 2 * s1;
+                for (int h = 2 * s0; h < h1; h += sweep_depth) {
                     const int nh = h1 - h < sweep_depth ? h1 - h : sweep_depth;
                     const bool in_a = (nl & 1) == 0;
-                    if (launch_sweep_tb(maps, g, in_a, in_a ? P2 : P, sweep_depth, nh, h & 1,
-                                        sweep_zchunk, wacc, use_tol ? status : nullptr,
-                                        use_tol && h == 2 * sweep, group, p.tol, pcur, in_a ? 1 : 0,
-                                        kerr, st) != 0)
+                    if (launch_sweep_tb(maps, g, in_a, in_a ? P2 : P, sweep_depth, nh, h & 1, sweep_zchunk,
+                                        wacc, use_tol ? status : nullptr, use_tol && h == 2 * s0, grp, p.tol,
+                                        pcur, in_a ? 1 : 0, kerr, gbase, s) != 0)
                         return fail(SMK_ERR_CUDA, "sweep kernel configuration failed");
                     ++nl;
                     ++launches;
                 }
+                return SMK_OK;
+            };
+            // In a captured step, the full groups run as a WHILE loop on the device: the body is
+            // one group (two when a group has an odd number of launches, so that every
+            // iteration starts from the same pressure buffer), the loop stops when the tolerance
+            // rule declares the solve done or the full groups are used up.  The launches and
+            // their order are those of the unrolled sequence minus the ones that would exit at
+            // entry, so results are identical.
+            const int nlg = (2 * G + sweep_depth - 1) / sweep_depth;
+            const int U = (nlg % 2 == 0) ? 1 : 2;
+            const int full = use_tol ? p.max_sweeps / G : 0;
+            const int loop_groups = (capturing && graph_loops && use_tol) ? (full / U) * U : 0;
+            if (loop_groups > U) {
+                SMK_CUDA(cudaMemsetAsync(gcount, 0, sizeof(int), st));
+                cudaStreamCaptureStatus cs;
+                cudaGraph_t cg = nullptr;
+                const cudaGraphNode_t* deps = nullptr;
+                size_t ndeps = 0;
+                SMK_CUDA(cudaStreamGetCaptureInfo(st, &cs, nullptr, &cg, &deps, nullptr, &ndeps));
+                cudaGraphConditionalHandle handle;
+                SMK_CUDA(cudaGraphConditionalHandleCreate(&handle, cg, 1, cudaGraphCondAssignDefault));
+                cudaGraphNodeParams np = {};
+                np.type = cudaGraphNodeTypeConditional;
+                np.conditional.handle = handle;
+                np.conditional.type = cudaGraphCondTypeWhile;
+                np.conditional.size = 1;
+                cudaGraphNode_t node;
+                SMK_CUDA(cudaGraphAddNode(&node, cg, deps, nullptr, ndeps, &np));
+                cudaGraph_t body = np.conditional.phGraph_out[0];
+                SMK_CUDA(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+                SMK_CUDA(cudaStreamBeginCaptureToGraph(body_stream, body, nullptr, nullptr, 0,
+                                                       cudaStreamCaptureModeThreadLocal));
+                const int nl0 = nl;
+                const long long l0 = launches;
+                int rc = SMK_OK;
+                for (int u = 0; u < U && rc == SMK_OK; ++u) rc = issue_group(u, u * G, (u + 1) * G, gcount, body_stream);
+                const int per_iter = (int)(launches - l0) + 1;
+                if (rc == SMK_OK)
+                    launch_group_loop_next(status, gcount, U, loop_groups, loop_launches, per_iter, handle, body_stream);
+                cudaGraph_t bg = nullptr;
+                const cudaError_t ee = cudaStreamEndCapture(body_stream, &bg);
+                if (rc != SMK_OK) return rc;
+                if (ee != cudaSuccess) return fail(SMK_ERR_CUDA, std::string("group loop capture: ") + cudaGetErrorString(ee));
+                // the body's launches are counted on the device, per executed iteration
+                launches = l0;
+                nl = nl0;  // U * nlg is even: the parity after each iteration is the same
+                sweep = loop_groups * G;
+                group = loop_groups;
+            }
+            while (sweep < p.max_sweeps) {
+                const int end = sweep + G < p.max_sweeps ? sweep + G : p.max_sweeps;
+                const int rc = issue_group(group, sweep, end, nullptr, st);
+                if (rc != SMK_OK) return rc;
                 sweep = end;
                 ++group;
             }
@@ -260,7 +326,7 @@ int smk_sim::enqueue(float dt, cudaStream_t st) {
             }
         }
         last_groups = group;
-        if (timed) SMK_CUDA(cudaEventRecord(ev[6], st));
+        if (timed) SMK_CUDA(rec(ev[6]));
         const bool tb_used = sweep_depth > 0 && p.max_sweeps > 0;
         if (!tb_used) SMK_CUDA(cudaMemsetAsync(pcur, 0, sizeof(int), st));
         if (bf16)
@@ -278,7 +344,7 @@ int smk_sim::enqueue(float dt, cudaStream_t st) {
         launch_div_max(g, pu, pv, pw, flags, status, st);
         ++launches;
     }
-    if (timed) SMK_CUDA(cudaEventRecord(ev[3], st));
+    if (timed) SMK_CUDA(rec(ev[3]));
 
     // a: advection (:805-810)
     if (bf16) {
@@ -297,7 +363,7 @@ int smk_sim::enqueue(float dt, cudaStream_t st) {
                               (const float*)v[past], (const float*)w[past], flags, dt, st);
     }
     launches += 2;
-    if (timed) SMK_CUDA(cudaEventRecord(ev[4], st));
+    if (timed) SMK_CUDA(rec(ev[4]));
     SMK_CUDA(cudaGetLastError());
     ++steps;
     last_projection = p.projection;
@@ -348,7 +414,7 @@ std::string smk_sim::graph_signature(float dt) const {
 // obstacles changed runs directly (it includes the one-off mask kernels), and so does a step
 // with stage timing on (events recorded inside a capture cannot be queried afterwards).
 int smk_sim::step(float dt, cudaStream_t st) {
-    if (!use_graphs || timing || mask_dirty || obstacles_dirty) return enqueue(dt, st);
+    if (!use_graphs || mask_dirty || obstacles_dirty) return enqueue(dt, st);
     GraphSlot& gs = graphs[index_now];
     std::string sig = graph_signature(dt);
     if (gs.exec == nullptr || gs.sig != sig) {
@@ -684,8 +750,15 @@ int smk_write_state(smk_sim* sim, const smk_host_state* st) {
     if (st && st->index_now != 0 && st->index_now != 1)
         return fail(SMK_ERR_INVALID, "index_now must be 0 or 1");
     int rc = state_copy(sim, st, true);
-    if (rc == SMK_OK) sim->index_now = st->index_now;
-    return rc;
+    if (rc != SMK_OK) return rc;
+    sim->index_now = st->index_now;
+    // the solver's pressure history belongs to the old state: a warm-started step after a
+    // write starts from zero, as the first step of a new simulation does
+    SMK_CUDA(cudaMemset(sim->P, 0, sim->elems() * sizeof(float)));
+    SMK_CUDA(cudaMemset(sim->P2, 0, sim->elems() * sizeof(float)));
+    SMK_CUDA(cudaMemset(sim->pcur, 0, sizeof(int)));
+    SMK_CUDA(cudaDeviceSynchronize());
+    return SMK_OK;
 }
 
 int smk_get_stats(smk_sim* sim, smk_stats* out) {
@@ -752,7 +825,16 @@ int smk_get_stage_times(smk_sim* sim, float* ms, int count) {
     return SMK_OK;
 }
 
-long long smk_launch_count(const smk_sim* sim) { return sim ? sim->launches : 0; }
+long long smk_launch_count(const smk_sim* sim) {
+    if (!sim) return 0;
+    // plus the launches of device-side group loops (counted on the device; reading synchronises)
+    unsigned long long dev = 0;
+    if (sim->loop_launches) {
+        DeviceGuard dg(sim->device);
+        if (cudaMemcpy(&dev, sim->loop_launches, sizeof(dev), cudaMemcpyDeviceToHost) != cudaSuccess) dev = 0;
+    }
+    return sim->launches + (long long)dev;
+}
 
 }  // extern "C"
 
@@ -771,6 +853,13 @@ int smk_set_sweep_kernel(smk_sim* sim, int depth, int zchunk) {
 int smk_set_graphs(smk_sim* sim, int enable) {
     if (!sim) return fail(SMK_ERR_INVALID, "sim is null");
     sim->use_graphs = enable != 0;
+    return SMK_OK;
+}
+
+int smk_set_graph_loops(smk_sim* sim, int enable) {
+    if (!sim) return fail(SMK_ERR_INVALID, "sim is null");
+    sim->graph_loops = enable != 0;
+    for (auto& gs : sim->graphs) gs.sig.clear();  // re-capture
     return SMK_OK;
 }
 
@@ -855,7 +944,7 @@ int smk_autotune(smk_sim* sim, int* depth_out, int* zchunk_out, float* us_per_sw
             const int nh = 2 * G - h < d ? 2 * G - h : d;
             if (launch_sweep_tb(sim->maps, g, true, sim->P2, d, nh, h & 1, zc, wacc,
                                 use_tol ? sim->tune_status : nullptr, use_tol && h == 0, 0, sim->p.tol,
-                                nullptr, 0, sim->kerr, st) != 0)
+                                nullptr, 0, sim->kerr, nullptr, st) != 0)
                 return fail(SMK_ERR_CUDA, "sweep kernel configuration failed");
         }
         return SMK_OK;

@@ -66,6 +66,8 @@ struct smk_sim {
     float* b = nullptr;
     int* pcur = nullptr;  // device: which pressure buffer the last executed sweep wrote
     int* kerr = nullptr;  // device: a bounded wait in a kernel gave up (sticky until read)
+    int* gcount = nullptr;  // device: tolerance groups done by a graph's device-side group loop
+    unsigned long long* loop_launches = nullptr;  // device: kernels launched by those loops
     smk::SweepMaps* maps = nullptr;  // TMA tensor maps of P, P2, b, flags
     uint8_t* s = nullptr;
     uint8_t* flags = nullptr;
@@ -107,8 +109,12 @@ struct smk_sim {
         int groups = 0;
     };
     bool use_graphs = true;
+    // in a captured step, the tolerance groups of the blocked solve run as a device-side WHILE
+    // loop (graph conditional node) instead of launches for every group up to the cap
+    bool graph_loops = true;
     GraphSlot graphs[2];
     cudaStream_t cap_stream = nullptr;
+    cudaStream_t body_stream = nullptr;  // captures the loop body
 
     int step(float dt, cudaStream_t st);
     int enqueue(float dt, cudaStream_t st);
