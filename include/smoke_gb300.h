@@ -249,6 +249,9 @@ int smk_server_create(size_t budget_bytes, int max_active, smk_server** out);
 #define SMK_SERVE_STREAMS 0
 #define SMK_SERVE_GROUPED 1
 int smk_server_set_mode(smk_server* server, int mode);
+/* smk_set_graph_loops for the requests admitted from now on (default off: with many request
+ * graphs in flight at once, the loop's per-iteration cost exceeds the launches it saves). */
+int smk_server_set_graph_loops(smk_server* server, int enable);
 int smk_server_submit(smk_server* server, const smk_request_desc* request, int* id);
 int smk_server_tick(smk_server* server, int* n_active, int* n_queued);
 int smk_server_request_status(smk_server* server, int id, int* state, int* steps_done, int* error);

@@ -409,7 +409,12 @@ int branches_step(smk_batch* b, const float* dts, float dt_all, cudaStream_t st)
         for (int i = 0; i < n && rc == SMK_OK && ce == cudaSuccess; ++i) {
             ce = cudaStreamWaitEvent(b->branch[i], b->fork, 0);
             if (ce != cudaSuccess) break;
+            // concurrent branches: unrolled group launches (a device-side loop per branch costs
+            // more than the launches it saves when many graphs run at once)
+            const bool loops = b->sims[i]->graph_loops;
+            b->sims[i]->graph_loops = false;
             rc = b->sims[i]->enqueue(dts ? dts[i] : dt_all, b->branch[i]);
+            b->sims[i]->graph_loops = loops;
             if (rc == SMK_OK) ce = cudaEventRecord(b->join[i], b->branch[i]);
             if (rc == SMK_OK && ce == cudaSuccess) ce = cudaStreamWaitEvent(b->origin, b->join[i], 0);
         }

@@ -91,6 +91,10 @@ struct smk_server {
     long long steps_completed = 0;
     int requests_completed = 0;
     int mode = SMK_SERVE_STREAMS;
+    // smk_set_graph_loops for every admitted request.  Off by default: with many requests'
+    // graphs running concurrently, each iteration of a device-side loop costs more than the
+    // launches it saves (measured: 40-request stream 3.0 vs 3.6 G cell-updates/s).
+    int graph_loops = 0;
     bool started = false;  // the form is fixed once a request was admitted
     cudaStream_t stream = nullptr;
     GroupRunner* runner = nullptr;
@@ -161,6 +165,12 @@ static void release_request(smk_server* s, Request* r) {
     r->stream = nullptr;
 }
 
+int smk_server_set_graph_loops(smk_server* s, int enable) {
+    if (!s) return sfail(SMK_ERR_INVALID, "server is null");
+    s->graph_loops = enable != 0;
+    return SMK_OK;
+}
+
 int smk_server_set_mode(smk_server* s, int mode) {
     if (!s) return sfail(SMK_ERR_INVALID, "server is null");
     if (mode != SMK_SERVE_STREAMS && mode != SMK_SERVE_GROUPED) return sfail(SMK_ERR_INVALID, "unknown serving form");
@@ -223,6 +233,7 @@ static void collect(smk_server* s, TickRec& t) {
 
 static int admit(smk_server* s, Request* r) {
     int rc = smk_create(r->nx, r->ny, r->nz, &r->params, &r->sim);
+    if (rc == SMK_OK) rc = smk_set_graph_loops(r->sim, s->graph_loops);
     if (rc == SMK_OK && !r->mask.empty()) rc = smk_set_solid_mask(r->sim, r->mask.data());
     for (size_t k = 0; rc == SMK_OK && k < r->boxes.size() / 9; ++k) {
         const float* b = &r->boxes[9 * k];

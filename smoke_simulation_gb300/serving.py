@@ -57,6 +57,7 @@ def _bind():
             ("smk_server_get_stats", i, [vp, C.POINTER(ServerStats)]),
             ("smk_server_destroy", i, [vp]),
             ("smk_server_set_mode", i, [vp, i]),
+            ("smk_server_set_graph_loops", i, [vp, i]),
             ("smk_server_last_error", C.c_char_p, [])):
         fn = getattr(L, name)
         fn.restype = res
@@ -84,6 +85,10 @@ class Server:
         _srv_check(L.smk_server_create(budget_bytes, max_active, C.byref(self.h)))
         if mode != SERVE_STREAMS:
             _srv_check(L.smk_server_set_mode(self.h, int(mode)))
+
+    def set_graph_loops(self, enable: bool):
+        """Device-side group loops in the requests' step graphs (default off)."""
+        _srv_check(_bind().smk_server_set_graph_loops(self.h, 1 if enable else 0))
         self._keep = {}
         self.outputs = {}
 
