@@ -85,12 +85,12 @@ class Server:
         _srv_check(L.smk_server_create(budget_bytes, max_active, C.byref(self.h)))
         if mode != SERVE_STREAMS:
             _srv_check(L.smk_server_set_mode(self.h, int(mode)))
+        self._keep = {}
+        self.outputs = {}
 
     def set_graph_loops(self, enable: bool):
         """Device-side group loops in the requests' step graphs (default off)."""
         _srv_check(_bind().smk_server_set_graph_loops(self.h, 1 if enable else 0))
-        self._keep = {}
-        self.outputs = {}
 
     def submit(self, scene, steps: Optional[int] = None, params: Optional[Params] = None,
                keep_output: bool = True, **param_overrides) -> int:
