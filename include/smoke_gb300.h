@@ -61,6 +61,12 @@ typedef struct smk_params {
     int warm_start;     /* PRESSURE only: keep the pressure across steps */
     int report_div;     /* measure max|div u| after the projection every step */
     int storage;        /* SMK_STORAGE_* (F32 only for PROJECT_REFERENCE) */
+    int refine;         /* PRESSURE with tol > 0: FP64-checked refinement rounds after the
+                           solve (0: none).  Each round measures max|div u| of the projected
+                           velocity with FP64 accumulation; while a cell exceeds tol it solves
+                           for a correction (refine_sweeps FP32 sweeps on the FP64 divergence,
+                           rounded) and applies it to the velocity and the pressure. */
+    int refine_sweeps;  /* sweeps of each correction solve */
 } smk_params;
 
 typedef struct smk_stats {
@@ -69,6 +75,8 @@ typedef struct smk_stats {
     float resid_max;    /* max |residual| at the last residual check */
     float div_max;      /* max |div u| after projection (report_div), else -1 */
     int step_index;     /* steps taken since creation */
+    int refine_rounds;  /* correction rounds applied by the last step (refine > 0) */
+    float div64_max;    /* max |div u| of the last FP64 measurement (refine > 0), else -1 */
 } smk_stats;
 
 /* Host copy of the full state in the reference's layout (both ping-pong buffers). */

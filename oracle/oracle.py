@@ -32,6 +32,7 @@ class OrcParams(C.Structure):
         ("spheres", _F), ("n_spheres", C.c_int),
         ("boxes", _F), ("n_boxes", C.c_int),
         ("obstacles", _F), ("n_obstacles", C.c_int),
+        ("refine", C.c_int), ("refine_sweeps", C.c_int),
     ]
 
 
@@ -46,7 +47,7 @@ class OrcState(C.Structure):
 
 class OrcStats(C.Structure):
     _fields_ = [("sweeps", C.c_int), ("converged", C.c_int), ("resid_max", C.c_float),
-                ("div_max", C.c_float)]
+                ("div_max", C.c_float), ("refine_rounds", C.c_int), ("div64_max", C.c_float)]
 
 
 _lib = None
@@ -149,6 +150,7 @@ class OracleSim:
         p.spheres, p.n_spheres = _fptr(self.spheres), self.n_spheres
         p.boxes, p.n_boxes = _fptr(self.boxes), self.n_boxes
         p.obstacles, p.n_obstacles = _fptr(self.obstacles), self.n_obstacles
+        p.refine, p.refine_sweeps = getattr(sc, "refine", 0), getattr(sc, "refine_sweeps", 10)
         return p
 
     def step(self, dt: Optional[float] = None) -> OrcStats:

@@ -51,6 +51,8 @@ typedef struct {
     const float* spheres;   int n_spheres;
     const float* boxes;     int n_boxes;
     const float* obstacles; int n_obstacles;
+    int refine;          // scheme 1 with tol > 0: FP64-checked refinement rounds (0: none)
+    int refine_sweeps;   // sweeps of each correction solve
 } orc_params;
 
 typedef struct {
@@ -70,6 +72,8 @@ typedef struct {
     int converged;      // scheme 1 with tol > 0: the tolerance rule ended the solve
     float resid_max;    // scheme 1: max |residual| at the last check (or final state)
     float div_max;      // max |div u| over projectable cells after projection
+    int refine_rounds;  // correction rounds applied (refine > 0)
+    float div64_max;    // max |div u| of the last FP64 measurement (refine > 0), else -1
 } orc_stats;
 
 }  // extern "C"
@@ -545,6 +549,86 @@ float max_div(const Dims& d, const T* u, const T* v, const T* w, const uint8_t* 
     return (float)m;
 }
 
+// FP64-checked refinement after the pressure projection (no counterpart in the reference).  A
+// round measures d = ((((-u0 + u1) + -v0) + v1) + -w0) + w1 per projectable cell in double from
+// the FP32 faces; when some |d| > tol it solves A e = (float)(-d) from e = 0 with `sweeps`
+// red-black sweeps (project_pressure's update), subtracts grad e on fluid-fluid faces and adds e
+// to P.  The last round only measures.  T = float only (the FP32 solve it refines).
+double measure_div64(const Dims& d, const float* u, const float* v, const float* w, const uint8_t* s,
+                     float* b, float* e, bool write, double tol, bool* need) {
+    double m = 0.0;
+    *need = false;
+    for (int z = 0; z < d.nz; ++z)
+        for (int y = 0; y < d.ny; ++y)
+            for (int x = 0; x < d.nx; ++x) {
+                long long c = d.c(x, y, z);
+                if (projectable(d, s, x, y, z)) {
+                    long long i = d.f(x, y, z);
+                    const double dv = ((((-(double)u[i] + (double)u[d.f(x + 1, y, z)]) + -(double)v[i]) +
+                                        (double)v[d.f(x, y + 1, z)]) + -(double)w[i]) + (double)w[d.f(x, y, z + 1)];
+                    const double a = std::fabs(dv);
+                    if (a > m || a != a) m = a;
+                    if (a > tol) *need = true;
+                    if (write) b[c] = (float)(-dv);
+                } else if (write) {
+                    b[c] = 0.0f;
+                }
+                if (write) e[c] = 0.0f;
+            }
+    return m;
+}
+
+void refine_pressure(const Dims& d, float* u, float* v, float* w, float* P, const uint8_t* s, int rounds,
+                     int sweeps, double omega, float tol, orc_stats* st) {
+    std::vector<float> b((size_t)d.nx * d.ny * d.nz), e((size_t)d.nx * d.ny * d.nz);
+    float wacc[7];
+    wacc[0] = 0.0f;
+    for (int a = 1; a <= 6; ++a) wacc[a] = (float)omega / (float)a;
+    bool need = false;
+    double m = measure_div64(d, u, v, w, s, b.data(), e.data(), true, (double)tol, &need);
+    int applied = 0;
+    for (int r = 0; r < rounds && need; ++r) {
+        for (int k = 0; k < sweeps; ++k)
+            for (int colour = 0; colour < 2; ++colour)
+                for (int z = 1; z < d.nz - 1; ++z)
+                    for (int y = 1; y < d.ny - 1; ++y)
+                        for (int x = 1 + ((1 + y + z + colour) & 1); x < d.nx - 1; x += 2) {
+                            if (!projectable(d, s, x, y, z)) continue;
+                            const int acc = fluid_nbrs(d, s, x, y, z);
+                            const long long c = d.c(x, y, z);
+                            const float sum = nbr_sum(d, e.data(), x, y, z);
+                            const float rr = fma_t<float>(-(float)acc, e[c], b[c] + sum);
+                            e[c] = fma_t<float>(wacc[acc], rr, e[c]);
+                        }
+        for (int z = 1; z < d.nz - 1; ++z)
+            for (int y = 1; y < d.ny - 1; ++y)
+                for (int x = 1; x < d.nx; ++x)
+                    if (s[d.c(x - 1, y, z)] && s[d.c(x, y, z)]) {
+                        long long i = d.f(x, y, z);
+                        u[i] = u[i] - (e[d.c(x, y, z)] - e[d.c(x - 1, y, z)]);
+                    }
+        for (int z = 1; z < d.nz - 1; ++z)
+            for (int y = 1; y < d.ny; ++y)
+                for (int x = 1; x < d.nx - 1; ++x)
+                    if (s[d.c(x, y - 1, z)] && s[d.c(x, y, z)]) {
+                        long long i = d.f(x, y, z);
+                        v[i] = v[i] - (e[d.c(x, y, z)] - e[d.c(x, y - 1, z)]);
+                    }
+        for (int z = 1; z < d.nz; ++z)
+            for (int y = 1; y < d.ny - 1; ++y)
+                for (int x = 1; x < d.nx - 1; ++x)
+                    if (s[d.c(x, y, z - 1)] && s[d.c(x, y, z)]) {
+                        long long i = d.f(x, y, z);
+                        w[i] = w[i] - (e[d.c(x, y, z)] - e[d.c(x, y, z - 1)]);
+                    }
+        for (size_t c = 0; c < e.size(); ++c) P[c] = P[c] + e[c];
+        ++applied;
+        m = measure_div64(d, u, v, w, s, b.data(), e.data(), r + 1 < rounds, (double)tol, &need);
+    }
+    st->refine_rounds = applied;
+    st->div64_max = (float)m;
+}
+
 // simulate (:774-819): flip, objects, forcing, projection, advection; result in rho[past].
 template <typename T>
 int step(orc_state* S, const orc_params* p, float dt, orc_stats* st) {
@@ -568,6 +652,10 @@ int step(orc_state* S, const orc_params* p, float dt, orc_stats* st) {
     } else {
         project_pressure<T>(d, u[now], v[now], w[now], (T*)S->P, (T*)S->b, S->s, p->iterations,
                             p->omega, p->tol, p->check_every, p->warm_start, &local);
+        local.div64_max = -1.0f;
+        if (p->refine > 0 && p->tol > 0.0f && sizeof(T) == sizeof(float))
+            refine_pressure(d, (float*)u[now], (float*)v[now], (float*)w[now], (float*)S->P, S->s, p->refine,
+                            p->refine_sweeps, p->omega, p->tol, &local);
     }
     local.div_max = max_div<T>(d, u[now], v[now], w[now], S->s);
     advect_velocity<T>(d, u[now], v[now], w[now], u[past], v[past], w[past], S->s, dt);

@@ -35,12 +35,14 @@ class Params(C.Structure):
         ("clamp_mode", C.c_int), ("projection", C.c_int), ("max_sweeps", C.c_int),
         ("omega", C.c_double), ("tol", C.c_float), ("check_every", C.c_int),
         ("warm_start", C.c_int), ("report_div", C.c_int), ("storage", C.c_int),
+        ("refine", C.c_int), ("refine_sweeps", C.c_int),
     ]
 
 
 class Stats(C.Structure):
     _fields_ = [("sweeps", C.c_int), ("converged", C.c_int), ("resid_max", C.c_float),
-                ("div_max", C.c_float), ("step_index", C.c_int)]
+                ("div_max", C.c_float), ("step_index", C.c_int), ("refine_rounds", C.c_int),
+                ("div64_max", C.c_float)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -372,6 +374,7 @@ def params_for_scene(scene, **overrides) -> Params:
     p.clamp_const, p.clamp_mode = scene.clamp_const, scene.clamp_mode
     p.projection, p.max_sweeps, p.omega = scene.scheme, scene.iterations, scene.omega
     p.tol, p.check_every, p.warm_start = scene.tol, scene.check_every, scene.warm_start
+    p.refine, p.refine_sweeps = scene.refine, scene.refine_sweeps
     for k, v in overrides.items():
         setattr(p, k, v)
     return p

@@ -277,7 +277,7 @@ int launch_config(const GroupSchedule& sched, const TableImage& t, GroupLaunch& 
 bool grouped_eligible(smk_sim* const* sims, int n) {
     if (n > MAX_GROUPED) return false;
     for (int i = 0; i < n; ++i)
-        if (sims[i]->p.projection != SMK_PROJECT_PRESSURE) return false;
+        if (sims[i]->p.projection != SMK_PROJECT_PRESSURE || sims[i]->p.refine > 0) return false;
     return true;
 }
 
@@ -293,6 +293,7 @@ void after_step(smk_sim* s) {
     s->last_tol = s->p.tol;
     s->last_max_sweeps = s->p.max_sweeps;
     s->last_check_every = s->p.check_every;
+    s->last_refine = 0;
 }
 
 int grouped_step(smk_batch* b, const float* dts, float dt_all, cudaStream_t st) {
@@ -453,6 +454,7 @@ int branches_step(smk_batch* b, const float* dts, float dt_all, cudaStream_t st)
         s->last_tol = s->p.tol;
         s->last_max_sweeps = s->p.max_sweeps;
         s->last_check_every = s->p.check_every;
+        s->last_refine = s->p.projection == SMK_PROJECT_PRESSURE ? s->p.refine : 0;
     }
     return SMK_OK;
 }
@@ -608,8 +610,8 @@ int smk_batch_set_mode(smk_batch* b, int mode) {
     if (mode != SMK_BATCH_AUTO && mode != SMK_BATCH_GROUPED && mode != SMK_BATCH_BRANCHES)
         return smk_fail(SMK_ERR_INVALID, "unknown batch mode");
     if (mode == SMK_BATCH_GROUPED && !grouped_eligible(b))
-        return smk_fail(SMK_ERR_INVALID, "the grouped form needs the PRESSURE projection in every member "
-                                         "(and at most 16384 members)");
+        return smk_fail(SMK_ERR_INVALID, "the grouped form needs the PRESSURE projection without "
+                                         "refinement in every member (and at most 16384 members)");
     b->mode = mode;
     return SMK_OK;
 }

@@ -47,6 +47,15 @@ struct StepStatus {
     unsigned rmax_bits[1];  // max |residual| per check group (flexible; sized at allocation)
 };
 
+// Device-side state of the projection's FP64-checked refinement rounds.
+struct RefineStatus {
+    unsigned long long div_bits;  // max |div u| of the last measurement (FP64, as IEEE bits)
+    int need;                     // the last measurement found a cell above tolerance
+    int rounds;                   // correction rounds applied in this step
+    int stop;                     // a measurement was within tolerance: later rounds do nothing
+    int pad;
+};
+
 // Object records (the reference's packing, smokeSimulation.cu:719-725, :750-758).
 struct SphereObj { float x, y, z, r; };
 struct ObstacleObj { float x, y, z, vx, vy, vz, r; };

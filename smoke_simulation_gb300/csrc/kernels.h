@@ -66,6 +66,12 @@ void launch_group_loop_next(const StepStatus* status, int* counter, int step, in
                             cudaGraphConditionalHandle handle, cudaStream_t st);
 void launch_div_max(const Grid& g, const float* u, const float* v, const float* w,
                     const uint8_t* flags, StepStatus* status, cudaStream_t st);
+// FP64-checked refinement rounds after the projection (u, v, w: the FP32 projected velocity;
+// us, vs, ws: the BF16 state to re-round, or NULL).  Adds the launches to *launches.
+template <typename Tv>
+void launch_refine(const Grid& g, float* u, float* v, float* w, Tv* us, Tv* vs, Tv* ws, float* b, float* P0,
+                   float* P1, const int* pcur, const uint8_t* flags, const float* wacc7, int rounds,
+                   int sweeps, double tol, RefineStatus* rs, long long* launches, cudaStream_t st);
 
 // Stage a: advection.
 template <typename Ti, typename To>

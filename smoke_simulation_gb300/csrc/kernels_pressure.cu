@@ -92,3 +92,160 @@ void launch_gradient_subtract(const Grid& g, float* u, float* v, float* w, const
 }
 
 }  // namespace smk
+
+// ---- FP64-checked refinement of the projection ----------------------------------------------
+//
+// After the FP32 solve and gradient subtract, the divergence of the projected velocity is
+// measured with FP64 accumulation: d = ((((-u0 + u1) + -v0) + v1) + -w0) + w1 over the six FP32
+// face values in double.  While some projectable cell has |d| > tol, a correction round solves
+// A e = b' with b' = (float)(-d) from e = 0 (the same FP32 red-black passes, a fixed number of
+// sweeps), subtracts grad e from the velocity on fluid-fluid faces (the gradient subtract's rule)
+// and adds e to the pressure, so the next warm start keeps the correction.  e lives in the
+// pressure buffer that does not hold the solution (*pcur selects).  Every kernel returns at
+// entry once a measurement was within tolerance.
+
+namespace smk {
+namespace {
+
+__device__ __forceinline__ unsigned long long block_max_u64(unsigned long long v) {
+    __shared__ unsigned long long red[32];
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = w > v ? w : v;
+    }
+    const int tid = threadIdx.x + blockDim.x * threadIdx.y;
+    const int nw = (blockDim.x * blockDim.y + 31) >> 5;
+    if ((tid & 31) == 0) red[tid >> 5] = v;
+    __syncthreads();
+    unsigned long long m = 0ull;
+    if (tid == 0)
+        for (int k = 0; k < nw; ++k) m = red[k] > m ? red[k] : m;
+    return m;  // valid in thread 0
+}
+
+__global__ void k_refine_reset(RefineStatus* rs, int start) {
+    if (start) {
+        rs->rounds = 0;
+        rs->stop = 0;
+    }
+    if (!rs->stop) {
+        rs->div_bits = 0ull;
+        rs->need = 0;
+    }
+}
+
+template <bool WRITE>
+__global__ void k_refine_measure(Grid g, const float* u, const float* v, const float* w,
+                                 const uint8_t* __restrict__ flags, float* b, float* P0, float* P1,
+                                 const int* pcur, RefineStatus* rs, double tol) {
+    if (*(volatile int*)&rs->stop) return;
+    const int x = (int)blockIdx.x * BX + (int)threadIdx.x;
+    const int y = (int)blockIdx.y * BY + (int)threadIdx.y;
+    const int z = (int)blockIdx.z;
+    double m = 0.0;
+    if (x < g.nx && y < g.ny && z < g.nz) {
+        const int i = g.idx(x, y, z);
+        if (flags[i] & F_PROJ) {
+            const double d = ((((-(double)u[i] + (double)u[i + 1]) + -(double)v[i]) + (double)v[i + g.X]) +
+                              -(double)w[i]) + (double)w[i + g.XY];
+            m = fabs(d);
+            if (WRITE) b[i] = (float)(-d);
+            if (m > tol) rs->need = 1;
+        } else if (WRITE) {
+            b[i] = 0.0f;
+        }
+        if (WRITE) ((*pcur == 1) ? P0 : P1)[i] = 0.0f;
+    }
+    const unsigned long long bm = block_max_u64((unsigned long long)__double_as_longlong(m));
+    if (threadIdx.x == 0 && threadIdx.y == 0 && bm > 0ull) atomicMax(&rs->div_bits, bm);
+}
+
+__global__ void k_refine_decide(RefineStatus* rs) {
+    if (!rs->stop && !rs->need) rs->stop = 1;
+}
+
+__global__ void k_refine_sweep(Grid g, float* P0, float* P1, const int* pcur, const float* b,
+                               const uint8_t* __restrict__ flags, int colour, WAcc wa,
+                               const RefineStatus* rs) {
+    if (*(volatile const int*)&rs->stop) return;
+    float* e = (*pcur == 1) ? P0 : P1;
+    body_sweep(g, e, b, flags, colour, wa, nullptr, blockIdx);
+}
+
+template <typename Tv>
+__global__ void k_refine_apply(Grid g, float* u, float* v, float* w, Tv* us, Tv* vs, Tv* ws, float* P0,
+                               float* P1, const int* pcur, const uint8_t* __restrict__ flags,
+                               RefineStatus* rs) {
+    if (*(volatile int*)&rs->stop) return;
+    const bool second = *pcur == 1;
+    float* Pc = second ? P1 : P0;
+    const float* e = second ? P0 : P1;
+    if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 && threadIdx.y == 0)
+        rs->rounds += 1;
+    const int x = 1 + (int)blockIdx.x * BX + (int)threadIdx.x;
+    const int y = 1 + (int)blockIdx.y * BY + (int)threadIdx.y;
+    const int z = 1 + (int)blockIdx.z;
+    if (x >= g.nx || y >= g.ny || z >= g.nz) return;
+    const int i = g.idx(x, y, z);
+    const uint8_t f = flags[i];
+    if (!(f & F_SELF)) return;
+    const bool inx = x <= g.nx - 2, iny = y <= g.ny - 2, inz = z <= g.nz - 2;
+    const float ec = e[i];
+    if (iny && inz && (f & F_XM)) {
+        u[i] = u[i] - (ec - e[i - 1]);
+        if (us) stv(us, i, u[i]);
+    }
+    if (inx && inz && (f & F_YM)) {
+        v[i] = v[i] - (ec - e[i - g.X]);
+        if (vs) stv(vs, i, v[i]);
+    }
+    if (inx && iny && (f & F_ZM)) {
+        w[i] = w[i] - (ec - e[i - g.XY]);
+        if (ws) stv(ws, i, w[i]);
+    }
+    if (inx && iny && inz) Pc[i] = Pc[i] + ec;
+}
+
+}  // namespace
+
+template <typename Tv>
+void launch_refine(const Grid& g, float* u, float* v, float* w, Tv* us, Tv* vs, Tv* ws, float* b, float* P0,
+                   float* P1, const int* pcur, const uint8_t* flags, const float* wacc7, int rounds,
+                   int sweeps, double tol, RefineStatus* rs, long long* launches, cudaStream_t st) {
+    if (g.nx < 3 || g.ny < 3 || g.nz < 3) return;
+    WAcc wa;
+    for (int k = 0; k < 7; ++k) wa.w[k] = wacc7[k];
+    wa.w[7] = 0.0f;
+    const int half = (g.nx - 2 + 1) / 2;
+    const dim3 blk(BX, BY);
+    k_refine_reset<<<1, 1, 0, st>>>(rs, 1);
+    k_refine_measure<true><<<grid3(g.nx, g.ny, g.nz), blk, 0, st>>>(g, u, v, w, flags, b, P0, P1, pcur, rs, tol);
+    k_refine_decide<<<1, 1, 0, st>>>(rs);
+    *launches += 3;
+    for (int r = 0; r < rounds; ++r) {
+        for (int s = 0; s < sweeps; ++s)
+            for (int colour = 0; colour < 2; ++colour)
+                k_refine_sweep<<<grid3(half, g.ny - 2, g.nz - 2), blk, 0, st>>>(g, P0, P1, pcur, b, flags, colour,
+                                                                                wa, rs);
+        k_refine_apply<Tv><<<grid3(g.nx - 1, g.ny - 1, g.nz - 1), blk, 0, st>>>(g, u, v, w, us, vs, ws, P0, P1,
+                                                                               pcur, flags, rs);
+        k_refine_reset<<<1, 1, 0, st>>>(rs, 0);
+        if (r + 1 < rounds)
+            k_refine_measure<true><<<grid3(g.nx, g.ny, g.nz), blk, 0, st>>>(g, u, v, w, flags, b, P0, P1, pcur,
+                                                                           rs, tol);
+        else
+            k_refine_measure<false><<<grid3(g.nx, g.ny, g.nz), blk, 0, st>>>(g, u, v, w, flags, b, P0, P1, pcur,
+                                                                            rs, tol);
+        k_refine_decide<<<1, 1, 0, st>>>(rs);
+        *launches += 2 * sweeps + 4;
+    }
+}
+template void launch_refine<float>(const Grid&, float*, float*, float*, float*, float*, float*, float*, float*,
+                                   float*, const int*, const uint8_t*, const float*, int, int, double,
+                                   RefineStatus*, long long*, cudaStream_t);
+template void launch_refine<__nv_bfloat16>(const Grid&, float*, float*, float*, __nv_bfloat16*, __nv_bfloat16*,
+                                           __nv_bfloat16*, float*, float*, float*, const int*, const uint8_t*,
+                                           const float*, int, int, double, RefineStatus*, long long*,
+                                           cudaStream_t);
+
+}  // namespace smk

@@ -44,6 +44,11 @@ int check_params(const smk_params* p) {
         return fail(SMK_ERR_INVALID, "unknown storage precision");
     if (p->storage != SMK_STORAGE_F32 && p->projection == SMK_PROJECT_REFERENCE)
         return fail(SMK_ERR_INVALID, "BF16 storage needs the pressure projection");
+    if (p->refine < 0 || p->refine > 16) return fail(SMK_ERR_INVALID, "refine must be 0..16");
+    if (p->refine > 0 && (p->projection != SMK_PROJECT_PRESSURE || !(p->tol > 0.0f)))
+        return fail(SMK_ERR_INVALID, "refinement needs the PRESSURE projection with tol > 0");
+    if (p->refine > 0 && (p->refine_sweeps < 1 || p->refine_sweeps > 100000))
+        return fail(SMK_ERR_INVALID, "refine_sweeps must be 1..100000");
     if (p->projection == SMK_PROJECT_PRESSURE && p->tol > 0 &&
         (p->max_sweeps + p->check_every - 1) / p->check_every > 4000)
         return fail(SMK_ERR_INVALID, "too many residual checks per step (max_sweeps/check_every > 4000)");
@@ -102,6 +107,8 @@ int smk_sim::alloc() {
     gcount = pcur + 2;
     SMK_CUDA(cudaMalloc((void**)&loop_launches, sizeof(unsigned long long)));
     SMK_CUDA(cudaMemset(loop_launches, 0, sizeof(unsigned long long)));
+    SMK_CUDA(cudaMalloc((void**)&refine, sizeof(RefineStatus)));
+    SMK_CUDA(cudaMemset(refine, 0, sizeof(RefineStatus)));
     SMK_CUDA(cudaMalloc((void**)&s, n));
     SMK_CUDA(cudaMalloc((void**)&flags, n));
     SMK_CUDA(cudaMemset(flags, 0, n));
@@ -129,6 +136,7 @@ void smk_sim::release() {
         if (f) cudaFree(f);
     if (pcur) cudaFree(pcur);
     if (loop_launches) cudaFree(loop_launches);
+    if (refine) cudaFree(refine);
     if (maps) destroy_sweep_maps(maps);
     if (s) cudaFree(s);
     if (flags) cudaFree(flags);
@@ -335,6 +343,15 @@ int smk_sim::enqueue(float dt, cudaStream_t st) {
         else
             launch_gradient_subtract(g, u[now], v[now], w[now], P, P2, pcur, flags, st);
         ++launches;
+        if (p.refine > 0) {
+            if (bf16)
+                launch_refine(g, proj[0], proj[1], proj[2], bf(u[now]), bf(v[now]), bf(w[now]), b, P, P2, pcur,
+                              flags, wacc, p.refine, p.refine_sweeps, (double)p.tol, refine, &launches, st);
+            else
+                launch_refine(g, u[now], v[now], w[now], (float*)nullptr, (float*)nullptr, (float*)nullptr, b, P,
+                              P2, pcur, flags, wacc, p.refine, p.refine_sweeps, (double)p.tol, refine,
+                              &launches, st);
+        }
     }
     // the projected velocity advection consumes: the state itself (FP32) or its FP32 copy
     const float* pu = bf16 ? proj[0] : u[now];
@@ -370,6 +387,7 @@ int smk_sim::enqueue(float dt, cudaStream_t st) {
     last_tol = p.tol;
     last_max_sweeps = p.max_sweeps;
     last_check_every = p.check_every;
+    last_refine = p.projection == SMK_PROJECT_PRESSURE ? p.refine : 0;
     return SMK_OK;
 }
 
@@ -453,6 +471,7 @@ int smk_sim::step(float dt, cudaStream_t st) {
     last_tol = p.tol;
     last_max_sweeps = p.max_sweeps;
     last_check_every = p.check_every;
+    last_refine = p.projection == SMK_PROJECT_PRESSURE ? p.refine : 0;
     return SMK_OK;
 }
 
@@ -475,6 +494,8 @@ void smk_default_params(smk_params* p) {
     p->warm_start = 0;
     p->report_div = 0;
     p->storage = SMK_STORAGE_F32;
+    p->refine = 0;
+    p->refine_sweeps = 10;
 }
 
 const char* smk_error_string(int code) {
@@ -767,6 +788,7 @@ int smk_get_stats(smk_sim* sim, smk_stats* out) {
     memset(out, 0, sizeof(*out));
     out->step_index = sim->steps;
     out->div_max = -1.0f;
+    out->div64_max = -1.0f;
     if (sim->steps == 0) return SMK_OK;
     std::vector<unsigned> host(4 + sim->status_groups);
     SMK_CUDA(cudaDeviceSynchronize());
@@ -800,6 +822,14 @@ int smk_get_stats(smk_sim* sim, smk_stats* out) {
         }
     } else {
         out->sweeps = sim->last_max_sweeps;
+    }
+    if (sim->last_refine > 0) {
+        RefineStatus rs;
+        SMK_CUDA(cudaMemcpy(&rs, sim->refine, sizeof(rs), cudaMemcpyDeviceToHost));
+        double d;
+        memcpy(&d, &rs.div_bits, sizeof(d));
+        out->div64_max = (float)d;
+        out->refine_rounds = rs.rounds;
     }
     return SMK_OK;
 }

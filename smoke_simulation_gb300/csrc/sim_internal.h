@@ -68,6 +68,7 @@ struct smk_sim {
     int* kerr = nullptr;  // device: a bounded wait in a kernel gave up (sticky until read)
     int* gcount = nullptr;  // device: tolerance groups done by a graph's device-side group loop
     unsigned long long* loop_launches = nullptr;  // device: kernels launched by those loops
+    smk::RefineStatus* refine = nullptr;          // device: FP64-checked refinement rounds
     smk::SweepMaps* maps = nullptr;  // TMA tensor maps of P, P2, b, flags
     uint8_t* s = nullptr;
     uint8_t* flags = nullptr;
@@ -96,6 +97,7 @@ struct smk_sim {
     int last_max_sweeps = 0;
     int last_check_every = 1;
     int last_groups = 0;
+    int last_refine = 0;
 
     size_t elems() const { return (size_t)g.XY * (size_t)(g.nz + 1); }
     int alloc();

@@ -88,6 +88,8 @@ class Scene:
     tol: float = 0.0
     check_every: int = 10
     warm_start: int = 0
+    refine: int = 0                            # FP64-checked refinement rounds (pressure, tol > 0)
+    refine_sweeps: int = 10
 
     @property
     def cells(self) -> int:

@@ -284,3 +284,39 @@ def test_device_group_loop_equals_unrolled_and_direct(gpu, depth, check):
     assert sims[0].launch_count() < sims[1].launch_count()
     for s in sims:
         s.close()
+
+
+@pytest.mark.parametrize("graphs", [True, False])
+def test_refinement_bit_exact_with_oracle(gpu, graphs):
+    """FP64-checked refinement rounds: the GPU gives the oracle's bits, sweep counts, rounds
+    applied and FP64 divergence, with the step replayed as a graph or launched directly."""
+    sc = S.small_scene(24, 20, 26, steps=4, seed=31, scheme=1, iterations=12, tol=1e-5,
+                       check_every=4, warm_start=1)
+    sc.refine, sc.refine_sweeps = 3, 8
+    sim = smk.from_scene(sc, report_div=1)
+    sim.set_graphs(graphs)
+    o = O.OracleSim(sc)
+    for k in range(sc.steps):
+        sim.step(sc.dt)
+        so = o.step()
+        sg = sim.stats()
+        assert (sg.sweeps, sg.refine_rounds) == (so.sweeps, so.refine_rounds), k
+        assert H.bits_equal(np.float32(sg.div64_max), np.float32(so.div64_max)), k
+        assert H.bits_equal(np.float32(sg.div_max), np.float32(so.div_max)), k
+    assert H.first_mismatch(sim.read_state(), H.oracle_state(o)) == ""
+    sim.close()
+
+
+def test_refinement_bf16_velocities_lowers_divergence(gpu):
+    sc = S.small_scene(24, 20, 26, steps=3, seed=31, scheme=1, iterations=12, tol=1e-5,
+                       check_every=4, warm_start=1)
+    plain = smk.from_scene(sc, report_div=1, storage=smk.STORAGE_BF16_VEL)
+    sc.refine, sc.refine_sweeps = 3, 8
+    ref = smk.from_scene(sc, report_div=1, storage=smk.STORAGE_BF16_VEL)
+    for _ in range(sc.steps):
+        plain.step(sc.dt)
+        ref.step(sc.dt)
+    a, b = plain.stats(), ref.stats()
+    assert b.refine_rounds == 3 and b.div64_max < 0.2 * a.div_max
+    plain.close()
+    ref.close()

@@ -164,3 +164,24 @@ def test_scene_generator_is_deterministic():
     assert len(sides) == 64 and min(sides) >= 32 and max(sides) <= 128
     r = S.SplitMix64(7).uniform(1000)
     assert 0.45 < r.mean() < 0.55
+
+
+def test_refinement_rounds_reduce_fp64_divergence():
+    """FP64-checked refinement (oracle): after a solve capped well short of a tight tolerance,
+    each correction round lowers the FP64-measured max|div u|; with a loose tolerance no round
+    is applied."""
+    from smoke_simulation_gb300 import scenes as S
+    out = {}
+    for refine, tol in ((0, 1e-5), (1, 1e-5), (3, 1e-5), (3, 10.0)):
+        sc = S.small_scene(24, 20, 26, steps=2, seed=31, scheme=1, iterations=12, tol=tol,
+                           check_every=4, warm_start=1)
+        sc.refine, sc.refine_sweeps = refine, 8
+        o = O.OracleSim(sc)
+        for _ in range(sc.steps):
+            st = o.step()
+        out[(refine, tol)] = st
+    assert out[(0, 1e-5)].refine_rounds == 0 and out[(0, 1e-5)].div64_max == -1.0
+    assert out[(1, 1e-5)].refine_rounds == 1 and out[(3, 1e-5)].refine_rounds == 3
+    assert out[(3, 1e-5)].div64_max < out[(1, 1e-5)].div64_max < out[(0, 1e-5)].div_max
+    assert out[(3, 10.0)].refine_rounds == 0
+    assert 0.0 <= out[(3, 10.0)].div64_max <= 10.0
