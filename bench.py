@@ -48,7 +48,7 @@ N_DEFAULT = 256
 # Sweeps the reference step is given in the CPU baseline and the reference arm: the
 # reference's projection has no convergence test, so it runs the sweep count that this
 # workload's tolerance rule takes on the GPU (mean over the benchmark's steps).
-REF_SWEEPS_DEFAULT = 170
+REF_SWEEPS_DEFAULT = 167
 # Algorithmic bytes per cell: one red+black sweep reads P, b, flags and writes P.
 SWEEP_BYTES_PER_CELL = 13.0
 CHECK_BYTES_PER_CELL = 9.0
@@ -195,7 +195,7 @@ def run_reference_arm(args, ws, rank):
     steps = max(1, min(args.steps, args.ref_max_steps))
     warm = min(args.warmup, 1)
     from oracle import oracle as O
-    sc = workload(args.n)
+    sc = workload(args.side)
     sc.scheme, sc.iterations, sc.tol = 0, args.ref_sweeps, 0.0
     cores = os.cpu_count() or 1
     if O.reference_available():
@@ -213,7 +213,7 @@ def run_reference_arm(args, ws, rank):
     dt = time.perf_counter() - t0
     rate = sc.cells * steps / dt
     sample = ("%d timed step(s) (+%d warm-up) of the %d^3 workload, reference step with %d "
-              "fixed red-black iterations, OpenMP over %d threads" % (steps, warm, args.n,
+              "fixed red-black iterations, OpenMP over %d threads" % (steps, warm, args.side,
                                                                      args.ref_sweeps, cores))
     line = {
         "metric": METRIC, "value": rate, "unit": UNIT, "impl": "reference", "n_gpus": ws,
@@ -221,7 +221,7 @@ def run_reference_arm(args, ws, rank):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
         "config": {"workload": "smoke step %d^3 FP32, 5%% random solids + 2 spheres r=24, 4 "
-                               "emitters, dt=0.02, red-black SOR %d sweeps" % (args.n, args.ref_sweeps),
+                               "emitters, dt=0.02, red-black SOR %d sweeps" % (args.side, args.ref_sweeps),
                    "cells": sc.cells, "l2": "inputs larger than L2 (CPU run)"},
         "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": kind,
                          "sample": sample},
@@ -237,7 +237,7 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--n", type=int, default=N_DEFAULT)
+    ap.add_argument("--side", type=int, default=N_DEFAULT, help="grid cells per side of the workload")
     ap.add_argument("--ref-sweeps", type=int, default=REF_SWEEPS_DEFAULT)
     ap.add_argument("--ref-max-steps", type=int, default=3)
     ap.add_argument("--cpu-steps", type=int, default=1)
@@ -267,7 +267,7 @@ def main():
         build.build()
     torch.cuda.set_device(local)
 
-    sc = workload(args.n)
+    sc = workload(args.side)
     sim = smk.from_scene(sc, report_div=1)
     initial = sim.read_state()  # the workload's initial fields; every timed segment starts here
     seg = sc.steps              # the workload is sc.steps (50) steps long
@@ -391,11 +391,11 @@ def main():
         # the reference step has no tolerance test and no stored pressure: it needs the sweeps
         # a zero-pressure start takes to reach the tolerance (the cold form's count)
         ref_sweeps = int(round(cold["mean_sweeps"])) if cold else REF_SWEEPS_DEFAULT
-        rate, kind, cores, secs = cpu_reference_rate(args.n, ref_sweeps, args.cpu_steps)
+        rate, kind, cores, secs = cpu_reference_rate(args.side, ref_sweeps, args.cpu_steps)
         cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": kind,
                "sample": "%d step(s) of the %d^3 workload with %d fixed red-black iterations "
                          "(the sweeps a zero-pressure start needs for max|div| <= 1e-4, measured "
-                         "on the GPU in this run), %.1f s" % (args.cpu_steps, args.n, ref_sweeps,
+                         "on the GPU in this run), %.1f s" % (args.cpu_steps, args.side, ref_sweeps,
                                                              secs)}
 
     forms = None
@@ -413,7 +413,7 @@ def main():
             "config": {"workload": "smoke step %d^3 FP32, 5%% random solids + 2 spheres r=24, 4 "
                                    "emitters, dt=0.02, warm-started pressure red-black SOR to "
                                    "max|div|<=1e-4 "
-                                   "(checked every 6 sweeps, cap 200)" % args.n,
+                                   "(checked every 6 sweeps, cap 200)" % args.side,
                        "cells": sc.cells, "parallelism": "replicas" if ws > 1 else "single",
                        "timed_steps": "%d steps: the %d-step workload from its initial fields, "
                                       "%d time(s) (fields written back between segments, outside "
