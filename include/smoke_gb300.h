@@ -227,6 +227,7 @@ int smk_batch_set_schedule(smk_batch* batch, int ctas_per_sm, int zslab, long lo
 #define SMK_REQ_ACTIVE 1
 #define SMK_REQ_DONE 2
 #define SMK_REQ_FAILED 3
+#define SMK_REQ_CANCELLED 4
 typedef struct smk_server smk_server;
 typedef struct smk_request_desc {
     int nx, ny, nz;            /* grid cells */
@@ -263,6 +264,14 @@ int smk_server_set_graph_loops(smk_server* server, int enable);
 int smk_server_submit(smk_server* server, const smk_request_desc* request, int* id);
 int smk_server_tick(smk_server* server, int* n_active, int* n_queued);
 int smk_server_request_status(smk_server* server, int id, int* state, int* steps_done, int* error);
+/* Cancel a request: a queued one is dropped now; an active one gets no further steps and is
+ * released (no density copy) by the tick after its issued steps have completed.  Cancelling a
+ * finished request does nothing. */
+int smk_server_cancel(smk_server* server, int id);
+
+/* Testing: the next `count` smk_create calls fail with SMK_ERR_OOM as a device allocation
+ * failure would, without touching the device (host-side fault injection). */
+int smk_inject_alloc_failures(int count);
 int smk_server_get_stats(smk_server* server, smk_server_stats* out);
 int smk_server_destroy(smk_server* server);
 const char* smk_server_last_error(void);

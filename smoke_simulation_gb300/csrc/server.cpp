@@ -23,6 +23,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <deque>
 #include <string>
@@ -54,6 +55,7 @@ struct Request {
     int steps_done = 0;
     int error = SMK_OK;
     size_t bytes = 0;
+    bool cancel = false;  // smk_server_cancel on an active request: no new steps, then released
     smk_sim* sim = nullptr;
     // STREAMS form: the request's own stream and two step slots (issue / collect)
     cudaStream_t stream = nullptr;
@@ -165,6 +167,26 @@ static void release_request(smk_server* s, Request* r) {
     r->stream = nullptr;
 }
 
+int smk_server_cancel(smk_server* s, int id) {
+    if (!s) return sfail(SMK_ERR_INVALID, "server is null");
+    for (auto it = s->queue.begin(); it != s->queue.end(); ++it) {
+        if ((*it)->id == id) {
+            (*it)->state = SMK_REQ_CANCELLED;
+            s->queue.erase(it);
+            return SMK_OK;
+        }
+    }
+    for (Request* r : s->active) {
+        if (r->id == id) {
+            r->cancel = true;  // released by a later tick once its issued steps have completed
+            return SMK_OK;
+        }
+    }
+    for (Request* r : s->all)
+        if (r->id == id) return SMK_OK;  // already finished, failed or cancelled
+    return sfail(SMK_ERR_INVALID, "unknown request id");
+}
+
 int smk_server_set_graph_loops(smk_server* s, int enable) {
     if (!s) return sfail(SMK_ERR_INVALID, "server is null");
     s->graph_loops = enable != 0;
@@ -187,8 +209,25 @@ int smk_server_destroy(smk_server* s) {
 
 int smk_server_submit(smk_server* s, const smk_request_desc* d, int* id) {
     if (!s || !d) return sfail(SMK_ERR_INVALID, "null argument");
-    if (d->nx < 3 || d->ny < 3 || d->nz < 3 || d->steps < 1 || !(d->dt > 0.0f))
-        return sfail(SMK_ERR_INVALID, "request needs a grid of at least 3^3 cells, steps >= 1, dt > 0");
+    if (d->nx < 3 || d->ny < 3 || d->nz < 3 || d->steps < 1 || !(d->dt > 0.0f) || !std::isfinite(d->dt))
+        return sfail(SMK_ERR_INVALID, "request needs a grid of at least 3^3 cells, steps >= 1, finite dt > 0");
+    if (d->n_spheres < 0 || d->n_boxes < 0 || d->n_obstacles < 0 ||
+        (d->n_spheres > 0 && !d->spheres) || (d->n_boxes > 0 && !d->boxes) || (d->n_obstacles > 0 && !d->obstacles))
+        return sfail(SMK_ERR_INVALID, "object counts and arrays do not match");
+    // non-finite host inputs are rejected here rather than propagated into the simulation
+    auto finite = [](const float* a, size_t n) {
+        for (size_t k = 0; k < n; ++k)
+            if (!std::isfinite(a[k])) return false;
+        return true;
+    };
+    if ((d->n_spheres > 0 && !finite(d->spheres, 4 * (size_t)d->n_spheres)) ||
+        (d->n_boxes > 0 && !finite(d->boxes, 9 * (size_t)d->n_boxes)) ||
+        (d->n_obstacles > 0 && !finite(d->obstacles, 7 * (size_t)d->n_obstacles)))
+        return sfail(SMK_ERR_INVALID, "non-finite value in the request's objects");
+    if (d->params && (!std::isfinite(d->params->gravity) || !std::isfinite(d->params->buoyancy) ||
+                      !std::isfinite(d->params->clamp_const) || !std::isfinite(d->params->omega) ||
+                      !std::isfinite(d->params->tol)))
+        return sfail(SMK_ERR_INVALID, "non-finite value in the request's parameters");
     Request* r = new Request();
     r->id = s->next_id++;
     r->nx = d->nx;
@@ -307,6 +346,11 @@ static int tick_streams(smk_server* s) {
             release_request(s, r);
             continue;
         }
+        if (r->cancel && r->steps_done >= r->steps_issued) {
+            r->state = SMK_REQ_CANCELLED;
+            release_request(s, r);
+            continue;
+        }
         if (r->steps_done >= r->steps) {
             int rc = SMK_OK;
             if (r->out) {
@@ -331,7 +375,7 @@ static int tick_streams(smk_server* s) {
     }
     // (3) one step per active request, each on its own stream
     for (Request* r : s->active) {
-        if (r->steps_issued >= r->steps) continue;
+        if (r->steps_issued >= r->steps || r->cancel) continue;
         const int k = r->steps_issued & 1;
         if (r->pending[k]) {  // its previous use is still in flight (not collected yet)
             if (cudaEventSynchronize(r->ev_end[k]) != cudaSuccess) {
@@ -376,7 +420,7 @@ static int tick_grouped(smk_server* s) {
         else if (q != cudaErrorNotReady) return sfail(SMK_ERR_CUDA, std::string("server step: ") + cudaGetErrorString(q));
     }
     bool work = false;
-    for (Request* r : s->active) work = work || r->steps_issued < r->steps;
+    for (Request* r : s->active) work = work || (r->steps_issued < r->steps && !r->cancel);
     if (!work && s->queue.empty()) {
         for (int k : {older, newer}) {
             TickRec& t = s->ticks[k];
@@ -388,6 +432,11 @@ static int tick_grouped(smk_server* s) {
     // retire requests whose last step completed
     std::vector<Request*> still;
     for (Request* r : s->active) {
+        if (r->cancel && r->steps_done >= r->steps_issued) {
+            r->state = SMK_REQ_CANCELLED;
+            release_request(s, r);
+            continue;
+        }
         if (r->steps_done >= r->steps) {
             int rc = SMK_OK;
             if (r->out) {
@@ -416,7 +465,7 @@ static int tick_grouped(smk_server* s) {
     std::vector<float> dts;
     std::vector<Request*> members, single;
     for (Request* r : s->active) {
-        if (r->steps_issued >= r->steps) continue;
+        if (r->steps_issued >= r->steps || r->cancel) continue;
         members.push_back(r);
         if (r->params.projection == SMK_PROJECT_PRESSURE) {
             grouped.push_back(r->sim);

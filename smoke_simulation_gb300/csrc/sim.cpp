@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -69,6 +70,10 @@ cudaMemcpy3DParms copy3d(void* dst, size_t dpitch, size_t dy, const void* src, s
 }  // namespace
 
 int smk_fail(int code, const std::string& msg) { return fail(code, msg); }
+
+// Fault injection for tests: the next N smk_create calls fail as a device allocation failure
+// would, before touching the device.
+static std::atomic<int> g_inject_alloc_failures{0};
 
 // ---- smk_sim --------------------------------------------------------------------------------
 
@@ -523,6 +528,9 @@ int smk_create(int nx, int ny, int nz, const smk_params* params, smk_sim** out) 
     long long X = ((long long)nx + 1 + 15) / 16 * 16;  // 16-element rows: TMA strides
     long long total = X * (ny + 1) * (long long)(nz + 1);
     if (total >= (1LL << 31)) return fail(SMK_ERR_INVALID, "grid too large for 32-bit indexing");
+    for (int k = g_inject_alloc_failures.load(); k > 0; k = g_inject_alloc_failures.load())
+        if (g_inject_alloc_failures.compare_exchange_weak(k, k - 1))
+            return fail(SMK_ERR_OOM, "injected device allocation failure");
     smk_sim* sim = new smk_sim();
     sim->g.nx = nx;
     sim->g.ny = ny;
@@ -852,6 +860,12 @@ int smk_get_stage_times(smk_sim* sim, float* ms, int count) {
     if (sim->last_projection == SMK_PROJECT_PRESSURE)
         SMK_CUDA(cudaEventElapsedTime(&t[5], sim->ev[5], sim->ev[6]));
     for (int k = 0; k < count && k < 6; ++k) ms[k] = t[k];
+    return SMK_OK;
+}
+
+int smk_inject_alloc_failures(int count) {
+    if (count < 0) return fail(SMK_ERR_INVALID, "count must be >= 0");
+    g_inject_alloc_failures.store(count);
     return SMK_OK;
 }
 

@@ -2,8 +2,9 @@
 seeded Poisson request stream used to exercise it.
 
 The server keeps requests resident on the GPU, admits new ones between ticks as memory and
-slots free up, and overlaps the steps of different requests on separate streams; this module
-only binds it (ctypes) and drives it in real time from an arrival schedule.
+slots free up, and overlaps the steps of different requests (separate streams, or one grouped
+step per tick); this module only binds it (ctypes) and drives it in real time from an arrival
+schedule.
 """
 from __future__ import annotations
 
@@ -18,7 +19,7 @@ import numpy as np
 from . import Params, _check, lib, params_for_scene
 from . import scenes as S
 
-REQ_QUEUED, REQ_ACTIVE, REQ_DONE, REQ_FAILED = 0, 1, 2, 3
+REQ_QUEUED, REQ_ACTIVE, REQ_DONE, REQ_FAILED, REQ_CANCELLED = 0, 1, 2, 3, 4
 
 _F = C.POINTER(C.c_float)
 
@@ -57,6 +58,7 @@ def _bind():
             ("smk_server_get_stats", i, [vp, C.POINTER(ServerStats)]),
             ("smk_server_destroy", i, [vp]),
             ("smk_server_set_mode", i, [vp, i]),
+            ("smk_server_cancel", i, [vp, i]),
             ("smk_server_set_graph_loops", i, [vp, i]),
             ("smk_server_last_error", C.c_char_p, [])):
         fn = getattr(L, name)
@@ -125,6 +127,9 @@ class Server:
         if out is not None:
             self.outputs[rid.value] = out
         return rid.value
+
+    def cancel(self, rid: int):
+        _srv_check(_bind().smk_server_cancel(self.h, int(rid)))
 
     def tick(self):
         a, q = C.c_int(), C.c_int()

@@ -69,3 +69,51 @@ def test_memory_budget_admission(gpu, mode):
         assert srv.status(rid)[0] == SV.REQ_DONE
         assert H.bits_equal(srv.outputs[rid], _alone(sc, steps))
     srv.close()
+
+
+def _drain(srv):
+    for _ in range(100000):
+        active, queued = srv.tick()
+        if active == 0 and queued == 0:
+            return
+    raise RuntimeError("server did not drain")
+
+
+@pytest.mark.parametrize("mode", [SV.SERVE_STREAMS, SV.SERVE_GROUPED])
+def test_injected_allocation_failure_fails_one_request(gpu, mode):
+    """A device allocation that fails at admission (injected on the host) fails that request
+    alone; the others run and give their results alone."""
+    reqs = _requests()[:3]
+    srv = SV.Server(budget_bytes=10**10, max_active=4, mode=mode)
+    smk.lib().smk_inject_alloc_failures(1)
+    ids = [srv.submit(sc, steps) for sc, steps in reqs]
+    _drain(srv)
+    smk.lib().smk_inject_alloc_failures(0)
+    states = [srv.status(i) for i in ids]
+    assert states[0][0] == SV.REQ_FAILED and states[0][2] == 3  # SMK_ERR_OOM
+    for rid, (sc, steps), st in list(zip(ids, reqs, states))[1:]:
+        assert st[0] == SV.REQ_DONE
+        assert H.bits_equal(srv.outputs[rid], _alone(sc, steps))
+    assert srv.stats().bytes_in_use == 0
+    srv.close()
+
+
+@pytest.mark.parametrize("mode", [SV.SERVE_STREAMS, SV.SERVE_GROUPED])
+def test_cancel_active_and_queued_requests(gpu, mode):
+    reqs = [(sc, steps + 20) for sc, steps in _requests()[:4]]
+    srv = SV.Server(budget_bytes=10**10, max_active=2, mode=mode)
+    ids = [srv.submit(sc, steps) for sc, steps in reqs]
+    for _ in range(3):
+        srv.tick()
+    assert srv.status(ids[0])[0] == SV.REQ_ACTIVE and srv.status(ids[3])[0] == SV.REQ_QUEUED
+    srv.cancel(ids[0])
+    srv.cancel(ids[3])
+    _drain(srv)
+    st0, done0, _ = srv.status(ids[0])
+    assert st0 == SV.REQ_CANCELLED and 0 < done0 < reqs[0][1]
+    assert srv.status(ids[3])[:2] == (SV.REQ_CANCELLED, 0)
+    for rid, (sc, steps) in zip(ids[1:3], reqs[1:3]):
+        assert srv.status(rid)[0] == SV.REQ_DONE
+        assert H.bits_equal(srv.outputs[rid], _alone(sc, steps))
+    assert srv.stats().bytes_in_use == 0
+    srv.close()

@@ -37,3 +37,44 @@ def test_poisson_stream_is_deterministic():
     assert all(48 <= x.scene.nx <= 192 and 50 <= x.steps <= 500 for x in a)
     gaps = [a[i + 1].t - a[i].t for i in range(len(a) - 1)]
     assert 0.001 < sum(gaps) / len(gaps) < 0.02  # ~1/200 s
+
+
+def test_non_finite_inputs_are_rejected(smoke_lib):
+    srv = SV.Server(budget_bytes=10**9, max_active=4)
+    sc = S.Scene("nan_sphere", 16, 16, 16, dt=0.05, steps=2, scheme=1)
+    sc.spheres = [(8.0, float("nan"), 8.0, 3.0)]
+    with pytest.raises(Exception):
+        srv.submit(sc)
+    sc2 = S.Scene("nan_param", 16, 16, 16, dt=0.05, steps=2, scheme=1)
+    with pytest.raises(Exception):
+        srv.submit(sc2, gravity=float("inf"))
+    sc3 = S.Scene("nan_dt", 16, 16, 16, dt=float("nan"), steps=2, scheme=1)
+    with pytest.raises(Exception):
+        srv.submit(sc3)
+    assert srv.stats().queued == 0
+    srv.close()
+
+
+def test_cancel_a_queued_request(smoke_lib):
+    srv = SV.Server(budget_bytes=10**9, max_active=1)
+    a = srv.submit(S.Scene("a", 16, 16, 16, dt=0.05, steps=2, scheme=1), keep_output=False)
+    b = srv.submit(S.Scene("b", 16, 16, 16, dt=0.05, steps=2, scheme=1), keep_output=False)
+    srv.cancel(b)
+    assert srv.status(b)[0] == SV.REQ_CANCELLED
+    assert srv.status(a)[0] == SV.REQ_QUEUED and srv.stats().queued == 1
+    srv.cancel(b)  # cancelling twice does nothing
+    with pytest.raises(Exception):
+        srv.cancel(12345)
+    srv.close()
+
+
+def test_injected_allocation_failure_hook(smoke_lib):
+    import smoke_simulation_gb300 as smk
+    L = smk.lib()
+    L.smk_inject_alloc_failures.argtypes = [C.c_int]
+    assert L.smk_inject_alloc_failures(1) == 0
+    h = C.c_void_p()
+    assert L.smk_create(8, 8, 8, None, C.byref(h)) == 3  # SMK_ERR_OOM, before any device work
+    assert not h.value
+    assert L.smk_inject_alloc_failures(-1) == 1
+    assert L.smk_inject_alloc_failures(0) == 0
