@@ -241,7 +241,11 @@ typedef struct smk_request_desc {
     int n_boxes;
     const float* obstacles;    /* obstacles, 7 floats each (x,y,z,vx,vy,vz,r) */
     int n_obstacles;
-    float* out_density;        /* host, nx*ny*nz floats, written at completion (may be NULL) */
+    float* out_density;        /* nx*ny*nz floats written at completion (may be NULL): host memory
+                                  (page-locked by the server while the request lives, so the copy
+                                  is asynchronous), or device memory when out_on_device */
+    int out_on_device;         /* out_density is device memory: the handoff is a stream-ordered
+                                  device-to-device copy, no host involvement */
 } smk_request_desc;
 typedef struct smk_server_stats {
     long long steps_completed;

@@ -49,7 +49,11 @@ struct Request {
     smk_params params{};
     std::vector<uint8_t> mask;  // empty: reference initial mask
     std::vector<float> spheres, boxes, obstacles;  // reference packing (4 / 9 / 7 floats)
-    float* out = nullptr;                          // caller's host buffer for the final density
+    float* out = nullptr;                          // caller's buffer for the final density
+    bool out_on_device = false;
+    bool out_pinned = false;                       // out was page-locked by the server
+    bool retiring = false;                         // final density copy in flight (retire_ev)
+    cudaEvent_t retire_ev = nullptr;
     int state = SMK_REQ_QUEUED;
     int steps_issued = 0;
     int steps_done = 0;
@@ -158,6 +162,12 @@ static void release_request(smk_server* s, Request* r) {
         r->sim = nullptr;
         s->used -= r->bytes;
     }
+    if (r->out_pinned) {
+        cudaHostUnregister(r->out);
+        r->out_pinned = false;
+    }
+    if (r->retire_ev) cudaEventDestroy(r->retire_ev);
+    r->retire_ev = nullptr;
     for (int k = 0; k < 2; ++k) {
         if (r->ev_start[k]) cudaEventDestroy(r->ev_start[k]);
         if (r->ev_end[k]) cudaEventDestroy(r->ev_end[k]);
@@ -243,6 +253,7 @@ int smk_server_submit(smk_server* s, const smk_request_desc* d, int* id) {
     if (d->n_boxes > 0) r->boxes.assign(d->boxes, d->boxes + 9 * d->n_boxes);
     if (d->n_obstacles > 0) r->obstacles.assign(d->obstacles, d->obstacles + 7 * d->n_obstacles);
     r->out = d->out_density;
+    r->out_on_device = d->out_on_device != 0;
     r->bytes = footprint(d->nx, d->ny, d->nz);
     s->all.push_back(r);
     if (r->bytes > s->budget) {
@@ -287,6 +298,15 @@ static int admit(smk_server* s, Request* r) {
         const float* o = &r->obstacles[7 * k];
         rc = smk_add_obstacle(r->sim, o[0], o[1], o[2], o[3], o[4], o[5], o[6], nullptr);
     }
+    if (rc == SMK_OK && cudaEventCreateWithFlags(&r->retire_ev, cudaEventDisableTiming) != cudaSuccess)
+        rc = SMK_ERR_CUDA;
+    if (rc == SMK_OK && r->out && !r->out_on_device) {
+        // page-lock the caller's buffer so the final copy does not block the host; if that is not
+        // possible the copy is made synchronously at retirement
+        const size_t bytes = (size_t)r->nx * r->ny * r->nz * sizeof(float);
+        r->out_pinned = cudaHostRegister(r->out, bytes, cudaHostRegisterDefault) == cudaSuccess;
+        if (!r->out_pinned) cudaGetLastError();
+    }
     if (rc == SMK_OK && s->mode == SMK_SERVE_STREAMS) {
         if (cudaStreamCreateWithFlags(&r->stream, cudaStreamNonBlocking) != cudaSuccess) rc = SMK_ERR_CUDA;
         for (int k = 0; rc == SMK_OK && k < 2; ++k)
@@ -306,6 +326,42 @@ static int admit(smk_server* s, Request* r) {
     }
     r->state = SMK_REQ_ACTIVE;
     return SMK_OK;
+}
+
+// ---- retirement: the final density handoff -----------------------------------------------
+
+static void finish(smk_server* s, Request* r, int rc) {
+    r->error = rc;
+    r->state = rc == SMK_OK ? SMK_REQ_DONE : SMK_REQ_FAILED;
+    s->requests_completed++;
+    release_request(s, r);
+}
+
+// A request whose last step has completed: its final density goes to the caller's buffer by a
+// stream-ordered copy followed by an event, and a later tick releases the request once the
+// event has completed, so the host never waits for the copy.  A pageable host buffer that could
+// not be page-locked is copied synchronously.  Returns true when the request is finished.
+static bool retire(smk_server* s, Request* r, cudaStream_t st) {
+    if (!r->retiring) {
+        if (!r->out) {
+            finish(s, r, check_kernel_error(r->sim));
+            return true;
+        }
+        int rc = smk_read_density(r->sim, r->out, r->out_on_device ? 1 : 0, st);
+        const bool async = r->out_on_device || r->out_pinned;
+        if (rc == SMK_OK && !async) rc = smk_sync(r->sim, st);
+        if (rc == SMK_OK && async && cudaEventRecord(r->retire_ev, st) != cudaSuccess) rc = SMK_ERR_CUDA;
+        if (rc != SMK_OK || !async) {
+            finish(s, r, rc);
+            return true;
+        }
+        r->retiring = true;
+        return false;
+    }
+    const cudaError_t q = cudaEventQuery(r->retire_ev);
+    if (q == cudaErrorNotReady) return false;
+    finish(s, r, q == cudaSuccess ? check_kernel_error(r->sim) : SMK_ERR_CUDA);
+    return true;
 }
 
 // ---- STREAMS form: every request's own step on its own stream ------------------------------
@@ -351,16 +407,8 @@ static int tick_streams(smk_server* s) {
             release_request(s, r);
             continue;
         }
-        if (r->steps_done >= r->steps) {
-            int rc = SMK_OK;
-            if (r->out) {
-                rc = smk_read_density(r->sim, r->out, 0, r->stream);
-                if (rc == SMK_OK) rc = smk_sync(r->sim, r->stream);
-            }
-            r->error = rc;
-            r->state = rc == SMK_OK ? SMK_REQ_DONE : SMK_REQ_FAILED;
-            s->requests_completed++;
-            release_request(s, r);
+        if (r->steps_done >= r->steps || r->retiring) {
+            if (!retire(s, r, r->stream)) still.push_back(r);
         } else {
             still.push_back(r);
         }
@@ -437,16 +485,8 @@ static int tick_grouped(smk_server* s) {
             release_request(s, r);
             continue;
         }
-        if (r->steps_done >= r->steps) {
-            int rc = SMK_OK;
-            if (r->out) {
-                rc = smk_read_density(r->sim, r->out, 0, s->stream);
-                if (rc == SMK_OK) rc = smk_sync(r->sim, s->stream);
-            }
-            r->error = rc;
-            r->state = rc == SMK_OK ? SMK_REQ_DONE : SMK_REQ_FAILED;
-            s->requests_completed++;
-            release_request(s, r);
+        if (r->steps_done >= r->steps || r->retiring) {
+            if (!retire(s, r, s->stream)) still.push_back(r);
         } else {
             still.push_back(r);
         }

@@ -482,6 +482,18 @@ int smk_sim::step(float dt, cudaStream_t st) {
 
 // ---- C ABI ----------------------------------------------------------------------------------
 
+// After a synchronisation: report (and clear) a bounded device wait that gave up.
+int check_kernel_error(smk_sim* sim) {
+    int e = 0;
+    SMK_CUDA(cudaMemcpy(&e, sim->kerr, sizeof(int), cudaMemcpyDeviceToHost));
+    if (e) {
+        SMK_CUDA(cudaMemset(sim->kerr, 0, sizeof(int)));
+        return fail(SMK_ERR_TIMEOUT, "a bounded device wait (TMA loads or a grid barrier) gave up; "
+                                     "the step's projection is incomplete");
+    }
+    return SMK_OK;
+}
+
 extern "C" {
 
 void smk_default_params(smk_params* p) {
@@ -685,18 +697,6 @@ int smk_read_density(smk_sim* sim, float* dst, int dst_on_device, void* stream) 
     auto m = copy3d(dst, (size_t)g.nx * 4, g.ny, src, (size_t)g.X * 4, g.ny + 1, (size_t)g.nx * 4, g.ny,
                     g.nz, dst_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost);
     SMK_CUDA(cudaMemcpy3DAsync(&m, (cudaStream_t)stream));
-    return SMK_OK;
-}
-
-// After a synchronisation: report (and clear) a bounded device wait that gave up.
-static int check_kernel_error(smk_sim* sim) {
-    int e = 0;
-    SMK_CUDA(cudaMemcpy(&e, sim->kerr, sizeof(int), cudaMemcpyDeviceToHost));
-    if (e) {
-        SMK_CUDA(cudaMemset(sim->kerr, 0, sizeof(int)));
-        return fail(SMK_ERR_TIMEOUT, "a bounded device wait (TMA loads or a grid barrier) gave up; "
-                                     "the step's projection is incomplete");
-    }
     return SMK_OK;
 }
 

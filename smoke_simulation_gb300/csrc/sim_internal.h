@@ -126,6 +126,10 @@ struct smk_sim {
     int prepare_mask(cudaStream_t st);
 };
 
+// After a synchronisation point of the simulation's work: report (and clear) a bounded device
+// wait that gave up (sim.cpp).
+int check_kernel_error(smk_sim* sim);
+
 // ---- grouped steps over many simulations (batch.cpp) -----------------------------------------
 namespace smk { struct GroupSchedule; }
 struct GroupRunner;

@@ -28,7 +28,8 @@ class RequestDesc(C.Structure):
     _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("steps", C.c_int),
                 ("dt", C.c_float), ("params", C.POINTER(Params)), ("mask", C.c_void_p),
                 ("spheres", _F), ("n_spheres", C.c_int), ("boxes", _F), ("n_boxes", C.c_int),
-                ("obstacles", _F), ("n_obstacles", C.c_int), ("out_density", C.c_void_p)]
+                ("obstacles", _F), ("n_obstacles", C.c_int), ("out_density", C.c_void_p),
+                ("out_on_device", C.c_int)]
 
 
 class ServerStats(C.Structure):
@@ -95,8 +96,10 @@ class Server:
         _srv_check(_bind().smk_server_set_graph_loops(self.h, 1 if enable else 0))
 
     def submit(self, scene, steps: Optional[int] = None, params: Optional[Params] = None,
-               keep_output: bool = True, **param_overrides) -> int:
-        """Queue `scene` (a scenes.Scene) for `steps` steps; returns the request id."""
+               keep_output: bool = True, out_device=None, **param_overrides) -> int:
+        """Queue `scene` (a scenes.Scene) for `steps` steps; returns the request id.  The final
+        density goes to a host array (self.outputs[id]) or, with `out_device` (a CUDA tensor
+        of the cell shape, float32), to device memory by a stream-ordered copy."""
         p = params if params is not None else params_for_scene(scene, **param_overrides)
         keep = [p]
         d = RequestDesc()
@@ -117,7 +120,12 @@ class Server:
                 setattr(d, field, a.ctypes.data_as(_F))
                 setattr(d, "n_" + field, len(rows))
         out = None
-        if keep_output:
+        if out_device is not None:
+            assert tuple(out_device.shape) == tuple(scene.cell_shape) and out_device.is_cuda
+            keep.append(out_device)
+            d.out_density = out_device.data_ptr()
+            d.out_on_device = 1
+        elif keep_output:
             out = np.zeros(scene.cell_shape, np.float32)
             keep.append(out)
             d.out_density = out.ctypes.data

@@ -117,3 +117,20 @@ def test_cancel_active_and_queued_requests(gpu, mode):
         assert H.bits_equal(srv.outputs[rid], _alone(sc, steps))
     assert srv.stats().bytes_in_use == 0
     srv.close()
+
+
+@pytest.mark.parametrize("mode", [SV.SERVE_STREAMS, SV.SERVE_GROUPED])
+def test_device_resident_outputs(gpu, mode):
+    """Final densities handed to device buffers (stream-ordered device copies, no host copy)
+    are the results each request gives alone."""
+    import torch
+    reqs = _requests()[:4]
+    srv = SV.Server(budget_bytes=10**10, max_active=2, mode=mode)
+    outs = [torch.full(tuple(sc.cell_shape), -1.0, dtype=torch.float32, device="cuda") for sc, _ in reqs]
+    ids = [srv.submit(sc, steps, out_device=o) for (sc, steps), o in zip(reqs, outs)]
+    _drain(srv)
+    torch.cuda.synchronize()
+    for rid, (sc, steps), o in zip(ids, reqs, outs):
+        assert srv.status(rid)[0] == SV.REQ_DONE
+        assert H.bits_equal(o.cpu().numpy(), _alone(sc, steps))
+    srv.close()
