@@ -248,6 +248,7 @@ def main():
     ap.add_argument("--forms-steps", type=int, default=10, help="timed steps of the batched/mixed forms")
     ap.add_argument("--mixed-n", type=int, default=512, help="mixed-precision grid side (0: skip)")
     ap.add_argument("--serve-requests", type=int, default=16, help="serving stream length (0: skip)")
+    ap.add_argument("--render-frames", type=int, default=20, help="timed frames of the render form (0: skip)")
     ap.add_argument("--no-forms", action="store_true", help="skip the batched/mixed/serving forms")
     ap.add_argument("--sweep-kernel", default="", help="D,Z: blocked sweep depth and z-chunk instead "
                     "of the autotuner's choice (to profile the configuration a timed run chose)")
@@ -569,6 +570,36 @@ def run_forms(args, smk, torch):
                                       "density too; errors vs the FP64 oracle are tested at 80^3"
                                       % (args.mixed_n, args.forms_steps),
                           "cells": float(sc.cells), **mixed}
+
+    # ---- headless rendering: the reference application's frame ---------------------------------
+    if args.render_frames > 0:
+        sc = S.config_ref80(steps=50, scheme=1)
+        sc.tol, sc.check_every, sc.iterations, sc.warm_start = 1e-4, 6, 200, 1
+        sim = smk.from_scene(sc)
+        sim.autotune()
+        for _ in range(sc.steps):
+            sim.step(sc.dt, sh)
+        rp = smk.default_render_params()
+        eye = torch.empty((rp.height, rp.width, 4), dtype=torch.float32, device="cuda")
+        comp = torch.empty((rp.height, rp.width, 3), dtype=torch.float32, device="cuda")
+        frame = lambda: sim.render_into(eye.data_ptr(), comp.data_ptr(), rp, sh)
+        for _ in range(3):
+            frame()
+        f_s = _timed_steps(frame, stream, args.render_frames, torch)
+        both = lambda: (sim.step(sc.dt, sh), frame())
+        for _ in range(3):
+            both()
+        b_s = _timed_steps(both, stream, args.render_frames, torch)
+        forms["render"] = {"workload": "the reference application's frame: 80^3 scene after 50 steps, "
+                                       "%dx%d eye buffer, %d^2 light buffer, %d half-angle planes, "
+                                       "RGBA16F buffers (smk_render, 2 kernels per frame); the reference's "
+                                       "OpenGL path and its 110 fps (RTX 3070) are unavailable on this box"
+                                       % (rp.width, rp.height, rp.light_res, rp.planes),
+                           "ms_per_frame": 1e3 * f_s / args.render_frames,
+                           "frames_per_s": args.render_frames / f_s,
+                           "step_plus_frame_per_s": args.render_frames / b_s,
+                           "covered_pixels": float((eye[..., 3] > 0.01).float().mean().item())}
+        sim.close()
 
     # ---- serving: Poisson stream, continuous admission ----------------------------------------
     if args.serve_requests > 0:

@@ -273,9 +273,6 @@ int smk_server_request_status(smk_server* server, int id, int* state, int* steps
  * finished request does nothing. */
 int smk_server_cancel(smk_server* server, int id);
 
-/* Testing: the next `count` smk_create calls fail with SMK_ERR_OOM as a device allocation
- * failure would, without touching the device (host-side fault injection). */
-int smk_inject_alloc_failures(int count);
 int smk_server_get_stats(smk_server* server, smk_server_stats* out);
 int smk_server_destroy(smk_server* server);
 const char* smk_server_last_error(void);
@@ -298,6 +295,43 @@ int smk_project_noalloc(float* u, float* v, float* w, const uint8_t* mask, int n
 /* The size limit above, and the message of the last failed smk_project_noalloc call. */
 long long smk_project_noalloc_max_elems(void);
 const char* smk_project_noalloc_last_error(void);
+
+/* Headless volume renderer: the reference's half-angle slice compositing with a light buffer
+ * (project/texVolume.frag:27-52, light.frag:16-23, the two-pass drawing and blend equations of
+ * main.cpp:369-419, 474-476, 660-661, 676-687, proxy planes of boundingBox.cpp:135-181,
+ * 228-345) restated as CUDA kernels writing device images; no graphics API is used.  Proxy
+ * plane i (of `planes`, perpendicular to the half vector between the view and light directions)
+ * is drawn into the eye buffer (density x light-buffer colour, blended front-to-back when camera
+ * and light face the same way, else back-to-front) and then into the light buffer (colour x
+ * (1 - density)).  Both buffers hold half-precision RGBA as the reference's RGBA16F framebuffers
+ * do.  Defaults are the reference application's (camera, light, 512^2 light buffer, 100 planes,
+ * 45-degree perspectives with near 5 / far 2000, box at the origin with unit cells). */
+typedef struct smk_render_params {
+    int width, height;        /* eye image (the reference: the window) */
+    int light_res;            /* light buffer side (lightMapResolution 512) */
+    int planes;               /* proxy planes (proxy_step_count 100) */
+    float camera_pos[3];      /* (1, 20, 100) */
+    float camera_dir[3];      /* toward the box centre */
+    float up[3];              /* (0, 1, 0) */
+    float fovy_deg, znear, zfar;                   /* 45, 5, 2000 */
+    float light_pos[3];                            /* (120, 80, 0) */
+    float light_fovy_deg, light_znear, light_zfar; /* 45, 5, 2000 (aspect 1) */
+    float light_color[3];     /* (0.9882, 0.9333, 0.7549) */
+    float box_pos[3];         /* box centre (0, 0, 0) */
+    float cell_size;          /* world units per cell (1) */
+    float bg_color[3];        /* 20/255 grey */
+} smk_render_params;
+void smk_default_render_params(smk_render_params* rp);
+/* Render the simulation's current density.  eye_rgba: device, width*height*4 floats (the eye
+ * buffer, rows bottom-up as in OpenGL); composite_rgb: device, width*height*3 floats (the eye
+ * buffer blended over bg_color as the reference's final pass does) or NULL.  Stream-ordered;
+ * scratch (the light buffer after every plane) is kept with the simulation. */
+int smk_render(smk_sim* sim, const smk_render_params* rp, float* eye_rgba, float* composite_rgb,
+               void* stream);
+
+/* Testing: the next `count` smk_create calls fail with SMK_ERR_OOM as a device allocation
+ * failure would, without touching the device (host-side fault injection). */
+int smk_inject_alloc_failures(int count);
 
 #ifdef __cplusplus
 }

@@ -52,9 +52,9 @@ def _stale(out: str, *srcs: str) -> bool:
 
 def build_restatement(force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
-    src = os.path.join(HERE, "smoke_oracle.cpp")
-    if force or _stale(ORACLE_SO, src):
-        _run(["g++", *CXXFLAGS, src, "-o", ORACLE_SO])
+    srcs = [os.path.join(HERE, "smoke_oracle.cpp"), os.path.join(HERE, "render_oracle.cpp")]
+    if force or any(_stale(ORACLE_SO, s) for s in srcs):
+        _run(["g++", *CXXFLAGS, *srcs, "-o", ORACLE_SO])
     return ORACLE_SO
 
 

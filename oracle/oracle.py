@@ -181,6 +181,31 @@ class OracleSim:
         return self.rho[self.past]
 
 
+def render(rho: np.ndarray, params) -> tuple:
+    """The renderer restatement (render_oracle.cpp) on a density array [nz, ny, nx]; params: an
+    smk_render_params-layout structure.  Returns (eye RGBA, composite RGB), rows bottom-up."""
+    lib = restatement()
+    r = np.ascontiguousarray(rho, np.float32)
+    nz, ny, nx = r.shape
+    eye = np.zeros((params.height, params.width, 4), np.float32)
+    comp = np.zeros((params.height, params.width, 3), np.float32)
+    fn = lib.orc_render
+    fn.restype = C.c_int
+    fn.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+    fn(r.ctypes.data, nx, ny, nz, C.addressof(params), eye.ctypes.data, comp.ctypes.data)
+    return eye, comp
+
+
+def round_half(x: np.ndarray) -> np.ndarray:
+    """The restatement's float -> binary16 -> float rounding (round to nearest even)."""
+    lib = restatement()
+    a = np.ascontiguousarray(x, np.float32)
+    out = np.empty_like(a)
+    lib.orc_round_half.argtypes = [C.c_void_p, C.c_void_p, C.c_int]
+    lib.orc_round_half(a.ctypes.data, out.ctypes.data, a.size)
+    return out
+
+
 class RefHostSim:
     """The reference's own step (host build), driven through its public API."""
 

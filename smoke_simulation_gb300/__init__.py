@@ -53,6 +53,16 @@ class HostState(C.Structure):
                 ("w", C.c_void_p * 2), ("s", C.c_void_p), ("index_now", C.c_int)]
 
 
+class RenderParams(C.Structure):
+    """smk_render_params: the headless renderer's camera, light and buffers."""
+    _fields_ = [("width", C.c_int), ("height", C.c_int), ("light_res", C.c_int), ("planes", C.c_int),
+                ("camera_pos", C.c_float * 3), ("camera_dir", C.c_float * 3), ("up", C.c_float * 3),
+                ("fovy_deg", C.c_float), ("znear", C.c_float), ("zfar", C.c_float),
+                ("light_pos", C.c_float * 3), ("light_fovy_deg", C.c_float), ("light_znear", C.c_float),
+                ("light_zfar", C.c_float), ("light_color", C.c_float * 3), ("box_pos", C.c_float * 3),
+                ("cell_size", C.c_float), ("bg_color", C.c_float * 3)]
+
+
 _lib = None
 
 
@@ -98,6 +108,8 @@ def lib() -> C.CDLL:
         "smk_autotune": (i, [vp, C.POINTER(i), C.POINTER(i), C.POINTER(f)]),
         "smk_set_graphs": (i, [vp, i]),
         "smk_set_graph_loops": (i, [vp, i]),
+        "smk_default_render_params": (None, [C.c_void_p]),
+        "smk_render": (i, [vp, C.c_void_p, vp, vp, vp]),
         "smk_batch_create": (i, [i, C.POINTER(vp), C.POINTER(vp)]),
         "smk_batch_step": (i, [vp, C.POINTER(f), f, vp]),
         "smk_batch_destroy": (i, [vp]),
@@ -224,6 +236,24 @@ class Simulation:
         _check(lib().smk_read_density(self.h, _ptr(out), 0, None))
         _check(lib().smk_sync(self.h, None))
         return out
+
+    def render(self, params: Optional["RenderParams"] = None, **overrides):
+        """Render the current density with the headless half-angle slice renderer; returns
+        (eye RGBA [height, width, 4], composite RGB [height, width, 3]) as numpy arrays, rows
+        bottom-up."""
+        import torch
+        rp = params if params is not None else default_render_params()
+        for k, v in overrides.items():
+            setattr(rp, k, v)
+        eye = torch.empty((rp.height, rp.width, 4), dtype=torch.float32, device="cuda")
+        comp = torch.empty((rp.height, rp.width, 3), dtype=torch.float32, device="cuda")
+        _check(lib().smk_render(self.h, C.byref(rp), eye.data_ptr(), comp.data_ptr(), None))
+        _check(lib().smk_sync(self.h, None))
+        return eye.cpu().numpy(), comp.cpu().numpy()
+
+    def render_into(self, eye_ptr: int, comp_ptr: int, params: "RenderParams", stream: int = 0):
+        """Stream-ordered smk_render into caller-owned device buffers (no synchronisation)."""
+        _check(lib().smk_render(self.h, C.byref(params), eye_ptr, comp_ptr or None, stream))
 
     def read_density_device(self, dev_ptr: int, stream: int = 0):
         _check(lib().smk_read_density(self.h, dev_ptr, 1, stream))
@@ -366,6 +396,14 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+def default_render_params(**overrides) -> RenderParams:
+    rp = RenderParams()
+    lib().smk_default_render_params(C.byref(rp))
+    for k, v in overrides.items():
+        setattr(rp, k, v)
+    return rp
 
 
 def params_for_scene(scene, **overrides) -> Params:

@@ -20,8 +20,11 @@ LIB = os.path.join(HERE, "libsmoke_gb300.so")
 ROOT = os.path.dirname(HERE)
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# -fmad=false (device) and -ffp-contract=off (host: g++ contracts a*b+c into FMA by default on
+# aarch64) keep every float expression rounding as written, on the device and the host side.
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC",
-              "-Xcompiler", "-O3", "--expt-relaxed-constexpr", "-I", os.path.join(ROOT, "include")]
+              "-Xcompiler", "-O3", "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr",
+              "-I", os.path.join(ROOT, "include")]
 
 
 def nvcc() -> str:

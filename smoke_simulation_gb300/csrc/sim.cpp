@@ -142,6 +142,7 @@ void smk_sim::release() {
     if (pcur) cudaFree(pcur);
     if (loop_launches) cudaFree(loop_launches);
     if (refine) cudaFree(refine);
+    if (render_scratch) cudaFree(render_scratch);
     if (maps) destroy_sweep_maps(maps);
     if (s) cudaFree(s);
     if (flags) cudaFree(flags);

@@ -69,6 +69,8 @@ struct smk_sim {
     int* gcount = nullptr;  // device: tolerance groups done by a graph's device-side group loop
     unsigned long long* loop_launches = nullptr;  // device: kernels launched by those loops
     smk::RefineStatus* refine = nullptr;          // device: FP64-checked refinement rounds
+    void* render_scratch = nullptr;               // device: the renderer's light buffer per plane
+    size_t render_scratch_bytes = 0;
     smk::SweepMaps* maps = nullptr;  // TMA tensor maps of P, P2, b, flags
     uint8_t* s = nullptr;
     uint8_t* flags = nullptr;
