@@ -134,30 +134,69 @@ __global__ void k_refine_reset(RefineStatus* rs, int start) {
     }
 }
 
-template <bool WRITE>
+// The refinement kernels are persistent: a fixed grid (a few CTAs per SM) walks the stage's
+// 64 x 4 blocks, so a round that is not needed costs only that grid's exit, not a full-size launch.
+__device__ __forceinline__ uint3 vblock(int vb, int nbx, int nby) {
+    uint3 b;
+    b.x = (unsigned)(vb % nbx);
+    b.y = (unsigned)((vb / nbx) % nby);
+    b.z = (unsigned)(vb / (nbx * nby));
+    return b;
+}
+
+// FP64 |div u| per projectable cell (read only): the max (as IEEE bits) and whether any cell
+// exceeds tol.
 __global__ void k_refine_measure(Grid g, const float* u, const float* v, const float* w,
-                                 const uint8_t* __restrict__ flags, float* b, float* P0, float* P1,
-                                 const int* pcur, RefineStatus* rs, double tol) {
+                                 const uint8_t* __restrict__ flags, RefineStatus* rs, double tol, int nbx,
+                                 int nby, int nvb) {
     if (*(volatile int*)&rs->stop) return;
-    const int x = (int)blockIdx.x * BX + (int)threadIdx.x;
-    const int y = (int)blockIdx.y * BY + (int)threadIdx.y;
-    const int z = (int)blockIdx.z;
     double m = 0.0;
-    if (x < g.nx && y < g.ny && z < g.nz) {
+    for (int vb = (int)blockIdx.x; vb < nvb; vb += (int)gridDim.x) {
+        const uint3 bid = vblock(vb, nbx, nby);
+        const int x = (int)bid.x * BX + (int)threadIdx.x;
+        const int y = (int)bid.y * BY + (int)threadIdx.y;
+        const int z = (int)bid.z;
+        if (x < g.nx && y < g.ny && z < g.nz) {
+            const int i = g.idx(x, y, z);
+            if (flags[i] & F_PROJ) {
+                const double d = ((((-(double)u[i] + (double)u[i + 1]) + -(double)v[i]) + (double)v[i + g.X]) +
+                                  -(double)w[i]) + (double)w[i + g.XY];
+                const double a = fabs(d);
+                if (!(a <= m)) m = a;  // NaN propagates as the largest value
+            }
+        }
+    }
+    // one flag store and at most one atomic per CTA, each only when it changes the stored value
+    const int any = __syncthreads_or(m > tol);
+    const unsigned long long bm = block_max_u64((unsigned long long)__double_as_longlong(m));
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        if (any && *(volatile int*)&rs->need == 0) rs->need = 1;
+        if (bm > *(volatile unsigned long long*)&rs->div_bits) atomicMax(&rs->div_bits, bm);
+    }
+}
+
+// A round that is needed: b = (float)(-d) (0 off the projectable set) and e = 0 over every cell.
+__global__ void k_refine_prepare(Grid g, const float* u, const float* v, const float* w,
+                                 const uint8_t* __restrict__ flags, float* b, float* P0, float* P1,
+                                 const int* pcur, const RefineStatus* rs, int nbx, int nby, int nvb) {
+    if (*(volatile const int*)&rs->stop) return;
+    float* e = (*pcur == 1) ? P0 : P1;
+    for (int vb = (int)blockIdx.x; vb < nvb; vb += (int)gridDim.x) {
+        const uint3 bid = vblock(vb, nbx, nby);
+        const int x = (int)bid.x * BX + (int)threadIdx.x;
+        const int y = (int)bid.y * BY + (int)threadIdx.y;
+        const int z = (int)bid.z;
+        if (x >= g.nx || y >= g.ny || z >= g.nz) continue;
         const int i = g.idx(x, y, z);
         if (flags[i] & F_PROJ) {
             const double d = ((((-(double)u[i] + (double)u[i + 1]) + -(double)v[i]) + (double)v[i + g.X]) +
                               -(double)w[i]) + (double)w[i + g.XY];
-            m = fabs(d);
-            if (WRITE) b[i] = (float)(-d);
-            if (m > tol) rs->need = 1;
-        } else if (WRITE) {
+            b[i] = (float)(-d);
+        } else {
             b[i] = 0.0f;
         }
-        if (WRITE) ((*pcur == 1) ? P0 : P1)[i] = 0.0f;
+        e[i] = 0.0f;
     }
-    const unsigned long long bm = block_max_u64((unsigned long long)__double_as_longlong(m));
-    if (threadIdx.x == 0 && threadIdx.y == 0 && bm > 0ull) atomicMax(&rs->div_bits, bm);
 }
 
 __global__ void k_refine_decide(RefineStatus* rs) {
@@ -166,44 +205,58 @@ __global__ void k_refine_decide(RefineStatus* rs) {
 
 __global__ void k_refine_sweep(Grid g, float* P0, float* P1, const int* pcur, const float* b,
                                const uint8_t* __restrict__ flags, int colour, WAcc wa,
-                               const RefineStatus* rs) {
+                               const RefineStatus* rs, int nbx, int nby, int nvb) {
     if (*(volatile const int*)&rs->stop) return;
     float* e = (*pcur == 1) ? P0 : P1;
-    body_sweep(g, e, b, flags, colour, wa, nullptr, blockIdx);
+    for (int vb = (int)blockIdx.x; vb < nvb; vb += (int)gridDim.x)
+        body_sweep(g, e, b, flags, colour, wa, nullptr, vblock(vb, nbx, nby));
 }
 
 template <typename Tv>
 __global__ void k_refine_apply(Grid g, float* u, float* v, float* w, Tv* us, Tv* vs, Tv* ws, float* P0,
                                float* P1, const int* pcur, const uint8_t* __restrict__ flags,
-                               RefineStatus* rs) {
+                               RefineStatus* rs, int nbx, int nby, int nvb) {
     if (*(volatile int*)&rs->stop) return;
     const bool second = *pcur == 1;
     float* Pc = second ? P1 : P0;
     const float* e = second ? P0 : P1;
-    if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 && threadIdx.y == 0)
-        rs->rounds += 1;
-    const int x = 1 + (int)blockIdx.x * BX + (int)threadIdx.x;
-    const int y = 1 + (int)blockIdx.y * BY + (int)threadIdx.y;
-    const int z = 1 + (int)blockIdx.z;
-    if (x >= g.nx || y >= g.ny || z >= g.nz) return;
-    const int i = g.idx(x, y, z);
-    const uint8_t f = flags[i];
-    if (!(f & F_SELF)) return;
-    const bool inx = x <= g.nx - 2, iny = y <= g.ny - 2, inz = z <= g.nz - 2;
-    const float ec = e[i];
-    if (iny && inz && (f & F_XM)) {
-        u[i] = u[i] - (ec - e[i - 1]);
-        if (us) stv(us, i, u[i]);
+    if (blockIdx.x == 0 && threadIdx.x == 0 && threadIdx.y == 0) rs->rounds += 1;
+    for (int vb = (int)blockIdx.x; vb < nvb; vb += (int)gridDim.x) {
+        const uint3 bid = vblock(vb, nbx, nby);
+        const int x = 1 + (int)bid.x * BX + (int)threadIdx.x;
+        const int y = 1 + (int)bid.y * BY + (int)threadIdx.y;
+        const int z = 1 + (int)bid.z;
+        if (x >= g.nx || y >= g.ny || z >= g.nz) continue;
+        const int i = g.idx(x, y, z);
+        const uint8_t f = flags[i];
+        if (!(f & F_SELF)) continue;
+        const bool inx = x <= g.nx - 2, iny = y <= g.ny - 2, inz = z <= g.nz - 2;
+        const float ec = e[i];
+        if (iny && inz && (f & F_XM)) {
+            u[i] = u[i] - (ec - e[i - 1]);
+            if (us) stv(us, i, u[i]);
+        }
+        if (inx && inz && (f & F_YM)) {
+            v[i] = v[i] - (ec - e[i - g.X]);
+            if (vs) stv(vs, i, v[i]);
+        }
+        if (inx && iny && (f & F_ZM)) {
+            w[i] = w[i] - (ec - e[i - g.XY]);
+            if (ws) stv(ws, i, w[i]);
+        }
+        if (inx && iny && inz) Pc[i] = Pc[i] + ec;
     }
-    if (inx && inz && (f & F_YM)) {
-        v[i] = v[i] - (ec - e[i - g.X]);
-        if (vs) stv(vs, i, v[i]);
+}
+
+int refine_ctas() {
+    static int ctas = 0;
+    if (ctas == 0) {
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        ctas = (sms > 0 ? sms : 132) * 8;
     }
-    if (inx && iny && (f & F_ZM)) {
-        w[i] = w[i] - (ec - e[i - g.XY]);
-        if (ws) stv(ws, i, w[i]);
-    }
-    if (inx && iny && inz) Pc[i] = Pc[i] + ec;
+    return ctas;
 }
 
 }  // namespace
@@ -216,28 +269,32 @@ void launch_refine(const Grid& g, float* u, float* v, float* w, Tv* us, Tv* vs, 
     WAcc wa;
     for (int k = 0; k < 7; ++k) wa.w[k] = wacc7[k];
     wa.w[7] = 0.0f;
-    const int half = (g.nx - 2 + 1) / 2;
     const dim3 blk(BX, BY);
+    const int ctas = refine_ctas();
+    auto grid_of = [ctas](int nvb) { return dim3((unsigned)(nvb < ctas ? nvb : ctas)); };
+    // block ranges of the single-grid launches of each stage
+    const dim3 cells = grid3(g.nx, g.ny, g.nz);
+    const int cbx = (int)cells.x, cby = (int)cells.y, cnv = cbx * cby * (int)cells.z;
+    const int half = (g.nx - 2 + 1) / 2;
+    const dim3 sw = grid3(half, g.ny - 2, g.nz - 2);
+    const int sbx = (int)sw.x, sby = (int)sw.y, snv = sbx * sby * (int)sw.z;
+    const dim3 fc = grid3(g.nx - 1, g.ny - 1, g.nz - 1);
+    const int fbx = (int)fc.x, fby = (int)fc.y, fnv = fbx * fby * (int)fc.z;
     k_refine_reset<<<1, 1, 0, st>>>(rs, 1);
-    k_refine_measure<true><<<grid3(g.nx, g.ny, g.nz), blk, 0, st>>>(g, u, v, w, flags, b, P0, P1, pcur, rs, tol);
+    k_refine_measure<<<grid_of(cnv), blk, 0, st>>>(g, u, v, w, flags, rs, tol, cbx, cby, cnv);
     k_refine_decide<<<1, 1, 0, st>>>(rs);
     *launches += 3;
     for (int r = 0; r < rounds; ++r) {
+        k_refine_prepare<<<grid_of(cnv), blk, 0, st>>>(g, u, v, w, flags, b, P0, P1, pcur, rs, cbx, cby, cnv);
         for (int s = 0; s < sweeps; ++s)
             for (int colour = 0; colour < 2; ++colour)
-                k_refine_sweep<<<grid3(half, g.ny - 2, g.nz - 2), blk, 0, st>>>(g, P0, P1, pcur, b, flags, colour,
-                                                                                wa, rs);
-        k_refine_apply<Tv><<<grid3(g.nx - 1, g.ny - 1, g.nz - 1), blk, 0, st>>>(g, u, v, w, us, vs, ws, P0, P1,
-                                                                               pcur, flags, rs);
+                k_refine_sweep<<<grid_of(snv), blk, 0, st>>>(g, P0, P1, pcur, b, flags, colour, wa, rs, sbx, sby, snv);
+        k_refine_apply<Tv><<<grid_of(fnv), blk, 0, st>>>(g, u, v, w, us, vs, ws, P0, P1, pcur, flags, rs, fbx, fby,
+                                                         fnv);
         k_refine_reset<<<1, 1, 0, st>>>(rs, 0);
-        if (r + 1 < rounds)
-            k_refine_measure<true><<<grid3(g.nx, g.ny, g.nz), blk, 0, st>>>(g, u, v, w, flags, b, P0, P1, pcur,
-                                                                           rs, tol);
-        else
-            k_refine_measure<false><<<grid3(g.nx, g.ny, g.nz), blk, 0, st>>>(g, u, v, w, flags, b, P0, P1, pcur,
-                                                                            rs, tol);
+        k_refine_measure<<<grid_of(cnv), blk, 0, st>>>(g, u, v, w, flags, rs, tol, cbx, cby, cnv);
         k_refine_decide<<<1, 1, 0, st>>>(rs);
-        *launches += 2 * sweeps + 4;
+        *launches += 2 * sweeps + 5;
     }
 }
 template void launch_refine<float>(const Grid&, float*, float*, float*, float*, float*, float*, float*, float*,
