@@ -67,6 +67,11 @@ typedef struct smk_params {
                            for a correction (refine_sweeps FP32 sweeps on the FP64 divergence,
                            rounded) and applies it to the velocity and the pressure. */
     int refine_sweeps;  /* sweeps of each correction solve */
+    int obstacle_velocity; /* 1: the obstacles' velocity (stored but unused by the reference,
+                              smokeSimulation.cu:299-301) drives the fluid: after forcing, every
+                              face touching a cell of the last obstacle (the one that decides the
+                              mask) takes that obstacle's velocity, a moving boundary the
+                              projection then respects.  0 (default): the reference's behaviour. */
 } smk_params;
 
 typedef struct smk_stats {

@@ -32,7 +32,7 @@ class OrcParams(C.Structure):
         ("spheres", _F), ("n_spheres", C.c_int),
         ("boxes", _F), ("n_boxes", C.c_int),
         ("obstacles", _F), ("n_obstacles", C.c_int),
-        ("refine", C.c_int), ("refine_sweeps", C.c_int),
+        ("refine", C.c_int), ("refine_sweeps", C.c_int), ("obstacle_velocity", C.c_int),
     ]
 
 
@@ -151,6 +151,7 @@ class OracleSim:
         p.boxes, p.n_boxes = _fptr(self.boxes), self.n_boxes
         p.obstacles, p.n_obstacles = _fptr(self.obstacles), self.n_obstacles
         p.refine, p.refine_sweeps = getattr(sc, "refine", 0), getattr(sc, "refine_sweeps", 10)
+        p.obstacle_velocity = getattr(sc, "obstacle_velocity", 0)
         return p
 
     def step(self, dt: Optional[float] = None) -> OrcStats:

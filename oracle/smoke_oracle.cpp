@@ -53,6 +53,7 @@ typedef struct {
     const float* obstacles; int n_obstacles;
     int refine;          // scheme 1 with tol > 0: FP64-checked refinement rounds (0: none)
     int refine_sweeps;   // sweeps of each correction solve
+    int obstacle_velocity;  // 1: faces touching a cell of the last obstacle take its velocity
 } orc_params;
 
 typedef struct {
@@ -549,6 +550,28 @@ float max_div(const Dims& d, const T* u, const T* v, const T* w, const uint8_t* 
     return (float)m;
 }
 
+// Moving-obstacle boundary (no counterpart in the reference, which stores the obstacles'
+// velocity without using it, :299-301): after forcing, every face with a cell of obstacle `o`
+// (interior, inside its sphere by fillObstacle's test) on either side takes o's velocity.
+template <typename T>
+void obstacle_velocity(const Dims& d, T* u, T* v, T* w, const float* o) {
+    auto cell = [&](int x, int y, int z) {
+        if (x < 1 || y < 1 || z < 1 || x > d.nx - 2 || y > d.ny - 2 || z > d.nz - 2) return false;
+        const float dx = (float)x - o[0], dy = (float)y - o[1], dz = (float)z - o[2];
+        const float dist = dx * dx + dy * dy + dz * dz;
+        return dist < o[6] * o[6];
+    };
+    for (int z = 0; z <= d.nz; ++z)
+        for (int y = 0; y <= d.ny; ++y)
+            for (int x = 0; x <= d.nx; ++x) {
+                const long long i = d.f(x, y, z);
+                const bool c = cell(x, y, z);
+                if (x >= 1 && x <= d.nx - 1 && y < d.ny && z < d.nz && (c || cell(x - 1, y, z))) u[i] = (T)o[3];
+                if (y >= 1 && y <= d.ny - 1 && x < d.nx && z < d.nz && (c || cell(x, y - 1, z))) v[i] = (T)o[4];
+                if (z >= 1 && z <= d.nz - 1 && x < d.nx && y < d.ny && (c || cell(x, y, z - 1))) w[i] = (T)o[5];
+            }
+}
+
 // FP64-checked refinement after the pressure projection (no counterpart in the reference).  A
 // round measures d = ((((-u0 + u1) + -v0) + v1) + -w0) + w1 per projectable cell in double from
 // the FP32 faces; when some |d| > tol it solves A e = (float)(-d) from e = 0 with `sweeps`
@@ -645,6 +668,8 @@ int step(orc_state* S, const orc_params* p, float dt, orc_stats* st) {
     if (p->n_obstacles) fill_obstacles(d, S->s, p->obstacles, p->n_obstacles);
     forcing<T>(d, u[now], v[now], w[now], rho[now], S->s, dt, p->gravity, p->buoyancy,
                p->clamp_const, p->clamp_mode);
+    if (p->obstacle_velocity && p->n_obstacles)
+        obstacle_velocity<T>(d, u[now], v[now], w[now], p->obstacles + 7 * (p->n_obstacles - 1));
     orc_stats local{};
     if (p->scheme == 0) {
         project_velocity<T>(d, u[now], v[now], w[now], S->s, p->iterations, p->omega);

@@ -35,7 +35,7 @@ class Params(C.Structure):
         ("clamp_mode", C.c_int), ("projection", C.c_int), ("max_sweeps", C.c_int),
         ("omega", C.c_double), ("tol", C.c_float), ("check_every", C.c_int),
         ("warm_start", C.c_int), ("report_div", C.c_int), ("storage", C.c_int),
-        ("refine", C.c_int), ("refine_sweeps", C.c_int),
+        ("refine", C.c_int), ("refine_sweeps", C.c_int), ("obstacle_velocity", C.c_int),
     ]
 
 
@@ -413,6 +413,7 @@ def params_for_scene(scene, **overrides) -> Params:
     p.projection, p.max_sweeps, p.omega = scene.scheme, scene.iterations, scene.omega
     p.tol, p.check_every, p.warm_start = scene.tol, scene.check_every, scene.warm_start
     p.refine, p.refine_sweeps = scene.refine, scene.refine_sweeps
+    p.obstacle_velocity = scene.obstacle_velocity
     for k, v in overrides.items():
         setattr(p, k, v)
     return p

@@ -277,7 +277,8 @@ int launch_config(const GroupSchedule& sched, const TableImage& t, GroupLaunch& 
 bool grouped_eligible(smk_sim* const* sims, int n) {
     if (n > MAX_GROUPED) return false;
     for (int i = 0; i < n; ++i)
-        if (sims[i]->p.projection != SMK_PROJECT_PRESSURE || sims[i]->p.refine > 0) return false;
+        if (sims[i]->p.projection != SMK_PROJECT_PRESSURE || sims[i]->p.refine > 0 || sims[i]->p.obstacle_velocity)
+            return false;
     return true;
 }
 

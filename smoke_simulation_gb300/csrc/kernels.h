@@ -22,6 +22,11 @@ void launch_fill_obstacles(const Grid& g, uint8_t* s, const ObstacleObj* ob, int
 // Neighbour flags from the mask; zeroes the pressure where a cell is not projectable.
 void launch_build_flags(const Grid& g, const uint8_t* s, uint8_t* flags, float* P, cudaStream_t st);
 
+// Moving-obstacle boundary (smk_params.obstacle_velocity): faces touching a cell of `last`
+// take its velocity.
+template <typename Tv>
+void launch_obstacle_velocity(const Grid& g, Tv* u, Tv* v, Tv* w, const ObstacleObj& last, cudaStream_t st);
+
 // Stage b: integrate (forcing) + velocityConfinement (clamp), fused.
 template <typename Tv, typename T>
 void launch_forcing(const Grid& g, Tv* u, Tv* v, Tv* w, const T* rho,

@@ -43,6 +43,30 @@ __global__ void k_fill_smoke(Grid g, T* __restrict__ rho0, T* __restrict__ rho1,
     body_fill_smoke(g, rho0, rho1, L.s, L.n, x0, y0, z0, x1, y1, z1, blockIdx);
 }
 
+// A cell the obstacle makes solid: interior, and inside its sphere by fillObstacle's test.
+__device__ __forceinline__ bool obstacle_cell(const Grid& g, const ObstacleObj& o, int x, int y, int z) {
+    if (x < 1 || y < 1 || z < 1 || x > g.nx - 2 || y > g.ny - 2 || z > g.nz - 2) return false;
+    const float dx = (float)x - o.x, dy = (float)y - o.y, dz = (float)z - o.z;
+    const float dist = dx * dx + dy * dy + dz * dz;
+    return dist < o.r * o.r;
+}
+
+// Moving-obstacle boundary: every face with a cell of obstacle `o` on either side takes the
+// obstacle's velocity component.  One thread per staggered index (x, y, z) <= (nx, ny, nz).
+template <typename Tv>
+__global__ void k_obstacle_velocity(Grid g, Tv* __restrict__ u, Tv* __restrict__ v, Tv* __restrict__ w,
+                                    ObstacleObj o) {
+    const int x = blockIdx.x * BX + threadIdx.x;
+    const int y = blockIdx.y * BY + threadIdx.y;
+    const int z = blockIdx.z;
+    if (x > g.nx || y > g.ny || z > g.nz) return;
+    const int i = g.idx(x, y, z);
+    const bool c = obstacle_cell(g, o, x, y, z);
+    if (x >= 1 && x <= g.nx - 1 && y < g.ny && z < g.nz && (c || obstacle_cell(g, o, x - 1, y, z))) stv(u, i, o.vx);
+    if (y >= 1 && y <= g.ny - 1 && x < g.nx && z < g.nz && (c || obstacle_cell(g, o, x, y - 1, z))) stv(v, i, o.vy);
+    if (z >= 1 && z <= g.nz - 1 && x < g.nx && y < g.ny && (c || obstacle_cell(g, o, x, y, z - 1))) stv(w, i, o.vz);
+}
+
 // fillObstacle (smokeSimulation.cu:289-313): interior cells; each obstacle overwrites the
 // cell, so the last one decides.
 __global__ void k_fill_obstacles(Grid g, uint8_t* __restrict__ s, ObstacleList L) {
@@ -232,6 +256,14 @@ void launch_fill_obstacles(const Grid& g, uint8_t* s, const ObstacleObj* ob, int
     L.o[0] = ob[no - 1];
     k_fill_obstacles<<<grid3(g.nx - 2, g.ny - 2, g.nz - 2), dim3(BX, BY), 0, st>>>(g, s, L);
 }
+
+template <typename Tv>
+void launch_obstacle_velocity(const Grid& g, Tv* u, Tv* v, Tv* w, const ObstacleObj& last, cudaStream_t st) {
+    k_obstacle_velocity<Tv><<<grid3(g.nx + 1, g.ny + 1, g.nz + 1), dim3(BX, BY), 0, st>>>(g, u, v, w, last);
+}
+template void launch_obstacle_velocity<float>(const Grid&, float*, float*, float*, const ObstacleObj&, cudaStream_t);
+template void launch_obstacle_velocity<__nv_bfloat16>(const Grid&, __nv_bfloat16*, __nv_bfloat16*, __nv_bfloat16*,
+                                                      const ObstacleObj&, cudaStream_t);
 
 void launch_build_flags(const Grid& g, const uint8_t* s, uint8_t* flags, float* P, cudaStream_t st) {
     k_build_flags<<<grid3(g.nx, g.ny, g.nz), dim3(BX, BY), 0, st>>>(g, s, flags, P);

@@ -223,6 +223,11 @@ int smk_sim::enqueue(float dt, cudaStream_t st) {
         launch_forcing(g, u[now], v[now], w[now], (const float*)rho[now], flags, dt, p.gravity, p.buoyancy,
                        p.clamp_const, p.clamp_mode, st);
     ++launches;
+    if (p.obstacle_velocity && !obstacles.empty()) {
+        if (bf16) launch_obstacle_velocity(g, bf(u[now]), bf(v[now]), bf(w[now]), obstacles.back(), st);
+        else launch_obstacle_velocity(g, u[now], v[now], w[now], obstacles.back(), st);
+        ++launches;
+    }
     if (timed) SMK_CUDA(rec(ev[2]));
 
     // c/d: projection (:795-801)

@@ -90,6 +90,7 @@ class Scene:
     warm_start: int = 0
     refine: int = 0                            # FP64-checked refinement rounds (pressure, tol > 0)
     refine_sweeps: int = 10
+    obstacle_velocity: int = 0                 # 1: obstacles' velocity drives the fluid
 
     @property
     def cells(self) -> int:

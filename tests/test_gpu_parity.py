@@ -320,3 +320,25 @@ def test_refinement_bf16_velocities_lowers_divergence(gpu):
     assert b.refine_rounds == 3 and b.div64_max < 0.2 * a.div_max
     plain.close()
     ref.close()
+
+
+@pytest.mark.parametrize("scheme", [0, 1])
+def test_moving_obstacle_velocity_bit_exact(gpu, scheme):
+    """An obstacle moved every step whose velocity drives the fluid (obstacle_velocity = 1):
+    bit-exact with the oracle in both projection schemes."""
+    sc = S.small_scene(28, 24, 30, steps=6, seed=41, scheme=scheme, iterations=30, obstacles=0)
+    if scheme == 1:
+        sc.tol, sc.check_every = 1e-4, 5
+    sc.obstacle_velocity = 1
+    sc.obstacles = [(10.0, 12.0, 15.0, 1.5, 0.25, -0.5, 4.0)]
+    sim = smk.from_scene(sc)
+    o = O.OracleSim(sc)
+    oid = len(sc.boxes) + len(sc.spheres)
+    for k in range(sc.steps):
+        pos = (10.0 + 1.5 * sc.dt * (k + 1) * 10.0, 12.0, 15.0 - 0.5 * sc.dt * (k + 1) * 10.0)
+        sim.update_object_pos(oid, *pos)
+        o.obstacles[0, :3] = pos
+        sim.step(sc.dt)
+        o.step()
+    assert H.first_mismatch(sim.read_state(), H.oracle_state(o)) == ""
+    sim.close()

@@ -185,3 +185,21 @@ def test_refinement_rounds_reduce_fp64_divergence():
     assert out[(3, 1e-5)].div64_max < out[(1, 1e-5)].div64_max < out[(0, 1e-5)].div_max
     assert out[(3, 10.0)].refine_rounds == 0
     assert 0.0 <= out[(3, 10.0)].div64_max <= 10.0
+
+
+def test_obstacle_velocity_drives_the_fluid():
+    """With obstacle_velocity on, the fluid next to a moving obstacle moves with it; with it off
+    (the reference), the obstacle's stored velocity has no effect."""
+    from smoke_simulation_gb300 import scenes as S
+    res = {}
+    for on in (0, 1):
+        for vx in (0.0, 2.0):
+            sc = S.small_scene(24, 20, 24, steps=4, seed=43, scheme=1, iterations=40, obstacles=0, noise=0.0)
+            sc.tol, sc.check_every, sc.obstacle_velocity = 1e-5, 5, on
+            sc.obstacles = [(12.0, 10.0, 12.0, vx, 0.0, 0.0, 4.0)]
+            o = O.OracleSim(sc)
+            o.run()
+            res[(on, vx)] = o.u[o.past].copy()
+    assert np.array_equal(res[(0, 0.0)], res[(0, 2.0)])  # reference: velocity stored, unused
+    near = np.s_[6:14, 6:14, 14:20]                       # (z, y, x) just past the obstacle
+    assert np.abs(res[(1, 2.0)][near]).max() > 5 * np.abs(res[(1, 0.0)][near]).max() + 0.1
