@@ -334,6 +334,15 @@ void smk_default_render_params(smk_render_params* rp);
 int smk_render(smk_sim* sim, const smk_render_params* rp, float* eye_rgba, float* composite_rgb,
                void* stream);
 
+/* Proxy-slice geometry on the device: the reference's proxy-plane polygons
+ * (boundingBox.cpp:135-181, 228-345) for callers that draw them with a graphics API.  Plane i of
+ * `planes` is perpendicular to normalize(-view_dir) at (i + 0.5) / planes between the box's
+ * extreme projections; outputs (device): vertices planes*7*3 floats (plane i: counts[i] polygon
+ * points sorted by pseudo-angle, then the centroid, rest 0), counts planes ints, triangles
+ * planes*6*3 ints (fan around the centroid, indices into the vertex array; -1 rows unused). */
+int smk_proxy_planes(const float view_origin[3], const float view_dir[3], const float box_pos[3],
+                     const float dims[3], int planes, float* vertices, int* counts, int* triangles, void* stream);
+
 /* Testing: the next `count` smk_create calls fail with SMK_ERR_OOM as a device allocation
  * failure would, without touching the device (host-side fault injection). */
 int smk_inject_alloc_failures(int count);

@@ -197,6 +197,21 @@ def render(rho: np.ndarray, params) -> tuple:
     return eye, comp
 
 
+def proxy_planes(view_origin, view_dir, box_pos, dims, planes: int):
+    """The proxy-plane restatement: (vertices [planes, 7, 3], counts [planes], triangles
+    [planes, 6, 3])."""
+    lib = restatement()
+    f3 = lambda v: np.ascontiguousarray(v, np.float32)
+    vo, vd, bp, dm = f3(view_origin), f3(view_dir), f3(box_pos), f3(dims)
+    verts = np.zeros((planes, 7, 3), np.float32)
+    counts = np.zeros(planes, np.int32)
+    tris = np.zeros((planes, 6, 3), np.int32)
+    lib.orc_proxy_planes.argtypes = [C.c_void_p] * 4 + [C.c_int] + [C.c_void_p] * 3
+    lib.orc_proxy_planes(vo.ctypes.data, vd.ctypes.data, bp.ctypes.data, dm.ctypes.data, planes,
+                         verts.ctypes.data, counts.ctypes.data, tris.ctypes.data)
+    return verts, counts, tris
+
+
 def round_half(x: np.ndarray) -> np.ndarray:
     """The restatement's float -> binary16 -> float rounding (round to nearest even)."""
     lib = restatement()

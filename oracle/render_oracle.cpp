@@ -22,6 +22,7 @@
 // with an OpenGL run is unpinned (no graphics stack on the build machines); this restatement is
 // the definition smk_render is checked against, bit for bit.
 // Build: g++ -O2 -ffp-contract=off (oracle/build_oracle.py).
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -295,6 +296,96 @@ int orc_render(const float* rho, int nx, int ny, int nz, const orc_render_params
                 for (int k = 0; k < 3; ++k) comp_rgb[3 * id + k] = e[k] * e[3] + S.bg[k] * om;
             }
         }
+    return 0;
+}
+
+// Proxy-plane polygons (boundingBox.cpp:135-181, 228-345), the checker of smk_proxy_planes:
+// plane i of P at start + (end - start) * ((i + 0.5) / P) along d = normalize(-view_dir); the
+// box's 12 edges (X edges for y, z in {-1, 1}, then Y edges for x, z, then Z edges for y, x)
+// intersected with the plane (edges parallel to it skipped), exact repeats dropped, centroid
+// appended, points sorted by pseudo-angle about the centroid (descending, std::sort as the
+// reference), fan triangulation.  Output layout as smk_proxy_planes.
+int orc_proxy_planes(const float* view_origin, const float* view_dir, const float* box_pos, const float* dims,
+                     int planes, float* verts, int* counts, int* tris) {
+    const V3 d = norm3(mk(-view_dir[0], -view_dir[1], -view_dir[2]));
+    const V3 box = mk(box_pos[0], box_pos[1], box_pos[2]);
+    const V3 dm = mk(dims[0], dims[1], dims[2]);
+    const V3 half = scl(dm, 0.5f);
+    const V3 vo = mk(view_origin[0], view_origin[1], view_origin[2]);
+    float mn = 0.0f, mx = 0.0f;
+    for (int c = 0; c < 8; ++c) {
+        const V3 corner = mk((c & 1) ? half.x : -half.x, (c & 2) ? half.y : -half.y, (c & 4) ? half.z : -half.z);
+        const float dd = dot3(sub(corner, vo), d);
+        if (c == 0 || dd < mn) mn = dd;
+        if (c == 0 || dd > mx) mx = dd;
+    }
+    const V3 start = add(vo, scl(d, mn)), end = add(vo, scl(d, mx));
+    const int MAXP = 7;
+    for (int i = 0; i < planes; ++i) {
+        const float t = ((float)i + 0.5f) / (float)planes;
+        const V3 o = add(start, scl(sub(end, start), t));
+        std::vector<V3> pts;
+        for (int axis = 0; axis < 3; ++axis)
+            for (int a = -1; a < 2; a += 2)
+                for (int b = -1; b < 2; b += 2) {
+                    V3 ro, rd;
+                    float len;
+                    if (axis == 0) {
+                        ro = sub(box, mk(half.x, half.y * a, half.z * b));
+                        rd = mk(1.0f, 0.0f, 0.0f);
+                        len = dm.x;
+                    } else if (axis == 1) {
+                        ro = sub(box, mk(half.x * a, half.y, half.z * b));
+                        rd = mk(0.0f, 1.0f, 0.0f);
+                        len = dm.y;
+                    } else {
+                        ro = sub(box, mk(half.x * b, half.y * a, half.z));
+                        rd = mk(0.0f, 0.0f, 1.0f);
+                        len = dm.z;
+                    }
+                    const float den = dot3(rd, d);
+                    if (den == 0.0f) continue;
+                    const float tt = dot3(sub(o, ro), d) / den;
+                    if (tt > len || tt < 0.0f) continue;
+                    const V3 p = add(ro, scl(rd, tt));
+                    bool dup = false;
+                    for (const V3& q : pts) dup = dup || (p.x == q.x && p.y == q.y && p.z == q.z);
+                    if (!dup && (int)pts.size() < MAXP - 1) pts.push_back(p);
+                }
+        const int k = (int)pts.size();
+        V3 c = mk(0.0f, 0.0f, 0.0f);
+        for (const V3& q : pts) c = add(c, q);
+        if (k > 0) c = scl(c, 1.0f / (float)k);
+        if (k > 0) {
+            const V3 ax = norm3(sub(pts[0], c));
+            const V3 ay = cross3(d, ax);
+            auto pa = [&](const V3& q) {
+                const V3 v = sub(q, c);
+                const float x = dot3(ax, v), y = dot3(ay, v);
+                const float r = x / (std::fabs(x) + std::fabs(y));
+                return y < 0.0f ? 1.0f + r : 3.0f - r;
+            };
+            std::sort(pts.begin(), pts.end(), [&](const V3& p1, const V3& p2) { return pa(p1) > pa(p2); });
+        }
+        pts.push_back(c);
+        counts[i] = k;
+        for (int q = 0; q < MAXP; ++q) {
+            const V3 p = q <= k ? pts[q] : mk(0.0f, 0.0f, 0.0f);
+            verts[3 * (MAXP * i + q) + 0] = p.x;
+            verts[3 * (MAXP * i + q) + 1] = p.y;
+            verts[3 * (MAXP * i + q) + 2] = p.z;
+        }
+        for (int q = 0; q < MAXP - 1; ++q) {
+            int* tr = tris + 3 * ((MAXP - 1) * i + q);
+            if (k >= 3 && q < k) {
+                tr[0] = MAXP * i + k;
+                tr[1] = MAXP * i + q;
+                tr[2] = MAXP * i + (q + 1 < k ? q + 1 : 0);
+            } else {
+                tr[0] = tr[1] = tr[2] = -1;
+            }
+        }
+    }
     return 0;
 }
 

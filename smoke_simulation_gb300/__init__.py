@@ -398,6 +398,22 @@ class Batch:
             pass
 
 
+def proxy_planes(view_origin, view_dir, box_pos, dims, planes: int):
+    """Proxy-plane polygons on the device (smk_proxy_planes): (vertices [planes, 7, 3], counts
+    [planes], triangles [planes, 6, 3]) as numpy arrays."""
+    import torch
+    f3 = lambda v: (C.c_float * 3)(*[float(x) for x in v])
+    verts = torch.zeros((planes, 7, 3), dtype=torch.float32, device="cuda")
+    counts = torch.zeros(planes, dtype=torch.int32, device="cuda")
+    tris = torch.zeros((planes, 6, 3), dtype=torch.int32, device="cuda")
+    L = lib()
+    L.smk_proxy_planes.argtypes = [C.c_void_p] * 4 + [C.c_int] + [C.c_void_p] * 4
+    _check(L.smk_proxy_planes(f3(view_origin), f3(view_dir), f3(box_pos), f3(dims), planes, verts.data_ptr(),
+                              counts.data_ptr(), tris.data_ptr(), None))
+    torch.cuda.synchronize()
+    return verts.cpu().numpy(), counts.cpu().numpy(), tris.cpu().numpy()
+
+
 def default_render_params(**overrides) -> RenderParams:
     rp = RenderParams()
     lib().smk_default_render_params(C.byref(rp))

@@ -46,3 +46,16 @@ def test_render_simulated_density(gpu, storage):
     assert np.array_equal(eye.view(np.uint32), oe.view(np.uint32))
     assert np.array_equal(comp.view(np.uint32), oc.view(np.uint32))
     sim.close()
+
+
+@pytest.mark.parametrize("view_dir", [(-0.3, -0.2, 0.93), (0.0, 0.0, 1.0), (1.0, 1.0, 0.0), (-0.51, 0.67, -0.2)])
+def test_proxy_planes_bit_exact_with_restatement(gpu, view_dir):
+    """Proxy-plane polygons on the device equal the restatement; every polygon of the default
+    box is a fan of at least 3 triangles around its centroid, inside the box."""
+    dims = (80.0, 80.0, 80.0)
+    v, c, t = smk.proxy_planes((0, 0, 0), view_dir, (0, 0, 0), dims, 50)
+    ov, oc, ot = O.proxy_planes((0, 0, 0), view_dir, (0, 0, 0), dims, 50)
+    assert np.array_equal(c, oc) and np.array_equal(t, ot)
+    assert np.array_equal(v.view(np.uint32), ov.view(np.uint32))
+    assert (c >= 3).all() and (c <= 6).all()
+    assert np.abs(v).max() <= 40.0 + 1e-4
