@@ -27,9 +27,11 @@
 // registers; the loop over z is unrolled by the ring length so every slot is a fixed register.
 // x-neighbours come from the patch or a warp shuffle (a tile row of 32 threads is one warp),
 // y-neighbours from the patch or a shared-memory copy of each in-flight plane, published once
-// per iteration (double-buffered: one barrier per iteration).  The published copy keeps the
-// patch's two columns (A = x0, B = x0+1) in separate float planes, so a warp's y-neighbour read
-// (one column) is 32 consecutive floats: one shared-memory wavefront, not two.
+// per iteration (double-buffered: one barrier per iteration).  All stages of an iteration
+// update the same colour pattern, so a stage needs one value per neighbour row (the row-1 value
+// of the thread above in one column, the row-0 value of the thread below in the other): only
+// those two are published per plane, each as a float plane so a warp's read is 32 consecutive
+// floats (one shared-memory wavefront); the residual plane of check launches publishes all four.
 //
 // Every update is  r = fma(-acc, P_c, b_c + (((P_x- + P_x+) + (P_y- + P_y+)) + (P_z- + P_z+)));
 // P_c = fma(omega/acc, r, P_c), the oracle's order, so every launch shape gives the same bits
@@ -151,7 +153,9 @@ k_sweep_tb(const __grid_constant__ TBMaps maps, Grid g, float* __restrict__ Pout
     // TMA destinations must be 128-byte aligned: align the dynamic base explicitly (the launch
     // requests 128 spare bytes)
     unsigned char* stages = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);  // [S][STAGE_BYTES]
-    // published planes: [2 buffers][T+1 planes][2 rows][2 columns A, B][TY+2][32] floats
+    // published planes, per buffer (2): the residual plane as 4 column planes (row 0 A, row 0 B,
+    // row 1 A, row 1 B), then for stages 1..T a row-0 and a row-1 plane; each [TY+2][32] floats
+    constexpr int NPUB = 4 + 2 * T;
     float* pub = reinterpret_cast<float*>(stages + TB_S * STAGE_BYTES);
     __shared__ __align__(8) uint64_t mbar[TB_S];
     __shared__ float2 coef[128];
@@ -177,7 +181,7 @@ k_sweep_tb(const __grid_constant__ TBMaps maps, Grid g, float* __restrict__ Pout
         coef[tid] = make_float2(-(float)acc, (tid & 0x40) ? wa.w[acc] : 0.0f);
     }
     // zero the padding rows of every published plane (never written afterwards)
-    for (int i = tid; i < 2 * (T + 1) * 2 * 2 * 2 * TB_TX; i += TB_TX * TB_TY) {
+    for (int i = tid; i < 2 * NPUB * 2 * TB_TX; i += TB_TX * TB_TY) {
         const int lane = i % TB_TX, edge = (i / TB_TX) % 2, set = i / (2 * TB_TX);
         pub[set * PROW + (edge ? (TB_TY + 1) * TB_TX : 0) + lane] = 0.0f;
     }
@@ -250,18 +254,23 @@ k_sweep_tb(const __grid_constant__ TBMaps maps, Grid g, float* __restrict__ Pout
                 ff[k] = f0 | (f1 << 16);
             }
             // ---- publish planes q-1-s (slot (k-1-s) mod R) for the y-neighbours; the residual
-            // plane (s = 0) only in check launches
-            // column plane of published plane s, row r (0 = y0, 1 = y0+1), column c (0 = A, 1 = B)
-            float* pb = pub + par * (T + 1) * 4 * PROW;
+            // plane (s = 0) only in check launches.  This iteration's stages all update (A0, B1)
+            // when sA, else (B0, A1): they read row 1 column A (resp. B) of the thread above and
+            // row 0 column B (resp. A) of the thread below.
+            const bool sA = ((k + p_par) & 1) == 0;
+            float* pb = pub + par * NPUB * PROW;
+            if (check) {
+                const int j = (k - 1 + 2 * R) % R;
+                pb[0 * PROW + me0] = p0[j].x;
+                pb[1 * PROW + me0] = p0[j].y;
+                pb[2 * PROW + me0] = p1[j].x;
+                pb[3 * PROW + me0] = p1[j].y;
+            }
 #pragma unroll
-            for (int s = 0; s <= T; ++s) {
-                if (s > 0 || check) {
-                    const int j = (k - 1 - s + 2 * R) % R;
-                    pb[(4 * s + 0) * PROW + me0] = p0[j].x;
-                    pb[(4 * s + 1) * PROW + me0] = p0[j].y;
-                    pb[(4 * s + 2) * PROW + me0] = p1[j].x;
-                    pb[(4 * s + 3) * PROW + me0] = p1[j].y;
-                }
+            for (int s = 1; s <= T; ++s) {
+                const int j = (k - 1 - s + 2 * R) % R;
+                pb[(2 + 2 * s) * PROW + me0] = sA ? p0[j].y : p0[j].x;  // row 0, read as y+2 from above
+                pb[(3 + 2 * s) * PROW + me0] = sA ? p1[j].x : p1[j].y;  // row 1, read as y-1 from below
             }
             if (__syncthreads_or(!ok)) {
                 // a TMA stage never completed: record it, drain what is in flight, stop
@@ -307,21 +316,21 @@ k_sweep_tb(const __grid_constant__ TBMaps maps, Grid g, float* __restrict__ Pout
                 }
             }
 
-            // ---- stages 1..T: plane q-1-t (slot k-1-t) from time t-1 to t
-            const bool sA = ((k + p_par) & 1) == 0;  // update (A0, B1), else (B0, A1)
+            // ---- stages 1..T: plane q-1-t (slot k-1-t) from time t-1 to t (pattern sA above)
 #pragma unroll
             for (int t = 1; t <= T; ++t) {
                 if (t <= nhalf) {
                     const int j = (k - 1 - t + 2 * R) % R;
                     const int ju = (k - t + 2 * R) % R;
                     const int jd = (k - 2 - t + 2 * R) % R;
-                    const float* ps = pb + (4 * t) * PROW;
+                    const float* r0 = pb + (2 + 2 * t) * PROW;  // row-0 values (the thread below's)
+                    const float* r1 = pb + (3 + 2 * t) * PROW;  // row-1 values (the thread above's)
                     const unsigned f = ff[j];
                     if (sA) {
                         const float lB0 = __shfl_up_sync(0xffffffffu, p0[j].y, 1);
                         const float rA1 = __shfl_down_sync(0xffffffffu, p1[j].x, 1);
-                        const float ymA = ps[2 * PROW + me0 - TB_TX];  // row y0-1, column A
-                        const float ypB = ps[PROW + me0 + TB_TX];      // row y0+2, column B
+                        const float ymA = r1[me0 - TB_TX];  // row y0-1, column A
+                        const float ypB = r0[me0 + TB_TX];  // row y0+2, column B
                         const unsigned ia = fidx(f, 0), ib = fidx(f, 3);
                         const float nA0 = relax(p0[j].x, b0[j].x, coef[ia], ia & 0x40u, lB0, p0[j].y,
                                                 ymA, p1[j].x, p0[jd].x, p0[ju].x);
@@ -332,8 +341,8 @@ k_sweep_tb(const __grid_constant__ TBMaps maps, Grid g, float* __restrict__ Pout
                     } else {
                         const float rA0 = __shfl_down_sync(0xffffffffu, p0[j].x, 1);
                         const float lB1 = __shfl_up_sync(0xffffffffu, p1[j].y, 1);
-                        const float ymB = ps[3 * PROW + me0 - TB_TX];  // row y0-1, column B
-                        const float ypA = ps[me0 + TB_TX];             // row y0+2, column A
+                        const float ymB = r1[me0 - TB_TX];  // row y0-1, column B
+                        const float ypA = r0[me0 + TB_TX];  // row y0+2, column A
                         const unsigned ia = fidx(f, 1), ib = fidx(f, 2);
                         const float nB0 = relax(p0[j].y, b0[j].y, coef[ia], ia & 0x40u, p0[j].x, rA0,
                                                 ymB, p1[j].y, p0[jd].y, p0[ju].y);
@@ -399,7 +408,7 @@ bool encode_3d(CUtensorMap* m, const void* base, bool is_u8, const Grid& g) {
 
 template <int T>
 constexpr size_t tb_smem_bytes() {
-    return 128 + (size_t)((T + 4) / 2) * STAGE_BYTES + sizeof(float2) * 2 * (T + 1) * 2 * (TB_TY + 2) * TB_TX;
+    return 128 + (size_t)((T + 4) / 2) * STAGE_BYTES + sizeof(float) * 2 * (4 + 2 * T) * (TB_TY + 2) * TB_TX;
 }
 
 template <int T>
