@@ -15,6 +15,16 @@
 
 Both libraries are compiled without FMA contraction (-ffp-contract=off): the restatement's
 float instantiation is then bit-identical to the reference's own arithmetic.
+
+3. The reference's own kernels built for the GPU ("oracle A", a timing baseline only):
+   a. when the reference checkout is present, project/smokeSimulation.cu is rewritten into
+      oracle/_ref/ref_step_gpu.cu (glm includes dropped, the module header inlined, the
+      iteration-count literal read from a variable with the same default) and the harness
+      oracle/ref_gpu_tail.inc is appended; kernels and launches are left as they are;
+   b. whenever oracle/_ref/ref_step_gpu.cu exists, nvcc compiles it for sm_103a with its
+      default floating-point options (as the reference's own CMake build does) into
+      oracle/_ref/libsmoke_ref_gpu.so.  Not part of the parity chain (nvcc contracts a*b+c
+      into FMAs, so it differs from the host build by rounding).
 """
 from __future__ import annotations
 
@@ -121,7 +131,65 @@ def build_reference(force: bool = False) -> str | None:
     return REF_SO
 
 
+REF_GPU_CU = os.path.join(REF_OUT, "ref_step_gpu.cu")
+REF_GPU_SO = os.path.join(REF_OUT, "libsmoke_ref_gpu.so")
+
+
+def rewrite_reference_gpu(text: str, header: str | None) -> str:
+    """Text rules for the GPU build: only what the module needs to build outside its checkout
+    (glm includes dropped, its header inlined) and the iteration count as a variable."""
+    out = ["static int ref_num_iterations = 30;  // num_iterations (smokeSimulation.cu:797)"]
+    for line in text.splitlines():
+        s = line.strip()
+        if s.startswith("#include <glm/") or s == "using namespace glm;":
+            out.append("// (glm include dropped: unused by the simulation)")
+            continue
+        if s == '#include "smokeSimulation.cuh"' and header is not None:
+            out.append("// ---- project/smokeSimulation.cuh (inlined) ----")
+            out.extend(header.splitlines())
+            continue
+        out.append(line.replace("int num_iterations = 30;",
+                                "int num_iterations = ref_num_iterations;"))
+    out.append('#include "ref_gpu_tail.inc"')
+    return "\n".join(out) + "\n"
+
+
+def generate_reference_gpu_tu() -> bool:
+    if not os.path.exists(REFERENCE_SRC):
+        return False
+    os.makedirs(REF_OUT, exist_ok=True)
+    with open(REFERENCE_SRC, "r", encoding="utf-8", errors="replace") as f:
+        text = f.read()
+    with open(os.path.join(os.path.dirname(REFERENCE_SRC), "smokeSimulation.cuh"), "r",
+              encoding="utf-8", errors="replace") as f:
+        header = f.read()
+    new = rewrite_reference_gpu(text, header)
+    if "num_iterations = ref_num_iterations" not in new:
+        raise RuntimeError("the iteration-count literal was not found")
+    old = None
+    if os.path.exists(REF_GPU_CU):
+        with open(REF_GPU_CU) as f:
+            old = f.read()
+    if old != new:
+        with open(REF_GPU_CU, "w") as f:
+            f.write(new)
+    return True
+
+
+def build_reference_gpu(force: bool = False) -> str | None:
+    """oracle/_ref/libsmoke_ref_gpu.so, or None when the generated source is absent."""
+    generate_reference_gpu_tu()
+    if not os.path.exists(REF_GPU_CU):
+        return None
+    deps = [REF_GPU_CU, os.path.join(HERE, "ref_gpu_tail.inc")]
+    if force or _stale(REF_GPU_SO, *deps):
+        _run(["nvcc", "-O3", "-gencode", "arch=compute_103a,code=sm_103a", "-Xcompiler", "-fPIC",
+              "-shared", "-w", "-I", HERE, REF_GPU_CU, "-o", REF_GPU_SO])
+    return REF_GPU_SO
+
+
 def build(force: bool = False) -> dict:
+    generate_reference_gpu_tu()
     return {"restatement": build_restatement(force), "reference": build_reference(force)}
 
 

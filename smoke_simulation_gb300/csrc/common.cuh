@@ -120,27 +120,30 @@ __device__ __forceinline__ float avgW(const T* __restrict__ f, const Grid& g, in
 }
 
 // sampleSmoke (smokeSimulation.cu:451-484): clamp the position to [1, n-1] with the CELL
-// dims, trilinear weights from (c - delta) - i0, eight terms summed in the reference order.
+// dims, trilinear weights from (c - delta) - i0, eight terms summed in the reference's order.
+// After the clamp c - delta >= 0.5 (n >= 2; c = 1 when n == 1), so floorf equals truncation,
+// and min(i0 + 1, n - 1) in integers equals the reference's float fminf of small integers: the
+// index arithmetic is cheaper and every result is the same.
 template <typename T>
 __device__ __forceinline__ float sample_ref(const T* __restrict__ f, const Grid& g, float px,
                                            float py, float pz, float dx, float dy, float dz) {
-    const float mx = (float)(unsigned)(g.nx - 1), my = (float)(unsigned)(g.ny - 1),
-                mz = (float)(unsigned)(g.nz - 1);
-    float x = fmaxf(fminf(px, mx), 1.0f);
-    float y = fmaxf(fminf(py, my), 1.0f);
-    float z = fmaxf(fminf(pz, mz), 1.0f);
-    int x0 = (int)fminf(floorf(x - dx), mx);
-    float xw1 = (x - dx) - (float)x0;
-    float xw0 = 1.0f - xw1;
-    int x1 = (int)fminf((float)(x0 + 1), mx);
-    int y0 = (int)fminf(floorf(y - dy), my);
-    float yw1 = (y - dy) - (float)y0;
-    float yw0 = 1.0f - yw1;
-    int y1 = (int)fminf((float)(y0 + 1), my);
-    int z0 = (int)fminf(floorf(z - dz), mz);
-    float zw1 = (z - dz) - (float)z0;
-    float zw0 = 1.0f - zw1;
-    int z1 = (int)fminf((float)(z0 + 1), mz);
+    const int lx = g.nx - 1, ly = g.ny - 1, lz = g.nz - 1;
+    const float mx = (float)(unsigned)lx, my = (float)(unsigned)ly, mz = (float)(unsigned)lz;
+    const float xs = fmaxf(fminf(px, mx), 1.0f) - dx;
+    const float ys = fmaxf(fminf(py, my), 1.0f) - dy;
+    const float zs = fmaxf(fminf(pz, mz), 1.0f) - dz;
+    const int x0 = min(__float2int_rz(xs), lx);
+    const float xw1 = xs - (float)x0;
+    const float xw0 = 1.0f - xw1;
+    const int x1 = min(x0 + 1, lx);
+    const int y0 = min(__float2int_rz(ys), ly);
+    const float yw1 = ys - (float)y0;
+    const float yw0 = 1.0f - yw1;
+    const int y1 = min(y0 + 1, ly);
+    const int z0 = min(__float2int_rz(zs), lz);
+    const float zw1 = zs - (float)z0;
+    const float zw0 = 1.0f - zw1;
+    const int z1 = min(z0 + 1, lz);
     const int X = g.X, XY = g.XY;
     const int r00 = y0 * X + z0 * XY, r10 = y1 * X + z0 * XY, r01 = y0 * X + z1 * XY,
               r11 = y1 * X + z1 * XY;
@@ -148,6 +151,20 @@ __device__ __forceinline__ float sample_ref(const T* __restrict__ f, const Grid&
            xw0 * yw1 * zw0 * ldv(f, x0 + r10) + xw1 * yw1 * zw0 * ldv(f, x1 + r10) +
            xw0 * yw0 * zw1 * ldv(f, x0 + r01) + xw1 * yw0 * zw1 * ldv(f, x1 + r01) +
            xw0 * yw1 * zw1 * ldv(f, x0 + r11) + xw1 * yw1 * zw1 * ldv(f, x1 + r11);
+}
+
+// Loads issued where they stand (volatile inline PTX): the compiler can neither sink them into
+// the conditional block that consumes them nor merge them away, so a warp has a cell's loads in
+// flight before it waits on the flag byte that decides whether the cell is updated.
+__device__ __forceinline__ float ld_eager(const float* p) {
+    float v;
+    asm volatile("ld.global.f32 %0, [%1];" : "=f"(v) : "l"(__cvta_generic_to_global(p)));
+    return v;
+}
+__device__ __forceinline__ float ld_eager(const __nv_bfloat16* p) {
+    unsigned short h;
+    asm volatile("ld.global.u16 %0, [%1];" : "=h"(h) : "l"(__cvta_generic_to_global(p)));
+    return __bfloat162float(__ushort_as_bfloat16(h));
 }
 
 }  // namespace smk

@@ -93,16 +93,15 @@ __device__ __forceinline__ void body_forcing(const Grid& g, Tv* __restrict__ u, 
     const int z = (int)bid.z;
     if (x >= g.nx || y >= g.ny || z >= g.nz) return;
     const int i = g.idx(x, y, z);
+    // every input is loaded before the flag byte is tested (the clamp reads u and w of the
+    // same index; the buoyancy reads the density): one memory round trip per cell
     const uint8_t f = flags[i];
-    float vt = ldv(v, i);
-    if ((f & F_SELF) && (f & F_YM)) {
-        const float r = ldv(rho, i);
-        const float buoy = alpha * (r - 0.0f);
-        vt = vt + (r * gravity * dt + buoy * dt);
-        if (!(x >= 1 && z >= 1 && clamp_mode != 2)) stv(v, i, vt);
-    }
-    if (x >= 1 && z >= 1 && clamp_mode != 2) {
-        const float ut = ldv(u, i), wt = ldv(w, i);
+    const float v0 = ldv(v, i), r = ldv(rho, i), ut = ldv(u, i), wt = ldv(w, i);
+    const bool force = (f & F_SELF) && (f & F_YM);
+    const bool clamp = x >= 1 && z >= 1 && clamp_mode != 2;
+    const float buoy = alpha * (r - 0.0f);
+    float vt = force ? v0 + (r * gravity * dt + buoy * dt) : v0;
+    if (clamp) {
         const float len = ut * ut + vt * vt + wt * wt;
         if (clamp_mode == 0) {
             if (len * dt > lim_sq) {
@@ -117,8 +116,8 @@ __device__ __forceinline__ void body_forcing(const Grid& g, Tv* __restrict__ u, 
             vt = vt * s;
             stv(w, i, wt * s);
         }
-        stv(v, i, vt);
     }
+    if (force || clamp) stv(v, i, vt);
 }
 
 // ---- pressure scheme ------------------------------------------------------------------------
@@ -139,16 +138,16 @@ __device__ __forceinline__ void body_rhs(const Grid& g, const T* u, const T* v, 
     const int z = (int)bid.z;
     if (x >= g.nx || y >= g.ny || z >= g.nz) return;
     const int i = g.idx(x, y, z);
-    if (flags[i] & F_PROJ) {
-        const float div = -ldv(u, i) + ldv(u, i + 1) + -ldv(v, i) + ldv(v, i + g.X) + -ldv(w, i) +
-                          ldv(w, i + g.XY);
-        b[i] = -div;
-        if (!warm) P[i] = 0.0f;
-        else if (pcur != nullptr && P2 != nullptr && *pcur == 1) P[i] = P2[i];
-    } else {
-        b[i] = 0.0f;
-        P[i] = 0.0f;
-    }
+    // the six faces are loaded for every cell (all indices stay inside the face arrays) and the
+    // flag selects the result, so the loads do not wait on the flag byte
+    const uint8_t f = flags[i];
+    const float u0 = ldv(u, i), u1 = ldv(u, i + 1), v0 = ldv(v, i), v1 = ldv(v, i + g.X),
+                w0 = ldv(w, i), w1 = ldv(w, i + g.XY);
+    const float div = -u0 + u1 + -v0 + v1 + -w0 + w1;
+    const bool proj = (f & F_PROJ) != 0;
+    b[i] = proj ? -div : 0.0f;
+    if (!proj || !warm) P[i] = 0.0f;
+    else if (pcur != nullptr && P2 != nullptr && *pcur == 1) P[i] = P2[i];
 }
 
 // One cell of a colour pass:  r = fma(-acc, P_c, b_c + (((P_x-+P_x+)+(P_y-+P_y+))+(P_z-+P_z+)));
@@ -228,13 +227,16 @@ __device__ __forceinline__ void body_gradient_subtract(const Grid& g, float* u, 
     const int z = 1 + (int)bid.z;
     if (x >= g.nx || y >= g.ny || z >= g.nz) return;
     const int i = g.idx(x, y, z);
+    // loads first, then the flag decides which faces change; every face of the range is
+    // written (unchanged ones with their own value), so no load waits on the flag byte
     const uint8_t f = flags[i];
-    if (!(f & F_SELF)) return;
+    const float pc = P[i], px = P[i - 1], py = P[i - g.X], pz = P[i - g.XY];
+    const float uu = u[i], vv = v[i], ww = w[i];
+    const bool self = (f & F_SELF) != 0;
     const bool inx = x <= g.nx - 2, iny = y <= g.ny - 2, inz = z <= g.nz - 2;
-    const float pc = P[i];
-    if (iny && inz && (f & F_XM)) u[i] = u[i] - (pc - P[i - 1]);
-    if (inx && inz && (f & F_YM)) v[i] = v[i] - (pc - P[i - g.X]);
-    if (inx && iny && (f & F_ZM)) w[i] = w[i] - (pc - P[i - g.XY]);
+    u[i] = (self && iny && inz && (f & F_XM)) ? uu - (pc - px) : uu;
+    v[i] = (self && inx && inz && (f & F_YM)) ? vv - (pc - py) : vv;
+    w[i] = (self && inx && iny && (f & F_ZM)) ? ww - (pc - pz) : ww;
 }
 
 // max |div u| over projectable cells.  Contains a block barrier.
@@ -298,34 +300,31 @@ __device__ __forceinline__ void body_advect_velocity(const Grid& g, const Ti* __
     const uint8_t f = flags[i];
     if (!(f & F_SELF)) return;
     const bool inx = x <= g.nx - 2, iny = y <= g.ny - 2, inz = z <= g.nz - 2;
-    if (iny && inz && (f & F_XM)) {
+    const bool du = iny && inz && (f & F_XM), dv = inx && inz && (f & F_YM),
+               dw = inx && iny && (f & F_ZM);
+    if (!(du || dv || dw)) return;
+    // The three 8-point averages at one index serve two faces each (avgU: v and w faces, avgV:
+    // u and w, avgW: u and v), so each is evaluated once.
+    const float au = avgU(u0, g, i), av = avgV(v0, g, i), aw = avgW(w0, g, i);
+    if (du) {
         float xt = (float)x, yt = (float)y + 0.5f, zt = (float)z + 0.5f;
-        const float uu = ldv(u0, i);
-        const float vv = avgV(v0, g, i);
-        const float ww = avgW(w0, g, i);
-        xt = xt - dt * uu;
-        yt = yt - dt * vv;
-        zt = zt - dt * ww;
+        xt = xt - dt * ldv(u0, i);
+        yt = yt - dt * av;
+        zt = zt - dt * aw;
         stv(u1, i, sample_ref(u0, g, xt, yt, zt, 0.0f, 0.5f, 0.5f));
     }
-    if (inx && inz && (f & F_YM)) {
+    if (dv) {
         float xt = (float)x + 0.5f, yt = (float)y, zt = (float)z + 0.5f;
-        const float uu = avgU(u0, g, i);
-        const float vv = ldv(v0, i);
-        const float ww = avgW(w0, g, i);
-        xt = xt - dt * uu;
-        yt = yt - dt * vv;
-        zt = zt - dt * ww;
+        xt = xt - dt * au;
+        yt = yt - dt * ldv(v0, i);
+        zt = zt - dt * aw;
         stv(v1, i, sample_ref(v0, g, xt, yt, zt, 0.5f, 0.0f, 0.5f));
     }
-    if (inx && iny && (f & F_ZM)) {
+    if (dw) {
         float xt = (float)x + 0.5f, yt = (float)y + 0.5f, zt = (float)z;
-        const float uu = avgU(u0, g, i);
-        const float vv = avgV(v0, g, i);
-        const float ww = ldv(w0, i);
-        xt = xt - dt * uu;
-        yt = yt - dt * vv;
-        zt = zt - dt * ww;
+        xt = xt - dt * au;
+        yt = yt - dt * av;
+        zt = zt - dt * ldv(w0, i);
         stv(w1, i, sample_ref(w0, g, xt, yt, zt, 0.5f, 0.5f, 0.0f));
     }
 }
@@ -348,10 +347,13 @@ __device__ __forceinline__ void body_advect_density(const Grid& g, const T* __re
     const int z = 1 + (int)bid.z;
     if (x > g.nx - 2 || y > g.ny - 2 || z > g.nz - 2) return;
     const int i = g.idx(x, y, z);
+    // the face velocities are loaded with the flag byte, not after it (ld_eager)
+    const float ua = ld_eager(u + i), ub = ld_eager(u + i + 1), va = ld_eager(v + i),
+                vb = ld_eager(v + i + g.X), wa = ld_eager(w + i), wb = ld_eager(w + i + g.XY);
     if (!(flags[i] & F_SELF)) return;
-    const float ut = (ldv(u, i) + ldv(u, i + 1)) / 2.0f;
-    const float vt = (ldv(v, i) + ldv(v, i + g.X)) / 2.0f;
-    const float wt = (ldv(w, i) + ldv(w, i + g.XY)) / 2.0f;
+    const float ut = (ua + ub) / 2.0f;
+    const float vt = (va + vb) / 2.0f;
+    const float wt = (wa + wb) / 2.0f;
     const float xt = __fsub_rn((float)x + 0.5f, ut * dt);
     const float yt = __fsub_rn((float)y + 0.5f, vt * dt);
     const float zt = __fsub_rn((float)z + 0.5f, wt * dt);
