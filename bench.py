@@ -250,8 +250,8 @@ def main():
     ap.add_argument("--serve-requests", type=int, default=16, help="serving stream length (0: skip)")
     ap.add_argument("--render-frames", type=int, default=20, help="timed frames of the render form (0: skip)")
     ap.add_argument("--no-forms", action="store_true", help="skip the batched/mixed/serving forms")
-    ap.add_argument("--sweep-kernel", default="", help="D,Z: blocked sweep depth and z-chunk instead "
-                    "of the autotuner's choice (to profile the configuration a timed run chose)")
+    ap.add_argument("--sweep-kernel", default="", help="D,Z[,R]: blocked sweep depth, z-chunk and patch "
+                    "rows instead of the autotuner's choice (to profile the configuration a timed run chose)")
     ap.add_argument("--batch-schedule", default="", help="C,Z,W: grouped projection schedule instead of "
                     "the autotuner's choice")
     args = ap.parse_args()
@@ -277,11 +277,14 @@ def main():
     stream = torch.cuda.Stream()
     sh = stream.cuda_stream
     if args.sweep_kernel:
-        depth, zchunk = (int(x) for x in args.sweep_kernel.split(","))
-        sim.set_sweep_kernel(depth, zchunk)
+        parts = [int(x) for x in args.sweep_kernel.split(",")]
+        depth, zchunk = parts[0], parts[1]
+        sim.set_sweep_kernel(depth, zchunk, rows=parts[2] if len(parts) > 2 else 2)
         tuned_us = None
     else:
         depth, zchunk, tuned_us = sim.autotune()
+    rows = sim.sweep_shape()[1]
+    kname = "k_sweep_tb<%d, %d>" % (depth, rows)
 
     # warm-up steps (graph capture, caches); the timed segments restart from the initial state
     for _ in range(max(args.warmup, 0)):
@@ -350,7 +353,7 @@ def main():
     if os.path.exists(tf) and depth > 0:
         with open(tf) as f:
             tr = json.load(f)
-        if tr.get("kernel") == "k_sweep_tb<%d>" % depth and tr.get("zchunk") == zchunk:
+        if tr.get("kernel") == kname and tr.get("zchunk") == zchunk:
             traffic = tr["bytes_per_cell_per_sweep"] * sweeps_per_launch * sc.cells
 
     # ---- e2e through the public API with host buffers ----------------------------------------
@@ -427,13 +430,13 @@ def main():
                        "l2": "inputs larger than L2 (%.0f MB resident state)" % (
                            sim_bytes(sc) / 1e6),
                        "mean_sweeps": mean_sweeps, "converged_frac": float(np.mean(conv)),
-                       "sweep_kernel": {"depth": depth, "zchunk": zchunk, "tuned_us_per_sweep": tuned_us},
+                       "sweep_kernel": {"depth": depth, "rows": rows, "zchunk": zchunk, "tuned_us_per_sweep": tuned_us},
                        "max_div_post_projection": float(np.max(divs)),
                        "max_div_measured": "after every projection of the workload's steps, in a "
                                            "separate pass (the timed steps run without the diagnostic)",
                        "pressure_start": "warm (previous step's pressure)",
                        "cold_start_form": cold},
-            "roofline": {"bound": "hbm", "kernel": "k_sweep_tb<%d> (z-chunk %d)" % (depth, zchunk),
+            "roofline": {"bound": "hbm", "kernel": "%s (z-chunk %d)" % (kname, zchunk),
                          "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": (achieved / peak) if achieved else None, "traffic": traffic,
                          "peak_kind": peak_kind, "bytes_per_launch": bytes_per_launch,

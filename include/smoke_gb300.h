@@ -170,6 +170,11 @@ long long smk_launch_count(const smk_sim* sim);
  * smokeSimulation.cu:795-801). */
 int smk_set_sweep_kernel(smk_sim* sim, int depth, int zchunk);
 int smk_get_sweep_kernel(const smk_sim* sim, int* depth, int* zchunk);
+/* The same with the blocked kernel's patch height: `rows` cell rows per thread (2 with depth 2,
+ * 4 or 6; 4 with depth 4: a 64 x 32 tile of 8 warps instead of 16).  smk_set_sweep_kernel is
+ * rows = 2. */
+int smk_set_sweep_shape(smk_sim* sim, int depth, int rows, int zchunk);
+int smk_get_sweep_shape(const smk_sim* sim, int* depth, int* rows, int* zchunk);
 /* Replay steady-state steps as a captured CUDA graph (default on).  A graph is re-captured
  * when dt, the parameters, the objects or the sweep kernel change; steps after a mask or
  * obstacle change run directly.  Results are identical either way. */
@@ -178,7 +183,7 @@ int smk_set_graphs(smk_sim* sim, int enable);
  * (a graph conditional node: no launches after the solve has converged; default on) or as the
  * unrolled launches up to max_sweeps (later ones exit at entry).  Results are identical. */
 int smk_set_graph_loops(smk_sim* sim, int enable);
-/* Time the blocked sweep kernel's depths and z-chunk sizes on this simulation's buffers and
+/* Time the blocked sweep kernel's shapes (depth, patch rows) and z-chunk sizes on this simulation's buffers and
  * keep the fastest (cached per grid shape and device for the process).  Synchronises; does not
  * change the simulation's results.  Outputs may be NULL; us_per_sweep is -1 on a cache hit.
  * No counterpart in the reference. */

@@ -102,6 +102,8 @@ def lib() -> C.CDLL:
         "smk_launch_count": (C.c_longlong, [vp]),
         "smk_set_sweep_kernel": (i, [vp, i, i]),
         "smk_get_sweep_kernel": (i, [vp, C.POINTER(i), C.POINTER(i)]),
+        "smk_set_sweep_shape": (i, [vp, i, i, i]),
+        "smk_get_sweep_shape": (i, [vp, C.POINTER(i), C.POINTER(i), C.POINTER(i)]),
         "smk_project_noalloc": (i, [vp, vp, vp, vp, i, i, i, C.POINTER(Params),
                                     C.POINTER(Stats), vp]),
         "smk_project_noalloc_max_elems": (C.c_longlong, []),
@@ -316,8 +318,10 @@ class Simulation:
     def set_graph_loops(self, enable: bool):
         _check(lib().smk_set_graph_loops(self.h, 1 if enable else 0))
 
-    def set_sweep_kernel(self, depth: int, zchunk: int = 32):
-        _check(lib().smk_set_sweep_kernel(self.h, depth, zchunk))
+    def set_sweep_kernel(self, depth: int, zchunk: int = 32, rows: int = 2):
+        """Blocked sweep kernel shape: `depth` colour passes per launch, z-chunks of `zchunk`
+        planes, patches of `rows` cell rows per thread (2, or 4 with depth 4)."""
+        _check(lib().smk_set_sweep_shape(self.h, depth, rows, zchunk))
 
     def autotune(self):
         """Pick the fastest sweep kernel shape for this grid; returns (depth, zchunk, us/sweep)."""
@@ -332,6 +336,12 @@ class Simulation:
         d, z = C.c_int(), C.c_int()
         _check(lib().smk_get_sweep_kernel(self.h, C.byref(d), C.byref(z)))
         return d.value, z.value
+
+    def sweep_shape(self):
+        """(depth, patch rows, zchunk) of the blocked sweep kernel."""
+        d, r, z = C.c_int(), C.c_int(), C.c_int()
+        _check(lib().smk_get_sweep_shape(self.h, C.byref(d), C.byref(r), C.byref(z)))
+        return d.value, r.value, z.value
 
 
 BATCH_AUTO, BATCH_GROUPED, BATCH_BRANCHES = 0, 1, 2

@@ -144,13 +144,23 @@ __device__ __forceinline__ float sample_ref(const T* __restrict__ f, const Grid&
     const float zw1 = zs - (float)z0;
     const float zw0 = 1.0f - zw1;
     const int z1 = min(z0 + 1, lz);
-    const int X = g.X, XY = g.XY;
-    const int r00 = y0 * X + z0 * XY, r10 = y1 * X + z0 * XY, r01 = y0 * X + z1 * XY,
-              r11 = y1 * X + z1 * XY;
-    return xw0 * yw0 * zw0 * ldv(f, x0 + r00) + xw1 * yw0 * zw0 * ldv(f, x1 + r00) +
-           xw0 * yw1 * zw0 * ldv(f, x0 + r10) + xw1 * yw1 * zw0 * ldv(f, x1 + r10) +
-           xw0 * yw0 * zw1 * ldv(f, x0 + r01) + xw1 * yw0 * zw1 * ldv(f, x1 + r01) +
-           xw0 * yw1 * zw1 * ldv(f, x0 + r11) + xw1 * yw1 * zw1 * ldv(f, x1 + r11);
+    // The upper corner differs from the lower one by +1 on each axis except where the position
+    // was clamped to the last cell (then it repeats it).  Every +1 neighbour lies inside the
+    // arrays (rows hold >= nx+1 elements, planes >= ny+1 rows, the field >= nz+1 planes), so the
+    // x+1 values are loaded at a fixed offset and replaced by the x0 values where x1 == x0: the
+    // eight loads need four row addresses, not eight index computations.
+    const T* r00 = f + (x0 + y0 * g.X + z0 * g.XY);
+    const T* r10 = r00 + (y1 - y0) * g.X;
+    const T* r01 = r00 + (z1 - z0) * g.XY;
+    const T* r11 = r01 + (y1 - y0) * g.X;
+    const bool sx = x1 != x0;
+    const float a000 = ldv(r00, 0), a010 = ldv(r10, 0), a001 = ldv(r01, 0), a011 = ldv(r11, 0);
+    const float b100 = ldv(r00, 1), b110 = ldv(r10, 1), b101 = ldv(r01, 1), b111 = ldv(r11, 1);
+    const float a100 = sx ? b100 : a000, a110 = sx ? b110 : a010, a101 = sx ? b101 : a001,
+                a111 = sx ? b111 : a011;
+    return xw0 * yw0 * zw0 * a000 + xw1 * yw0 * zw0 * a100 + xw0 * yw1 * zw0 * a010 +
+           xw1 * yw1 * zw0 * a110 + xw0 * yw0 * zw1 * a001 + xw1 * yw0 * zw1 * a101 +
+           xw0 * yw1 * zw1 * a011 + xw1 * yw1 * zw1 * a111;
 }
 
 // Loads issued where they stand (volatile inline PTX): the compiler can neither sink them into

@@ -51,7 +51,8 @@ void launch_gradient_subtract(const Grid& g, float* u, float* v, float* w, const
 // Temporally blocked sweeps: nhalf <= T colour passes in one pass over HBM, P_in -> P_out;
 // `check` launches also record the residual of the input state for tolerance group `group`.
 // The pressure buffers are read through TMA tensor maps built once per simulation.
-int sweep_tb_depth_supported(int T);
+// Supported shapes: `rows` = cell rows of a thread's patch (2: T = 2, 4, 6; 4: T = 4).
+int sweep_tb_shape_supported(int T, int rows);
 // Set the kernels' shared-memory attributes once (outside any stream capture).
 int prepare_sweep_kernels();
 struct SweepMaps;
@@ -60,10 +61,10 @@ SweepMaps* create_sweep_maps(const Grid& g, const float* Pa, const float* Pb, co
 void destroy_sweep_maps(SweepMaps* m);
 // group_base (device, may be NULL): the launch's group index is group + *group_base (a graph's
 // device-side group loop).
-int launch_sweep_tb(const SweepMaps* m, const Grid& g, bool in_is_a, float* Pout, int T, int nhalf,
-                    int colour0, int zchunk, const float* wacc7, StepStatus* status, int check,
-                    int group, float tol, int* pcur, int out_idx, int* kerr, const int* group_base,
-                    cudaStream_t st);
+int launch_sweep_tb(const SweepMaps* m, const Grid& g, bool in_is_a, float* Pout, int T, int rows,
+                    int nhalf, int colour0, int zchunk, const float* wacc7, StepStatus* status,
+                    int check, int group, float tol, int* pcur, int out_idx, int* kerr,
+                    const int* group_base, cudaStream_t st);
 // Last node of a device-side group loop's body: counter += step; loop again while the solve is
 // not done and counter < limit; *launches += launches_per_iter.
 void launch_group_loop_next(const StepStatus* status, int* counter, int step, int limit,

@@ -142,8 +142,9 @@ __global__ void k_project_velocity(Grid g, float* __restrict__ u, float* __restr
 }
 
 // ---- a: velocityAdvectionU/V/W (:527-615) and advectSmoke (:617-638) ------------------------
+// The advection kernels are latency-bound gathers: 32 registers keep 8 blocks (64 warps) per SM.
 template <typename Ti, typename To>
-__global__ void k_advect_velocity(Grid g, const Ti* __restrict__ u0, const Ti* __restrict__ v0,
+__global__ void __launch_bounds__(BX * BY, 8) k_advect_velocity(Grid g, const Ti* __restrict__ u0, const Ti* __restrict__ v0,
                                   const Ti* __restrict__ w0, To* __restrict__ u1,
                                   To* __restrict__ v1, To* __restrict__ w1,
                                   const uint8_t* __restrict__ flags, float dt) {
@@ -151,7 +152,7 @@ __global__ void k_advect_velocity(Grid g, const Ti* __restrict__ u0, const Ti* _
 }
 
 template <typename T, typename Tv>
-__global__ void k_advect_density(Grid g, const T* __restrict__ r0, T* __restrict__ r1,
+__global__ void __launch_bounds__(BX * BY, 8) k_advect_density(Grid g, const T* __restrict__ r0, T* __restrict__ r1,
                                  const Tv* __restrict__ u, const Tv* __restrict__ v,
                                  const Tv* __restrict__ w, const uint8_t* __restrict__ flags,
                                  float dt) {

@@ -51,14 +51,24 @@ namespace smk {
 namespace {
 
 constexpr int TB_TX = 32;      // threads per tile row (one warp) = 64 cells
-constexpr int TB_TY = 16;      // tile rows of threads = 32 cell rows
 constexpr int BOX_F = 68;      // float box width: 64 cells + up to 2 alignment cells, 16-B multiple
 constexpr int BOX_U8 = 80;     // flag box width in bytes: 64 + up to 15 alignment bytes
-constexpr int ROWS = 2 * TB_TY;
-constexpr int STAGE_P = ROWS * BOX_F * 4;     // bytes
-constexpr int STAGE_F = ROWS * BOX_U8;        // bytes
-constexpr int STAGE_BYTES = 2 * STAGE_P + STAGE_F;
 constexpr unsigned WAIT_LIMIT = 1u << 20;
+
+// Tile geometry for a patch of PY rows per thread: TY tile rows of threads (warps) give
+// ROWS = PY * TY cell rows.  PY = 2: 16 warps, 32 rows; PY = 4: 10 warps, 40 rows (the ring of a
+// 4-row patch needs ~180 registers per thread).
+template <int PY>
+struct TBGeom {
+    static_assert(PY == 2 || PY == 4, "patch rows");
+    static constexpr int TY = PY == 2 ? 16 : 8;
+    static constexpr int ROWS = PY * TY;
+    static constexpr int STAGE_P = ROWS * BOX_F * 4;  // bytes (a multiple of 128)
+    static constexpr int STAGE_F = ROWS * BOX_U8;     // bytes (a multiple of 128)
+    static constexpr int STAGE_BYTES = 2 * STAGE_P + STAGE_F;
+    static constexpr int PROW = (TY + 2) * TB_TX;     // floats per published plane (zero row above/below)
+    static constexpr int THREADS = TB_TX * TY;
+};
 
 struct WAcc8 { float w[8]; };
 
@@ -110,12 +120,14 @@ __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map
 }
 
 // Issue the three boxes of plane z into stage `st` (thread 0 only).
+template <int PY>
 __device__ __forceinline__ void issue_plane(const TBMaps& m, unsigned char* stage, uint32_t bar,
                                             int xf, int xb, int y, int z) {
-    mbar_expect_tx(bar, (uint32_t)STAGE_BYTES);
+    using G = TBGeom<PY>;
+    mbar_expect_tx(bar, (uint32_t)G::STAGE_BYTES);
     tma_load_3d(smem_u32(stage), &m.pin, xf, y, z, bar);
-    tma_load_3d(smem_u32(stage + STAGE_P), &m.b, xf, y, z, bar);
-    tma_load_3d(smem_u32(stage + 2 * STAGE_P), &m.f, xb, y, z, bar);
+    tma_load_3d(smem_u32(stage + G::STAGE_P), &m.b, xf, y, z, bar);
+    tma_load_3d(smem_u32(stage + 2 * G::STAGE_P), &m.f, xb, y, z, bar);
 }
 
 // One cell update in the oracle's operation order; `c` = {-acc, omega/acc} from the flag
@@ -135,26 +147,30 @@ __device__ __forceinline__ unsigned resid_bits(float pc, float bc, float2 c, boo
     return proj ? __float_as_uint(fabsf(r)) : 0u;
 }
 
-// flag byte of cell k (0..3 = A0, B0, A1, B1) of a packed patch word -> table index:
-// bits 0-5 the six fluid-neighbour bits, bit 6 "projectable"
+// flag byte of cell k (0..3 = A, B of the word's first row, A, B of its second row) of a packed
+// flag word -> table index: bits 0-5 the six fluid-neighbour bits, bit 6 "projectable"
 __device__ __forceinline__ unsigned fidx(unsigned f, int k) { return (f >> (8 * k + 1)) & 0x7fu; }
 
-template <int T>
-__global__ void __launch_bounds__(TB_TX * TB_TY, 1)
+template <int T, int PY>
+__global__ void __launch_bounds__(TBGeom<PY>::THREADS, 1)
 k_sweep_tb(const __grid_constant__ TBMaps maps, Grid g, float* __restrict__ Pout, int nhalf,
            int colour0, int zchunk, WAcc8 wa, StepStatus* status, int check, int group, float tol,
            int* __restrict__ pcur, int out_idx, int* __restrict__ kerr, const int* __restrict__ group_base) {
+    using G = TBGeom<PY>;
+    constexpr int TY = G::TY, ROWS = G::ROWS, PROW = G::PROW, STAGE_BYTES = G::STAGE_BYTES,
+                  STAGE_P = G::STAGE_P;
+    constexpr int L = PY - 1;                // last row of the patch
     constexpr int R = T + 4;                 // register ring length (even, >= T + 3)
     constexpr int TB_S = R / 2;              // TMA stages (planes in flight)
     constexpr int IX = 2 * TB_TX - 2 * T;    // interior columns
     constexpr int IY = ROWS - 2 * T;         // interior rows
-    constexpr int PROW = (TB_TY + 2) * TB_TX;  // floats per published column plane (zero row above/below)
     extern __shared__ __align__(128) unsigned char smem_raw[];
     // TMA destinations must be 128-byte aligned: align the dynamic base explicitly (the launch
     // requests 128 spare bytes)
     unsigned char* stages = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);  // [S][STAGE_BYTES]
     // published planes, per buffer (2): the residual plane as 4 column planes (row 0 A, row 0 B,
-    // row 1 A, row 1 B), then for stages 1..T a row-0 and a row-1 plane; each [TY+2][32] floats
+    // last row A, last row B), then for stages 1..T a row-0 and a last-row plane; each
+    // [TY+2][32] floats
     constexpr int NPUB = 4 + 2 * T;
     float* pub = reinterpret_cast<float*>(stages + TB_S * STAGE_BYTES);
     __shared__ __align__(8) uint64_t mbar[TB_S];
@@ -181,9 +197,9 @@ k_sweep_tb(const __grid_constant__ TBMaps maps, Grid g, float* __restrict__ Pout
         coef[tid] = make_float2(-(float)acc, (tid & 0x40) ? wa.w[acc] : 0.0f);
     }
     // zero the padding rows of every published plane (never written afterwards)
-    for (int i = tid; i < 2 * NPUB * 2 * TB_TX; i += TB_TX * TB_TY) {
+    for (int i = tid; i < 2 * NPUB * 2 * TB_TX; i += G::THREADS) {
         const int lane = i % TB_TX, edge = (i / TB_TX) % 2, set = i / (2 * TB_TX);
-        pub[set * PROW + (edge ? (TB_TY + 1) * TB_TX : 0) + lane] = 0.0f;
+        pub[set * PROW + (edge ? (TY + 1) * TB_TX : 0) + lane] = 0.0f;
     }
     if (pcur != nullptr && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && leader)
         *pcur = out_idx;
@@ -195,14 +211,15 @@ k_sweep_tb(const __grid_constant__ TBMaps maps, Grid g, float* __restrict__ Pout
     const int of = X0 - xf + 2 * tx;          // this thread's column in the float box
     const int ob = X0 - xb + 2 * tx;          // ... in the flag box
     const int x0 = X0 + 2 * tx;
-    const int y0 = Y0 + 2 * ty;
+    const int y0 = Y0 + PY * ty;
     const int za = (int)blockIdx.z * zchunk;
     const int zb = min(za + zchunk, g.nz);
     const bool inx = (2 * tx >= T) && (2 * tx < T + IX) && x0 < g.nx;
-    const bool in0 = inx && (2 * ty >= T) && (2 * ty < T + IY) && y0 >= 0 && y0 < g.ny;
-    const bool in1 = in0 && y0 + 1 < g.ny;
+    bool in[PY];  // row r of the patch is an interior row of the tile inside the grid
+#pragma unroll
+    for (int r = 0; r < PY; ++r)
+        in[r] = inx && (PY * ty + r >= T) && (PY * ty + r < T + IY) && y0 + r >= 0 && y0 + r < g.ny;
     const int off0 = x0 + g.X * y0;
-    const int off1 = off0 + g.X;
 
     const int qbeg = za - T;
     const int qend = zb + T;
@@ -214,15 +231,17 @@ k_sweep_tb(const __grid_constant__ TBMaps maps, Grid g, float* __restrict__ Pout
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         for (int s = 0; s < TB_S; ++s)
-            issue_plane(maps, stages + s * STAGE_BYTES, smem_u32(&mbar[s]), xf, xb, Y0, qbeg + s);
+            issue_plane<PY>(maps, stages + s * STAGE_BYTES, smem_u32(&mbar[s]), xf, xb, Y0, qbeg + s);
     }
 
-    float2 p0[R], p1[R], b0[R], b1[R];  // P and b, rows 0 and 1, slot = plane mod R
-    unsigned ff[R];                     // flags: bytes A0, B0, A1, B1
+    float2 pp[PY][R], bb[PY][R];  // P and b per patch row, slot = plane mod R
+    unsigned ff[PY / 2][R];       // flags: bytes A, B of rows 2h and 2h+1
 #pragma unroll
     for (int j = 0; j < R; ++j) {
-        p0[j] = p1[j] = b0[j] = b1[j] = make_float2(0.f, 0.f);
-        ff[j] = 0u;
+#pragma unroll
+        for (int r = 0; r < PY; ++r) pp[r][j] = bb[r][j] = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int h = 0; h < PY / 2; ++h) ff[h][j] = 0u;
     }
 
     unsigned rmax = 0u;
@@ -244,33 +263,40 @@ k_sweep_tb(const __grid_constant__ TBMaps maps, Grid g, float* __restrict__ Pout
                 const float* sp = reinterpret_cast<const float*>(S_);
                 const float* sb = reinterpret_cast<const float*>(S_ + STAGE_P);
                 const unsigned char* sf = S_ + 2 * STAGE_P;
-                const int r0 = (2 * ty) * BOX_F + of, r1 = r0 + BOX_F;
-                p0[k] = *reinterpret_cast<const float2*>(sp + r0);
-                p1[k] = *reinterpret_cast<const float2*>(sp + r1);
-                b0[k] = *reinterpret_cast<const float2*>(sb + r0);
-                b1[k] = *reinterpret_cast<const float2*>(sb + r1);
-                const unsigned f0 = *reinterpret_cast<const unsigned short*>(sf + (2 * ty) * BOX_U8 + ob);
-                const unsigned f1 = *reinterpret_cast<const unsigned short*>(sf + (2 * ty + 1) * BOX_U8 + ob);
-                ff[k] = f0 | (f1 << 16);
+#pragma unroll
+                for (int r = 0; r < PY; ++r) {
+                    const int rr = (PY * ty + r) * BOX_F + of;
+                    pp[r][k] = *reinterpret_cast<const float2*>(sp + rr);
+                    bb[r][k] = *reinterpret_cast<const float2*>(sb + rr);
+                }
+#pragma unroll
+                for (int h = 0; h < PY / 2; ++h) {
+                    const unsigned f0 =
+                        *reinterpret_cast<const unsigned short*>(sf + (PY * ty + 2 * h) * BOX_U8 + ob);
+                    const unsigned f1 =
+                        *reinterpret_cast<const unsigned short*>(sf + (PY * ty + 2 * h + 1) * BOX_U8 + ob);
+                    ff[h][k] = f0 | (f1 << 16);
+                }
             }
             // ---- publish planes q-1-s (slot (k-1-s) mod R) for the y-neighbours; the residual
-            // plane (s = 0) only in check launches.  This iteration's stages all update (A0, B1)
-            // when sA, else (B0, A1): they read row 1 column A (resp. B) of the thread above and
-            // row 0 column B (resp. A) of the thread below.
+            // plane (s = 0) only in check launches.  This iteration's stages all update column A
+            // of the even rows and B of the odd rows when sA, else the opposite (PY is even, so
+            // the pattern is the same for every thread): a stage reads the last row's other
+            // column of the thread above and row 0's other column of the thread below.
             const bool sA = ((k + p_par) & 1) == 0;
             float* pb = pub + par * NPUB * PROW;
             if (check) {
                 const int j = (k - 1 + 2 * R) % R;
-                pb[0 * PROW + me0] = p0[j].x;
-                pb[1 * PROW + me0] = p0[j].y;
-                pb[2 * PROW + me0] = p1[j].x;
-                pb[3 * PROW + me0] = p1[j].y;
+                pb[0 * PROW + me0] = pp[0][j].x;
+                pb[1 * PROW + me0] = pp[0][j].y;
+                pb[2 * PROW + me0] = pp[L][j].x;
+                pb[3 * PROW + me0] = pp[L][j].y;
             }
 #pragma unroll
             for (int s = 1; s <= T; ++s) {
                 const int j = (k - 1 - s + 2 * R) % R;
-                pb[(2 + 2 * s) * PROW + me0] = sA ? p0[j].y : p0[j].x;  // row 0, read as y+2 from above
-                pb[(3 + 2 * s) * PROW + me0] = sA ? p1[j].x : p1[j].y;  // row 1, read as y-1 from below
+                pb[(2 + 2 * s) * PROW + me0] = sA ? pp[0][j].y : pp[0][j].x;  // row 0, read from above
+                pb[(3 + 2 * s) * PROW + me0] = sA ? pp[L][j].x : pp[L][j].y;  // last row, read from below
             }
             if (__syncthreads_or(!ok)) {
                 // a TMA stage never completed: record it, drain what is in flight, stop
@@ -287,31 +313,33 @@ k_sweep_tb(const __grid_constant__ TBMaps maps, Grid g, float* __restrict__ Pout
             }
             // every thread has read stage st: refill it with plane q + S
             if (leader && q + TB_S <= qfinal)
-                issue_plane(maps, stages + st * STAGE_BYTES, smem_u32(&mbar[st]), xf, xb, Y0, q + TB_S);
+                issue_plane<PY>(maps, stages + st * STAGE_BYTES, smem_u32(&mbar[st]), xf, xb, Y0, q + TB_S);
 
             // ---- stage 0: residual of plane q-1 at time 0
             if (check) {
                 const int j = (k - 1 + R) % R, ju = k, jd = (k - 2 + R) % R;
-                const float lB0 = __shfl_up_sync(0xffffffffu, p0[j].y, 1);
-                const float lB1 = __shfl_up_sync(0xffffffffu, p1[j].y, 1);
-                const float rA0 = __shfl_down_sync(0xffffffffu, p0[j].x, 1);
-                const float rA1 = __shfl_down_sync(0xffffffffu, p1[j].x, 1);
+                float lB[PY], rA[PY];
+#pragma unroll
+                for (int r = 0; r < PY; ++r) {
+                    lB[r] = __shfl_up_sync(0xffffffffu, pp[r][j].y, 1);
+                    rA[r] = __shfl_down_sync(0xffffffffu, pp[r][j].x, 1);
+                }
                 const int zp = q - 1;
-                if (zp >= za && zp < zb && in0) {
-                    // row y0-1 (thread above, row 1) and row y0+2 (thread below, row 0)
+                if (zp >= za && zp < zb) {
+                    // row y0-1 (thread above, last row) and row y0+PY (thread below, row 0)
                     const float2 up = make_float2(pb[2 * PROW + me0 - TB_TX], pb[3 * PROW + me0 - TB_TX]);
                     const float2 dn = make_float2(pb[me0 + TB_TX], pb[PROW + me0 + TB_TX]);
-                    const unsigned f = ff[j];
-                    const unsigned i0 = fidx(f, 0), i1 = fidx(f, 1), i2 = fidx(f, 2), i3 = fidx(f, 3);
-                    rmax = max(rmax, resid_bits(p0[j].x, b0[j].x, coef[i0], i0 & 0x40u, lB0, p0[j].y,
-                                                up.x, p1[j].x, p0[jd].x, p0[ju].x));
-                    rmax = max(rmax, resid_bits(p0[j].y, b0[j].y, coef[i1], i1 & 0x40u, p0[j].x, rA0,
-                                                up.y, p1[j].y, p0[jd].y, p0[ju].y));
-                    if (in1) {
-                        rmax = max(rmax, resid_bits(p1[j].x, b1[j].x, coef[i2], i2 & 0x40u, lB1, p1[j].y,
-                                                    p0[j].x, dn.x, p1[jd].x, p1[ju].x));
-                        rmax = max(rmax, resid_bits(p1[j].y, b1[j].y, coef[i3], i3 & 0x40u, p1[j].x, rA1,
-                                                    p0[j].y, dn.y, p1[jd].y, p1[ju].y));
+#pragma unroll
+                    for (int r = 0; r < PY; ++r) {
+                        if (!in[r]) continue;
+                        const float2 ym = r == 0 ? up : pp[r - 1][j];
+                        const float2 yp = r == L ? dn : pp[r + 1][j];
+                        const unsigned f = ff[r / 2][j];
+                        const unsigned ia = fidx(f, 2 * (r & 1)), ib = fidx(f, 2 * (r & 1) + 1);
+                        rmax = max(rmax, resid_bits(pp[r][j].x, bb[r][j].x, coef[ia], ia & 0x40u, lB[r],
+                                                    pp[r][j].y, ym.x, yp.x, pp[r][jd].x, pp[r][ju].x));
+                        rmax = max(rmax, resid_bits(pp[r][j].y, bb[r][j].y, coef[ib], ib & 0x40u, pp[r][j].x,
+                                                    rA[r], ym.y, yp.y, pp[r][jd].y, pp[r][ju].y));
                     }
                 }
             }
@@ -324,32 +352,60 @@ k_sweep_tb(const __grid_constant__ TBMaps maps, Grid g, float* __restrict__ Pout
                     const int ju = (k - t + 2 * R) % R;
                     const int jd = (k - 2 - t + 2 * R) % R;
                     const float* r0 = pb + (2 + 2 * t) * PROW;  // row-0 values (the thread below's)
-                    const float* r1 = pb + (3 + 2 * t) * PROW;  // row-1 values (the thread above's)
-                    const unsigned f = ff[j];
+                    const float* rl = pb + (3 + 2 * t) * PROW;  // last-row values (the thread above's)
+                    const float above = rl[me0 - TB_TX];       // row y0-1, the column row 0 updates
+                    const float below = r0[me0 + TB_TX];       // row y0+PY, the column row L updates
+                    float nv[PY];
                     if (sA) {
-                        const float lB0 = __shfl_up_sync(0xffffffffu, p0[j].y, 1);
-                        const float rA1 = __shfl_down_sync(0xffffffffu, p1[j].x, 1);
-                        const float ymA = r1[me0 - TB_TX];  // row y0-1, column A
-                        const float ypB = r0[me0 + TB_TX];  // row y0+2, column B
-                        const unsigned ia = fidx(f, 0), ib = fidx(f, 3);
-                        const float nA0 = relax(p0[j].x, b0[j].x, coef[ia], ia & 0x40u, lB0, p0[j].y,
-                                                ymA, p1[j].x, p0[jd].x, p0[ju].x);
-                        const float nB1 = relax(p1[j].y, b1[j].y, coef[ib], ib & 0x40u, p1[j].x, rA1,
-                                                p0[j].y, ypB, p1[jd].y, p1[ju].y);
-                        p0[j].x = nA0;
-                        p1[j].y = nB1;
+#pragma unroll
+                        for (int r = 0; r < PY; ++r) {
+                            const unsigned f = ff[r / 2][j];
+                            if ((r & 1) == 0) {  // column A
+                                const float lB = __shfl_up_sync(0xffffffffu, pp[r][j].y, 1);
+                                const float ym = r == 0 ? above : pp[r - 1][j].x;
+                                const float yp = pp[r + 1][j].x;
+                                const unsigned ia = fidx(f, 0);
+                                nv[r] = relax(pp[r][j].x, bb[r][j].x, coef[ia], ia & 0x40u, lB, pp[r][j].y,
+                                              ym, yp, pp[r][jd].x, pp[r][ju].x);
+                            } else {              // column B
+                                const float rA = __shfl_down_sync(0xffffffffu, pp[r][j].x, 1);
+                                const float ym = pp[r - 1][j].y;
+                                const float yp = r == L ? below : pp[r + 1 < PY ? r + 1 : r][j].y;
+                                const unsigned ib = fidx(f, 3);
+                                nv[r] = relax(pp[r][j].y, bb[r][j].y, coef[ib], ib & 0x40u, pp[r][j].x, rA,
+                                              ym, yp, pp[r][jd].y, pp[r][ju].y);
+                            }
+                        }
+#pragma unroll
+                        for (int r = 0; r < PY; ++r) {
+                            if ((r & 1) == 0) pp[r][j].x = nv[r];
+                            else pp[r][j].y = nv[r];
+                        }
                     } else {
-                        const float rA0 = __shfl_down_sync(0xffffffffu, p0[j].x, 1);
-                        const float lB1 = __shfl_up_sync(0xffffffffu, p1[j].y, 1);
-                        const float ymB = r1[me0 - TB_TX];  // row y0-1, column B
-                        const float ypA = r0[me0 + TB_TX];  // row y0+2, column A
-                        const unsigned ia = fidx(f, 1), ib = fidx(f, 2);
-                        const float nB0 = relax(p0[j].y, b0[j].y, coef[ia], ia & 0x40u, p0[j].x, rA0,
-                                                ymB, p1[j].y, p0[jd].y, p0[ju].y);
-                        const float nA1 = relax(p1[j].x, b1[j].x, coef[ib], ib & 0x40u, lB1, p1[j].y,
-                                                p0[j].x, ypA, p1[jd].x, p1[ju].x);
-                        p0[j].y = nB0;
-                        p1[j].x = nA1;
+#pragma unroll
+                        for (int r = 0; r < PY; ++r) {
+                            const unsigned f = ff[r / 2][j];
+                            if ((r & 1) == 0) {  // column B
+                                const float rA = __shfl_down_sync(0xffffffffu, pp[r][j].x, 1);
+                                const float ym = r == 0 ? above : pp[r - 1][j].y;
+                                const float yp = pp[r + 1][j].y;
+                                const unsigned ib = fidx(f, 1);
+                                nv[r] = relax(pp[r][j].y, bb[r][j].y, coef[ib], ib & 0x40u, pp[r][j].x, rA,
+                                              ym, yp, pp[r][jd].y, pp[r][ju].y);
+                            } else {              // column A
+                                const float lB = __shfl_up_sync(0xffffffffu, pp[r][j].y, 1);
+                                const float ym = pp[r - 1][j].x;
+                                const float yp = r == L ? below : pp[r + 1 < PY ? r + 1 : r][j].x;
+                                const unsigned ia = fidx(f, 2);
+                                nv[r] = relax(pp[r][j].x, bb[r][j].x, coef[ia], ia & 0x40u, lB, pp[r][j].y,
+                                              ym, yp, pp[r][jd].x, pp[r][ju].x);
+                            }
+                        }
+#pragma unroll
+                        for (int r = 0; r < PY; ++r) {
+                            if ((r & 1) == 0) pp[r][j].y = nv[r];
+                            else pp[r][j].x = nv[r];
+                        }
                     }
                 }
             }
@@ -358,8 +414,9 @@ k_sweep_tb(const __grid_constant__ TBMaps maps, Grid g, float* __restrict__ Pout
             const int zo = q - 1 - T;
             if (zo >= za && zo < zb) {
                 const int j = (k - 1 - T + 2 * R) % R;
-                if (in0) *reinterpret_cast<float2*>(Pout + off0 + g.XY * zo) = p0[j];
-                if (in1) *reinterpret_cast<float2*>(Pout + off1 + g.XY * zo) = p1[j];
+#pragma unroll
+                for (int r = 0; r < PY; ++r)
+                    if (in[r]) *reinterpret_cast<float2*>(Pout + off0 + r * g.X + g.XY * zo) = pp[r][j];
             }
             par ^= 1;
         }
@@ -367,7 +424,6 @@ k_sweep_tb(const __grid_constant__ TBMaps maps, Grid g, float* __restrict__ Pout
 
     if (check) block_max_to(rmax, &status->rmax_bits[group]);
 }
-
 
 // ---- host side --------------------------------------------------------------------------------
 
@@ -391,13 +447,13 @@ EncodeTiledFn encode_fn() {
     return fn;
 }
 
-bool encode_3d(CUtensorMap* m, const void* base, bool is_u8, const Grid& g) {
+bool encode_3d(CUtensorMap* m, const void* base, bool is_u8, const Grid& g, int rows) {
     EncodeTiledFn fn = encode_fn();
     if (!fn || base == nullptr || (reinterpret_cast<uintptr_t>(base) & 15u) != 0) return false;
     const size_t es = is_u8 ? 1 : 4;
     cuuint64_t dims[3] = {(cuuint64_t)g.X, (cuuint64_t)(g.ny + 1), (cuuint64_t)(g.nz + 1)};
     cuuint64_t strides[2] = {(cuuint64_t)g.X * es, (cuuint64_t)g.XY * es};
-    cuuint32_t box[3] = {(cuuint32_t)(is_u8 ? BOX_U8 : BOX_F), (cuuint32_t)ROWS, 1u};
+    cuuint32_t box[3] = {(cuuint32_t)(is_u8 ? BOX_U8 : BOX_F), (cuuint32_t)rows, 1u};
     cuuint32_t estr[3] = {1u, 1u, 1u};
     CUresult r = fn(m, is_u8 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
                     const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
@@ -406,30 +462,33 @@ bool encode_3d(CUtensorMap* m, const void* base, bool is_u8, const Grid& g) {
     return r == CUDA_SUCCESS;
 }
 
-template <int T>
+template <int T, int PY>
 constexpr size_t tb_smem_bytes() {
-    return 128 + (size_t)((T + 4) / 2) * STAGE_BYTES + sizeof(float) * 2 * (4 + 2 * T) * (TB_TY + 2) * TB_TX;
+    using G = TBGeom<PY>;
+    return 128 + (size_t)((T + 4) / 2) * G::STAGE_BYTES + sizeof(float) * 2 * (4 + 2 * T) * G::PROW;
 }
 
-template <int T>
+template <int T, int PY>
 int configure_tb() {
-    return cudaFuncSetAttribute(k_sweep_tb<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)tb_smem_bytes<T>()) == cudaSuccess ? 0 : -1;
+    return cudaFuncSetAttribute(k_sweep_tb<T, PY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)tb_smem_bytes<T, PY>()) == cudaSuccess ? 0 : -1;
 }
 
-template <int T>
+template <int T, int PY>
 int launch_tb(const TBMaps& maps, const Grid& g, float* Pout, int nhalf, int colour0, int zchunk,
               const float* wacc7, StepStatus* status, int check, int group, float tol, int* pcur,
               int out_idx, int* kerr, const int* group_base, cudaStream_t st) {
-    const size_t smem = tb_smem_bytes<T>();
+    using G = TBGeom<PY>;
+    const size_t smem = tb_smem_bytes<T, PY>();
     WAcc8 wa;
     for (int k = 0; k < 7; ++k) wa.w[k] = wacc7[k];
     wa.w[7] = 0.0f;
-    constexpr int IX = 2 * TB_TX - 2 * T, IY = ROWS - 2 * T;
+    constexpr int IX = 2 * TB_TX - 2 * T, IY = G::ROWS - 2 * T;
     dim3 grid((unsigned)((g.nx + IX - 1) / IX), (unsigned)((g.ny + IY - 1) / IY),
               (unsigned)((g.nz + zchunk - 1) / zchunk));
-    k_sweep_tb<T><<<grid, dim3(TB_TX, TB_TY), smem, st>>>(maps, g, Pout, nhalf, colour0, zchunk, wa, status,
-                                                         check, group, tol, pcur, out_idx, kerr, group_base);
+    k_sweep_tb<T, PY><<<grid, dim3(TB_TX, G::TY), smem, st>>>(maps, g, Pout, nhalf, colour0, zchunk, wa,
+                                                             status, check, group, tol, pcur, out_idx,
+                                                             kerr, group_base);
     return 0;
 }
 
@@ -447,41 +506,54 @@ __global__ void k_group_loop_next(const StepStatus* status, int* counter, int st
 
 }  // namespace
 
-int sweep_tb_depth_supported(int T) { return T == 2 || T == 4 || T == 6; }
+int sweep_tb_shape_supported(int T, int rows) {
+    return (rows == 2 && (T == 2 || T == 4 || T == 6)) || (rows == 4 && T == 4);
+}
 
-int prepare_sweep_kernels() { return configure_tb<2>() | configure_tb<4>() | configure_tb<6>(); }
+int prepare_sweep_kernels() {
+    return configure_tb<2, 2>() | configure_tb<4, 2>() | configure_tb<6, 2>() | configure_tb<4, 4>();
+}
 
-// Tensor maps for the sweep's TMA loads: P_a, P_b, b (float) and flags (u8).
+// Tensor maps for the sweep's TMA loads: P_a, P_b, b (float) and flags (u8), for the box
+// heights of the 2-row ([0]) and 4-row ([1]) patch kernels.
 struct SweepMaps {
-    CUtensorMap pa, pb, b, f;
+    CUtensorMap pa[2], pb[2], b[2], f[2];
 };
 
 SweepMaps* create_sweep_maps(const Grid& g, const float* Pa, const float* Pb, const float* b,
                              const uint8_t* flags) {
     SweepMaps* m = new SweepMaps();
-    if (!encode_3d(&m->pa, Pa, false, g) || !encode_3d(&m->pb, Pb, false, g) ||
-        !encode_3d(&m->b, b, false, g) || !encode_3d(&m->f, flags, true, g)) {
-        delete m;
-        return nullptr;
+    const int rows[2] = {TBGeom<2>::ROWS, TBGeom<4>::ROWS};
+    for (int v = 0; v < 2; ++v) {
+        if (!encode_3d(&m->pa[v], Pa, false, g, rows[v]) || !encode_3d(&m->pb[v], Pb, false, g, rows[v]) ||
+            !encode_3d(&m->b[v], b, false, g, rows[v]) || !encode_3d(&m->f[v], flags, true, g, rows[v])) {
+            delete m;
+            return nullptr;
+        }
     }
     return m;
 }
 
 void destroy_sweep_maps(SweepMaps* m) { delete m; }
 
-int launch_sweep_tb(const SweepMaps* m, const Grid& g, bool in_is_a, float* Pout, int T, int nhalf,
-                    int colour0, int zchunk, const float* wacc7, StepStatus* status, int check,
-                    int group, float tol, int* pcur, int out_idx, int* kerr, const int* group_base,
-                    cudaStream_t st) {
+int launch_sweep_tb(const SweepMaps* m, const Grid& g, bool in_is_a, float* Pout, int T, int rows,
+                    int nhalf, int colour0, int zchunk, const float* wacc7, StepStatus* status,
+                    int check, int group, float tol, int* pcur, int out_idx, int* kerr,
+                    const int* group_base, cudaStream_t st) {
+    if (!sweep_tb_shape_supported(T, rows)) return -1;
+    const int v = rows == 4 ? 1 : 0;
     TBMaps maps;
-    maps.pin = in_is_a ? m->pa : m->pb;
-    maps.b = m->b;
-    maps.f = m->f;
+    maps.pin = in_is_a ? m->pa[v] : m->pb[v];
+    maps.b = m->b[v];
+    maps.f = m->f[v];
+#define SMK_TB_ARGS maps, g, Pout, nhalf, colour0, zchunk, wacc7, status, check, group, tol, pcur, out_idx, kerr, group_base, st
+    if (rows == 4) return launch_tb<4, 4>(SMK_TB_ARGS);
     switch (T) {
-        case 2: return launch_tb<2>(maps, g, Pout, nhalf, colour0, zchunk, wacc7, status, check, group, tol, pcur, out_idx, kerr, group_base, st);
-        case 4: return launch_tb<4>(maps, g, Pout, nhalf, colour0, zchunk, wacc7, status, check, group, tol, pcur, out_idx, kerr, group_base, st);
-        default: return launch_tb<6>(maps, g, Pout, nhalf, colour0, zchunk, wacc7, status, check, group, tol, pcur, out_idx, kerr, group_base, st);
+        case 2: return launch_tb<2, 2>(SMK_TB_ARGS);
+        case 4: return launch_tb<4, 2>(SMK_TB_ARGS);
+        default: return launch_tb<6, 2>(SMK_TB_ARGS);
     }
+#undef SMK_TB_ARGS
 }
 
 void launch_group_loop_next(const StepStatus* status, int* counter, int step, int limit,

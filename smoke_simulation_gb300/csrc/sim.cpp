@@ -266,7 +266,7 @@ int smk_sim::enqueue(float dt, cudaStream_t st) {
                 for (int h = 2 * s0; h < h1; h += sweep_depth) {
                     const int nh = h1 - h < sweep_depth ? h1 - h : sweep_depth;
                     const bool in_a = (nl & 1) == 0;
-                    if (launch_sweep_tb(maps, g, in_a, in_a ? P2 : P, sweep_depth, nh, h & 1, sweep_zchunk,
+                    if (launch_sweep_tb(maps, g, in_a, in_a ? P2 : P, sweep_depth, sweep_rows, nh, h & 1, sweep_zchunk,
                                         wacc, use_tol ? status : nullptr, use_tol && h == 2 * s0, grp, p.tol,
                                         pcur, in_a ? 1 : 0, kerr, gbase, s) != 0)
                         return fail(SMK_ERR_CUDA, "sweep kernel configuration failed");
@@ -431,6 +431,7 @@ std::string smk_sim::graph_signature(float dt) const {
     put(&p, sizeof(p));
     put(&sweep_depth, sizeof(sweep_depth));
     put(&sweep_zchunk, sizeof(sweep_zchunk));
+    put(&sweep_rows, sizeof(sweep_rows));
     const char t = timing ? 1 : 0;
     put(&t, 1);
     for (const Object& o : objects) put(&o, sizeof(o));
@@ -890,14 +891,19 @@ long long smk_launch_count(const smk_sim* sim) {
 
 extern "C" {
 
-int smk_set_sweep_kernel(smk_sim* sim, int depth, int zchunk) {
+int smk_set_sweep_shape(smk_sim* sim, int depth, int rows, int zchunk) {
     if (!sim) return fail(SMK_ERR_INVALID, "sim is null");
-    if (depth != 0 && !sweep_tb_depth_supported(depth))
-        return fail(SMK_ERR_INVALID, "sweep depth must be 0, 2, 4 or 6");
+    if (depth != 0 && !sweep_tb_shape_supported(depth, rows))
+        return fail(SMK_ERR_INVALID, "sweep shape must be depth 0, depth 2/4/6 with 2 rows, or depth 4 with 4 rows");
     if (zchunk < 1) return fail(SMK_ERR_INVALID, "zchunk must be >= 1");
     sim->sweep_depth = depth;
+    sim->sweep_rows = depth != 0 ? rows : 2;
     sim->sweep_zchunk = zchunk;
     return SMK_OK;
+}
+
+int smk_set_sweep_kernel(smk_sim* sim, int depth, int zchunk) {
+    return smk_set_sweep_shape(sim, depth, 2, zchunk);
 }
 
 int smk_set_graphs(smk_sim* sim, int enable) {
@@ -916,6 +922,14 @@ int smk_set_graph_loops(smk_sim* sim, int enable) {
 int smk_get_sweep_kernel(const smk_sim* sim, int* depth, int* zchunk) {
     if (!sim) return fail(SMK_ERR_INVALID, "sim is null");
     if (depth) *depth = sim->sweep_depth;
+    if (zchunk) *zchunk = sim->sweep_zchunk;
+    return SMK_OK;
+}
+
+int smk_get_sweep_shape(const smk_sim* sim, int* depth, int* rows, int* zchunk) {
+    if (!sim) return fail(SMK_ERR_INVALID, "sim is null");
+    if (depth) *depth = sim->sweep_depth;
+    if (rows) *rows = sim->sweep_rows;
     if (zchunk) *zchunk = sim->sweep_zchunk;
     return SMK_OK;
 }
@@ -940,7 +954,8 @@ int smk_get_sweep_kernel(const smk_sim* sim, int* depth, int* zchunk) {
 namespace {
 std::mutex g_tune_mutex;
 // key: device, grid shape, tolerance group size (0 = no tolerance)
-std::map<std::tuple<int, int, int, int, int>, std::pair<int, int>> g_tune_cache;
+struct TunedShape { int depth, rows, zchunk; };
+std::map<std::tuple<int, int, int, int, int>, TunedShape> g_tune_cache;
 }  // namespace
 
 extern "C" {
@@ -957,8 +972,9 @@ int smk_autotune(smk_sim* sim, int* depth_out, int* zchunk_out, float* us_per_sw
         std::lock_guard<std::mutex> lock(g_tune_mutex);
         auto it = g_tune_cache.find(key);
         if (it != g_tune_cache.end()) {
-            sim->sweep_depth = it->second.first;
-            sim->sweep_zchunk = it->second.second;
+            sim->sweep_depth = it->second.depth;
+            sim->sweep_rows = it->second.rows;
+            sim->sweep_zchunk = it->second.zchunk;
             if (depth_out) *depth_out = sim->sweep_depth;
             if (zchunk_out) *zchunk_out = sim->sweep_zchunk;
             if (us_per_sweep_out) *us_per_sweep_out = -1.0f;
@@ -981,35 +997,36 @@ int smk_autotune(smk_sim* sim, int* depth_out, int* zchunk_out, float* us_per_sw
     cudaEvent_t e0, e1;
     SMK_CUDA(cudaEventCreate(&e0));
     SMK_CUDA(cudaEventCreate(&e1));
-    int best_d = sim->sweep_depth, best_z = sim->sweep_zchunk;
+    int best_d = sim->sweep_depth, best_r = sim->sweep_rows, best_z = sim->sweep_zchunk;
     float best = 1e30f;
-    const int depths[3] = {2, 4, 6};
+    const int shapes[4][2] = {{2, 2}, {4, 2}, {6, 2}, {4, 4}};  // (depth, patch rows)
     // time one tolerance group exactly as a step issues it: 2G colour passes in launches of
     // `d` (the last one partial when d does not divide 2G), the first with the fused residual
     const bool use_tol = sim->p.tol > 0.0f;
     const int G = use_tol ? sim->p.check_every : std::max(1, std::min(sim->p.max_sweeps, 20));
-    auto run_group = [&](int d, int zc) -> int {
+    auto run_group = [&](int d, int rows, int zc) -> int {
         if (use_tol) SMK_CUDA(cudaMemsetAsync(sim->tune_status, 0, sizeof(StepStatus) + sizeof(unsigned), st));
         for (int h = 0; h < 2 * G; h += d) {
             const int nh = 2 * G - h < d ? 2 * G - h : d;
-            if (launch_sweep_tb(sim->maps, g, true, sim->P2, d, nh, h & 1, zc, wacc,
+            if (launch_sweep_tb(sim->maps, g, true, sim->P2, d, rows, nh, h & 1, zc, wacc,
                                 use_tol ? sim->tune_status : nullptr, use_tol && h == 0, 0, sim->p.tol,
                                 nullptr, 0, sim->kerr, nullptr, st) != 0)
                 return fail(SMK_ERR_CUDA, "sweep kernel configuration failed");
         }
         return SMK_OK;
     };
-    for (int d : depths) {
+    for (const auto& shape : shapes) {
+        const int d = shape[0], rows = shape[1];
         const int R = d + 4;
         for (int m = 2; m <= 16; ++m) {
             const int zc = R * m - 2 * d - 1;
             if (zc < 8) continue;
             if (zc > g.nz + R) break;
             const int reps = 2;
-            int rc = run_group(d, zc);  // warm
+            int rc = run_group(d, rows, zc);  // warm
             if (rc) return rc;
             SMK_CUDA(cudaEventRecord(e0, st));
-            for (int r = 0; r < reps && rc == SMK_OK; ++r) rc = run_group(d, zc);
+            for (int r = 0; r < reps && rc == SMK_OK; ++r) rc = run_group(d, rows, zc);
             if (rc) return rc;
             SMK_CUDA(cudaEventRecord(e1, st));
             SMK_CUDA(cudaEventSynchronize(e1));
@@ -1019,6 +1036,7 @@ int smk_autotune(smk_sim* sim, int* depth_out, int* zchunk_out, float* us_per_sw
             if (us_per_sweep < best) {
                 best = us_per_sweep;
                 best_d = d;
+                best_r = rows;
                 best_z = zc;
             }
             if (zc > g.nz) break;
@@ -1031,10 +1049,11 @@ int smk_autotune(smk_sim* sim, int* depth_out, int* zchunk_out, float* us_per_sw
     int krc = check_kernel_error(sim);
     if (krc) return krc;
     sim->sweep_depth = best_d;
+    sim->sweep_rows = best_r;
     sim->sweep_zchunk = best_z;
     {
         std::lock_guard<std::mutex> lock(g_tune_mutex);
-        g_tune_cache[key] = std::make_pair(best_d, best_z);
+        g_tune_cache[key] = TunedShape{best_d, best_r, best_z};
     }
     if (depth_out) *depth_out = best_d;
     if (zchunk_out) *zchunk_out = best_z;

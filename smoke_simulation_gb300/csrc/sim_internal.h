@@ -87,6 +87,7 @@ struct smk_sim {
     // launch over z-chunks of sweep_zchunk planes (chosen by smk_set_sweep_kernel / autotune)
     int sweep_depth = 4;
     int sweep_zchunk = 47;
+    int sweep_rows = 2;  // cell rows of a thread's patch in the blocked kernel (2 or 4)
 
     bool timing = false;
     cudaEvent_t ev[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
