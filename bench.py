@@ -518,6 +518,7 @@ def run_forms(args, smk, torch):
                          "max_div_post_projection": float(max(x.div_max for x in st)),
                          "launches_per_step": (l1 - l0) / args.forms_steps,
                          "schedule": {"ctas_per_sm_zslab_wavebytes": b.schedule(),
+                                      "blocked_zchunk": b.blocked(),
                                       "tuned_us_per_sweep": sched_us}}
         dens[name] = [s.read_density() for s in sims]
         b.close()
@@ -538,8 +539,10 @@ def run_forms(args, smk, torch):
         s.close()
     forms["batched"] = {"workload": "64 grids, cube side log-uniform 32..128 (seed 2), sphere solid + box "
                                     "emitter each, dt=0.05, warm-started pressure to max|div|<=1e-4; "
-                                    "one persistent launch per stage over all grids (grouped form), "
-                                    "CUDA-graph replay, schedule from the autotuner",
+                                    "one persistent launch per stage over all grids (grouped form; the "
+                                    "solve as cooperative colour passes or blocked launches over every "
+                                    "grid's tiles, whichever the autotuner finds faster), CUDA-graph "
+                                    "replay",
                         "cells": cells, "steps": args.forms_steps, "grouped": batched, "plain": plain,
                         "grouped_bf16_vs_plain": batched["bf16"]["value"] / plain["value"],
                         "grouped_f32_vs_plain": batched["f32"]["value"] / plain["value"]}

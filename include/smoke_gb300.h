@@ -214,9 +214,10 @@ int smk_batch_set_graphs(smk_batch* batch, int enable);
 /* The form the last step ran (SMK_BATCH_GROUPED or SMK_BATCH_BRANCHES; 0 before the first
  * step) and the kernels the batch has launched so far (either pointer may be NULL). */
 int smk_batch_get_info(const smk_batch* batch, int* last_mode, long long* launches);
-/* Time the grouped projection kernel's schedules (CTAs per SM, z planes per tile, solve-wave
- * budget) on the members' scratch pressure buffers and keep the fastest.  Synchronises; does
- * not change any member's results.  Outputs may be NULL. */
+/* Time the grouped projection's schedules (the cooperative colour-pass kernel: CTAs per SM, z
+ * planes per tile, solve-wave budget; the blocked solve: z-chunk) on the members' scratch
+ * pressure buffers and keep the fastest.  Synchronises; does not change any member's results.
+ * Outputs may be NULL (ctas_per_sm is 0 when the blocked solve wins). */
 int smk_batch_autotune(smk_batch* batch, int* ctas_per_sm, float* us_per_sweep);
 /* The grouped projection's schedule: cooperative CTAs per SM (0: all resident), z planes per
  * sweep tile, and the solve-wave budget in bytes of pressure + rhs + flags (0: one wave; else
@@ -224,6 +225,14 @@ int smk_batch_autotune(smk_batch* batch, int* ctas_per_sm, float* us_per_sweep);
  * Results do not depend on it. */
 int smk_batch_get_schedule(const smk_batch* batch, int* ctas_per_sm, int* zslab, long long* wave_bytes);
 int smk_batch_set_schedule(smk_batch* batch, int ctas_per_sm, int zslab, long long wave_bytes);
+/* The grouped form's blocked solve: zchunk > 0 replaces the cooperative kernel's colour passes
+ * by launches of the temporally blocked sweep kernel over every member's tiles (3 sweeps per
+ * launch, z-chunks of `zchunk` planes, the tolerance groups as a device-side loop in the
+ * captured step), when every member has a tolerance rule with the same group size and sweep
+ * cap; 0 = colour passes.  smk_batch_set_schedule resets it to 0.  Results do not depend on
+ * it. */
+int smk_batch_set_blocked(smk_batch* batch, int zchunk);
+int smk_batch_get_blocked(const smk_batch* batch, int* zchunk);
 
 /* Serving: many simulation requests kept resident on one GPU with continuous admission.  No
  * counterpart in the reference (one simulation stepped from the render loop, main.cpp:889-896).

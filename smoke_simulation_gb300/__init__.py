@@ -121,6 +121,8 @@ def lib() -> C.CDLL:
         "smk_batch_autotune": (i, [vp, C.POINTER(i), C.POINTER(f)]),
         "smk_batch_get_schedule": (i, [vp, C.POINTER(i), C.POINTER(i), C.POINTER(C.c_longlong)]),
         "smk_batch_set_schedule": (i, [vp, i, i, C.c_longlong]),
+        "smk_batch_set_blocked": (i, [vp, i]),
+        "smk_batch_get_blocked": (i, [vp, C.POINTER(i)]),
         "smk_project_noalloc_last_error": (C.c_char_p, []),
     }
     for name, (res, args) in sig.items():
@@ -387,6 +389,15 @@ class Batch:
 
     def set_schedule(self, ctas_per_sm: int, zslab: int, wave_bytes: int):
         _check(lib().smk_batch_set_schedule(self.h, int(ctas_per_sm), int(zslab), int(wave_bytes)))
+
+    def set_blocked(self, zchunk: int):
+        """Blocked grouped solve with z-chunks of `zchunk` planes (0: cooperative colour passes)."""
+        _check(lib().smk_batch_set_blocked(self.h, int(zchunk)))
+
+    def blocked(self) -> int:
+        z = C.c_int()
+        _check(lib().smk_batch_get_blocked(self.h, C.byref(z)))
+        return z.value
 
     def step(self, dt, stream: int = 0):
         """dt: one float for every member, or a sequence with one dt per member."""

@@ -42,6 +42,7 @@ struct smk_batch {
     std::vector<cudaStream_t> branch;
     std::vector<cudaEvent_t> join;
     cudaStream_t origin = nullptr;
+    cudaStream_t body = nullptr;  // captures the grouped blocked solve's loop body
     cudaEvent_t fork = nullptr;
     cudaGraphExec_t exec = nullptr;
     std::string sig;
@@ -56,13 +57,15 @@ struct smk_batch {
         cudaGraphExec_t exec = nullptr;
         GroupArgs args{};
         GroupLaunch L{};
+        GroupTBLaunch tb{};
+        bool blocked = false;
         int kernels = 0;
         unsigned long long used = 0;
     };
     Slot slots[2];
     unsigned long long clock = 0;
     // schedule of the grouped projection; ctas_per_sm 0 = all resident CTAs
-    GroupSchedule sched{0, 4, 0};
+    GroupSchedule sched{0, 4, 0, 0};
 };
 
 namespace {
@@ -79,7 +82,26 @@ struct TableImage {
     std::vector<SphereObj> spheres;
     int zslab = 1, nwaves = 1;
     size_t off_grids = 0, off_starts = 0, off_boxes = 0, off_spheres = 0, bytes = 0;
+    // blocked solve: one record per grid (tensor maps, buffers), tile prefix sums, loop counter
+    bool blocked = false;
+    int tb_zchunk = 0, tb_total = 0, tb_check_every = 0, tb_max_sweeps = 0;
+    std::vector<unsigned char> tb_recs;
+    std::vector<int> tb_starts;
+    size_t off_tb = 0, off_tb_starts = 0, off_tb_counter = 0;
 };
+
+// The blocked solve needs every member to share the tolerance group size and the sweep cap,
+// with a tolerance rule (the launches of a group run in lockstep over all grids).
+bool blocked_eligible(smk_sim* const* sims, int n) {
+    if (n <= 0) return false;
+    for (int i = 0; i < n; ++i) {
+        const smk_params& p = sims[i]->p;
+        if (!sims[i]->maps || p.tol <= 0.0f || p.max_sweeps <= 0 || p.check_every < 1 ||
+            p.check_every != sims[0]->p.check_every || p.max_sweeps != sims[0]->p.max_sweeps)
+            return false;
+    }
+    return true;
+}
 
 // Solve waves: first-fit decreasing on each grid's solver working set (P, b: 4 bytes, flags:
 // 1 byte per element), so that one wave's passes can stay in L2.  A grid larger than the
@@ -201,6 +223,28 @@ int build_table(smk_sim* const* sims, int n, const float* dts, float dt_all, con
     for (int i = 0; i < n; ++i) fill_record(sims[i], dts ? dts[i] : dt_all, t, t.grids[i]);
     t.zslab = std::max(1, sch.zslab);
     t.nwaves = assign_waves(t.grids, sch.wave_bytes);
+    t.blocked = sch.blocked_zchunk > 0 && blocked_eligible(sims, n);
+    if (t.blocked) {
+        const size_t rb = group_tb_record_bytes();
+        t.tb_zchunk = sch.blocked_zchunk;
+        t.tb_check_every = sims[0]->p.check_every;
+        t.tb_max_sweeps = sims[0]->p.max_sweeps;
+        t.tb_recs.assign(rb * n, 0);
+        t.tb_starts.assign(n + 1, 0);
+        long long acc = 0;
+        for (int i = 0; i < n; ++i) {
+            smk_sim* sm = sims[i];
+            float wacc[7];
+            wacc[0] = 0.0f;
+            for (int a = 1; a <= 6; ++a) wacc[a] = (float)sm->p.omega / (float)a;
+            t.tb_starts[i] = (int)acc;
+            acc += group_tb_fill(&t.tb_recs[rb * i], sm->maps, sm->g, sm->P, sm->P2, sm->status, sm->pcur, sm->kerr,
+                                 wacc, sm->p.tol, t.tb_zchunk);
+            if (acc > INT_MAX / 2) return smk_fail(SMK_ERR_INVALID, "batch too large for one blocked launch");
+        }
+        t.tb_starts[n] = (int)acc;
+        t.tb_total = (int)acc;
+    }
     t.starts.assign((size_t)GS_COUNT * (n + 1), 0);
     for (int s = 0; s < GS_COUNT; ++s) {
         long long acc = 0;
@@ -220,6 +264,14 @@ int build_table(smk_sim* const* sims, int n, const float* dts, float dt_all, con
     off = align_up(off + sizeof(BoxObj) * std::max<size_t>(1, t.boxes.size()), 256);
     t.off_spheres = off;
     off = align_up(off + sizeof(SphereObj) * std::max<size_t>(1, t.spheres.size()), 256);
+    if (t.blocked) {
+        t.off_tb = off;  // 256-byte aligned: the tensor maps in the records need 64
+        off = align_up(off + t.tb_recs.size(), 256);
+        t.off_tb_starts = off;
+        off = align_up(off + sizeof(int) * t.tb_starts.size(), 256);
+        t.off_tb_counter = off;
+        off = align_up(off + sizeof(int), 256);
+    }
     t.bytes = off;
     return SMK_OK;
 }
@@ -231,6 +283,26 @@ void pack_table(const TableImage& t, char* blob) {
     memcpy(blob + t.off_starts, t.starts.data(), sizeof(int) * t.starts.size());
     if (!t.boxes.empty()) memcpy(blob + t.off_boxes, t.boxes.data(), sizeof(BoxObj) * t.boxes.size());
     if (!t.spheres.empty()) memcpy(blob + t.off_spheres, t.spheres.data(), sizeof(SphereObj) * t.spheres.size());
+    if (t.blocked) {
+        memcpy(blob + t.off_tb, t.tb_recs.data(), t.tb_recs.size());
+        memcpy(blob + t.off_tb_starts, t.tb_starts.data(), sizeof(int) * t.tb_starts.size());
+    }
+}
+
+// Blocked-solve launch description for a table whose device copy starts at `dev`.
+GroupTBLaunch tb_launch(const TableImage& t, void* dev, int n, cudaStream_t body) {
+    GroupTBLaunch tb{};
+    char* base = static_cast<char*>(dev);
+    tb.grids = base + t.off_tb;
+    tb.starts = reinterpret_cast<const int*>(base + t.off_tb_starts);
+    tb.n = n;
+    tb.total = t.tb_total;
+    tb.zchunk = t.tb_zchunk;
+    tb.check_every = t.tb_check_every;
+    tb.max_sweeps = t.tb_max_sweeps;
+    tb.counter = reinterpret_cast<int*>(base + t.off_tb_counter);
+    tb.body = body;
+    return tb;
 }
 
 // Kernel arguments for a table whose device copy starts at `dev`.
@@ -245,6 +317,7 @@ void table_args(const TableImage& t, void* dev, GroupArgs& a, int n) {
     a.zslab = t.zslab;
     a.nwaves = t.nwaves;
     a.sweeps_only = 0;
+    a.phases = GP_ALL;
 }
 
 // Copy a table image into `dev` (synchronous; callers hold no step that reads it in flight).
@@ -338,10 +411,16 @@ int grouped_step(smk_batch* b, const float* dts, float dt_all, cudaStream_t st) 
         if (rc) return rc;
         rc = launch_config(b->sched, t, slot->L, slot->kernels);
         if (rc) return rc;
+        slot->blocked = t.blocked;
+        if (t.blocked) {
+            slot->tb = tb_launch(t, slot->dev, n, b->body);
+            slot->kernels += 1;  // the projection's second cooperative launch (the blocked solve's
+                                 // launches, some inside a device-side loop, are not counted)
+        }
         if (b->use_graphs && b->graphs_ok) {
             cudaGraph_t graph = nullptr;
             SMK_CUDA(cudaStreamBeginCapture(b->origin, cudaStreamCaptureModeThreadLocal));
-            const int lrc = launch_group_step(slot->args, slot->L, b->origin);
+            const int lrc = launch_group_step(slot->args, slot->L, b->origin, slot->blocked ? &slot->tb : nullptr);
             const cudaError_t ee = cudaStreamEndCapture(b->origin, &graph);
             cudaError_t ie = cudaErrorUnknown;
             if (lrc == 0 && ee == cudaSuccess) ie = cudaGraphInstantiate(&slot->exec, graph, 0);
@@ -359,7 +438,7 @@ int grouped_step(smk_batch* b, const float* dts, float dt_all, cudaStream_t st) 
     if (slot->exec) {
         SMK_CUDA(cudaGraphLaunch(slot->exec, st));
     } else {
-        const int lrc = launch_group_step(slot->args, slot->L, st);
+        const int lrc = launch_group_step(slot->args, slot->L, st, slot->blocked ? &slot->tb : nullptr);
         if (lrc) return smk_fail(SMK_ERR_CUDA, std::string("grouped step: ") + cudaGetErrorString((cudaError_t)lrc));
     }
     b->launches += slot->kernels;
@@ -542,7 +621,9 @@ int group_runner_step(GroupRunner* r, smk_sim* const* sims, const float* dts, in
     int nk = 0;
     rc = launch_config(sched, t, L, nk);
     if (rc) return rc;
-    const int lrc = launch_group_step(a, L, st);
+    GroupTBLaunch tb{};
+    if (t.blocked) tb = tb_launch(t, sl.dev, n, nullptr);
+    const int lrc = launch_group_step(a, L, st, t.blocked ? &tb : nullptr);
     if (lrc) return smk_fail(SMK_ERR_CUDA, std::string("grouped step: ") + cudaGetErrorString((cudaError_t)lrc));
     SMK_CUDA(cudaEventRecord(sl.done, st));
     sl.used = true;
@@ -569,10 +650,12 @@ int smk_batch_create(int count, smk_sim* const* sims, smk_batch** out) {
         for (auto s : b->branch) if (s) cudaStreamDestroy(s);
         for (auto e : b->join) if (e) cudaEventDestroy(e);
         if (b->origin) cudaStreamDestroy(b->origin);
+        if (b->body) cudaStreamDestroy(b->body);
         if (b->fork) cudaEventDestroy(b->fork);
         delete b;
     };
     if (cudaStreamCreateWithFlags(&b->origin, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&b->body, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess) {
         cleanup();
         return smk_fail(SMK_ERR_CUDA, "batch stream/event creation failed");
@@ -601,6 +684,7 @@ int smk_batch_destroy(smk_batch* b) {
     for (auto s : b->branch) cudaStreamDestroy(s);
     for (auto e : b->join) cudaEventDestroy(e);
     cudaStreamDestroy(b->origin);
+    cudaStreamDestroy(b->body);
     cudaEventDestroy(b->fork);
     delete b;
     return SMK_OK;
@@ -729,6 +813,55 @@ int smk_batch_autotune(smk_batch* b, int* ctas_per_sm, float* us_per_sweep) {
             }
         }
     }
+    // the blocked solve (when every member can use it): depth-6 launches over all grids' tiles,
+    // timed without tolerance checks, reading P and writing the scratch P2 (no status, no pcur)
+    const int zchunks[] = {17, 27, 37, 57, 117, 137, 257};  // 10 m - 13: no padding of the 10-plane unroll
+    if (!rc && blocked_eligible(b->sims.data(), n)) {
+        for (int zc : zchunks) {
+            TableImage t;
+            rc = build_table(b->sims.data(), n, nullptr, 0.0f, GroupSchedule{0, 4, 0, zc}, t);
+            if (rc) break;
+            const size_t rb = group_tb_record_bytes();
+            for (int i = 0; i < n; ++i) {
+                smk_sim* sm = b->sims[i];
+                float wacc[7];
+                wacc[0] = 0.0f;
+                for (int a = 1; a <= 6; ++a) wacc[a] = (float)sm->p.omega / (float)a;
+                group_tb_fill(&t.tb_recs[rb * i], sm->maps, sm->g, sm->P, sm->P2, nullptr, nullptr, sm->kerr, wacc,
+                              sm->p.tol, zc);
+            }
+            if (cap < t.bytes) {
+                if (dev) cudaFree(dev);
+                dev = nullptr;
+                if (cudaMalloc(&dev, t.bytes) != cudaSuccess) {
+                    rc = smk_fail(SMK_ERR_OOM, "autotune table allocation failed");
+                    break;
+                }
+                cap = t.bytes;
+            }
+            GroupArgs a{};
+            rc = upload_table(t, dev, a, n);
+            if (rc) break;
+            const GroupTBLaunch tb = tb_launch(t, dev, n, nullptr);
+            const int reps = 3, launches = 3;  // 9 sweeps per repetition
+            int lrc = launch_group_tb_sweeps(tb, launches, st);  // warm
+            if (!lrc) lrc = (int)cudaEventRecord(e0, st);
+            for (int r = 0; r < reps && !lrc; ++r) lrc = launch_group_tb_sweeps(tb, launches, st);
+            if (!lrc) lrc = (int)cudaEventRecord(e1, st);
+            if (!lrc) lrc = (int)cudaEventSynchronize(e1);
+            if (lrc) {
+                rc = smk_fail(SMK_ERR_CUDA, std::string("autotune launch: ") + cudaGetErrorString((cudaError_t)lrc));
+                break;
+            }
+            float ms = 0.0f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            const float us = 1e3f * ms / (reps * launches * 3);
+            if (us < best) {
+                best = us;
+                best_s = GroupSchedule{0, 4, 0, zc};
+            }
+        }
+    }
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
     if (st) cudaStreamDestroy(st);
@@ -758,7 +891,20 @@ int smk_batch_set_schedule(smk_batch* b, int ctas_per_sm, int zslab, long long w
     if (!b) return smk_fail(SMK_ERR_INVALID, "batch is null");
     if (ctas_per_sm < 0 || zslab < 1 || zslab > 4096 || wave_bytes < 0)
         return smk_fail(SMK_ERR_INVALID, "invalid grouped schedule");
-    b->sched = GroupSchedule{ctas_per_sm, zslab, wave_bytes};
+    b->sched = GroupSchedule{ctas_per_sm, zslab, wave_bytes, 0};
+    return SMK_OK;
+}
+
+int smk_batch_set_blocked(smk_batch* b, int zchunk) {
+    if (!b) return smk_fail(SMK_ERR_INVALID, "batch is null");
+    if (zchunk < 0) return smk_fail(SMK_ERR_INVALID, "zchunk must be >= 0");
+    b->sched.blocked_zchunk = zchunk;
+    return SMK_OK;
+}
+
+int smk_batch_get_blocked(const smk_batch* b, int* zchunk) {
+    if (!b) return smk_fail(SMK_ERR_INVALID, "batch is null");
+    if (zchunk) *zchunk = b->sched.blocked_zchunk;
     return SMK_OK;
 }
 

@@ -82,6 +82,9 @@ struct GroupSync {
     int pad;
 };
 
+// Phases of the cooperative projection kernel.
+enum : int { GP_RHS = 1, GP_SOLVE = 2, GP_FINISH = 4, GP_ALL = 7 };
+
 struct GroupArgs {
     const GroupGrid* grids;
     const int* starts;  // GS_COUNT rows of n + 1 tile prefix sums
@@ -92,6 +95,23 @@ struct GroupArgs {
     int zslab;        // z planes per sweep / residual / divergence tile (a thread walks them)
     int nwaves;       // solve waves (every grid's `wave` is below this)
     int sweeps_only;  // tuning: only the sweep passes (fixed count, no checks), on scratch buffers
+    int phases;       // GP_* bits: rhs + pressure start, colour-pass solve, subtract + divergence
+};
+
+// The blocked form of the grouped solve (host side): instead of the cooperative kernel's colour
+// passes, launches of the temporally blocked sweep kernel over every grid's tiles, each
+// launch depth 6, a tolerance check in the first launch of each group (all grids share the
+// group size and the sweep cap), the full groups as a device-side WHILE loop when captured.
+struct GroupTBLaunch {
+    const void* grids;   // device records (group_tb_record_bytes() each)
+    const int* starts;   // device: n + 1 tile prefix sums
+    int n;
+    int total;           // tiles of one launch
+    int zchunk;
+    int check_every;     // sweeps per tolerance group
+    int max_sweeps;
+    int* counter;        // device: the loop's group counter
+    cudaStream_t body;   // stream used to capture the loop body
 };
 
 __host__ __device__ inline int group_div_up(int a, int b) { return (a + b - 1) / b; }
@@ -152,6 +172,7 @@ struct GroupSchedule {
     int ctas_per_sm;        // cooperative CTAs per SM
     int zslab;              // planes per flattened tile
     long long wave_bytes;   // pressure + rhs + flags bytes per solve wave (0: one wave)
+    int blocked_zchunk;     // > 0: blocked solve (GroupTBLaunch) with z-chunks of this many planes
 };
 
 // Launch configuration of one grouped step (host side).
@@ -163,7 +184,9 @@ struct GroupLaunch {
 
 // Host launchers (kernels_group.cu).  Return 0 or a cudaError_t value.
 int group_occupancy(int* coop_per_sm, int* stage_per_sm, int* sms);
-int launch_group_step(const GroupArgs& a, const GroupLaunch& L, cudaStream_t st);
+int launch_group_step(const GroupArgs& a, const GroupLaunch& L, cudaStream_t st,
+                      const GroupTBLaunch* tb = nullptr);
+int launch_group_tb_sweeps(const GroupTBLaunch& tb, int launches, cudaStream_t st);
 int launch_group_sweeps_only(const GroupArgs& a, const GroupLaunch& L, cudaStream_t st);
 
 }  // namespace smk

@@ -65,6 +65,19 @@ int launch_sweep_tb(const SweepMaps* m, const Grid& g, bool in_is_a, float* Pout
                     int nhalf, int colour0, int zchunk, const float* wacc7, StepStatus* status,
                     int check, int group, float tol, int* pcur, int out_idx, int* kerr,
                     const int* group_base, cudaStream_t st);
+// Grouped blocked solve over many grids (depth 6, 2-row patches): one record per grid (its
+// tensor maps, buffers and tolerance), tiles of all grids in one launch.
+size_t group_tb_record_bytes();
+// Fill one record (rec: group_tb_record_bytes(), 64-byte aligned in the device copy); returns
+// the grid's tile count for `zchunk`-plane chunks.
+int group_tb_fill(void* rec, const SweepMaps* m, const Grid& g, float* P, float* P2, StepStatus* status, int* pcur,
+                  int* kerr, const float* wacc7, float tol, int zchunk);
+int launch_group_sweep_tb(const void* grids, const int* starts, int n, int total_tiles, bool in_a, int nhalf,
+                          int colour0, int zchunk, int check, int group, const int* group_base, cudaStream_t st);
+// Last node of a grouped solve's device-side loop body: counter += step; loop again while some
+// grid's solve is not done and counter < limit.
+void launch_group_tb_loop_next(const void* grids, int n, int* counter, int step, int limit,
+                               cudaGraphConditionalHandle handle, cudaStream_t st);
 // Last node of a device-side group loop's body: counter += step; loop again while the solve is
 // not done and counter < limit; *launches += launches_per_iter.
 void launch_group_loop_next(const StepStatus* status, int* counter, int step, int limit,

@@ -21,6 +21,7 @@
 
 #include "common.cuh"
 #include "group.h"
+#include "kernels.h"
 #include "stage_bodies.cuh"
 
 namespace smk {
@@ -236,7 +237,7 @@ __global__ void __launch_bounds__(GROUP_TILE) k_group_project(const GroupArgs a)
     unsigned long long target = 0;
     for (int j = tid; j < a.n; j += GROUP_TILE) gst[j] = 0;
 
-    if (!a.sweeps_only) {
+    if (!a.sweeps_only && (a.phases & GP_RHS)) {
         // this step's status words (zeroed by one CTA per grid), then b and the pressure start
         for (int j = (int)blockIdx.x; j < a.n; j += (int)gridDim.x) {
             unsigned* w = reinterpret_cast<unsigned*>(a.grids[j].status);
@@ -264,7 +265,8 @@ __global__ void __launch_bounds__(GROUP_TILE) k_group_project(const GroupArgs a)
 
     // the solve waves run one after another; inside a wave every grid runs its own colour
     // passes and tolerance rule, pass by pass in lockstep with the wave's other grids
-    for (int wave = 0; wave < a.nwaves; ++wave)
+    const int nwaves = (a.phases & GP_SOLVE) ? a.nwaves : 0;
+    for (int wave = 0; wave < nwaves; ++wave)
     for (int s = 0;; ++s) {
         // which grids sweep now, and which record a residual first (group starts)
         int act = 0, chk = 0;
@@ -353,19 +355,21 @@ __global__ void __launch_bounds__(GROUP_TILE) k_group_project(const GroupArgs a)
             }
         }
     }
-    if (a.sweeps_only) return;
+    if (a.sweeps_only || !(a.phases & GP_FINISH)) return;
 
+    // the pressure is the first buffer after the colour-pass solve (*pcur == 0), or where the
+    // blocked solve's last launch left it
     for_tiles(a, GS_PROJECT, nullptr, 0, [&](int j, int local) {
         const GroupGrid& d = a.grids[j];
         int rx, ry, rz;
         group_extent(GS_PROJECT, d, rx, ry, rz);
         const uint3 bid = tile_bid(local, rx, ry);
         if (d.kind == GK_F32)
-            body_gradient_subtract(d.g, (float*)d.u_now, (float*)d.v_now, (float*)d.w_now, d.P, nullptr, nullptr,
+            body_gradient_subtract(d.g, (float*)d.u_now, (float*)d.v_now, (float*)d.w_now, d.P, d.P2, d.pcur,
                                    d.flags, bid);
         else
             body_project_bf16(d.g, (__nv_bfloat16*)d.u_now, (__nv_bfloat16*)d.v_now, (__nv_bfloat16*)d.w_now,
-                              d.P, nullptr, nullptr, d.flags, d.pu, d.pv, d.pw, bid);
+                              d.P, d.P2, d.pcur, d.flags, d.pu, d.pv, d.pw, bid);
     });
 
     if (a.starts[GS_DIV * (a.n + 1) + a.n] > 0) {
@@ -452,14 +456,101 @@ int group_occupancy(int* coop_per_sm, int* stage_per_sm, int* sms) {
     return 0;
 }
 
-int launch_group_step(const GroupArgs& a, const GroupLaunch& L, cudaStream_t st) {
+// The blocked solve's launches for groups [g0, g1): group k covers sweeps [k G, (k+1) G) (the
+// last one may be partial), depth-6 launches, the first of each with the tolerance check.
+// Inside a loop body (group_base set) the group index is relative to *group_base; `nl` counts
+// launches so far (the input buffer alternates, starting from P).
+int issue_tb_groups(const GroupTBLaunch& tb, int g0, int g1, const int* group_base, int& nl, cudaStream_t st) {
+    constexpr int T = 6;
+    for (int grp = g0; grp < g1; ++grp) {
+        const int first = grp * tb.check_every;
+        const int end = first + tb.check_every < tb.max_sweeps ? first + tb.check_every : tb.max_sweeps;
+        for (int h = 2 * first; h < 2 * end; h += T) {
+            const int nh = 2 * end - h < T ? 2 * end - h : T;
+            const int rc = launch_group_sweep_tb(tb.grids, tb.starts, tb.n, tb.total, (nl & 1) == 0, nh, h & 1,
+                                                 tb.zchunk, h == 2 * first ? 1 : 0, grp, group_base, st);
+            if (rc) return rc;
+            ++nl;
+        }
+    }
+    return 0;
+}
+
+// The whole blocked solve: the full groups as a device-side WHILE loop when the stream is being
+// captured (the loop stops when every grid's tolerance rule is satisfied), then the groups
+// left (a partial last group), whose launches exit at entry for grids that are done.
+int launch_tb_solve(const GroupTBLaunch& tb, cudaStream_t st) {
+    constexpr int T = 6;
+    const int G = tb.check_every;
+    const int nlg = (2 * G + T - 1) / T;
+    const int U = (nlg % 2 == 0) ? 1 : 2;
+    const int full = tb.max_sweeps / G;
+    const int groups = (tb.max_sweeps + G - 1) / G;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    cudaError_t e = cudaStreamIsCapturing(st, &cs);
+    if (e != cudaSuccess) return (int)e;
+    const int loop_groups = (cs == cudaStreamCaptureStatusActive && tb.body) ? (full / U) * U : 0;
+    int nl = 0, done_groups = 0;
+    if (loop_groups > U) {
+        e = cudaMemsetAsync(tb.counter, 0, sizeof(int), st);
+        cudaGraph_t cg = nullptr;
+        const cudaGraphNode_t* deps = nullptr;
+        size_t ndeps = 0;
+        if (e == cudaSuccess) e = cudaStreamGetCaptureInfo(st, &cs, nullptr, &cg, &deps, nullptr, &ndeps);
+        cudaGraphConditionalHandle handle;
+        if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&handle, cg, 1, cudaGraphCondAssignDefault);
+        cudaGraphNodeParams np = {};
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = handle;
+        np.conditional.type = cudaGraphCondTypeWhile;
+        np.conditional.size = 1;
+        cudaGraphNode_t node;
+        if (e == cudaSuccess) e = cudaGraphAddNode(&node, cg, deps, nullptr, ndeps, &np);
+        if (e == cudaSuccess)
+            e = cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+        if (e == cudaSuccess)
+            e = cudaStreamBeginCaptureToGraph(tb.body, np.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                              cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return (int)e;
+        int rc = issue_tb_groups(tb, 0, U, tb.counter, nl, tb.body);
+        if (!rc) launch_group_tb_loop_next(tb.grids, tb.n, tb.counter, U, loop_groups, handle, tb.body);
+        cudaGraph_t bg = nullptr;
+        e = cudaStreamEndCapture(tb.body, &bg);
+        if (rc) return rc;
+        if (e != cudaSuccess) return (int)e;
+        nl = 0;  // U groups launch an even number of times: every iteration starts from P
+        done_groups = loop_groups;
+    }
+    return issue_tb_groups(tb, done_groups, groups, nullptr, nl, st);
+}
+
+int launch_group_step(const GroupArgs& a, const GroupLaunch& L, cudaStream_t st, const GroupTBLaunch* tb) {
     int rc = ensure_occupancy();
     if (!rc) rc = launch_grid_stride((const void*)k_group_objects, L.total[GS_OBJECTS], g_occ[1], a, st);
     if (!rc) rc = launch_grid_stride((const void*)k_group_forcing, L.total[GS_FORCE], g_occ[2], a, st);
-    if (!rc) rc = launch_project(a, L, st);
+    if (tb == nullptr) {
+        if (!rc) rc = launch_project(a, L, st);
+    } else {
+        GroupArgs r = a;
+        r.phases = GP_RHS;
+        if (!rc) rc = launch_project(r, L, st);
+        if (!rc) rc = launch_tb_solve(*tb, st);
+        r.phases = GP_FINISH;
+        if (!rc) rc = launch_project(r, L, st);
+    }
     if (!rc) rc = launch_grid_stride((const void*)k_group_adv_vel, L.total[GS_ADV_VEL], g_occ[3], a, st);
     if (!rc) rc = launch_grid_stride((const void*)k_group_adv_rho, L.total[GS_ADV_RHO], g_occ[4], a, st);
     return rc;
+}
+
+int launch_group_tb_sweeps(const GroupTBLaunch& tb, int launches, cudaStream_t st) {
+    // tuning: `launches` depth-6 launches without tolerance checks, each reading P and writing P2
+    for (int k = 0; k < launches; ++k) {
+        const int rc = launch_group_sweep_tb(tb.grids, tb.starts, tb.n, tb.total, true, 6, 0, tb.zchunk, 0, 0,
+                                             nullptr, st);
+        if (rc) return rc;
+    }
+    return 0;
 }
 
 int launch_group_sweeps_only(const GroupArgs& a, const GroupLaunch& L, cudaStream_t st) {

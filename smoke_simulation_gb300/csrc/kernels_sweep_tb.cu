@@ -72,6 +72,8 @@ struct TBGeom {
 
 struct WAcc8 { float w[8]; };
 
+constexpr int GROUP_TB_DEPTH = 6;  // colour passes per launch of the grouped blocked solve
+
 struct TBMaps {
     CUtensorMap pin;  // P_in
     CUtensorMap b;
@@ -151,11 +153,21 @@ __device__ __forceinline__ unsigned resid_bits(float pc, float bc, float2 c, boo
 // flag word -> table index: bits 0-5 the six fluid-neighbour bits, bit 6 "projectable"
 __device__ __forceinline__ unsigned fidx(unsigned f, int k) { return (f >> (8 * k + 1)) & 0x7fu; }
 
-template <int T, int PY>
-__global__ void __launch_bounds__(TBGeom<PY>::THREADS, 1)
-k_sweep_tb(const __grid_constant__ TBMaps maps, Grid g, float* __restrict__ Pout, int nhalf,
-           int colour0, int zchunk, WAcc8 wa, StepStatus* status, int check, int group, float tol,
-           int* __restrict__ pcur, int out_idx, int* __restrict__ kerr, const int* __restrict__ group_base) {
+// Make the tensor map at `map` (global memory, written before the launch) current for the
+// TMA unit's tensor-map reads from this CTA.
+__device__ __forceinline__ void tensormap_acquire(const CUtensorMap* map) {
+    asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(reinterpret_cast<uint64_t>(map))
+                 : "memory");
+}
+
+// One tile (bx, by, bz) of a blocked launch: the CTA's whole job.  `group` is absolute.
+// GLOBAL_MAPS: the tensor maps are in global memory (grouped launches), not kernel parameters.
+template <int T, int PY, bool GLOBAL_MAPS = false>
+__device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, float* __restrict__ Pout,
+                                           int nhalf, int colour0, int zchunk, const WAcc8& wa,
+                                           StepStatus* status, int check, int group, float tol,
+                                           int* __restrict__ pcur, int out_idx, int* __restrict__ kerr,
+                                           int bx, int by, int bz) {
     using G = TBGeom<PY>;
     constexpr int TY = G::TY, ROWS = G::ROWS, PROW = G::PROW, STAGE_BYTES = G::STAGE_BYTES,
                   STAGE_P = G::STAGE_P;
@@ -176,13 +188,11 @@ k_sweep_tb(const __grid_constant__ TBMaps maps, Grid g, float* __restrict__ Pout
     __shared__ __align__(8) uint64_t mbar[TB_S];
     __shared__ float2 coef[128];
 
-    // inside a graph's device-side group loop the group index is relative to the loop counter
-    if (group_base != nullptr) group += *group_base;
+    const bool first_tile = (bx | by | bz) == 0;
     if (status != nullptr) {
         if (*(volatile int*)&status->done) return;
         if (check && group > 0 && __uint_as_float(status->rmax_bits[group - 1]) <= tol) {
-            if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 &&
-                threadIdx.y == 0) {
+            if (first_tile && threadIdx.x == 0 && threadIdx.y == 0) {
                 status->done = 1;
                 status->done_group = group;
             }
@@ -201,18 +211,17 @@ k_sweep_tb(const __grid_constant__ TBMaps maps, Grid g, float* __restrict__ Pout
         const int lane = i % TB_TX, edge = (i / TB_TX) % 2, set = i / (2 * TB_TX);
         pub[set * PROW + (edge ? (TY + 1) * TB_TX : 0) + lane] = 0.0f;
     }
-    if (pcur != nullptr && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && leader)
-        *pcur = out_idx;
+    if (pcur != nullptr && first_tile && leader) *pcur = out_idx;
 
-    const int X0 = (int)blockIdx.x * IX - T;  // even; first tile column
-    const int Y0 = (int)blockIdx.y * IY - T;  // even; first tile row
+    const int X0 = bx * IX - T;  // even; first tile column
+    const int Y0 = by * IY - T;  // even; first tile row
     const int xf = X0 - (X0 & 3);             // 16-byte aligned float box start
     const int xb = X0 - (X0 & 15);            // 16-byte aligned flag box start
     const int of = X0 - xf + 2 * tx;          // this thread's column in the float box
     const int ob = X0 - xb + 2 * tx;          // ... in the flag box
     const int x0 = X0 + 2 * tx;
     const int y0 = Y0 + PY * ty;
-    const int za = (int)blockIdx.z * zchunk;
+    const int za = bz * zchunk;
     const int zb = min(za + zchunk, g.nz);
     const bool inx = (2 * tx >= T) && (2 * tx < T + IX) && x0 < g.nx;
     bool in[PY];  // row r of the patch is an interior row of the tile inside the grid
@@ -227,6 +236,11 @@ k_sweep_tb(const __grid_constant__ TBMaps maps, Grid g, float* __restrict__ Pout
     const int qfinal = qbeg + nouter * R - 1;  // last iteration executed
 
     if (leader) {
+        if (GLOBAL_MAPS) {
+            tensormap_acquire(&maps.pin);
+            tensormap_acquire(&maps.b);
+            tensormap_acquire(&maps.f);
+        }
         for (int s = 0; s < TB_S; ++s) mbar_init(smem_u32(&mbar[s]), 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -425,6 +439,80 @@ k_sweep_tb(const __grid_constant__ TBMaps maps, Grid g, float* __restrict__ Pout
     if (check) block_max_to(rmax, &status->rmax_bits[group]);
 }
 
+template <int T, int PY>
+__global__ void __launch_bounds__(TBGeom<PY>::THREADS, 1)
+k_sweep_tb(const __grid_constant__ TBMaps maps, Grid g, float* __restrict__ Pout, int nhalf,
+           int colour0, int zchunk, const __grid_constant__ WAcc8 wa, StepStatus* status, int check, int group,
+           float tol, int* __restrict__ pcur, int out_idx, int* __restrict__ kerr,
+           const int* __restrict__ group_base) {
+    // inside a graph's device-side group loop the group index is relative to the loop counter
+    if (group_base != nullptr) group += *group_base;
+    sweep_tile<T, PY>(maps, g, Pout, nhalf, colour0, zchunk, wa, status, check, group, tol, pcur, out_idx,
+                      kerr, (int)blockIdx.x, (int)blockIdx.y, (int)blockIdx.z);
+}
+
+// ---- grouped form: one blocked launch over the tiles of every grid of a batch ---------------
+
+// One grid of a grouped blocked launch.  The tensor maps live in global memory (64-byte
+// aligned records), one set per input buffer: maps[0] reads P, maps[1] reads P2.
+struct GroupTBGrid {
+    TBMaps maps[2];
+    Grid g;
+    float* P;
+    float* P2;
+    StepStatus* status;
+    int* pcur;
+    int* kerr;
+    WAcc8 wa;
+    float tol;
+    int tiles_x, tiles_y, zchunks;
+};
+
+// CTA b of the launch takes tile b of the flat index space (the tiles of one grid are
+// contiguous; `starts` holds n + 1 prefix sums).  in_a: read P and write P2, else the reverse.
+template <int T>
+__global__ void __launch_bounds__(TBGeom<2>::THREADS, 1)
+k_group_sweep_tb(const GroupTBGrid* __restrict__ grids, const int* __restrict__ starts, int n, int in_a,
+                 int nhalf, int colour0, int zchunk, int check, int group, const int* __restrict__ group_base) {
+    const int t = (int)blockIdx.x;
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (starts[mid] <= t) lo = mid;
+        else hi = mid - 1;
+    }
+    const GroupTBGrid& d = grids[lo];
+    const int local = t - starts[lo];
+    const int tx = d.tiles_x, per = tx * d.tiles_y;
+    const int bz = local / per, r = local - bz * per, by = r / tx, bx = r - by * tx;
+    if (group_base != nullptr) group += *group_base;
+    // the record's scalars in registers; the tensor maps and omega/acc stay in global memory
+    const Grid g = d.g;
+    float* const Pout = in_a ? d.P2 : d.P;
+    StepStatus* const status = d.status;
+    int* const pcur = d.pcur;
+    int* const kerr = d.kerr;
+    const float tol = d.tol;
+    sweep_tile<T, 2, true>(d.maps[in_a ? 0 : 1], g, Pout, nhalf, colour0, zchunk, d.wa, status, check, group, tol,
+                           pcur, in_a ? 1 : 0, kerr, bx, by, bz);
+}
+
+// End of one iteration of a grouped step's device-side loop over tolerance groups: advance
+// the group counter; loop again while some grid's solve is not done and full groups remain.
+// One block.
+__global__ void k_group_tb_loop_next(const GroupTBGrid* __restrict__ grids, int n, int* counter, int step,
+                                     int limit, cudaGraphConditionalHandle handle) {
+    int open = 0;
+    for (int j = (int)threadIdx.x; j < n; j += (int)blockDim.x)
+        open |= *(volatile const int*)&grids[j].status->done == 0;
+    open = __syncthreads_or(open);
+    if (threadIdx.x == 0) {
+        const int c = *counter + step;
+        *counter = c;
+        cudaGraphSetConditional(handle, (open && c < limit) ? 1u : 0u);
+    }
+}
+
 // ---- host side --------------------------------------------------------------------------------
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
@@ -511,7 +599,9 @@ int sweep_tb_shape_supported(int T, int rows) {
 }
 
 int prepare_sweep_kernels() {
-    return configure_tb<2, 2>() | configure_tb<4, 2>() | configure_tb<6, 2>() | configure_tb<4, 4>();
+    const int grouped = cudaFuncSetAttribute(k_group_sweep_tb<GROUP_TB_DEPTH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)tb_smem_bytes<GROUP_TB_DEPTH, 2>()) == cudaSuccess ? 0 : -1;
+    return configure_tb<2, 2>() | configure_tb<4, 2>() | configure_tb<6, 2>() | configure_tb<4, 4>() | grouped;
 }
 
 // Tensor maps for the sweep's TMA loads: P_a, P_b, b (float) and flags (u8), for the box
@@ -554,6 +644,49 @@ int launch_sweep_tb(const SweepMaps* m, const Grid& g, bool in_is_a, float* Pout
         default: return launch_tb<6, 2>(SMK_TB_ARGS);
     }
 #undef SMK_TB_ARGS
+}
+
+size_t group_tb_record_bytes() { return sizeof(GroupTBGrid); }
+
+int group_tb_fill(void* rec, const SweepMaps* m, const Grid& g, float* P, float* P2, StepStatus* status, int* pcur,
+                  int* kerr, const float* wacc7, float tol, int zchunk) {
+    constexpr int T = GROUP_TB_DEPTH;
+    constexpr int IX = 2 * TB_TX - 2 * T, IY = TBGeom<2>::ROWS - 2 * T;
+    GroupTBGrid d;
+    memset(&d, 0, sizeof(d));
+    d.maps[0].pin = m->pa[0];
+    d.maps[1].pin = m->pb[0];
+    d.maps[0].b = d.maps[1].b = m->b[0];
+    d.maps[0].f = d.maps[1].f = m->f[0];
+    d.g = g;
+    d.P = P;
+    d.P2 = P2;
+    d.status = status;
+    d.pcur = pcur;
+    d.kerr = kerr;
+    for (int k = 0; k < 7; ++k) d.wa.w[k] = wacc7[k];
+    d.wa.w[7] = 0.0f;
+    d.tol = tol;
+    d.tiles_x = (g.nx + IX - 1) / IX;
+    d.tiles_y = (g.ny + IY - 1) / IY;
+    d.zchunks = (g.nz + zchunk - 1) / zchunk;
+    memcpy(rec, &d, sizeof(d));
+    return d.tiles_x * d.tiles_y * d.zchunks;
+}
+
+int launch_group_sweep_tb(const void* grids, const int* starts, int n, int total_tiles, bool in_a, int nhalf,
+                          int colour0, int zchunk, int check, int group, const int* group_base, cudaStream_t st) {
+    if (total_tiles <= 0) return 0;
+    k_group_sweep_tb<GROUP_TB_DEPTH><<<(unsigned)total_tiles, dim3(TB_TX, TBGeom<2>::TY),
+                                       tb_smem_bytes<GROUP_TB_DEPTH, 2>(), st>>>(
+        static_cast<const GroupTBGrid*>(grids), starts, n, in_a ? 1 : 0, nhalf, colour0, zchunk, check, group,
+        group_base);
+    return (int)cudaGetLastError();
+}
+
+void launch_group_tb_loop_next(const void* grids, int n, int* counter, int step, int limit,
+                               cudaGraphConditionalHandle handle, cudaStream_t st) {
+    k_group_tb_loop_next<<<1, 256, 0, st>>>(static_cast<const GroupTBGrid*>(grids), n, counter, step, limit, handle);
 }
 
 void launch_group_loop_next(const StepStatus* status, int* counter, int step, int limit,

@@ -211,3 +211,84 @@ def test_grouped_schedules_do_not_change_results(gpu, sched):
     batch.close()
     for s in sims + ref:
         s.close()
+
+
+def _blocked_scenes(count=7, seed=31, lo=8, hi=70):
+    scs = S.config_batched(count=count, steps=6, seed=seed, lo=lo, hi=hi, scheme=1, iterations=40)
+    for i, sc in enumerate(scs):
+        sc.u0, sc.v0, sc.w0 = S.noise_velocity(sc.face_shape, 0.3, seed=300 + i)
+        sc.tol, sc.check_every = 2e-4, 6  # one group size and sweep cap for every member
+        sc.warm_start = i % 2
+    return scs
+
+
+@pytest.mark.parametrize("zchunk,graphs,storage", [(17, True, smk.STORAGE_F32), (5, False, smk.STORAGE_F32),
+                                                   (64, True, smk.STORAGE_BF16_VEL)])
+def test_grouped_blocked_solve_equals_alone(gpu, zchunk, graphs, storage):
+    """The grouped form with the blocked solve (depth-6 launches over every member's tiles, the
+    tolerance groups as a device-side loop when captured, direct launches otherwise) is
+    bit-identical to each grid stepped alone, sweep counts and residuals included, with warm
+    and cold pressure starts, BF16 velocity storage and a step where the members' ping-pong
+    parities differ."""
+    scs = _blocked_scenes()
+    batch_sims = [smk.from_scene(sc, report_div=1, storage=storage) for sc in scs]
+    alone = [smk.from_scene(sc, report_div=1, storage=storage) for sc in scs]
+    for s in alone:
+        s.set_graphs(False)
+        s.set_sweep_kernel(0, 1)
+    batch = smk.Batch(batch_sims, mode=smk.BATCH_GROUPED)
+    batch.set_blocked(zchunk)
+    assert batch.blocked() == zchunk
+    if not graphs:
+        batch.set_graphs(False)
+    for k in range(6):
+        if k == 3:
+            batch_sims[0].step(0.05)
+            alone[0].step(0.05)
+        batch.step(0.05)
+        for s in alone:
+            s.step(0.05)
+    assert batch.info()[0] == smk.BATCH_GROUPED
+    for i in range(len(scs)):
+        assert H.first_mismatch(batch_sims[i].read_state(), alone[i].read_state()) == "", i
+        sa, sb = batch_sims[i].stats(), alone[i].stats()
+        assert (sa.sweeps, sa.converged, sa.div_max, sa.resid_max) == (sb.sweeps, sb.converged, sb.div_max,
+                                                                       sb.resid_max), i
+    batch.close()
+    for s in batch_sims + alone:
+        s.close()
+
+
+def test_grouped_blocked_needs_shared_groups(gpu):
+    """Members with different tolerance group sizes fall back to the colour-pass solve (same
+    results); the autotuner may pick the blocked solve only when every member can use it."""
+    scs = _grouped_scenes(count=5, seed=37)  # mixed group sizes and tolerances
+    ref = [smk.from_scene(sc, report_div=1) for sc in scs]
+    sims = [smk.from_scene(sc, report_div=1) for sc in scs]
+    batch = smk.Batch(sims, mode=smk.BATCH_GROUPED)
+    batch.set_blocked(17)
+    for _ in range(3):
+        batch.step(0.05)
+        for s in ref:
+            s.step(0.05)
+    for i in range(len(scs)):
+        assert H.first_mismatch(sims[i].read_state(), ref[i].read_state()) == "", i
+    batch.close()
+    scs2 = _blocked_scenes(count=5, seed=41, lo=20, hi=60)
+    sims2 = [smk.from_scene(sc, report_div=1) for sc in scs2]
+    ref2 = [smk.from_scene(sc, report_div=1) for sc in scs2]
+    b2 = smk.Batch(sims2, mode=smk.BATCH_GROUPED)
+    b2.step(0.05)
+    for s in ref2:
+        s.step(0.05)
+    c, us = b2.autotune()
+    assert us > 0 and (c == 0) == (b2.blocked() > 0)
+    for _ in range(3):
+        b2.step(0.05)
+        for s in ref2:
+            s.step(0.05)
+    for i in range(len(scs2)):
+        assert H.first_mismatch(sims2[i].read_state(), ref2[i].read_state()) == "", i
+    b2.close()
+    for s in sims + ref + sims2 + ref2:
+        s.close()
