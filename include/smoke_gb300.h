@@ -284,6 +284,9 @@ int smk_server_set_mode(smk_server* server, int mode);
 /* smk_set_graph_loops for the requests admitted from now on (default off: with many request
  * graphs in flight at once, the loop's per-iteration cost exceeds the launches it saves). */
 int smk_server_set_graph_loops(smk_server* server, int enable);
+/* GROUPED form: the blocked solve for the ticks whose requests share a tolerance group size and
+ * sweep cap (smk_batch_set_blocked; 0 = cooperative colour passes, the default). */
+int smk_server_set_blocked(smk_server* server, int zchunk);
 int smk_server_submit(smk_server* server, const smk_request_desc* request, int* id);
 int smk_server_tick(smk_server* server, int* n_active, int* n_queued);
 int smk_server_request_status(smk_server* server, int id, int* state, int* steps_done, int* error);

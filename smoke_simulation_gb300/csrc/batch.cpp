@@ -43,6 +43,7 @@ struct smk_batch {
     std::vector<cudaEvent_t> join;
     cudaStream_t origin = nullptr;
     cudaStream_t body = nullptr;  // captures the grouped blocked solve's loop body
+    unsigned long long* dev_launches = nullptr;  // kernels run inside device-side loops
     cudaEvent_t fork = nullptr;
     cudaGraphExec_t exec = nullptr;
     std::string sig;
@@ -414,13 +415,14 @@ int grouped_step(smk_batch* b, const float* dts, float dt_all, cudaStream_t st) 
         slot->blocked = t.blocked;
         if (t.blocked) {
             slot->tb = tb_launch(t, slot->dev, n, b->body);
-            slot->kernels += 1;  // the projection's second cooperative launch (the blocked solve's
-                                 // launches, some inside a device-side loop, are not counted)
+            slot->tb.launches = b->dev_launches;
+            slot->kernels += 1;  // the projection's second cooperative launch
         }
         if (b->use_graphs && b->graphs_ok) {
             cudaGraph_t graph = nullptr;
             SMK_CUDA(cudaStreamBeginCapture(b->origin, cudaStreamCaptureModeThreadLocal));
             const int lrc = launch_group_step(slot->args, slot->L, b->origin, slot->blocked ? &slot->tb : nullptr);
+            if (lrc == 0 && slot->blocked) slot->kernels += slot->tb.issued;  // outside the loop
             const cudaError_t ee = cudaStreamEndCapture(b->origin, &graph);
             cudaError_t ie = cudaErrorUnknown;
             if (lrc == 0 && ee == cudaSuccess) ie = cudaGraphInstantiate(&slot->exec, graph, 0);
@@ -440,6 +442,7 @@ int grouped_step(smk_batch* b, const float* dts, float dt_all, cudaStream_t st) 
     } else {
         const int lrc = launch_group_step(slot->args, slot->L, st, slot->blocked ? &slot->tb : nullptr);
         if (lrc) return smk_fail(SMK_ERR_CUDA, std::string("grouped step: ") + cudaGetErrorString((cudaError_t)lrc));
+        if (slot->blocked) b->launches += slot->tb.issued;  // direct: every group issued
     }
     b->launches += slot->kernels;
     for (smk_sim* s : b->sims) after_step(s);
@@ -628,7 +631,7 @@ int group_runner_step(GroupRunner* r, smk_sim* const* sims, const float* dts, in
     SMK_CUDA(cudaEventRecord(sl.done, st));
     sl.used = true;
     for (int i = 0; i < n; ++i) after_step(sims[i]);
-    if (kernels) *kernels = k + nk;
+    if (kernels) *kernels = k + nk + (t.blocked ? 1 + tb.issued : 0);
     return SMK_OK;
 }
 
@@ -652,11 +655,14 @@ int smk_batch_create(int count, smk_sim* const* sims, smk_batch** out) {
         if (b->origin) cudaStreamDestroy(b->origin);
         if (b->body) cudaStreamDestroy(b->body);
         if (b->fork) cudaEventDestroy(b->fork);
+        if (b->dev_launches) cudaFree(b->dev_launches);
         delete b;
     };
     if (cudaStreamCreateWithFlags(&b->origin, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&b->body, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess) {
+        cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaMalloc((void**)&b->dev_launches, sizeof(unsigned long long)) != cudaSuccess ||
+        cudaMemset(b->dev_launches, 0, sizeof(unsigned long long)) != cudaSuccess) {
         cleanup();
         return smk_fail(SMK_ERR_CUDA, "batch stream/event creation failed");
     }
@@ -686,6 +692,7 @@ int smk_batch_destroy(smk_batch* b) {
     cudaStreamDestroy(b->origin);
     cudaStreamDestroy(b->body);
     cudaEventDestroy(b->fork);
+    cudaFree(b->dev_launches);
     delete b;
     return SMK_OK;
 }
@@ -710,7 +717,15 @@ int smk_batch_set_graphs(smk_batch* b, int enable) {
 int smk_batch_get_info(const smk_batch* b, int* last_mode, long long* launches) {
     if (!b) return smk_fail(SMK_ERR_INVALID, "batch is null");
     if (last_mode) *last_mode = b->last_mode;
-    if (launches) *launches = b->launches;
+    if (launches) {
+        // plus the kernels run inside device-side loops (counted on the device)
+        unsigned long long dev = 0;
+        if (b->dev_launches) {
+            DeviceGuard dg(b->device);
+            SMK_CUDA(cudaMemcpy(&dev, b->dev_launches, sizeof(dev), cudaMemcpyDeviceToHost));
+        }
+        *launches = b->launches + (long long)dev;
+    }
     return SMK_OK;
 }
 

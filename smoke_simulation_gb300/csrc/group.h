@@ -112,6 +112,8 @@ struct GroupTBLaunch {
     int max_sweeps;
     int* counter;        // device: the loop's group counter
     cudaStream_t body;   // stream used to capture the loop body
+    unsigned long long* launches;  // device (may be NULL): kernels run inside the loop
+    int issued;          // set by launch_group_step: kernels the host issued for the solve
 };
 
 __host__ __device__ inline int group_div_up(int a, int b) { return (a + b - 1) / b; }
@@ -185,7 +187,7 @@ struct GroupLaunch {
 // Host launchers (kernels_group.cu).  Return 0 or a cudaError_t value.
 int group_occupancy(int* coop_per_sm, int* stage_per_sm, int* sms);
 int launch_group_step(const GroupArgs& a, const GroupLaunch& L, cudaStream_t st,
-                      const GroupTBLaunch* tb = nullptr);
+                      GroupTBLaunch* tb = nullptr);
 int launch_group_tb_sweeps(const GroupTBLaunch& tb, int launches, cudaStream_t st);
 int launch_group_sweeps_only(const GroupArgs& a, const GroupLaunch& L, cudaStream_t st);
 

@@ -75,8 +75,10 @@ int group_tb_fill(void* rec, const SweepMaps* m, const Grid& g, float* P, float*
 int launch_group_sweep_tb(const void* grids, const int* starts, int n, int total_tiles, bool in_a, int nhalf,
                           int colour0, int zchunk, int check, int group, const int* group_base, cudaStream_t st);
 // Last node of a grouped solve's device-side loop body: counter += step; loop again while some
-// grid's solve is not done and counter < limit.
+// grid's solve is not done and counter < limit; *launches += launches_per_iter (launches may be
+// NULL).
 void launch_group_tb_loop_next(const void* grids, int n, int* counter, int step, int limit,
+                               unsigned long long* launches, int launches_per_iter,
                                cudaGraphConditionalHandle handle, cudaStream_t st);
 // Last node of a device-side group loop's body: counter += step; loop again while the solve is
 // not done and counter < limit; *launches += launches_per_iter.

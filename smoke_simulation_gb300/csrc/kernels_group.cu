@@ -479,7 +479,7 @@ int issue_tb_groups(const GroupTBLaunch& tb, int g0, int g1, const int* group_ba
 // The whole blocked solve: the full groups as a device-side WHILE loop when the stream is being
 // captured (the loop stops when every grid's tolerance rule is satisfied), then the groups
 // left (a partial last group), whose launches exit at entry for grids that are done.
-int launch_tb_solve(const GroupTBLaunch& tb, cudaStream_t st) {
+int launch_tb_solve(GroupTBLaunch& tb, cudaStream_t st) {
     constexpr int T = 6;
     const int G = tb.check_every;
     const int nlg = (2 * G + T - 1) / T;
@@ -513,7 +513,9 @@ int launch_tb_solve(const GroupTBLaunch& tb, cudaStream_t st) {
                                               cudaStreamCaptureModeThreadLocal);
         if (e != cudaSuccess) return (int)e;
         int rc = issue_tb_groups(tb, 0, U, tb.counter, nl, tb.body);
-        if (!rc) launch_group_tb_loop_next(tb.grids, tb.n, tb.counter, U, loop_groups, handle, tb.body);
+        if (!rc)
+            launch_group_tb_loop_next(tb.grids, tb.n, tb.counter, U, loop_groups, tb.launches, nl + 1, handle,
+                                      tb.body);
         cudaGraph_t bg = nullptr;
         e = cudaStreamEndCapture(tb.body, &bg);
         if (rc) return rc;
@@ -521,10 +523,12 @@ int launch_tb_solve(const GroupTBLaunch& tb, cudaStream_t st) {
         nl = 0;  // U groups launch an even number of times: every iteration starts from P
         done_groups = loop_groups;
     }
-    return issue_tb_groups(tb, done_groups, groups, nullptr, nl, st);
+    const int rc = issue_tb_groups(tb, done_groups, groups, nullptr, nl, st);
+    tb.issued = nl;
+    return rc;
 }
 
-int launch_group_step(const GroupArgs& a, const GroupLaunch& L, cudaStream_t st, const GroupTBLaunch* tb) {
+int launch_group_step(const GroupArgs& a, const GroupLaunch& L, cudaStream_t st, GroupTBLaunch* tb) {
     int rc = ensure_occupancy();
     if (!rc) rc = launch_grid_stride((const void*)k_group_objects, L.total[GS_OBJECTS], g_occ[1], a, st);
     if (!rc) rc = launch_grid_stride((const void*)k_group_forcing, L.total[GS_FORCE], g_occ[2], a, st);

@@ -501,7 +501,8 @@ k_group_sweep_tb(const GroupTBGrid* __restrict__ grids, const int* __restrict__ 
 // the group counter; loop again while some grid's solve is not done and full groups remain.
 // One block.
 __global__ void k_group_tb_loop_next(const GroupTBGrid* __restrict__ grids, int n, int* counter, int step,
-                                     int limit, cudaGraphConditionalHandle handle) {
+                                     int limit, unsigned long long* launches, int launches_per_iter,
+                                     cudaGraphConditionalHandle handle) {
     int open = 0;
     for (int j = (int)threadIdx.x; j < n; j += (int)blockDim.x)
         open |= *(volatile const int*)&grids[j].status->done == 0;
@@ -509,6 +510,7 @@ __global__ void k_group_tb_loop_next(const GroupTBGrid* __restrict__ grids, int 
     if (threadIdx.x == 0) {
         const int c = *counter + step;
         *counter = c;
+        if (launches != nullptr) *launches += (unsigned long long)launches_per_iter;
         cudaGraphSetConditional(handle, (open && c < limit) ? 1u : 0u);
     }
 }
@@ -685,8 +687,10 @@ int launch_group_sweep_tb(const void* grids, const int* starts, int n, int total
 }
 
 void launch_group_tb_loop_next(const void* grids, int n, int* counter, int step, int limit,
+                               unsigned long long* launches, int launches_per_iter,
                                cudaGraphConditionalHandle handle, cudaStream_t st) {
-    k_group_tb_loop_next<<<1, 256, 0, st>>>(static_cast<const GroupTBGrid*>(grids), n, counter, step, limit, handle);
+    k_group_tb_loop_next<<<1, 256, 0, st>>>(static_cast<const GroupTBGrid*>(grids), n, counter, step, limit,
+                                            launches, launches_per_iter, handle);
 }
 
 void launch_group_loop_next(const StepStatus* status, int* counter, int step, int limit,

@@ -104,7 +104,7 @@ struct smk_server {
     bool started = false;  // the form is fixed once a request was admitted
     cudaStream_t stream = nullptr;
     GroupRunner* runner = nullptr;
-    smk::GroupSchedule sched{0, 4, 0};
+    smk::GroupSchedule sched{0, 4, 0, 0};
     TickRec ticks[2];
     int tick_next = 0;
 };
@@ -200,6 +200,13 @@ int smk_server_cancel(smk_server* s, int id) {
 int smk_server_set_graph_loops(smk_server* s, int enable) {
     if (!s) return sfail(SMK_ERR_INVALID, "server is null");
     s->graph_loops = enable != 0;
+    return SMK_OK;
+}
+
+int smk_server_set_blocked(smk_server* s, int zchunk) {
+    if (!s) return sfail(SMK_ERR_INVALID, "server is null");
+    if (zchunk < 0) return sfail(SMK_ERR_INVALID, "zchunk must be >= 0");
+    s->sched.blocked_zchunk = zchunk;
     return SMK_OK;
 }
 

@@ -61,6 +61,7 @@ def _bind():
             ("smk_server_set_mode", i, [vp, i]),
             ("smk_server_cancel", i, [vp, i]),
             ("smk_server_set_graph_loops", i, [vp, i]),
+            ("smk_server_set_blocked", i, [vp, i]),
             ("smk_server_last_error", C.c_char_p, [])):
         fn = getattr(L, name)
         fn.restype = res
@@ -94,6 +95,10 @@ class Server:
     def set_graph_loops(self, enable: bool):
         """Device-side group loops in the requests' step graphs (default off)."""
         _srv_check(_bind().smk_server_set_graph_loops(self.h, 1 if enable else 0))
+
+    def set_blocked(self, zchunk: int):
+        """GROUPED form: blocked solve with z-chunks of `zchunk` planes (0: colour passes)."""
+        _srv_check(_bind().smk_server_set_blocked(self.h, int(zchunk)))
 
     def submit(self, scene, steps: Optional[int] = None, params: Optional[Params] = None,
                keep_output: bool = True, out_device=None, **param_overrides) -> int:
