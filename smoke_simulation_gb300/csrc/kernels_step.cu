@@ -17,6 +17,7 @@ namespace smk {
 namespace {
 
 constexpr int BX = SB_BX, BY = SB_BY;
+constexpr int ADV_ZC = 4;  // z planes per advection block
 
 inline dim3 grid3(int rx, int ry, int rz) {
     return dim3((unsigned)((rx + BX - 1) / BX), (unsigned)((ry + BY - 1) / BY), (unsigned)rz);
@@ -142,21 +143,32 @@ __global__ void k_project_velocity(Grid g, float* __restrict__ u, float* __restr
 }
 
 // ---- a: velocityAdvectionU/V/W (:527-615) and advectSmoke (:617-638) ------------------------
-// The advection kernels are latency-bound gathers: 32 registers keep 8 blocks (64 warps) per SM.
+// The advection kernels are latency-bound gathers: the register caps keep 6 (velocity, 40
+// registers) and 8 (density, 32) blocks of 8 warps per SM.  Each block walks ADV_ZC consecutive
+// planes in ascending z: the planes a cell's averages and samples read overlap the next
+// cell's and stay in L1 between them (3% faster than one plane per block at 256^3).
 template <typename Ti, typename To>
-__global__ void __launch_bounds__(BX * BY, 8) k_advect_velocity(Grid g, const Ti* __restrict__ u0, const Ti* __restrict__ v0,
+__global__ void __launch_bounds__(BX * BY, 6) k_advect_velocity(Grid g, const Ti* __restrict__ u0, const Ti* __restrict__ v0,
                                   const Ti* __restrict__ w0, To* __restrict__ u1,
                                   To* __restrict__ v1, To* __restrict__ w1,
-                                  const uint8_t* __restrict__ flags, float dt) {
-    body_advect_velocity(g, u0, v0, w0, u1, v1, w1, flags, dt, blockIdx);
+                                  const uint8_t* __restrict__ flags, float dt, int rz) {
+    for (int k = 0; k < ADV_ZC; ++k) {
+        const int zz = (int)blockIdx.z * ADV_ZC + k;
+        if (zz >= rz) break;
+        body_advect_velocity(g, u0, v0, w0, u1, v1, w1, flags, dt, make_uint3(blockIdx.x, blockIdx.y, (unsigned)zz));
+    }
 }
 
 template <typename T, typename Tv>
 __global__ void __launch_bounds__(BX * BY, 8) k_advect_density(Grid g, const T* __restrict__ r0, T* __restrict__ r1,
                                  const Tv* __restrict__ u, const Tv* __restrict__ v,
                                  const Tv* __restrict__ w, const uint8_t* __restrict__ flags,
-                                 float dt) {
-    body_advect_density(g, r0, r1, u, v, w, flags, dt, blockIdx);
+                                 float dt, int rz) {
+    for (int k = 0; k < ADV_ZC; ++k) {
+        const int zz = (int)blockIdx.z * ADV_ZC + k;
+        if (zz >= rz) break;
+        body_advect_density(g, r0, r1, u, v, w, flags, dt, make_uint3(blockIdx.x, blockIdx.y, (unsigned)zz));
+    }
 }
 
 __global__ void k_project_bf16(Grid g, __nv_bfloat16* __restrict__ u, __nv_bfloat16* __restrict__ v,
@@ -293,8 +305,8 @@ void launch_advect_velocity(const Grid& g, const Ti* u0, const Ti* v0, const Ti*
                             To* u1, To* v1, To* w1, const uint8_t* flags, float dt,
                             cudaStream_t st) {
     if (g.nx < 2 || g.ny < 2 || g.nz < 2) return;
-    k_advect_velocity<<<grid3(g.nx - 1, g.ny - 1, g.nz - 1), dim3(BX, BY), 0, st>>>(
-        g, u0, v0, w0, u1, v1, w1, flags, dt);
+    k_advect_velocity<<<grid3(g.nx - 1, g.ny - 1, (g.nz - 1 + ADV_ZC - 1) / ADV_ZC), dim3(BX, BY), 0, st>>>(
+        g, u0, v0, w0, u1, v1, w1, flags, dt, g.nz - 1);
 }
 
 template <typename T, typename Tv>
@@ -302,8 +314,8 @@ void launch_advect_density(const Grid& g, const T* r0, T* r1, const Tv* u1,
                            const Tv* v1, const Tv* w1, const uint8_t* flags, float dt,
                            cudaStream_t st) {
     if (g.nx < 3 || g.ny < 3 || g.nz < 3) return;
-    k_advect_density<<<grid3(g.nx - 2, g.ny - 2, g.nz - 2), dim3(BX, BY), 0, st>>>(g, r0, r1, u1, v1,
-                                                                                   w1, flags, dt);
+    k_advect_density<<<grid3(g.nx - 2, g.ny - 2, (g.nz - 2 + ADV_ZC - 1) / ADV_ZC), dim3(BX, BY), 0, st>>>(
+        g, r0, r1, u1, v1, w1, flags, dt, g.nz - 2);
 }
 
 void launch_div_max(const Grid& g, const float* u, const float* v, const float* w,

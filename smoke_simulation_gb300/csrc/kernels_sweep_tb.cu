@@ -503,15 +503,15 @@ k_group_sweep_tb(const GroupTBGrid* __restrict__ grids, const int* __restrict__ 
 __global__ void k_group_tb_loop_next(const GroupTBGrid* __restrict__ grids, int n, int* counter, int step,
                                      int limit, unsigned long long* launches, int launches_per_iter,
                                      cudaGraphConditionalHandle handle) {
-    int open = 0;
+    int active = 0;
     for (int j = (int)threadIdx.x; j < n; j += (int)blockDim.x)
-        open |= *(volatile const int*)&grids[j].status->done == 0;
-    open = __syncthreads_or(open);
+        active |= *(volatile const int*)&grids[j].status->done == 0;
+    active = __syncthreads_or(active);
     if (threadIdx.x == 0) {
         const int c = *counter + step;
         *counter = c;
         if (launches != nullptr) *launches += (unsigned long long)launches_per_iter;
-        cudaGraphSetConditional(handle, (open && c < limit) ? 1u : 0u);
+        cudaGraphSetConditional(handle, (active && c < limit) ? 1u : 0u);
     }
 }
 
