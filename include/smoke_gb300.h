@@ -35,6 +35,8 @@ extern "C" {
 /* Projection schemes. */
 #define SMK_PROJECT_REFERENCE 0 /* in-place velocity red-black SOR, bit-exact with the reference */
 #define SMK_PROJECT_PRESSURE 1  /* pressure red-black SOR on P, then one pass subtracting grad P */
+#define SMK_SOLVER_RBSOR 0
+#define SMK_SOLVER_JACOBI 1
 
 /* Velocity clamp modes. */
 #define SMK_CLAMP_REFERENCE 0 /* if |u|^2*dt > c^2 scale by c^2/(|u|^2*dt) (smokeSimulation.cu:343-349) */
@@ -72,6 +74,10 @@ typedef struct smk_params {
                               face touching a cell of the last obstacle (the one that decides the
                               mask) takes that obstacle's velocity, a moving boundary the
                               projection then respects.  0 (default): the reference's behaviour. */
+    int solver;         /* PRESSURE only: SMK_SOLVER_RBSOR (default) red-black SOR, or
+                           SMK_SOLVER_JACOBI weighted Jacobi: every cell from the previous
+                           iterate, P += (omega/acc) * residual, one iteration per "sweep" (use
+                           omega <= 1; not with refine). */
 } smk_params;
 
 typedef struct smk_stats {

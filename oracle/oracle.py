@@ -33,6 +33,7 @@ class OrcParams(C.Structure):
         ("boxes", _F), ("n_boxes", C.c_int),
         ("obstacles", _F), ("n_obstacles", C.c_int),
         ("refine", C.c_int), ("refine_sweeps", C.c_int), ("obstacle_velocity", C.c_int),
+        ("solver", C.c_int),
     ]
 
 
@@ -152,6 +153,7 @@ class OracleSim:
         p.obstacles, p.n_obstacles = _fptr(self.obstacles), self.n_obstacles
         p.refine, p.refine_sweeps = getattr(sc, "refine", 0), getattr(sc, "refine_sweeps", 10)
         p.obstacle_velocity = getattr(sc, "obstacle_velocity", 0)
+        p.solver = getattr(sc, "solver", 0)
         return p
 
     def step(self, dt: Optional[float] = None) -> OrcStats:

@@ -54,6 +54,7 @@ typedef struct {
     int refine;          // scheme 1 with tol > 0: FP64-checked refinement rounds (0: none)
     int refine_sweeps;   // sweeps of each correction solve
     int obstacle_velocity;  // 1: faces touching a cell of the last obstacle take its velocity
+    int solver;          // scheme 1: 0 red-black SOR, 1 weighted Jacobi (weight omega)
 } orc_params;
 
 typedef struct {
@@ -309,7 +310,8 @@ T residual_max(const Dims& d, const T* P, const T* b, const uint8_t* s) {
 // <= tol the solve ends after them.  The GPU kernels follow the same rule.
 template <typename T>
 int project_pressure(const Dims& d, T* u, T* v, T* w, T* P, T* b, const uint8_t* s, int max_sweeps,
-                     double omega, float tol, int check_every, int warm_start, orc_stats* st) {
+                     double omega, float tol, int check_every, int warm_start, orc_stats* st,
+                     int solver = 0) {
     // right-hand side
 #pragma omp parallel for schedule(static)
     for (int z = 0; z < d.nz; ++z)
@@ -344,7 +346,29 @@ int project_pressure(const Dims& d, T* u, T* v, T* w, T* P, T* b, const uint8_t*
             if (last_r <= (T)tol) stop_after_group = true;
         }
         int group_end = (tol > 0.0f) ? std::min(max_sweeps, (sweeps / G + 1) * G) : max_sweeps;
-        for (; sweeps < group_end; ++sweeps)
+        for (; sweeps < group_end; ++sweeps) {
+            if (solver == 1) {
+                // weighted Jacobi: every projectable cell from the previous iterate, the same
+                // residual and update expressions as a colour pass
+                std::vector<T> Pn((size_t)d.nx * d.ny * d.nz, (T)0);
+#pragma omp parallel for schedule(static)
+                for (int z = 1; z < d.nz - 1; ++z)
+                    for (int y = 1; y < d.ny - 1; ++y)
+                        for (int x = 1; x < d.nx - 1; ++x) {
+                            if (!projectable(d, s, x, y, z)) continue;
+                            int acc = fluid_nbrs(d, s, x, y, z);
+                            long long c = d.c(x, y, z);
+                            T sum = nbr_sum(d, P, x, y, z);
+                            T r = fma_t<T>(-(T)acc, P[c], b[c] + sum);
+                            Pn[c] = fma_t<T>(wacc[acc], r, P[c]);
+                        }
+#pragma omp parallel for schedule(static)
+                for (int z = 1; z < d.nz - 1; ++z)
+                    for (int y = 1; y < d.ny - 1; ++y)
+                        for (int x = 1; x < d.nx - 1; ++x)
+                            if (projectable(d, s, x, y, z)) P[d.c(x, y, z)] = Pn[d.c(x, y, z)];
+                continue;
+            }
             for (int colour = 0; colour < 2; ++colour) {
 #pragma omp parallel for schedule(static)
                 for (int z = 1; z < d.nz - 1; ++z)
@@ -360,6 +384,7 @@ int project_pressure(const Dims& d, T* u, T* v, T* w, T* P, T* b, const uint8_t*
                         }
                     }
             }
+        }
         if (stop_after_group) {
             converged = 1;
             break;
@@ -676,7 +701,7 @@ int step(orc_state* S, const orc_params* p, float dt, orc_stats* st) {
         local.sweeps = p->iterations;
     } else {
         project_pressure<T>(d, u[now], v[now], w[now], (T*)S->P, (T*)S->b, S->s, p->iterations,
-                            p->omega, p->tol, p->check_every, p->warm_start, &local);
+                            p->omega, p->tol, p->check_every, p->warm_start, &local, p->solver);
         local.div64_max = -1.0f;
         if (p->refine > 0 && p->tol > 0.0f && sizeof(T) == sizeof(float))
             refine_pressure(d, (float*)u[now], (float*)v[now], (float*)w[now], (float*)S->P, S->s, p->refine,

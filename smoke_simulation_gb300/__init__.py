@@ -19,6 +19,7 @@ LIB_PATH = os.path.join(HERE, "libsmoke_gb300.so")
 SMK_OK = 0
 PROJECT_REFERENCE = 0
 PROJECT_PRESSURE = 1
+SOLVER_RBSOR, SOLVER_JACOBI = 0, 1
 CLAMP_REFERENCE, CLAMP_MAGNITUDE, CLAMP_NONE = 0, 1, 2
 STORAGE_F32, STORAGE_BF16, STORAGE_BF16_VEL = 0, 1, 2
 
@@ -36,6 +37,7 @@ class Params(C.Structure):
         ("omega", C.c_double), ("tol", C.c_float), ("check_every", C.c_int),
         ("warm_start", C.c_int), ("report_div", C.c_int), ("storage", C.c_int),
         ("refine", C.c_int), ("refine_sweeps", C.c_int), ("obstacle_velocity", C.c_int),
+        ("solver", C.c_int),
     ]
 
 
@@ -451,6 +453,7 @@ def params_for_scene(scene, **overrides) -> Params:
     p.tol, p.check_every, p.warm_start = scene.tol, scene.check_every, scene.warm_start
     p.refine, p.refine_sweeps = scene.refine, scene.refine_sweeps
     p.obstacle_velocity = scene.obstacle_velocity
+    p.solver = scene.solver
     for k, v in overrides.items():
         setattr(p, k, v)
     return p

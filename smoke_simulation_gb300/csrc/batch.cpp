@@ -351,7 +351,8 @@ int launch_config(const GroupSchedule& sched, const TableImage& t, GroupLaunch& 
 bool grouped_eligible(smk_sim* const* sims, int n) {
     if (n > MAX_GROUPED) return false;
     for (int i = 0; i < n; ++i)
-        if (sims[i]->p.projection != SMK_PROJECT_PRESSURE || sims[i]->p.refine > 0 || sims[i]->p.obstacle_velocity)
+        if (sims[i]->p.projection != SMK_PROJECT_PRESSURE || sims[i]->p.refine > 0 || sims[i]->p.obstacle_velocity ||
+            sims[i]->p.solver != SMK_SOLVER_RBSOR)
             return false;
     return true;
 }

@@ -41,6 +41,9 @@ void launch_project_velocity(const Grid& g, float* u, float* v, float* w, const 
 template <typename T>
 void launch_rhs(const Grid& g, const T* u, const T* v, const T* w, const uint8_t* flags,
                 float* b, float* P, const float* P2, const int* pcur, int warm, cudaStream_t st);
+// One weighted Jacobi iteration Pin -> Pout (see k_jacobi); *pcur = out_idx when it runs.
+void launch_jacobi(const Grid& g, const float* Pin, float* Pout, const float* b, const uint8_t* flags,
+                   const float* wacc7, const StepStatus* status, int* pcur, int out_idx, cudaStream_t st);
 void launch_sweep(const Grid& g, float* P, const float* b, const uint8_t* flags, int colour,
                   const float* wacc7, const StepStatus* status, cudaStream_t st);
 void launch_resid_check(const Grid& g, const float* P, const float* b, const uint8_t* flags,

@@ -39,6 +39,33 @@ __global__ void k_sweep(Grid g, float* __restrict__ P, const float* __restrict__
     body_sweep(g, P, b, flags, colour, wa, status, blockIdx);
 }
 
+// Weighted Jacobi: every projectable interior cell from the previous iterate Pin, into Pout, with
+// the colour pass's expressions (cell_sweep); other interior cells get 0, as P holds there.
+// Skipped once the tolerance rule has ended the solve; the first thread records which buffer
+// the launch wrote.
+__global__ void k_jacobi(Grid g, const float* __restrict__ Pin, float* __restrict__ Pout,
+                         const float* __restrict__ b, const uint8_t* __restrict__ flags, WAcc wa,
+                         const StepStatus* __restrict__ status, int* __restrict__ pcur, int out_idx) {
+    if (status && *(volatile const int*)&status->done) return;
+    if (pcur && blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && threadIdx.x == 0 && threadIdx.y == 0)
+        *pcur = out_idx;
+    const int x = 1 + (int)blockIdx.x * BX + (int)threadIdx.x;
+    const int y = 1 + (int)blockIdx.y * BY + (int)threadIdx.y;
+    const int z = 1 + (int)blockIdx.z;
+    if (x > g.nx - 2 || y > g.ny - 2) return;
+    const int i = g.idx(x, y, z);
+    const uint8_t f = flags[i];
+    if (!(f & F_PROJ)) {
+        Pout[i] = 0.0f;
+        return;
+    }
+    const int acc = __popc((unsigned)(f & F_NBRS));
+    const float sum = ((Pin[i - 1] + Pin[i + 1]) + (Pin[i - g.X] + Pin[i + g.X])) + (Pin[i - g.XY] + Pin[i + g.XY]);
+    const float pc = Pin[i];
+    const float r = fmaf(-(float)acc, pc, b[i] + sum);
+    Pout[i] = fmaf(wa.w[acc], r, pc);
+}
+
 __global__ void k_resid_check(Grid g, const float* __restrict__ P, const float* __restrict__ b,
                               const uint8_t* __restrict__ flags, StepStatus* status, int group,
                               float tol) {
@@ -74,6 +101,16 @@ void launch_sweep(const Grid& g, float* P, const float* b, const uint8_t* flags,
     int half = (g.nx - 2 + 1) / 2;
     k_sweep<<<grid3(half, g.ny - 2, g.nz - 2), dim3(BX, BY), 0, st>>>(g, P, b, flags, colour, wa,
                                                                       status);
+}
+
+void launch_jacobi(const Grid& g, const float* Pin, float* Pout, const float* b, const uint8_t* flags,
+                   const float* wacc7, const StepStatus* status, int* pcur, int out_idx, cudaStream_t st) {
+    if (g.nx < 3 || g.ny < 3 || g.nz < 3) return;
+    WAcc wa;
+    for (int k = 0; k < 7; ++k) wa.w[k] = wacc7[k];
+    wa.w[7] = 0.0f;
+    k_jacobi<<<grid3(g.nx - 2, g.ny - 2, g.nz - 2), dim3(BX, BY), 0, st>>>(g, Pin, Pout, b, flags, wa, status, pcur,
+                                                                           out_idx);
 }
 
 void launch_resid_check(const Grid& g, const float* P, const float* b, const uint8_t* flags,

@@ -50,6 +50,9 @@ int check_params(const smk_params* p) {
         return fail(SMK_ERR_INVALID, "refinement needs the PRESSURE projection with tol > 0");
     if (p->refine > 0 && (p->refine_sweeps < 1 || p->refine_sweeps > 100000))
         return fail(SMK_ERR_INVALID, "refine_sweeps must be 1..100000");
+    if (p->solver != SMK_SOLVER_RBSOR && p->solver != SMK_SOLVER_JACOBI) return fail(SMK_ERR_INVALID, "unknown solver");
+    if (p->solver == SMK_SOLVER_JACOBI && (p->projection != SMK_PROJECT_PRESSURE || p->refine > 0))
+        return fail(SMK_ERR_INVALID, "the Jacobi solver needs the PRESSURE projection and no refinement");
     if (p->projection == SMK_PROJECT_PRESSURE && p->tol > 0 &&
         (p->max_sweeps + p->check_every - 1) / p->check_every > 4000)
         return fail(SMK_ERR_INVALID, "too many residual checks per step (max_sweeps/check_every > 4000)");
@@ -255,7 +258,25 @@ int smk_sim::enqueue(float dt, cudaStream_t st) {
         const int G = use_tol ? p.check_every : (p.max_sweeps > 0 ? p.max_sweeps : 1);
         int sweep = 0, group = 0;
         if (timed) SMK_CUDA(rec(ev[5]));
-        if (sweep_depth > 0) {
+        if (p.solver == SMK_SOLVER_JACOBI) {
+            // weighted Jacobi, ping-ponging P <-> P2 (each launch records in *pcur where it wrote);
+            // the check of each group reads the buffer holding the current iterate
+            int nl = 0;
+            while (sweep < p.max_sweeps) {
+                if (use_tol) {
+                    launch_resid_check(g, (nl & 1) ? P2 : P, b, flags, status, group, p.tol, st);
+                    ++launches;
+                }
+                const int end = sweep + G < p.max_sweeps ? sweep + G : p.max_sweeps;
+                for (; sweep < end; ++sweep, ++nl) {
+                    const bool from_a = (nl & 1) == 0;
+                    launch_jacobi(g, from_a ? P : P2, from_a ? P2 : P, b, flags, wacc, use_tol ? status : nullptr,
+                                  pcur, from_a ? 1 : 0, st);
+                    ++launches;
+                }
+                ++group;
+            }
+        } else if (sweep_depth > 0) {
             // temporally blocked: each launch applies up to sweep_depth colour passes,
             // ping-ponging P <-> P2; group starts are the check launches
             int nl = 0;
@@ -346,8 +367,9 @@ int smk_sim::enqueue(float dt, cudaStream_t st) {
         }
         last_groups = group;
         if (timed) SMK_CUDA(rec(ev[6]));
-        const bool tb_used = sweep_depth > 0 && p.max_sweeps > 0;
-        if (!tb_used) SMK_CUDA(cudaMemsetAsync(pcur, 0, sizeof(int), st));
+        // the blocked and Jacobi solves record where the pressure is; the colour passes keep it in P
+        const bool pcur_set = (sweep_depth > 0 || p.solver == SMK_SOLVER_JACOBI) && p.max_sweeps > 0;
+        if (!pcur_set) SMK_CUDA(cudaMemsetAsync(pcur, 0, sizeof(int), st));
         if (bf16)
             launch_project_bf16(g, bf(u[now]), bf(v[now]), bf(w[now]), P, P2, pcur, flags, proj[0], proj[1],
                                 proj[2], st);

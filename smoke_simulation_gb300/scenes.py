@@ -91,6 +91,7 @@ class Scene:
     refine: int = 0                            # FP64-checked refinement rounds (pressure, tol > 0)
     refine_sweeps: int = 10
     obstacle_velocity: int = 0                 # 1: obstacles' velocity drives the fluid
+    solver: int = 0                            # pressure scheme: 0 red-black SOR, 1 Jacobi (omega <= 1)
 
     @property
     def cells(self) -> int:

@@ -342,3 +342,33 @@ def test_moving_obstacle_velocity_bit_exact(gpu, scheme):
         o.step()
     assert H.first_mismatch(sim.read_state(), H.oracle_state(o)) == ""
     sim.close()
+
+
+@pytest.mark.parametrize("tol,warm", [(0.0, 0), (1e-3, 0), (1e-3, 1)])
+def test_jacobi_solver_equals_oracle(gpu, tol, warm):
+    """The weighted Jacobi option of the pressure scheme (P and P2 ping-pong, one launch per
+    iteration) reproduces the oracle bit for bit, tolerance rule and warm start included, with
+    graph replay; a batch of Jacobi members runs as branches with the same results."""
+    sc = S.small_scene(33, 17, 29, steps=5, seed=41, scheme=1, iterations=37, tol=tol, check_every=5,
+                       obstacles=2, solver=smk.SOLVER_JACOBI, omega=0.9, warm_start=warm)
+    o = O.OracleSim(sc)
+    sim = smk.from_scene(sc, report_div=1)
+    twin = smk.from_scene(sc, report_div=1)
+    batch = smk.Batch([twin])
+    for k in range(sc.steps):
+        ost = o.step()
+        sim.step(sc.dt)
+        batch.step(sc.dt)
+        st = sim.stats()
+        assert st.sweeps == ost.sweeps, (k, st.sweeps, ost.sweeps)
+        assert st.converged == ost.converged
+        if tol > 0:
+            assert st.resid_max == ost.resid_max
+        assert st.div_max == ost.div_max
+        msg = H.first_mismatch(sim.read_state(), H.oracle_state(o))
+        assert msg == "", "step %d: %s" % (k, msg)
+    assert batch.info()[0] == smk.BATCH_BRANCHES
+    assert H.first_mismatch(twin.read_state(), sim.read_state()) == ""
+    batch.close()
+    sim.close()
+    twin.close()

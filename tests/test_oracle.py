@@ -203,3 +203,44 @@ def test_obstacle_velocity_drives_the_fluid():
     assert np.array_equal(res[(0, 0.0)], res[(0, 2.0)])  # reference: velocity stored, unused
     near = np.s_[6:14, 6:14, 14:20]                       # (z, y, x) just past the obstacle
     assert np.abs(res[(1, 2.0)][near]).max() > 5 * np.abs(res[(1, 0.0)][near]).max() + 0.1
+
+
+def test_jacobi_first_iteration_is_the_scaled_rhs():
+    """The restatement's Jacobi solver (pressure scheme, solver 1), pinned by a direct numpy
+    restatement: from a zero start one iteration sets P = (omega/acc) * b on every projectable
+    cell (interior, fluid, >= 1 fluid neighbour; acc = its fluid neighbours) and 0 elsewhere."""
+    sc = S.small_scene(20, 16, 18, steps=1, seed=5, scheme=1, iterations=1, solver=1, omega=0.8)
+    o = O.OracleSim(sc)
+    o.step()
+    s = o.s.astype(bool)  # (z, y, x)
+    nz, ny, nx = s.shape
+    acc = np.zeros(s.shape, np.int32)
+    inner = (slice(1, nz - 1), slice(1, ny - 1), slice(1, nx - 1))
+    for ax in range(3):
+        for sh in (-1, 1):
+            acc[inner] += np.roll(s, sh, axis=ax)[inner]
+    proj = np.zeros(s.shape, bool)
+    proj[inner] = s[inner] & (acc[inner] > 0)
+    w = np.zeros(s.shape, np.float32)
+    w[proj] = np.float32(0.8) / acc[proj].astype(np.float32)
+    expected = np.where(proj, w * o.b, np.float32(0))
+    assert np.array_equal(o.P, expected)
+    assert np.count_nonzero(o.P) > 0
+
+
+def test_jacobi_reaches_the_sor_solution():
+    """Solved to a tight tolerance, weighted Jacobi and red-black SOR give the same step (both
+    satisfy the same discrete Poisson problem); Jacobi needs more iterations."""
+    out = {}
+    for solver, omega in ((0, 1.9), (1, 1.0)):
+        sc = S.small_scene(20, 16, 18, steps=2, seed=7, scheme=1, iterations=20000, tol=1e-7,
+                           check_every=10, solver=solver, omega=omega)
+        o = O.OracleSim(sc, dtype=np.float64)
+        sweeps = [o.step().sweeps for _ in range(sc.steps)]
+        out[solver] = (o, sweeps)
+    a, b = out[0][0], out[1][0]
+    for k in ("u", "v", "w", "rho"):
+        for j in range(2):
+            x, y = getattr(a, k)[j], getattr(b, k)[j]
+            assert H.rel_l2(x, y) < 1e-5, (k, j, H.rel_l2(x, y))
+    assert min(out[1][1]) > max(out[0][1])
