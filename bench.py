@@ -11,8 +11,9 @@ configured workload rather than of an ever longer simulation.
   value   cell-updates/s with the state resident in HBM (CUDA events on the step stream)
   e2e     the same metric through smk_simulate (the reference's simulate(): step plus a
           blocking copy of the density into pinned host memory), host wall clock
-  roofline  the sweep phase (red-black passes + residual checks), algorithmic bytes from the
-          per-cell model in the design doc, over its event-timed duration in the timed steps
+  roofline  the sweep phase (red-black passes + residual checks), algorithmic bytes (each sweep
+          reads P, b and the flag byte and writes P: 13 B per cell), over its event-timed
+          duration in the timed steps
   cpu_baseline  the reference's own step built for the host (OpenMP, all cores) on a bounded
           sample of the same workload
   forms   the chosen forms beside the plain step: 64 uneven grids in the grouped batch form
@@ -47,9 +48,9 @@ UNIT = "cell-updates/s"
 N_DEFAULT = 256
 # Sweeps the reference step is given in the CPU baseline and the reference arm: the
 # reference's projection has no convergence test, so it runs the sweep count that this
-# workload's tolerance rule takes on the GPU (mean over the benchmark's steps).
+# workload's tolerance rule takes on the GPU from a zero pressure (mean over the workload's steps).
 REF_SWEEPS_DEFAULT = 167
-# Algorithmic bytes per cell (DESIGN.md): one red+black sweep reads P, b, flags and writes P.
+# Algorithmic bytes per cell: one red+black sweep reads P, b, flags and writes P.
 SWEEP_BYTES_PER_CELL = 13.0
 CHECK_BYTES_PER_CELL = 9.0
 
