@@ -88,6 +88,7 @@ struct TableImage {
     int tb_zchunk = 0, tb_total = 0, tb_check_every = 0, tb_max_sweeps = 0;
     std::vector<unsigned char> tb_recs;
     std::vector<int> tb_starts;
+    std::vector<int> tb_order;  // member of each record
     size_t off_tb = 0, off_tb_starts = 0, off_tb_counter = 0;
 };
 
@@ -232,9 +233,16 @@ int build_table(smk_sim* const* sims, int n, const float* dts, float dt_all, con
         t.tb_max_sweeps = sims[0]->p.max_sweeps;
         t.tb_recs.assign(rb * n, 0);
         t.tb_starts.assign(n + 1, 0);
+        // grids with the longest tiles (most planes per z-chunk) first: CTAs are dispatched in
+        // index order, so the short tiles fill the last wave
+        t.tb_order.resize(n);
+        for (int i = 0; i < n; ++i) t.tb_order[i] = i;
+        std::stable_sort(t.tb_order.begin(), t.tb_order.end(), [&](int a, int c) {
+            return std::min(sims[a]->g.nz, t.tb_zchunk) > std::min(sims[c]->g.nz, t.tb_zchunk);
+        });
         long long acc = 0;
         for (int i = 0; i < n; ++i) {
-            smk_sim* sm = sims[i];
+            smk_sim* sm = sims[t.tb_order[i]];
             float wacc[7];
             wacc[0] = 0.0f;
             for (int a = 1; a <= 6; ++a) wacc[a] = (float)sm->p.omega / (float)a;
@@ -839,7 +847,7 @@ int smk_batch_autotune(smk_batch* b, int* ctas_per_sm, float* us_per_sweep) {
             if (rc) break;
             const size_t rb = group_tb_record_bytes();
             for (int i = 0; i < n; ++i) {
-                smk_sim* sm = b->sims[i];
+                smk_sim* sm = b->sims[t.tb_order[i]];
                 float wacc[7];
                 wacc[0] = 0.0f;
                 for (int a = 1; a <= 6; ++a) wacc[a] = (float)sm->p.omega / (float)a;
