@@ -72,10 +72,11 @@ __device__ __forceinline__ void for_tiles(const GroupArgs& a, int stage, const u
 
 template <typename T, typename Tv>
 __device__ __forceinline__ void objects_cell(const GroupGrid& d, const GroupArgs& a, int x, int y, int z) {
+    const Grid gg = d.g;
     if (x >= d.bx0 && x < d.bx1 && y >= d.by0 && y < d.by1 && z >= d.bz0 && z < d.bz1)
-        cell_emit_boxes(d.g, (T*)d.rho0, (T*)d.rho1, (Tv*)d.v_now, a.boxes + d.box0, d.nbox, x, y, z);
+        cell_emit_boxes(gg, (T*)d.rho0, (T*)d.rho1, (Tv*)d.v_now, a.boxes + d.box0, d.nbox, x, y, z);
     if (x >= d.sx0 && x < d.sx1 && y >= d.sy0 && y < d.sy1 && z >= d.sz0 && z < d.sz1)
-        cell_fill_smoke(d.g, (T*)d.rho0, (T*)d.rho1, a.spheres + d.sph0, d.nsph, x, y, z);
+        cell_fill_smoke(gg, (T*)d.rho0, (T*)d.rho1, a.spheres + d.sph0, d.nsph, x, y, z);
 }
 
 __global__ void __launch_bounds__(GROUP_TILE) k_group_objects(const GroupArgs a) {
@@ -95,16 +96,17 @@ __global__ void __launch_bounds__(GROUP_TILE) k_group_objects(const GroupArgs a)
 __global__ void __launch_bounds__(GROUP_TILE) k_group_forcing(const GroupArgs a) {
     for_tiles(a, GS_FORCE, nullptr, 0, [&](int j, int local) {
         const GroupGrid& d = a.grids[j];
+        const Grid gg = d.g;  // in registers: the stores of the body cannot alias it
         const uint3 bid = tile_bid(local, d.g.nx, d.g.ny - 1);
         typedef __nv_bfloat16 h;
         if (d.kind == GK_BF16)
-            body_forcing<h, h>(d.g, (h*)d.u_now, (h*)d.v_now, (h*)d.w_now, (const h*)d.rho_now, d.flags, d.dt,
+            body_forcing<h, h>(gg, (h*)d.u_now, (h*)d.v_now, (h*)d.w_now, (const h*)d.rho_now, d.flags, d.dt,
                                d.gravity, d.alpha, d.lim_sq, d.lim, d.clamp_mode, bid);
         else if (d.kind == GK_BF16_VEL)
-            body_forcing<h, float>(d.g, (h*)d.u_now, (h*)d.v_now, (h*)d.w_now, (const float*)d.rho_now, d.flags,
+            body_forcing<h, float>(gg, (h*)d.u_now, (h*)d.v_now, (h*)d.w_now, (const float*)d.rho_now, d.flags,
                                    d.dt, d.gravity, d.alpha, d.lim_sq, d.lim, d.clamp_mode, bid);
         else
-            body_forcing<float, float>(d.g, (float*)d.u_now, (float*)d.v_now, (float*)d.w_now,
+            body_forcing<float, float>(gg, (float*)d.u_now, (float*)d.v_now, (float*)d.w_now,
                                        (const float*)d.rho_now, d.flags, d.dt, d.gravity, d.alpha, d.lim_sq,
                                        d.lim, d.clamp_mode, bid);
     });
@@ -113,13 +115,14 @@ __global__ void __launch_bounds__(GROUP_TILE) k_group_forcing(const GroupArgs a)
 __global__ void __launch_bounds__(GROUP_TILE) k_group_adv_vel(const GroupArgs a) {
     for_tiles(a, GS_ADV_VEL, nullptr, 0, [&](int j, int local) {
         const GroupGrid& d = a.grids[j];
+        const Grid gg = d.g;  // in registers: the stores of the body cannot alias it
         const uint3 bid = tile_bid(local, d.g.nx - 1, d.g.ny - 1);
         typedef __nv_bfloat16 h;
         if (d.kind == GK_F32)
-            body_advect_velocity<float, float>(d.g, d.pu, d.pv, d.pw, (float*)d.u_past, (float*)d.v_past,
+            body_advect_velocity<float, float>(gg, d.pu, d.pv, d.pw, (float*)d.u_past, (float*)d.v_past,
                                                (float*)d.w_past, d.flags, d.dt, bid);
         else
-            body_advect_velocity<float, h>(d.g, d.pu, d.pv, d.pw, (h*)d.u_past, (h*)d.v_past, (h*)d.w_past,
+            body_advect_velocity<float, h>(gg, d.pu, d.pv, d.pw, (h*)d.u_past, (h*)d.v_past, (h*)d.w_past,
                                            d.flags, d.dt, bid);
     });
 }
@@ -127,16 +130,17 @@ __global__ void __launch_bounds__(GROUP_TILE) k_group_adv_vel(const GroupArgs a)
 __global__ void __launch_bounds__(GROUP_TILE) k_group_adv_rho(const GroupArgs a) {
     for_tiles(a, GS_ADV_RHO, nullptr, 0, [&](int j, int local) {
         const GroupGrid& d = a.grids[j];
+        const Grid gg = d.g;  // in registers: the stores of the body cannot alias it
         const uint3 bid = tile_bid(local, d.g.nx - 2, d.g.ny - 2);
         typedef __nv_bfloat16 h;
         if (d.kind == GK_BF16)
-            body_advect_density<h, h>(d.g, (const h*)d.rho_now, (h*)d.rho_past, (const h*)d.u_past,
+            body_advect_density<h, h>(gg, (const h*)d.rho_now, (h*)d.rho_past, (const h*)d.u_past,
                                       (const h*)d.v_past, (const h*)d.w_past, d.flags, d.dt, bid);
         else if (d.kind == GK_BF16_VEL)
-            body_advect_density<float, h>(d.g, (const float*)d.rho_now, (float*)d.rho_past, (const h*)d.u_past,
+            body_advect_density<float, h>(gg, (const float*)d.rho_now, (float*)d.rho_past, (const h*)d.u_past,
                                           (const h*)d.v_past, (const h*)d.w_past, d.flags, d.dt, bid);
         else
-            body_advect_density<float, float>(d.g, (const float*)d.rho_now, (float*)d.rho_past,
+            body_advect_density<float, float>(gg, (const float*)d.rho_now, (float*)d.rho_past,
                                               (const float*)d.u_past, (const float*)d.v_past,
                                               (const float*)d.w_past, d.flags, d.dt, bid);
     });
@@ -245,12 +249,13 @@ __global__ void __launch_bounds__(GROUP_TILE) k_group_project(const GroupArgs a)
         }
         for_tiles(a, GS_RHS, nullptr, 0, [&](int j, int local) {
             const GroupGrid& d = a.grids[j];
+            const Grid gg = d.g;  // in registers: the stores of the body cannot alias it
             const uint3 bid = tile_bid(local, d.g.nx, d.g.ny);
             if (d.kind == GK_F32)
-                body_rhs<float>(d.g, (const float*)d.u_now, (const float*)d.v_now, (const float*)d.w_now, d.flags,
+                body_rhs<float>(gg, (const float*)d.u_now, (const float*)d.v_now, (const float*)d.w_now, d.flags,
                                 d.b, d.P, d.P2, d.pcur, d.warm, bid);
             else
-                body_rhs<__nv_bfloat16>(d.g, (const __nv_bfloat16*)d.u_now, (const __nv_bfloat16*)d.v_now,
+                body_rhs<__nv_bfloat16>(gg, (const __nv_bfloat16*)d.u_now, (const __nv_bfloat16*)d.v_now,
                                         (const __nv_bfloat16*)d.w_now, d.flags, d.b, d.P, d.P2, d.pcur, d.warm,
                                         bid);
         });
@@ -311,7 +316,7 @@ __global__ void __launch_bounds__(GROUP_TILE) k_group_project(const GroupArgs a)
                     mb = 0u;
                 }
                 const GroupGrid& d = a.grids[j];
-                const Grid& g = d.g;
+                const Grid g = d.g;  // in registers: the stores below cannot alias it
                 const int tpp = group_interior_tpp(g);
                 const int z0 = 1 + (local / tpp) * a.zslab;
                 const int z1 = min(z0 + a.zslab, g.nz - 1);
@@ -333,7 +338,7 @@ __global__ void __launch_bounds__(GROUP_TILE) k_group_project(const GroupArgs a)
         for (int colour = 0; colour < 2; ++colour) {
             for_tiles(a, GS_SWEEP, gst, GA_SWEEP, [&](int j, int local) {
                 const GroupGrid& d = a.grids[j];
-                const Grid& g = d.g;
+                const Grid g = d.g;  // in registers: the stores below cannot alias it
                 const int tpp = group_sweep_tpp(g);
                 const int z0 = 1 + (local / tpp) * a.zslab;
                 const int z1 = min(z0 + a.zslab, g.nz - 1);
@@ -361,14 +366,15 @@ __global__ void __launch_bounds__(GROUP_TILE) k_group_project(const GroupArgs a)
     // blocked solve's last launch left it
     for_tiles(a, GS_PROJECT, nullptr, 0, [&](int j, int local) {
         const GroupGrid& d = a.grids[j];
+        const Grid gg = d.g;  // in registers: the stores of the body cannot alias it
         int rx, ry, rz;
         group_extent(GS_PROJECT, d, rx, ry, rz);
         const uint3 bid = tile_bid(local, rx, ry);
         if (d.kind == GK_F32)
-            body_gradient_subtract(d.g, (float*)d.u_now, (float*)d.v_now, (float*)d.w_now, d.P, d.P2, d.pcur,
+            body_gradient_subtract(gg, (float*)d.u_now, (float*)d.v_now, (float*)d.w_now, d.P, d.P2, d.pcur,
                                    d.flags, bid);
         else
-            body_project_bf16(d.g, (__nv_bfloat16*)d.u_now, (__nv_bfloat16*)d.v_now, (__nv_bfloat16*)d.w_now,
+            body_project_bf16(gg, (__nv_bfloat16*)d.u_now, (__nv_bfloat16*)d.v_now, (__nv_bfloat16*)d.w_now,
                               d.P, d.P2, d.pcur, d.flags, d.pu, d.pv, d.pw, bid);
     });
 
@@ -386,7 +392,7 @@ __global__ void __launch_bounds__(GROUP_TILE) k_group_project(const GroupArgs a)
                 mb = 0u;
             }
             const GroupGrid& d = a.grids[j];
-            const Grid& g = d.g;
+            const Grid g = d.g;  // in registers: the stores below cannot alias it
             const int tpp = group_interior_tpp(g);
             const int z0 = 1 + (local / tpp) * a.zslab;
             const int z1 = min(z0 + a.zslab, g.nz - 1);
