@@ -285,7 +285,7 @@ def main():
     else:
         depth, zchunk, tuned_us = sim.autotune()
     rows = sim.sweep_shape()[1]
-    kname = "k_sweep_tb<%d, %d>" % (depth, rows)
+    kname = ("k_sweep_tb_ycl<%d>" % depth) if rows & smk.SWEEP_YCLUSTER else ("k_sweep_tb<%d, %d>" % (depth, rows))
 
     # warm-up steps (graph capture, caches); the timed segments restart from the initial state
     for _ in range(max(args.warmup, 0)):

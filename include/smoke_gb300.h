@@ -177,8 +177,11 @@ long long smk_launch_count(const smk_sim* sim);
 int smk_set_sweep_kernel(smk_sim* sim, int depth, int zchunk);
 int smk_get_sweep_kernel(const smk_sim* sim, int* depth, int* zchunk);
 /* The same with the blocked kernel's patch height: `rows` cell rows per thread (2 with depth 2,
- * 4 or 6; 4 with depth 4: a 64 x 32 tile of 8 warps instead of 16).  smk_set_sweep_kernel is
- * rows = 2. */
+ * 4 or 6; 4 with depth 4: a 64 x 32 tile of 8 warps instead of 16), or 2 | SMK_SWEEP_YCLUSTER
+ * with depth 6 (ny <= 256): the CTAs of one x-z column form a thread-block cluster spanning y
+ * and exchange their boundary rows through distributed shared memory instead of recomputing a
+ * halo.  smk_set_sweep_kernel is rows = 2. */
+#define SMK_SWEEP_YCLUSTER 0x100
 int smk_set_sweep_shape(smk_sim* sim, int depth, int rows, int zchunk);
 int smk_get_sweep_shape(const smk_sim* sim, int* depth, int* rows, int* zchunk);
 /* Replay steady-state steps as a captured CUDA graph (default on).  A graph is re-captured

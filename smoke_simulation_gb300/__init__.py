@@ -20,6 +20,7 @@ SMK_OK = 0
 PROJECT_REFERENCE = 0
 PROJECT_PRESSURE = 1
 SOLVER_RBSOR, SOLVER_JACOBI = 0, 1
+SWEEP_YCLUSTER = 0x100  # smk_set_sweep_shape rows flag: y-column clusters exchanging boundary rows
 CLAMP_REFERENCE, CLAMP_MAGNITUDE, CLAMP_NONE = 0, 1, 2
 STORAGE_F32, STORAGE_BF16, STORAGE_BF16_VEL = 0, 1, 2
 

@@ -54,8 +54,13 @@ void launch_gradient_subtract(const Grid& g, float* u, float* v, float* w, const
 // Temporally blocked sweeps: nhalf <= T colour passes in one pass over HBM, P_in -> P_out;
 // `check` launches also record the residual of the input state for tolerance group `group`.
 // The pressure buffers are read through TMA tensor maps built once per simulation.
-// Supported shapes: `rows` = cell rows of a thread's patch (2: T = 2, 4, 6; 4: T = 4).
+// Supported shapes: `rows` = cell rows of a thread's patch (2: T = 2, 4, 6; 4: T = 4), or
+// 2 | SWEEP_YCLUSTER with T = 6: 2-row patches whose y-column of CTAs is one thread-block
+// cluster exchanging boundary rows through distributed shared memory (ny <= 256).
+constexpr int SWEEP_YCLUSTER = 0x100;
 int sweep_tb_shape_supported(int T, int rows);
+// Clusters of the y-cluster form that can be resident at once for grid g (0: not usable).
+int sweep_ycluster_usable(const Grid& g);
 // Set the kernels' shared-memory attributes once (outside any stream capture).
 int prepare_sweep_kernels();
 struct SweepMaps;

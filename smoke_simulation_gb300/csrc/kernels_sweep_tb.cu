@@ -160,9 +160,30 @@ __device__ __forceinline__ void tensormap_acquire(const CUtensorMap* map) {
                  : "memory");
 }
 
+// Cluster barrier: every thread of every CTA of the cluster arrives (release) and waits
+// (acquire); it also orders this CTA's shared-memory accesses like __syncthreads.
+__device__ __forceinline__ void cluster_sync_all() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+
+// Address of this CTA's shared-memory word `local` in the shared memory of cluster CTA `rank`.
+__device__ __forceinline__ uint32_t cluster_map(uint32_t local, uint32_t rank) {
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(local), "r"(rank));
+    return r;
+}
+
+__device__ __forceinline__ void st_cluster(uint32_t addr, float v) {
+    asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(addr), "f"(v) : "memory");
+}
+
 // One tile (bx, by, bz) of a blocked launch: the CTA's whole job.  `group` is absolute.
 // GLOBAL_MAPS: the tensor maps are in global memory (grouped launches), not kernel parameters.
-template <int T, int PY, bool GLOBAL_MAPS = false>
+// YCLUSTER: the launch's gridDim.y CTAs of one (bx, bz) form a thread-block cluster covering the
+// whole y extent (ny <= 32 gridDim.y); instead of recomputing a T-row halo in y, every CTA
+// writes its boundary rows' published values into its neighbours' shared memory (the padding
+// rows of their published planes), and the per-iteration barrier is a cluster barrier.
+template <int T, int PY, bool GLOBAL_MAPS = false, bool YCLUSTER = false>
 __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, float* __restrict__ Pout,
                                            int nhalf, int colour0, int zchunk, const WAcc8& wa,
                                            StepStatus* status, int check, int group, float tol,
@@ -175,7 +196,8 @@ __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, fl
     constexpr int R = T + 4;                 // register ring length (even, >= T + 3)
     constexpr int TB_S = R / 2;              // TMA stages (planes in flight)
     constexpr int IX = 2 * TB_TX - 2 * T;    // interior columns
-    constexpr int IY = ROWS - 2 * T;         // interior rows
+    constexpr int HY = YCLUSTER ? 0 : T;     // halo rows in y
+    constexpr int IY = ROWS - 2 * HY;        // interior rows
     extern __shared__ __align__(128) unsigned char smem_raw[];
     // TMA destinations must be 128-byte aligned: align the dynamic base explicitly (the launch
     // requests 128 spare bytes)
@@ -187,6 +209,7 @@ __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, fl
     float* pub = reinterpret_cast<float*>(stages + TB_S * STAGE_BYTES);
     __shared__ __align__(8) uint64_t mbar[TB_S];
     __shared__ float2 coef[128];
+    __shared__ int tma_bad;  // YCLUSTER: a TMA stage of this CTA never completed
 
     const bool first_tile = (bx | by | bz) == 0;
     if (status != nullptr) {
@@ -206,15 +229,17 @@ __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, fl
         const int acc = __popc(tid & 0x3f);
         coef[tid] = make_float2(-(float)acc, (tid & 0x40) ? wa.w[acc] : 0.0f);
     }
-    // zero the padding rows of every published plane (never written afterwards)
+    // zero the padding rows of every published plane (never written afterwards, except by the
+    // cluster neighbours in the YCLUSTER form)
+    if (YCLUSTER && tid == 0) tma_bad = 0;
     for (int i = tid; i < 2 * NPUB * 2 * TB_TX; i += G::THREADS) {
         const int lane = i % TB_TX, edge = (i / TB_TX) % 2, set = i / (2 * TB_TX);
         pub[set * PROW + (edge ? (TY + 1) * TB_TX : 0) + lane] = 0.0f;
     }
     if (pcur != nullptr && first_tile && leader) *pcur = out_idx;
 
-    const int X0 = bx * IX - T;  // even; first tile column
-    const int Y0 = by * IY - T;  // even; first tile row
+    const int X0 = bx * IX - T;   // even; first tile column
+    const int Y0 = by * IY - HY;  // even; first tile row
     const int xf = X0 - (X0 & 3);             // 16-byte aligned float box start
     const int xb = X0 - (X0 & 15);            // 16-byte aligned flag box start
     const int of = X0 - xf + 2 * tx;          // this thread's column in the float box
@@ -227,7 +252,7 @@ __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, fl
     bool in[PY];  // row r of the patch is an interior row of the tile inside the grid
 #pragma unroll
     for (int r = 0; r < PY; ++r)
-        in[r] = inx && (PY * ty + r >= T) && (PY * ty + r < T + IY) && y0 + r >= 0 && y0 + r < g.ny;
+        in[r] = inx && (PY * ty + r >= HY) && (PY * ty + r < HY + IY) && y0 + r >= 0 && y0 + r < g.ny;
     const int off0 = x0 + g.X * y0;
 
     const int qbeg = za - T;
@@ -262,7 +287,18 @@ __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, fl
     const int p_par = (qbeg + colour0) & 1;  // stage colour parity of the first iteration
     int par = 0;                             // publish-buffer parity
     const int me0 = (ty + 1) * TB_TX + tx;   // my slot in a padded published row set
-    __syncthreads();                         // barriers, table and padding visible
+    // YCLUSTER: the neighbours' copies of my boundary rows go to the padding rows of their
+    // published planes (row TY+1 of the CTA above, row 0 of the CTA below)
+    const bool push_up = YCLUSTER && ty == 0 && by > 0;
+    const bool push_dn = YCLUSTER && ty == TY - 1 && by + 1 < (int)gridDim.y;
+    uint32_t up_base = 0, dn_base = 0;
+    if (YCLUSTER) {
+        up_base = cluster_map(smem_u32(pub + (TY + 1) * TB_TX + tx), (uint32_t)(by - 1 >= 0 ? by - 1 : 0));
+        dn_base = cluster_map(smem_u32(pub + tx), (uint32_t)(by + 1 < (int)gridDim.y ? by + 1 : by));
+        cluster_sync_all();  // every CTA's padding is zero before any neighbour writes into it
+    } else {
+        __syncthreads();  // barriers, table and padding visible
+    }
 
     for (int base = qbeg; base <= qend; base += R) {
 #pragma unroll
@@ -299,20 +335,39 @@ __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, fl
             // column of the thread above and row 0's other column of the thread below.
             const bool sA = ((k + p_par) & 1) == 0;
             float* pb = pub + par * NPUB * PROW;
+            const uint32_t pofs = (uint32_t)(par * NPUB * PROW) * 4u;  // byte offset of this buffer
             if (check) {
                 const int j = (k - 1 + 2 * R) % R;
                 pb[0 * PROW + me0] = pp[0][j].x;
                 pb[1 * PROW + me0] = pp[0][j].y;
                 pb[2 * PROW + me0] = pp[L][j].x;
                 pb[3 * PROW + me0] = pp[L][j].y;
+                if (push_up) {
+                    st_cluster(up_base + pofs + 0u * PROW * 4u, pp[0][j].x);
+                    st_cluster(up_base + pofs + 1u * PROW * 4u, pp[0][j].y);
+                }
+                if (push_dn) {
+                    st_cluster(dn_base + pofs + 2u * PROW * 4u, pp[L][j].x);
+                    st_cluster(dn_base + pofs + 3u * PROW * 4u, pp[L][j].y);
+                }
             }
 #pragma unroll
             for (int s = 1; s <= T; ++s) {
                 const int j = (k - 1 - s + 2 * R) % R;
-                pb[(2 + 2 * s) * PROW + me0] = sA ? pp[0][j].y : pp[0][j].x;  // row 0, read from above
-                pb[(3 + 2 * s) * PROW + me0] = sA ? pp[L][j].x : pp[L][j].y;  // last row, read from below
+                const float v0 = sA ? pp[0][j].y : pp[0][j].x;  // row 0, read from above
+                const float vl = sA ? pp[L][j].x : pp[L][j].y;  // last row, read from below
+                pb[(2 + 2 * s) * PROW + me0] = v0;
+                pb[(3 + 2 * s) * PROW + me0] = vl;
+                if (push_up) st_cluster(up_base + pofs + (uint32_t)(2 + 2 * s) * PROW * 4u, v0);
+                if (push_dn) st_cluster(dn_base + pofs + (uint32_t)(3 + 2 * s) * PROW * 4u, vl);
             }
-            if (__syncthreads_or(!ok)) {
+            if (YCLUSTER) {
+                // every CTA of the cluster runs the same number of cluster barriers, so a CTA
+                // whose TMA stage never completed records it and carries on (its results are
+                // void; the error is reported) instead of leaving its neighbours waiting
+                if (!ok) tma_bad = 1;
+                cluster_sync_all();
+            } else if (__syncthreads_or(!ok)) {
                 // a TMA stage never completed: record it, drain what is in flight, stop
                 if (leader) {
                     atomicExch(kerr, 1);
@@ -436,7 +491,18 @@ __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, fl
         }
     }
 
+    if (YCLUSTER && tma_bad) {
+        // a stage failed: report it and wait (bounded) for this CTA's copies still in flight
+        if (leader) {
+            atomicExch(kerr, 1);
+            for (int pq = qfinal - TB_S + 1; pq <= qfinal; ++pq) {
+                const int d = pq - qbeg;
+                mbar_wait(smem_u32(&mbar[d % TB_S]), (uint32_t)((d / TB_S) & 1));
+            }
+        }
+    }
     if (check) block_max_to(rmax, &status->rmax_bits[group]);
+    if (YCLUSTER) cluster_sync_all();  // no CTA leaves while a neighbour may still address it
 }
 
 template <int T, int PY>
@@ -449,6 +515,17 @@ k_sweep_tb(const __grid_constant__ TBMaps maps, Grid g, float* __restrict__ Pout
     if (group_base != nullptr) group += *group_base;
     sweep_tile<T, PY>(maps, g, Pout, nhalf, colour0, zchunk, wa, status, check, group, tol, pcur, out_idx,
                       kerr, (int)blockIdx.x, (int)blockIdx.y, (int)blockIdx.z);
+}
+
+// The y-cluster form (2-row patches): the gridDim.y CTAs of a column form one cluster.
+template <int T>
+__global__ void __launch_bounds__(TBGeom<2>::THREADS, 1)
+k_sweep_tb_ycl(const __grid_constant__ TBMaps maps, Grid g, float* __restrict__ Pout, int nhalf, int colour0,
+               int zchunk, const __grid_constant__ WAcc8 wa, StepStatus* status, int check, int group, float tol,
+               int* __restrict__ pcur, int out_idx, int* __restrict__ kerr, const int* __restrict__ group_base) {
+    if (group_base != nullptr) group += *group_base;
+    sweep_tile<T, 2, false, true>(maps, g, Pout, nhalf, colour0, zchunk, wa, status, check, group, tol, pcur,
+                                  out_idx, kerr, (int)blockIdx.x, (int)blockIdx.y, (int)blockIdx.z);
 }
 
 // ---- grouped form: one blocked launch over the tiles of every grid of a batch ---------------
@@ -582,6 +659,41 @@ int launch_tb(const TBMaps& maps, const Grid& g, float* Pout, int nhalf, int col
     return 0;
 }
 
+constexpr int YCL_DEPTH = 6;  // the y-cluster form's depth
+
+// CTAs per y-cluster for a grid (one cluster spans the y extent), or 0 when it is too tall.
+inline int ycl_size(const Grid& g) {
+    const int c = (g.ny + TBGeom<2>::ROWS - 1) / TBGeom<2>::ROWS;
+    return c <= 8 ? c : 0;
+}
+
+int launch_tb_ycl(const TBMaps& maps, const Grid& g, float* Pout, int nhalf, int colour0, int zchunk,
+                  const float* wacc7, StepStatus* status, int check, int group, float tol, int* pcur, int out_idx,
+                  int* kerr, const int* group_base, cudaStream_t st) {
+    constexpr int T = YCL_DEPTH;
+    const int cl = ycl_size(g);
+    if (cl < 1) return -1;
+    WAcc8 wa;
+    for (int k = 0; k < 7; ++k) wa.w[k] = wacc7[k];
+    wa.w[7] = 0.0f;
+    constexpr int IX = 2 * TB_TX - 2 * T;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)((g.nx + IX - 1) / IX), (unsigned)cl, (unsigned)((g.nz + zchunk - 1) / zchunk));
+    cfg.blockDim = dim3(TB_TX, TBGeom<2>::TY);
+    cfg.dynamicSmemBytes = tb_smem_bytes<T, 2>();
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 1;
+    attr[0].val.clusterDim.y = (unsigned)cl;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, k_sweep_tb_ycl<T>, maps, g, Pout, nhalf, colour0, zchunk, wa,
+                                             status, check, group, tol, pcur, out_idx, kerr, group_base);
+    return e == cudaSuccess ? 0 : -1;
+}
+
 // End of one iteration of a graph's device-side loop over tolerance groups: advance the group
 // counter and keep looping while the solve is not done and full groups remain.  One thread.
 __global__ void k_group_loop_next(const StepStatus* status, int* counter, int step, int limit,
@@ -597,13 +709,38 @@ __global__ void k_group_loop_next(const StepStatus* status, int* counter, int st
 }  // namespace
 
 int sweep_tb_shape_supported(int T, int rows) {
-    return (rows == 2 && (T == 2 || T == 4 || T == 6)) || (rows == 4 && T == 4);
+    return (rows == 2 && (T == 2 || T == 4 || T == 6)) || (rows == 4 && T == 4) ||
+           (rows == (2 | SWEEP_YCLUSTER) && T == YCL_DEPTH);
+}
+
+int sweep_ycluster_usable(const Grid& g) {
+    const int cl = ycl_size(g);
+    if (cl < 1) return 0;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(1u, (unsigned)cl, 1u);
+    cfg.blockDim = dim3(TB_TX, TBGeom<2>::TY);
+    cfg.dynamicSmemBytes = tb_smem_bytes<YCL_DEPTH, 2>();
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = 1;
+    attr[0].val.clusterDim.y = (unsigned)cl;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, k_sweep_tb_ycl<YCL_DEPTH>, &cfg) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
 }
 
 int prepare_sweep_kernels() {
     const int grouped = cudaFuncSetAttribute(k_group_sweep_tb<GROUP_TB_DEPTH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)tb_smem_bytes<GROUP_TB_DEPTH, 2>()) == cudaSuccess ? 0 : -1;
-    return configure_tb<2, 2>() | configure_tb<4, 2>() | configure_tb<6, 2>() | configure_tb<4, 4>() | grouped;
+    const int ycl = cudaFuncSetAttribute(k_sweep_tb_ycl<YCL_DEPTH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)tb_smem_bytes<YCL_DEPTH, 2>()) == cudaSuccess ? 0 : -1;
+    return configure_tb<2, 2>() | configure_tb<4, 2>() | configure_tb<6, 2>() | configure_tb<4, 4>() | grouped | ycl;
 }
 
 // Tensor maps for the sweep's TMA loads: P_a, P_b, b (float) and flags (u8), for the box
@@ -639,6 +776,7 @@ int launch_sweep_tb(const SweepMaps* m, const Grid& g, bool in_is_a, float* Pout
     maps.b = m->b[v];
     maps.f = m->f[v];
 #define SMK_TB_ARGS maps, g, Pout, nhalf, colour0, zchunk, wacc7, status, check, group, tol, pcur, out_idx, kerr, group_base, st
+    if (rows & SWEEP_YCLUSTER) return launch_tb_ycl(SMK_TB_ARGS);
     if (rows == 4) return launch_tb<4, 4>(SMK_TB_ARGS);
     switch (T) {
         case 2: return launch_tb<2, 2>(SMK_TB_ARGS);

@@ -916,7 +916,13 @@ extern "C" {
 int smk_set_sweep_shape(smk_sim* sim, int depth, int rows, int zchunk) {
     if (!sim) return fail(SMK_ERR_INVALID, "sim is null");
     if (depth != 0 && !sweep_tb_shape_supported(depth, rows))
-        return fail(SMK_ERR_INVALID, "sweep shape must be depth 0, depth 2/4/6 with 2 rows, or depth 4 with 4 rows");
+        return fail(SMK_ERR_INVALID, "sweep shape must be depth 0, depth 2/4/6 with 2 rows, depth 4 with 4 rows, "
+                                     "or depth 6 with 2 rows | SMK_SWEEP_YCLUSTER");
+    if (depth != 0 && (rows & SWEEP_YCLUSTER)) {
+        DeviceGuard dg(sim->device);
+        if (sweep_ycluster_usable(sim->g) < 1)
+            return fail(SMK_ERR_INVALID, "the y-cluster sweep needs ny <= 256 and co-resident clusters");
+    }
     if (zchunk < 1) return fail(SMK_ERR_INVALID, "zchunk must be >= 1");
     sim->sweep_depth = depth;
     sim->sweep_rows = depth != 0 ? rows : 2;
@@ -1021,7 +1027,11 @@ int smk_autotune(smk_sim* sim, int* depth_out, int* zchunk_out, float* us_per_sw
     SMK_CUDA(cudaEventCreate(&e1));
     int best_d = sim->sweep_depth, best_r = sim->sweep_rows, best_z = sim->sweep_zchunk;
     float best = 1e30f;
-    const int shapes[4][2] = {{2, 2}, {4, 2}, {6, 2}, {4, 4}};  // (depth, patch rows)
+    int shapes[5][2] = {{2, 2}, {4, 2}, {6, 2}, {4, 4}, {0, 0}};  // (depth, patch rows)
+    if (sweep_ycluster_usable(g) > 0) {
+        shapes[4][0] = 6;
+        shapes[4][1] = 2 | SWEEP_YCLUSTER;
+    }
     // time one tolerance group exactly as a step issues it: 2G colour passes in launches of
     // `d` (the last one partial when d does not divide 2G), the first with the fused residual
     const bool use_tol = sim->p.tol > 0.0f;
@@ -1039,6 +1049,7 @@ int smk_autotune(smk_sim* sim, int* depth_out, int* zchunk_out, float* us_per_sw
     };
     for (const auto& shape : shapes) {
         const int d = shape[0], rows = shape[1];
+        if (d == 0) continue;
         const int R = d + 4;
         for (int m = 2; m <= 16; ++m) {
             const int zc = R * m - 2 * d - 1;

@@ -114,10 +114,12 @@ def test_reference_api_symbols_match_golden_app80(gpu):
 
 @pytest.mark.parametrize("dims,seed", [((20, 16, 18), 11), ((33, 17, 29), 41), ((64, 64, 64), 42)])
 @pytest.mark.parametrize("tol", [0.0, 1e-3])
-@pytest.mark.parametrize("kernel", [(0, 1), (2, 7), (4, 32), (6, 5), (4, 3), (4, 32, 4), (4, 3, 4)])
+@pytest.mark.parametrize("kernel", [(0, 1), (2, 7), (4, 32), (6, 5), (4, 3), (4, 32, 4), (4, 3, 4),
+                                    (6, 5, 2 | smk.SWEEP_YCLUSTER), (6, 117, 2 | smk.SWEEP_YCLUSTER)])
 def test_pressure_scheme_equals_oracle(gpu, dims, seed, tol, kernel):
     """Every sweep kernel (one colour pass per launch, or temporally blocked with depth 2-6
-    over several z-chunk sizes, with 2- and 4-row patches) reproduces the oracle bit for bit,
+    over several z-chunk sizes, with 2- and 4-row patches, and the y-cluster form exchanging
+    boundary rows through distributed shared memory) reproduces the oracle bit for bit,
     including the tolerance rule's sweep counts and residuals."""
     sc = S.small_scene(*dims, steps=5, seed=seed, scheme=1, iterations=41, tol=tol,
                        check_every=5, obstacles=2)
@@ -138,7 +140,7 @@ def test_pressure_scheme_equals_oracle(gpu, dims, seed, tol, kernel):
     sim.close()
 
 
-@pytest.mark.parametrize("kernel", [(0, 1), (4, 11), (6, 25), (4, 11, 4)])
+@pytest.mark.parametrize("kernel", [(0, 1), (4, 11), (6, 25), (4, 11, 4), (6, 25, 2 | smk.SWEEP_YCLUSTER)])
 def test_warm_start_equals_oracle(gpu, kernel):
     """Warm start (the pressure carried across steps, including through the blocked kernel's
     second buffer) follows the oracle bit for bit, and stays within the tolerance."""
@@ -254,7 +256,8 @@ def test_graphs_and_autotune_do_not_change_results(gpu):
     b.close()
 
 
-@pytest.mark.parametrize("depth,check,rows", [(6, 6, 2), (4, 6, 2), (2, 5, 2), (6, 1, 2), (4, 6, 4)])
+@pytest.mark.parametrize("depth,check,rows", [(6, 6, 2), (4, 6, 2), (2, 5, 2), (6, 1, 2), (4, 6, 4),
+                                              (6, 6, 2 | smk.SWEEP_YCLUSTER)])
 def test_device_group_loop_equals_unrolled_and_direct(gpu, depth, check, rows):
     """The graph's device-side WHILE loop over tolerance groups gives the bits, sweep counts,
     residuals and divergence of the unrolled graph and of direct launches, with stage timing on
@@ -372,3 +375,12 @@ def test_jacobi_solver_equals_oracle(gpu, tol, warm):
     batch.close()
     sim.close()
     twin.close()
+
+
+def test_ycluster_sweep_rejects_tall_grids(gpu):
+    """The y-cluster form needs one cluster to span y (ny <= 256)."""
+    sc = S.small_scene(8, 300, 8, steps=1, seed=3, scheme=1, iterations=6)
+    sim = smk.from_scene(sc)
+    with pytest.raises(smk.SmokeError):
+        sim.set_sweep_kernel(6, 17, 2 | smk.SWEEP_YCLUSTER)
+    sim.close()
