@@ -21,15 +21,16 @@
 // not projectable).  Waits are bounded: on timeout the kernel records an error, waits (bounded)
 // for its own copies still in flight and returns.
 //
-// Per thread: a 2 x 2 patch (x0, x0+1) x (y0, y0+1) with x0, y0 even, so a cell's colour is
-// the parity of z alone and the two cells updated per stage are (A, row 0) + (B, row 1) or
-// (B, row 0) + (A, row 1), uniformly over the CTA.  The z-rings of P, b and flags live in
-// registers; the loop over z is unrolled by the ring length so every slot is a fixed register.
-// x-neighbours come from the patch or a warp shuffle (a tile row of 32 threads is one warp),
-// y-neighbours from the patch or a shared-memory copy of each in-flight plane, published once
-// per iteration (double-buffered: one barrier per iteration).  All stages of an iteration
-// update the same colour pattern, so a stage needs one value per neighbour row (the row-1 value
-// of the thread above in one column, the row-0 value of the thread below in the other): only
+// Per thread: a 2 x PY patch (columns x0, x0+1 = A, B; PY = 2 or 4 rows) with x0, y0 even, so
+// a cell's colour is the parity of z alone and the cells updated per stage are column A of the
+// even rows and B of the odd rows, or the reverse, uniformly over the CTA.  The z-rings of P, b
+// and flags live in registers; the loop over z is unrolled by the ring length so every slot is
+// a fixed register.  x-neighbours come from the patch or a warp shuffle (a tile row of 32
+// threads is one warp), y-neighbours from the patch or a shared-memory copy of each in-flight
+// plane, published once per iteration (double-buffered: one barrier per iteration).  All
+// stages of an iteration update the same colour pattern, so a stage needs one value per
+// neighbour row (the last-row value of the thread above in one column, the row-0 value of the
+// thread below in the other): only
 // those two are published per plane, each as a float plane so a warp's read is 32 consecutive
 // floats (one shared-memory wavefront); the residual plane of check launches publishes all four.
 //
@@ -37,6 +38,12 @@
 // P_c = fma(omega/acc, r, P_c), the oracle's order, so every launch shape gives the same bits
 // as one colour pass per launch.  (-acc, omega/acc) come from a 128-entry table indexed by the
 // flag byte (six neighbour bits + "projectable").
+//
+// Forms (one tile body, sweep_tile): k_sweep_tb<T, PY> (one grid, tensor maps as kernel
+// parameters), k_group_sweep_tb<6> (the tiles of every grid of a batch in one launch, each
+// grid's tensor maps in global memory), k_sweep_tb_ycl<6> (the CTAs of an x-z column as one
+// thread-block cluster that exchanges boundary rows through distributed shared memory instead
+// of recomputing a y-halo).
 #include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
