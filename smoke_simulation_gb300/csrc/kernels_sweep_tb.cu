@@ -30,9 +30,9 @@
 // plane, published once per iteration (double-buffered: one barrier per iteration).  All
 // stages of an iteration update the same colour pattern, so a stage needs one value per
 // neighbour row (the last-row value of the thread above in one column, the row-0 value of the
-// thread below in the other): only
-// those two are published per plane, each as a float plane so a warp's read is 32 consecutive
-// floats (one shared-memory wavefront); the residual plane of check launches publishes all four.
+// thread below in the other): only those two are published per plane, each as a float plane so
+// a warp's read is 32 consecutive floats (one shared-memory wavefront); the residual plane of
+// check launches publishes all four.
 //
 // Every update is  r = fma(-acc, P_c, b_c + (((P_x- + P_x+) + (P_y- + P_y+)) + (P_z- + P_z+)));
 // P_c = fma(omega/acc, r, P_c), the oracle's order, so every launch shape gives the same bits
@@ -63,8 +63,8 @@ constexpr int BOX_U8 = 80;     // flag box width in bytes: 64 + up to 15 alignme
 constexpr unsigned WAIT_LIMIT = 1u << 20;
 
 // Tile geometry for a patch of PY rows per thread: TY tile rows of threads (warps) give
-// ROWS = PY * TY cell rows.  PY = 2: 16 warps, 32 rows; PY = 4: 10 warps, 40 rows (the ring of a
-// 4-row patch needs ~180 registers per thread).
+// ROWS = PY * TY cell rows.  PY = 2: 16 warps, 32 rows; PY = 4: 8 warps, 32 rows (the ring of a
+// 4-row patch needs ~225 registers per thread).
 template <int PY>
 struct TBGeom {
     static_assert(PY == 2 || PY == 4, "patch rows");
