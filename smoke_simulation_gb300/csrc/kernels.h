@@ -1,5 +1,6 @@
 // Host-side launchers of the step's kernels (implemented in the .cu files).
 #pragma once
+#include <initializer_list>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -54,6 +55,16 @@ void launch_gradient_subtract(const Grid& g, float* u, float* v, float* w, const
 // Temporally blocked sweeps: nhalf <= T colour passes in one pass over HBM, P_in -> P_out;
 // `check` launches also record the residual of the input state for tolerance group `group`.
 // The pressure buffers are read through TMA tensor maps built once per simulation.
+// The 4-wide stage kernels (16-byte loads and stores of four consecutive x) need rows that start
+// on 16-byte boundaries: a row pitch that is a multiple of 4 elements and 16-byte aligned
+// float arrays (4-byte aligned byte arrays).  Callers with other layouts get the per-cell kernels.
+inline bool vec4_layout(const Grid& g, std::initializer_list<const void*> floats, const void* bytes) {
+    if (g.X % 4 != 0 || g.XY % 4 != 0) return false;
+    for (const void* p : floats)
+        if (p != nullptr && (reinterpret_cast<uintptr_t>(p) & 15u) != 0) return false;
+    return (reinterpret_cast<uintptr_t>(bytes) & 3u) == 0;
+}
+
 // Supported shapes: `rows` = cell rows of a thread's patch (2: T = 2, 4, 6; 4: T = 4), or
 // 2 | SWEEP_YCLUSTER with T = 6: 2-row patches whose y-column of CTAs is one thread-block
 // cluster exchanging boundary rows through distributed shared memory (ny <= 256).

@@ -82,6 +82,39 @@ __device__ __forceinline__ void body_fill_smoke(const Grid& g, T* __restrict__ r
 }
 
 // ---- forcing: integrate (smokeSimulation.cu:315-329) + velocityConfinement (:331-352) -------
+
+// One face index of the forcing: buoyancy/gravity on v where the cell and the one below are
+// fluid, then the velocity clamp (x >= 1, z >= 1).  Updates (ut, vt, wt) in place; returns bit 0
+// when v is to be stored, bit 1 when u and w are (the clamp scaled them).
+__device__ __forceinline__ unsigned cell_forcing(uint8_t f, int x, int z, float r, float& ut, float& vt,
+                                                 float& wt, float dt, float gravity, float alpha, float lim_sq,
+                                                 float lim, int clamp_mode) {
+    const bool force = (f & F_SELF) && (f & F_YM);
+    const bool clamp = x >= 1 && z >= 1 && clamp_mode != 2;
+    const float buoy = alpha * (r - 0.0f);
+    if (force) vt = vt + (r * gravity * dt + buoy * dt);
+    unsigned wr = (force || clamp) ? 1u : 0u;
+    if (clamp) {
+        const float len = ut * ut + vt * vt + wt * wt;
+        if (clamp_mode == 0) {
+            if (len * dt > lim_sq) {
+                const float s = lim_sq / (len * dt);
+                ut = ut * s;
+                vt = vt * s;
+                wt = wt * s;
+                wr |= 2u;
+            }
+        } else if (len > lim * lim) {
+            const float s = lim / sqrtf(len);
+            ut = ut * s;
+            vt = vt * s;
+            wt = wt * s;
+            wr |= 2u;
+        }
+    }
+    return wr;
+}
+
 template <typename Tv, typename T>
 __device__ __forceinline__ void body_forcing(const Grid& g, Tv* __restrict__ u, Tv* __restrict__ v,
                                              Tv* __restrict__ w, const T* __restrict__ rho,
@@ -96,28 +129,14 @@ __device__ __forceinline__ void body_forcing(const Grid& g, Tv* __restrict__ u, 
     // every input is loaded before the flag byte is tested (the clamp reads u and w of the
     // same index; the buoyancy reads the density): one memory round trip per cell
     const uint8_t f = flags[i];
-    const float v0 = ldv(v, i), r = ldv(rho, i), ut = ldv(u, i), wt = ldv(w, i);
-    const bool force = (f & F_SELF) && (f & F_YM);
-    const bool clamp = x >= 1 && z >= 1 && clamp_mode != 2;
-    const float buoy = alpha * (r - 0.0f);
-    float vt = force ? v0 + (r * gravity * dt + buoy * dt) : v0;
-    if (clamp) {
-        const float len = ut * ut + vt * vt + wt * wt;
-        if (clamp_mode == 0) {
-            if (len * dt > lim_sq) {
-                const float s = lim_sq / (len * dt);
-                stv(u, i, ut * s);
-                vt = vt * s;
-                stv(w, i, wt * s);
-            }
-        } else if (len > lim * lim) {
-            const float s = lim / sqrtf(len);
-            stv(u, i, ut * s);
-            vt = vt * s;
-            stv(w, i, wt * s);
-        }
+    float vt = ldv(v, i), ut = ldv(u, i), wt = ldv(w, i);
+    const float r = ldv(rho, i);
+    const unsigned wr = cell_forcing(f, x, z, r, ut, vt, wt, dt, gravity, alpha, lim_sq, lim, clamp_mode);
+    if (wr & 2u) {
+        stv(u, i, ut);
+        stv(w, i, wt);
     }
-    if (force || clamp) stv(v, i, vt);
+    if (wr & 1u) stv(v, i, vt);
 }
 
 // ---- pressure scheme ------------------------------------------------------------------------
