@@ -37,7 +37,8 @@
 // Every update is  r = fma(-acc, P_c, b_c + (((P_x- + P_x+) + (P_y- + P_y+)) + (P_z- + P_z+)));
 // P_c = fma(omega/acc, r, P_c), the oracle's order, so every launch shape gives the same bits
 // as one colour pass per launch.  (-acc, omega/acc) come from a 128-entry table indexed by the
-// flag byte (six neighbour bits + "projectable").
+// flag byte (six neighbour bits + "projectable"), kept in shared memory once per lane so that
+// lookups never conflict.
 //
 // Forms (one tile body, sweep_tile): k_sweep_tb<T, PY> (one grid, tensor maps as kernel
 // parameters), k_group_sweep_tb<6> (the tiles of every grid of a batch in one launch, each
@@ -214,9 +215,13 @@ __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, fl
     // [TY+2][32] floats
     constexpr int NPUB = 4 + 2 * T;
     float* pub = reinterpret_cast<float*>(stages + TB_S * STAGE_BYTES);
+    // the (-acc, omega/acc) table, one copy per lane: entry e of lane l at [e][l], so a warp's
+    // lookup touches each bank pair once whatever the 32 flag bytes are (one shared copy made
+    // a lookup near scattered solids take ~3.5 wavefronts instead of 2)
+    float2* coef_all = reinterpret_cast<float2*>(pub + 2 * NPUB * PROW);
     __shared__ __align__(8) uint64_t mbar[TB_S];
-    __shared__ float2 coef[128];
-    __shared__ int tma_bad;  // YCLUSTER: a TMA stage of this CTA never completed
+    __shared__ float2 coef_one[128];  // the table once, replicated into coef_all
+    __shared__ int tma_bad;           // YCLUSTER: a TMA stage of this CTA never completed
 
     const bool first_tile = (bx | by | bz) == 0;
     if (status != nullptr) {
@@ -232,10 +237,13 @@ __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, fl
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int tid = ty * TB_TX + tx;
     const bool leader = tid == 0;
-    if (tid < 128) {
+    if (tid < 128) {  // one read of omega/acc per entry (global memory in the grouped form)
         const int acc = __popc(tid & 0x3f);
-        coef[tid] = make_float2(-(float)acc, (tid & 0x40) ? wa.w[acc] : 0.0f);
+        coef_one[tid] = make_float2(-(float)acc, (tid & 0x40) ? wa.w[acc] : 0.0f);
     }
+    __syncthreads();
+    for (int i = tid; i < 128 * TB_TX; i += G::THREADS) coef_all[i] = coef_one[i / TB_TX];
+    const float2* coef = coef_all + tx;  // this lane's copy: entry e at coef[e * TB_TX]
     // zero the padding rows of every published plane (never written afterwards, except by the
     // cluster neighbours in the YCLUSTER form)
     if (YCLUSTER && tid == 0) tma_bad = 0;
@@ -358,15 +366,26 @@ __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, fl
                     st_cluster(dn_base + pofs + 3u * PROW * 4u, pp[L][j].y);
                 }
             }
-#pragma unroll
-            for (int s = 1; s <= T; ++s) {
-                const int j = (k - 1 - s + 2 * R) % R;
-                const float v0 = sA ? pp[0][j].y : pp[0][j].x;  // row 0, read from above
-                const float vl = sA ? pp[L][j].x : pp[L][j].y;  // last row, read from below
+            // v0: row 0's value, read from above; vl: the last row's, read from below (the column
+            // is chosen by branching once per iteration, not by a select per value)
+            auto publish = [&](int s, float v0, float vl) {
                 pb[(2 + 2 * s) * PROW + me0] = v0;
                 pb[(3 + 2 * s) * PROW + me0] = vl;
                 if (push_up) st_cluster(up_base + pofs + (uint32_t)(2 + 2 * s) * PROW * 4u, v0);
                 if (push_dn) st_cluster(dn_base + pofs + (uint32_t)(3 + 2 * s) * PROW * 4u, vl);
+            };
+            if (sA) {
+#pragma unroll
+                for (int s = 1; s <= T; ++s) {
+                    const int j = (k - 1 - s + 2 * R) % R;
+                    publish(s, pp[0][j].y, pp[L][j].x);
+                }
+            } else {
+#pragma unroll
+                for (int s = 1; s <= T; ++s) {
+                    const int j = (k - 1 - s + 2 * R) % R;
+                    publish(s, pp[0][j].x, pp[L][j].y);
+                }
             }
             if (YCLUSTER) {
                 // every CTA of the cluster runs the same number of cluster barriers, so a CTA
@@ -412,9 +431,9 @@ __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, fl
                         const float2 yp = r == L ? dn : pp[r + 1][j];
                         const unsigned f = ff[r / 2][j];
                         const unsigned ia = fidx(f, 2 * (r & 1)), ib = fidx(f, 2 * (r & 1) + 1);
-                        rmax = max(rmax, resid_bits(pp[r][j].x, bb[r][j].x, coef[ia], ia & 0x40u, lB[r],
+                        rmax = max(rmax, resid_bits(pp[r][j].x, bb[r][j].x, coef[ia * TB_TX], ia & 0x40u, lB[r],
                                                     pp[r][j].y, ym.x, yp.x, pp[r][jd].x, pp[r][ju].x));
-                        rmax = max(rmax, resid_bits(pp[r][j].y, bb[r][j].y, coef[ib], ib & 0x40u, pp[r][j].x,
+                        rmax = max(rmax, resid_bits(pp[r][j].y, bb[r][j].y, coef[ib * TB_TX], ib & 0x40u, pp[r][j].x,
                                                     rA[r], ym.y, yp.y, pp[r][jd].y, pp[r][ju].y));
                     }
                 }
@@ -441,14 +460,14 @@ __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, fl
                                 const float ym = r == 0 ? above : pp[r - 1][j].x;
                                 const float yp = pp[r + 1][j].x;
                                 const unsigned ia = fidx(f, 0);
-                                nv[r] = relax(pp[r][j].x, bb[r][j].x, coef[ia], ia & 0x40u, lB, pp[r][j].y,
+                                nv[r] = relax(pp[r][j].x, bb[r][j].x, coef[ia * TB_TX], ia & 0x40u, lB, pp[r][j].y,
                                               ym, yp, pp[r][jd].x, pp[r][ju].x);
                             } else {              // column B
                                 const float rA = __shfl_down_sync(0xffffffffu, pp[r][j].x, 1);
                                 const float ym = pp[r - 1][j].y;
                                 const float yp = r == L ? below : pp[r + 1 < PY ? r + 1 : r][j].y;
                                 const unsigned ib = fidx(f, 3);
-                                nv[r] = relax(pp[r][j].y, bb[r][j].y, coef[ib], ib & 0x40u, pp[r][j].x, rA,
+                                nv[r] = relax(pp[r][j].y, bb[r][j].y, coef[ib * TB_TX], ib & 0x40u, pp[r][j].x, rA,
                                               ym, yp, pp[r][jd].y, pp[r][ju].y);
                             }
                         }
@@ -466,14 +485,14 @@ __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, fl
                                 const float ym = r == 0 ? above : pp[r - 1][j].y;
                                 const float yp = pp[r + 1][j].y;
                                 const unsigned ib = fidx(f, 1);
-                                nv[r] = relax(pp[r][j].y, bb[r][j].y, coef[ib], ib & 0x40u, pp[r][j].x, rA,
+                                nv[r] = relax(pp[r][j].y, bb[r][j].y, coef[ib * TB_TX], ib & 0x40u, pp[r][j].x, rA,
                                               ym, yp, pp[r][jd].y, pp[r][ju].y);
                             } else {              // column A
                                 const float lB = __shfl_up_sync(0xffffffffu, pp[r][j].y, 1);
                                 const float ym = pp[r - 1][j].x;
                                 const float yp = r == L ? below : pp[r + 1 < PY ? r + 1 : r][j].x;
                                 const unsigned ia = fidx(f, 2);
-                                nv[r] = relax(pp[r][j].x, bb[r][j].x, coef[ia], ia & 0x40u, lB, pp[r][j].y,
+                                nv[r] = relax(pp[r][j].x, bb[r][j].x, coef[ia * TB_TX], ia & 0x40u, lB, pp[r][j].y,
                                               ym, yp, pp[r][jd].x, pp[r][ju].x);
                             }
                         }
@@ -639,7 +658,8 @@ bool encode_3d(CUtensorMap* m, const void* base, bool is_u8, const Grid& g, int 
 template <int T, int PY>
 constexpr size_t tb_smem_bytes() {
     using G = TBGeom<PY>;
-    return 128 + (size_t)((T + 4) / 2) * G::STAGE_BYTES + sizeof(float) * 2 * (4 + 2 * T) * G::PROW;
+    return 128 + (size_t)((T + 4) / 2) * G::STAGE_BYTES + sizeof(float) * 2 * (4 + 2 * T) * G::PROW +
+           sizeof(float2) * 128 * TB_TX;
 }
 
 template <int T, int PY>
