@@ -285,7 +285,11 @@ def main():
     else:
         depth, zchunk, tuned_us = sim.autotune()
     rows = sim.sweep_shape()[1]
-    kname = ("k_sweep_tb_ycl<%d>" % depth) if rows & smk.SWEEP_YCLUSTER else ("k_sweep_tb<%d, %d>" % (depth, rows))
+    if rows & smk.SWEEP_YCLUSTER:
+        ncl = (rows >> 9) & 0xF
+        kname = "k_sweep_tb_ycl<%d> (%s)" % (depth, "clusters of %d" % ncl if ncl else "one cluster spanning y")
+    else:
+        kname = "k_sweep_tb<%d, %d>" % (depth, rows)
 
     # warm-up steps (graph capture, caches); the timed segments restart from the initial state
     for _ in range(max(args.warmup, 0)):

@@ -180,8 +180,11 @@ int smk_get_sweep_kernel(const smk_sim* sim, int* depth, int* zchunk);
  * 4 or 6; 4 with depth 4: a 64 x 32 tile of 8 warps instead of 16), or 2 | SMK_SWEEP_YCLUSTER
  * with depth 6 (ny <= 256): the CTAs of one x-z column form a thread-block cluster spanning y
  * and exchange their boundary rows through distributed shared memory instead of recomputing a
- * halo.  smk_set_sweep_kernel is rows = 2. */
+ * halo; 2 | SMK_SWEEP_YCLUSTER | SMK_SWEEP_YCLUSTER_N(n), n = 2 or 4, with depth 6 (any ny):
+ * clusters of n CTAs along y exchange boundary rows the same way, with a halo only at the ends
+ * of each cluster's rows.  smk_set_sweep_kernel is rows = 2. */
 #define SMK_SWEEP_YCLUSTER 0x100
+#define SMK_SWEEP_YCLUSTER_N(n) ((n) << 9)
 int smk_set_sweep_shape(smk_sim* sim, int depth, int rows, int zchunk);
 int smk_get_sweep_shape(const smk_sim* sim, int* depth, int* rows, int* zchunk);
 /* Replay steady-state steps as a captured CUDA graph (default on).  A graph is re-captured

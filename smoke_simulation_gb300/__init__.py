@@ -21,6 +21,11 @@ PROJECT_REFERENCE = 0
 PROJECT_PRESSURE = 1
 SOLVER_RBSOR, SOLVER_JACOBI = 0, 1
 SWEEP_YCLUSTER = 0x100  # smk_set_sweep_shape rows flag: y-column clusters exchanging boundary rows
+
+
+def SWEEP_YCLUSTER_N(n: int) -> int:
+    """rows field of a y-cluster shape with clusters of n (2 or 4) CTAs along y."""
+    return n << 9
 CLAMP_REFERENCE, CLAMP_MAGNITUDE, CLAMP_NONE = 0, 1, 2
 STORAGE_F32, STORAGE_BF16, STORAGE_BF16_VEL = 0, 1, 2
 
@@ -325,7 +330,8 @@ class Simulation:
 
     def set_sweep_kernel(self, depth: int, zchunk: int = 32, rows: int = 2):
         """Blocked sweep kernel shape: `depth` colour passes per launch, z-chunks of `zchunk`
-        planes, patches of `rows` cell rows per thread (2, or 4 with depth 4)."""
+        planes, patches of `rows` cell rows per thread (2, or 4 with depth 4), or with depth 6
+        2 | SWEEP_YCLUSTER [| SWEEP_YCLUSTER_N(2 or 4)]: thread-block clusters along y."""
         _check(lib().smk_set_sweep_shape(self.h, depth, rows, zchunk))
 
     def autotune(self):

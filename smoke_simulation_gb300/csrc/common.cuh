@@ -121,41 +121,44 @@ __device__ __forceinline__ float avgW(const T* __restrict__ f, const Grid& g, in
 
 // sampleSmoke (smokeSimulation.cu:451-484): clamp the position to [1, n-1] with the CELL
 // dims, trilinear weights from (c - delta) - i0, eight terms summed in the reference's order.
-// After the clamp c - delta >= 0.5 (n >= 2; c = 1 when n == 1), so floorf equals truncation,
-// and min(i0 + 1, n - 1) in integers equals the reference's float fminf of small integers: the
-// index arithmetic is cheaper and every result is the same.
-template <typename T>
+// HX, HY, HZ: delta = 0.5 on that axis (1) or 0 (0); every call site has n >= 2 on every axis
+// (it samples only from cells with an interior neighbour).  After the clamp c lies in [1, n-1],
+// so c - delta >= 0.5 and floorf equals truncation, and the reference's fminf(i0, n-1) never
+// changes i0.  Its upper corner fminf(i0 + 1, n - 1): with delta = 0.5, c - delta <= n - 1.5,
+// so i0 <= n - 2 and the corner is always i0 + 1; with delta = 0 it is i0 + 1 unless i0 = n - 1
+// (a position clamped to the last cell), where it repeats i0.  Integer index arithmetic with
+// these facts gives every result of the reference's float index arithmetic.
+template <int HX, int HY, int HZ, typename T>
 __device__ __forceinline__ float sample_ref(const T* __restrict__ f, const Grid& g, float px,
-                                           float py, float pz, float dx, float dy, float dz) {
+                                           float py, float pz) {
     const int lx = g.nx - 1, ly = g.ny - 1, lz = g.nz - 1;
     const float mx = (float)(unsigned)lx, my = (float)(unsigned)ly, mz = (float)(unsigned)lz;
-    const float xs = fmaxf(fminf(px, mx), 1.0f) - dx;
-    const float ys = fmaxf(fminf(py, my), 1.0f) - dy;
-    const float zs = fmaxf(fminf(pz, mz), 1.0f) - dz;
-    const int x0 = min(__float2int_rz(xs), lx);
+    const float xs = fmaxf(fminf(px, mx), 1.0f) - (HX ? 0.5f : 0.0f);
+    const float ys = fmaxf(fminf(py, my), 1.0f) - (HY ? 0.5f : 0.0f);
+    const float zs = fmaxf(fminf(pz, mz), 1.0f) - (HZ ? 0.5f : 0.0f);
+    const int x0 = __float2int_rz(xs);
     const float xw1 = xs - (float)x0;
     const float xw0 = 1.0f - xw1;
-    const int x1 = min(x0 + 1, lx);
-    const int y0 = min(__float2int_rz(ys), ly);
+    const int y0 = __float2int_rz(ys);
     const float yw1 = ys - (float)y0;
     const float yw0 = 1.0f - yw1;
-    const int y1 = min(y0 + 1, ly);
-    const int z0 = min(__float2int_rz(zs), lz);
+    const int z0 = __float2int_rz(zs);
     const float zw1 = zs - (float)z0;
     const float zw0 = 1.0f - zw1;
-    const int z1 = min(z0 + 1, lz);
-    // The upper corner differs from the lower one by +1 on each axis except where the position
-    // was clamped to the last cell (then it repeats it).  Every +1 neighbour lies inside the
-    // arrays (rows hold >= nx+1 elements, planes >= ny+1 rows, the field >= nz+1 planes), so the
-    // x+1 values are loaded at a fixed offset and replaced by the x0 values where x1 == x0: the
+    // The upper corner is +1 on each axis except where a delta-0 axis was clamped to the last
+    // cell (then it repeats the lower one).  Every +1 neighbour lies inside the arrays (rows
+    // hold >= nx+1 elements, planes >= ny+1 rows, the field >= nz+1 planes), so the x+1 values
+    // are loaded at a fixed offset and replaced by the x0 values where the corner repeats: the
     // eight loads need four row addresses, not eight index computations.
+    const int sy = (HY || y0 < ly) ? g.X : 0;
+    const int sz = (HZ || z0 < lz) ? g.XY : 0;
     const T* r00 = f + (x0 + y0 * g.X + z0 * g.XY);
-    const T* r10 = r00 + (y1 - y0) * g.X;
-    const T* r01 = r00 + (z1 - z0) * g.XY;
-    const T* r11 = r01 + (y1 - y0) * g.X;
-    const bool sx = x1 != x0;
+    const T* r10 = r00 + sy;
+    const T* r01 = r00 + sz;
+    const T* r11 = r01 + sy;
     const float a000 = ldv(r00, 0), a010 = ldv(r10, 0), a001 = ldv(r01, 0), a011 = ldv(r11, 0);
     const float b100 = ldv(r00, 1), b110 = ldv(r10, 1), b101 = ldv(r01, 1), b111 = ldv(r11, 1);
+    const bool sx = HX || x0 < lx;
     const float a100 = sx ? b100 : a000, a110 = sx ? b110 : a010, a101 = sx ? b101 : a001,
                 a111 = sx ? b111 : a011;
     return xw0 * yw0 * zw0 * a000 + xw1 * yw0 * zw0 * a100 + xw0 * yw1 * zw0 * a010 +

@@ -66,12 +66,17 @@ inline bool vec4_layout(const Grid& g, std::initializer_list<const void*> floats
 }
 
 // Supported shapes: `rows` = cell rows of a thread's patch (2: T = 2, 4, 6; 4: T = 4), or
-// 2 | SWEEP_YCLUSTER with T = 6: 2-row patches whose y-column of CTAs is one thread-block
-// cluster exchanging boundary rows through distributed shared memory (ny <= 256).
+// 2 | SWEEP_YCLUSTER | (n << SWEEP_YCLUSTER_N_SHIFT) with T = 6: 2-row patches whose CTAs form
+// thread-block clusters along y exchanging boundary rows through distributed shared memory;
+// n = 0: one cluster spans the y extent (ny <= 256), n = 2 or 4: clusters of n CTAs with a
+// halo only at the ends of each cluster's rows.
 constexpr int SWEEP_YCLUSTER = 0x100;
+constexpr int SWEEP_YCLUSTER_N_SHIFT = 9;
+inline int sweep_ycluster_n(int rows) { return (rows >> SWEEP_YCLUSTER_N_SHIFT) & 0xf; }
 int sweep_tb_shape_supported(int T, int rows);
-// Clusters of the y-cluster form that can be resident at once for grid g (0: not usable).
-int sweep_ycluster_usable(const Grid& g);
+// Clusters of the y-cluster form with n_req CTAs each (0: one spanning y) that can be resident
+// at once for grid g (0: not usable).
+int sweep_ycluster_usable(const Grid& g, int n_req);
 // Set the kernels' shared-memory attributes once (outside any stream capture).
 int prepare_sweep_kernels();
 struct SweepMaps;

@@ -42,9 +42,9 @@
 //
 // Forms (one tile body, sweep_tile): k_sweep_tb<T, PY> (one grid, tensor maps as kernel
 // parameters), k_group_sweep_tb<6> (the tiles of every grid of a batch in one launch, each
-// grid's tensor maps in global memory), k_sweep_tb_ycl<6> (the CTAs of an x-z column as one
-// thread-block cluster that exchanges boundary rows through distributed shared memory instead
-// of recomputing a y-halo).
+// grid's tensor maps in global memory), k_sweep_tb_ycl<6> (runs of 2, 4 or all of the CTAs of
+// an x-z column as thread-block clusters that exchange boundary rows through distributed shared
+// memory instead of recomputing a y-halo between them).
 #include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -187,16 +187,18 @@ __device__ __forceinline__ void st_cluster(uint32_t addr, float v) {
 
 // One tile (bx, by, bz) of a blocked launch: the CTA's whole job.  `group` is absolute.
 // GLOBAL_MAPS: the tensor maps are in global memory (grouped launches), not kernel parameters.
-// YCLUSTER: the launch's gridDim.y CTAs of one (bx, bz) form a thread-block cluster covering the
-// whole y extent (ny <= 32 gridDim.y); instead of recomputing a T-row halo in y, every CTA
-// writes its boundary rows' published values into its neighbours' shared memory (the padding
-// rows of their published planes), and the per-iteration barrier is a cluster barrier.
+// YCLUSTER: runs of `ycl_n` CTAs along y (blockIdx.y / ycl_n = the run, blockIdx.y % ycl_n = the
+// CTA's rank in it) form thread-block clusters; a run covers ycl_n * ROWS consecutive rows of
+// which the first and last `ycl_hy` are halo (0 when one run spans the whole y extent, else T).
+// Instead of recomputing a T-row halo between the CTAs of a run, every CTA writes its boundary
+// rows' published values into its neighbours' shared memory (the padding rows of their
+// published planes), and the per-iteration barrier is a cluster barrier.
 template <int T, int PY, bool GLOBAL_MAPS = false, bool YCLUSTER = false>
 __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, float* __restrict__ Pout,
                                            int nhalf, int colour0, int zchunk, const WAcc8& wa,
                                            StepStatus* status, int check, int group, float tol,
                                            int* __restrict__ pcur, int out_idx, int* __restrict__ kerr,
-                                           int bx, int by, int bz) {
+                                           int bx, int by, int bz, int ycl_n = 1, int ycl_hy = 0) {
     using G = TBGeom<PY>;
     constexpr int TY = G::TY, ROWS = G::ROWS, PROW = G::PROW, STAGE_BYTES = G::STAGE_BYTES,
                   STAGE_P = G::STAGE_P;
@@ -204,8 +206,9 @@ __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, fl
     constexpr int R = T + 4;                 // register ring length (even, >= T + 3)
     constexpr int TB_S = R / 2;              // TMA stages (planes in flight)
     constexpr int IX = 2 * TB_TX - 2 * T;    // interior columns
-    constexpr int HY = YCLUSTER ? 0 : T;     // halo rows in y
-    constexpr int IY = ROWS - 2 * HY;        // interior rows
+    constexpr int HY = T;                    // halo rows in y (not YCLUSTER)
+    constexpr int IY = ROWS - 2 * HY;        // interior rows (not YCLUSTER)
+    const int yrank = YCLUSTER ? by % ycl_n : 0;  // rank in the cluster (clusters run along y)
     extern __shared__ __align__(128) unsigned char smem_raw[];
     // TMA destinations must be 128-byte aligned: align the dynamic base explicitly (the launch
     // requests 128 spare bytes)
@@ -254,7 +257,8 @@ __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, fl
     if (pcur != nullptr && first_tile && leader) *pcur = out_idx;
 
     const int X0 = bx * IX - T;   // even; first tile column
-    const int Y0 = by * IY - HY;  // even; first tile row
+    // even; first tile row
+    const int Y0 = YCLUSTER ? (by / ycl_n) * (ycl_n * ROWS - 2 * ycl_hy) - ycl_hy + yrank * ROWS : by * IY - HY;
     const int xf = X0 - (X0 & 3);             // 16-byte aligned float box start
     const int xb = X0 - (X0 & 15);            // 16-byte aligned flag box start
     const int of = X0 - xf + 2 * tx;          // this thread's column in the float box
@@ -267,7 +271,10 @@ __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, fl
     bool in[PY];  // row r of the patch is an interior row of the tile inside the grid
 #pragma unroll
     for (int r = 0; r < PY; ++r)
-        in[r] = inx && (PY * ty + r >= HY) && (PY * ty + r < HY + IY) && y0 + r >= 0 && y0 + r < g.ny;
+        in[r] = inx &&
+                (YCLUSTER ? (yrank * ROWS + PY * ty + r >= ycl_hy && yrank * ROWS + PY * ty + r < ycl_n * ROWS - ycl_hy)
+                          : (PY * ty + r >= HY && PY * ty + r < HY + IY)) &&
+                y0 + r >= 0 && y0 + r < g.ny;
     const int off0 = x0 + g.X * y0;
 
     const int qbeg = za - T;
@@ -304,12 +311,12 @@ __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, fl
     const int me0 = (ty + 1) * TB_TX + tx;   // my slot in a padded published row set
     // YCLUSTER: the neighbours' copies of my boundary rows go to the padding rows of their
     // published planes (row TY+1 of the CTA above, row 0 of the CTA below)
-    const bool push_up = YCLUSTER && ty == 0 && by > 0;
-    const bool push_dn = YCLUSTER && ty == TY - 1 && by + 1 < (int)gridDim.y;
+    const bool push_up = YCLUSTER && ty == 0 && yrank > 0;
+    const bool push_dn = YCLUSTER && ty == TY - 1 && yrank + 1 < ycl_n;
     uint32_t up_base = 0, dn_base = 0;
     if (YCLUSTER) {
-        up_base = cluster_map(smem_u32(pub + (TY + 1) * TB_TX + tx), (uint32_t)(by - 1 >= 0 ? by - 1 : 0));
-        dn_base = cluster_map(smem_u32(pub + tx), (uint32_t)(by + 1 < (int)gridDim.y ? by + 1 : by));
+        up_base = cluster_map(smem_u32(pub + (TY + 1) * TB_TX + tx), (uint32_t)(yrank > 0 ? yrank - 1 : 0));
+        dn_base = cluster_map(smem_u32(pub + tx), (uint32_t)(yrank + 1 < ycl_n ? yrank + 1 : yrank));
         cluster_sync_all();  // every CTA's padding is zero before any neighbour writes into it
     } else {
         __syncthreads();  // barriers, table and padding visible
@@ -543,15 +550,17 @@ k_sweep_tb(const __grid_constant__ TBMaps maps, Grid g, float* __restrict__ Pout
                       kerr, (int)blockIdx.x, (int)blockIdx.y, (int)blockIdx.z);
 }
 
-// The y-cluster form (2-row patches): the gridDim.y CTAs of a column form one cluster.
+// The y-cluster form (2-row patches): runs of ycl_n CTAs along y form clusters, with a halo of
+// ycl_hy rows at each end of a run.
 template <int T>
 __global__ void __launch_bounds__(TBGeom<2>::THREADS, 1)
 k_sweep_tb_ycl(const __grid_constant__ TBMaps maps, Grid g, float* __restrict__ Pout, int nhalf, int colour0,
                int zchunk, const __grid_constant__ WAcc8 wa, StepStatus* status, int check, int group, float tol,
-               int* __restrict__ pcur, int out_idx, int* __restrict__ kerr, const int* __restrict__ group_base) {
+               int* __restrict__ pcur, int out_idx, int* __restrict__ kerr, const int* __restrict__ group_base,
+               int ycl_n, int ycl_hy) {
     if (group_base != nullptr) group += *group_base;
     sweep_tile<T, 2, false, true>(maps, g, Pout, nhalf, colour0, zchunk, wa, status, check, group, tol, pcur,
-                                  out_idx, kerr, (int)blockIdx.x, (int)blockIdx.y, (int)blockIdx.z);
+                                  out_idx, kerr, (int)blockIdx.x, (int)blockIdx.y, (int)blockIdx.z, ycl_n, ycl_hy);
 }
 
 // ---- grouped form: one blocked launch over the tiles of every grid of a batch ---------------
@@ -688,36 +697,56 @@ int launch_tb(const TBMaps& maps, const Grid& g, float* Pout, int nhalf, int col
 
 constexpr int YCL_DEPTH = 6;  // the y-cluster form's depth
 
-// CTAs per y-cluster for a grid (one cluster spans the y extent), or 0 when it is too tall.
-inline int ycl_size(const Grid& g) {
-    const int c = (g.ny + TBGeom<2>::ROWS - 1) / TBGeom<2>::ROWS;
-    return c <= 8 ? c : 0;
+// Cluster geometry of a y-cluster shape: `n` CTAs per cluster, `hy` halo rows at each end of a
+// cluster's run of rows, `grid_y` CTAs along y.  n_req = 0: one cluster spans the y extent
+// (ny <= 256, no halo); 2 or 4: clusters of that many CTAs, each run of n * 32 rows overlapping
+// the next by 2T halo rows.  False when the shape does not fit the grid.
+struct YclGeom {
+    int n, hy, grid_y;
+};
+inline bool ycl_geom(const Grid& g, int n_req, YclGeom* o) {
+    constexpr int ROWS = TBGeom<2>::ROWS, T = YCL_DEPTH;
+    if (n_req == 0) {
+        const int c = (g.ny + ROWS - 1) / ROWS;
+        if (c > 8) return false;
+        *o = YclGeom{c, 0, c};
+        return true;
+    }
+    if (n_req != 2 && n_req != 4) return false;
+    const int run = n_req * ROWS - 2 * T;  // interior rows per cluster
+    *o = YclGeom{n_req, T, ((g.ny + run - 1) / run) * n_req};
+    return true;
 }
 
-int launch_tb_ycl(const TBMaps& maps, const Grid& g, float* Pout, int nhalf, int colour0, int zchunk,
-                  const float* wacc7, StepStatus* status, int check, int group, float tol, int* pcur, int out_idx,
-                  int* kerr, const int* group_base, cudaStream_t st) {
-    constexpr int T = YCL_DEPTH;
-    const int cl = ycl_size(g);
-    if (cl < 1) return -1;
-    WAcc8 wa;
-    for (int k = 0; k < 7; ++k) wa.w[k] = wacc7[k];
-    wa.w[7] = 0.0f;
-    constexpr int IX = 2 * TB_TX - 2 * T;
+cudaLaunchConfig_t ycl_config(const Grid& g, const YclGeom& y, int zchunk, cudaLaunchAttribute* attr) {
+    constexpr int IX = 2 * TB_TX - 2 * YCL_DEPTH;
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)((g.nx + IX - 1) / IX), (unsigned)cl, (unsigned)((g.nz + zchunk - 1) / zchunk));
+    cfg.gridDim = dim3((unsigned)((g.nx + IX - 1) / IX), (unsigned)y.grid_y, (unsigned)((g.nz + zchunk - 1) / zchunk));
     cfg.blockDim = dim3(TB_TX, TBGeom<2>::TY);
-    cfg.dynamicSmemBytes = tb_smem_bytes<T, 2>();
-    cfg.stream = st;
-    cudaLaunchAttribute attr[1];
+    cfg.dynamicSmemBytes = tb_smem_bytes<YCL_DEPTH, 2>();
     attr[0].id = cudaLaunchAttributeClusterDimension;
     attr[0].val.clusterDim.x = 1;
-    attr[0].val.clusterDim.y = (unsigned)cl;
+    attr[0].val.clusterDim.y = (unsigned)y.n;
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    const cudaError_t e = cudaLaunchKernelEx(&cfg, k_sweep_tb_ycl<T>, maps, g, Pout, nhalf, colour0, zchunk, wa,
-                                             status, check, group, tol, pcur, out_idx, kerr, group_base);
+    return cfg;
+}
+
+int launch_tb_ycl(int n_req, const TBMaps& maps, const Grid& g, float* Pout, int nhalf, int colour0, int zchunk,
+                  const float* wacc7, StepStatus* status, int check, int group, float tol, int* pcur, int out_idx,
+                  int* kerr, const int* group_base, cudaStream_t st) {
+    YclGeom y;
+    if (!ycl_geom(g, n_req, &y)) return -1;
+    WAcc8 wa;
+    for (int k = 0; k < 7; ++k) wa.w[k] = wacc7[k];
+    wa.w[7] = 0.0f;
+    cudaLaunchAttribute attr[1];
+    cudaLaunchConfig_t cfg = ycl_config(g, y, zchunk, attr);
+    cfg.stream = st;
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, k_sweep_tb_ycl<YCL_DEPTH>, maps, g, Pout, nhalf, colour0, zchunk,
+                                             wa, status, check, group, tol, pcur, out_idx, kerr, group_base, y.n,
+                                             y.hy);
     return e == cudaSuccess ? 0 : -1;
 }
 
@@ -736,24 +765,22 @@ __global__ void k_group_loop_next(const StepStatus* status, int* counter, int st
 }  // namespace
 
 int sweep_tb_shape_supported(int T, int rows) {
-    return (rows == 2 && (T == 2 || T == 4 || T == 6)) || (rows == 4 && T == 4) ||
-           (rows == (2 | SWEEP_YCLUSTER) && T == YCL_DEPTH);
+    if (rows & SWEEP_YCLUSTER) {
+        const int n = sweep_ycluster_n(rows);
+        return T == YCL_DEPTH && (rows & ~(SWEEP_YCLUSTER | (0xf << SWEEP_YCLUSTER_N_SHIFT))) == 2 &&
+               (n == 0 || n == 2 || n == 4);
+    }
+    return (rows == 2 && (T == 2 || T == 4 || T == 6)) || (rows == 4 && T == 4);
 }
 
-int sweep_ycluster_usable(const Grid& g) {
-    const int cl = ycl_size(g);
-    if (cl < 1) return 0;
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(1u, (unsigned)cl, 1u);
-    cfg.blockDim = dim3(TB_TX, TBGeom<2>::TY);
-    cfg.dynamicSmemBytes = tb_smem_bytes<YCL_DEPTH, 2>();
+int sweep_ycluster_usable(const Grid& g, int n_req) {
+    YclGeom y;
+    if (!ycl_geom(g, n_req, &y)) return 0;
+    y.grid_y = y.n;  // one cluster's worth is enough for the query
     cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = 1;
-    attr[0].val.clusterDim.y = (unsigned)cl;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
+    cudaLaunchConfig_t cfg = ycl_config(g, y, g.nz, attr);
+    cfg.gridDim.x = 1;
+    cfg.gridDim.z = 1;
     int n = 0;
     if (cudaOccupancyMaxActiveClusters(&n, k_sweep_tb_ycl<YCL_DEPTH>, &cfg) != cudaSuccess) {
         cudaGetLastError();
@@ -803,7 +830,7 @@ int launch_sweep_tb(const SweepMaps* m, const Grid& g, bool in_is_a, float* Pout
     maps.b = m->b[v];
     maps.f = m->f[v];
 #define SMK_TB_ARGS maps, g, Pout, nhalf, colour0, zchunk, wacc7, status, check, group, tol, pcur, out_idx, kerr, group_base, st
-    if (rows & SWEEP_YCLUSTER) return launch_tb_ycl(SMK_TB_ARGS);
+    if (rows & SWEEP_YCLUSTER) return launch_tb_ycl(sweep_ycluster_n(rows), SMK_TB_ARGS);
     if (rows == 4) return launch_tb<4, 4>(SMK_TB_ARGS);
     switch (T) {
         case 2: return launch_tb<2, 2>(SMK_TB_ARGS);

@@ -917,11 +917,12 @@ int smk_set_sweep_shape(smk_sim* sim, int depth, int rows, int zchunk) {
     if (!sim) return fail(SMK_ERR_INVALID, "sim is null");
     if (depth != 0 && !sweep_tb_shape_supported(depth, rows))
         return fail(SMK_ERR_INVALID, "sweep shape must be depth 0, depth 2/4/6 with 2 rows, depth 4 with 4 rows, "
-                                     "or depth 6 with 2 rows | SMK_SWEEP_YCLUSTER");
+                                     "or depth 6 with 2 rows | SMK_SWEEP_YCLUSTER [| SMK_SWEEP_YCLUSTER_N(2 or 4)]");
     if (depth != 0 && (rows & SWEEP_YCLUSTER)) {
         DeviceGuard dg(sim->device);
-        if (sweep_ycluster_usable(sim->g) < 1)
-            return fail(SMK_ERR_INVALID, "the y-cluster sweep needs ny <= 256 and co-resident clusters");
+        if (sweep_ycluster_usable(sim->g, sweep_ycluster_n(rows)) < 1)
+            return fail(SMK_ERR_INVALID, "the y-cluster sweep needs co-resident clusters (and ny <= 256 when one "
+                                         "cluster spans y)");
     }
     if (zchunk < 1) return fail(SMK_ERR_INVALID, "zchunk must be >= 1");
     sim->sweep_depth = depth;
@@ -1027,10 +1028,13 @@ int smk_autotune(smk_sim* sim, int* depth_out, int* zchunk_out, float* us_per_sw
     SMK_CUDA(cudaEventCreate(&e1));
     int best_d = sim->sweep_depth, best_r = sim->sweep_rows, best_z = sim->sweep_zchunk;
     float best = 1e30f;
-    int shapes[5][2] = {{2, 2}, {4, 2}, {6, 2}, {4, 4}, {0, 0}};  // (depth, patch rows)
-    if (sweep_ycluster_usable(g) > 0) {
-        shapes[4][0] = 6;
-        shapes[4][1] = 2 | SWEEP_YCLUSTER;
+    int shapes[7][2] = {{2, 2}, {4, 2}, {6, 2}, {4, 4}, {0, 0}, {0, 0}, {0, 0}};  // (depth, patch rows)
+    for (int c = 0; c < 3; ++c) {  // y-cluster forms: one cluster spanning y, clusters of 2 and of 4
+        const int n = c * 2;
+        if (sweep_ycluster_usable(g, n) > 0) {
+            shapes[4 + c][0] = 6;
+            shapes[4 + c][1] = 2 | SWEEP_YCLUSTER | (n << SWEEP_YCLUSTER_N_SHIFT);
+        }
     }
     // time one tolerance group exactly as a step issues it: 2G colour passes in launches of
     // `d` (the last one partial when d does not divide 2G), the first with the fused residual

@@ -330,21 +330,21 @@ __device__ __forceinline__ void body_advect_velocity(const Grid& g, const Ti* __
         xt = xt - dt * ldv(u0, i);
         yt = yt - dt * av;
         zt = zt - dt * aw;
-        stv(u1, i, sample_ref(u0, g, xt, yt, zt, 0.0f, 0.5f, 0.5f));
+        stv(u1, i, sample_ref<0, 1, 1>(u0, g, xt, yt, zt));
     }
     if (dv) {
         float xt = (float)x + 0.5f, yt = (float)y, zt = (float)z + 0.5f;
         xt = xt - dt * au;
         yt = yt - dt * ldv(v0, i);
         zt = zt - dt * aw;
-        stv(v1, i, sample_ref(v0, g, xt, yt, zt, 0.5f, 0.0f, 0.5f));
+        stv(v1, i, sample_ref<1, 0, 1>(v0, g, xt, yt, zt));
     }
     if (dw) {
         float xt = (float)x + 0.5f, yt = (float)y + 0.5f, zt = (float)z;
         xt = xt - dt * au;
         yt = yt - dt * av;
         zt = zt - dt * ldv(w0, i);
-        stv(w1, i, sample_ref(w0, g, xt, yt, zt, 0.5f, 0.5f, 0.0f));
+        stv(w1, i, sample_ref<1, 1, 0>(w0, g, xt, yt, zt));
     }
 }
 
@@ -376,7 +376,7 @@ __device__ __forceinline__ void body_advect_density(const Grid& g, const T* __re
     const float xt = __fsub_rn((float)x + 0.5f, ut * dt);
     const float yt = __fsub_rn((float)y + 0.5f, vt * dt);
     const float zt = __fsub_rn((float)z + 0.5f, wt * dt);
-    stv(r1, i, sample_ref(r0, g, xt, yt, zt, 0.5f, 0.5f, 0.5f));
+    stv(r1, i, sample_ref<1, 1, 1>(r0, g, xt, yt, zt));
 }
 
 }  // namespace smk

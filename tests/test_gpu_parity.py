@@ -115,12 +115,15 @@ def test_reference_api_symbols_match_golden_app80(gpu):
 @pytest.mark.parametrize("dims,seed", [((20, 16, 18), 11), ((33, 17, 29), 41), ((64, 64, 64), 42)])
 @pytest.mark.parametrize("tol", [0.0, 1e-3])
 @pytest.mark.parametrize("kernel", [(0, 1), (2, 7), (4, 32), (6, 5), (4, 3), (4, 32, 4), (4, 3, 4),
-                                    (6, 5, 2 | smk.SWEEP_YCLUSTER), (6, 117, 2 | smk.SWEEP_YCLUSTER)])
+                                    (6, 5, 2 | smk.SWEEP_YCLUSTER), (6, 117, 2 | smk.SWEEP_YCLUSTER),
+                                    (6, 5, 2 | smk.SWEEP_YCLUSTER | smk.SWEEP_YCLUSTER_N(2)),
+                                    (6, 117, 2 | smk.SWEEP_YCLUSTER | smk.SWEEP_YCLUSTER_N(4))])
 def test_pressure_scheme_equals_oracle(gpu, dims, seed, tol, kernel):
     """Every sweep kernel (one colour pass per launch, or temporally blocked with depth 2-6
-    over several z-chunk sizes, with 2- and 4-row patches, and the y-cluster form exchanging
-    boundary rows through distributed shared memory) reproduces the oracle bit for bit,
-    including the tolerance rule's sweep counts and residuals."""
+    over several z-chunk sizes, with 2- and 4-row patches, and the y-cluster forms exchanging
+    boundary rows through distributed shared memory: one cluster spanning y, clusters of 2 and
+    of 4) reproduces the oracle bit for bit, including the tolerance rule's sweep counts and
+    residuals."""
     sc = S.small_scene(*dims, steps=5, seed=seed, scheme=1, iterations=41, tol=tol,
                        check_every=5, obstacles=2)
     o = O.OracleSim(sc)
@@ -140,7 +143,8 @@ def test_pressure_scheme_equals_oracle(gpu, dims, seed, tol, kernel):
     sim.close()
 
 
-@pytest.mark.parametrize("kernel", [(0, 1), (4, 11), (6, 25), (4, 11, 4), (6, 25, 2 | smk.SWEEP_YCLUSTER)])
+@pytest.mark.parametrize("kernel", [(0, 1), (4, 11), (6, 25), (4, 11, 4), (6, 25, 2 | smk.SWEEP_YCLUSTER),
+                                    (6, 25, 2 | smk.SWEEP_YCLUSTER | smk.SWEEP_YCLUSTER_N(2))])
 def test_warm_start_equals_oracle(gpu, kernel):
     """Warm start (the pressure carried across steps, including through the blocked kernel's
     second buffer) follows the oracle bit for bit, and stays within the tolerance."""
@@ -257,7 +261,8 @@ def test_graphs_and_autotune_do_not_change_results(gpu):
 
 
 @pytest.mark.parametrize("depth,check,rows", [(6, 6, 2), (4, 6, 2), (2, 5, 2), (6, 1, 2), (4, 6, 4),
-                                              (6, 6, 2 | smk.SWEEP_YCLUSTER)])
+                                              (6, 6, 2 | smk.SWEEP_YCLUSTER),
+                                              (6, 6, 2 | smk.SWEEP_YCLUSTER | smk.SWEEP_YCLUSTER_N(2))])
 def test_device_group_loop_equals_unrolled_and_direct(gpu, depth, check, rows):
     """The graph's device-side WHILE loop over tolerance groups gives the bits, sweep counts,
     residuals and divergence of the unrolled graph and of direct launches, with stage timing on
@@ -378,9 +383,34 @@ def test_jacobi_solver_equals_oracle(gpu, tol, warm):
 
 
 def test_ycluster_sweep_rejects_tall_grids(gpu):
-    """The y-cluster form needs one cluster to span y (ny <= 256)."""
+    """The y-cluster form with one cluster spanning y needs ny <= 256; clusters of 2 or 4 CTAs
+    take any height, and other cluster sizes are rejected."""
     sc = S.small_scene(8, 300, 8, steps=1, seed=3, scheme=1, iterations=6)
     sim = smk.from_scene(sc)
     with pytest.raises(smk.SmokeError):
         sim.set_sweep_kernel(6, 17, 2 | smk.SWEEP_YCLUSTER)
+    for n in (2, 4):
+        sim.set_sweep_kernel(6, 17, 2 | smk.SWEEP_YCLUSTER | smk.SWEEP_YCLUSTER_N(n))
+    for n in (1, 3, 8):
+        with pytest.raises(smk.SmokeError):
+            sim.set_sweep_kernel(6, 17, 2 | smk.SWEEP_YCLUSTER | smk.SWEEP_YCLUSTER_N(n))
+    sim.close()
+
+
+@pytest.mark.parametrize("n", [2, 4])
+def test_ycluster_runs_equal_oracle_on_tall_grid(gpu, n):
+    """Clusters of 2 and of 4 CTAs on a grid several clusters tall (140 rows: 3 clusters of 2,
+    2 clusters of 4), so the halo at the ends of each cluster's rows and the exchange between the
+    CTAs of a cluster both decide cells of the result: bit-exact with the oracle."""
+    sc = S.small_scene(20, 140, 18, steps=4, seed=61, scheme=1, iterations=48, tol=1e-3,
+                       check_every=6, obstacles=2, warm_start=1)
+    o = O.OracleSim(sc)
+    sim = smk.from_scene(sc, report_div=1)
+    sim.set_sweep_kernel(6, 7, 2 | smk.SWEEP_YCLUSTER | smk.SWEEP_YCLUSTER_N(n))
+    for k in range(sc.steps):
+        ost = o.step()
+        sim.step(sc.dt)
+        st = sim.stats()
+        assert st.sweeps == ost.sweeps and st.resid_max == ost.resid_max and st.div_max == ost.div_max
+        assert H.first_mismatch(sim.read_state(), H.oracle_state(o)) == "", k
     sim.close()
