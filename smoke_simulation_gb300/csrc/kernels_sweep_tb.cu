@@ -185,6 +185,23 @@ __device__ __forceinline__ void st_cluster(uint32_t addr, float v) {
     asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(addr), "f"(v) : "memory");
 }
 
+// Windows along an axis of n cells, W cells wide with a T-cell halo.  A side of a window that
+// reaches the grid's first or last cell needs no halo: those cells (the boundary ring) and every
+// cell outside the grid are never projectable, so they never change, and a wrong value beyond
+// the window (a zero padding row, a shuffle that wrapped) only ever enters their own update,
+// which keeps their value.  So the first window starts at cell 0 and owns W - T cells, the middle
+// ones start T cells before the cells they own and own W - 2T, and the last owns the rest (at most
+// W - T, its window reaching the last cell); one window owns everything when n <= W.
+__host__ __device__ inline int edge_windows(int n, int W, int T) {
+    if (n <= W) return 1;
+    const int rest = n - 2 * (W - T);
+    return 2 + (rest > 0 ? (rest + W - 2 * T - 1) / (W - 2 * T) : 0);
+}
+// First cell owned by window k; window k starts there (k = 0) or T cells before it.
+__host__ __device__ inline int edge_window_lo(int k, int W, int T) {
+    return k == 0 ? 0 : (W - T) + (k - 1) * (W - 2 * T);
+}
+
 // One tile (bx, by, bz) of a blocked launch: the CTA's whole job.  `group` is absolute.
 // GLOBAL_MAPS: the tensor maps are in global memory (grouped launches), not kernel parameters.
 // YCLUSTER: runs of `ycl_n` CTAs along y (blockIdx.y / ycl_n = the run, blockIdx.y % ycl_n = the
@@ -205,9 +222,6 @@ __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, fl
     constexpr int L = PY - 1;                // last row of the patch
     constexpr int R = T + 4;                 // register ring length (even, >= T + 3)
     constexpr int TB_S = R / 2;              // TMA stages (planes in flight)
-    constexpr int IX = 2 * TB_TX - 2 * T;    // interior columns
-    constexpr int HY = T;                    // halo rows in y (not YCLUSTER)
-    constexpr int IY = ROWS - 2 * HY;        // interior rows (not YCLUSTER)
     const int yrank = YCLUSTER ? by % ycl_n : 0;  // rank in the cluster (clusters run along y)
     extern __shared__ __align__(128) unsigned char smem_raw[];
     // TMA destinations must be 128-byte aligned: align the dynamic base explicitly (the launch
@@ -256,9 +270,15 @@ __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, fl
     }
     if (pcur != nullptr && first_tile && leader) *pcur = out_idx;
 
-    const int X0 = bx * IX - T;   // even; first tile column
-    // even; first tile row
-    const int Y0 = YCLUSTER ? (by / ycl_n) * (ycl_n * ROWS - 2 * ycl_hy) - ycl_hy + yrank * ROWS : by * IY - HY;
+    // owned columns [xlo, xhi) and rows [ylo, yhi) of the grid; X0, Y0 (even) = the window's
+    // first column and row (edge_windows)
+    const int xlo = edge_window_lo(bx, 2 * TB_TX, T);
+    const int xhi = bx + 1 < edge_windows(g.nx, 2 * TB_TX, T) ? edge_window_lo(bx + 1, 2 * TB_TX, T) : g.nx;
+    const int X0 = bx == 0 ? 0 : xlo - T;
+    const int ylo = YCLUSTER ? 0 : edge_window_lo(by, ROWS, T);
+    const int yhi = YCLUSTER ? 0 : (by + 1 < edge_windows(g.ny, ROWS, T) ? edge_window_lo(by + 1, ROWS, T) : g.ny);
+    const int Y0 = YCLUSTER ? (by / ycl_n) * (ycl_n * ROWS - 2 * ycl_hy) - ycl_hy + yrank * ROWS
+                            : (by == 0 ? 0 : ylo - T);
     const int xf = X0 - (X0 & 3);             // 16-byte aligned float box start
     const int xb = X0 - (X0 & 15);            // 16-byte aligned flag box start
     const int of = X0 - xf + 2 * tx;          // this thread's column in the float box
@@ -267,17 +287,19 @@ __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, fl
     const int y0 = Y0 + PY * ty;
     const int za = bz * zchunk;
     const int zb = min(za + zchunk, g.nz);
-    const bool inx = (2 * tx >= T) && (2 * tx < T + IX) && x0 < g.nx;
-    bool in[PY];  // row r of the patch is an interior row of the tile inside the grid
+    const bool inx = x0 >= xlo && x0 < xhi;
+    bool in[PY];  // row r of the patch is a row this tile owns, inside the grid
 #pragma unroll
     for (int r = 0; r < PY; ++r)
         in[r] = inx &&
                 (YCLUSTER ? (yrank * ROWS + PY * ty + r >= ycl_hy && yrank * ROWS + PY * ty + r < ycl_n * ROWS - ycl_hy)
-                          : (PY * ty + r >= HY && PY * ty + r < HY + IY)) &&
+                          : (y0 + r >= ylo && y0 + r < yhi)) &&
                 y0 + r >= 0 && y0 + r < g.ny;
     const int off0 = x0 + g.X * y0;
 
-    const int qbeg = za - T;
+    // planes below 0 are never projectable: a chunk near z = 0 starts at plane 0 (the ring's
+    // zero-initialised slots stand for the planes below, as the zero-filled loads did)
+    const int qbeg = max(za - T, 0);
     const int qend = zb + T;
     const int nouter = (qend - qbeg + R) / R;
     const int qfinal = qbeg + nouter * R - 1;  // last iteration executed
@@ -686,8 +708,7 @@ int launch_tb(const TBMaps& maps, const Grid& g, float* Pout, int nhalf, int col
     WAcc8 wa;
     for (int k = 0; k < 7; ++k) wa.w[k] = wacc7[k];
     wa.w[7] = 0.0f;
-    constexpr int IX = 2 * TB_TX - 2 * T, IY = G::ROWS - 2 * T;
-    dim3 grid((unsigned)((g.nx + IX - 1) / IX), (unsigned)((g.ny + IY - 1) / IY),
+    dim3 grid((unsigned)edge_windows(g.nx, 2 * TB_TX, T), (unsigned)edge_windows(g.ny, G::ROWS, T),
               (unsigned)((g.nz + zchunk - 1) / zchunk));
     k_sweep_tb<T, PY><<<grid, dim3(TB_TX, G::TY), smem, st>>>(maps, g, Pout, nhalf, colour0, zchunk, wa,
                                                              status, check, group, tol, pcur, out_idx,
@@ -719,9 +740,9 @@ inline bool ycl_geom(const Grid& g, int n_req, YclGeom* o) {
 }
 
 cudaLaunchConfig_t ycl_config(const Grid& g, const YclGeom& y, int zchunk, cudaLaunchAttribute* attr) {
-    constexpr int IX = 2 * TB_TX - 2 * YCL_DEPTH;
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)((g.nx + IX - 1) / IX), (unsigned)y.grid_y, (unsigned)((g.nz + zchunk - 1) / zchunk));
+    cfg.gridDim = dim3((unsigned)edge_windows(g.nx, 2 * TB_TX, YCL_DEPTH), (unsigned)y.grid_y,
+                       (unsigned)((g.nz + zchunk - 1) / zchunk));
     cfg.blockDim = dim3(TB_TX, TBGeom<2>::TY);
     cfg.dynamicSmemBytes = tb_smem_bytes<YCL_DEPTH, 2>();
     attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -845,7 +866,6 @@ size_t group_tb_record_bytes() { return sizeof(GroupTBGrid); }
 int group_tb_fill(void* rec, const SweepMaps* m, const Grid& g, float* P, float* P2, StepStatus* status, int* pcur,
                   int* kerr, const float* wacc7, float tol, int zchunk) {
     constexpr int T = GROUP_TB_DEPTH;
-    constexpr int IX = 2 * TB_TX - 2 * T, IY = TBGeom<2>::ROWS - 2 * T;
     GroupTBGrid d;
     memset(&d, 0, sizeof(d));
     d.maps[0].pin = m->pa[0];
@@ -861,8 +881,8 @@ int group_tb_fill(void* rec, const SweepMaps* m, const Grid& g, float* P, float*
     for (int k = 0; k < 7; ++k) d.wa.w[k] = wacc7[k];
     d.wa.w[7] = 0.0f;
     d.tol = tol;
-    d.tiles_x = (g.nx + IX - 1) / IX;
-    d.tiles_y = (g.ny + IY - 1) / IY;
+    d.tiles_x = edge_windows(g.nx, 2 * TB_TX, T);
+    d.tiles_y = edge_windows(g.ny, TBGeom<2>::ROWS, T);
     d.zchunks = (g.nz + zchunk - 1) / zchunk;
     memcpy(rec, &d, sizeof(d));
     return d.tiles_x * d.tiles_y * d.zchunks;
