@@ -175,6 +175,9 @@ void fill_record(smk_sim* s, float dt, TableImage& t, GroupGrid& d) {
     d.check_every = p.check_every > 0 ? p.check_every : 1;
     d.max_sweeps = p.max_sweeps;
     d.warm = p.warm_start;
+    // the 4-wide forcing, rhs and subtract bodies (FP32 storage; as the single-grid launchers)
+    d.vec4 = d.kind == GK_F32 &&
+             vec4_layout(s->g, {d.u_now, d.v_now, d.w_now, d.rho_now, d.P, d.P2, d.b}, d.flags);
 
     // emitters: boxes clipped to the grid (as the single-grid launcher does), then spheres
     const Grid& g = s->g;

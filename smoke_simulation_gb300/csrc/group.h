@@ -73,6 +73,7 @@ struct GroupGrid {
     int sx0, sy0, sz0, sx1, sy1, sz1;  // region of the spheres (interior, one cell margin)
     int ox0, oy0, oz0, ox1, oy1, oz1;  // union of both: the objects stage's tiles
     int wave;  // solve wave: waves run one after another, each to completion
+    int vec4;  // FP32 storage with 16-byte aligned rows: forcing, rhs and subtract take the 4-wide bodies
 };
 
 // Grid barrier of the cooperative projection kernel (reset before every launch).
@@ -152,15 +153,47 @@ __host__ __device__ inline void group_extent(int stage, const GroupGrid& d, int&
     }
 }
 
+// Advection tiles walk GROUP_ADV_ZC consecutive planes (as the single-grid advection kernels).
+constexpr int GROUP_ADV_ZC = 4;
+
+// 4-wide tiles (grids with vec4): 16 groups of 4 consecutive x by 16 rows of one plane, over
+// gx groups (from x = 0), ry rows and rz planes.
+constexpr int GX4_GX = 16, GX4_GY = 16;
+__host__ __device__ inline int group_x4_tiles(int gx, int ry, int rz) {
+    if (gx <= 0 || ry <= 0 || rz <= 0) return 0;
+    return group_div_up(gx, GX4_GX) * group_div_up(ry, GX4_GY) * rz;
+}
+// Range of a 4-wide stage: groups of x, rows (from y0) and planes (from z0).
+__host__ __device__ inline bool group_x4_extent(int stage, const GroupGrid& d, int& gx, int& ry, int& rz, int& y0,
+                                                int& z0) {
+    if (d.kind != GK_F32 || !d.vec4) return false;
+    const Grid& g = d.g;
+    gx = group_div_up(g.nx, 4);
+    switch (stage) {
+        case GS_FORCE: ry = g.ny - 1; rz = g.nz; y0 = 1; z0 = 0; return true;
+        case GS_RHS: ry = g.ny; rz = g.nz; y0 = 0; z0 = 0; return true;
+        case GS_PROJECT: ry = g.ny - 1; rz = g.nz - 1; y0 = 1; z0 = 1; return true;
+        default: return false;
+    }
+}
+
 // Tiles of a stage for one grid; the flattened stages cut the interior planes into slabs of
 // `zslab` planes.
 __host__ __device__ inline int group_tiles(int stage, const GroupGrid& d, int zslab) {
     const Grid& g = d.g;
     const int slabs = g.nz >= 3 ? group_div_up(g.nz - 2, zslab) : 0;
+    int gx, ry4, rz4, y0, z0;
+    if (group_x4_extent(stage, d, gx, ry4, rz4, y0, z0)) return group_x4_tiles(gx, ry4, rz4);
     switch (stage) {
         case GS_SWEEP: return group_sweep_tpp(g) * slabs;
         case GS_RESID: return group_interior_tpp(g) * slabs;
         case GS_DIV: return d.report_div ? group_interior_tpp(g) * slabs : 0;
+        case GS_ADV_VEL:
+        case GS_ADV_RHO: {
+            int rx, ry, rz;
+            group_extent(stage, d, rx, ry, rz);
+            return group_block_tiles(rx, ry, group_div_up(rz, GROUP_ADV_ZC));
+        }
         default: {
             int rx, ry, rz;
             group_extent(stage, d, rx, ry, rz);

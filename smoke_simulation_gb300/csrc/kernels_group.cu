@@ -48,6 +48,15 @@ __device__ __forceinline__ uint3 tile_bid(int local, int rx, int ry) {
     return b;
 }
 
+// Group of 4 x, row and plane of this thread in tile `local` of a 4-wide stage (group_x4_tiles).
+__device__ __forceinline__ void x4_coords(int local, int gx, int ry, int y0, int z0, int& x, int& y, int& z) {
+    const int nbx = group_div_up(gx, GX4_GX), nby = group_div_up(ry, GX4_GY);
+    const int t = tid256();
+    x = 4 * ((local % nbx) * GX4_GX + t % GX4_GX);
+    y = y0 + ((local / nbx) % nby) * GX4_GY + t / GX4_GX;
+    z = z0 + local / (nbx * nby);
+}
+
 // f(j, local) for every tile of `stage` this CTA owns (grid-stride over the batch's tiles).
 // With `mask` (shared memory, one byte per grid), grids whose byte has none of the bits
 // `need` are skipped as a whole.  j is uniform over the CTA, so f may contain block barriers.
@@ -106,6 +115,14 @@ __global__ void __launch_bounds__(GROUP_TILE) k_group_forcing(const GroupArgs a)
     for_tiles(a, GS_FORCE, nullptr, 0, [&](int j, int local) {
         const GroupGrid& d = a.grids[j];
         const Grid gg = d.g;  // in registers: the stores of the body cannot alias it
+        int gx, ry, rz, y0, z0;
+        if (group_x4_extent(GS_FORCE, d, gx, ry, rz, y0, z0)) {
+            int x, y, z;
+            x4_coords(local, gx, ry, y0, z0, x, y, z);
+            body_forcing_x4(gg, (float*)d.u_now, (float*)d.v_now, (float*)d.w_now, (const float*)d.rho_now, d.flags,
+                            d.dt, d.gravity, d.alpha, d.lim_sq, d.lim, d.clamp_mode, x, y, z);
+            return;
+        }
         const uint3 bid = tile_bid(local, d.g.nx, d.g.ny - 1);
         typedef __nv_bfloat16 h;
         if (d.kind == GK_BF16)
@@ -121,37 +138,48 @@ __global__ void __launch_bounds__(GROUP_TILE) k_group_forcing(const GroupArgs a)
     });
 }
 
-__global__ void __launch_bounds__(GROUP_TILE) k_group_adv_vel(const GroupArgs a) {
+// The advection tiles walk GROUP_ADV_ZC consecutive planes (the planes neighbouring cells'
+// averages and samples share stay in L1); register caps of 5 (velocity: 48 registers, no
+// spills) and 8 (density) CTAs per SM.
+__global__ void __launch_bounds__(GROUP_TILE, 5) k_group_adv_vel(const GroupArgs a) {
     for_tiles(a, GS_ADV_VEL, nullptr, 0, [&](int j, int local) {
         const GroupGrid& d = a.grids[j];
         const Grid gg = d.g;  // in registers: the stores of the body cannot alias it
         const uint3 bid = tile_bid(local, d.g.nx - 1, d.g.ny - 1);
         typedef __nv_bfloat16 h;
-        if (d.kind == GK_F32)
-            body_advect_velocity<float, float>(gg, d.pu, d.pv, d.pw, (float*)d.u_past, (float*)d.v_past,
-                                               (float*)d.w_past, d.flags, d.dt, bid);
-        else
-            body_advect_velocity<float, h>(gg, d.pu, d.pv, d.pw, (h*)d.u_past, (h*)d.v_past, (h*)d.w_past,
-                                           d.flags, d.dt, bid);
+        for (int k = 0; k < GROUP_ADV_ZC; ++k) {
+            const uint3 b = make_uint3(bid.x, bid.y, bid.z * GROUP_ADV_ZC + k);
+            if ((int)b.z >= d.g.nz - 1) break;
+            if (d.kind == GK_F32)
+                body_advect_velocity<float, float>(gg, d.pu, d.pv, d.pw, (float*)d.u_past, (float*)d.v_past,
+                                                   (float*)d.w_past, d.flags, d.dt, b);
+            else
+                body_advect_velocity<float, h>(gg, d.pu, d.pv, d.pw, (h*)d.u_past, (h*)d.v_past, (h*)d.w_past,
+                                               d.flags, d.dt, b);
+        }
     });
 }
 
-__global__ void __launch_bounds__(GROUP_TILE) k_group_adv_rho(const GroupArgs a) {
+__global__ void __launch_bounds__(GROUP_TILE, 8) k_group_adv_rho(const GroupArgs a) {
     for_tiles(a, GS_ADV_RHO, nullptr, 0, [&](int j, int local) {
         const GroupGrid& d = a.grids[j];
         const Grid gg = d.g;  // in registers: the stores of the body cannot alias it
         const uint3 bid = tile_bid(local, d.g.nx - 2, d.g.ny - 2);
         typedef __nv_bfloat16 h;
-        if (d.kind == GK_BF16)
-            body_advect_density<h, h>(gg, (const h*)d.rho_now, (h*)d.rho_past, (const h*)d.u_past,
-                                      (const h*)d.v_past, (const h*)d.w_past, d.flags, d.dt, bid);
-        else if (d.kind == GK_BF16_VEL)
-            body_advect_density<float, h>(gg, (const float*)d.rho_now, (float*)d.rho_past, (const h*)d.u_past,
-                                          (const h*)d.v_past, (const h*)d.w_past, d.flags, d.dt, bid);
-        else
-            body_advect_density<float, float>(gg, (const float*)d.rho_now, (float*)d.rho_past,
-                                              (const float*)d.u_past, (const float*)d.v_past,
-                                              (const float*)d.w_past, d.flags, d.dt, bid);
+        for (int k = 0; k < GROUP_ADV_ZC; ++k) {
+            const uint3 b = make_uint3(bid.x, bid.y, bid.z * GROUP_ADV_ZC + k);
+            if ((int)b.z >= d.g.nz - 2) break;
+            if (d.kind == GK_BF16)
+                body_advect_density<h, h>(gg, (const h*)d.rho_now, (h*)d.rho_past, (const h*)d.u_past,
+                                          (const h*)d.v_past, (const h*)d.w_past, d.flags, d.dt, b);
+            else if (d.kind == GK_BF16_VEL)
+                body_advect_density<float, h>(gg, (const float*)d.rho_now, (float*)d.rho_past, (const h*)d.u_past,
+                                              (const h*)d.v_past, (const h*)d.w_past, d.flags, d.dt, b);
+            else
+                body_advect_density<float, float>(gg, (const float*)d.rho_now, (float*)d.rho_past,
+                                                  (const float*)d.u_past, (const float*)d.v_past,
+                                                  (const float*)d.w_past, d.flags, d.dt, b);
+        }
     });
 }
 
@@ -259,6 +287,14 @@ __global__ void __launch_bounds__(GROUP_TILE) k_group_project(const GroupArgs a)
         for_tiles(a, GS_RHS, nullptr, 0, [&](int j, int local) {
             const GroupGrid& d = a.grids[j];
             const Grid gg = d.g;  // in registers: the stores of the body cannot alias it
+            int gx, ry, rz, y0, z0;
+            if (group_x4_extent(GS_RHS, d, gx, ry, rz, y0, z0)) {
+                int x, y, z;
+                x4_coords(local, gx, ry, y0, z0, x, y, z);
+                body_rhs_x4(gg, (const float*)d.u_now, (const float*)d.v_now, (const float*)d.w_now, d.flags, d.b,
+                            d.P, d.P2, d.pcur, d.warm, x, y, z);
+                return;
+            }
             const uint3 bid = tile_bid(local, d.g.nx, d.g.ny);
             if (d.kind == GK_F32)
                 body_rhs<float>(gg, (const float*)d.u_now, (const float*)d.v_now, (const float*)d.w_now, d.flags,
@@ -376,7 +412,14 @@ __global__ void __launch_bounds__(GROUP_TILE) k_group_project(const GroupArgs a)
     for_tiles(a, GS_PROJECT, nullptr, 0, [&](int j, int local) {
         const GroupGrid& d = a.grids[j];
         const Grid gg = d.g;  // in registers: the stores of the body cannot alias it
-        int rx, ry, rz;
+        int gx, y0, z0, rx, ry, rz;
+        if (group_x4_extent(GS_PROJECT, d, gx, ry, rz, y0, z0)) {
+            int x, y, z;
+            x4_coords(local, gx, ry, y0, z0, x, y, z);
+            const float* P = (d.pcur != nullptr && *d.pcur == 1) ? d.P2 : d.P;
+            body_gradient_subtract_x4(gg, (float*)d.u_now, (float*)d.v_now, (float*)d.w_now, P, d.flags, x, y, z);
+            return;
+        }
         group_extent(GS_PROJECT, d, rx, ry, rz);
         const uint3 bid = tile_bid(local, rx, ry);
         if (d.kind == GK_F32)

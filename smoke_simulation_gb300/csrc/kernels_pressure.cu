@@ -35,112 +35,25 @@ __global__ void k_rhs(Grid g, const T* __restrict__ u, const T* __restrict__ v,
     body_rhs(g, u, v, w, flags, b, P, P2, pcur, warm, blockIdx);
 }
 
-// FP32 rhs with four consecutive x per thread (16-byte loads and stores); groups not entirely
-// inside [0, nx) take the per-cell body.  Same expressions as body_rhs.
+// FP32 rhs with four consecutive x per thread (16-byte loads and stores; body_rhs_x4).
 __global__ void __launch_bounds__(256) k_rhs_x4(Grid g, const float* __restrict__ u, const float* __restrict__ v,
                                                 const float* __restrict__ w, const uint8_t* __restrict__ flags,
                                                 float* __restrict__ b, float* __restrict__ P,
                                                 const float* __restrict__ P2, const int* __restrict__ pcur,
                                                 int warm) {
-    const int x0 = 4 * ((int)blockIdx.x * 32 + (int)threadIdx.x);
-    const int y = (int)blockIdx.y * 8 + (int)threadIdx.y;
-    const int z = (int)blockIdx.z;
-    if (x0 >= g.nx || y >= g.ny) return;
-    const int i = g.idx(x0, y, z);
-    const bool from2 = warm && pcur != nullptr && P2 != nullptr && *pcur == 1;
-    if (x0 + 3 < g.nx) {
-        const uchar4 f = *reinterpret_cast<const uchar4*>(flags + i);
-        const float4 u0 = *reinterpret_cast<const float4*>(u + i);
-        const float u4 = u[i + 4];  // x0 + 4 <= nx: a face of the same row
-        const float4 v0 = *reinterpret_cast<const float4*>(v + i);
-        const float4 v1 = *reinterpret_cast<const float4*>(v + i + g.X);
-        const float4 w0 = *reinterpret_cast<const float4*>(w + i);
-        const float4 w1 = *reinterpret_cast<const float4*>(w + i + g.XY);
-        const bool p0 = (f.x & F_PROJ) != 0, p1 = (f.y & F_PROJ) != 0, p2 = (f.z & F_PROJ) != 0,
-                   p3 = (f.w & F_PROJ) != 0;
-        const float d0 = -u0.x + u0.y + -v0.x + v1.x + -w0.x + w1.x;
-        const float d1 = -u0.y + u0.z + -v0.y + v1.y + -w0.y + w1.y;
-        const float d2 = -u0.z + u0.w + -v0.z + v1.z + -w0.z + w1.z;
-        const float d3 = -u0.w + u4 + -v0.w + v1.w + -w0.w + w1.w;
-        *reinterpret_cast<float4*>(b + i) =
-            make_float4(p0 ? -d0 : 0.0f, p1 ? -d1 : 0.0f, p2 ? -d2 : 0.0f, p3 ? -d3 : 0.0f);
-        if (!warm) {
-            *reinterpret_cast<float4*>(P + i) = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        } else if (from2) {
-            const float4 q = *reinterpret_cast<const float4*>(P2 + i);
-            *reinterpret_cast<float4*>(P + i) =
-                make_float4(p0 ? q.x : 0.0f, p1 ? q.y : 0.0f, p2 ? q.z : 0.0f, p3 ? q.w : 0.0f);
-        } else {
-            if (!p0) P[i] = 0.0f;
-            if (!p1) P[i + 1] = 0.0f;
-            if (!p2) P[i + 2] = 0.0f;
-            if (!p3) P[i + 3] = 0.0f;
-        }
-        return;
-    }
-    for (int c = 0; c < 4 && x0 + c < g.nx; ++c) {
-        const int k = i + c;
-        const float div = -u[k] + u[k + 1] + -v[k] + v[k + g.X] + -w[k] + w[k + g.XY];
-        const bool proj = (flags[k] & F_PROJ) != 0;
-        b[k] = proj ? -div : 0.0f;
-        if (!proj || !warm) P[k] = 0.0f;
-        else if (from2) P[k] = P2[k];
-    }
+    body_rhs_x4(g, u, v, w, flags, b, P, P2, pcur, warm, 4 * ((int)blockIdx.x * 32 + (int)threadIdx.x),
+                (int)blockIdx.y * 8 + (int)threadIdx.y, (int)blockIdx.z);
 }
 
-// FP32 gradient subtract with four consecutive x per thread; groups not entirely inside
-// [1, nx) take the per-face path.  Same expressions as body_gradient_subtract (every face of the
-// range is stored, unchanged ones with their own value).
+// FP32 gradient subtract with four consecutive x per thread (body_gradient_subtract_x4).
 __global__ void __launch_bounds__(256) k_gradient_subtract_x4(Grid g, float* __restrict__ u, float* __restrict__ v,
                                                               float* __restrict__ w, const float* __restrict__ P0,
                                                               const float* __restrict__ P1,
                                                               const int* __restrict__ pcur,
                                                               const uint8_t* __restrict__ flags) {
     const float* P = (pcur != nullptr && *pcur == 1) ? P1 : P0;
-    const int x0 = 4 * ((int)blockIdx.x * 32 + (int)threadIdx.x);
-    const int y = 1 + (int)blockIdx.y * 8 + (int)threadIdx.y;
-    const int z = 1 + (int)blockIdx.z;
-    if (x0 >= g.nx || y >= g.ny) return;
-    const int i = g.idx(x0, y, z);
-    const bool iny = y <= g.ny - 2, inz = z <= g.nz - 2;
-    if (x0 >= 1 && x0 + 3 <= g.nx - 1) {
-        const uchar4 f = *reinterpret_cast<const uchar4*>(flags + i);
-        const float4 pc = *reinterpret_cast<const float4*>(P + i);
-        const float pxm = P[i - 1];
-        const float4 py = *reinterpret_cast<const float4*>(P + i - g.X);
-        const float4 pz = *reinterpret_cast<const float4*>(P + i - g.XY);
-        float4 uu = *reinterpret_cast<const float4*>(u + i);
-        float4 vv = *reinterpret_cast<const float4*>(v + i);
-        float4 ww = *reinterpret_cast<const float4*>(w + i);
-        const float pcs[4] = {pc.x, pc.y, pc.z, pc.w}, pxs[4] = {pxm, pc.x, pc.y, pc.z},
-                    pys[4] = {py.x, py.y, py.z, py.w}, pzs[4] = {pz.x, pz.y, pz.z, pz.w};
-        const uint8_t fs[4] = {f.x, f.y, f.z, f.w};
-        float us[4] = {uu.x, uu.y, uu.z, uu.w}, vs[4] = {vv.x, vv.y, vv.z, vv.w}, ws[4] = {ww.x, ww.y, ww.z, ww.w};
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-            const bool self = (fs[c] & F_SELF) != 0;
-            const bool inx = x0 + c <= g.nx - 2;
-            if (self && iny && inz && (fs[c] & F_XM)) us[c] = us[c] - (pcs[c] - pxs[c]);
-            if (self && inx && inz && (fs[c] & F_YM)) vs[c] = vs[c] - (pcs[c] - pys[c]);
-            if (self && inx && iny && (fs[c] & F_ZM)) ws[c] = ws[c] - (pcs[c] - pzs[c]);
-        }
-        *reinterpret_cast<float4*>(u + i) = make_float4(us[0], us[1], us[2], us[3]);
-        *reinterpret_cast<float4*>(v + i) = make_float4(vs[0], vs[1], vs[2], vs[3]);
-        *reinterpret_cast<float4*>(w + i) = make_float4(ws[0], ws[1], ws[2], ws[3]);
-        return;
-    }
-    for (int c = 0; c < 4; ++c) {
-        const int x = x0 + c;
-        if (x < 1 || x >= g.nx) continue;
-        const int k = i + c;
-        const uint8_t f = flags[k];
-        const bool self = (f & F_SELF) != 0;
-        const bool inx = x <= g.nx - 2;
-        const float pc = P[k];
-        if (self && iny && inz && (f & F_XM)) u[k] = u[k] - (pc - P[k - 1]);
-        if (self && inx && inz && (f & F_YM)) v[k] = v[k] - (pc - P[k - g.X]);
-        if (self && inx && iny && (f & F_ZM)) w[k] = w[k] - (pc - P[k - g.XY]);
-    }
+    body_gradient_subtract_x4(g, u, v, w, P, flags, 4 * ((int)blockIdx.x * 32 + (int)threadIdx.x),
+                              1 + (int)blockIdx.y * 8 + (int)threadIdx.y, 1 + (int)blockIdx.z);
 }
 
 __global__ void k_gradient_subtract(Grid g, float* __restrict__ u, float* __restrict__ v,

@@ -114,45 +114,14 @@ __global__ void k_forcing(Grid g, Tv* __restrict__ u, Tv* __restrict__ v, Tv* __
     body_forcing(g, u, v, w, rho, flags, dt, gravity, alpha, lim_sq, lim, clamp_mode, blockIdx);
 }
 
-// FP32 forcing with four consecutive x per thread (16-byte loads and stores; a group's faces
-// that do not change are stored back unchanged).  Groups not entirely inside [0, nx) take the
-// per-face path.  Same arithmetic as body_forcing (cell_forcing).
+// FP32 forcing with four consecutive x per thread (16-byte loads and stores; body_forcing_x4).
 __global__ void __launch_bounds__(256) k_forcing_x4(Grid g, float* __restrict__ u, float* __restrict__ v,
                                                     float* __restrict__ w, const float* __restrict__ rho,
                                                     const uint8_t* __restrict__ flags, float dt, float gravity,
                                                     float alpha, float lim_sq, float lim, int clamp_mode) {
-    const int x0 = 4 * ((int)blockIdx.x * 32 + (int)threadIdx.x);
-    const int y = 1 + (int)blockIdx.y * 8 + (int)threadIdx.y;
-    const int z = (int)blockIdx.z;
-    if (x0 >= g.nx || y >= g.ny) return;
-    const int i = g.idx(x0, y, z);
-    if (x0 + 3 < g.nx) {
-        const uchar4 f = *reinterpret_cast<const uchar4*>(flags + i);
-        float4 uu = *reinterpret_cast<const float4*>(u + i);
-        float4 vv = *reinterpret_cast<const float4*>(v + i);
-        float4 ww = *reinterpret_cast<const float4*>(w + i);
-        const float4 r = *reinterpret_cast<const float4*>(rho + i);
-        unsigned wr = cell_forcing(f.x, x0, z, r.x, uu.x, vv.x, ww.x, dt, gravity, alpha, lim_sq, lim, clamp_mode);
-        wr |= cell_forcing(f.y, x0 + 1, z, r.y, uu.y, vv.y, ww.y, dt, gravity, alpha, lim_sq, lim, clamp_mode);
-        wr |= cell_forcing(f.z, x0 + 2, z, r.z, uu.z, vv.z, ww.z, dt, gravity, alpha, lim_sq, lim, clamp_mode);
-        wr |= cell_forcing(f.w, x0 + 3, z, r.w, uu.w, vv.w, ww.w, dt, gravity, alpha, lim_sq, lim, clamp_mode);
-        if (wr & 1u) *reinterpret_cast<float4*>(v + i) = vv;
-        if (wr & 2u) {
-            *reinterpret_cast<float4*>(u + i) = uu;
-            *reinterpret_cast<float4*>(w + i) = ww;
-        }
-        return;
-    }
-    for (int c = 0; c < 4 && x0 + c < g.nx; ++c) {
-        float ut = u[i + c], vt = v[i + c], wt = w[i + c];
-        const unsigned wr = cell_forcing(flags[i + c], x0 + c, z, rho[i + c], ut, vt, wt, dt, gravity, alpha, lim_sq,
-                                         lim, clamp_mode);
-        if (wr & 2u) {
-            u[i + c] = ut;
-            w[i + c] = wt;
-        }
-        if (wr & 1u) v[i + c] = vt;
-    }
+    body_forcing_x4(g, u, v, w, rho, flags, dt, gravity, alpha, lim_sq, lim, clamp_mode,
+                    4 * ((int)blockIdx.x * 32 + (int)threadIdx.x), 1 + (int)blockIdx.y * 8 + (int)threadIdx.y,
+                    (int)blockIdx.z);
 }
 
 // ---- d (reference scheme): divergence kernel (smokeSimulation.cu:356-394) ------------------

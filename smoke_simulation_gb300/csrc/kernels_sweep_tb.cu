@@ -189,17 +189,34 @@ __device__ __forceinline__ void st_cluster(uint32_t addr, float v) {
 // reaches the grid's first or last cell needs no halo: those cells (the boundary ring) and every
 // cell outside the grid are never projectable, so they never change, and a wrong value beyond
 // the window (a zero padding row, a shuffle that wrapped) only ever enters their own update,
-// which keeps their value.  So the first window starts at cell 0 and owns W - T cells, the middle
-// ones start T cells before the cells they own and own W - 2T, and the last owns the rest (at most
-// W - T, its window reaching the last cell); one window owns everything when n <= W.
+// which keeps their value.  So in the edge placement the first window starts at cell 0 and owns
+// W - T cells, the middle ones start T cells before the cells they own and own W - 2T, and the
+// last owns the rest (at most W - T, its window reaching the last cell); one window owns
+// everything when n <= W.  The plain placement gives every window a halo on both sides (window k
+// starts at k(W - 2T) - T).  The edge placement is used only where it needs fewer windows (small
+// grids): at equal counts the plain one measured faster (256^3: 136.7 against 139.7 us a launch).
 __host__ __device__ inline int edge_windows(int n, int W, int T) {
     if (n <= W) return 1;
     const int rest = n - 2 * (W - T);
     return 2 + (rest > 0 ? (rest + W - 2 * T - 1) / (W - 2 * T) : 0);
 }
-// First cell owned by window k; window k starts there (k = 0) or T cells before it.
-__host__ __device__ inline int edge_window_lo(int k, int W, int T) {
-    return k == 0 ? 0 : (W - T) + (k - 1) * (W - 2 * T);
+__host__ __device__ inline int plain_windows(int n, int W, int T) { return (n + W - 2 * T - 1) / (W - 2 * T); }
+__host__ __device__ inline int sweep_windows(int n, int W, int T) {
+    const int e = edge_windows(n, W, T), p = plain_windows(n, W, T);
+    return e < p ? e : p;
+}
+// Window k of sweep_windows(n, W, T): its first cell (even for even T) and the cells [lo, hi) it owns.
+__host__ __device__ inline void sweep_window(int n, int W, int T, int k, int& start, int& lo, int& hi) {
+    const int nw = sweep_windows(n, W, T);
+    if (edge_windows(n, W, T) < plain_windows(n, W, T)) {
+        lo = k == 0 ? 0 : (W - T) + (k - 1) * (W - 2 * T);
+        hi = k + 1 < nw ? (W - T) + k * (W - 2 * T) : n;
+        start = k == 0 ? 0 : lo - T;
+    } else {
+        lo = k * (W - 2 * T);
+        hi = k + 1 < nw ? lo + (W - 2 * T) : n;
+        start = lo - T;
+    }
 }
 
 // One tile (bx, by, bz) of a blocked launch: the CTA's whole job.  `group` is absolute.
@@ -271,14 +288,11 @@ __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, fl
     if (pcur != nullptr && first_tile && leader) *pcur = out_idx;
 
     // owned columns [xlo, xhi) and rows [ylo, yhi) of the grid; X0, Y0 (even) = the window's
-    // first column and row (edge_windows)
-    const int xlo = edge_window_lo(bx, 2 * TB_TX, T);
-    const int xhi = bx + 1 < edge_windows(g.nx, 2 * TB_TX, T) ? edge_window_lo(bx + 1, 2 * TB_TX, T) : g.nx;
-    const int X0 = bx == 0 ? 0 : xlo - T;
-    const int ylo = YCLUSTER ? 0 : edge_window_lo(by, ROWS, T);
-    const int yhi = YCLUSTER ? 0 : (by + 1 < edge_windows(g.ny, ROWS, T) ? edge_window_lo(by + 1, ROWS, T) : g.ny);
-    const int Y0 = YCLUSTER ? (by / ycl_n) * (ycl_n * ROWS - 2 * ycl_hy) - ycl_hy + yrank * ROWS
-                            : (by == 0 ? 0 : ylo - T);
+    // first column and row (sweep_window)
+    int X0, xlo, xhi, Yw, ylo = 0, yhi = 0;
+    sweep_window(g.nx, 2 * TB_TX, T, bx, X0, xlo, xhi);
+    if (!YCLUSTER) sweep_window(g.ny, ROWS, T, by, Yw, ylo, yhi);
+    const int Y0 = YCLUSTER ? (by / ycl_n) * (ycl_n * ROWS - 2 * ycl_hy) - ycl_hy + yrank * ROWS : Yw;
     const int xf = X0 - (X0 & 3);             // 16-byte aligned float box start
     const int xb = X0 - (X0 & 15);            // 16-byte aligned flag box start
     const int of = X0 - xf + 2 * tx;          // this thread's column in the float box
@@ -297,10 +311,11 @@ __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, fl
                 y0 + r >= 0 && y0 + r < g.ny;
     const int off0 = x0 + g.X * y0;
 
-    // planes below 0 are never projectable: a chunk near z = 0 starts at plane 0 (the ring's
-    // zero-initialised slots stand for the planes below, as the zero-filled loads did)
-    const int qbeg = max(za - T, 0);
+    // planes below 0 are never projectable: a chunk near z = 0 may start at plane 0 (the ring's
+    // zero-initialised slots stand for the planes below, as the zero-filled loads do), which it
+    // does where that saves a pass of the unrolled loop
     const int qend = zb + T;
+    const int qbeg = (za - T < 0 && (qend + R) / R < (qend - (za - T) + R) / R) ? 0 : za - T;
     const int nouter = (qend - qbeg + R) / R;
     const int qfinal = qbeg + nouter * R - 1;  // last iteration executed
 
@@ -708,7 +723,7 @@ int launch_tb(const TBMaps& maps, const Grid& g, float* Pout, int nhalf, int col
     WAcc8 wa;
     for (int k = 0; k < 7; ++k) wa.w[k] = wacc7[k];
     wa.w[7] = 0.0f;
-    dim3 grid((unsigned)edge_windows(g.nx, 2 * TB_TX, T), (unsigned)edge_windows(g.ny, G::ROWS, T),
+    dim3 grid((unsigned)sweep_windows(g.nx, 2 * TB_TX, T), (unsigned)sweep_windows(g.ny, G::ROWS, T),
               (unsigned)((g.nz + zchunk - 1) / zchunk));
     k_sweep_tb<T, PY><<<grid, dim3(TB_TX, G::TY), smem, st>>>(maps, g, Pout, nhalf, colour0, zchunk, wa,
                                                              status, check, group, tol, pcur, out_idx,
@@ -741,7 +756,7 @@ inline bool ycl_geom(const Grid& g, int n_req, YclGeom* o) {
 
 cudaLaunchConfig_t ycl_config(const Grid& g, const YclGeom& y, int zchunk, cudaLaunchAttribute* attr) {
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)edge_windows(g.nx, 2 * TB_TX, YCL_DEPTH), (unsigned)y.grid_y,
+    cfg.gridDim = dim3((unsigned)sweep_windows(g.nx, 2 * TB_TX, YCL_DEPTH), (unsigned)y.grid_y,
                        (unsigned)((g.nz + zchunk - 1) / zchunk));
     cfg.blockDim = dim3(TB_TX, TBGeom<2>::TY);
     cfg.dynamicSmemBytes = tb_smem_bytes<YCL_DEPTH, 2>();
@@ -881,8 +896,8 @@ int group_tb_fill(void* rec, const SweepMaps* m, const Grid& g, float* P, float*
     for (int k = 0; k < 7; ++k) d.wa.w[k] = wacc7[k];
     d.wa.w[7] = 0.0f;
     d.tol = tol;
-    d.tiles_x = edge_windows(g.nx, 2 * TB_TX, T);
-    d.tiles_y = edge_windows(g.ny, TBGeom<2>::ROWS, T);
+    d.tiles_x = sweep_windows(g.nx, 2 * TB_TX, T);
+    d.tiles_y = sweep_windows(g.ny, TBGeom<2>::ROWS, T);
     d.zchunks = (g.nz + zchunk - 1) / zchunk;
     memcpy(rec, &d, sizeof(d));
     return d.tiles_x * d.tiles_y * d.zchunks;

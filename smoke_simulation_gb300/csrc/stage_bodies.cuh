@@ -258,6 +258,144 @@ __device__ __forceinline__ void body_gradient_subtract(const Grid& g, float* u, 
     w[i] = (self && inx && iny && (f & F_ZM)) ? ww - (pc - pz) : ww;
 }
 
+// ---- four consecutive x per thread (FP32 storage, 16-byte aligned rows) ----------------------
+//
+// The thread's group is x0..x0+3 (x0 a multiple of 4) of row (y, z); a group not entirely inside
+// the stage's x range takes the per-element path.  Same expressions, in the same order, as the
+// per-cell bodies above, so every result is the same.  Plain pointers, as for the projection
+// bodies (the grouped projection runs the rhs and the subtract as phases of one launch).
+
+// Forcing (body_forcing, cell_forcing): a group's faces that do not change are stored back
+// unchanged.  Rows y >= 1.
+__device__ __forceinline__ void body_forcing_x4(const Grid& g, float* u, float* v, float* w, const float* rho,
+                                                const uint8_t* flags, float dt, float gravity, float alpha,
+                                                float lim_sq, float lim, int clamp_mode, int x0, int y, int z) {
+    if (x0 >= g.nx || y >= g.ny || z >= g.nz) return;
+    const int i = g.idx(x0, y, z);
+    if (x0 + 3 < g.nx) {
+        const uchar4 f = *reinterpret_cast<const uchar4*>(flags + i);
+        float4 uu = *reinterpret_cast<const float4*>(u + i);
+        float4 vv = *reinterpret_cast<const float4*>(v + i);
+        float4 ww = *reinterpret_cast<const float4*>(w + i);
+        const float4 r = *reinterpret_cast<const float4*>(rho + i);
+        unsigned wr = cell_forcing(f.x, x0, z, r.x, uu.x, vv.x, ww.x, dt, gravity, alpha, lim_sq, lim, clamp_mode);
+        wr |= cell_forcing(f.y, x0 + 1, z, r.y, uu.y, vv.y, ww.y, dt, gravity, alpha, lim_sq, lim, clamp_mode);
+        wr |= cell_forcing(f.z, x0 + 2, z, r.z, uu.z, vv.z, ww.z, dt, gravity, alpha, lim_sq, lim, clamp_mode);
+        wr |= cell_forcing(f.w, x0 + 3, z, r.w, uu.w, vv.w, ww.w, dt, gravity, alpha, lim_sq, lim, clamp_mode);
+        if (wr & 1u) *reinterpret_cast<float4*>(v + i) = vv;
+        if (wr & 2u) {
+            *reinterpret_cast<float4*>(u + i) = uu;
+            *reinterpret_cast<float4*>(w + i) = ww;
+        }
+        return;
+    }
+    for (int c = 0; c < 4 && x0 + c < g.nx; ++c) {
+        float ut = u[i + c], vt = v[i + c], wt = w[i + c];
+        const unsigned wr = cell_forcing(flags[i + c], x0 + c, z, rho[i + c], ut, vt, wt, dt, gravity, alpha, lim_sq,
+                                         lim, clamp_mode);
+        if (wr & 2u) {
+            u[i + c] = ut;
+            w[i + c] = wt;
+        }
+        if (wr & 1u) v[i + c] = vt;
+    }
+}
+
+// rhs (body_rhs).  Rows y >= 0, planes z >= 0.
+__device__ __forceinline__ void body_rhs_x4(const Grid& g, const float* u, const float* v, const float* w,
+                                            const uint8_t* flags, float* b, float* P, const float* P2,
+                                            const int* pcur, int warm, int x0, int y, int z) {
+    if (x0 >= g.nx || y >= g.ny || z >= g.nz) return;
+    const int i = g.idx(x0, y, z);
+    const bool from2 = warm && pcur != nullptr && P2 != nullptr && *pcur == 1;
+    if (x0 + 3 < g.nx) {
+        const uchar4 f = *reinterpret_cast<const uchar4*>(flags + i);
+        const float4 u0 = *reinterpret_cast<const float4*>(u + i);
+        const float u4 = u[i + 4];  // x0 + 4 <= nx: a face of the same row
+        const float4 v0 = *reinterpret_cast<const float4*>(v + i);
+        const float4 v1 = *reinterpret_cast<const float4*>(v + i + g.X);
+        const float4 w0 = *reinterpret_cast<const float4*>(w + i);
+        const float4 w1 = *reinterpret_cast<const float4*>(w + i + g.XY);
+        const bool p0 = (f.x & F_PROJ) != 0, p1 = (f.y & F_PROJ) != 0, p2 = (f.z & F_PROJ) != 0,
+                   p3 = (f.w & F_PROJ) != 0;
+        const float d0 = -u0.x + u0.y + -v0.x + v1.x + -w0.x + w1.x;
+        const float d1 = -u0.y + u0.z + -v0.y + v1.y + -w0.y + w1.y;
+        const float d2 = -u0.z + u0.w + -v0.z + v1.z + -w0.z + w1.z;
+        const float d3 = -u0.w + u4 + -v0.w + v1.w + -w0.w + w1.w;
+        *reinterpret_cast<float4*>(b + i) =
+            make_float4(p0 ? -d0 : 0.0f, p1 ? -d1 : 0.0f, p2 ? -d2 : 0.0f, p3 ? -d3 : 0.0f);
+        if (!warm) {
+            *reinterpret_cast<float4*>(P + i) = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        } else if (from2) {
+            const float4 q = *reinterpret_cast<const float4*>(P2 + i);
+            *reinterpret_cast<float4*>(P + i) =
+                make_float4(p0 ? q.x : 0.0f, p1 ? q.y : 0.0f, p2 ? q.z : 0.0f, p3 ? q.w : 0.0f);
+        } else {
+            if (!p0) P[i] = 0.0f;
+            if (!p1) P[i + 1] = 0.0f;
+            if (!p2) P[i + 2] = 0.0f;
+            if (!p3) P[i + 3] = 0.0f;
+        }
+        return;
+    }
+    for (int c = 0; c < 4 && x0 + c < g.nx; ++c) {
+        const int k = i + c;
+        const float div = -u[k] + u[k + 1] + -v[k] + v[k + g.X] + -w[k] + w[k + g.XY];
+        const bool proj = (flags[k] & F_PROJ) != 0;
+        b[k] = proj ? -div : 0.0f;
+        if (!proj || !warm) P[k] = 0.0f;
+        else if (from2) P[k] = P2[k];
+    }
+}
+
+// Gradient subtract (body_gradient_subtract) with the pressure P already chosen: every face of
+// the range [1, nx) x [1, ny) x [1, nz) is stored, unchanged ones with their own value.
+__device__ __forceinline__ void body_gradient_subtract_x4(const Grid& g, float* u, float* v, float* w,
+                                                          const float* P, const uint8_t* flags, int x0, int y,
+                                                          int z) {
+    if (x0 >= g.nx || y >= g.ny || z >= g.nz || y < 1 || z < 1) return;
+    const int i = g.idx(x0, y, z);
+    const bool iny = y <= g.ny - 2, inz = z <= g.nz - 2;
+    if (x0 >= 1 && x0 + 3 <= g.nx - 1) {
+        const uchar4 f = *reinterpret_cast<const uchar4*>(flags + i);
+        const float4 pc = *reinterpret_cast<const float4*>(P + i);
+        const float pxm = P[i - 1];
+        const float4 py = *reinterpret_cast<const float4*>(P + i - g.X);
+        const float4 pz = *reinterpret_cast<const float4*>(P + i - g.XY);
+        float4 uu = *reinterpret_cast<const float4*>(u + i);
+        float4 vv = *reinterpret_cast<const float4*>(v + i);
+        float4 ww = *reinterpret_cast<const float4*>(w + i);
+        const float pcs[4] = {pc.x, pc.y, pc.z, pc.w}, pxs[4] = {pxm, pc.x, pc.y, pc.z},
+                    pys[4] = {py.x, py.y, py.z, py.w}, pzs[4] = {pz.x, pz.y, pz.z, pz.w};
+        const uint8_t fs[4] = {f.x, f.y, f.z, f.w};
+        float us[4] = {uu.x, uu.y, uu.z, uu.w}, vs[4] = {vv.x, vv.y, vv.z, vv.w}, ws[4] = {ww.x, ww.y, ww.z, ww.w};
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            const bool self = (fs[c] & F_SELF) != 0;
+            const bool inx = x0 + c <= g.nx - 2;
+            if (self && iny && inz && (fs[c] & F_XM)) us[c] = us[c] - (pcs[c] - pxs[c]);
+            if (self && inx && inz && (fs[c] & F_YM)) vs[c] = vs[c] - (pcs[c] - pys[c]);
+            if (self && inx && iny && (fs[c] & F_ZM)) ws[c] = ws[c] - (pcs[c] - pzs[c]);
+        }
+        *reinterpret_cast<float4*>(u + i) = make_float4(us[0], us[1], us[2], us[3]);
+        *reinterpret_cast<float4*>(v + i) = make_float4(vs[0], vs[1], vs[2], vs[3]);
+        *reinterpret_cast<float4*>(w + i) = make_float4(ws[0], ws[1], ws[2], ws[3]);
+        return;
+    }
+    for (int c = 0; c < 4; ++c) {
+        const int x = x0 + c;
+        if (x < 1 || x >= g.nx) continue;
+        const int k = i + c;
+        const uint8_t f = flags[k];
+        const bool self = (f & F_SELF) != 0;
+        const bool inx = x <= g.nx - 2;
+        const float pc = P[k];
+        if (self && iny && inz && (f & F_XM)) u[k] = u[k] - (pc - P[k - 1]);
+        if (self && inx && inz && (f & F_YM)) v[k] = v[k] - (pc - P[k - g.X]);
+        if (self && inx && iny && (f & F_ZM)) w[k] = w[k] - (pc - P[k - g.XY]);
+    }
+}
+
 // max |div u| over projectable cells.  Contains a block barrier.
 __device__ __forceinline__ void body_div_max(const Grid& g, const float* u, const float* v,
                                              const float* w, const uint8_t* __restrict__ flags,
