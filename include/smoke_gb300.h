@@ -195,6 +195,11 @@ int smk_set_graphs(smk_sim* sim, int enable);
  * (a graph conditional node: no launches after the solve has converged; default on) or as the
  * unrolled launches up to max_sweeps (later ones exit at entry).  Results are identical. */
 int smk_set_graph_loops(smk_sim* sim, int enable);
+/* Run the forcing, rhs and gradient-subtract / BF16-projection stages with four consecutive x
+ * per thread (vector loads and stores; default on, used where the arrays' rows start on vector
+ * boundaries, as every simulation's own arrays do) or one cell per thread.  Results are
+ * identical; batches follow each member's setting.  No counterpart in the reference. */
+int smk_set_vector_stages(smk_sim* sim, int enable);
 /* Time the blocked sweep kernel's shapes (depth, patch rows) and z-chunk sizes on this simulation's buffers and
  * keep the fastest (cached per grid shape and device for the process).  Synchronises; does not
  * change the simulation's results.  Outputs may be NULL; us_per_sweep is -1 on a cache hit.

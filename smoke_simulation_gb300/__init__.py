@@ -118,6 +118,7 @@ def lib() -> C.CDLL:
         "smk_autotune": (i, [vp, C.POINTER(i), C.POINTER(i), C.POINTER(f)]),
         "smk_set_graphs": (i, [vp, i]),
         "smk_set_graph_loops": (i, [vp, i]),
+        "smk_set_vector_stages": (i, [vp, i]),
         "smk_default_render_params": (None, [C.c_void_p]),
         "smk_render": (i, [vp, C.c_void_p, vp, vp, vp]),
         "smk_batch_create": (i, [i, C.POINTER(vp), C.POINTER(vp)]),
@@ -327,6 +328,11 @@ class Simulation:
 
     def set_graph_loops(self, enable: bool):
         _check(lib().smk_set_graph_loops(self.h, 1 if enable else 0))
+
+    def set_vector_stages(self, enable: bool):
+        """Forcing, rhs and subtract / BF16 projection with four x per thread (default) or one
+        cell per thread; results are identical."""
+        _check(lib().smk_set_vector_stages(self.h, 1 if enable else 0))
 
     def set_sweep_kernel(self, depth: int, zchunk: int = 32, rows: int = 2):
         """Blocked sweep kernel shape: `depth` colour passes per launch, z-chunks of `zchunk`

@@ -175,9 +175,17 @@ void fill_record(smk_sim* s, float dt, TableImage& t, GroupGrid& d) {
     d.check_every = p.check_every > 0 ? p.check_every : 1;
     d.max_sweeps = p.max_sweeps;
     d.warm = p.warm_start;
-    // the 4-wide forcing, rhs and subtract bodies (FP32 storage; as the single-grid launchers)
-    d.vec4 = d.kind == GK_F32 &&
-             vec4_layout(s->g, {d.u_now, d.v_now, d.w_now, d.rho_now, d.P, d.P2, d.b}, d.flags);
+    // the 4-wide forcing, rhs and subtract / BF16 projection bodies (as the single-grid launchers)
+    typedef __nv_bfloat16 h;
+    if (!s->vec_stages)
+        d.vec4 = 0;
+    else if (d.kind == GK_F32)
+        d.vec4 = vec4_layout(s->g, {d.u_now, d.v_now, d.w_now, d.rho_now, d.P, d.P2, d.b}, d.flags);
+    else
+        d.vec4 = vec4_layout_of<h>(s->g, {(const h*)d.u_now, (const h*)d.v_now, (const h*)d.w_now},
+                                   {d.P, d.P2, d.b, d.pu, d.pv, d.pw}, d.flags) &&
+                 (d.kind == GK_BF16 ? vec4_layout_of<h>(s->g, {(const h*)d.rho_now}, {}, d.flags)
+                                    : vec4_layout(s->g, {d.rho_now}, d.flags));
 
     // emitters: boxes clipped to the grid (as the single-grid launcher does), then spheres
     const Grid& g = s->g;

@@ -94,6 +94,38 @@ __device__ __forceinline__ float ldv(const __nv_bfloat16* __restrict__ p, int i)
 __device__ __forceinline__ void stv(float* __restrict__ p, int i, float v) { p[i] = v; }
 __device__ __forceinline__ void stv(__nv_bfloat16* __restrict__ p, int i, float v) { p[i] = __float2bfloat16_rn(v); }
 
+// Four consecutive stored values (index a multiple of 4 in a row with 16-byte aligned float or
+// 8-byte aligned bf16 rows): one vector load, the raw bits kept so that a store can leave the
+// lanes that did not change bit for bit as they were.  A bf16 value widens to float exactly by
+// its bits (the conversion ldv makes).
+struct Raw4f { float4 v; };
+struct Raw4h { uint2 r; };
+__device__ __forceinline__ Raw4f ld4raw(const float* p) { return Raw4f{*reinterpret_cast<const float4*>(p)}; }
+__device__ __forceinline__ Raw4h ld4raw(const __nv_bfloat16* p) { return Raw4h{*reinterpret_cast<const uint2*>(p)}; }
+__device__ __forceinline__ float4 to4(const Raw4f& a) { return a.v; }
+__device__ __forceinline__ float4 to4(const Raw4h& a) {
+    return make_float4(__uint_as_float(a.r.x << 16), __uint_as_float(a.r.x & 0xffff0000u),
+                       __uint_as_float(a.r.y << 16), __uint_as_float(a.r.y & 0xffff0000u));
+}
+// Store the four values; lane c keeps its raw bits unless bit c of `changed` is set (a float lane
+// that did not change holds its loaded value, so storing it is the same).
+__device__ __forceinline__ void st4(float* p, const Raw4f&, float4 v, unsigned) {
+    *reinterpret_cast<float4*>(p) = v;
+}
+__device__ __forceinline__ unsigned bf16_bits(float v) {
+    return (unsigned)__bfloat16_as_ushort(__float2bfloat16_rn(v));
+}
+__device__ __forceinline__ void st4(__nv_bfloat16* p, const Raw4h& a, float4 v, unsigned changed) {
+    const unsigned h0 = (changed & 1u) ? bf16_bits(v.x) : (a.r.x & 0xffffu);
+    const unsigned h1 = (changed & 2u) ? bf16_bits(v.y) : (a.r.x >> 16);
+    const unsigned h2 = (changed & 4u) ? bf16_bits(v.z) : (a.r.y & 0xffffu);
+    const unsigned h3 = (changed & 8u) ? bf16_bits(v.w) : (a.r.y >> 16);
+    *reinterpret_cast<uint2*>(p) = make_uint2(h0 | (h1 << 16), h2 | (h3 << 16));
+}
+template <typename T> struct Raw4;
+template <> struct Raw4<float> { typedef Raw4f type; };
+template <> struct Raw4<__nv_bfloat16> { typedef Raw4h type; };
+
 // ---- reference-exact helpers ---------------------------------------------------------------
 
 // avgU/avgV/avgW (smokeSimulation.cu:409-447): 8-point sums in the reference's order, / 8.

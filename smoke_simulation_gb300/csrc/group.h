@@ -73,7 +73,7 @@ struct GroupGrid {
     int sx0, sy0, sz0, sx1, sy1, sz1;  // region of the spheres (interior, one cell margin)
     int ox0, oy0, oz0, ox1, oy1, oz1;  // union of both: the objects stage's tiles
     int wave;  // solve wave: waves run one after another, each to completion
-    int vec4;  // FP32 storage with 16-byte aligned rows: forcing, rhs and subtract take the 4-wide bodies
+    int vec4;  // rows on vector boundaries (vec4_layout): forcing, rhs and the subtract / BF16 projection take the 4-wide bodies
 };
 
 // Grid barrier of the cooperative projection kernel (reset before every launch).
@@ -166,13 +166,16 @@ __host__ __device__ inline int group_x4_tiles(int gx, int ry, int rz) {
 // Range of a 4-wide stage: groups of x, rows (from y0) and planes (from z0).
 __host__ __device__ inline bool group_x4_extent(int stage, const GroupGrid& d, int& gx, int& ry, int& rz, int& y0,
                                                 int& z0) {
-    if (d.kind != GK_F32 || !d.vec4) return false;
+    if (!d.vec4) return false;
     const Grid& g = d.g;
     gx = group_div_up(g.nx, 4);
     switch (stage) {
         case GS_FORCE: ry = g.ny - 1; rz = g.nz; y0 = 1; z0 = 0; return true;
         case GS_RHS: ry = g.ny; rz = g.nz; y0 = 0; z0 = 0; return true;
-        case GS_PROJECT: ry = g.ny - 1; rz = g.nz - 1; y0 = 1; z0 = 1; return true;
+        case GS_PROJECT:
+            if (d.kind == GK_F32) { ry = g.ny - 1; rz = g.nz - 1; y0 = 1; z0 = 1; }  // gradient subtract
+            else { gx = group_div_up(g.nx + 1, 4); ry = g.ny + 1; rz = g.nz + 1; y0 = 0; z0 = 0; }  // BF16 projection
+            return true;
         default: return false;
     }
 }

@@ -32,7 +32,7 @@ void launch_obstacle_velocity(const Grid& g, Tv* u, Tv* v, Tv* w, const Obstacle
 template <typename Tv, typename T>
 void launch_forcing(const Grid& g, Tv* u, Tv* v, Tv* w, const T* rho,
                     const uint8_t* flags, float dt, float gravity, float buoyancy, float clamp_const,
-                    int clamp_mode, cudaStream_t st);
+                    int clamp_mode, cudaStream_t st, bool vec = true);
 
 // Stage d (reference scheme): one colour pass of the in-place velocity red-black SOR.
 void launch_project_velocity(const Grid& g, float* u, float* v, float* w, const uint8_t* flags,
@@ -41,7 +41,7 @@ void launch_project_velocity(const Grid& g, float* u, float* v, float* w, const 
 // Stage c/d (pressure scheme).
 template <typename T>
 void launch_rhs(const Grid& g, const T* u, const T* v, const T* w, const uint8_t* flags,
-                float* b, float* P, const float* P2, const int* pcur, int warm, cudaStream_t st);
+                float* b, float* P, const float* P2, const int* pcur, int warm, cudaStream_t st, bool vec = true);
 // One weighted Jacobi iteration Pin -> Pout (see k_jacobi); *pcur = out_idx when it runs.
 void launch_jacobi(const Grid& g, const float* Pin, float* Pout, const float* b, const uint8_t* flags,
                    const float* wacc7, const StepStatus* status, int* pcur, int out_idx, cudaStream_t st);
@@ -51,18 +51,32 @@ void launch_resid_check(const Grid& g, const float* P, const float* b, const uin
                         StepStatus* status, int group, float tol, cudaStream_t st);
 void launch_gradient_subtract(const Grid& g, float* u, float* v, float* w, const float* P0,
                               const float* P1, const int* pcur, const uint8_t* flags,
-                              cudaStream_t st);
+                              cudaStream_t st, bool vec = true);
 // Temporally blocked sweeps: nhalf <= T colour passes in one pass over HBM, P_in -> P_out;
 // `check` launches also record the residual of the input state for tolerance group `group`.
 // The pressure buffers are read through TMA tensor maps built once per simulation.
-// The 4-wide stage kernels (16-byte loads and stores of four consecutive x) need rows that start
-// on 16-byte boundaries: a row pitch that is a multiple of 4 elements and 16-byte aligned
-// float arrays (4-byte aligned byte arrays).  Callers with other layouts get the per-cell kernels.
-inline bool vec4_layout(const Grid& g, std::initializer_list<const void*> floats, const void* bytes) {
+// The 4-wide stage kernels (vector loads and stores of four consecutive x) need rows that start
+// on vector boundaries: a row pitch that is a multiple of 4 elements, 16-byte aligned float
+// arrays, 8-byte aligned bf16 arrays and 4-byte aligned byte arrays.  Callers with other layouts
+// get the per-cell kernels.
+inline bool vec4_layout(const Grid& g, std::initializer_list<const void*> floats, const void* bytes,
+                        std::initializer_list<const void*> halves = {}) {
     if (g.X % 4 != 0 || g.XY % 4 != 0) return false;
     for (const void* p : floats)
         if (p != nullptr && (reinterpret_cast<uintptr_t>(p) & 15u) != 0) return false;
+    for (const void* p : halves)
+        if (p != nullptr && (reinterpret_cast<uintptr_t>(p) & 7u) != 0) return false;
     return (reinterpret_cast<uintptr_t>(bytes) & 3u) == 0;
+}
+// vec4_layout for arrays of storage type T (float or bf16).
+template <typename T>
+inline bool vec4_layout_of(const Grid& g, std::initializer_list<const T*> ts,
+                           std::initializer_list<const void*> floats, const void* bytes) {
+    for (const T* p : ts) {
+        const uintptr_t m = sizeof(T) == 4 ? 15u : 7u;
+        if (p != nullptr && (reinterpret_cast<uintptr_t>(p) & m) != 0) return false;
+    }
+    return vec4_layout(g, floats, bytes);
 }
 
 // Supported shapes: `rows` = cell rows of a thread's patch (2: T = 2, 4, 6; 4: T = 4), or
@@ -128,7 +142,7 @@ void launch_advect_density(const Grid& g, const T* r0, T* r1, const Tv* u1, cons
 // BF16 storage form: the projection written in FP32 over every face, and rounded into the state.
 void launch_project_bf16(const Grid& g, __nv_bfloat16* u, __nv_bfloat16* v, __nv_bfloat16* w,
                          const float* P0, const float* P1, const int* pcur, const uint8_t* flags,
-                         float* pu, float* pv, float* pw, cudaStream_t st);
+                         float* pu, float* pv, float* pw, cudaStream_t st, bool vec = true);
 void launch_convert(const __nv_bfloat16* src, float* dst, size_t n, cudaStream_t st);
 void launch_convert(const float* src, __nv_bfloat16* dst, size_t n, cudaStream_t st);
 

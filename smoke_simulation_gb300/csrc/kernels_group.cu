@@ -116,15 +116,23 @@ __global__ void __launch_bounds__(GROUP_TILE) k_group_forcing(const GroupArgs a)
         const GroupGrid& d = a.grids[j];
         const Grid gg = d.g;  // in registers: the stores of the body cannot alias it
         int gx, ry, rz, y0, z0;
+        typedef __nv_bfloat16 h;
         if (group_x4_extent(GS_FORCE, d, gx, ry, rz, y0, z0)) {
             int x, y, z;
             x4_coords(local, gx, ry, y0, z0, x, y, z);
-            body_forcing_x4(gg, (float*)d.u_now, (float*)d.v_now, (float*)d.w_now, (const float*)d.rho_now, d.flags,
-                            d.dt, d.gravity, d.alpha, d.lim_sq, d.lim, d.clamp_mode, x, y, z);
+            if (d.kind == GK_BF16)
+                body_forcing_x4<h, h>(gg, (h*)d.u_now, (h*)d.v_now, (h*)d.w_now, (const h*)d.rho_now, d.flags, d.dt,
+                                      d.gravity, d.alpha, d.lim_sq, d.lim, d.clamp_mode, x, y, z);
+            else if (d.kind == GK_BF16_VEL)
+                body_forcing_x4<h, float>(gg, (h*)d.u_now, (h*)d.v_now, (h*)d.w_now, (const float*)d.rho_now,
+                                          d.flags, d.dt, d.gravity, d.alpha, d.lim_sq, d.lim, d.clamp_mode, x, y, z);
+            else
+                body_forcing_x4<float, float>(gg, (float*)d.u_now, (float*)d.v_now, (float*)d.w_now,
+                                              (const float*)d.rho_now, d.flags, d.dt, d.gravity, d.alpha, d.lim_sq,
+                                              d.lim, d.clamp_mode, x, y, z);
             return;
         }
         const uint3 bid = tile_bid(local, d.g.nx, d.g.ny - 1);
-        typedef __nv_bfloat16 h;
         if (d.kind == GK_BF16)
             body_forcing<h, h>(gg, (h*)d.u_now, (h*)d.v_now, (h*)d.w_now, (const h*)d.rho_now, d.flags, d.dt,
                                d.gravity, d.alpha, d.lim_sq, d.lim, d.clamp_mode, bid);
@@ -291,8 +299,13 @@ __global__ void __launch_bounds__(GROUP_TILE) k_group_project(const GroupArgs a)
             if (group_x4_extent(GS_RHS, d, gx, ry, rz, y0, z0)) {
                 int x, y, z;
                 x4_coords(local, gx, ry, y0, z0, x, y, z);
-                body_rhs_x4(gg, (const float*)d.u_now, (const float*)d.v_now, (const float*)d.w_now, d.flags, d.b,
-                            d.P, d.P2, d.pcur, d.warm, x, y, z);
+                if (d.kind == GK_F32)
+                    body_rhs_x4<float>(gg, (const float*)d.u_now, (const float*)d.v_now, (const float*)d.w_now,
+                                       d.flags, d.b, d.P, d.P2, d.pcur, d.warm, x, y, z);
+                else
+                    body_rhs_x4<__nv_bfloat16>(gg, (const __nv_bfloat16*)d.u_now, (const __nv_bfloat16*)d.v_now,
+                                               (const __nv_bfloat16*)d.w_now, d.flags, d.b, d.P, d.P2, d.pcur,
+                                               d.warm, x, y, z);
                 return;
             }
             const uint3 bid = tile_bid(local, d.g.nx, d.g.ny);
@@ -417,7 +430,11 @@ __global__ void __launch_bounds__(GROUP_TILE) k_group_project(const GroupArgs a)
             int x, y, z;
             x4_coords(local, gx, ry, y0, z0, x, y, z);
             const float* P = (d.pcur != nullptr && *d.pcur == 1) ? d.P2 : d.P;
-            body_gradient_subtract_x4(gg, (float*)d.u_now, (float*)d.v_now, (float*)d.w_now, P, d.flags, x, y, z);
+            if (d.kind == GK_F32)
+                body_gradient_subtract_x4(gg, (float*)d.u_now, (float*)d.v_now, (float*)d.w_now, P, d.flags, x, y, z);
+            else
+                body_project_bf16_x4(gg, (__nv_bfloat16*)d.u_now, (__nv_bfloat16*)d.v_now, (__nv_bfloat16*)d.w_now, P,
+                                     d.flags, d.pu, d.pv, d.pw, x, y, z);
             return;
         }
         group_extent(GS_PROJECT, d, rx, ry, rz);

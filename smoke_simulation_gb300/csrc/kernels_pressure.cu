@@ -35,9 +35,10 @@ __global__ void k_rhs(Grid g, const T* __restrict__ u, const T* __restrict__ v,
     body_rhs(g, u, v, w, flags, b, P, P2, pcur, warm, blockIdx);
 }
 
-// FP32 rhs with four consecutive x per thread (16-byte loads and stores; body_rhs_x4).
-__global__ void __launch_bounds__(256) k_rhs_x4(Grid g, const float* __restrict__ u, const float* __restrict__ v,
-                                                const float* __restrict__ w, const uint8_t* __restrict__ flags,
+// rhs with four consecutive x per thread (vector loads and stores; body_rhs_x4).
+template <typename T>
+__global__ void __launch_bounds__(256) k_rhs_x4(Grid g, const T* __restrict__ u, const T* __restrict__ v,
+                                                const T* __restrict__ w, const uint8_t* __restrict__ flags,
                                                 float* __restrict__ b, float* __restrict__ P,
                                                 const float* __restrict__ P2, const int* __restrict__ pcur,
                                                 int warm) {
@@ -107,24 +108,20 @@ __global__ void k_resid_check(Grid g, const float* __restrict__ P, const float* 
 
 template <typename T>
 void launch_rhs(const Grid& g, const T* u, const T* v, const T* w, const uint8_t* flags,
-                float* b, float* P, const float* P2, const int* pcur, int warm, cudaStream_t st) {
-    if constexpr (std::is_same<T, float>::value) {
-        if (!vec4_layout(g, {u, v, w, b, P, P2}, flags)) {
-            k_rhs<<<grid3(g.nx, g.ny, g.nz), dim3(BX, BY), 0, st>>>(g, u, v, w, flags, b, P, P2, pcur, warm);
-            return;
-        }
+                float* b, float* P, const float* P2, const int* pcur, int warm, cudaStream_t st, bool vec) {
+    if (vec && vec4_layout_of<T>(g, {u, v, w}, {b, P, P2}, flags)) {
         const int groups = (g.nx + 3) / 4;
-        k_rhs_x4<<<dim3((unsigned)((groups + 31) / 32), (unsigned)((g.ny + 7) / 8), (unsigned)g.nz), dim3(32, 8), 0,
-                   st>>>(g, u, v, w, flags, b, P, P2, pcur, warm);
+        k_rhs_x4<T><<<dim3((unsigned)((groups + 31) / 32), (unsigned)((g.ny + 7) / 8), (unsigned)g.nz), dim3(32, 8),
+                      0, st>>>(g, u, v, w, flags, b, P, P2, pcur, warm);
         return;
     }
     k_rhs<<<grid3(g.nx, g.ny, g.nz), dim3(BX, BY), 0, st>>>(g, u, v, w, flags, b, P, P2, pcur, warm);
 }
 template void launch_rhs<float>(const Grid&, const float*, const float*, const float*, const uint8_t*, float*,
-                                float*, const float*, const int*, int, cudaStream_t);
+                                float*, const float*, const int*, int, cudaStream_t, bool);
 template void launch_rhs<__nv_bfloat16>(const Grid&, const __nv_bfloat16*, const __nv_bfloat16*,
                                         const __nv_bfloat16*, const uint8_t*, float*, float*, const float*,
-                                        const int*, int, cudaStream_t);
+                                        const int*, int, cudaStream_t, bool);
 
 void launch_sweep(const Grid& g, float* P, const float* b, const uint8_t* flags, int colour,
                   const float* wacc7, const StepStatus* status, cudaStream_t st) {
@@ -156,9 +153,9 @@ void launch_resid_check(const Grid& g, const float* P, const float* b, const uin
 
 void launch_gradient_subtract(const Grid& g, float* u, float* v, float* w, const float* P0,
                               const float* P1, const int* pcur, const uint8_t* flags,
-                              cudaStream_t st) {
+                              cudaStream_t st, bool vec) {
     if (g.nx < 2 || g.ny < 2 || g.nz < 2) return;
-    if (!vec4_layout(g, {u, v, w, P0, P1}, flags)) {
+    if (!vec || !vec4_layout(g, {u, v, w, P0, P1}, flags)) {
         k_gradient_subtract<<<grid3(g.nx - 1, g.ny - 1, g.nz - 1), dim3(BX, BY), 0, st>>>(
             g, u, v, w, P0, P1, pcur, flags);
         return;

@@ -114,9 +114,10 @@ __global__ void k_forcing(Grid g, Tv* __restrict__ u, Tv* __restrict__ v, Tv* __
     body_forcing(g, u, v, w, rho, flags, dt, gravity, alpha, lim_sq, lim, clamp_mode, blockIdx);
 }
 
-// FP32 forcing with four consecutive x per thread (16-byte loads and stores; body_forcing_x4).
-__global__ void __launch_bounds__(256) k_forcing_x4(Grid g, float* __restrict__ u, float* __restrict__ v,
-                                                    float* __restrict__ w, const float* __restrict__ rho,
+// Forcing with four consecutive x per thread (vector loads and stores; body_forcing_x4).
+template <typename Tv, typename T>
+__global__ void __launch_bounds__(256) k_forcing_x4(Grid g, Tv* __restrict__ u, Tv* __restrict__ v,
+                                                    Tv* __restrict__ w, const T* __restrict__ rho,
                                                     const uint8_t* __restrict__ flags, float dt, float gravity,
                                                     float alpha, float lim_sq, float lim, int clamp_mode) {
     body_forcing_x4(g, u, v, w, rho, flags, dt, gravity, alpha, lim_sq, lim, clamp_mode,
@@ -181,6 +182,18 @@ __global__ void __launch_bounds__(BX * BY, 8) k_advect_density(Grid g, const T* 
         if (zz >= rz) break;
         body_advect_density(g, r0, r1, u, v, w, flags, dt, make_uint3(blockIdx.x, blockIdx.y, (unsigned)zz));
     }
+}
+
+// The BF16 projection with four consecutive x per thread (body_project_bf16_x4).
+__global__ void __launch_bounds__(256) k_project_bf16_x4(Grid g, __nv_bfloat16* __restrict__ u,
+                                                         __nv_bfloat16* __restrict__ v, __nv_bfloat16* __restrict__ w,
+                                                         const float* __restrict__ P0, const float* __restrict__ P1,
+                                                         const int* __restrict__ pcur,
+                                                         const uint8_t* __restrict__ flags, float* __restrict__ pu,
+                                                         float* __restrict__ pv, float* __restrict__ pw) {
+    const float* P = (pcur != nullptr && *pcur == 1) ? P1 : P0;
+    body_project_bf16_x4(g, u, v, w, P, flags, pu, pv, pw, 4 * ((int)blockIdx.x * 32 + (int)threadIdx.x),
+                         (int)blockIdx.y * 8 + (int)threadIdx.y, (int)blockIdx.z);
 }
 
 __global__ void k_project_bf16(Grid g, __nv_bfloat16* __restrict__ u, __nv_bfloat16* __restrict__ v,
@@ -297,19 +310,14 @@ void launch_build_flags(const Grid& g, const uint8_t* s, uint8_t* flags, float* 
 template <typename Tv, typename T>
 void launch_forcing(const Grid& g, Tv* u, Tv* v, Tv* w, const T* rho,
                     const uint8_t* flags, float dt, float gravity, float buoyancy, float clamp_const,
-                    int clamp_mode, cudaStream_t st) {
+                    int clamp_mode, cudaStream_t st, bool vec) {
     if (g.ny < 2) return;
     float lim_sq = clamp_const * clamp_const;
-    if constexpr (std::is_same<Tv, float>::value && std::is_same<T, float>::value) {
-        if (!vec4_layout(g, {u, v, w, rho}, flags)) {
-            k_forcing<<<grid3(g.nx, g.ny - 1, g.nz), dim3(BX, BY), 0, st>>>(
-                g, u, v, w, rho, flags, dt, gravity, buoyancy, lim_sq, clamp_const, clamp_mode);
-            return;
-        }
+    if (vec && vec4_layout_of<Tv>(g, {u, v, w}, {}, flags) && vec4_layout_of<T>(g, {rho}, {}, flags)) {
         const int groups = (g.nx + 3) / 4;
-        k_forcing_x4<<<dim3((unsigned)((groups + 31) / 32), (unsigned)((g.ny - 1 + 7) / 8), (unsigned)g.nz),
-                       dim3(32, 8), 0, st>>>(g, u, v, w, rho, flags, dt, gravity, buoyancy, lim_sq, clamp_const,
-                                             clamp_mode);
+        k_forcing_x4<Tv, T><<<dim3((unsigned)((groups + 31) / 32), (unsigned)((g.ny - 1 + 7) / 8), (unsigned)g.nz),
+                              dim3(32, 8), 0, st>>>(g, u, v, w, rho, flags, dt, gravity, buoyancy, lim_sq,
+                                                    clamp_const, clamp_mode);
         return;
     }
     k_forcing<<<grid3(g.nx, g.ny - 1, g.nz), dim3(BX, BY), 0, st>>>(
@@ -350,7 +358,13 @@ void launch_div_max(const Grid& g, const float* u, const float* v, const float* 
 
 void launch_project_bf16(const Grid& g, __nv_bfloat16* u, __nv_bfloat16* v, __nv_bfloat16* w,
                          const float* P0, const float* P1, const int* pcur, const uint8_t* flags,
-                         float* pu, float* pv, float* pw, cudaStream_t st) {
+                         float* pu, float* pv, float* pw, cudaStream_t st, bool vec) {
+    if (vec && vec4_layout_of<__nv_bfloat16>(g, {u, v, w}, {P0, P1, pu, pv, pw}, flags)) {
+        const int groups = (g.nx + 1 + 3) / 4;
+        k_project_bf16_x4<<<dim3((unsigned)((groups + 31) / 32), (unsigned)((g.ny + 1 + 7) / 8), (unsigned)(g.nz + 1)),
+                            dim3(32, 8), 0, st>>>(g, u, v, w, P0, P1, pcur, flags, pu, pv, pw);
+        return;
+    }
     k_project_bf16<<<grid3(g.nx + 1, g.ny + 1, g.nz + 1), dim3(BX, BY), 0, st>>>(g, u, v, w, P0, P1, pcur,
                                                                                flags, pu, pv, pw);
 }
@@ -374,13 +388,13 @@ template void launch_fill_smoke<float>(const Grid&, float*, float*, const Sphere
 template void launch_fill_smoke<__nv_bfloat16>(const Grid&, __nv_bfloat16*, __nv_bfloat16*, const SphereObj*,
                                                int, cudaStream_t);
 template void launch_forcing<float, float>(const Grid&, float*, float*, float*, const float*, const uint8_t*,
-                                           float, float, float, float, int, cudaStream_t);
+                                           float, float, float, float, int, cudaStream_t, bool);
 template void launch_forcing<__nv_bfloat16, __nv_bfloat16>(const Grid&, __nv_bfloat16*, __nv_bfloat16*,
                                                            __nv_bfloat16*, const __nv_bfloat16*, const uint8_t*,
-                                                           float, float, float, float, int, cudaStream_t);
+                                                           float, float, float, float, int, cudaStream_t, bool);
 template void launch_forcing<__nv_bfloat16, float>(const Grid&, __nv_bfloat16*, __nv_bfloat16*, __nv_bfloat16*,
                                                    const float*, const uint8_t*, float, float, float, float, int,
-                                                   cudaStream_t);
+                                                   cudaStream_t, bool);
 template void launch_advect_velocity<float, float>(const Grid&, const float*, const float*, const float*,
                                                    float*, float*, float*, const uint8_t*, float, cudaStream_t);
 template void launch_advect_velocity<float, __nv_bfloat16>(const Grid&, const float*, const float*,

@@ -218,13 +218,13 @@ int smk_sim::enqueue(float dt, cudaStream_t st) {
     // b: integrate + velocityConfinement (:789-791)
     if (rho_bf16)
         launch_forcing(g, bf(u[now]), bf(v[now]), bf(w[now]), (const __nv_bfloat16*)bf(rho[now]), flags, dt,
-                       p.gravity, p.buoyancy, p.clamp_const, p.clamp_mode, st);
+                       p.gravity, p.buoyancy, p.clamp_const, p.clamp_mode, st, vec_stages);
     else if (bf16)
         launch_forcing(g, bf(u[now]), bf(v[now]), bf(w[now]), (const float*)rho[now], flags, dt, p.gravity,
-                       p.buoyancy, p.clamp_const, p.clamp_mode, st);
+                       p.buoyancy, p.clamp_const, p.clamp_mode, st, vec_stages);
     else
         launch_forcing(g, u[now], v[now], w[now], (const float*)rho[now], flags, dt, p.gravity, p.buoyancy,
-                       p.clamp_const, p.clamp_mode, st);
+                       p.clamp_const, p.clamp_mode, st, vec_stages);
     ++launches;
     if (p.obstacle_velocity && !obstacles.empty()) {
         if (bf16) launch_obstacle_velocity(g, bf(u[now]), bf(v[now]), bf(w[now]), obstacles.back(), st);
@@ -249,10 +249,10 @@ int smk_sim::enqueue(float dt, cudaStream_t st) {
         for (int a = 1; a <= 6; ++a) wacc[a] = (float)p.omega / (float)a;
         if (bf16)
             launch_rhs(g, (const __nv_bfloat16*)bf(u[now]), (const __nv_bfloat16*)bf(v[now]),
-                       (const __nv_bfloat16*)bf(w[now]), flags, b, P, P2, pcur, p.warm_start, st);
+                       (const __nv_bfloat16*)bf(w[now]), flags, b, P, P2, pcur, p.warm_start, st, vec_stages);
         else
             launch_rhs(g, (const float*)u[now], (const float*)v[now], (const float*)w[now], flags, b, P, P2,
-                       pcur, p.warm_start, st);
+                       pcur, p.warm_start, st, vec_stages);
         ++launches;
         const bool use_tol = p.tol > 0.0f;
         const int G = use_tol ? p.check_every : (p.max_sweeps > 0 ? p.max_sweeps : 1);
@@ -372,9 +372,9 @@ int smk_sim::enqueue(float dt, cudaStream_t st) {
         if (!pcur_set) SMK_CUDA(cudaMemsetAsync(pcur, 0, sizeof(int), st));
         if (bf16)
             launch_project_bf16(g, bf(u[now]), bf(v[now]), bf(w[now]), P, P2, pcur, flags, proj[0], proj[1],
-                                proj[2], st);
+                                proj[2], st, vec_stages);
         else
-            launch_gradient_subtract(g, u[now], v[now], w[now], P, P2, pcur, flags, st);
+            launch_gradient_subtract(g, u[now], v[now], w[now], P, P2, pcur, flags, st, vec_stages);
         ++launches;
         if (p.refine > 0) {
             if (bf16)
@@ -938,6 +938,13 @@ int smk_set_sweep_kernel(smk_sim* sim, int depth, int zchunk) {
 int smk_set_graphs(smk_sim* sim, int enable) {
     if (!sim) return fail(SMK_ERR_INVALID, "sim is null");
     sim->use_graphs = enable != 0;
+    return SMK_OK;
+}
+
+int smk_set_vector_stages(smk_sim* sim, int enable) {
+    if (!sim) return fail(SMK_ERR_INVALID, "sim is null");
+    sim->vec_stages = enable != 0;
+    for (auto& gs : sim->graphs) gs.sig.clear();  // re-capture
     return SMK_OK;
 }
 

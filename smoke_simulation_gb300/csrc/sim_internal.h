@@ -117,6 +117,7 @@ struct smk_sim {
     // in a captured step, the tolerance groups of the blocked solve run as a device-side WHILE
     // loop (graph conditional node) instead of launches for every group up to the cap
     bool graph_loops = true;
+    bool vec_stages = true;  // 4-wide forcing / rhs / subtract kernels where the layout allows
     GraphSlot graphs[2];
     cudaStream_t cap_stream = nullptr;
     cudaStream_t body_stream = nullptr;  // captures the loop body

@@ -265,44 +265,50 @@ __device__ __forceinline__ void body_gradient_subtract(const Grid& g, float* u, 
 // per-cell bodies above, so every result is the same.  Plain pointers, as for the projection
 // bodies (the grouped projection runs the rhs and the subtract as phases of one launch).
 
-// Forcing (body_forcing, cell_forcing): a group's faces that do not change are stored back
-// unchanged.  Rows y >= 1.
-__device__ __forceinline__ void body_forcing_x4(const Grid& g, float* u, float* v, float* w, const float* rho,
+// Forcing (body_forcing, cell_forcing) for velocities stored as Tv and density as T: a group's
+// faces that do not change keep their bits (st4).  Rows y >= 1.
+template <typename Tv, typename T>
+__device__ __forceinline__ void body_forcing_x4(const Grid& g, Tv* u, Tv* v, Tv* w, const T* rho,
                                                 const uint8_t* flags, float dt, float gravity, float alpha,
                                                 float lim_sq, float lim, int clamp_mode, int x0, int y, int z) {
     if (x0 >= g.nx || y >= g.ny || z >= g.nz) return;
     const int i = g.idx(x0, y, z);
     if (x0 + 3 < g.nx) {
         const uchar4 f = *reinterpret_cast<const uchar4*>(flags + i);
-        float4 uu = *reinterpret_cast<const float4*>(u + i);
-        float4 vv = *reinterpret_cast<const float4*>(v + i);
-        float4 ww = *reinterpret_cast<const float4*>(w + i);
-        const float4 r = *reinterpret_cast<const float4*>(rho + i);
-        unsigned wr = cell_forcing(f.x, x0, z, r.x, uu.x, vv.x, ww.x, dt, gravity, alpha, lim_sq, lim, clamp_mode);
-        wr |= cell_forcing(f.y, x0 + 1, z, r.y, uu.y, vv.y, ww.y, dt, gravity, alpha, lim_sq, lim, clamp_mode);
-        wr |= cell_forcing(f.z, x0 + 2, z, r.z, uu.z, vv.z, ww.z, dt, gravity, alpha, lim_sq, lim, clamp_mode);
-        wr |= cell_forcing(f.w, x0 + 3, z, r.w, uu.w, vv.w, ww.w, dt, gravity, alpha, lim_sq, lim, clamp_mode);
-        if (wr & 1u) *reinterpret_cast<float4*>(v + i) = vv;
-        if (wr & 2u) {
-            *reinterpret_cast<float4*>(u + i) = uu;
-            *reinterpret_cast<float4*>(w + i) = ww;
+        const typename Raw4<Tv>::type ru = ld4raw(u + i), rv = ld4raw(v + i), rw = ld4raw(w + i);
+        float4 uu = to4(ru), vv = to4(rv), ww = to4(rw);
+        const float4 r = to4(ld4raw(rho + i));
+        const unsigned w0 = cell_forcing(f.x, x0, z, r.x, uu.x, vv.x, ww.x, dt, gravity, alpha, lim_sq, lim, clamp_mode);
+        const unsigned w1 =
+            cell_forcing(f.y, x0 + 1, z, r.y, uu.y, vv.y, ww.y, dt, gravity, alpha, lim_sq, lim, clamp_mode);
+        const unsigned w2 =
+            cell_forcing(f.z, x0 + 2, z, r.z, uu.z, vv.z, ww.z, dt, gravity, alpha, lim_sq, lim, clamp_mode);
+        const unsigned w3 =
+            cell_forcing(f.w, x0 + 3, z, r.w, uu.w, vv.w, ww.w, dt, gravity, alpha, lim_sq, lim, clamp_mode);
+        const unsigned mv = (w0 & 1u) | ((w1 & 1u) << 1) | ((w2 & 1u) << 2) | ((w3 & 1u) << 3);
+        const unsigned muw = ((w0 >> 1) & 1u) | (w1 & 2u) | ((w2 & 2u) << 1) | ((w3 & 2u) << 2);
+        if (mv) st4(v + i, rv, vv, mv);
+        if (muw) {
+            st4(u + i, ru, uu, muw);
+            st4(w + i, rw, ww, muw);
         }
         return;
     }
     for (int c = 0; c < 4 && x0 + c < g.nx; ++c) {
-        float ut = u[i + c], vt = v[i + c], wt = w[i + c];
-        const unsigned wr = cell_forcing(flags[i + c], x0 + c, z, rho[i + c], ut, vt, wt, dt, gravity, alpha, lim_sq,
-                                         lim, clamp_mode);
+        float ut = ldv(u, i + c), vt = ldv(v, i + c), wt = ldv(w, i + c);
+        const unsigned wr = cell_forcing(flags[i + c], x0 + c, z, ldv(rho, i + c), ut, vt, wt, dt, gravity, alpha,
+                                         lim_sq, lim, clamp_mode);
         if (wr & 2u) {
-            u[i + c] = ut;
-            w[i + c] = wt;
+            stv(u, i + c, ut);
+            stv(w, i + c, wt);
         }
-        if (wr & 1u) v[i + c] = vt;
+        if (wr & 1u) stv(v, i + c, vt);
     }
 }
 
-// rhs (body_rhs).  Rows y >= 0, planes z >= 0.
-__device__ __forceinline__ void body_rhs_x4(const Grid& g, const float* u, const float* v, const float* w,
+// rhs (body_rhs) for velocities stored as T.  Rows y >= 0, planes z >= 0.
+template <typename T>
+__device__ __forceinline__ void body_rhs_x4(const Grid& g, const T* u, const T* v, const T* w,
                                             const uint8_t* flags, float* b, float* P, const float* P2,
                                             const int* pcur, int warm, int x0, int y, int z) {
     if (x0 >= g.nx || y >= g.ny || z >= g.nz) return;
@@ -310,12 +316,12 @@ __device__ __forceinline__ void body_rhs_x4(const Grid& g, const float* u, const
     const bool from2 = warm && pcur != nullptr && P2 != nullptr && *pcur == 1;
     if (x0 + 3 < g.nx) {
         const uchar4 f = *reinterpret_cast<const uchar4*>(flags + i);
-        const float4 u0 = *reinterpret_cast<const float4*>(u + i);
-        const float u4 = u[i + 4];  // x0 + 4 <= nx: a face of the same row
-        const float4 v0 = *reinterpret_cast<const float4*>(v + i);
-        const float4 v1 = *reinterpret_cast<const float4*>(v + i + g.X);
-        const float4 w0 = *reinterpret_cast<const float4*>(w + i);
-        const float4 w1 = *reinterpret_cast<const float4*>(w + i + g.XY);
+        const float4 u0 = to4(ld4raw(u + i));
+        const float u4 = ldv(u, i + 4);  // x0 + 4 <= nx: a face of the same row
+        const float4 v0 = to4(ld4raw(v + i));
+        const float4 v1 = to4(ld4raw(v + i + g.X));
+        const float4 w0 = to4(ld4raw(w + i));
+        const float4 w1 = to4(ld4raw(w + i + g.XY));
         const bool p0 = (f.x & F_PROJ) != 0, p1 = (f.y & F_PROJ) != 0, p2 = (f.z & F_PROJ) != 0,
                    p3 = (f.w & F_PROJ) != 0;
         const float d0 = -u0.x + u0.y + -v0.x + v1.x + -w0.x + w1.x;
@@ -340,11 +346,71 @@ __device__ __forceinline__ void body_rhs_x4(const Grid& g, const float* u, const
     }
     for (int c = 0; c < 4 && x0 + c < g.nx; ++c) {
         const int k = i + c;
-        const float div = -u[k] + u[k + 1] + -v[k] + v[k + g.X] + -w[k] + w[k + g.XY];
+        const float div = -ldv(u, k) + ldv(u, k + 1) + -ldv(v, k) + ldv(v, k + g.X) + -ldv(w, k) + ldv(w, k + g.XY);
         const bool proj = (flags[k] & F_PROJ) != 0;
         b[k] = proj ? -div : 0.0f;
         if (!proj || !warm) P[k] = 0.0f;
         else if (from2) P[k] = P2[k];
+    }
+}
+
+// BF16 projection (body_project_bf16) with the pressure P already chosen: every index of
+// [0, nx] x [0, ny] x [0, nz] gets its FP32 projected velocities in pu, pv, pw; the BF16 faces a
+// cell changes are rounded back into u, v, w (the others keep their bits).
+__device__ __forceinline__ void body_project_bf16_x4(const Grid& g, __nv_bfloat16* u, __nv_bfloat16* v,
+                                                     __nv_bfloat16* w, const float* P, const uint8_t* flags,
+                                                     float* pu, float* pv, float* pw, int x0, int y, int z) {
+    if (x0 > g.nx || y > g.ny || z > g.nz) return;
+    const int i = g.idx(x0, y, z);
+    if (x0 >= 4 && x0 + 3 <= g.nx - 1 && y >= 1 && y <= g.ny - 1 && z >= 1 && z <= g.nz - 1) {
+        // four cells: x0..x0+3 in [1, nx), y in [1, ny), z in [1, nz)
+        const uchar4 f = *reinterpret_cast<const uchar4*>(flags + i);
+        const Raw4h ru = ld4raw(u + i), rv = ld4raw(v + i), rw = ld4raw(w + i);
+        const float4 u4 = to4(ru), v4 = to4(rv), w4 = to4(rw);
+        const float4 pc = *reinterpret_cast<const float4*>(P + i);
+        const float pxm = P[i - 1];
+        const float4 py = *reinterpret_cast<const float4*>(P + i - g.X);
+        const float4 pz = *reinterpret_cast<const float4*>(P + i - g.XY);
+        const float pcs[4] = {pc.x, pc.y, pc.z, pc.w}, pxs[4] = {pxm, pc.x, pc.y, pc.z},
+                    pys[4] = {py.x, py.y, py.z, py.w}, pzs[4] = {pz.x, pz.y, pz.z, pz.w};
+        const uint8_t fs[4] = {f.x, f.y, f.z, f.w};
+        float us[4] = {u4.x, u4.y, u4.z, u4.w}, vs[4] = {v4.x, v4.y, v4.z, v4.w}, ws[4] = {w4.x, w4.y, w4.z, w4.w};
+        const bool iny = y <= g.ny - 2, inz = z <= g.nz - 2;
+        unsigned mu = 0u, mv = 0u, mw = 0u;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            if (!(fs[c] & F_SELF)) continue;
+            const bool inx = x0 + c <= g.nx - 2;
+            if (iny && inz && (fs[c] & F_XM)) { us[c] = us[c] - (pcs[c] - pxs[c]); mu |= 1u << c; }
+            if (inx && inz && (fs[c] & F_YM)) { vs[c] = vs[c] - (pcs[c] - pys[c]); mv |= 1u << c; }
+            if (inx && iny && (fs[c] & F_ZM)) { ws[c] = ws[c] - (pcs[c] - pzs[c]); mw |= 1u << c; }
+        }
+        const float4 uo = make_float4(us[0], us[1], us[2], us[3]), vo = make_float4(vs[0], vs[1], vs[2], vs[3]),
+                     wo = make_float4(ws[0], ws[1], ws[2], ws[3]);
+        if (mu) st4(u + i, ru, uo, mu);
+        if (mv) st4(v + i, rv, vo, mv);
+        if (mw) st4(w + i, rw, wo, mw);
+        *reinterpret_cast<float4*>(pu + i) = uo;
+        *reinterpret_cast<float4*>(pv + i) = vo;
+        *reinterpret_cast<float4*>(pw + i) = wo;
+        return;
+    }
+    for (int c = 0; c < 4 && x0 + c <= g.nx; ++c) {
+        const int x = x0 + c, k = i + c;
+        float uu = ldv(u, k), vv = ldv(v, k), ww = ldv(w, k);
+        if (x < g.nx && y < g.ny && z < g.nz && x >= 1 && y >= 1 && z >= 1) {
+            const uint8_t f = flags[k];
+            if (f & F_SELF) {
+                const bool inx = x <= g.nx - 2, iny = y <= g.ny - 2, inz = z <= g.nz - 2;
+                const float pc = P[k];
+                if (iny && inz && (f & F_XM)) { uu = uu - (pc - P[k - 1]); stv(u, k, uu); }
+                if (inx && inz && (f & F_YM)) { vv = vv - (pc - P[k - g.X]); stv(v, k, vv); }
+                if (inx && iny && (f & F_ZM)) { ww = ww - (pc - P[k - g.XY]); stv(w, k, ww); }
+            }
+        }
+        pu[k] = uu;
+        pv[k] = vv;
+        pw[k] = ww;
     }
 }
 

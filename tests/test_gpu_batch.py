@@ -292,3 +292,26 @@ def test_grouped_blocked_needs_shared_groups(gpu):
     b2.close()
     for s in sims + ref + sims2 + ref2:
         s.close()
+
+
+@pytest.mark.parametrize("storage", [smk.STORAGE_F32, smk.STORAGE_BF16_VEL, smk.STORAGE_BF16])
+def test_grouped_vector_stages_equal_per_cell(gpu, storage):
+    """A grouped batch whose members use the 4-wide stage bodies gives the bits of the same batch
+    with one cell per thread (grid sides 8..44: rows ending anywhere in a group of four)."""
+    scs = _grouped_scenes(count=5, seed=19)
+    a = [smk.from_scene(sc, report_div=1, storage=storage) for sc in scs]
+    b = [smk.from_scene(sc, report_div=1, storage=storage) for sc in scs]
+    for s in b:
+        s.set_vector_stages(False)
+    ba = smk.Batch(a, mode=smk.BATCH_GROUPED)
+    bb = smk.Batch(b, mode=smk.BATCH_GROUPED)
+    for _ in range(5):
+        ba.step([0.05] * len(scs))
+        bb.step([0.05] * len(scs))
+    for i in range(len(scs)):
+        assert H.first_mismatch(a[i].read_state(), b[i].read_state()) == "", i
+        assert a[i].stats().div_max == b[i].stats().div_max, i
+    ba.close()
+    bb.close()
+    for s in a + b:
+        s.close()

@@ -77,3 +77,25 @@ def test_storage_is_fixed_at_creation(gpu):
     with pytest.raises(smk.SmokeError):
         sim.set_params(storage=smk.STORAGE_F32)
     sim.close()
+
+
+@pytest.mark.parametrize("storage", [smk.STORAGE_F32, smk.STORAGE_BF16_VEL, smk.STORAGE_BF16])
+@pytest.mark.parametrize("dims", [(37, 22, 19), (40, 17, 24)])
+def test_vector_stages_equal_per_cell_stages(gpu, storage, dims):
+    """The 4-wide forcing, rhs and gradient-subtract / BF16-projection kernels (four consecutive
+    x per thread; BF16 lanes a stage does not change keep their bits) give the bits of the
+    per-cell kernels, on rows that end inside a group of four (nx = 37) and at its end (40)."""
+    sc = S.small_scene(*dims, steps=6, seed=71, scheme=1, iterations=40, tol=1e-3, check_every=5,
+                       obstacles=2, warm_start=1)
+    sc.u0, sc.v0, sc.w0 = S.noise_velocity(sc.face_shape, 0.3, seed=72)
+    a = smk.from_scene(sc, report_div=1, storage=storage)
+    b = smk.from_scene(sc, report_div=1, storage=storage)
+    b.set_vector_stages(False)
+    for k in range(sc.steps):
+        a.step(sc.dt)
+        b.step(sc.dt)
+        sa, sb = a.stats(), b.stats()
+        assert sa.sweeps == sb.sweeps and sa.div_max == sb.div_max, k
+        assert H.first_mismatch(a.read_state(), b.read_state()) == "", k
+    a.close()
+    b.close()
