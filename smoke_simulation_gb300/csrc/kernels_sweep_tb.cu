@@ -227,12 +227,15 @@ __host__ __device__ inline void sweep_window(int n, int W, int T, int k, int& st
 // Instead of recomputing a T-row halo between the CTAs of a run, every CTA writes its boundary
 // rows' published values into its neighbours' shared memory (the padding rows of their
 // published planes), and the per-iteration barrier is a cluster barrier.
-template <int T, int PY, bool GLOBAL_MAPS = false, bool YCLUSTER = false>
+// FULL: the launch applies all T colour passes (nhalf == T), so the stages need no test; CHK: 0
+// or 1 = the launch is (not) a tolerance-check launch, fixed at compile time; -1 = `check` decides.
+template <int T, int PY, bool GLOBAL_MAPS = false, bool YCLUSTER = false, bool FULL = false, int CHK = -1>
 __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, float* __restrict__ Pout,
                                            int nhalf, int colour0, int zchunk, const WAcc8& wa,
                                            StepStatus* status, int check, int group, float tol,
                                            int* __restrict__ pcur, int out_idx, int* __restrict__ kerr,
                                            int bx, int by, int bz, int ycl_n = 1, int ycl_hy = 0) {
+    const bool chk = CHK < 0 ? check != 0 : CHK == 1;
     using G = TBGeom<PY>;
     constexpr int TY = G::TY, ROWS = G::ROWS, PROW = G::PROW, STAGE_BYTES = G::STAGE_BYTES,
                   STAGE_P = G::STAGE_P;
@@ -260,7 +263,7 @@ __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, fl
     const bool first_tile = (bx | by | bz) == 0;
     if (status != nullptr) {
         if (*(volatile int*)&status->done) return;
-        if (check && group > 0 && __uint_as_float(status->rmax_bits[group - 1]) <= tol) {
+        if (chk && group > 0 && __uint_as_float(status->rmax_bits[group - 1]) <= tol) {
             if (first_tile && threadIdx.x == 0 && threadIdx.y == 0) {
                 status->done = 1;
                 status->done_group = group;
@@ -395,7 +398,7 @@ __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, fl
             const bool sA = ((k + p_par) & 1) == 0;
             float* pb = pub + par * NPUB * PROW;
             const uint32_t pofs = (uint32_t)(par * NPUB * PROW) * 4u;  // byte offset of this buffer
-            if (check) {
+            if (chk) {
                 const int j = (k - 1 + 2 * R) % R;
                 pb[0 * PROW + me0] = pp[0][j].x;
                 pb[1 * PROW + me0] = pp[0][j].y;
@@ -455,7 +458,7 @@ __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, fl
                 issue_plane<PY>(maps, stages + st * STAGE_BYTES, smem_u32(&mbar[st]), xf, xb, Y0, q + TB_S);
 
             // ---- stage 0: residual of plane q-1 at time 0
-            if (check) {
+            if (chk) {
                 const int j = (k - 1 + R) % R, ju = k, jd = (k - 2 + R) % R;
                 float lB[PY], rA[PY];
 #pragma unroll
@@ -486,7 +489,7 @@ __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, fl
             // ---- stages 1..T: plane q-1-t (slot k-1-t) from time t-1 to t (pattern sA above)
 #pragma unroll
             for (int t = 1; t <= T; ++t) {
-                if (t <= nhalf) {
+                if (FULL || t <= nhalf) {  // FULL: nhalf == T, one basic block per stage run
                     const int j = (k - 1 - t + 2 * R) % R;
                     const int ju = (k - t + 2 * R) % R;
                     const int jd = (k - 2 - t + 2 * R) % R;
@@ -571,11 +574,11 @@ __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, fl
             }
         }
     }
-    if (check) block_max_to(rmax, &status->rmax_bits[group]);
+    if (chk) block_max_to(rmax, &status->rmax_bits[group]);
     if (YCLUSTER) cluster_sync_all();  // no CTA leaves while a neighbour may still address it
 }
 
-template <int T, int PY>
+template <int T, int PY, bool FULL, int CHK>
 __global__ void __launch_bounds__(TBGeom<PY>::THREADS, 1)
 k_sweep_tb(const __grid_constant__ TBMaps maps, Grid g, float* __restrict__ Pout, int nhalf,
            int colour0, int zchunk, const __grid_constant__ WAcc8 wa, StepStatus* status, int check, int group,
@@ -583,8 +586,9 @@ k_sweep_tb(const __grid_constant__ TBMaps maps, Grid g, float* __restrict__ Pout
            const int* __restrict__ group_base) {
     // inside a graph's device-side group loop the group index is relative to the loop counter
     if (group_base != nullptr) group += *group_base;
-    sweep_tile<T, PY>(maps, g, Pout, nhalf, colour0, zchunk, wa, status, check, group, tol, pcur, out_idx,
-                      kerr, (int)blockIdx.x, (int)blockIdx.y, (int)blockIdx.z);
+    sweep_tile<T, PY, false, false, FULL, CHK>(maps, g, Pout, nhalf, colour0, zchunk, wa, status, check, group,
+                                               tol, pcur, out_idx, kerr, (int)blockIdx.x, (int)blockIdx.y,
+                                               (int)blockIdx.z);
 }
 
 // The y-cluster form (2-row patches): runs of ycl_n CTAs along y form clusters, with a halo of
@@ -619,7 +623,7 @@ struct GroupTBGrid {
 
 // CTA b of the launch takes tile b of the flat index space (the tiles of one grid are
 // contiguous; `starts` holds n + 1 prefix sums).  in_a: read P and write P2, else the reverse.
-template <int T>
+template <int T, bool FULL, int CHK>
 __global__ void __launch_bounds__(TBGeom<2>::THREADS, 1)
 k_group_sweep_tb(const GroupTBGrid* __restrict__ grids, const int* __restrict__ starts, int n, int in_a,
                  int nhalf, int colour0, int zchunk, int check, int group, const int* __restrict__ group_base) {
@@ -642,8 +646,8 @@ k_group_sweep_tb(const GroupTBGrid* __restrict__ grids, const int* __restrict__ 
     int* const pcur = d.pcur;
     int* const kerr = d.kerr;
     const float tol = d.tol;
-    sweep_tile<T, 2, true>(d.maps[in_a ? 0 : 1], g, Pout, nhalf, colour0, zchunk, d.wa, status, check, group, tol,
-                           pcur, in_a ? 1 : 0, kerr, bx, by, bz);
+    sweep_tile<T, 2, true, false, FULL, CHK>(d.maps[in_a ? 0 : 1], g, Pout, nhalf, colour0, zchunk, d.wa, status,
+                                             check, group, tol, pcur, in_a ? 1 : 0, kerr, bx, by, bz);
 }
 
 // End of one iteration of a grouped step's device-side loop over tolerance groups: advance
@@ -710,8 +714,12 @@ constexpr size_t tb_smem_bytes() {
 
 template <int T, int PY>
 int configure_tb() {
-    return cudaFuncSetAttribute(k_sweep_tb<T, PY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)tb_smem_bytes<T, PY>()) == cudaSuccess ? 0 : -1;
+    const int bytes = (int)tb_smem_bytes<T, PY>();
+    const cudaFuncAttribute attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    const bool ok = cudaFuncSetAttribute(k_sweep_tb<T, PY, false, -1>, attr, bytes) == cudaSuccess &&
+                    cudaFuncSetAttribute(k_sweep_tb<T, PY, true, 0>, attr, bytes) == cudaSuccess &&
+                    cudaFuncSetAttribute(k_sweep_tb<T, PY, true, 1>, attr, bytes) == cudaSuccess;
+    return ok ? 0 : -1;
 }
 
 template <int T, int PY>
@@ -725,9 +733,16 @@ int launch_tb(const TBMaps& maps, const Grid& g, float* Pout, int nhalf, int col
     wa.w[7] = 0.0f;
     dim3 grid((unsigned)sweep_windows(g.nx, 2 * TB_TX, T), (unsigned)sweep_windows(g.ny, G::ROWS, T),
               (unsigned)((g.nz + zchunk - 1) / zchunk));
-    k_sweep_tb<T, PY><<<grid, dim3(TB_TX, G::TY), smem, st>>>(maps, g, Pout, nhalf, colour0, zchunk, wa,
-                                                             status, check, group, tol, pcur, out_idx,
-                                                             kerr, group_base);
+    // a launch of all T colour passes runs an instantiation without per-stage tests and with the
+    // check code present or absent; a partial launch decides both at run time
+#define SMK_TB_LAUNCH(FULL, CHK)                                                                             \
+    k_sweep_tb<T, PY, FULL, CHK><<<grid, dim3(TB_TX, G::TY), smem, st>>>(maps, g, Pout, nhalf, colour0, zchunk, \
+                                                                        wa, status, check, group, tol, pcur,  \
+                                                                        out_idx, kerr, group_base)
+    if (nhalf == T && check) SMK_TB_LAUNCH(true, 1);
+    else if (nhalf == T) SMK_TB_LAUNCH(true, 0);
+    else SMK_TB_LAUNCH(false, -1);
+#undef SMK_TB_LAUNCH
     return 0;
 }
 
@@ -826,8 +841,12 @@ int sweep_ycluster_usable(const Grid& g, int n_req) {
 }
 
 int prepare_sweep_kernels() {
-    const int grouped = cudaFuncSetAttribute(k_group_sweep_tb<GROUP_TB_DEPTH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)tb_smem_bytes<GROUP_TB_DEPTH, 2>()) == cudaSuccess ? 0 : -1;
+    const int gbytes = (int)tb_smem_bytes<GROUP_TB_DEPTH, 2>();
+    const cudaFuncAttribute gattr = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    const int grouped = (cudaFuncSetAttribute(k_group_sweep_tb<GROUP_TB_DEPTH, false, -1>, gattr, gbytes) == cudaSuccess &&
+                         cudaFuncSetAttribute(k_group_sweep_tb<GROUP_TB_DEPTH, true, 0>, gattr, gbytes) == cudaSuccess &&
+                         cudaFuncSetAttribute(k_group_sweep_tb<GROUP_TB_DEPTH, true, 1>, gattr, gbytes) == cudaSuccess)
+                            ? 0 : -1;
     const int ycl = cudaFuncSetAttribute(k_sweep_tb_ycl<YCL_DEPTH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)tb_smem_bytes<YCL_DEPTH, 2>()) == cudaSuccess ? 0 : -1;
     return configure_tb<2, 2>() | configure_tb<4, 2>() | configure_tb<6, 2>() | configure_tb<4, 4>() | grouped | ycl;
@@ -906,10 +925,16 @@ int group_tb_fill(void* rec, const SweepMaps* m, const Grid& g, float* P, float*
 int launch_group_sweep_tb(const void* grids, const int* starts, int n, int total_tiles, bool in_a, int nhalf,
                           int colour0, int zchunk, int check, int group, const int* group_base, cudaStream_t st) {
     if (total_tiles <= 0) return 0;
-    k_group_sweep_tb<GROUP_TB_DEPTH><<<(unsigned)total_tiles, dim3(TB_TX, TBGeom<2>::TY),
-                                       tb_smem_bytes<GROUP_TB_DEPTH, 2>(), st>>>(
-        static_cast<const GroupTBGrid*>(grids), starts, n, in_a ? 1 : 0, nhalf, colour0, zchunk, check, group,
-        group_base);
+    // as launch_tb: full launches without per-stage tests, check code present only where needed
+#define SMK_GTB_LAUNCH(FULL, CHK)                                                                             \
+    k_group_sweep_tb<GROUP_TB_DEPTH, FULL, CHK><<<(unsigned)total_tiles, dim3(TB_TX, TBGeom<2>::TY),          \
+                                                 tb_smem_bytes<GROUP_TB_DEPTH, 2>(), st>>>(                  \
+        static_cast<const GroupTBGrid*>(grids), starts, n, in_a ? 1 : 0, nhalf, colour0, zchunk, check, group, \
+        group_base)
+    if (nhalf == GROUP_TB_DEPTH && check) SMK_GTB_LAUNCH(true, 1);
+    else if (nhalf == GROUP_TB_DEPTH) SMK_GTB_LAUNCH(true, 0);
+    else SMK_GTB_LAUNCH(false, -1);
+#undef SMK_GTB_LAUNCH
     return (int)cudaGetLastError();
 }
 
