@@ -364,6 +364,10 @@ def main():
     # ---- e2e through the public API with host buffers ----------------------------------------
     e2e_steps = args.e2e_steps or args.steps
     out = torch.empty(sc.cell_shape, dtype=torch.float32, pin_memory=True).numpy()
+    # warm-up calls (graph capture for this output buffer); the timed segments restart from the
+    # initial state
+    for _ in range(max(args.warmup, 1)):
+        sim.simulate(out, sc.dt)
     e2e_dt = 0.0
     for n in segments(e2e_steps):
         sim.write_state(initial)

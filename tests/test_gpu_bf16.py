@@ -99,3 +99,27 @@ def test_vector_stages_equal_per_cell_stages(gpu, storage, dims):
         assert H.first_mismatch(a.read_state(), b.read_state()) == "", k
     a.close()
     b.close()
+
+
+@pytest.mark.parametrize("storage", [smk.STORAGE_F32, smk.STORAGE_BF16_VEL, smk.STORAGE_BF16])
+def test_simulate_into_pinned_buffer_equals_copy(gpu, storage):
+    """smk_simulate into a pinned buffer (as the benchmark's end-to-end leg uses) returns the bits
+    of smk_simulate into a pageable buffer (as the reference's caller passes), step by step,
+    including a step that runs uncaptured (an object moved)."""
+    torch = pytest.importorskip("torch")
+    sc = S.small_scene(37, 22, 19, steps=6, seed=81, scheme=1, iterations=40, tol=1e-3, check_every=5,
+                       obstacles=1, warm_start=1)
+    a = smk.from_scene(sc, report_div=1, storage=storage)
+    b = smk.from_scene(sc, report_div=1, storage=storage)
+    pinned = torch.empty(sc.cell_shape, dtype=torch.float32, pin_memory=True).numpy()
+    pageable = np.empty(sc.cell_shape, np.float32)
+    for k in range(sc.steps):
+        if k == 3:
+            for s in (a, b):
+                s.update_object_pos(0, 12.0, 9.0, 8.0)
+        a.simulate(pinned, sc.dt)
+        b.simulate(pageable, sc.dt)
+        assert np.array_equal(pinned.view(np.uint32), pageable.view(np.uint32)), k
+    assert H.first_mismatch(a.read_state(), b.read_state()) == ""
+    a.close()
+    b.close()
