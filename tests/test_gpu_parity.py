@@ -414,3 +414,23 @@ def test_ycluster_runs_equal_oracle_on_tall_grid(gpu, n):
         assert st.sweeps == ost.sweeps and st.resid_max == ost.resid_max and st.div_max == ost.div_max
         assert H.first_mismatch(sim.read_state(), H.oracle_state(o)) == "", k
     sim.close()
+
+
+@pytest.mark.parametrize("kernel", [(6, 21), (6, 117), (4, 17), (2, 15), (4, 17, 4)])
+def test_edge_windows_equal_oracle(gpu, kernel):
+    """Windows that reach the grid's edge carry no halo on that side where that saves windows
+    (depth 6: two along x at nx = 110, three along y at ny = 64), and a first z-chunk starts at
+    plane 0 where that saves a pass of the unrolled loop (z-chunks 21, 17, 15): bit-exact with the
+    oracle, sweep counts and residuals included."""
+    sc = S.small_scene(110, 64, 40, steps=4, seed=91, scheme=1, iterations=36, tol=1e-3, check_every=6,
+                       obstacles=2, warm_start=1)
+    o = O.OracleSim(sc)
+    sim = smk.from_scene(sc, report_div=1)
+    sim.set_sweep_kernel(*kernel)
+    for k in range(sc.steps):
+        ost = o.step()
+        sim.step(sc.dt)
+        st = sim.stats()
+        assert st.sweeps == ost.sweeps and st.resid_max == ost.resid_max and st.div_max == ost.div_max, k
+        assert H.first_mismatch(sim.read_state(), H.oracle_state(o)) == "", k
+    sim.close()
