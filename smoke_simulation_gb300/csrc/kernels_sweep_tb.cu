@@ -11,7 +11,9 @@
 // t = 1..T, so plane q-1-T leaves the pipeline finished.  A colour-t cell reads only
 // opposite-colour neighbours, whose time t-1 values are exactly what the neighbouring planes
 // hold at that moment, so one copy of each plane suffices.  Halo cells are recomputed
-// redundantly; cells within T - t of the interior are exact after half-sweep t.
+// redundantly; cells within T - t of the interior are exact after half-sweep t.  A window side
+// that reaches the grid's edge needs no halo where that saves windows (sweep_window), and a
+// z-chunk near plane 0 starts there where that saves a pass of the unrolled loop (qbeg).
 //
 // Loads.  Planes arrive through TMA: thread 0 issues cp.async.bulk.tensor copies of the
 // tile's P, b and flag boxes for plane q+S into an S-stage shared-memory ring (S = (T+4)/2,
@@ -40,11 +42,13 @@
 // flag byte (six neighbour bits + "projectable"), kept in shared memory once per lane so that
 // lookups never conflict.
 //
-// Forms (one tile body, sweep_tile): k_sweep_tb<T, PY> (one grid, tensor maps as kernel
-// parameters), k_group_sweep_tb<6> (the tiles of every grid of a batch in one launch, each
-// grid's tensor maps in global memory), k_sweep_tb_ycl<6> (runs of 2, 4 or all of the CTAs of
-// an x-z column as thread-block clusters that exchange boundary rows through distributed shared
-// memory instead of recomputing a y-halo between them).
+// Forms (one tile body, sweep_tile): k_sweep_tb<T, PY, FULL, CHK> (one grid, tensor maps as
+// kernel parameters), k_group_sweep_tb<6, FULL, CHK> (the tiles of every grid of a batch in one
+// launch, each grid's tensor maps in global memory), k_sweep_tb_ycl<6> (runs of 2, 4 or all of
+// the CTAs of an x-z column as thread-block clusters that exchange boundary rows through
+// distributed shared memory instead of recomputing a y-halo between them).  Launches of all T
+// colour passes run the FULL instantiations (no per-stage tests), with the tolerance-check code
+// compiled in (CHK = 1) or out (CHK = 0); partial launches test both at run time.
 #include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
