@@ -317,18 +317,24 @@ int smk_server_destroy(smk_server* server);
 const char* smk_server_last_error(void);
 
 /* Pressure projection of a caller-owned velocity field that allocates no device memory.
- * No counterpart in the reference: it is for callers that cannot call cudaMalloc when they need
- * the projection (inside a stream capture, under a fixed-budget or framework-owned memory
- * pool, in a hook where a synchronising allocation is not allowed).  u, v, w: device arrays in
- * the reference's face layout ((nx+1)(ny+1)(nz+1) floats, x fastest), projected in place;
- * mask: device array of nx*ny*nz bytes, nonzero = fluid.  Uses params->max_sweeps, omega, tol
- * and check_every with the PRESSURE scheme's arithmetic (results equal smk_step's projection).
- * Scratch comes from one fixed device array inside the library (about 19 MB, held by every GPU
- * that loads the library until exit): grids with (nx+1)(ny+1)(nz+1) > 2,097,152 are rejected
- * with SMK_ERR_INVALID.  All calls share that array: calls that overlap on the GPU race; order
- * them on one stream.  The first call on a device looks up the array's address
- * (cudaGetSymbolAddress): make it before any stream capture.  stats may be NULL (stream-ordered
- * call); when given, the call synchronises `stream` and fills sweeps/converged/resid/div. */
+ * No counterpart in the reference.  It is for callers that cannot call cudaMalloc when they need
+ * the projection: an application that has handed the device's memory to its own pool allocator
+ * or runs under a fixed memory budget, or a plugin called from a per-frame or per-request
+ * callback where cudaMalloc's implicit device-wide synchronisation would stall other work.
+ * u, v, w: device arrays in the reference's face layout ((nx+1)(ny+1)(nz+1) floats, x fastest),
+ * projected in place; mask: device array of nx*ny*nz bytes, nonzero = fluid.  Runs the PRESSURE
+ * scheme's red-black SOR from a zero pressure (params->projection must be SMK_PROJECT_PRESSURE,
+ * solver SMK_SOLVER_RBSOR, refine 0; warm_start is ignored) with params->max_sweeps, omega
+ * (0 < omega < 2), tol and check_every; the result equals, bit for bit, the projection that
+ * smk_step's PRESSURE scheme applies to the same field and mask from a zero pressure.  Scratch comes from one fixed device array inside the
+ * library (about 19 MB, held by every GPU that loads the library until exit): grids with
+ * (nx+1)(ny+1)(nz+1) > 2,097,152 or nz > 65535 are rejected with SMK_ERR_INVALID.  All calls
+ * share that array and find the previous call's contents in it (each call rewrites what it
+ * reads): calls that overlap on the GPU race; order them on one stream.  The first call on a
+ * device, with that device current, looks up the array's address (cudaGetSymbolAddress; again
+ * after the device's context was replaced, e.g. by cudaDeviceReset): make it before any stream
+ * capture.  stats may be NULL (stream-ordered call); when given, the call synchronises `stream`
+ * and fills sweeps/converged/resid/div, and `stream` must not be under capture. */
 int smk_project_noalloc(float* u, float* v, float* w, const uint8_t* mask, int nx, int ny, int nz,
                         const smk_params* params, smk_stats* stats, void* stream);
 /* The size limit above, and the message of the last failed smk_project_noalloc call. */

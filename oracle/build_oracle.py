@@ -25,6 +25,17 @@ float instantiation is then bit-identical to the reference's own arithmetic.
       default floating-point options (as the reference's own CMake build does) into
       oracle/_ref/libsmoke_ref_gpu.so.  Not part of the parity chain (nvcc contracts a*b+c
       into FMAs, so it differs from the host build by rounding).
+
+4. The reference's proxy-plane geometry built for the host (the checker of smk_proxy_planes):
+   where the reference checkout is present, the free functions pseudoangle, getMinMaxPoints,
+   teselate, sortPoints, rayPlaneIntersection, planeBoxIntersections, duplicate and the member
+   BoundingBox::generateProxyGeometry are taken verbatim from project/boundingBox.cpp (whole
+   function bodies, found by their signature lines and brace matching) into
+   oracle/_ref/ref_proxy_host.cpp between oracle/ref_proxy_prelude.inc (the declarations they
+   need; boundingBox.h itself includes OpenGL) and oracle/ref_proxy_tail.inc (a C entry point),
+   and compiled with g++ against the checkout's vendored glm (external_src/glm/include) into
+   oracle/_ref/libsmoke_ref_proxy.so.  glm is not on machines without the checkout, so this
+   build exists only here; tests/golden/make_golden.py records its outputs as fixtures.
 """
 from __future__ import annotations
 
@@ -36,8 +47,13 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
+# The reference checkout: SMOKE_REFERENCE_SRC names its project/smokeSimulation.cu directly;
+# otherwise SMOKE_REFERENCE_ROOT names the checkout, by default a directory `reference` beside
+# this repository's own checkout.
+REFERENCE_ROOT = os.environ.get(
+    "SMOKE_REFERENCE_ROOT", os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference"))
 REFERENCE_SRC = os.environ.get(
-    "SMOKE_REFERENCE_SRC", "/root/reference/project/smokeSimulation.cu")
+    "SMOKE_REFERENCE_SRC", os.path.join(REFERENCE_ROOT, "project", "smokeSimulation.cu"))
 
 ORACLE_SO = os.path.join(BUILD, "libsmoke_oracle.so")
 REF_CPP = os.path.join(REF_OUT, "ref_step_host.cpp")
@@ -186,6 +202,73 @@ def build_reference_gpu(force: bool = False) -> str | None:
         _run(["nvcc", "-O3", "-gencode", "arch=compute_103a,code=sm_103a", "-Xcompiler", "-fPIC",
               "-shared", "-w", "-I", HERE, REF_GPU_CU, "-o", REF_GPU_SO])
     return REF_GPU_SO
+
+
+REF_PROXY_CPP = os.path.join(REF_OUT, "ref_proxy_host.cpp")
+REF_PROXY_SO = os.path.join(REF_OUT, "libsmoke_ref_proxy.so")
+BOUNDING_BOX_SRC = os.path.join(REFERENCE_ROOT, "project", "boundingBox.cpp")
+GLM_INCLUDE = os.path.join(REFERENCE_ROOT, "external_src", "glm", "include")
+# signature lines (at the start of a line) of the functions taken from boundingBox.cpp
+PROXY_FUNCTIONS = [
+    "float pseudoangle(float y, float x)",
+    "void BoundingBox::generateProxyGeometry(",
+    "void getMinMaxPoints(",
+    "std::vector<short> teselate(",
+    "void sortPoints(",
+    "bool rayPlaneIntersection(",
+    "std::vector<vec3> planeBoxIntersections(",
+    "bool duplicate(",
+]
+
+
+def extract_function(text: str, signature: str) -> str:
+    """The whole definition that starts with `signature` at the start of a line: from that line
+    to the brace closing its body (the functions contain no braces in strings or comments)."""
+    m = re.search(r"^" + re.escape(signature), text, re.M)
+    if m is None:
+        raise RuntimeError("function not found in boundingBox.cpp: " + signature)
+    open_at = text.index("{", m.start())
+    depth = 0
+    for k in range(open_at, len(text)):
+        if text[k] == "{":
+            depth += 1
+        elif text[k] == "}":
+            depth -= 1
+            if depth == 0:
+                return text[m.start():k + 1]
+    raise RuntimeError("unbalanced braces after " + signature)
+
+
+def generate_reference_proxy_tu() -> bool:
+    if not (os.path.exists(BOUNDING_BOX_SRC) and os.path.isdir(GLM_INCLUDE)):
+        return False
+    os.makedirs(REF_OUT, exist_ok=True)
+    with open(BOUNDING_BOX_SRC, "r", encoding="utf-8", errors="replace") as f:
+        text = f.read()
+    parts = ['#include "ref_proxy_prelude.inc"']
+    for sig in PROXY_FUNCTIONS:
+        parts.append("// ---- from project/boundingBox.cpp ----")
+        parts.append(extract_function(text, sig))
+    parts.append('#include "ref_proxy_tail.inc"')
+    new = "\n\n".join(parts) + "\n"
+    old = None
+    if os.path.exists(REF_PROXY_CPP):
+        with open(REF_PROXY_CPP) as f:
+            old = f.read()
+    if old != new:
+        with open(REF_PROXY_CPP, "w") as f:
+            f.write(new)
+    return True
+
+
+def build_reference_proxy(force: bool = False) -> str | None:
+    """oracle/_ref/libsmoke_ref_proxy.so, or None without the reference checkout and its glm."""
+    if not generate_reference_proxy_tu():
+        return None
+    deps = [REF_PROXY_CPP, os.path.join(HERE, "ref_proxy_prelude.inc"), os.path.join(HERE, "ref_proxy_tail.inc")]
+    if force or _stale(REF_PROXY_SO, *deps):
+        _run(["g++", *CXXFLAGS, "-w", "-I", GLM_INCLUDE, "-I", HERE, REF_PROXY_CPP, "-o", REF_PROXY_SO])
+    return REF_PROXY_SO
 
 
 def build(force: bool = False) -> dict:

@@ -1,28 +1,36 @@
 // smk_project_noalloc: the pressure projection for callers that cannot allocate device memory.
 //
-// Some callers cannot call cudaMalloc at the time they need a projection: code running inside
-// a CUDA graph being captured, a host that has handed the whole device memory pool to another
-// allocator (a framework caching allocator, a fixed-budget serving arena), or a hook invoked
-// from a context where a blocking, device-synchronising allocation is not allowed.  This entry
-// point projects a caller-owned velocity field in place and takes its scratch -- the pressure,
-// the right-hand side, the neighbour flags and the solver status -- from one file-scope device
-// array of fixed size instead of allocating.
+// Some callers of a projection cannot call cudaMalloc when they need one: a host application
+// that has handed the device's memory to its own pool allocator (a framework's caching
+// allocator, a serving arena with a fixed budget) and so has nothing left for a library to
+// take, or a plugin called from a per-frame or per-request callback, where cudaMalloc's implicit
+// device-wide synchronisation would stall the other work on the GPU.  This entry point projects
+// a caller-owned velocity field in place and takes its scratch -- the pressure, the right-hand
+// side, the neighbour flags and the solver status -- from one file-scope device array of fixed
+// size instead of allocating.
 //
 // Limits and sharing:
 //   - at most NOALLOC_MAX_ELEMS = 2,097,152 face-grid elements, (nx+1)(ny+1)(nz+1) (e.g. a
-//     127^3 grid); larger grids are rejected with SMK_ERR_INVALID;
+//     127^3 grid), and nz <= 65535; larger grids are rejected with SMK_ERR_INVALID;
 //   - the scratch array (about 19 MB) is held by every GPU that loads the library, until exit;
-//   - every call shares it: calls whose work overlaps on the GPU (different streams, or the same
-//     array from several host threads without ordering) race and corrupt each other.  Callers
-//     must order their calls on one stream or synchronise between them;
-//   - the first call on a device looks up the array's device address with
-//     cudaGetSymbolAddress; make that first call before any stream capture.
+//   - every call shares it and finds it holding the previous call's contents: the call zeroes
+//     the solver status and rewrites the flags, the right-hand side and the pressure of its
+//     own grid before reading them;
+//   - calls whose work overlaps on the GPU (different streams, or several host threads without
+//     ordering) race on the array and corrupt each other.  Callers must order their calls on one
+//     stream or synchronise between them;
+//   - the first call on a device (and the first after that device's primary context was
+//     replaced, e.g. by cudaDeviceReset) looks up the array's device address with
+//     cudaGetSymbolAddress, with that device current; make that first call before any stream
+//     capture.
 // The entry point calls no cudaMalloc/cudaFree (nor any allocating library routine): only kernel
 // launches, cudaMemsetAsync on the scratch, and -- when statistics are requested -- a
 // synchronisation and small device-to-host copies.
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <cmath>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -46,7 +54,12 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[SCRATCH_BYTES];
 
 constexpr int MAX_DEVICES = 64;
 std::mutex g_mutex;
-void* g_scratch_dev[MAX_DEVICES] = {nullptr};
+// per device: the scratch array's device address and the context it was looked up in
+struct ScratchAddr {
+    void* ptr = nullptr;
+    CUcontext ctx = nullptr;
+};
+ScratchAddr g_scratch_dev[MAX_DEVICES];
 thread_local std::string g_err;
 
 // Neighbour flags from a caller's tight mask (nx*ny*nz bytes, x fastest) into the face-pitched
@@ -79,21 +92,47 @@ int fail(int code, const std::string& m) {
     return code;
 }
 
-// Device address of the scratch array on the current device (looked up once per device).
+// The current context (driver entry point fetched through the runtime, so the library needs
+// no link against libcuda).
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+CUcontext current_context() {
+    static CtxGetCurrentFn fn = nullptr;
+    static bool tried = false;
+    if (!tried) {
+        tried = true;
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<CtxGetCurrentFn>(p);
+    }
+    CUcontext c = nullptr;
+    if (fn == nullptr || fn(&c) != CUDA_SUCCESS) return nullptr;
+    return c;
+}
+
+// Device address of the scratch array on the current device: looked up once per device and
+// again when the device's context changed since (a cudaDeviceReset replaces it, and with it
+// the array's address).
 int scratch_for_current_device(unsigned char** out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return fail(SMK_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
     if (dev < 0 || dev >= MAX_DEVICES) return fail(SMK_ERR_INVALID, "device index out of range");
+    // null when this thread has not used the device yet: the lookup below makes the device's
+    // primary context current, and the context is read again after it
+    const CUcontext ctx = current_context();
     std::lock_guard<std::mutex> lock(g_mutex);
-    if (g_scratch_dev[dev] == nullptr) {
+    ScratchAddr& a = g_scratch_dev[dev];
+    if (a.ptr == nullptr || ctx == nullptr || a.ctx != ctx) {
         void* p = nullptr;
         e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || p == nullptr)
             return fail(SMK_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
-        g_scratch_dev[dev] = p;
+        a.ptr = p;
+        a.ctx = current_context();
     }
-    *out = static_cast<unsigned char*>(g_scratch_dev[dev]);
+    *out = static_cast<unsigned char*>(a.ptr);
     return SMK_OK;
 }
 
@@ -115,20 +154,37 @@ int smk_project_noalloc(float* u, float* v, float* w, const uint8_t* mask, int n
                         const smk_params* params, smk_stats* stats, void* stream) {
     if (!u || !v || !w || !mask || !params) return fail(SMK_ERR_INVALID, "null argument");
     if (nx < 1 || ny < 1 || nz < 1) return fail(SMK_ERR_INVALID, "grid dimensions must be >= 1");
-    const long long elems = (long long)(nx + 1) * (ny + 1) * (nz + 1);
+    // widened before the additions: nx + 1 must not wrap for nx near INT_MAX
+    const long long elems = ((long long)nx + 1) * ((long long)ny + 1) * ((long long)nz + 1);
     if (elems > NOALLOC_MAX_ELEMS)
         return fail(SMK_ERR_INVALID,
                     "grid too large for the no-allocation projection: (nx+1)(ny+1)(nz+1) = " +
                         std::to_string(elems) + " exceeds the fixed scratch of " +
                         std::to_string(NOALLOC_MAX_ELEMS) + " elements");
+    if (nz > 65535) return fail(SMK_ERR_INVALID, "nz must be <= 65535 (one launch plane per z)");
     const smk_params& p = *params;
     const bool use_tol = p.tol > 0.0f;
-    if (p.max_sweeps < 0) return fail(SMK_ERR_INVALID, "max_sweeps must be >= 0");
+    if (p.projection != SMK_PROJECT_PRESSURE || p.solver != SMK_SOLVER_RBSOR)
+        return fail(SMK_ERR_INVALID, "the no-allocation projection runs the PRESSURE scheme's red-black SOR only "
+                                     "(projection = SMK_PROJECT_PRESSURE, solver = SMK_SOLVER_RBSOR)");
+    if (p.refine != 0) return fail(SMK_ERR_INVALID, "the no-allocation projection has no refinement rounds (refine = 0)");
+    if (!std::isfinite(p.omega) || !(p.omega > 0.0) || !(p.omega < 2.0))
+        return fail(SMK_ERR_INVALID, "omega must be finite and in (0, 2)");
+    if (!std::isfinite(p.tol) || p.tol < 0.0f) return fail(SMK_ERR_INVALID, "tol must be finite and >= 0");
+    if (p.max_sweeps < 0 || p.max_sweeps > 1000000) return fail(SMK_ERR_INVALID, "max_sweeps must be 0..1000000");
     if (use_tol && p.check_every <= 0) return fail(SMK_ERR_INVALID, "check_every must be positive when tol > 0");
     const int G = use_tol ? p.check_every : (p.max_sweeps > 0 ? p.max_sweeps : 1);
     const int ngroups = (p.max_sweeps + G - 1) / G;
     if (ngroups > NOALLOC_GROUPS) return fail(SMK_ERR_INVALID, "too many residual checks per call");
 
+    cudaStream_t st = (cudaStream_t)stream;
+    if (stats) {
+        // statistics need a synchronisation of `stream`, which a stream under capture refuses
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        NA_CUDA(cudaStreamIsCapturing(st, &cs));
+        if (cs != cudaStreamCaptureStatusNone)
+            return fail(SMK_ERR_INVALID, "stats must be NULL while `stream` is being captured");
+    }
     unsigned char* scratch = nullptr;
     int rc = scratch_for_current_device(&scratch);
     if (rc) return rc;
@@ -136,7 +192,6 @@ int smk_project_noalloc(float* u, float* v, float* w, const uint8_t* mask, int n
     float* b = reinterpret_cast<float*>(scratch + OFF_B);
     uint8_t* flags = scratch + OFF_F;
     smk::StepStatus* status = reinterpret_cast<smk::StepStatus*>(scratch + OFF_STATUS);
-    cudaStream_t st = (cudaStream_t)stream;
 
     // The caller's faces use the reference layout (stride nx+1): solve on that pitch.
     smk::Grid g;

@@ -1,0 +1,147 @@
+"""Parity at the benchmark's own configurations.
+
+The benchmark times the 256^3 workload (5% random solids + two spheres, four emitters, dt 0.02,
+warm-started pressure red-black SOR to max|residual| <= 1e-4 checked every 6 sweeps, cap 200)
+with the autotuned blocked sweep shape, CUDA-graph replay and the device-side tolerance loop,
+and the 512^3 mixed-precision form (FP32, BF16 velocities, all-BF16 storage, FP64-checked
+refinement).  These tests run exactly those paths and compare them with the oracle:
+
+  - 256^3: every field of both ping-pong buffers bit for bit against the FP32 restatement after
+    every step (autotuned shape, and the shape the recorded benchmark runs chose: depth 6, 2-row
+    patches, z-chunk 117, three z-chunks of which one is partial), plus the error of each step's
+    fields against the FP64 oracle of the same discretisation;
+  - 512^3: the three storage forms against the FP64 oracle (and the FP32 form bit for bit
+    against the FP32 restatement), 2 steps.
+
+Reference logic: project/smokeSimulation.cu:774-819 through the pinned restatement.  When the
+environment variable SMK_RECORD_DIR names a directory, the measured errors are written there as
+JSON (the benchmark line quotes them).
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import smoke_simulation_gb300 as smk
+from oracle import oracle as O
+from smoke_simulation_gb300 import scenes as S
+from tests import helpers as H
+
+pytestmark = pytest.mark.gpu
+
+# BF16 storage tolerances against the FP64 oracle (density relative L2): the velocities alone in
+# BF16 keep the 1e-3 bar; all-BF16 storage rounds every stored density (relative error up to
+# 2^-9), so its bar is 3e-3.
+BF16_VEL_RHO_REL_L2 = 1e-3
+BF16_ALL_RHO_REL_L2 = 3e-3
+
+
+def _record(name, data):
+    d = os.environ.get("SMK_RECORD_DIR")
+    if not d:
+        return
+    os.makedirs(d, exist_ok=True)
+    with open(os.path.join(d, name), "w") as f:
+        json.dump(data, f, indent=1, sort_keys=True)
+
+
+def _errors(st, o64):
+    """max-abs and rel-L2 of every field of both buffers against the FP64 oracle."""
+    out = {}
+    for k in ("rho", "u", "v", "w"):
+        ma, rl = 0.0, 0.0
+        for j in range(2):
+            ma = max(ma, H.max_abs(st[k][j], getattr(o64, k)[j]))
+            rl = max(rl, H.rel_l2(st[k][j], getattr(o64, k)[j]))
+        out[k] = {"max_abs": ma, "rel_l2": rl}
+    return out
+
+
+def _within_fp32_tolerances(err):
+    assert err["rho"]["max_abs"] <= H.DENSITY_MAX_ABS and err["rho"]["rel_l2"] <= H.DENSITY_REL_L2, err
+    for k in ("u", "v", "w"):
+        assert err[k]["max_abs"] <= H.VELOCITY_MAX_ABS and err[k]["rel_l2"] <= H.VELOCITY_REL_L2, err
+
+
+def test_large256_bit_exact_with_oracle_and_error_vs_fp64(gpu):
+    import torch
+    steps = 5
+    sc = S.config_large(n=256, steps=steps)
+    sc.warm_start = 1
+    tuned = smk.from_scene(sc, report_div=1)
+    depth, zchunk, _ = tuned.autotune()
+    fixed = smk.from_scene(sc, report_div=1)
+    fixed.set_sweep_kernel(6, 117, 2)
+    stream = torch.cuda.Stream()
+    o32 = O.OracleSim(sc)
+    o64 = O.OracleSim(sc, np.float64)
+    per_step = []
+    for k in range(steps):
+        s32 = o32.step()
+        s64 = o64.step()
+        for sim in (tuned, fixed):
+            sim.step(sc.dt, stream.cuda_stream)
+            torch.cuda.synchronize()
+            st = sim.stats()
+            assert (st.sweeps, st.converged) == (s32.sweeps, s32.converged), (k, st.sweeps, s32.sweeps)
+            assert st.resid_max == s32.resid_max and st.div_max == s32.div_max, k
+            msg = H.first_mismatch(sim.read_state(), H.oracle_state(o32))
+            assert msg == "", "step %d, shape %s: %s" % (k, sim.sweep_shape(), msg)
+        err = _errors(H.oracle_state(o32), o64)
+        _within_fp32_tolerances(err)
+        per_step.append({"step": k + 1, "sweeps": s32.sweeps, "sweeps_fp64": s64.sweeps,
+                         "div_max": s32.div_max, "err_vs_fp64": err})
+    worst = {k: {m: max(p["err_vs_fp64"][k][m] for p in per_step) for m in ("max_abs", "rel_l2")}
+             for k in ("rho", "u", "v", "w")}
+    _record("err_large256.json", {
+        "workload": "256^3 benchmark workload, warm start, %d steps" % steps,
+        "shapes_bit_exact": [list(tuned.sweep_shape()), list(fixed.sweep_shape())],
+        "autotuned": {"depth": depth, "zchunk": zchunk},
+        "worst_vs_fp64": worst, "per_step": per_step})
+    tuned.close()
+    fixed.close()
+
+
+def test_mixed512_forms_error_vs_fp64(gpu):
+    """The 512^3 mixed-precision form of the benchmark (2% random solids, one 32x8x32 emitter,
+    dt 0.02, warm-started FP32 pressure SOR to 1e-4 checked every 10 sweeps, FP64-checked
+    refinement of up to 2 rounds of 10 sweeps): FP32 storage bit for bit with the FP32
+    restatement, and every storage form's density and velocities against the FP64 oracle."""
+    import torch
+    steps = 2
+    sc = S.config_mixed(512, steps=steps)
+    sc.warm_start, sc.refine, sc.refine_sweeps = 1, 2, 10
+    stream = torch.cuda.Stream()
+    results = {}
+    states = {}
+    for name, storage in (("f32", smk.STORAGE_F32), ("bf16_vel", smk.STORAGE_BF16_VEL),
+                          ("bf16_all", smk.STORAGE_BF16)):
+        sim = smk.from_scene(sc, report_div=1, storage=storage)
+        sim.autotune()
+        divs = []
+        for _ in range(steps):
+            sim.step(sc.dt, stream.cuda_stream)
+            torch.cuda.synchronize()
+            st = sim.stats()
+            divs.append(max(st.div_max, st.div64_max))
+        states[name] = sim.read_state()
+        results[name] = {"max_div_post_projection": max(divs)}
+        sim.close()
+        torch.cuda.empty_cache()
+    o32 = O.OracleSim(sc).run(steps)
+    msg = H.first_mismatch(states["f32"], H.oracle_state(o32))
+    assert msg == "", msg
+    del o32
+    o64 = O.OracleSim(sc, np.float64).run(steps)
+    for name in results:
+        err = _errors(states[name], o64)
+        results[name]["err_vs_fp64"] = err
+        if name == "f32":
+            _within_fp32_tolerances(err)
+        results[name]["density_rel_l2_vs_f32"] = max(
+            H.rel_l2(states[name]["rho"][j], states["f32"]["rho"][j]) for j in range(2))
+    assert results["bf16_vel"]["err_vs_fp64"]["rho"]["rel_l2"] <= BF16_VEL_RHO_REL_L2, results
+    assert results["bf16_all"]["err_vs_fp64"]["rho"]["rel_l2"] <= BF16_ALL_RHO_REL_L2, results
+    _record("err_mixed512.json", {"workload": "512^3 mixed-precision form, %d steps" % steps,
+                                   "forms": results})
