@@ -214,6 +214,55 @@ def proxy_planes(view_origin, view_dir, box_pos, dims, planes: int):
     return verts, counts, tris
 
 
+_refp = None
+
+
+def reference_proxy_available() -> bool:
+    global _refp
+    if _refp is None:
+        path = build_oracle.build_reference_proxy()
+        if path is None or not os.path.exists(path):
+            return False
+        _refp = C.CDLL(path)
+        _refp.refp_proxy.restype = C.c_int
+        _refp.refp_proxy.argtypes = [C.c_void_p] * 4 + [C.c_int, C.c_void_p, C.c_int, C.c_void_p,
+                                                          C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
+                                                          C.c_void_p]
+    return True
+
+
+def reference_proxy_planes(view_origin, view_dir, box_pos, dims, planes: int):
+    """The reference's own BoundingBox::generateProxyGeometry (project/boundingBox.cpp:133-181,
+    built for the host by oracle/build_oracle.py step 4), converted to smk_proxy_planes' layout:
+    (vertices [planes, 7, 3], counts [planes], triangles [planes, 6, 3] as indices into the
+    [planes * 7] vertex array, -1 rows unused)."""
+    if not reference_proxy_available():
+        raise RuntimeError("reference proxy-geometry build unavailable (needs the reference checkout)")
+    f3 = lambda v: np.ascontiguousarray(v, np.float32)
+    vo, vd, bp, dm = f3(view_origin), f3(view_dir), f3(box_pos), f3(dims)
+    maxv, maxi = 7 * planes, 18 * planes
+    flat_v = np.zeros((maxv, 3), np.float32)
+    flat_i = np.zeros(maxi, np.int16)
+    nv, ni = C.c_int(), C.c_int()
+    pts = np.zeros(planes, np.int32)
+    toff = np.zeros(planes, np.int32)
+    rc = _refp.refp_proxy(vo.ctypes.data, vd.ctypes.data, bp.ctypes.data, dm.ctypes.data, planes,
+                          flat_v.ctypes.data, maxv, C.byref(nv), flat_i.ctypes.data, maxi, C.byref(ni),
+                          pts.ctypes.data, toff.ctypes.data)
+    if rc != 0:
+        raise RuntimeError("refp_proxy: output too small")
+    verts = np.zeros((planes, 7, 3), np.float32)
+    tris = np.full((planes, 6, 3), -1, np.int32)
+    voff = 0
+    for i in range(planes):
+        k = int(pts[i])
+        verts[i, :k + 1] = flat_v[voff:voff + k + 1]
+        t = flat_i[3 * toff[i]:3 * (toff[i] + k)].reshape(k, 3).astype(np.int32)
+        tris[i, :k] = t - voff + 7 * i
+        voff += k + 1
+    return verts, pts.copy(), tris
+
+
 def round_half(x: np.ndarray) -> np.ndarray:
     """The restatement's float -> binary16 -> float rounding (round to nearest even)."""
     lib = restatement()

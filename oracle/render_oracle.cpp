@@ -299,73 +299,96 @@ int orc_render(const float* rho, int nx, int ny, int nz, const orc_render_params
     return 0;
 }
 
-// Proxy-plane polygons (boundingBox.cpp:135-181, 228-345), the checker of smk_proxy_planes:
-// plane i of P at start + (end - start) * ((i + 0.5) / P) along d = normalize(-view_dir); the
-// box's 12 edges (X edges for y, z in {-1, 1}, then Y edges for x, z, then Z edges for y, x)
-// intersected with the plane (edges parallel to it skipped), exact repeats dropped, centroid
-// appended, points sorted by pseudo-angle about the centroid (descending, std::sort as the
-// reference), fan triangulation.  Output layout as smk_proxy_planes.
+// Proxy-plane polygons (boundingBox.cpp:87-92, 133-181, 231-360), the checker of
+// smk_proxy_planes, in the reference's own order of operations: d1 = normalize(-view_dir) (the
+// ray direction); getMinMaxPoints and sortPoints normalise it once more (d2 = normalize(d1));
+// the extreme projections of the box corners vec3(+-1,+-1,+-1) * dims / 2 (about the world
+// origin) on d2 give start = origin + d1 * min and end = origin + d1 * max; plane i (step
+// i + 0.5) lies at start + (end - start) * (step / planes), normal d1; the box's 12 edges (X
+// edges for y, z in {-1, 1}, then Y edges for x, z, then Z edges for y, x) are intersected with
+// it (t = dot(o - ro, d1) / dot(rd, d1), kept when 0 <= t <= edge length; edges parallel to the
+// plane are skipped), exact repeats dropped; the centroid is the sum divided by the count; the
+// points are sorted by pseudo-angle about it (ax = normalize(p0 - c), ay = cross(d2, ax), key
+// 1 + r below the ax axis, 3 - r above, evaluated in double as the reference's literals are),
+// descending, by a stable insertion sort (std::sort's order on the at most 6 points); fan
+// triangulation.  Output layout as smk_proxy_planes.
+static float proxy_key(float x, float y) {
+    const float r = x / (std::fabs(x) + std::fabs(y));
+    if (y < 0.0f) return (float)(1.0 + (double)r);
+    return (float)(3.0 - (double)r);
+}
+
 int orc_proxy_planes(const float* view_origin, const float* view_dir, const float* box_pos, const float* dims,
                      int planes, float* verts, int* counts, int* tris) {
-    const V3 d = norm3(mk(-view_dir[0], -view_dir[1], -view_dir[2]));
+    const V3 d1 = norm3(mk(-view_dir[0], -view_dir[1], -view_dir[2]));
+    const V3 d2 = norm3(d1);
     const V3 box = mk(box_pos[0], box_pos[1], box_pos[2]);
     const V3 dm = mk(dims[0], dims[1], dims[2]);
-    const V3 half = scl(dm, 0.5f);
+    const V3 half = mk(dm.x / 2.0f, dm.y / 2.0f, dm.z / 2.0f);
     const V3 vo = mk(view_origin[0], view_origin[1], view_origin[2]);
+    static const float corner_sign[8][3] = {{-1, -1, 1}, {1, -1, 1}, {-1, 1, 1}, {1, 1, 1},
+                                            {-1, -1, -1}, {1, -1, -1}, {-1, 1, -1}, {1, 1, -1}};
     float mn = 0.0f, mx = 0.0f;
     for (int c = 0; c < 8; ++c) {
-        const V3 corner = mk((c & 1) ? half.x : -half.x, (c & 2) ? half.y : -half.y, (c & 4) ? half.z : -half.z);
-        const float dd = dot3(sub(corner, vo), d);
-        if (c == 0 || dd < mn) mn = dd;
-        if (c == 0 || dd > mx) mx = dd;
+        const V3 corner = mk(corner_sign[c][0] * dm.x / 2.0f, corner_sign[c][1] * dm.y / 2.0f,
+                             corner_sign[c][2] * dm.z / 2.0f);
+        const float dd = dot3(sub(corner, vo), d2);
+        if (c == 0) mn = mx = dd;
+        if (dd < mn) mn = dd;
+        if (dd > mx) mx = dd;
     }
-    const V3 start = add(vo, scl(d, mn)), end = add(vo, scl(d, mx));
+    const V3 start = add(vo, scl(d1, mn)), end = add(vo, scl(d1, mx));
     const int MAXP = 7;
     for (int i = 0; i < planes; ++i) {
         const float t = ((float)i + 0.5f) / (float)planes;
         const V3 o = add(start, scl(sub(end, start), t));
         std::vector<V3> pts;
+        V3 c = mk(0.0f, 0.0f, 0.0f);
         for (int axis = 0; axis < 3; ++axis)
             for (int a = -1; a < 2; a += 2)
                 for (int b = -1; b < 2; b += 2) {
                     V3 ro, rd;
                     float len;
                     if (axis == 0) {
-                        ro = sub(box, mk(half.x, half.y * a, half.z * b));
+                        ro = sub(box, mk(half.x, half.y * (float)a, half.z * (float)b));
                         rd = mk(1.0f, 0.0f, 0.0f);
                         len = dm.x;
                     } else if (axis == 1) {
-                        ro = sub(box, mk(half.x * a, half.y, half.z * b));
+                        ro = sub(box, mk(half.x * (float)a, half.y, half.z * (float)b));
                         rd = mk(0.0f, 1.0f, 0.0f);
                         len = dm.y;
                     } else {
-                        ro = sub(box, mk(half.x * b, half.y * a, half.z));
+                        ro = sub(box, mk(half.x * (float)b, half.y * (float)a, half.z));
                         rd = mk(0.0f, 0.0f, 1.0f);
                         len = dm.z;
                     }
-                    const float den = dot3(rd, d);
+                    const float den = dot3(rd, d1);
                     if (den == 0.0f) continue;
-                    const float tt = dot3(sub(o, ro), d) / den;
+                    const float tt = dot3(sub(o, ro), d1) / den;
                     if (tt > len || tt < 0.0f) continue;
                     const V3 p = add(ro, scl(rd, tt));
                     bool dup = false;
                     for (const V3& q : pts) dup = dup || (p.x == q.x && p.y == q.y && p.z == q.z);
-                    if (!dup && (int)pts.size() < MAXP - 1) pts.push_back(p);
+                    if (!dup && (int)pts.size() < MAXP - 1) {
+                        pts.push_back(p);
+                        c = add(c, p);
+                    }
                 }
         const int k = (int)pts.size();
-        V3 c = mk(0.0f, 0.0f, 0.0f);
-        for (const V3& q : pts) c = add(c, q);
-        if (k > 0) c = scl(c, 1.0f / (float)k);
+        if (k > 0) c = mk(c.x / (float)k, c.y / (float)k, c.z / (float)k);
         if (k > 0) {
             const V3 ax = norm3(sub(pts[0], c));
-            const V3 ay = cross3(d, ax);
-            auto pa = [&](const V3& q) {
-                const V3 v = sub(q, c);
-                const float x = dot3(ax, v), y = dot3(ay, v);
-                const float r = x / (std::fabs(x) + std::fabs(y));
-                return y < 0.0f ? 1.0f + r : 3.0f - r;
-            };
-            std::sort(pts.begin(), pts.end(), [&](const V3& p1, const V3& p2) { return pa(p1) > pa(p2); });
+            const V3 ay = cross3(d2, ax);
+            std::vector<float> key(k);
+            for (int q = 0; q < k; ++q) {
+                const V3 v = sub(pts[q], c);
+                key[q] = proxy_key(dot3(ax, v), dot3(ay, v));
+            }
+            for (int q = 1; q < k; ++q)
+                for (int r = q; r > 0 && key[r] > key[r - 1]; --r) {
+                    std::swap(key[r], key[r - 1]);
+                    std::swap(pts[r], pts[r - 1]);
+                }
         }
         pts.push_back(c);
         counts[i] = k;

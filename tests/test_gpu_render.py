@@ -1,6 +1,8 @@
 """GPU tests of the headless half-angle slice renderer (smk_render): bit-exact with the CPU
 restatement (oracle/render_oracle.cpp) for both blending orders, for an analytic density and for
 a simulated one, in FP32 and BF16 density storage."""
+import os
+
 import numpy as np
 import pytest
 
@@ -59,3 +61,18 @@ def test_proxy_planes_bit_exact_with_restatement(gpu, view_dir):
     assert np.array_equal(v.view(np.uint32), ov.view(np.uint32))
     assert (c >= 3).all() and (c <= 6).all()
     assert np.abs(v).max() <= 40.0 + 1e-4
+
+
+def test_proxy_planes_bit_exact_with_reference_golden(gpu):
+    """Proxy-plane polygons on the device equal, bit for bit, the reference's own
+    BoundingBox::generateProxyGeometry (project/boundingBox.cpp:133-181) recorded in
+    tests/golden/proxy_planes.npz: the application's view, axis-aligned, diagonal and seeded
+    directions, unequal box sides."""
+    d = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "proxy_planes.npz"))
+    n = len([f for f in d.files if f.endswith("_args")])
+    assert n >= 10
+    for k in range(n):
+        a = d["case%02d_args" % k]
+        v, c, t = smk.proxy_planes(a[0:3], a[3:6], a[6:9], a[9:12], int(a[12]))
+        assert np.array_equal(c, d["case%02d_counts" % k]) and np.array_equal(t, d["case%02d_triangles" % k]), k
+        assert np.array_equal(v.view(np.uint32), d["case%02d_vertices" % k].view(np.uint32)), k

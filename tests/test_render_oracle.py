@@ -41,3 +41,40 @@ def test_alpha_grows_with_density(smoke_lib):
     a2 = O.render(0.6 * blob, rp)[0][..., 3]
     assert a1.max() > 0.05
     assert (a2 >= a1 - 1e-3).all() and a2.sum() > a1.sum()
+
+
+def _proxy_golden():
+    import os
+    d = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "proxy_planes.npz"))
+    out = []
+    for k in range(len([f for f in d.files if f.endswith("_args")])):
+        a = d["case%02d_args" % k]
+        args = (a[0:3], a[3:6], a[6:9], a[9:12], int(a[12]))
+        out.append((args, d["case%02d_vertices" % k], d["case%02d_counts" % k], d["case%02d_triangles" % k]))
+    return out
+
+
+def test_proxy_restatement_equals_reference_golden():
+    """The proxy-plane restatement (the checker of smk_proxy_planes) gives, bit for bit, the
+    reference's own BoundingBox::generateProxyGeometry output recorded in
+    tests/golden/proxy_planes.npz (project/boundingBox.cpp:133-181 built for the host)."""
+    for args, gv, gc, gt in _proxy_golden():
+        v, c, t = O.proxy_planes(*args)
+        assert np.array_equal(c, gc) and np.array_equal(t, gt), args
+        assert np.array_equal(v.view(np.uint32), gv.view(np.uint32)), args
+
+
+def test_proxy_restatement_equals_live_reference_build():
+    """Where the reference checkout is present, the restatement equals the reference's own
+    proxy-plane functions built for the host for many seeded view directions and plane counts."""
+    if not O.reference_proxy_available():
+        pytest.skip("the reference's proxy-plane build needs the reference checkout")
+    rng = np.random.default_rng(5)
+    for k in range(60):
+        d = rng.standard_normal(3)
+        dims = (80.0, 80.0, 80.0) if k % 3 else tuple(float(x) for x in rng.integers(8, 160, 3))
+        args = (tuple(rng.uniform(-50, 50, 3)), tuple(d), (0.0, 0.0, 0.0), dims, int(rng.integers(2, 120)))
+        rv, rc, rt = O.reference_proxy_planes(*args)
+        v, c, t = O.proxy_planes(*args)
+        assert np.array_equal(c, rc) and np.array_equal(t, rt), args
+        assert np.array_equal(v.view(np.uint32), rv.view(np.uint32)), args
