@@ -190,11 +190,38 @@ def cpu_reference_rate(n: int, sweeps: int, steps: int, threads: int = 0):
     return sc.cells * steps / dt, kind, cores, dt
 
 
+def max_div_reference(u, v, w, s) -> float:
+    """max |div u| over the cells the reference's projection updates (interior, fluid, at least
+    one fluid neighbour; project/smokeSimulation.cu:356-394), on face arrays (z, y, x) of shape
+    (nz+1, ny+1, nx+1) and a cell mask (nz, ny, nx)."""
+    s = np.asarray(s) != 0
+    nz, ny, nx = s.shape
+    div = ((u[:nz, :ny, 1:nx + 1].astype(np.float64) - u[:nz, :ny, :nx])
+           + (v[:nz, 1:ny + 1, :nx].astype(np.float64) - v[:nz, :ny, :nx])
+           + (w[1:nz + 1, :ny, :nx].astype(np.float64) - w[:nz, :ny, :nx]))
+    inner = np.zeros_like(s)
+    inner[1:-1, 1:-1, 1:-1] = True
+    nb = np.zeros(s.shape, np.int32)
+    nb[:, :, 1:] += s[:, :, :-1]
+    nb[:, :, :-1] += s[:, :, 1:]
+    nb[:, 1:, :] += s[:, :-1, :]
+    nb[:, :-1, :] += s[:, 1:, :]
+    nb[1:, :, :] += s[:-1, :, :]
+    nb[:-1, :, :] += s[1:, :, :]
+    proj = inner & s & (nb > 0)
+    return float(np.abs(div[proj]).max()) if proj.any() else 0.0
+
+
 def run_reference_arm(args, ws, rank):
+    """The reference's own step (host build, OpenMP over every host core) on the same workload,
+    timing exactly --steps steps after --warmup untimed ones, like the library's arm.  The
+    reference's projection has no convergence test: it runs --ref-sweeps fixed red-black
+    iterations (the sweeps a zero-pressure start needs for max|div| <= 1e-4 on this workload),
+    and the line reports the max|div u| its projected velocity reaches."""
     if rank != 0:
         return 0
-    steps = max(1, min(args.steps, args.ref_max_steps))
-    warm = min(args.warmup, 1)
+    steps = max(1, args.steps)
+    warm = max(0, args.warmup)
     from oracle import oracle as O
     sc = workload(args.side)
     sc.scheme, sc.iterations, sc.tol = 0, args.ref_sweeps, 0.0
@@ -213,9 +240,17 @@ def run_reference_arm(args, ws, rank):
         sim.step()
     dt = time.perf_counter() - t0
     rate = sc.cells * steps / dt
-    sample = ("%d timed step(s) (+%d warm-up) of the %d^3 workload, reference step with %d "
-              "fixed red-black iterations, OpenMP over %d threads" % (steps, warm, args.side,
-                                                                     args.ref_sweeps, cores))
+    if kind == "reference":
+        st = sim.state()
+        now = st["index_now"]
+        div = max_div_reference(st["u"][now], st["v"][now], st["w"][now], st["s"])
+        sim.close()
+    else:
+        now = sim.index_now
+        div = max_div_reference(sim.u[now], sim.v[now], sim.w[now], sim.s)
+    sample = ("%d timed step(s) after %d warm-up step(s) of the %d^3 workload, reference step with "
+              "%d fixed red-black iterations, OpenMP over %d threads" % (steps, warm, args.side,
+                                                                        args.ref_sweeps, cores))
     line = {
         "metric": METRIC, "value": rate, "unit": UNIT, "impl": "reference", "n_gpus": ws,
         "steps": steps, "warmup": warm, "ms_per_step": 1e3 * dt / steps,
@@ -223,7 +258,10 @@ def run_reference_arm(args, ws, rank):
         "data": "synthetic",
         "config": {"workload": "smoke step %d^3 FP32, 5%% random solids + 2 spheres r=24, 4 "
                                "emitters, dt=0.02, red-black SOR %d sweeps" % (args.side, args.ref_sweeps),
-                   "cells": sc.cells, "l2": "inputs larger than L2 (CPU run)"},
+                   "cells": sc.cells, "l2": "inputs larger than L2 (CPU run)",
+                   "ref_sweeps": args.ref_sweeps,
+                   "max_div_post_projection": div,
+                   "pressure_start": "zero every step (the reference's projection)"},
         "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": kind,
                          "sample": sample},
         "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -235,12 +273,11 @@ def run_reference_arm(args, ws, rank):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--side", type=int, default=N_DEFAULT, help="grid cells per side of the workload")
     ap.add_argument("--ref-sweeps", type=int, default=REF_SWEEPS_DEFAULT)
-    ap.add_argument("--ref-max-steps", type=int, default=3)
     ap.add_argument("--cpu-steps", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=0, help="0: same as --steps")
@@ -309,8 +346,11 @@ def main():
     # also restarts the pressure history, as a new simulation has none)
     launches = 0
     elapsed = 0.0
+    # clocks are sampled from here until the last timed region of the plain workload (the
+    # device-timed steps, the e2e steps and the zero-pressure-start steps) has ended
     clocks = ClockSampler(local)
     clocks.start()
+    t_clk0 = time.perf_counter()
     for n in segments(args.steps):
         sim.write_state(initial)
         launches0 = sim.launch_count()
@@ -319,7 +359,6 @@ def main():
         elapsed += _timed_steps(lambda: sim.step(sc.dt, sh), stream, n, torch)
         launches += sim.launch_count() - launches0
     dist_barrier(ws)
-    clk = clocks.stop()
 
     # per-step statistics and stage times: one more pass over the workload's steps with a sync
     # after each (outside the timed region) to read the solver status and the sweep phase timed
@@ -401,6 +440,9 @@ def main():
                 "steps": args.cold_steps,
                 "note": "pressure restarted from zero every step, as the reference's projection "
                         "does; same tolerance rule; the first steps of the workload"}
+    clk = clocks.stop()
+    clk["window_s"] = time.perf_counter() - t_clk0
+    clk["window"] = "device-timed, e2e and zero-pressure-start steps of the plain workload"
 
     # ---- CPU baseline (rank 0, N=1 only) -------------------------------------------------------
     cpu = None
@@ -444,6 +486,13 @@ def main():
                        "max_div_measured": "after every projection of the workload's steps, in a "
                                            "separate pass (the timed steps run without the diagnostic)",
                        "pressure_start": "warm (previous step's pressure)",
+                       # the same workload with the pressure restarted from zero every step (the
+                       # reference's projection): the like-for-like comparison with the
+                       # reference arm; value / cold_value is what warm starting contributes
+                       "cold_value": cold["value"] if cold else None,
+                       "cold_ms_per_step": cold["ms_per_step"] if cold else None,
+                       "cold_mean_sweeps": cold["mean_sweeps"] if cold else None,
+                       "warm_start_gain": (value / cold["value"]) if cold else None,
                        "cold_start_form": cold},
             "roofline": {"bound": "hbm", "kernel": "%s (z-chunk %d)" % (kname, zchunk),
                          "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -546,6 +595,19 @@ def run_forms(args, smk, torch):
              "mean_sweeps": float(np.mean([s.stats().sweeps for s in sims]))}
     for s in sims:
         s.close()
+    # plain_warm: the same grids one at a time, FP32, with the warm-started pressure the grouped
+    # form also uses: the ratio against it is what batching itself contributes
+    sims = [smk.from_scene(sc, warm_start=1) for sc in scs]
+    for s in sims:
+        s.autotune()
+    for _ in range(args.warmup):
+        for s, sc in zip(sims, scs):
+            s.step(sc.dt, sh)
+    secs = _timed_steps(lambda: [s.step(sc.dt, sh) for s, sc in zip(sims, scs)], stream, args.forms_steps, torch)
+    plain_warm = {"value": cells * args.forms_steps / secs, "ms_per_step": 1e3 * secs / args.forms_steps,
+                  "mean_sweeps": float(np.mean([s.stats().sweeps for s in sims]))}
+    for s in sims:
+        s.close()
     forms["batched"] = {"workload": "64 grids, cube side log-uniform 32..128 (seed 2), sphere solid + box "
                                     "emitter each, dt=0.05, warm-started pressure to max|div|<=1e-4; "
                                     "one persistent launch per stage over all grids (grouped form; the "
@@ -553,8 +615,11 @@ def run_forms(args, smk, torch):
                                     "grid's tiles, whichever the autotuner finds faster), CUDA-graph "
                                     "replay",
                         "cells": cells, "steps": args.forms_steps, "grouped": batched, "plain": plain,
+                        "plain_warm": plain_warm,
                         "grouped_bf16_vs_plain": batched["bf16"]["value"] / plain["value"],
-                        "grouped_f32_vs_plain": batched["f32"]["value"] / plain["value"]}
+                        "grouped_f32_vs_plain": batched["f32"]["value"] / plain["value"],
+                        "grouped_bf16_vs_plain_warm": batched["bf16"]["value"] / plain_warm["value"],
+                        "grouped_f32_vs_plain_warm": batched["f32"]["value"] / plain_warm["value"]}
 
     # ---- mixed precision at 512^3 -------------------------------------------------------------
     if args.mixed_n > 0:
@@ -632,6 +697,13 @@ def run_forms(args, smk, torch):
         plain1 = {"value": st1.cell_updates / wall1, "wall_s": wall1, "p50_step_ms": st1.p50_step_ms,
                   "p99_step_ms": st1.p99_step_ms}
         srv.close()
+        # the same, with the warm-started pressure the served form uses
+        srv = SV.Server(budget_bytes=120 * 10**9, max_active=1)
+        wall2, _ = SV.drive(srv, arr)
+        st2 = srv.stats()
+        plain_warm1 = {"value": st2.cell_updates / wall2, "wall_s": wall2, "p50_step_ms": st2.p50_step_ms,
+                       "p99_step_ms": st2.p99_step_ms}
+        srv.close()
         forms["serving"] = {"workload": "%d requests, Poisson 200/s (seed 4), cube side log-uniform 48..192, "
                                         "50..500 steps, sphere solid + box emitter, tol 1e-4; served with "
                                         "u,v,w in BF16 (density FP32), warm-started pressure, up to 64 "
@@ -640,7 +712,9 @@ def run_forms(args, smk, torch):
                                         "from zero each step; cell-updates/s over host wall time"
                                         % args.serve_requests,
                             "served": serve, "plain_one_at_a_time": plain1,
-                            "served_vs_plain": serve["value"] / plain1["value"]}
+                            "plain_warm_one_at_a_time": plain_warm1,
+                            "served_vs_plain": serve["value"] / plain1["value"],
+                            "served_vs_plain_warm": serve["value"] / plain_warm1["value"]}
     return forms
 
 

@@ -11,7 +11,10 @@ the library's stages on the same GPU, workload and initial state:
              tolerance rule); plus simulate() itself end to end (blocking density read-back).
   library:   the PRESSURE-scheme step with per-stage CUDA events (direct launches), warm-started
              pressure, the solve stopped by the tolerance rule; mean over the workload's 50
-             steps from its initial fields.
+             steps from its initial fields;
+  drop-in:   the library's REFERENCE-scheme step (what the reference's own simulate() symbol
+             runs, bit-exact with the reference) at the same iteration counts as the reference,
+             per stage, and smk_simulate end to end.
 
 Usage (on a machine with a GPU; the reference's generated source must be in oracle/_ref/):
     python -m oracle.time_reference_gpu [--side 256] [--steps 4] [--json OUT.json]
@@ -137,9 +140,47 @@ def time_library(sc, warmup: int) -> dict:
                     "warm-started pressure, solve stopped by the tolerance rule"}
 
 
+def time_library_dropin(sc, iterations: int, steps: int, warmup: int) -> dict:
+    """Stage times (ms) of the library's drop-in path: the REFERENCE projection scheme (the
+    reference's in-place velocity red-black SOR, bit-exact with it) at `iterations` fixed
+    iterations from the workload's initial fields, direct launches with per-stage events; plus
+    smk_simulate (the reference's simulate(): step and blocking density read-back) end to end."""
+    import copy
+    import torch
+    import smoke_simulation_gb300 as smk
+    sc = copy.copy(sc)
+    sc.scheme, sc.iterations, sc.tol, sc.warm_start = 0, iterations, 0.0, 0
+    sim = smk.from_scene(sc, report_div=0)
+    stream = torch.cuda.Stream()
+    sh = stream.cuda_stream
+    sim.set_timing(True)
+    rows = []
+    for k in range(warmup + steps):
+        sim.step(sc.dt, sh)
+        if k >= warmup:
+            rows.append([float(x) for x in sim.stage_times()[:5]])
+    sim.set_timing(False)
+    t = np.mean(np.array(rows), axis=0)
+    out = torch.empty(sc.cell_shape, dtype=torch.float32, pin_memory=True).numpy()
+    for _ in range(warmup):
+        sim.simulate(out, sc.dt)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        sim.simulate(out, sc.dt)
+    e2e = (time.perf_counter() - t0) / steps * 1e3
+    sim.close()
+    return {"objects": float(t[0]), "forcing": float(t[1]), "projection": float(t[2]),
+            "advection": float(t[3]), "device_step_ms": float(t[4]),
+            "per_iteration_ms": float(t[2] / iterations) if iterations else None,
+            "simulate_e2e_ms": e2e, "iterations": iterations}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--side", type=int, default=256)
+    ap.add_argument("--scene", default="large", choices=["large", "ref80"],
+                    help="large: the single-large-grid workload at --side; ref80: the 80^3 "
+                         "reference-step configuration (sphere obstacle, box emitter, noise)")
     ap.add_argument("--steps", type=int, default=4)
     ap.add_argument("--warmup", type=int, default=2)
     ap.add_argument("--iterations", default="30,167")
@@ -149,14 +190,16 @@ def main():
     torch.cuda.init()
     torch.zeros(1, device="cuda")
     from smoke_simulation_gb300 import scenes as S
-    sc = S.config_large(args.side)
+    sc = S.config_large(args.side) if args.scene == "large" else S.config_ref80(steps=50)
     L = load_reference_gpu()
     ref = {}
     for it in (int(x) for x in args.iterations.split(",")):
         ref[str(it)] = time_reference(L, sc, it, args.steps, args.warmup)
-    ours = time_library(sc, args.warmup)
+    ours = time_library(sc, args.warmup) if args.scene == "large" else None
+    dropin = {str(it): time_library_dropin(sc, it, args.steps, args.warmup)
+              for it in (int(x) for x in args.iterations.split(","))}
     res = {"workload": sc.name, "cells": sc.cells, "gpu": torch.cuda.get_device_name(0),
-           "reference_gpu": ref, "library": ours}
+           "reference_gpu": ref, "library": ours, "library_dropin": dropin}
     txt = json.dumps(res)
     print(txt)
     if args.json:

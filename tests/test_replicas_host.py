@@ -58,3 +58,7 @@ def test_reference_arm_runs_on_rank0_only_under_torchrun():
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
     assert d["e2e"]["value"] == d["value"] and d["cpu_baseline"]["value"] == d["value"]
+    # the timed steps are exactly --steps after --warmup, and the reference's own divergence
+    # after its fixed iterations is reported
+    assert d["steps"] == 1 and d["warmup"] == 0
+    assert d["config"]["max_div_post_projection"] >= 0.0
