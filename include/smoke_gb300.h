@@ -187,6 +187,15 @@ int smk_get_sweep_kernel(const smk_sim* sim, int* depth, int* zchunk);
 #define SMK_SWEEP_YCLUSTER_N(n) ((n) << 9)
 int smk_set_sweep_shape(smk_sim* sim, int depth, int rows, int zchunk);
 int smk_get_sweep_shape(const smk_sim* sim, int* depth, int* rows, int* zchunk);
+/* Projection kernel of the REFERENCE scheme (the reference's in-place velocity red-black SOR,
+ * smokeSimulation.cu:356-394 run max_sweeps times, :795-801).  depth 0 (default): one colour pass
+ * per launch, as the reference launches it; depth 2 or 4: temporally blocked, `depth` colour
+ * passes per pass over HBM on z-chunks of `zchunk` planes (0: chosen from the grid), with the
+ * simulation's pressure buffers as scratch (a later PRESSURE step then restarts its pressure from
+ * zero); smk_autotune picks the fastest.  Results are bit-identical for every choice.  FP32
+ * storage only.  No counterpart in the reference's API. */
+int smk_set_velocity_sweep(smk_sim* sim, int depth, int zchunk);
+int smk_get_velocity_sweep(const smk_sim* sim, int* depth, int* zchunk);
 /* Replay steady-state steps as a captured CUDA graph (default on).  A graph is re-captured
  * when dt, the parameters, the objects or the sweep kernel change; steps after a mask or
  * obstacle change run directly.  Results are identical either way. */
@@ -201,9 +210,11 @@ int smk_set_graph_loops(smk_sim* sim, int enable);
  * identical; batches follow each member's setting.  No counterpart in the reference. */
 int smk_set_vector_stages(smk_sim* sim, int enable);
 /* Time the blocked sweep kernel's shapes (depth, patch rows) and z-chunk sizes on this simulation's buffers and
- * keep the fastest (cached per grid shape and device for the process).  Synchronises; does not
- * change the simulation's results.  Outputs may be NULL; us_per_sweep is -1 on a cache hit.
- * No counterpart in the reference. */
+ * keep the fastest (cached per grid shape and device for the process).  With the REFERENCE
+ * projection it times the velocity sweep instead (one colour pass per launch, or the blocked
+ * kernel with depth 2 or 4 over its z-chunks; smk_set_velocity_sweep) and reports the time per
+ * iteration.  Synchronises; does not change the simulation's results.  Outputs may be NULL;
+ * us_per_sweep is -1 on a cache hit.  No counterpart in the reference. */
 int smk_autotune(smk_sim* sim, int* depth, int* zchunk, float* us_per_sweep);
 
 /* Batches: many independent grids of any sizes stepped together.  Members keep their own state
@@ -386,6 +397,10 @@ int smk_proxy_planes(const float view_origin[3], const float view_dir[3], const 
 /* Testing: the next `count` smk_create calls fail with SMK_ERR_OOM as a device allocation
  * failure would, without touching the device (host-side fault injection). */
 int smk_inject_alloc_failures(int count);
+/* Testing (host only, no device): the exact arithmetic of the blocked REFERENCE-scheme sweep on
+ * n values: scaled[i] = float(double(x[i]) * omega) and quotient[i] = x[i] / d[i] (d in 1..6) as
+ * the kernel computes them without the FP64 pipe (either output may be NULL). */
+int smk_test_exact_arith(const float* x, const int* d, int n, double omega, float* scaled, float* quotient);
 
 #ifdef __cplusplus
 }

@@ -30,6 +30,9 @@ CLAMP_REFERENCE, CLAMP_MAGNITUDE, CLAMP_NONE = 0, 1, 2
 STORAGE_F32, STORAGE_BF16, STORAGE_BF16_VEL = 0, 1, 2
 
 
+ERR_INVALID, ERR_CUDA, ERR_OOM, ERR_STATE, ERR_TIMEOUT = 1, 2, 3, 4, 5
+
+
 class SmokeError(RuntimeError):
     def __init__(self, code: int, msg: str):
         super().__init__("smoke_gb300 error %d: %s" % (code, msg))
@@ -111,6 +114,8 @@ def lib() -> C.CDLL:
         "smk_set_sweep_kernel": (i, [vp, i, i]),
         "smk_get_sweep_kernel": (i, [vp, C.POINTER(i), C.POINTER(i)]),
         "smk_set_sweep_shape": (i, [vp, i, i, i]),
+        "smk_set_velocity_sweep": (i, [vp, i, i]),
+        "smk_get_velocity_sweep": (i, [vp, C.POINTER(i), C.POINTER(i)]),
         "smk_get_sweep_shape": (i, [vp, C.POINTER(i), C.POINTER(i), C.POINTER(i)]),
         "smk_project_noalloc": (i, [vp, vp, vp, vp, i, i, i, C.POINTER(Params),
                                     C.POINTER(Stats), vp]),
@@ -339,6 +344,17 @@ class Simulation:
         planes, patches of `rows` cell rows per thread (2, or 4 with depth 4), or with depth 6
         2 | SWEEP_YCLUSTER [| SWEEP_YCLUSTER_N(2 or 4)]: thread-block clusters along y."""
         _check(lib().smk_set_sweep_shape(self.h, depth, rows, zchunk))
+
+    def set_velocity_sweep(self, depth: int, zchunk: int = 0):
+        """REFERENCE-scheme projection kernel: depth 0 = one colour pass per launch, 2 or 4 =
+        temporally blocked (depth passes per pass over HBM, z-chunks of zchunk planes, 0 = from
+        the grid); results are identical."""
+        _check(lib().smk_set_velocity_sweep(self.h, depth, zchunk))
+
+    def velocity_sweep(self):
+        d, z = C.c_int(), C.c_int()
+        _check(lib().smk_get_velocity_sweep(self.h, C.byref(d), C.byref(z)))
+        return d.value, z.value
 
     def autotune(self):
         """Pick the fastest sweep kernel shape for this grid; returns (depth, zchunk, us/sweep)."""

@@ -123,6 +123,31 @@ void launch_group_tb_loop_next(const void* grids, int n, int* counter, int step,
 void launch_group_loop_next(const StepStatus* status, int* counter, int step, int limit,
                             unsigned long long* launches, int launches_per_iter,
                             cudaGraphConditionalHandle handle, cudaStream_t st);
+// Reference scheme, temporally blocked (kernels_vsweep_tb.cu): T colour passes of the in-place
+// velocity red-black SOR per pass over HBM, bit-exact with launch_project_velocity.
+// OmegaSplit: omega's sign, 53-bit significand (hi 21 / lo 32 bits) and exponent, and the range
+// of biased float exponents for which float(double(q) * omega) is evaluated with integer
+// arithmetic (exact_scale.cuh).
+struct OmegaSplit {
+    uint32_t mo_hi, mo_lo;
+    int eo;
+    uint32_t sign;
+    int emin, emax;
+};
+OmegaSplit omega_split(double omega);
+struct VSweepMaps;
+int vsweep_depth_supported(int T);  // T = 2 or 4
+int prepare_vsweep_kernels();
+// Tensor maps of the state's face arrays (both ping-pong buffers), the scratch face arrays and
+// the flags; all buffers must exist.  NULL on failure.
+VSweepMaps* create_vsweep_maps(const Grid& g, float* const* u, float* const* v, float* const* w, const float* xu,
+                               const float* xv, const float* xw, const uint8_t* flags);
+void destroy_vsweep_maps(VSweepMaps* m);
+// One launch: nhalf <= T colour passes starting at colour0 on the state buffer `buf`
+// (from_state) or on the scratch arrays, written to (uo, vo, wo); z-chunks of zchunk planes.
+int launch_vsweep_tb(const VSweepMaps* m, const Grid& g, int buf, bool from_state, float* uo, float* vo, float* wo,
+                     int T, int nhalf, int colour0, int zchunk, double omega, const OmegaSplit& os, int* kerr,
+                     cudaStream_t st);
 void launch_div_max(const Grid& g, const float* u, const float* v, const float* w,
                     const uint8_t* flags, StepStatus* status, cudaStream_t st);
 // FP64-checked refinement rounds after the projection (u, v, w: the FP32 projected velocity;

@@ -57,15 +57,14 @@
 
 #include "common.cuh"
 #include "kernels.h"
+#include "tb_common.cuh"
 
 namespace smk {
 
 namespace {
 
-constexpr int TB_TX = 32;      // threads per tile row (one warp) = 64 cells
-constexpr int BOX_F = 68;      // float box width: 64 cells + up to 2 alignment cells, 16-B multiple
-constexpr int BOX_U8 = 80;     // flag box width in bytes: 64 + up to 15 alignment bytes
-constexpr unsigned WAIT_LIMIT = 1u << 20;
+using namespace tb;
+constexpr int TB_TX = tb::TX;  // threads per tile row (one warp) = 64 cells
 
 // Tile geometry for a patch of PY rows per thread: TY tile rows of threads (warps) give
 // ROWS = PY * TY cell rows.  PY = 2: 16 warps, 32 rows; PY = 4: 8 warps, 32 rows (the ring of a
@@ -91,47 +90,6 @@ struct TBMaps {
     CUtensorMap b;
     CUtensorMap f;
 };
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) {
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
-                 : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-// Bounded wait on an mbarrier phase.
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
-    for (unsigned i = 0; i < WAIT_LIMIT; ++i)
-        if (mbar_try_wait(bar, parity)) return true;
-    return false;
-}
-
-__device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map, int x, int y, int z,
-                                            uint32_t bar) {
-    asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-        " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(dst),
-        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(bar)
-        : "memory");
-}
 
 // Issue the three boxes of plane z into stage `st` (thread 0 only).
 template <int PY>
@@ -187,40 +145,6 @@ __device__ __forceinline__ uint32_t cluster_map(uint32_t local, uint32_t rank) {
 
 __device__ __forceinline__ void st_cluster(uint32_t addr, float v) {
     asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(addr), "f"(v) : "memory");
-}
-
-// Windows along an axis of n cells, W cells wide with a T-cell halo.  A side of a window that
-// reaches the grid's first or last cell needs no halo: those cells (the boundary ring) and every
-// cell outside the grid are never projectable, so they never change, and a wrong value beyond
-// the window (a zero padding row, a shuffle that wrapped) only ever enters their own update,
-// which keeps their value.  So in the edge placement the first window starts at cell 0 and owns
-// W - T cells, the middle ones start T cells before the cells they own and own W - 2T, and the
-// last owns the rest (at most W - T, its window reaching the last cell); one window owns
-// everything when n <= W.  The plain placement gives every window a halo on both sides (window k
-// starts at k(W - 2T) - T).  The edge placement is used only where it needs fewer windows (small
-// grids): at equal counts the plain one measured faster (256^3: 136.7 against 139.7 us a launch).
-__host__ __device__ inline int edge_windows(int n, int W, int T) {
-    if (n <= W) return 1;
-    const int rest = n - 2 * (W - T);
-    return 2 + (rest > 0 ? (rest + W - 2 * T - 1) / (W - 2 * T) : 0);
-}
-__host__ __device__ inline int plain_windows(int n, int W, int T) { return (n + W - 2 * T - 1) / (W - 2 * T); }
-__host__ __device__ inline int sweep_windows(int n, int W, int T) {
-    const int e = edge_windows(n, W, T), p = plain_windows(n, W, T);
-    return e < p ? e : p;
-}
-// Window k of sweep_windows(n, W, T): its first cell (even for even T) and the cells [lo, hi) it owns.
-__host__ __device__ inline void sweep_window(int n, int W, int T, int k, int& start, int& lo, int& hi) {
-    const int nw = sweep_windows(n, W, T);
-    if (edge_windows(n, W, T) < plain_windows(n, W, T)) {
-        lo = k == 0 ? 0 : (W - T) + (k - 1) * (W - 2 * T);
-        hi = k + 1 < nw ? (W - T) + k * (W - 2 * T) : n;
-        start = k == 0 ? 0 : lo - T;
-    } else {
-        lo = k * (W - 2 * T);
-        hi = k + 1 < nw ? lo + (W - 2 * T) : n;
-        start = lo - T;
-    }
 }
 
 // One tile (bx, by, bz) of a blocked launch: the CTA's whole job.  `group` is absolute.
@@ -694,21 +618,6 @@ EncodeTiledFn encode_fn() {
     return fn;
 }
 
-bool encode_3d(CUtensorMap* m, const void* base, bool is_u8, const Grid& g, int rows) {
-    EncodeTiledFn fn = encode_fn();
-    if (!fn || base == nullptr || (reinterpret_cast<uintptr_t>(base) & 15u) != 0) return false;
-    const size_t es = is_u8 ? 1 : 4;
-    cuuint64_t dims[3] = {(cuuint64_t)g.X, (cuuint64_t)(g.ny + 1), (cuuint64_t)(g.nz + 1)};
-    cuuint64_t strides[2] = {(cuuint64_t)g.X * es, (cuuint64_t)g.XY * es};
-    cuuint32_t box[3] = {(cuuint32_t)(is_u8 ? BOX_U8 : BOX_F), (cuuint32_t)rows, 1u};
-    cuuint32_t estr[3] = {1u, 1u, 1u};
-    CUresult r = fn(m, is_u8 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
-                    const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                    CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    return r == CUDA_SUCCESS;
-}
-
 template <int T, int PY>
 constexpr size_t tb_smem_bytes() {
     using G = TBGeom<PY>;
@@ -818,6 +727,23 @@ __global__ void k_group_loop_next(const StepStatus* status, int* counter, int st
 }
 
 }  // namespace
+
+namespace tb {
+bool encode_3d(CUtensorMap* m, const void* base, bool is_u8, const Grid& g, int rows) {
+    EncodeTiledFn fn = encode_fn();
+    if (!fn || base == nullptr || (reinterpret_cast<uintptr_t>(base) & 15u) != 0) return false;
+    const size_t es = is_u8 ? 1 : 4;
+    cuuint64_t dims[3] = {(cuuint64_t)g.X, (cuuint64_t)(g.ny + 1), (cuuint64_t)(g.nz + 1)};
+    cuuint64_t strides[2] = {(cuuint64_t)g.X * es, (cuuint64_t)g.XY * es};
+    cuuint32_t box[3] = {(cuuint32_t)(is_u8 ? BOX_U8 : BOX_F), (cuuint32_t)rows, 1u};
+    cuuint32_t estr[3] = {1u, 1u, 1u};
+    CUresult r = fn(m, is_u8 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
+                    const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                    CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                    CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS;
+}
+}  // namespace tb
 
 int sweep_tb_shape_supported(int T, int rows) {
     if (rows & SWEEP_YCLUSTER) {

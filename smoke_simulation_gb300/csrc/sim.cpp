@@ -59,6 +59,19 @@ int check_params(const smk_params* p) {
     return SMK_OK;
 }
 
+// z-chunk of the blocked velocity sweep when none was chosen: about four CTAs' worth of planes
+// per SM-wave of x-y tiles, at least 2T + 8 planes so the chunk's halo stays a minor part.
+int default_vsweep_zchunk(const Grid& g, int T) {
+    const int rows = T == 2 ? 24 : 32;
+    const int tiles = ((g.nx + 1 + 63 - 2 * T) / (64 - 2 * T)) * ((g.ny + 1 + rows - 1 - 2 * T) / (rows - 2 * T));
+    const int planes = g.nz + 1;
+    int chunks = (4 * 152 + tiles - 1) / (tiles > 0 ? tiles : 1);
+    if (chunks < 1) chunks = 1;
+    int zc = (planes + chunks - 1) / chunks;
+    if (zc < 2 * T + 8) zc = 2 * T + 8;
+    return zc;
+}
+
 cudaMemcpy3DParms copy3d(void* dst, size_t dpitch, size_t dy, const void* src, size_t spitch,
                          size_t sy, size_t width_bytes, size_t h, size_t d, cudaMemcpyKind kind) {
     cudaMemcpy3DParms m;
@@ -123,6 +136,10 @@ int smk_sim::alloc() {
     // the tensor maps capture the buffer addresses: every buffer must exist first
     maps = create_sweep_maps(g, P, P2, b, flags);
     if (!maps) return fail(SMK_ERR_CUDA, "could not encode the TMA tensor maps of the sweep kernel");
+    if (!bf16) {
+        vmaps = create_vsweep_maps(g, u, v, w, P, P2, b, flags);
+        if (!vmaps) return fail(SMK_ERR_CUDA, "could not encode the TMA tensor maps of the velocity sweep kernel");
+    }
     status_groups = 4096;
     SMK_CUDA(cudaMalloc((void**)&status, sizeof(StepStatus) + sizeof(unsigned) * status_groups));
     SMK_CUDA(cudaMemset(status, 0, sizeof(StepStatus) + sizeof(unsigned) * status_groups));
@@ -130,7 +147,8 @@ int smk_sim::alloc() {
     for (auto& e : ev) SMK_CUDA(cudaEventCreate(&e));
     SMK_CUDA(cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking));
     SMK_CUDA(cudaStreamCreateWithFlags(&body_stream, cudaStreamNonBlocking));
-    if (prepare_sweep_kernels() != 0) return fail(SMK_ERR_CUDA, "sweep kernel configuration failed");
+    if (prepare_sweep_kernels() != 0 || prepare_vsweep_kernels() != 0)
+        return fail(SMK_ERR_CUDA, "sweep kernel configuration failed");
     // initializeVolume's mask: fluid except the y = 0 floor (smokeSimulation.cu:200-207)
     std::vector<uint8_t> host((size_t)g.nx * g.ny * g.nz, 1);
     for (int z = 0; z < g.nz; ++z)
@@ -147,6 +165,7 @@ void smk_sim::release() {
     if (refine) cudaFree(refine);
     if (render_scratch) cudaFree(render_scratch);
     if (maps) destroy_sweep_maps(maps);
+    if (vmaps) destroy_vsweep_maps(vmaps);
     if (s) cudaFree(s);
     if (flags) cudaFree(flags);
     if (status) cudaFree(status);
@@ -238,10 +257,44 @@ int smk_sim::enqueue(float dt, cudaStream_t st) {
     SMK_CUDA(cudaMemsetAsync(status, 0, status_bytes, st));
     last_groups = 0;
     if (p.projection == SMK_PROJECT_REFERENCE) {
-        for (int it = 0; it < p.max_sweeps; ++it) {
-            launch_project_velocity(g, u[now], v[now], w[now], flags, 0, p.omega, st);
-            launch_project_velocity(g, u[now], v[now], w[now], flags, 1, p.omega, st);
-            launches += 2;
+        if (vsweep_depth > 0 && vmaps != nullptr && p.max_sweeps > 0) {
+            // temporally blocked: launches of up to T colour passes alternating between the state
+            // (u, v, w)[now] and the scratch arrays (P, P2, b), an even number of them so that the
+            // result ends in the state; the passes are those of the loop below, in the same order
+            const int T = vsweep_depth;
+            const int H = 2 * p.max_sweeps;
+            std::vector<int> plan;
+            for (int h = 0; h < H; h += T) plan.push_back(H - h < T ? H - h : T);
+            if (plan.size() % 2 == 1) {  // split one launch in two (both keep >= 1 pass)
+                if (plan.back() >= 2) {
+                    plan.back() -= 1;
+                    plan.push_back(1);
+                } else {
+                    plan[plan.size() - 2] -= 1;
+                    plan.push_back(1);
+                }
+            }
+            const OmegaSplit os = omega_split(p.omega);
+            const int zc = vsweep_zchunk > 0 ? vsweep_zchunk : default_vsweep_zchunk(g, T);
+            int h = 0;
+            for (size_t l = 0; l < plan.size(); ++l) {
+                const bool from_state = (l % 2) == 0;
+                float* uo = from_state ? P : u[now];
+                float* vo = from_state ? P2 : v[now];
+                float* wo = from_state ? b : w[now];
+                if (launch_vsweep_tb(vmaps, g, now, from_state, uo, vo, wo, T, plan[l], h & 1, zc, p.omega, os, kerr,
+                                     st) != 0)
+                    return fail(SMK_ERR_CUDA, "velocity sweep kernel launch failed");
+                h += plan[l];
+                ++launches;
+            }
+            pressure_clobbered = true;
+        } else {
+            for (int it = 0; it < p.max_sweeps; ++it) {
+                launch_project_velocity(g, u[now], v[now], w[now], flags, 0, p.omega, st);
+                launch_project_velocity(g, u[now], v[now], w[now], flags, 1, p.omega, st);
+                launches += 2;
+            }
         }
     } else {
         float wacc[7];
@@ -454,6 +507,8 @@ std::string smk_sim::graph_signature(float dt) const {
     put(&sweep_depth, sizeof(sweep_depth));
     put(&sweep_zchunk, sizeof(sweep_zchunk));
     put(&sweep_rows, sizeof(sweep_rows));
+    put(&vsweep_depth, sizeof(vsweep_depth));
+    put(&vsweep_zchunk, sizeof(vsweep_zchunk));
     const char t = timing ? 1 : 0;
     put(&t, 1);
     for (const Object& o : objects) put(&o, sizeof(o));
@@ -466,6 +521,14 @@ std::string smk_sim::graph_signature(float dt) const {
 // obstacles changed runs directly (it includes the one-off mask kernels), and so does a step
 // with stage timing on (events recorded inside a capture cannot be queried afterwards).
 int smk_sim::step(float dt, cudaStream_t st) {
+    if (pressure_clobbered && p.projection == SMK_PROJECT_PRESSURE) {
+        // the blocked velocity sweep of earlier REFERENCE steps left its scratch in P, P2, b: the
+        // pressure history starts over, as after smk_write_state
+        SMK_CUDA(cudaMemsetAsync(P, 0, elems() * sizeof(float), st));
+        SMK_CUDA(cudaMemsetAsync(P2, 0, elems() * sizeof(float), st));
+        SMK_CUDA(cudaMemsetAsync(pcur, 0, sizeof(int), st));
+        pressure_clobbered = false;
+    }
     if (!use_graphs || mask_dirty || obstacles_dirty) return enqueue(dt, st);
     GraphSlot& gs = graphs[index_now];
     std::string sig = graph_signature(dt);
@@ -931,6 +994,26 @@ int smk_set_sweep_shape(smk_sim* sim, int depth, int rows, int zchunk) {
     return SMK_OK;
 }
 
+int smk_set_velocity_sweep(smk_sim* sim, int depth, int zchunk) {
+    if (!sim) return fail(SMK_ERR_INVALID, "sim is null");
+    if (depth != 0 && !vsweep_depth_supported(depth))
+        return fail(SMK_ERR_INVALID, "velocity sweep depth must be 0 (one colour pass per launch), 2 or 4");
+    if (zchunk < 0) return fail(SMK_ERR_INVALID, "zchunk must be >= 0 (0: chosen from the grid)");
+    if (depth != 0 && sim->vmaps == nullptr)
+        return fail(SMK_ERR_INVALID, "the blocked velocity sweep needs FP32 storage");
+    sim->vsweep_depth = depth;
+    sim->vsweep_zchunk = zchunk;
+    return SMK_OK;
+}
+
+int smk_get_velocity_sweep(const smk_sim* sim, int* depth, int* zchunk) {
+    if (!sim) return fail(SMK_ERR_INVALID, "sim is null");
+    const int d = sim->vmaps ? sim->vsweep_depth : 0;
+    if (depth) *depth = d;
+    if (zchunk) *zchunk = d == 0 ? 0 : (sim->vsweep_zchunk > 0 ? sim->vsweep_zchunk : default_vsweep_zchunk(sim->g, d));
+    return SMK_OK;
+}
+
 int smk_set_sweep_kernel(smk_sim* sim, int depth, int zchunk) {
     return smk_set_sweep_shape(sim, depth, 2, zchunk);
 }
@@ -996,9 +1079,110 @@ std::map<std::tuple<int, int, int, int, int>, TunedShape> g_tune_cache;
 
 extern "C" {
 
+// REFERENCE scheme: time the velocity sweep's forms -- one colour pass per launch, and the
+// temporally blocked kernel with depth 2 and 4 over z-chunks without unroll padding -- per
+// iteration (red + black pass) and keep the fastest.  The blocked launches read the state and
+// write the scratch arrays (P, P2, b); the one-pass kernel runs in place on the scratch arrays,
+// so the state is untouched.  Cached per grid shape and device.
+static int autotune_velocity_sweep(smk_sim* sim, int* depth_out, int* zchunk_out, float* us_out) {
+    const Grid& g = sim->g;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const auto key = std::make_tuple(dev, g.nx, g.ny, g.nz, -100000);
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mutex);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) {
+            sim->vsweep_depth = sim->vmaps ? it->second.depth : 0;
+            sim->vsweep_zchunk = it->second.zchunk;
+            if (depth_out) *depth_out = sim->vsweep_depth;
+            if (zchunk_out) *zchunk_out = sim->vsweep_zchunk;
+            if (us_out) *us_out = -1.0f;
+            return SMK_OK;
+        }
+    }
+    SMK_CUDA(cudaDeviceSynchronize());
+    cudaStream_t st = nullptr;
+    SMK_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    cudaEvent_t e0, e1;
+    SMK_CUDA(cudaEventCreate(&e0));
+    SMK_CUDA(cudaEventCreate(&e1));
+    const int now = sim->index_now;
+    const OmegaSplit os = omega_split(sim->p.omega);
+    // microseconds per iteration of one candidate, issued as a step issues it
+    auto time_it = [&](int depth, int zc, float* us) -> int {
+        const int iters = 4;
+        auto run = [&]() -> int {
+            if (depth == 0) {
+                for (int it = 0; it < iters; ++it) {
+                    launch_project_velocity(g, sim->P, sim->P2, sim->b, sim->flags, 0, sim->p.omega, st);
+                    launch_project_velocity(g, sim->P, sim->P2, sim->b, sim->flags, 1, sim->p.omega, st);
+                }
+                return SMK_OK;
+            }
+            for (int h = 0; h < 2 * iters; h += depth)
+                if (launch_vsweep_tb(sim->vmaps, g, now, true, sim->P, sim->P2, sim->b, depth, depth, h & 1, zc,
+                                     sim->p.omega, os, sim->kerr, st) != 0)
+                    return fail(SMK_ERR_CUDA, "velocity sweep kernel launch failed");
+            return SMK_OK;
+        };
+        int rc = run();  // warm
+        if (rc) return rc;
+        SMK_CUDA(cudaEventRecord(e0, st));
+        for (int r = 0; r < 2 && rc == SMK_OK; ++r) rc = run();
+        if (rc) return rc;
+        SMK_CUDA(cudaEventRecord(e1, st));
+        SMK_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.0f;
+        SMK_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        *us = 1e3f * ms / (2 * iters);
+        return SMK_OK;
+    };
+    int best_d = 0, best_z = 0;
+    float best = 1e30f;
+    int rc = time_it(0, 0, &best);
+    const int depths[2] = {2, 4};
+    for (int di = 0; di < 2 && rc == SMK_OK && sim->vmaps != nullptr; ++di) {
+        const int T = depths[di], R = T + 2;
+        for (int m = 2; m <= 40 && rc == SMK_OK; ++m) {
+            const int zc = R * m - 2 * T - 1;
+            if (zc < 4) continue;
+            if (zc > g.nz + 1 + R) break;
+            float us = 0.0f;
+            rc = time_it(T, zc, &us);
+            if (rc == SMK_OK && us < best) {
+                best = us;
+                best_d = T;
+                best_z = zc;
+            }
+            if (zc > g.nz + 1) break;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaStreamDestroy(st);
+    if (rc) return rc;
+    SMK_CUDA(cudaGetLastError());
+    sim->pressure_clobbered = true;
+    int krc = check_kernel_error(sim);
+    if (krc) return krc;
+    sim->vsweep_depth = best_d;
+    sim->vsweep_zchunk = best_z;
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mutex);
+        g_tune_cache[key] = TunedShape{best_d, 2, best_z};
+    }
+    if (depth_out) *depth_out = best_d;
+    if (zchunk_out) *zchunk_out = best_z;
+    if (us_out) *us_out = best;
+    return SMK_OK;
+}
+
 int smk_autotune(smk_sim* sim, int* depth_out, int* zchunk_out, float* us_per_sweep_out) {
     if (!sim) return fail(SMK_ERR_INVALID, "sim is null");
     DeviceGuard dg(sim->device);
+    if (sim->p.projection == SMK_PROJECT_REFERENCE)
+        return autotune_velocity_sweep(sim, depth_out, zchunk_out, us_per_sweep_out);
     const Grid& g = sim->g;
     int dev = 0;
     cudaGetDevice(&dev);

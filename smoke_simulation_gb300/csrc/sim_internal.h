@@ -9,7 +9,7 @@
 #include "../../include/smoke_gb300.h"
 #include "common.cuh"
 
-namespace smk { struct SweepMaps; }
+namespace smk { struct SweepMaps; struct VSweepMaps; }
 
 // Records `msg` as smk_last_error's text and returns `code` (sim.cpp).
 int smk_fail(int code, const std::string& msg);
@@ -72,6 +72,7 @@ struct smk_sim {
     void* render_scratch = nullptr;               // device: the renderer's light buffer per plane
     size_t render_scratch_bytes = 0;
     smk::SweepMaps* maps = nullptr;  // TMA tensor maps of P, P2, b, flags
+    smk::VSweepMaps* vmaps = nullptr;  // TMA tensor maps of u, v, w (both buffers), P, P2, b, flags
     uint8_t* s = nullptr;
     uint8_t* flags = nullptr;
     smk::StepStatus* status = nullptr;
@@ -88,6 +89,14 @@ struct smk_sim {
     int sweep_depth = 4;
     int sweep_zchunk = 47;
     int sweep_rows = 2;  // cell rows of a thread's patch in the blocked kernel (2 or 4)
+    // reference scheme: 0 = one colour pass per launch (k_project_velocity); T = 2 or 4 = the
+    // temporally blocked velocity sweep, T passes per launch over z-chunks of vsweep_zchunk planes
+    // (the pressure buffers P, P2, b hold the intermediate face arrays); smk_autotune chooses
+    int vsweep_depth = 0;
+    int vsweep_zchunk = 0;  // 0: chosen from the grid
+    // the blocked velocity sweep used P, P2, b as scratch: a PRESSURE step must restart its
+    // pressure from zero (cleared in step(), outside any captured graph)
+    bool pressure_clobbered = false;
 
     bool timing = false;
     cudaEvent_t ev[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};

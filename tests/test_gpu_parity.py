@@ -434,3 +434,78 @@ def test_edge_windows_equal_oracle(gpu, kernel):
         assert st.sweeps == ost.sweeps and st.resid_max == ost.resid_max and st.div_max == ost.div_max, k
         assert H.first_mismatch(sim.read_state(), H.oracle_state(o)) == "", k
     sim.close()
+
+
+@pytest.mark.parametrize("dims,seed,kw", [
+    ((20, 16, 18), 11, {}),
+    ((110, 70, 40), 12, {"obstacles": 2, "sources": 2}),   # two x windows, several y windows
+    ((33, 17, 29), 13, {"noise": 4.0}),                     # clamp-triggering velocities
+    ((3, 40, 4), 14, {}),
+    ((64, 64, 64), 15, {"obstacles": 3}),
+])
+@pytest.mark.parametrize("kernel", [(0, 0), (2, 0), (4, 0), (4, 5), (2, 9), (4, 137)])
+def test_velocity_sweep_kernels_equal_oracle(gpu, dims, seed, kw, kernel):
+    """The reference scheme's projection with one colour pass per launch (depth 0) or
+    temporally blocked (depth 2 or 4 passes per pass over HBM, several z-chunks, windows along x
+    and y, partial launches from odd pass counts) gives the oracle's bits on every field of both
+    ping-pong buffers after every step."""
+    # 7 iterations: 14 passes (depth 4: launches of 4, 4, 4, 2); 6: 12 passes, an odd launch
+    # count that the plan splits (4, 4, 3, 1) so the result ends in the state's buffer
+    sc = S.small_scene(*dims, steps=3, seed=seed, iterations=7 if seed % 2 else 6, **kw)
+    o = O.OracleSim(sc)
+    sim = smk.from_scene(sc)
+    sim.set_velocity_sweep(*kernel)
+    for k in range(sc.steps):
+        o.step()
+        sim.step(sc.dt)
+        msg = H.first_mismatch(sim.read_state(), H.oracle_state(o))
+        assert msg == "", "step %d: %s" % (k, msg)
+    sim.close()
+
+
+def test_velocity_sweep_golden_ref80_and_scheme_switch(gpu):
+    """The 80^3 workload with the blocked velocity sweep reproduces the reference's golden
+    density hashes; switching a simulation that used it to the warm-started PRESSURE scheme
+    afterwards starts its pressure from zero (the sweep's scratch is not taken for a pressure
+    history), as the oracle does."""
+    g = H.golden()["scenes"]["ref80"]
+    sc = S.config_ref80(steps=100)
+    sim = smk.from_scene(sc)
+    sim.set_velocity_sweep(4, 0)
+    out = np.zeros(sc.cell_shape, np.float32)
+    for k in range(40):
+        sim.simulate(out, sc.dt)
+        if (k + 1) % 20 == 0:
+            assert H.sha(out) == g["density_every_20"][str(k + 1)], k + 1
+    sc2 = S.small_scene(30, 24, 26, steps=4, seed=77, iterations=9)
+    o = O.OracleSim(sc2)
+    a = smk.from_scene(sc2)
+    a.set_velocity_sweep(2, 0)
+    for _ in range(2):
+        a.step(sc2.dt)
+        o.step()
+    a.set_params(projection=smk.PROJECT_PRESSURE, warm_start=1, tol=1e-3, check_every=3, max_sweeps=30)
+    o.scheme = 1
+    sc2.tol, sc2.check_every, sc2.iterations, sc2.warm_start = 1e-3, 3, 30, 1
+    for k in range(2):
+        a.step(sc2.dt)
+        o.step()
+        assert H.first_mismatch(a.read_state(), H.oracle_state(o)) == "", k
+    sim.close()
+    a.close()
+
+
+def test_velocity_sweep_autotune_keeps_results(gpu):
+    """The REFERENCE-scheme autotuner (one-pass or blocked velocity sweep, z-chunks) does not
+    change results: after tuning, the steps still give the oracle's bits."""
+    sc = S.small_scene(70, 44, 52, steps=3, seed=19, iterations=11, obstacles=2)
+    o = O.OracleSim(sc)
+    sim = smk.from_scene(sc)
+    depth, zchunk, us = sim.autotune()
+    assert depth in (0, 2, 4) and us > 0
+    assert sim.velocity_sweep()[0] == depth
+    for k in range(sc.steps):
+        o.step()
+        sim.step(sc.dt)
+        assert H.first_mismatch(sim.read_state(), H.oracle_state(o)) == "", k
+    sim.close()
