@@ -285,7 +285,10 @@ def main():
                     help="timed steps of the zero-pressure-start form (0: skip)")
     ap.add_argument("--forms-steps", type=int, default=10, help="timed steps of the batched/mixed forms")
     ap.add_argument("--mixed-n", type=int, default=512, help="mixed-precision grid side (0: skip)")
-    ap.add_argument("--serve-requests", type=int, default=16, help="serving stream length (0: skip)")
+    ap.add_argument("--serve-requests", type=int, default=200, help="serving stream length (0: skip)")
+    ap.add_argument("--serve-tight-requests", type=int, default=60,
+                    help="requests of the serving run under a binding memory budget (0: skip)")
+    ap.add_argument("--serve-tight-gb", type=float, default=1.5, help="that run's device-memory budget (GB)")
     ap.add_argument("--render-frames", type=int, default=20, help="timed frames of the render form (0: skip)")
     ap.add_argument("--no-forms", action="store_true", help="skip the batched/mixed/serving forms")
     ap.add_argument("--sweep-kernel", default="", help="D,Z[,R]: blocked sweep depth, z-chunk and patch "
@@ -684,35 +687,39 @@ def run_forms(args, smk, torch):
     # ---- serving: Poisson stream, continuous admission ----------------------------------------
     if args.serve_requests > 0:
         arr = SV.poisson_stream(args.serve_requests)
-        srv = SV.Server(budget_bytes=120 * 10**9, max_active=64)
-        wall, _ = SV.drive(srv, arr, storage=smk.STORAGE_BF16_VEL)
-        st = srv.stats()
-        serve = {"value": st.cell_updates / wall, "wall_s": wall, "p50_step_ms": st.p50_step_ms,
-                 "p99_step_ms": st.p99_step_ms, "max_step_ms": st.max_step_ms,
-                 "requests": st.requests_completed, "steps": st.steps_completed}
-        srv.close()
-        srv = SV.Server(budget_bytes=120 * 10**9, max_active=1)
-        wall1, _ = SV.drive(srv, arr, warm_start=0)
-        st1 = srv.stats()
-        plain1 = {"value": st1.cell_updates / wall1, "wall_s": wall1, "p50_step_ms": st1.p50_step_ms,
-                  "p99_step_ms": st1.p99_step_ms}
-        srv.close()
-        # the same, with the warm-started pressure the served form uses
-        srv = SV.Server(budget_bytes=120 * 10**9, max_active=1)
-        wall2, _ = SV.drive(srv, arr)
-        st2 = srv.stats()
-        plain_warm1 = {"value": st2.cell_updates / wall2, "wall_s": wall2, "p50_step_ms": st2.p50_step_ms,
-                       "p99_step_ms": st2.p99_step_ms}
-        srv.close()
+
+        def serve_run(arrivals, budget, slots, **kw):
+            srv = SV.Server(budget_bytes=budget, max_active=slots)
+            wall, _ = SV.drive(srv, arrivals, **kw)
+            st = srv.stats()
+            srv.close()
+            return {"value": st.cell_updates / wall, "wall_s": wall, "requests": st.requests_completed,
+                    "steps": st.steps_completed, "p50_step_ms": st.p50_step_ms, "p99_step_ms": st.p99_step_ms,
+                    "max_step_ms": st.max_step_ms, "p50_queue_ms": st.p50_queue_ms,
+                    "p99_queue_ms": st.p99_queue_ms, "max_queue_ms": st.max_queue_ms,
+                    "peak_active": st.peak_active, "peak_queued": st.peak_queued,
+                    "peak_gb": st.peak_bytes / 1e9, "budget_gb": budget / 1e9}
+
+        serve = serve_run(arr, 120 * 10**9, 64, storage=smk.STORAGE_BF16_VEL)
+        # the same kind of stream under a budget that binds: admission waits on device memory
+        tight = serve_run(arr[:args.serve_tight_requests], int(args.serve_tight_gb * 1e9), 64,
+                          storage=smk.STORAGE_BF16_VEL) if args.serve_tight_requests > 0 else None
+        # one request at a time in plain FP32, on every 12th request of the stream (a sample that
+        # spans its sizes and step counts): pressure from zero each step, and warm-started
+        sample = arr[::12]
+        plain1 = serve_run(sample, 120 * 10**9, 1, warm_start=0)
+        plain_warm1 = serve_run(sample, 120 * 10**9, 1)
         forms["serving"] = {"workload": "%d requests, Poisson 200/s (seed 4), cube side log-uniform 48..192, "
                                         "50..500 steps, sphere solid + box emitter, tol 1e-4; served with "
                                         "u,v,w in BF16 (density FP32), warm-started pressure, up to 64 "
                                         "resident (120 GB budget), each request's step on its own stream; "
-                                        "plain = the same stream one request at a time, FP32, pressure "
-                                        "from zero each step; cell-updates/s over host wall time"
-                                        % args.serve_requests,
-                            "served": serve, "plain_one_at_a_time": plain1,
-                            "plain_warm_one_at_a_time": plain_warm1,
+                                        "tight = the first %d requests under a %.1f GB budget; plain = every "
+                                        "12th request of the stream one at a time, FP32, pressure from zero "
+                                        "each step (plain_warm: warm-started); cell-updates/s over host wall "
+                                        "time; queue = submission to admission"
+                                        % (args.serve_requests, args.serve_tight_requests, args.serve_tight_gb),
+                            "served": serve, "served_tight_budget": tight,
+                            "plain_one_at_a_time": plain1, "plain_warm_one_at_a_time": plain_warm1,
                             "served_vs_plain": serve["value"] / plain1["value"],
                             "served_vs_plain_warm": serve["value"] / plain_warm1["value"]}
     return forms

@@ -301,6 +301,10 @@ typedef struct smk_server_stats {
     double cell_updates;
     size_t bytes_in_use;
     float p50_step_ms, p99_step_ms, max_step_ms;
+    /* queueing delay of the admitted requests: host time from smk_server_submit to admission */
+    float p50_queue_ms, p99_queue_ms, max_queue_ms;
+    int peak_active, peak_queued;  /* most requests resident / waiting at once */
+    size_t peak_bytes;             /* most budgeted device memory in use at once */
 } smk_server_stats;
 int smk_server_create(size_t budget_bytes, int max_active, smk_server** out);
 /* Serving form, before the first request runs: STREAMS (default) steps every request with its
@@ -397,6 +401,15 @@ int smk_proxy_planes(const float view_origin[3], const float view_dir[3], const 
 /* Testing: the next `count` smk_create calls fail with SMK_ERR_OOM as a device allocation
  * failure would, without touching the device (host-side fault injection). */
 int smk_inject_alloc_failures(int count);
+/* Testing: the next cooperative grouped-projection launch made outside a graph capture (batch
+ * GROUPED form with graphs off) has its CTA 0 skip its arrival at grid barrier `barrier`
+ * (1-based; 0 cancels a pending injection), and its barrier waits give up after wait_ms
+ * (1..10000) instead of 2 s: every wait on that barrier runs out, every CTA leaves the kernel, and
+ * the members' next synchronisation reports SMK_ERR_TIMEOUT.  No device fault is involved; the
+ * context stays usable.  smk_barrier_timeout_report synchronises the device and gives, for that
+ * launch, how many CTAs left because a barrier gave up and how many it had. */
+int smk_inject_barrier_timeout(int barrier, int wait_ms);
+int smk_barrier_timeout_report(int* ctas_left, int* ctas);
 /* Testing (host only, no device): the exact arithmetic of the blocked REFERENCE-scheme sweep on
  * n values: scaled[i] = float(double(x[i]) * omega) and quotient[i] = x[i] / d[i] (d in 1..6) as
  * the kernel computes them without the FP64 pipe (either output may be NULL). */

@@ -80,7 +80,7 @@ struct GroupGrid {
 struct GroupSync {
     unsigned long long count;  // arrivals so far
     int abort;                 // a wait gave up: every CTA leaves at its next barrier
-    int pad;
+    int left;                  // CTAs that left the kernel because a barrier gave up
 };
 
 // Phases of the cooperative projection kernel.
@@ -97,6 +97,8 @@ struct GroupArgs {
     int nwaves;       // solve waves (every grid's `wave` is below this)
     int sweeps_only;  // tuning: only the sweep passes (fixed count, no checks), on scratch buffers
     int phases;       // GP_* bits: rhs + pressure start, colour-pass solve, subtract + divergence
+    unsigned long long wait_ns;  // a barrier wait gives up after this long (%globaltimer)
+    int skip_barrier;            // testing: CTA 0 does not arrive at this barrier (1-based; 0 = none)
 };
 
 // The blocked form of the grouped solve (host side): instead of the cooperative kernel's colour

@@ -19,9 +19,12 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
+
 #include "common.cuh"
 #include "group.h"
 #include "kernels.h"
+#include "sim_internal.h"
 #include "stage_bodies.cuh"
 
 namespace smk {
@@ -29,6 +32,14 @@ namespace smk {
 namespace {
 
 constexpr unsigned long long GROUP_WAIT_NS = 2000000000ull;  // a barrier wait gives up after 2 s
+
+// Testing (smk_inject_barrier_timeout): the next cooperative projection launch made outside a
+// capture gets a skipped arrival and a short wait; its barrier state is remembered for the report.
+std::mutex g_inject_mutex;
+int g_inject_barrier = 0;
+unsigned long long g_inject_wait_ns = 0;
+GroupSync* g_injected_sync = nullptr;
+int g_injected_ctas = 0;
 
 __device__ __forceinline__ unsigned long long global_ns() {
     unsigned long long t;
@@ -196,15 +207,19 @@ __global__ void __launch_bounds__(GROUP_TILE, 8) k_group_adv_rho(const GroupArgs
 
 // Grid barrier over the cooperative launch (all CTAs co-resident).  Arrivals count up in one
 // 64-bit counter that is zeroed before the launch; a CTA waits for `target` = its barrier
-// number x gridDim.x.  The wait is bounded: after 2 s it raises `abort`, and a CTA that sees
-// `abort` leaves too.  Returns false when the kernel must stop.
+// number x gridDim.x.  The wait is bounded: after a.wait_ns (2 s unless a test shortened it) it
+// raises `abort`, and a CTA that sees `abort` leaves too (each leaving CTA is counted in
+// sync->left).  a.skip_barrier (testing, host-injected) makes CTA 0 not arrive at that barrier,
+// so every wait on it runs out.  Returns false when the kernel must stop.
 __device__ bool group_barrier(const GroupArgs& a, unsigned long long& target) {
     __shared__ int ok_s;
     __syncthreads();
     target += gridDim.x;
     if (tid256() == 0) {
         __threadfence();
-        atomicAdd(&a.sync->count, 1ull);
+        const bool skip = a.skip_barrier > 0 && blockIdx.x == 0 &&
+                          target == (unsigned long long)a.skip_barrier * gridDim.x;
+        if (!skip) atomicAdd(&a.sync->count, 1ull);
         int ok = 1;
         const unsigned long long t0 = global_ns();
         while (*(volatile unsigned long long*)&a.sync->count < target) {
@@ -212,7 +227,7 @@ __device__ bool group_barrier(const GroupArgs& a, unsigned long long& target) {
                 ok = 0;
                 break;
             }
-            if (global_ns() - t0 > GROUP_WAIT_NS) {
+            if (global_ns() - t0 > a.wait_ns) {
                 atomicExch(&a.sync->abort, 1);
                 ok = 0;
                 break;
@@ -220,6 +235,7 @@ __device__ bool group_barrier(const GroupArgs& a, unsigned long long& target) {
             __nanosleep(32);
         }
         __threadfence();
+        if (!ok) atomicAdd(&a.sync->left, 1);
         ok_s = ok;
     }
     __syncthreads();
@@ -511,7 +527,24 @@ int launch_grid_stride(const void* kernel, int total, int occ, const GroupArgs& 
     return (int)cudaLaunchKernel(kernel, dim3((unsigned)ctas), dim3(SB_BX, SB_BY), args, 0, st);
 }
 
-int launch_project(const GroupArgs& a, const GroupLaunch& L, cudaStream_t st) {
+int launch_project(const GroupArgs& args, const GroupLaunch& L, cudaStream_t st) {
+    GroupArgs a = args;
+    a.wait_ns = GROUP_WAIT_NS;
+    a.skip_barrier = 0;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cap) != cudaSuccess) return (int)cudaGetLastError();
+    if (cap == cudaStreamCaptureStatusNone) {
+        // a pending barrier-timeout injection (testing) applies to this launch, made outside any
+        // graph capture (a captured launch would replay it), and is consumed
+        std::lock_guard<std::mutex> lock(g_inject_mutex);
+        if (g_inject_barrier > 0) {
+            a.skip_barrier = g_inject_barrier;
+            a.wait_ns = g_inject_wait_ns;
+            g_inject_barrier = 0;
+            g_injected_sync = a.sync;
+            g_injected_ctas = L.coop_ctas;
+        }
+    }
     cudaError_t e = cudaMemsetAsync(a.sync, 0, sizeof(GroupSync), st);
     if (e != cudaSuccess) return (int)e;
     cudaLaunchConfig_t cfg = {};
@@ -646,3 +679,31 @@ int launch_group_sweeps_only(const GroupArgs& a, const GroupLaunch& L, cudaStrea
 }
 
 }  // namespace smk
+
+// ---- testing: a grid-barrier wait that runs out, without any fault ------------------------------
+
+extern "C" int smk_inject_barrier_timeout(int barrier, int wait_ms) {
+    if (barrier < 0 || wait_ms < 1 || wait_ms > 10000)
+        return smk_fail(SMK_ERR_INVALID, "barrier must be >= 0 and wait_ms 1..10000");
+    std::lock_guard<std::mutex> lock(smk::g_inject_mutex);
+    smk::g_inject_barrier = barrier;
+    smk::g_inject_wait_ns = (unsigned long long)wait_ms * 1000000ull;
+    return SMK_OK;
+}
+
+extern "C" int smk_barrier_timeout_report(int* ctas_left, int* ctas) {
+    smk::GroupSync* sync = nullptr;
+    int n = 0;
+    {
+        std::lock_guard<std::mutex> lock(smk::g_inject_mutex);
+        sync = smk::g_injected_sync;
+        n = smk::g_injected_ctas;
+    }
+    if (sync == nullptr) return smk_fail(SMK_ERR_STATE, "no barrier-timeout injection has run");
+    SMK_CUDA(cudaDeviceSynchronize());
+    smk::GroupSync h;
+    SMK_CUDA(cudaMemcpy(&h, sync, sizeof(h), cudaMemcpyDeviceToHost));
+    if (ctas_left) *ctas_left = h.left;
+    if (ctas) *ctas = n;
+    return SMK_OK;
+}

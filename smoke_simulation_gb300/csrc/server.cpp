@@ -23,6 +23,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <deque>
@@ -66,6 +67,7 @@ struct Request {
     cudaEvent_t ev_start[2] = {nullptr, nullptr};
     cudaEvent_t ev_end[2] = {nullptr, nullptr};
     bool pending[2] = {false, false};
+    std::chrono::steady_clock::time_point submitted;  // host clock at smk_server_submit
 };
 
 // One issued server step: its events and the requests it advanced.
@@ -93,6 +95,9 @@ struct smk_server {
     std::vector<Request*> active;
     std::vector<Request*> all;  // owned
     std::vector<float> latencies_ms;
+    std::vector<float> queue_ms;  // per admitted request: submission to admission (host clock)
+    int peak_active = 0, peak_queued = 0;
+    size_t peak_bytes = 0;
     double cell_updates = 0.0;
     long long steps_completed = 0;
     int requests_completed = 0;
@@ -262,6 +267,7 @@ int smk_server_submit(smk_server* s, const smk_request_desc* d, int* id) {
     r->out = d->out_density;
     r->out_on_device = d->out_on_device != 0;
     r->bytes = footprint(d->nx, d->ny, d->nz);
+    r->submitted = std::chrono::steady_clock::now();
     s->all.push_back(r);
     if (r->bytes > s->budget) {
         r->state = SMK_REQ_FAILED;
@@ -286,6 +292,14 @@ static void collect(smk_server* s, TickRec& t) {
     }
     t.members.clear();
     t.pending = false;
+}
+
+// Queueing delay and occupancy bookkeeping of an admission.
+static void note_admission(smk_server* s, Request* r) {
+    const auto now = std::chrono::steady_clock::now();
+    s->queue_ms.push_back(std::chrono::duration<float, std::milli>(now - r->submitted).count());
+    s->peak_active = std::max(s->peak_active, (int)s->active.size());
+    s->peak_bytes = std::max(s->peak_bytes, s->used);
 }
 
 static int admit(smk_server* s, Request* r) {
@@ -426,8 +440,12 @@ static int tick_streams(smk_server* s) {
            s->used + s->queue.front()->bytes <= s->budget) {
         Request* r = s->queue.front();
         s->queue.pop_front();
-        if (admit(s, r) == SMK_OK) s->active.push_back(r);
+        if (admit(s, r) == SMK_OK) {
+            s->active.push_back(r);
+            note_admission(s, r);
+        }
     }
+    s->peak_queued = std::max(s->peak_queued, (int)s->queue.size());
     // (3) one step per active request, each on its own stream
     for (Request* r : s->active) {
         if (r->steps_issued >= r->steps || r->cancel) continue;
@@ -504,8 +522,12 @@ static int tick_grouped(smk_server* s) {
            s->used + s->queue.front()->bytes <= s->budget) {
         Request* r = s->queue.front();
         s->queue.pop_front();
-        if (admit(s, r) == SMK_OK) s->active.push_back(r);
+        if (admit(s, r) == SMK_OK) {
+            s->active.push_back(r);
+            note_admission(s, r);
+        }
     }
+    s->peak_queued = std::max(s->peak_queued, (int)s->queue.size());
     // (3) one grouped step over every active request with steps left (requests on the
     // reference projection, which the grouped kernels do not run, step on their own)
     std::vector<smk_sim*> grouped;
@@ -590,17 +612,24 @@ int smk_server_get_stats(smk_server* s, smk_server_stats* out) {
     out->active = (int)s->active.size();
     out->queued = (int)s->queue.size();
     out->bytes_in_use = s->used;
+    auto pct = [](std::vector<float> v, double q) {
+        size_t i = (size_t)std::min<double>((double)v.size() - 1, q * (double)(v.size() - 1) + 0.5);
+        std::nth_element(v.begin(), v.begin() + i, v.end());
+        return v[i];
+    };
     if (!s->latencies_ms.empty()) {
-        std::vector<float> v = s->latencies_ms;
-        auto pct = [&v](double q) {
-            size_t i = (size_t)std::min<double>((double)v.size() - 1, q * (double)(v.size() - 1) + 0.5);
-            std::nth_element(v.begin(), v.begin() + i, v.end());
-            return v[i];
-        };
-        out->p50_step_ms = pct(0.50);
-        out->p99_step_ms = pct(0.99);
-        out->max_step_ms = *std::max_element(v.begin(), v.end());
+        out->p50_step_ms = pct(s->latencies_ms, 0.50);
+        out->p99_step_ms = pct(s->latencies_ms, 0.99);
+        out->max_step_ms = *std::max_element(s->latencies_ms.begin(), s->latencies_ms.end());
     }
+    if (!s->queue_ms.empty()) {
+        out->p50_queue_ms = pct(s->queue_ms, 0.50);
+        out->p99_queue_ms = pct(s->queue_ms, 0.99);
+        out->max_queue_ms = *std::max_element(s->queue_ms.begin(), s->queue_ms.end());
+    }
+    out->peak_active = s->peak_active;
+    out->peak_queued = s->peak_queued;
+    out->peak_bytes = s->peak_bytes;
     return SMK_OK;
 }
 

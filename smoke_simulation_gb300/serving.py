@@ -36,7 +36,9 @@ class ServerStats(C.Structure):
     _fields_ = [("steps_completed", C.c_longlong), ("requests_completed", C.c_int),
                 ("active", C.c_int), ("queued", C.c_int), ("cell_updates", C.c_double),
                 ("bytes_in_use", C.c_size_t), ("p50_step_ms", C.c_float),
-                ("p99_step_ms", C.c_float), ("max_step_ms", C.c_float)]
+                ("p99_step_ms", C.c_float), ("max_step_ms", C.c_float),
+                ("p50_queue_ms", C.c_float), ("p99_queue_ms", C.c_float), ("max_queue_ms", C.c_float),
+                ("peak_active", C.c_int), ("peak_queued", C.c_int), ("peak_bytes", C.c_size_t)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

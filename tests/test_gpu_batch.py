@@ -315,3 +315,49 @@ def test_grouped_vector_stages_equal_per_cell(gpu, storage):
     bb.close()
     for s in a + b:
         s.close()
+
+
+@pytest.mark.parametrize("barrier", [1, 3])
+def test_grid_barrier_wait_runs_out_and_recovers(gpu, barrier):
+    """A grid-barrier wait of the cooperative grouped projection that runs out (CTA 0 made to
+    skip one arrival, waits shortened to 20 ms): every CTA leaves the kernel, every member's next
+    synchronisation reports SMK_ERR_TIMEOUT, and the context stays usable -- a new batch of fresh
+    members then gives, bit for bit, what the same grids give stepped alone."""
+    import ctypes as C
+    scs = [sc for i, sc in enumerate(_scenes()) if i != 2]  # PRESSURE members only (GROUPED)
+    sims = [smk.from_scene(sc, report_div=1) for sc in scs]
+    batch = smk.Batch(sims, mode=smk.BATCH_GROUPED)
+    batch.set_graphs(False)
+    batch.set_schedule(0, 4, 0)  # the cooperative colour-pass solve: several grid barriers
+    batch.step(scs[0].dt)
+    for s in sims:
+        s.sync()
+    L = smk.lib()
+    L.smk_inject_barrier_timeout.argtypes = [C.c_int, C.c_int]
+    L.smk_barrier_timeout_report.argtypes = [C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    assert L.smk_inject_barrier_timeout(barrier, 20) == 0
+    batch.step(scs[0].dt)
+    left, ctas = C.c_int(), C.c_int()
+    assert L.smk_barrier_timeout_report(C.byref(left), C.byref(ctas)) == 0
+    assert ctas.value > 0 and left.value == ctas.value
+    for s in sims:
+        with pytest.raises(smk.SmokeError) as e:
+            s.sync()
+        assert e.value.code == smk.ERR_TIMEOUT
+        s.sync()  # reported once; the context is usable
+    batch.close()
+    for s in sims:
+        s.close()
+    # fresh members on the same context: batched == alone, bit for bit
+    fresh = [smk.from_scene(sc, report_div=1) for sc in scs]
+    alone = [smk.from_scene(sc, report_div=1) for sc in scs]
+    b2 = smk.Batch(fresh, mode=smk.BATCH_GROUPED)
+    for _ in range(3):
+        b2.step(scs[0].dt)
+        for s, sc in zip(alone, scs):
+            s.step(sc.dt)
+    for a, b in zip(fresh, alone):
+        assert H.first_mismatch(a.read_state(), b.read_state()) == ""
+    b2.close()
+    for s in fresh + alone:
+        s.close()
