@@ -290,6 +290,7 @@ def main():
                     help="requests of the serving run under a binding memory budget (0: skip)")
     ap.add_argument("--serve-tight-gb", type=float, default=1.5, help="that run's device-memory budget (GB)")
     ap.add_argument("--render-frames", type=int, default=20, help="timed frames of the render form (0: skip)")
+    ap.add_argument("--dropin-steps", type=int, default=20, help="timed steps of the drop-in form (0: skip)")
     ap.add_argument("--no-forms", action="store_true", help="skip the batched/mixed/serving forms")
     ap.add_argument("--sweep-kernel", default="", help="D,Z[,R]: blocked sweep depth, z-chunk and patch "
                     "rows instead of the autotuner's choice (to profile the configuration a timed run chose)")
@@ -624,33 +625,68 @@ def run_forms(args, smk, torch):
                         "grouped_bf16_vs_plain_warm": batched["bf16"]["value"] / plain_warm["value"],
                         "grouped_f32_vs_plain_warm": batched["f32"]["value"] / plain_warm["value"]}
 
+    # ---- the drop-in path: the reference's simulate() on the REFERENCE scheme -----------------
+    if args.dropin_steps > 0:
+        dropin = {}
+        for name, sc, iters in (("256", S.config_large(256, steps=args.dropin_steps), 30),
+                                ("80", S.config_ref80(steps=args.dropin_steps), 40)):
+            # the reference's projection: in-place velocity red-black SOR, fixed iterations (30 is
+            # the reference's own count, 40 the 80^3 configuration's); bit-exact with the reference
+            sc.scheme, sc.iterations, sc.tol, sc.warm_start = 0, iters, 0.0, 0
+            sim = smk.from_scene(sc)
+            kernel = sim.autotune()[:2]
+            out = torch.empty(sc.cell_shape, dtype=torch.float32, pin_memory=True).numpy()
+            for _ in range(max(args.warmup, 2)):
+                sim.simulate(out, sc.dt)
+            t0 = time.perf_counter()
+            for _ in range(args.dropin_steps):
+                sim.simulate(out, sc.dt)
+            e2e_s = (time.perf_counter() - t0) / args.dropin_steps
+            dev_s = _timed_steps(lambda: sim.step(sc.dt, sh), stream, args.dropin_steps, torch) / args.dropin_steps
+            dropin[name] = {"iterations": iters, "velocity_sweep": list(kernel),
+                            "device_ms_per_step": 1e3 * dev_s, "simulate_ms_per_step": 1e3 * e2e_s,
+                            "value": sc.cells / dev_s, "simulate_value": sc.cells / e2e_s}
+            sim.close()
+        forms["dropin"] = {"workload": "smk_simulate / simulate() on the REFERENCE scheme (the reference's "
+                                       "in-place velocity SOR, bit-exact with the reference): the 256^3 workload "
+                                       "at the reference's 30 iterations and the 80^3 configuration at 40; "
+                                       "velocity-sweep kernel from the autotuner (depth, z-chunk); the "
+                                       "reference's own kernels on the same GPU: oracle/time_reference_gpu.py, "
+                                       "profiles/reference_gpu_step_large256.md",
+                           **dropin}
+
     # ---- mixed precision at 512^3 -------------------------------------------------------------
     if args.mixed_n > 0:
         sc = S.config_mixed(args.mixed_n, steps=args.forms_steps)
         sc.warm_start = 1
         mixed = {}
         rho = {}
-        for name, storage in (("f32", smk.STORAGE_F32), ("bf16_vel", smk.STORAGE_BF16_VEL),
-                              ("bf16_all", smk.STORAGE_BF16)):
+        for name, storage, extra in (("f32", smk.STORAGE_F32, {}), ("bf16_vel", smk.STORAGE_BF16_VEL, {}),
+                                     ("bf16_all", smk.STORAGE_BF16, {}),
+                                     # the configuration as specified: FP32 weighted Jacobi (weight 1)
+                                     ("bf16_all_jacobi", smk.STORAGE_BF16,
+                                      {"solver": smk.SOLVER_JACOBI, "omega": 1.0})):
             # FP32 pressure solve with the FP64-checked refinement (2 rounds of 10 sweeps at most)
-            sim = smk.from_scene(sc, report_div=1, storage=storage, refine=2, refine_sweeps=10)
+            sim = smk.from_scene(sc, report_div=1, storage=storage, refine=2, refine_sweeps=10, **extra)
             sim.autotune()
             sim.step(sc.dt, sh)  # mask upload step (direct launches)
             secs = _timed_steps(lambda: sim.step(sc.dt, sh), stream, args.forms_steps - 1, torch)
             st = sim.stats()
             mixed[name] = {"value": float(sc.cells) * (args.forms_steps - 1) / secs,
                            "ms_per_step": 1e3 * secs / (args.forms_steps - 1), "sweeps_last": st.sweeps,
+                           "converged_last": st.converged,
                            "max_div_post_projection": st.div_max, "max_div_fp64": st.div64_max,
                            "refine_rounds_last": st.refine_rounds}
             rho[name] = sim.read_density()
             sim.close()
-        for name in ("bf16_vel", "bf16_all"):
+        for name in ("bf16_vel", "bf16_all", "bf16_all_jacobi"):
             mixed[name]["density_rel_l2_vs_f32"] = _rel_l2(rho[name], rho["f32"])
         forms["mixed"] = {"workload": "%d^3, 2%% random solids (seed 3), one 32x8x32 emitter, dt=0.02, "
                                       "warm-started FP32 pressure red-black SOR to max|div|<=1e-4 (checked every "
                                       "10 sweeps), then max|div| measured with FP64 accumulation and "
                                       "corrected by up to 2 refinement rounds while above 1e-4, %d steps; bf16_vel = u,v,w in BF16 + density FP32, bf16_all = "
-                                      "density too; errors vs the FP64 oracle are tested at 80^3"
+                                      "density too; bf16_all_jacobi = all-BF16 with the FP32 weighted-Jacobi solve (weight 1) "
+                                      "and the same refinement; errors vs the FP64 oracle: tests/test_gpu_headline.py (512^3, 2 steps)"
                                       % (args.mixed_n, args.forms_steps),
                           "cells": float(sc.cells), **mixed}
 

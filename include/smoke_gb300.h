@@ -77,7 +77,7 @@ typedef struct smk_params {
     int solver;         /* PRESSURE only: SMK_SOLVER_RBSOR (default) red-black SOR, or
                            SMK_SOLVER_JACOBI weighted Jacobi: every cell from the previous
                            iterate, P += (omega/acc) * residual, one iteration per "sweep" (use
-                           omega <= 1; not with refine). */
+                           omega <= 1); the refinement rounds' correction solves stay red-black. */
 } smk_params;
 
 typedef struct smk_stats {

@@ -51,8 +51,8 @@ int check_params(const smk_params* p) {
     if (p->refine > 0 && (p->refine_sweeps < 1 || p->refine_sweeps > 100000))
         return fail(SMK_ERR_INVALID, "refine_sweeps must be 1..100000");
     if (p->solver != SMK_SOLVER_RBSOR && p->solver != SMK_SOLVER_JACOBI) return fail(SMK_ERR_INVALID, "unknown solver");
-    if (p->solver == SMK_SOLVER_JACOBI && (p->projection != SMK_PROJECT_PRESSURE || p->refine > 0))
-        return fail(SMK_ERR_INVALID, "the Jacobi solver needs the PRESSURE projection and no refinement");
+    if (p->solver == SMK_SOLVER_JACOBI && p->projection != SMK_PROJECT_PRESSURE)
+        return fail(SMK_ERR_INVALID, "the Jacobi solver needs the PRESSURE projection");
     if (p->projection == SMK_PROJECT_PRESSURE && p->tol > 0 &&
         (p->max_sweeps + p->check_every - 1) / p->check_every > 4000)
         return fail(SMK_ERR_INVALID, "too many residual checks per step (max_sweeps/check_every > 4000)");

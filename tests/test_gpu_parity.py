@@ -509,3 +509,22 @@ def test_velocity_sweep_autotune_keeps_results(gpu):
         sim.step(sc.dt)
         assert H.first_mismatch(sim.read_state(), H.oracle_state(o)) == "", k
     sim.close()
+
+
+def test_jacobi_with_refinement_bit_exact_with_oracle(gpu):
+    """The FP32 weighted-Jacobi solve followed by FP64-checked refinement rounds (the
+    mixed-precision configuration's solver): the oracle's bits, sweep counts, rounds and FP64
+    divergence, with graph replay."""
+    sc = S.small_scene(26, 22, 24, steps=4, seed=37, scheme=1, iterations=30, tol=1e-5, check_every=5,
+                       warm_start=1, solver=smk.SOLVER_JACOBI, omega=0.9)
+    sc.refine, sc.refine_sweeps = 2, 8
+    sim = smk.from_scene(sc, report_div=1)
+    o = O.OracleSim(sc)
+    for k in range(sc.steps):
+        sim.step(sc.dt)
+        so = o.step()
+        sg = sim.stats()
+        assert (sg.sweeps, sg.refine_rounds) == (so.sweeps, so.refine_rounds), k
+        assert H.bits_equal(np.float32(sg.div64_max), np.float32(so.div64_max)), k
+    assert H.first_mismatch(sim.read_state(), H.oracle_state(o)) == ""
+    sim.close()
