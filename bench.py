@@ -461,6 +461,19 @@ def main():
                          "on the GPU in this run), %.1f s" % (args.cpu_steps, args.side, ref_sweeps,
                                                              secs)}
 
+    # errors of this workload's fields against the FP64 oracle, as measured by the headline parity
+    # test (tests/test_gpu_headline.py: the GPU fields are bit-exact with the FP32 oracle there)
+    err_keys = {}
+    ef = os.path.join(ROOT, "profiles", "err_vs_fp64.json")
+    if os.path.exists(ef) and args.side == 256:
+        with open(ef) as f:
+            worst = json.load(f)["large256"]["worst_vs_fp64"]
+        err_keys = {"err_rho_max_abs_vs_fp64": worst["rho"]["max_abs"],
+                    "err_rho_rel_l2_vs_fp64": worst["rho"]["rel_l2"],
+                    "err_vel_max_abs_vs_fp64": max(worst[k]["max_abs"] for k in "uvw"),
+                    "err_vel_rel_l2_vs_fp64": max(worst[k]["rel_l2"] for k in "uvw"),
+                    "err_source": "tests/test_gpu_headline.py, first 5 steps, bit-exact with the FP32 oracle"}
+
     forms = None
     if rank == 0 and ws == 1 and not args.no_forms:
         sim.close()
@@ -497,6 +510,7 @@ def main():
                        "cold_ms_per_step": cold["ms_per_step"] if cold else None,
                        "cold_mean_sweeps": cold["mean_sweeps"] if cold else None,
                        "warm_start_gain": (value / cold["value"]) if cold else None,
+                       **err_keys,
                        "cold_start_form": cold},
             "roofline": {"bound": "hbm", "kernel": "%s (z-chunk %d)" % (kname, zchunk),
                          "achieved": achieved, "peak": peak, "unit": "GB/s",
