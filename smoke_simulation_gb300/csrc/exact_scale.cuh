@@ -87,13 +87,13 @@ __host__ __device__ __forceinline__ float omega_scale(float q, const OmegaSplit&
     return es_bits(sign + ((uint32_t)((int)E + s.eo + big - 1) << 23) + t24);
 }
 
-// x / d, d = 1..6, r = RN(1/d).
-__host__ __device__ __forceinline__ float div_small(float x, int d, float r) {
+// x / d, d = 1..6 given as the float df, r = RN(1/d).
+__host__ __device__ __forceinline__ float div_small(float x, float df, float r) {
     const float ax = fabsf(x);
     if (ax == 0.0f) return x;
-    if (!(ax >= 0x1p-100f && ax < 0x1p100f)) return es_div_slow(x, (float)d);
+    if (!(ax >= 0x1p-100f && ax < 0x1p100f)) return es_div_slow(x, df);
     const float y = x * r;
-    const float e = fmaf(-y, (float)d, x);
+    const float e = fmaf(-y, df, x);
     return fmaf(e, r, y);
 }
 

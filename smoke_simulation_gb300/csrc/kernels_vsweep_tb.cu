@@ -81,24 +81,39 @@ struct VMaps {
 
 __device__ __forceinline__ float fsel(unsigned f, unsigned bit) { return (f & bit) ? 1.0f : 0.0f; }
 
-// p_t of a cell with flag byte f from its six faces; 0 for a cell that is not projectable
-// (every use of p_t is predicated on the projectable bit).  The divisor is kept >= 1 so that a
-// non-projectable cell's quotient stays finite.  rcp[d] = RN(1/d).
-__device__ __forceinline__ float cell_pt(unsigned f, float uc, float ux, float vc, float vy, float wc, float wz,
-                                         const float* rcp, const OmegaSplit& os, double omega) {
+// Per neighbour pattern (the flag byte's six neighbour bits, e = (f >> 1) & 63): the divisor acc
+// (>= 1, so a non-projectable cell's quotient stays finite) as a float, RN(1/acc), and the six 0/1
+// face multipliers s(x-1), s(y-1), s(z-1) | s(x+1), s(y+1), s(z+1), from a shared table
+// (two 16-byte reads instead of a population count, a conversion and six selects per update).
+struct CellCoef {
+    float4 a;  // acc, RN(1/acc), s(x-1), s(y-1)
+    float4 b;  // s(z-1), s(x+1), s(y+1), s(z+1)
+};
+
+__device__ __forceinline__ CellCoef make_coef(int e) {
+    const int acc = max(__popc((unsigned)e), 1);
+    CellCoef c;
+    c.a = make_float4((float)acc, 1.0f / (float)acc, (e & 1) ? 1.f : 0.f, (e & 4) ? 1.f : 0.f);
+    c.b = make_float4((e & 16) ? 1.f : 0.f, (e & 2) ? 1.f : 0.f, (e & 8) ? 1.f : 0.f, (e & 32) ? 1.f : 0.f);
+    return c;
+}
+
+// p_t of a cell from its six faces; 0 for a cell that is not projectable (every use of p_t is
+// predicated on the projectable bit).
+__device__ __forceinline__ float cell_pt(unsigned f, const CellCoef& c, float uc, float ux, float vc, float vy,
+                                         float wc, float wz, const OmegaSplit& os, double omega) {
     const float div = -uc + ux + -vc + vy + -wc + wz;
-    const int acc = max(__popc(f & F_NBRS), 1);
-    const float q = div_small(-div, acc, rcp[acc]);
+    const float q = div_small(-div, c.a.x, c.a.y);
     const float pt = omega_scale(q, os, omega);
     return (f & F_PROJ) ? pt : 0.0f;
 }
 
 // Own (lower) faces of an updated cell: u_x -= p_t*s(x-1), v_y -= p_t*s(y-1), w_z -= p_t*s(z-1).
-__device__ __forceinline__ void own_faces(unsigned f, float pt, float& u, float& v, float& w) {
+__device__ __forceinline__ void own_faces(unsigned f, const CellCoef& c, float pt, float& u, float& v, float& w) {
     if (f & F_PROJ) {
-        u = u - pt * fsel(f, F_XM);
-        v = v - pt * fsel(f, F_YM);
-        w = w - pt * fsel(f, F_ZM);
+        u = u - pt * c.a.z;
+        v = v - pt * c.a.w;
+        w = w - pt * c.b.x;
     }
 }
 
@@ -128,12 +143,12 @@ __device__ __forceinline__ void vsweep_tile(const VMaps& maps, const Grid& g, fl
     unsigned char* stages = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
     float* pub = reinterpret_cast<float*>(stages + S * VT_STAGE);
     __shared__ __align__(8) uint64_t mbar[S];
-    __shared__ float rcp[8];  // RN(1/d), d = 1..7 (0 unused)
+    __shared__ CellCoef ctab[64];  // per neighbour pattern (make_coef)
 
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int tid = ty * TX + tx;
     const bool leader = tid == 0;
-    if (tid < 8) rcp[tid] = tid > 0 ? 1.0f / (float)tid : 0.0f;
+    if (tid < 64) ctab[tid] = make_coef(tid);
     // zero the padding rows of every published plane (never written afterwards)
     for (int i = tid; i < 2 * NPUB * 2 * TX; i += VT_THREADS) {
         const int lane = i % TX, edge = (i / TX) % 2, set = i / (2 * TX);
@@ -162,7 +177,11 @@ __device__ __forceinline__ void vsweep_tile(const VMaps& maps, const Grid& g, fl
     // zero-initialised ring stands for them, so a chunk near z = 0 may start at plane 0 where that
     // saves a pass of the unrolled loop
     const int qend = zb + T;
-    const int qbeg = (za - T < 0 && (qend + R) / R < (qend - (za - T) + R) / R) ? 0 : za - T;
+    int qbeg = (za - T < 0 && (qend + R) / R < (qend - (za - T) + R) / R) ? 0 : za - T;
+    // start one plane lower where needed so that iteration k of every unrolled pass has the
+    // update pattern of k's parity (fixed at compile time: one pattern's code per iteration); the
+    // extra plane is one more halo plane (zero-filled below plane 0)
+    qbeg -= (qbeg + colour0 - 1) & 1;
     const int nouter = (qend - qbeg + R) / R;
     const int qfinal = qbeg + nouter * R - 1;
 
@@ -192,7 +211,6 @@ __device__ __forceinline__ void vsweep_tile(const VMaps& maps, const Grid& g, fl
     }
     const int me0 = (ty + 1) * TX + tx;
     int par = 0;
-    const int c_par = (qbeg + colour0 - 1) & 1;
     __syncthreads();  // barriers initialised, table and padding visible
 
     for (int base = qbeg; base <= qend; base += R) {
@@ -201,8 +219,9 @@ __device__ __forceinline__ void vsweep_tile(const VMaps& maps, const Grid& g, fl
             const int q = base + k;
             const int st = k % S;
             const uint32_t phase = (uint32_t)((k / S) & 1);
-            // updated cells of every stage of this iteration: A0 and B1 (sA), else B0 and A1
-            const bool sA = ((k + c_par) & 1) == 0;
+            // updated cells of every stage of this iteration: A0 and B1 (sA), else B0 and A1; the
+            // pattern follows (q + colour0 - 1), which qbeg's choice makes k's parity
+            const bool sA = (k & 1) == 0;
             float* cur = pub + par * NPUB * VT_PROW;              // written this iteration
             const float* prv = pub + (par ^ 1) * NPUB * VT_PROW;  // written by the last one
 
@@ -278,41 +297,43 @@ __device__ __forceinline__ void vsweep_tile(const VMaps& maps, const Grid& g, fl
                 const float vb = prv[(2 * (t - 1)) * VT_PROW + me0 + TX];
                 if (sA) {
                     const unsigned fA0 = fbyte(f, 0), fB1 = fbyte(f, 3), fA1 = fbyte(f, 2);
+                    const CellCoef cA0 = ctab[(fA0 >> 1) & 63u], cB1 = ctab[(fB1 >> 1) & 63u];
                     const float uR = __shfl_down_sync(0xffffffffu, U[1][j].x, 1);  // lane + 1's A1
-                    const float pA0 = cell_pt(fA0, U[0][j].x, U[0][j].y, V[0][j].x, V[1][j].x, W[0][j].x,
-                                              W[0][jn].x, rcp, os, omega);
-                    const float pB1 = cell_pt(fB1, U[1][j].y, uR, V[1][j].y, vb, W[1][j].y, W[1][jn].y, rcp, os,
+                    const float pA0 = cell_pt(fA0, cA0, U[0][j].x, U[0][j].y, V[0][j].x, V[1][j].x, W[0][j].x,
+                                              W[0][jn].x, os, omega);
+                    const float pB1 = cell_pt(fB1, cB1, U[1][j].y, uR, V[1][j].y, vb, W[1][j].y, W[1][jn].y, os,
                                               omega);
-                    own_faces(fA0, pA0, U[0][j].x, V[0][j].x, W[0][j].x);
-                    own_faces(fB1, pB1, U[1][j].y, V[1][j].y, W[1][j].y);
+                    own_faces(fA0, cA0, pA0, U[0][j].x, V[0][j].x, W[0][j].x);
+                    own_faces(fB1, cB1, pB1, U[1][j].y, V[1][j].y, W[1][j].y);
                     const float pL = __shfl_up_sync(0xffffffffu, pB1, 1);  // lane - 1's B1
                     if (fA0 & F_PROJ) {
-                        U[0][j].y = U[0][j].y + pA0 * fsel(fA0, F_XP);    // B0's u
-                        V[1][j].x = V[1][j].x + pA0 * fsel(fA0, F_YP);    // A1's v
-                        W[0][jn].x = W[0][jn].x + pA0 * fsel(fA0, F_ZP);  // w above A0
+                        U[0][j].y = U[0][j].y + pA0 * cA0.b.y;    // B0's u
+                        V[1][j].x = V[1][j].x + pA0 * cA0.b.z;    // A1's v
+                        W[0][jn].x = W[0][jn].x + pA0 * cA0.b.w;  // w above A0
                     }
                     if (gb & G_XA1) U[1][j].x = U[1][j].x + pL * fsel(fA1, F_SELF);
-                    if (fB1 & F_PROJ) W[1][jn].y = W[1][jn].y + pB1 * fsel(fB1, F_ZP);
+                    if (fB1 & F_PROJ) W[1][jn].y = W[1][jn].y + pB1 * cB1.b.w;
                     cur[(2 * t) * VT_PROW + me0] = V[0][j].x;
                     cur[(2 * t + 1) * VT_PROW + me0] = pB1;
                 } else {
                     const unsigned fB0 = fbyte(f, 1), fA1 = fbyte(f, 2), fA0 = fbyte(f, 0);
+                    const CellCoef cB0 = ctab[(fB0 >> 1) & 63u], cA1 = ctab[(fA1 >> 1) & 63u];
                     const float uR = __shfl_down_sync(0xffffffffu, U[0][j].x, 1);  // lane + 1's A0
-                    const float pB0 = cell_pt(fB0, U[0][j].y, uR, V[0][j].y, V[1][j].y, W[0][j].y, W[0][jn].y,
-                                              rcp, os, omega);
-                    const float pA1 = cell_pt(fA1, U[1][j].x, U[1][j].y, V[1][j].x, vb, W[1][j].x, W[1][jn].x, rcp,
+                    const float pB0 = cell_pt(fB0, cB0, U[0][j].y, uR, V[0][j].y, V[1][j].y, W[0][j].y, W[0][jn].y,
                                               os, omega);
-                    own_faces(fB0, pB0, U[0][j].y, V[0][j].y, W[0][j].y);
-                    own_faces(fA1, pA1, U[1][j].x, V[1][j].x, W[1][j].x);
+                    const float pA1 = cell_pt(fA1, cA1, U[1][j].x, U[1][j].y, V[1][j].x, vb, W[1][j].x, W[1][jn].x,
+                                              os, omega);
+                    own_faces(fB0, cB0, pB0, U[0][j].y, V[0][j].y, W[0][j].y);
+                    own_faces(fA1, cA1, pA1, U[1][j].x, V[1][j].x, W[1][j].x);
                     const float pL = __shfl_up_sync(0xffffffffu, pB0, 1);  // lane - 1's B0
                     if (fB0 & F_PROJ) {
-                        V[1][j].y = V[1][j].y + pB0 * fsel(fB0, F_YP);    // B1's v
-                        W[0][jn].y = W[0][jn].y + pB0 * fsel(fB0, F_ZP);  // w above B0
+                        V[1][j].y = V[1][j].y + pB0 * cB0.b.z;    // B1's v
+                        W[0][jn].y = W[0][jn].y + pB0 * cB0.b.w;  // w above B0
                     }
                     if (gb & G_XA0) U[0][j].x = U[0][j].x + pL * fsel(fA0, F_SELF);
                     if (fA1 & F_PROJ) {
-                        U[1][j].y = U[1][j].y + pA1 * fsel(fA1, F_XP);    // B1's u
-                        W[1][jn].x = W[1][jn].x + pA1 * fsel(fA1, F_ZP);  // w above A1
+                        U[1][j].y = U[1][j].y + pA1 * cA1.b.y;    // B1's u
+                        W[1][jn].x = W[1][jn].x + pA1 * cA1.b.w;  // w above A1
                     }
                     cur[(2 * t) * VT_PROW + me0] = V[0][j].y;
                     cur[(2 * t + 1) * VT_PROW + me0] = pA1;
@@ -479,7 +500,7 @@ extern "C" int smk_test_exact_arith(const float* x, const int* d, int n, double 
         if (scaled) scaled[i] = smk::omega_scale(x[i], os, omega);
         if (quotient && d) {
             const int k = d[i] < 1 ? 1 : (d[i] > 6 ? 6 : d[i]);
-            quotient[i] = smk::div_small(x[i], k, 1.0f / (float)k);
+            quotient[i] = smk::div_small(x[i], (float)k, 1.0f / (float)k);
         }
     }
     return 0;
