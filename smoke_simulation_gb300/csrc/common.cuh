@@ -151,6 +151,16 @@ __device__ __forceinline__ float avgW(const T* __restrict__ f, const Grid& g, in
     return s / 8.0f;
 }
 
+// The eight weighted corner terms of sampleSmoke (smokeSimulation.cu:474-482), summed in the
+// reference's order.
+__device__ __forceinline__ float trilinear_ref(float xw0, float xw1, float yw0, float yw1, float zw0, float zw1,
+                                               float a000, float a100, float a010, float a110, float a001,
+                                               float a101, float a011, float a111) {
+    return xw0 * yw0 * zw0 * a000 + xw1 * yw0 * zw0 * a100 + xw0 * yw1 * zw0 * a010 +
+           xw1 * yw1 * zw0 * a110 + xw0 * yw0 * zw1 * a001 + xw1 * yw0 * zw1 * a101 +
+           xw0 * yw1 * zw1 * a011 + xw1 * yw1 * zw1 * a111;
+}
+
 // sampleSmoke (smokeSimulation.cu:451-484): clamp the position to [1, n-1] with the CELL
 // dims, trilinear weights from (c - delta) - i0, eight terms summed in the reference's order.
 // HX, HY, HZ: delta = 0.5 on that axis (1) or 0 (0); every call site has n >= 2 on every axis
@@ -193,9 +203,7 @@ __device__ __forceinline__ float sample_ref(const T* __restrict__ f, const Grid&
     const bool sx = HX || x0 < lx;
     const float a100 = sx ? b100 : a000, a110 = sx ? b110 : a010, a101 = sx ? b101 : a001,
                 a111 = sx ? b111 : a011;
-    return xw0 * yw0 * zw0 * a000 + xw1 * yw0 * zw0 * a100 + xw0 * yw1 * zw0 * a010 +
-           xw1 * yw1 * zw0 * a110 + xw0 * yw0 * zw1 * a001 + xw1 * yw0 * zw1 * a101 +
-           xw0 * yw1 * zw1 * a011 + xw1 * yw1 * zw1 * a111;
+    return trilinear_ref(xw0, xw1, yw0, yw1, zw0, zw1, a000, a100, a010, a110, a001, a101, a011, a111);
 }
 
 // Loads issued where they stand (volatile inline PTX): the compiler can neither sink them into

@@ -157,10 +157,17 @@ void launch_refine(const Grid& g, float* u, float* v, float* w, Tv* us, Tv* vs, 
                    float* P1, const int* pcur, const uint8_t* flags, const float* wacc7, int rounds,
                    int sweeps, double tol, RefineStatus* rs, long long* launches, cudaStream_t st);
 
-// Stage a: advection.
-template <typename Ti, typename To>
-void launch_advect_velocity(const Grid& g, const Ti* u0, const Ti* v0, const Ti* w0, To* u1, To* v1,
-                            To* w1, const uint8_t* flags, float dt, cudaStream_t st);
+// Stage a: advection.  The velocity advection reads its FP32 input planes through TMA tensor
+// maps: create_advect_maps encodes n <= 2 input sets (u[k], v[k], w[k]) once the buffers exist
+// (NULL on failure); a launch names the set its u0, v0, w0 are.
+struct AdvectMaps;
+AdvectMaps* create_advect_maps(const Grid& g, const float* const* u, const float* const* v, const float* const* w,
+                               int n);
+void destroy_advect_maps(AdvectMaps* m);
+template <typename To>
+int launch_advect_velocity_tile(const AdvectMaps* m, int set, const Grid& g, const float* u0, const float* v0,
+                                const float* w0, To* u1, To* v1, To* w1, const uint8_t* flags, float dt, int* kerr,
+                                cudaStream_t st);
 template <typename T, typename Tv>
 void launch_advect_density(const Grid& g, const T* r0, T* r1, const Tv* u1, const Tv* v1, const Tv* w1,
                            const uint8_t* flags, float dt, cudaStream_t st);

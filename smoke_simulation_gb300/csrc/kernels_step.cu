@@ -155,24 +155,11 @@ __global__ void k_project_velocity(Grid g, float* __restrict__ u, float* __restr
     w[iz] = w[iz] + pt * (float)sz1;
 }
 
-// ---- a: velocityAdvectionU/V/W (:527-615) and advectSmoke (:617-638) ------------------------
-// The advection kernels are latency-bound gathers: the register caps keep 8 blocks of 8 warps
-// per SM (32 registers; the velocity kernel spills 4 bytes there and still runs 3% faster than at
-// 6 blocks with 40 registers).  Each block walks ADV_ZC consecutive
-// planes in ascending z: the planes a cell's averages and samples read overlap the next
-// cell's and stay in L1 between them (3% faster than one plane per block at 256^3).
-template <typename Ti, typename To>
-__global__ void __launch_bounds__(BX * BY, 8) k_advect_velocity(Grid g, const Ti* __restrict__ u0, const Ti* __restrict__ v0,
-                                  const Ti* __restrict__ w0, To* __restrict__ u1,
-                                  To* __restrict__ v1, To* __restrict__ w1,
-                                  const uint8_t* __restrict__ flags, float dt, int rz) {
-    for (int k = 0; k < ADV_ZC; ++k) {
-        const int zz = (int)blockIdx.z * ADV_ZC + k;
-        if (zz >= rz) break;
-        body_advect_velocity(g, u0, v0, w0, u1, v1, w1, flags, dt, make_uint3(blockIdx.x, blockIdx.y, (unsigned)zz));
-    }
-}
-
+// ---- a: advectSmoke (:617-638); the velocity advection is kernels_advect_tile.cu -------------
+// The density advection is a latency-bound gather: the register cap keeps 8 blocks of 8 warps
+// per SM (32 registers).  Each block walks ADV_ZC consecutive planes in ascending z: the planes
+// a cell's sample reads overlap the next cell's and stay in L1 between them (3% faster than one
+// plane per block at 256^3).
 template <typename T, typename Tv>
 __global__ void __launch_bounds__(BX * BY, 8) k_advect_density(Grid g, const T* __restrict__ r0, T* __restrict__ r1,
                                  const Tv* __restrict__ u, const Tv* __restrict__ v,
@@ -333,15 +320,6 @@ void launch_project_velocity(const Grid& g, float* u, float* v, float* w, const 
                                                                                  colour, omega);
 }
 
-template <typename Ti, typename To>
-void launch_advect_velocity(const Grid& g, const Ti* u0, const Ti* v0, const Ti* w0,
-                            To* u1, To* v1, To* w1, const uint8_t* flags, float dt,
-                            cudaStream_t st) {
-    if (g.nx < 2 || g.ny < 2 || g.nz < 2) return;
-    k_advect_velocity<<<grid3(g.nx - 1, g.ny - 1, (g.nz - 1 + ADV_ZC - 1) / ADV_ZC), dim3(BX, BY), 0, st>>>(
-        g, u0, v0, w0, u1, v1, w1, flags, dt, g.nz - 1);
-}
-
 template <typename T, typename Tv>
 void launch_advect_density(const Grid& g, const T* r0, T* r1, const Tv* u1,
                            const Tv* v1, const Tv* w1, const uint8_t* flags, float dt,
@@ -396,11 +374,6 @@ template void launch_forcing<__nv_bfloat16, __nv_bfloat16>(const Grid&, __nv_bfl
 template void launch_forcing<__nv_bfloat16, float>(const Grid&, __nv_bfloat16*, __nv_bfloat16*, __nv_bfloat16*,
                                                    const float*, const uint8_t*, float, float, float, float, int,
                                                    cudaStream_t, bool);
-template void launch_advect_velocity<float, float>(const Grid&, const float*, const float*, const float*,
-                                                   float*, float*, float*, const uint8_t*, float, cudaStream_t);
-template void launch_advect_velocity<float, __nv_bfloat16>(const Grid&, const float*, const float*,
-                                                           const float*, __nv_bfloat16*, __nv_bfloat16*,
-                                                           __nv_bfloat16*, const uint8_t*, float, cudaStream_t);
 template void launch_advect_density<float, float>(const Grid&, const float*, float*, const float*,
                                                   const float*, const float*, const uint8_t*, float,
                                                   cudaStream_t);

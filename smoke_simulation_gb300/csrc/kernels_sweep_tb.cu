@@ -730,12 +730,17 @@ __global__ void k_group_loop_next(const StepStatus* status, int* counter, int st
 
 namespace tb {
 bool encode_3d(CUtensorMap* m, const void* base, bool is_u8, const Grid& g, int rows) {
+    return encode_3d_box(m, base, is_u8, g, is_u8 ? BOX_U8 : BOX_F, rows);
+}
+
+bool encode_3d_box(CUtensorMap* m, const void* base, bool is_u8, const Grid& g, int box_w, int rows) {
     EncodeTiledFn fn = encode_fn();
     if (!fn || base == nullptr || (reinterpret_cast<uintptr_t>(base) & 15u) != 0) return false;
     const size_t es = is_u8 ? 1 : 4;
+    if (box_w <= 0 || box_w > 256 || (box_w * es) % 16 != 0) return false;
     cuuint64_t dims[3] = {(cuuint64_t)g.X, (cuuint64_t)(g.ny + 1), (cuuint64_t)(g.nz + 1)};
     cuuint64_t strides[2] = {(cuuint64_t)g.X * es, (cuuint64_t)g.XY * es};
-    cuuint32_t box[3] = {(cuuint32_t)(is_u8 ? BOX_U8 : BOX_F), (cuuint32_t)rows, 1u};
+    cuuint32_t box[3] = {(cuuint32_t)box_w, (cuuint32_t)rows, 1u};
     cuuint32_t estr[3] = {1u, 1u, 1u};
     CUresult r = fn(m, is_u8 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3,
                     const_cast<void*>(base), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,

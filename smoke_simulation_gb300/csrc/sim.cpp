@@ -139,7 +139,18 @@ int smk_sim::alloc() {
     if (!bf16) {
         vmaps = create_vsweep_maps(g, u, v, w, P, P2, b, flags);
         if (!vmaps) return fail(SMK_ERR_CUDA, "could not encode the TMA tensor maps of the velocity sweep kernel");
+        const float* au[2] = {u[0], u[1]};
+        const float* av[2] = {v[0], v[1]};
+        const float* aw[2] = {w[0], w[1]};
+        amaps = create_advect_maps(g, au, av, aw, 2);
+    } else {
+        // the BF16 forms advect from the FP32 copy of the projected faces
+        const float* au[1] = {proj[0]};
+        const float* av[1] = {proj[1]};
+        const float* aw[1] = {proj[2]};
+        amaps = create_advect_maps(g, au, av, aw, 1);
     }
+    if (!amaps) return fail(SMK_ERR_CUDA, "could not encode the TMA tensor maps of the velocity advection");
     status_groups = 4096;
     SMK_CUDA(cudaMalloc((void**)&status, sizeof(StepStatus) + sizeof(unsigned) * status_groups));
     SMK_CUDA(cudaMemset(status, 0, sizeof(StepStatus) + sizeof(unsigned) * status_groups));
@@ -166,6 +177,7 @@ void smk_sim::release() {
     if (render_scratch) cudaFree(render_scratch);
     if (maps) destroy_sweep_maps(maps);
     if (vmaps) destroy_vsweep_maps(vmaps);
+    if (amaps) destroy_advect_maps(amaps);
     if (s) cudaFree(s);
     if (flags) cudaFree(flags);
     if (status) cudaFree(status);
@@ -451,7 +463,9 @@ int smk_sim::enqueue(float dt, cudaStream_t st) {
 
     // a: advection (:805-810)
     if (bf16) {
-        launch_advect_velocity(g, pu, pv, pw, bf(u[past]), bf(v[past]), bf(w[past]), flags, dt, st);
+        if (launch_advect_velocity_tile(amaps, 0, g, pu, pv, pw, bf(u[past]), bf(v[past]), bf(w[past]), flags, dt,
+                                        kerr, st) != 0)
+            return fail(SMK_ERR_CUDA, "velocity advection launch failed");
         if (rho_bf16)
             launch_advect_density(g, (const __nv_bfloat16*)bf(rho[now]), bf(rho[past]),
                                   (const __nv_bfloat16*)bf(u[past]), (const __nv_bfloat16*)bf(v[past]),
@@ -461,7 +475,9 @@ int smk_sim::enqueue(float dt, cudaStream_t st) {
                                   (const __nv_bfloat16*)bf(v[past]), (const __nv_bfloat16*)bf(w[past]),
                                   flags, dt, st);
     } else {
-        launch_advect_velocity(g, pu, pv, pw, u[past], v[past], w[past], flags, dt, st);
+        if (launch_advect_velocity_tile(amaps, now, g, pu, pv, pw, u[past], v[past], w[past], flags, dt, kerr, st) !=
+            0)
+            return fail(SMK_ERR_CUDA, "velocity advection launch failed");
         launch_advect_density(g, (const float*)rho[now], rho[past], (const float*)u[past],
                               (const float*)v[past], (const float*)w[past], flags, dt, st);
     }

@@ -9,7 +9,7 @@
 #include "../../include/smoke_gb300.h"
 #include "common.cuh"
 
-namespace smk { struct SweepMaps; struct VSweepMaps; }
+namespace smk { struct SweepMaps; struct VSweepMaps; struct AdvectMaps; }
 
 // Records `msg` as smk_last_error's text and returns `code` (sim.cpp).
 int smk_fail(int code, const std::string& msg);
@@ -72,6 +72,7 @@ struct smk_sim {
     void* render_scratch = nullptr;               // device: the renderer's light buffer per plane
     size_t render_scratch_bytes = 0;
     smk::SweepMaps* maps = nullptr;  // TMA tensor maps of P, P2, b, flags
+    smk::AdvectMaps* amaps = nullptr;  // TMA tensor maps of the velocity advection's inputs
     smk::VSweepMaps* vmaps = nullptr;  // TMA tensor maps of u, v, w (both buffers), P, P2, b, flags
     uint8_t* s = nullptr;
     uint8_t* flags = nullptr;

@@ -96,6 +96,8 @@ __host__ __device__ inline void sweep_window(int n, int W, int T, int k, int& st
 // floats or bytes), boxes of BOX_F (BOX_U8) x rows x 1; false when the base is null or not
 // 16-byte aligned or the driver refuses the map.  Defined in kernels_sweep_tb.cu.
 bool encode_3d(CUtensorMap* m, const void* base, bool is_u8, const Grid& g, int rows);
+// The same with a box box_w elements wide (box_w x element size a multiple of 16 bytes).
+bool encode_3d_box(CUtensorMap* m, const void* base, bool is_u8, const Grid& g, int box_w, int rows);
 
 }  // namespace tb
 }  // namespace smk
