@@ -88,6 +88,8 @@ typedef struct smk_stats {
     int step_index;     /* steps taken since creation */
     int refine_rounds;  /* correction rounds applied by the last step (refine > 0) */
     float div64_max;    /* max |div u| of the last FP64 measurement (refine > 0), else -1 */
+    int subtract_fused; /* 1: the last step's gradient subtract ran inside its last sweep launch
+                           (PRESSURE, FP32, blocked sweeps), 0: as a pass of its own */
 } smk_stats;
 
 /* Host copy of the full state in the reference's layout (both ping-pong buffers). */
@@ -209,6 +211,15 @@ int smk_set_graph_loops(smk_sim* sim, int enable);
  * boundaries, as every simulation's own arrays do) or one cell per thread.  Results are
  * identical; batches follow each member's setting.  No counterpart in the reference. */
 int smk_set_vector_stages(smk_sim* sim, int enable);
+/* PRESSURE scheme, FP32 state, blocked sweeps: apply the gradient subtract inside the sweep
+ * launch that ends the solve (the launch that applies the last colour pass moves every face by
+ * the final pressure gradient) instead of as a pass of its own after the solve.  Where only the
+ * device knows which tolerance group ends the solve, each group's last launch is issued as a
+ * pair, of which exactly one does the work.  Bit-identical to the separate pass; default off:
+ * at 256^3 the fused launch measures 465 us against 117 us for the plain launch plus 81 us for
+ * the separate pass (smk_stats.subtract_fused reports which way a step went).  Reference: the
+ * face updates inside every colour pass of divergence(), smokeSimulation.cu:384-391. */
+int smk_set_fused_subtract(smk_sim* sim, int enable);
 /* Time the blocked sweep kernel's shapes (depth, patch rows) and z-chunk sizes on this simulation's buffers and
  * keep the fastest (cached per grid shape and device for the process).  With the REFERENCE
  * projection it times the velocity sweep instead (one colour pass per launch, or the blocked

@@ -53,7 +53,7 @@ class Params(C.Structure):
 class Stats(C.Structure):
     _fields_ = [("sweeps", C.c_int), ("converged", C.c_int), ("resid_max", C.c_float),
                 ("div_max", C.c_float), ("step_index", C.c_int), ("refine_rounds", C.c_int),
-                ("div64_max", C.c_float)]
+                ("div64_max", C.c_float), ("subtract_fused", C.c_int)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -124,6 +124,7 @@ def lib() -> C.CDLL:
         "smk_set_graphs": (i, [vp, i]),
         "smk_set_graph_loops": (i, [vp, i]),
         "smk_set_vector_stages": (i, [vp, i]),
+        "smk_set_fused_subtract": (i, [vp, i]),
         "smk_default_render_params": (None, [C.c_void_p]),
         "smk_render": (i, [vp, C.c_void_p, vp, vp, vp]),
         "smk_batch_create": (i, [i, C.POINTER(vp), C.POINTER(vp)]),
@@ -338,6 +339,11 @@ class Simulation:
         """Forcing, rhs and subtract / BF16 projection with four x per thread (default) or one
         cell per thread; results are identical."""
         _check(lib().smk_set_vector_stages(self.h, 1 if enable else 0))
+
+    def set_fused_subtract(self, enable: bool):
+        """PRESSURE, FP32, blocked sweeps: the gradient subtract inside the solve's last sweep
+        launch (default off); results are identical."""
+        _check(lib().smk_set_fused_subtract(self.h, 1 if enable else 0))
 
     def set_sweep_kernel(self, depth: int, zchunk: int = 32, rows: int = 2):
         """Blocked sweep kernel shape: `depth` colour passes per launch, z-chunks of `zchunk`

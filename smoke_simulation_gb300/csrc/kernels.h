@@ -49,9 +49,11 @@ void launch_sweep(const Grid& g, float* P, const float* b, const uint8_t* flags,
                   const float* wacc7, const StepStatus* status, cudaStream_t st);
 void launch_resid_check(const Grid& g, const float* P, const float* b, const uint8_t* flags,
                         StepStatus* status, int group, float tol, cudaStream_t st);
+// skip (device, may be NULL): when *skip is set at run time the launch does nothing (a blocked
+// launch already applied the subtract, SweepFuse).
 void launch_gradient_subtract(const Grid& g, float* u, float* v, float* w, const float* P0,
                               const float* P1, const int* pcur, const uint8_t* flags,
-                              cudaStream_t st, bool vec = true);
+                              cudaStream_t st, bool vec = true, const int* skip = nullptr);
 // Temporally blocked sweeps: nhalf <= T colour passes in one pass over HBM, P_in -> P_out;
 // `check` launches also record the residual of the input state for tolerance group `group`.
 // The pressure buffers are read through TMA tensor maps built once per simulation.
@@ -97,12 +99,35 @@ struct SweepMaps;
 SweepMaps* create_sweep_maps(const Grid& g, const float* Pa, const float* Pb, const float* b,
                              const uint8_t* flags);
 void destroy_sweep_maps(SweepMaps* m);
+// The gradient subtract fused into the last launch of a solve: u, v, w (FP32, the grid's
+// layout) move by the final pressure's gradient inside the launch that applies the last colour
+// pass, and *sub_done is set so that the separate subtract (launch_gradient_subtract with
+// skip = sub_done) does nothing.  mode 1: the launch ends the solve (fixed sweep count, or the
+// last group under the sweep cap).  Where only the device knows (the launch ends the solve when
+// the residual its tolerance group started from was within tol: the tolerance rule then stops
+// before the next group; or its group is the last one, last_group, under the sweep cap), the
+// launch is issued twice, mode 3 then mode 2: the mode-3 launch (plain kernel) works unless the
+// launch ends the solve, the mode-2 launch (fused kernel) only when it does, so the fused
+// kernel, which needs more registers, runs once per solve.
+struct SweepFuse {
+    float* u;
+    float* v;
+    float* w;
+    int* sub_done;
+    int mode;
+    int last_group;
+};
+// Whether launch_sweep_tb can fuse the subtract into a launch of this shape (full launches of
+// the plain 2-row and 4-row kernels, not check launches).
+bool sweep_tb_fusable(int T, int rows, int nhalf, int check);
+
 // group_base (device, may be NULL): the launch's group index is group + *group_base (a graph's
-// device-side group loop).
+// device-side group loop).  fuse (may be NULL, or mode 0): see SweepFuse; ignored where
+// sweep_tb_fusable is false.
 int launch_sweep_tb(const SweepMaps* m, const Grid& g, bool in_is_a, float* Pout, int T, int rows,
                     int nhalf, int colour0, int zchunk, const float* wacc7, StepStatus* status,
                     int check, int group, float tol, int* pcur, int out_idx, int* kerr,
-                    const int* group_base, cudaStream_t st);
+                    const int* group_base, cudaStream_t st, const SweepFuse* fuse = nullptr);
 // Grouped blocked solve over many grids (depth 6, 2-row patches): one record per grid (its
 // tensor maps, buffers and tolerance), tiles of all grids in one launch.
 size_t group_tb_record_bytes();

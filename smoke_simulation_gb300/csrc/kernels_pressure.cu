@@ -51,7 +51,9 @@ __global__ void __launch_bounds__(256) k_gradient_subtract_x4(Grid g, float* __r
                                                               float* __restrict__ w, const float* __restrict__ P0,
                                                               const float* __restrict__ P1,
                                                               const int* __restrict__ pcur,
-                                                              const uint8_t* __restrict__ flags) {
+                                                              const uint8_t* __restrict__ flags,
+                                                              const int* __restrict__ skip) {
+    if (skip != nullptr && *skip) return;
     const float* P = (pcur != nullptr && *pcur == 1) ? P1 : P0;
     body_gradient_subtract_x4(g, u, v, w, P, flags, 4 * ((int)blockIdx.x * 32 + (int)threadIdx.x),
                               1 + (int)blockIdx.y * 8 + (int)threadIdx.y, 1 + (int)blockIdx.z);
@@ -60,7 +62,8 @@ __global__ void __launch_bounds__(256) k_gradient_subtract_x4(Grid g, float* __r
 __global__ void k_gradient_subtract(Grid g, float* __restrict__ u, float* __restrict__ v,
                                     float* __restrict__ w, const float* __restrict__ P0,
                                     const float* __restrict__ P1, const int* __restrict__ pcur,
-                                    const uint8_t* __restrict__ flags) {
+                                    const uint8_t* __restrict__ flags, const int* __restrict__ skip) {
+    if (skip != nullptr && *skip) return;
     body_gradient_subtract(g, u, v, w, P0, P1, pcur, flags, blockIdx);
 }
 
@@ -153,16 +156,16 @@ void launch_resid_check(const Grid& g, const float* P, const float* b, const uin
 
 void launch_gradient_subtract(const Grid& g, float* u, float* v, float* w, const float* P0,
                               const float* P1, const int* pcur, const uint8_t* flags,
-                              cudaStream_t st, bool vec) {
+                              cudaStream_t st, bool vec, const int* skip) {
     if (g.nx < 2 || g.ny < 2 || g.nz < 2) return;
     if (!vec || !vec4_layout(g, {u, v, w, P0, P1}, flags)) {
         k_gradient_subtract<<<grid3(g.nx - 1, g.ny - 1, g.nz - 1), dim3(BX, BY), 0, st>>>(
-            g, u, v, w, P0, P1, pcur, flags);
+            g, u, v, w, P0, P1, pcur, flags, skip);
         return;
     }
     const int groups = (g.nx + 3) / 4;  // x in [1, nx): groups of 4 from x = 0
     k_gradient_subtract_x4<<<dim3((unsigned)((groups + 31) / 32), (unsigned)((g.ny - 1 + 7) / 8), (unsigned)(g.nz - 1)),
-                             dim3(32, 8), 0, st>>>(g, u, v, w, P0, P1, pcur, flags);
+                             dim3(32, 8), 0, st>>>(g, u, v, w, P0, P1, pcur, flags, skip);
 }
 
 }  // namespace smk

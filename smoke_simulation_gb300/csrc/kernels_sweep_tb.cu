@@ -147,6 +147,24 @@ __device__ __forceinline__ void st_cluster(uint32_t addr, float v) {
     asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(addr), "f"(v) : "memory");
 }
 
+// The faces next to cell (x, y, z) that the gradient subtract moves, from the cell's flag byte f
+// (body_gradient_subtract's rule: a face moves when its two cells are fluid and it lies in the
+// range [1, nx) x [1, ny) x [1, nz) with its other two coordinates in [1, n - 2]), as bits:
+// 0 the lower x face (index i), 1 the upper x face (i + 1), 2 lower y (i), 3 upper y (i + X),
+// 4 lower z (i), 5 upper z (i + XY).  x >= 0.
+__device__ __forceinline__ unsigned fused_face_mask(const Grid& g, unsigned f, int x, int y, int z) {
+    if (!(f & F_SELF)) return 0u;
+    const bool inx = x >= 1 && x <= g.nx - 2, iny = y >= 1 && y <= g.ny - 2, inz = z >= 1 && z <= g.nz - 2;
+    unsigned m = 0u;
+    if ((f & F_XM) && x >= 1 && x <= g.nx - 1 && iny && inz) m |= 1u;
+    if ((f & F_XP) && x + 1 <= g.nx - 1 && iny && inz) m |= 2u;
+    if ((f & F_YM) && y >= 1 && y <= g.ny - 1 && inx && inz) m |= 4u;
+    if ((f & F_YP) && y + 1 <= g.ny - 1 && inx && inz) m |= 8u;
+    if ((f & F_ZM) && z >= 1 && z <= g.nz - 1 && inx && iny) m |= 16u;
+    if ((f & F_ZP) && z + 1 <= g.nz - 1 && inx && iny) m |= 32u;
+    return m;
+}
+
 // One tile (bx, by, bz) of a blocked launch: the CTA's whole job.  `group` is absolute.
 // GLOBAL_MAPS: the tensor maps are in global memory (grouped launches), not kernel parameters.
 // YCLUSTER: runs of `ycl_n` CTAs along y (blockIdx.y / ycl_n = the run, blockIdx.y % ycl_n = the
@@ -157,12 +175,22 @@ __device__ __forceinline__ void st_cluster(uint32_t addr, float v) {
 // published planes), and the per-iteration barrier is a cluster barrier.
 // FULL: the launch applies all T colour passes (nhalf == T), so the stages need no test; CHK: 0
 // or 1 = the launch is (not) a tolerance-check launch, fixed at compile time; -1 = `check` decides.
-template <int T, int PY, bool GLOBAL_MAPS = false, bool YCLUSTER = false, bool FULL = false, int CHK = -1>
+// FUSE (full non-check launches of the plain form): when fz says this launch ends the solve, the
+// gradient subtract is applied inside it.  Pass T changes one colour only, so every face has
+// exactly one cell of that colour next to it; the thread owning that cell moves the face with
+// the operands of the cell's last update (its new value and its six neighbours, which pass T
+// leaves at their final values), one iteration after the pass, the face loads issued before
+// the iteration's wait so that their latency overlaps it.  The face values are those of
+// body_gradient_subtract on the final pressure, bit for bit.
+template <int T, int PY, bool GLOBAL_MAPS = false, bool YCLUSTER = false, bool FULL = false, int CHK = -1,
+          bool FUSE = false>
 __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, float* __restrict__ Pout,
                                            int nhalf, int colour0, int zchunk, const WAcc8& wa,
                                            StepStatus* status, int check, int group, float tol,
                                            int* __restrict__ pcur, int out_idx, int* __restrict__ kerr,
-                                           int bx, int by, int bz, int ycl_n = 1, int ycl_hy = 0) {
+                                           int bx, int by, int bz, int ycl_n = 1, int ycl_hy = 0,
+                                           SweepFuse fz = SweepFuse{}) {
+    static_assert(!FUSE || (FULL && CHK == 0 && !YCLUSTER && !GLOBAL_MAPS), "fused subtract: plain full launches");
     const bool chk = CHK < 0 ? check != 0 : CHK == 1;
     using G = TBGeom<PY>;
     constexpr int TY = G::TY, ROWS = G::ROWS, PROW = G::PROW, STAGE_BYTES = G::STAGE_BYTES,
@@ -178,12 +206,21 @@ __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, fl
     // published planes, per buffer (2): the residual plane as 4 column planes (row 0 A, row 0 B,
     // last row A, last row B), then for stages 1..T a row-0 and a last-row plane; each
     // [TY+2][32] floats
-    constexpr int NPUB = 4 + 2 * T;
+    // the fused form has no check launch, so no residual planes: stage s publishes planes
+    // PR - 2 + 2s (row 0) and PR - 1 + 2s (last row)
+    constexpr int PR = FUSE ? 0 : 4;
+    constexpr int NPUB = PR + 2 * T;
+    // copies of the coefficient table: one per lane (the fused form: one per half-warp lane, to
+    // make room for its staged faces; two lanes then share a copy)
+    constexpr int CL = FUSE ? 16 : TB_TX;
     float* pub = reinterpret_cast<float*>(stages + TB_S * STAGE_BYTES);
     // the (-acc, omega/acc) table, one copy per lane: entry e of lane l at [e][l], so a warp's
     // lookup touches each bank pair once whatever the 32 flag bytes are (one shared copy made
     // a lookup near scattered solids take ~3.5 wavefronts instead of 2)
     float2* coef_all = reinterpret_cast<float2*>(pub + 2 * NPUB * PROW);
+    // FUSE: the faces a thread moves, staged by cp.async two planes ahead, in two slots
+    // ([plane & 1][row * 6 + face][thread])
+    float* fbuf = reinterpret_cast<float*>(coef_all + 128 * CL);
     __shared__ __align__(8) uint64_t mbar[TB_S];
     __shared__ float2 coef_one[128];  // the table once, replicated into coef_all
     __shared__ int tma_bad;           // YCLUSTER: a TMA stage of this CTA never completed
@@ -199,16 +236,25 @@ __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, fl
             return;
         }
     }
+    // modes 2 and 3 are the two launches of a pair of which exactly one works: the fused one when
+    // this launch ends the solve (the residual its group started from, recorded by the group's
+    // check launch, was within tol, or the group is the last under the sweep cap), the plain one
+    // otherwise
+    if ((fz.mode == 2 || fz.mode == 3) && status != nullptr &&
+        (group == fz.last_group || __uint_as_float(status->rmax_bits[group]) <= tol) != (fz.mode == 2))
+        return;
+    const bool fuse = FUSE && (fz.mode == 1 || fz.mode == 2);
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int tid = ty * TB_TX + tx;
     const bool leader = tid == 0;
+    if (fuse && first_tile && leader) *fz.sub_done = 1;
     if (tid < 128) {  // one read of omega/acc per entry (global memory in the grouped form)
         const int acc = __popc(tid & 0x3f);
         coef_one[tid] = make_float2(-(float)acc, (tid & 0x40) ? wa.w[acc] : 0.0f);
     }
     __syncthreads();
-    for (int i = tid; i < 128 * TB_TX; i += G::THREADS) coef_all[i] = coef_one[i / TB_TX];
-    const float2* coef = coef_all + tx;  // this lane's copy: entry e at coef[e * TB_TX]
+    for (int i = tid; i < 128 * CL; i += G::THREADS) coef_all[i] = coef_one[i / CL];
+    const float2* coef = coef_all + tx % CL;  // this lane's copy: entry e at coef[e * CL]
     // zero the padding rows of every published plane (never written afterwards, except by the
     // cluster neighbours in the YCLUSTER form)
     if (YCLUSTER && tid == 0) tma_bad = 0;
@@ -245,7 +291,9 @@ __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, fl
     // planes below 0 are never projectable: a chunk near z = 0 may start at plane 0 (the ring's
     // zero-initialised slots stand for the planes below, as the zero-filled loads do), which it
     // does where that saves a pass of the unrolled loop
-    const int qend = zb + T;
+    // a fused launch runs one iteration more: the subtract of a plane comes one iteration after it
+    // leaves the pipeline
+    const int qend = zb + T + (fuse ? 1 : 0);
     const int qbeg = (za - T < 0 && (qend + R) / R < (qend - (za - T) + R) / R) ? 0 : za - T;
     const int nouter = (qend - qbeg + R) / R;
     const int qfinal = qbeg + nouter * R - 1;  // last iteration executed
@@ -296,6 +344,19 @@ __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, fl
             const int q = base + k;
             const int st = k % TB_S;
             const uint32_t phase = (uint32_t)((k / TB_S) & 1);
+            // ---- FUSE: plane zs = q-2-T left the pipeline last iteration; its faces move below.
+            // The y-neighbours pass T read at the patch's edges (row y0-1 in row 0's column, row
+            // y0+PY in the last row's) come from last iteration's published planes, read before
+            // this iteration's barrier (nobody writes that buffer again before it)
+            const int zs = q - 2 - T;
+            const bool sub = fuse && zs >= za && zs < zb;
+            const bool sAp = ((k + R - 1 + p_par) & 1) == 0;  // last iteration's stage pattern
+            float sv_above = 0.0f, sv_below = 0.0f;
+            if (FUSE && sub) {
+                const float* pq = pub + (par ^ 1) * NPUB * PROW;
+                sv_above = pq[(PR - 1 + 2 * T) * PROW + me0 - TB_TX];
+                sv_below = pq[(PR - 2 + 2 * T) * PROW + me0 + TB_TX];
+            }
             // ---- plane q: wait for its TMA stage, take this thread's patch into slot k
             const bool ok = mbar_wait(smem_u32(&mbar[st]), phase);
             {
@@ -344,10 +405,10 @@ __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, fl
             // v0: row 0's value, read from above; vl: the last row's, read from below (the column
             // is chosen by branching once per iteration, not by a select per value)
             auto publish = [&](int s, float v0, float vl) {
-                pb[(2 + 2 * s) * PROW + me0] = v0;
-                pb[(3 + 2 * s) * PROW + me0] = vl;
-                if (push_up) st_cluster(up_base + pofs + (uint32_t)(2 + 2 * s) * PROW * 4u, v0);
-                if (push_dn) st_cluster(dn_base + pofs + (uint32_t)(3 + 2 * s) * PROW * 4u, vl);
+                pb[(PR - 2 + 2 * s) * PROW + me0] = v0;
+                pb[(PR - 1 + 2 * s) * PROW + me0] = vl;
+                if (push_up) st_cluster(up_base + pofs + (uint32_t)(PR - 2 + 2 * s) * PROW * 4u, v0);
+                if (push_dn) st_cluster(dn_base + pofs + (uint32_t)(PR - 1 + 2 * s) * PROW * 4u, vl);
             };
             if (sA) {
 #pragma unroll
@@ -378,12 +439,76 @@ __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, fl
                         mbar_wait(smem_u32(&mbar[d % TB_S]), (uint32_t)((d / TB_S) & 1));
                     }
                 }
+                if (FUSE && fuse) cp_async_wait_all();
                 __syncthreads();
                 return;
             }
             // every thread has read stage st: refill it with plane q + S
             if (leader && q + TB_S <= qfinal)
                 issue_plane<PY>(maps, stages + st * STAGE_BYTES, smem_u32(&mbar[st]), xf, xb, Y0, q + TB_S);
+
+            // ---- FUSE: move the faces of plane zs, then stage the faces of plane q-T (two
+            // iterations ahead; its last pass comes next iteration, with the opposite pattern).
+            // Plane zs's last-colour cells hold their final values (slot js), their neighbours in
+            // planes zs-1, zs, zs+1 the values pass T read (other colour: final, and exact one
+            // cell beyond the owned region); the x-neighbours come from the patch or the next
+            // lane, the y-neighbours at the patch's edge from pass T's reads (sv_above, sv_below)
+            if (FUSE && fuse) {
+                if (sub) {
+                    cp_async_wait_one();  // plane zs's copies (two groups back) have landed
+                    const int js = (k - 2 - T + 2 * R) % R, jm = (k - 3 - T + 2 * R) % R,
+                              jp = (k - 1 - T + 2 * R) % R;
+                    const float* fs = fbuf + (zs & 1) * (6 * PY * G::THREADS) + tid;
+#pragma unroll
+                    for (int r = 0; r < PY; ++r) {
+                        const int cb = (r & 1) ^ (sAp ? 0 : 1);
+                        // the x-neighbour in the next lane: B of the lane to the left (column A), A
+                        // of the lane to the right (column B); every lane takes part
+                        const float nx = cb ? __shfl_down_sync(0xffffffffu, pp[r][js].x, 1)
+                                            : __shfl_up_sync(0xffffffffu, pp[r][js].y, 1);
+                        const unsigned f = (ff[r / 2][js] >> (8 * (2 * (r & 1) + cb))) & 0xffu;
+                        const unsigned m = in[r] ? fused_face_mask(g, f, x0 + cb, y0 + r, zs) : 0u;
+                        if (m == 0u) continue;
+                        const int ru = r > 0 ? r - 1 : 0, rd = r < L ? r + 1 : L;
+                        const float pn = cb ? pp[r][js].y : pp[r][js].x;
+                        const float xm = cb ? pp[r][js].x : nx;
+                        const float xp = cb ? nx : pp[r][js].y;
+                        const float ym = r == 0 ? sv_above : (cb ? pp[ru][js].y : pp[ru][js].x);
+                        const float yp = r == L ? sv_below : (cb ? pp[rd][js].y : pp[rd][js].x);
+                        const float zm = cb ? pp[r][jm].y : pp[r][jm].x;
+                        const float zp = cb ? pp[r][jp].y : pp[r][jp].x;
+                        const int i = off0 + cb + r * g.X + g.XY * zs;
+                        const float* fr = fs + r * 6 * G::THREADS;
+                        if (m & 1u) fz.u[i] = fr[0] - (pn - xm);
+                        if (m & 2u) fz.u[i + 1] = fr[G::THREADS] - (xp - pn);
+                        if (m & 4u) fz.v[i] = fr[2 * G::THREADS] - (pn - ym);
+                        if (m & 8u) fz.v[i + g.X] = fr[3 * G::THREADS] - (yp - pn);
+                        if (m & 16u) fz.w[i] = fr[4 * G::THREADS] - (pn - zm);
+                        if (m & 32u) fz.w[i + g.XY] = fr[5 * G::THREADS] - (zp - pn);
+                    }
+                }
+                const int zl = q - T;
+                if (zl >= za && zl < zb) {
+                    const int jl = (k - T + 2 * R) % R;
+                    const bool sAn = !((((k + p_par) & 1) == 0));  // next iteration's stage pattern
+                    const uint32_t d0 = smem_u32(fbuf + (zl & 1) * (6 * PY * G::THREADS) + tid);
+#pragma unroll
+                    for (int r = 0; r < PY; ++r) {
+                        const int cb = (r & 1) ^ (sAn ? 0 : 1);
+                        const unsigned f = (ff[r / 2][jl] >> (8 * (2 * (r & 1) + cb))) & 0xffu;
+                        const unsigned m = in[r] ? fused_face_mask(g, f, x0 + cb, y0 + r, zl) : 0u;
+                        const int i = off0 + cb + r * g.X + g.XY * zl;
+                        const uint32_t d = d0 + 4u * (uint32_t)(r * 6 * G::THREADS);
+                        if (m & 1u) cp_async4(d, fz.u + i);
+                        if (m & 2u) cp_async4(d + 4u * G::THREADS, fz.u + i + 1);
+                        if (m & 4u) cp_async4(d + 8u * G::THREADS, fz.v + i);
+                        if (m & 8u) cp_async4(d + 12u * G::THREADS, fz.v + i + g.X);
+                        if (m & 16u) cp_async4(d + 16u * G::THREADS, fz.w + i);
+                        if (m & 32u) cp_async4(d + 20u * G::THREADS, fz.w + i + g.XY);
+                    }
+                }
+                cp_async_commit();  // one group per iteration, empty or not
+            }
 
             // ---- stage 0: residual of plane q-1 at time 0
             if (chk) {
@@ -406,9 +531,9 @@ __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, fl
                         const float2 yp = r == L ? dn : pp[r + 1][j];
                         const unsigned f = ff[r / 2][j];
                         const unsigned ia = fidx(f, 2 * (r & 1)), ib = fidx(f, 2 * (r & 1) + 1);
-                        rmax = max(rmax, resid_bits(pp[r][j].x, bb[r][j].x, coef[ia * TB_TX], ia & 0x40u, lB[r],
+                        rmax = max(rmax, resid_bits(pp[r][j].x, bb[r][j].x, coef[ia * CL], ia & 0x40u, lB[r],
                                                     pp[r][j].y, ym.x, yp.x, pp[r][jd].x, pp[r][ju].x));
-                        rmax = max(rmax, resid_bits(pp[r][j].y, bb[r][j].y, coef[ib * TB_TX], ib & 0x40u, pp[r][j].x,
+                        rmax = max(rmax, resid_bits(pp[r][j].y, bb[r][j].y, coef[ib * CL], ib & 0x40u, pp[r][j].x,
                                                     rA[r], ym.y, yp.y, pp[r][jd].y, pp[r][ju].y));
                     }
                 }
@@ -421,8 +546,8 @@ __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, fl
                     const int j = (k - 1 - t + 2 * R) % R;
                     const int ju = (k - t + 2 * R) % R;
                     const int jd = (k - 2 - t + 2 * R) % R;
-                    const float* r0 = pb + (2 + 2 * t) * PROW;  // row-0 values (the thread below's)
-                    const float* rl = pb + (3 + 2 * t) * PROW;  // last-row values (the thread above's)
+                    const float* r0 = pb + (PR - 2 + 2 * t) * PROW;  // row-0 values (the thread below's)
+                    const float* rl = pb + (PR - 1 + 2 * t) * PROW;  // last-row values (the thread above's)
                     const float above = rl[me0 - TB_TX];       // row y0-1, the column row 0 updates
                     const float below = r0[me0 + TB_TX];       // row y0+PY, the column row L updates
                     float nv[PY];
@@ -435,14 +560,14 @@ __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, fl
                                 const float ym = r == 0 ? above : pp[r - 1][j].x;
                                 const float yp = pp[r + 1][j].x;
                                 const unsigned ia = fidx(f, 0);
-                                nv[r] = relax(pp[r][j].x, bb[r][j].x, coef[ia * TB_TX], ia & 0x40u, lB, pp[r][j].y,
+                                nv[r] = relax(pp[r][j].x, bb[r][j].x, coef[ia * CL], ia & 0x40u, lB, pp[r][j].y,
                                               ym, yp, pp[r][jd].x, pp[r][ju].x);
                             } else {              // column B
                                 const float rA = __shfl_down_sync(0xffffffffu, pp[r][j].x, 1);
                                 const float ym = pp[r - 1][j].y;
                                 const float yp = r == L ? below : pp[r + 1 < PY ? r + 1 : r][j].y;
                                 const unsigned ib = fidx(f, 3);
-                                nv[r] = relax(pp[r][j].y, bb[r][j].y, coef[ib * TB_TX], ib & 0x40u, pp[r][j].x, rA,
+                                nv[r] = relax(pp[r][j].y, bb[r][j].y, coef[ib * CL], ib & 0x40u, pp[r][j].x, rA,
                                               ym, yp, pp[r][jd].y, pp[r][ju].y);
                             }
                         }
@@ -460,14 +585,14 @@ __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, fl
                                 const float ym = r == 0 ? above : pp[r - 1][j].y;
                                 const float yp = pp[r + 1][j].y;
                                 const unsigned ib = fidx(f, 1);
-                                nv[r] = relax(pp[r][j].y, bb[r][j].y, coef[ib * TB_TX], ib & 0x40u, pp[r][j].x, rA,
+                                nv[r] = relax(pp[r][j].y, bb[r][j].y, coef[ib * CL], ib & 0x40u, pp[r][j].x, rA,
                                               ym, yp, pp[r][jd].y, pp[r][ju].y);
                             } else {              // column A
                                 const float lB = __shfl_up_sync(0xffffffffu, pp[r][j].y, 1);
                                 const float ym = pp[r - 1][j].x;
                                 const float yp = r == L ? below : pp[r + 1 < PY ? r + 1 : r][j].x;
                                 const unsigned ia = fidx(f, 2);
-                                nv[r] = relax(pp[r][j].x, bb[r][j].x, coef[ia * TB_TX], ia & 0x40u, lB, pp[r][j].y,
+                                nv[r] = relax(pp[r][j].x, bb[r][j].x, coef[ia * CL], ia & 0x40u, lB, pp[r][j].y,
                                               ym, yp, pp[r][jd].x, pp[r][ju].x);
                             }
                         }
@@ -502,6 +627,7 @@ __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, fl
             }
         }
     }
+    if (FUSE && fuse) cp_async_wait_all();  // no staged copy outlives the CTA
     if (chk) block_max_to(rmax, &status->rmax_bits[group]);
     if (YCLUSTER) cluster_sync_all();  // no CTA leaves while a neighbour may still address it
 }
@@ -511,12 +637,24 @@ __global__ void __launch_bounds__(TBGeom<PY>::THREADS, 1)
 k_sweep_tb(const __grid_constant__ TBMaps maps, Grid g, float* __restrict__ Pout, int nhalf,
            int colour0, int zchunk, const __grid_constant__ WAcc8 wa, StepStatus* status, int check, int group,
            float tol, int* __restrict__ pcur, int out_idx, int* __restrict__ kerr,
-           const int* __restrict__ group_base) {
+           const int* __restrict__ group_base, int pair_mode, int last_group) {
     // inside a graph's device-side group loop the group index is relative to the loop counter
     if (group_base != nullptr) group += *group_base;
     sweep_tile<T, PY, false, false, FULL, CHK>(maps, g, Pout, nhalf, colour0, zchunk, wa, status, check, group,
                                                tol, pcur, out_idx, kerr, (int)blockIdx.x, (int)blockIdx.y,
-                                               (int)blockIdx.z);
+                                               (int)blockIdx.z, 1, 0, SweepFuse{nullptr, nullptr, nullptr, nullptr, pair_mode, last_group});
+}
+
+// A full non-check launch that may end the solve: the gradient subtract fused (sweep_tile FUSE).
+template <int T, int PY>
+__global__ void __launch_bounds__(TBGeom<PY>::THREADS, 1)
+k_sweep_tb_fused(const __grid_constant__ TBMaps maps, Grid g, float* __restrict__ Pout, int colour0, int zchunk,
+                 const __grid_constant__ WAcc8 wa, StepStatus* status, int group, float tol, int* __restrict__ pcur,
+                 int out_idx, int* __restrict__ kerr, const int* __restrict__ group_base, SweepFuse fz) {
+    if (group_base != nullptr) group += *group_base;
+    sweep_tile<T, PY, false, false, true, 0, true>(maps, g, Pout, T, colour0, zchunk, wa, status, 0, group, tol, pcur,
+                                                   out_idx, kerr, (int)blockIdx.x, (int)blockIdx.y, (int)blockIdx.z,
+                                                   1, 0, fz);
 }
 
 // The y-cluster form (2-row patches): runs of ycl_n CTAs along y form clusters, with a halo of
@@ -625,20 +763,32 @@ constexpr size_t tb_smem_bytes() {
            sizeof(float2) * 128 * TB_TX;
 }
 
+// The fused-subtract form: no residual planes, 16 copies of the coefficient table, and the
+// staged faces (two planes of 6 floats per patch row and thread).
+template <int T, int PY>
+constexpr size_t tb_smem_bytes_fused() {
+    using G = TBGeom<PY>;
+    return 128 + (size_t)((T + 4) / 2) * G::STAGE_BYTES + sizeof(float) * 2 * (2 * T) * G::PROW +
+           sizeof(float2) * 128 * 16 + sizeof(float) * 2 * 6 * PY * G::THREADS;
+}
+
 template <int T, int PY>
 int configure_tb() {
     const int bytes = (int)tb_smem_bytes<T, PY>();
+    static_assert(tb_smem_bytes_fused<T, PY>() <= 227 * 1024, "shared memory of the fused form");
     const cudaFuncAttribute attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
     const bool ok = cudaFuncSetAttribute(k_sweep_tb<T, PY, false, -1>, attr, bytes) == cudaSuccess &&
                     cudaFuncSetAttribute(k_sweep_tb<T, PY, true, 0>, attr, bytes) == cudaSuccess &&
-                    cudaFuncSetAttribute(k_sweep_tb<T, PY, true, 1>, attr, bytes) == cudaSuccess;
+                    cudaFuncSetAttribute(k_sweep_tb<T, PY, true, 1>, attr, bytes) == cudaSuccess &&
+                    cudaFuncSetAttribute(k_sweep_tb_fused<T, PY>, attr, (int)tb_smem_bytes_fused<T, PY>()) ==
+                        cudaSuccess;
     return ok ? 0 : -1;
 }
 
 template <int T, int PY>
 int launch_tb(const TBMaps& maps, const Grid& g, float* Pout, int nhalf, int colour0, int zchunk,
               const float* wacc7, StepStatus* status, int check, int group, float tol, int* pcur,
-              int out_idx, int* kerr, const int* group_base, cudaStream_t st) {
+              int out_idx, int* kerr, const int* group_base, cudaStream_t st, const SweepFuse* fuse) {
     using G = TBGeom<PY>;
     const size_t smem = tb_smem_bytes<T, PY>();
     WAcc8 wa;
@@ -651,8 +801,16 @@ int launch_tb(const TBMaps& maps, const Grid& g, float* Pout, int nhalf, int col
 #define SMK_TB_LAUNCH(FULL, CHK)                                                                             \
     k_sweep_tb<T, PY, FULL, CHK><<<grid, dim3(TB_TX, G::TY), smem, st>>>(maps, g, Pout, nhalf, colour0, zchunk, \
                                                                         wa, status, check, group, tol, pcur,  \
-                                                                        out_idx, kerr, group_base)
+                                                                        out_idx, kerr, group_base, 0, -1)
+    const int mode = fuse != nullptr ? fuse->mode : 0;
     if (nhalf == T && check) SMK_TB_LAUNCH(true, 1);
+    else if (nhalf == T && (mode == 1 || mode == 2))
+        k_sweep_tb_fused<T, PY><<<grid, dim3(TB_TX, G::TY), tb_smem_bytes_fused<T, PY>(), st>>>(
+            maps, g, Pout, colour0, zchunk, wa, status, group, tol, pcur, out_idx, kerr, group_base, *fuse);
+    else if (nhalf == T && mode == 3)
+        k_sweep_tb<T, PY, true, 0><<<grid, dim3(TB_TX, G::TY), smem, st>>>(
+            maps, g, Pout, nhalf, colour0, zchunk, wa, status, check, group, tol, pcur, out_idx, kerr, group_base, 3,
+            fuse->last_group);
     else if (nhalf == T) SMK_TB_LAUNCH(true, 0);
     else SMK_TB_LAUNCH(false, -1);
 #undef SMK_TB_LAUNCH
@@ -750,6 +908,10 @@ bool encode_3d_box(CUtensorMap* m, const void* base, bool is_u8, const Grid& g, 
 }
 }  // namespace tb
 
+bool sweep_tb_fusable(int T, int rows, int nhalf, int check) {
+    return (rows == 2 || rows == 4) && sweep_tb_shape_supported(T, rows) && nhalf == T && !check;
+}
+
 int sweep_tb_shape_supported(int T, int rows) {
     if (rows & SWEEP_YCLUSTER) {
         const int n = sweep_ycluster_n(rows);
@@ -812,8 +974,9 @@ void destroy_sweep_maps(SweepMaps* m) { delete m; }
 int launch_sweep_tb(const SweepMaps* m, const Grid& g, bool in_is_a, float* Pout, int T, int rows,
                     int nhalf, int colour0, int zchunk, const float* wacc7, StepStatus* status,
                     int check, int group, float tol, int* pcur, int out_idx, int* kerr,
-                    const int* group_base, cudaStream_t st) {
+                    const int* group_base, cudaStream_t st, const SweepFuse* fuse) {
     if (!sweep_tb_shape_supported(T, rows)) return -1;
+    if (fuse != nullptr && (fuse->mode == 0 || !sweep_tb_fusable(T, rows, nhalf, check))) fuse = nullptr;
     const int v = rows == 4 ? 1 : 0;
     TBMaps maps;
     maps.pin = in_is_a ? m->pa[v] : m->pb[v];
@@ -821,6 +984,8 @@ int launch_sweep_tb(const SweepMaps* m, const Grid& g, bool in_is_a, float* Pout
     maps.f = m->f[v];
 #define SMK_TB_ARGS maps, g, Pout, nhalf, colour0, zchunk, wacc7, status, check, group, tol, pcur, out_idx, kerr, group_base, st
     if (rows & SWEEP_YCLUSTER) return launch_tb_ycl(sweep_ycluster_n(rows), SMK_TB_ARGS);
+#undef SMK_TB_ARGS
+#define SMK_TB_ARGS maps, g, Pout, nhalf, colour0, zchunk, wacc7, status, check, group, tol, pcur, out_idx, kerr, group_base, st, fuse
     if (rows == 4) return launch_tb<4, 4>(SMK_TB_ARGS);
     switch (T) {
         case 2: return launch_tb<2, 2>(SMK_TB_ARGS);

@@ -322,6 +322,7 @@ int smk_sim::enqueue(float dt, cudaStream_t st) {
         const bool use_tol = p.tol > 0.0f;
         const int G = use_tol ? p.check_every : (p.max_sweeps > 0 ? p.max_sweeps : 1);
         int sweep = 0, group = 0;
+        bool subtract_fused = false;  // a blocked launch that certainly runs applied the subtract
         if (timed) SMK_CUDA(rec(ev[5]));
         if (p.solver == SMK_SOLVER_JACOBI) {
             // weighted Jacobi, ping-ponging P <-> P2 (each launch records in *pcur where it wrote);
@@ -343,21 +344,47 @@ int smk_sim::enqueue(float dt, cudaStream_t st) {
             }
         } else if (sweep_depth > 0) {
             // temporally blocked: each launch applies up to sweep_depth colour passes,
-            // ping-ponging P <-> P2; group starts are the check launches
+            // ping-ponging P <-> P2; group starts are the check launches, and a launch of fewer
+            // passes comes first in its group, so that the group ends with a full launch
             int nl = 0;
-            // the launches of one group [s0, s1) in sweeps; `grp` is the group index, relative to
-            // *gbase when gbase is set (device-side loop)
-            auto issue_group = [&](int grp, int s0, int s1, const int* gbase, cudaStream_t s) -> int {
-                const int h1 = 2 * s1;
-                for (int h = 2 * s0; h < h1; h += sweep_depth) {
-                    const int nh = h1 - h < sweep_depth ? h1 - h : sweep_depth;
+            // With smk_set_fused_subtract, the gradient subtract is fused into the group's last
+            // launch where it can end the solve (FP32 state, a group of two launches or more):
+            // one launch of the fused kernel where the host knows it ends the solve (no
+            // tolerance, or the group at the sweep cap), else a pair (the plain kernel, then the
+            // fused one; one of them works)
+            int* sub_done = reinterpret_cast<int*>(&status->rmax_bits[status_groups]);
+            const bool fusable = fuse_subtract && !bf16 && p.max_sweeps > 0;
+            const int last_group = (p.max_sweeps + G - 1) / G - 1;
+            bool fused_known = false;  // a launch that certainly runs ends the solve fused
+            // at_cap: the group ends at the sweep cap (unrolled groups only)
+            auto issue_group = [&](int grp, int s0, int s1, const int* gbase, cudaStream_t s, bool at_cap) -> int {
+                const int h0 = 2 * s0, h1 = 2 * s1;
+                const int first = (h1 - h0) % sweep_depth;
+                for (int h = h0; h < h1;) {
+                    const int nh = (h == h0 && first != 0) ? first : sweep_depth;
                     const bool in_a = (nl & 1) == 0;
-                    if (launch_sweep_tb(maps, g, in_a, in_a ? P2 : P, sweep_depth, sweep_rows, nh, h & 1, sweep_zchunk,
-                                        wacc, use_tol ? status : nullptr, use_tol && h == 2 * s0, grp, p.tol,
-                                        pcur, in_a ? 1 : 0, kerr, gbase, s) != 0)
-                        return fail(SMK_ERR_CUDA, "sweep kernel configuration failed");
+                    const bool chk = use_tol && h == h0;
+                    const bool last = h + nh == h1;
+                    int modes[2] = {0, -1};
+                    if (fusable && last && h > h0 && sweep_tb_fusable(sweep_depth, sweep_rows, nh, chk)) {
+                        if (!use_tol || at_cap) {
+                            modes[0] = 1;
+                            fused_known = fused_known || !use_tol;
+                        } else {
+                            modes[0] = 3;
+                            modes[1] = 2;
+                        }
+                    }
+                    for (int m = 0; m < 2 && modes[m] >= 0; ++m) {
+                        const SweepFuse fz{u[now], v[now], w[now], sub_done, modes[m], last_group};
+                        if (launch_sweep_tb(maps, g, in_a, in_a ? P2 : P, sweep_depth, sweep_rows, nh, h & 1,
+                                            sweep_zchunk, wacc, use_tol ? status : nullptr, chk, grp, p.tol, pcur,
+                                            in_a ? 1 : 0, kerr, gbase, s, modes[m] ? &fz : nullptr) != 0)
+                            return fail(SMK_ERR_CUDA, "sweep kernel configuration failed");
+                        ++launches;
+                    }
                     ++nl;
-                    ++launches;
+                    h += nh;
                 }
                 return SMK_OK;
             };
@@ -394,7 +421,7 @@ int smk_sim::enqueue(float dt, cudaStream_t st) {
                 const int nl0 = nl;
                 const long long l0 = launches;
                 int rc = SMK_OK;
-                for (int u = 0; u < U && rc == SMK_OK; ++u) rc = issue_group(u, u * G, (u + 1) * G, gcount, body_stream);
+                for (int u = 0; u < U && rc == SMK_OK; ++u) rc = issue_group(u, u * G, (u + 1) * G, gcount, body_stream, false);
                 const int per_iter = (int)(launches - l0) + 1;
                 if (rc == SMK_OK)
                     launch_group_loop_next(status, gcount, U, loop_groups, loop_launches, per_iter, handle, body_stream);
@@ -410,11 +437,12 @@ int smk_sim::enqueue(float dt, cudaStream_t st) {
             }
             while (sweep < p.max_sweeps) {
                 const int end = sweep + G < p.max_sweeps ? sweep + G : p.max_sweeps;
-                const int rc = issue_group(group, sweep, end, nullptr, st);
+                const int rc = issue_group(group, sweep, end, nullptr, st, end == p.max_sweeps);
                 if (rc != SMK_OK) return rc;
                 sweep = end;
                 ++group;
             }
+            subtract_fused = fused_known;
         } else {
             while (sweep < p.max_sweeps) {
                 if (use_tol) {
@@ -435,12 +463,16 @@ int smk_sim::enqueue(float dt, cudaStream_t st) {
         // the blocked and Jacobi solves record where the pressure is; the colour passes keep it in P
         const bool pcur_set = (sweep_depth > 0 || p.solver == SMK_SOLVER_JACOBI) && p.max_sweeps > 0;
         if (!pcur_set) SMK_CUDA(cudaMemsetAsync(pcur, 0, sizeof(int), st));
-        if (bf16)
+        if (bf16) {
             launch_project_bf16(g, bf(u[now]), bf(v[now]), bf(w[now]), P, P2, pcur, flags, proj[0], proj[1],
                                 proj[2], st, vec_stages);
-        else
-            launch_gradient_subtract(g, u[now], v[now], w[now], P, P2, pcur, flags, st, vec_stages);
-        ++launches;
+            ++launches;
+        } else if (!subtract_fused) {
+            // skipped at run time when a blocked launch applied it (SweepFuse)
+            launch_gradient_subtract(g, u[now], v[now], w[now], P, P2, pcur, flags, st, vec_stages,
+                                     reinterpret_cast<const int*>(&status->rmax_bits[status_groups]));
+            ++launches;
+        }
         if (p.refine > 0) {
             if (bf16)
                 launch_refine(g, proj[0], proj[1], proj[2], bf(u[now]), bf(v[now]), bf(w[now]), b, P, P2, pcur,
@@ -906,12 +938,14 @@ int smk_get_stats(smk_sim* sim, smk_stats* out) {
     out->div_max = -1.0f;
     out->div64_max = -1.0f;
     if (sim->steps == 0) return SMK_OK;
-    std::vector<unsigned> host(4 + sim->status_groups);
+    // the header words, the group residuals, and the fused-subtract word after them
+    std::vector<unsigned> host(5 + sim->status_groups);
     SMK_CUDA(cudaDeviceSynchronize());
     int krc = check_kernel_error(sim);
     if (krc) return krc;
     SMK_CUDA(cudaMemcpy(host.data(), sim->status, sizeof(StepStatus) + sizeof(unsigned) * sim->status_groups,
                         cudaMemcpyDeviceToHost));
+    out->subtract_fused = host[4 + sim->status_groups] != 0u ? 1 : 0;
     StepStatus hs;
     memcpy(&hs, host.data(), sizeof(StepStatus) - sizeof(unsigned));
     const unsigned* rmax = host.data() + 4;
@@ -1043,6 +1077,13 @@ int smk_set_graphs(smk_sim* sim, int enable) {
 int smk_set_vector_stages(smk_sim* sim, int enable) {
     if (!sim) return fail(SMK_ERR_INVALID, "sim is null");
     sim->vec_stages = enable != 0;
+    for (auto& gs : sim->graphs) gs.sig.clear();  // re-capture
+    return SMK_OK;
+}
+
+int smk_set_fused_subtract(smk_sim* sim, int enable) {
+    if (!sim) return fail(SMK_ERR_INVALID, "sim is null");
+    sim->fuse_subtract = enable != 0;
     for (auto& gs : sim->graphs) gs.sig.clear();  // re-capture
     return SMK_OK;
 }
@@ -1244,17 +1285,18 @@ int smk_autotune(smk_sim* sim, int* depth_out, int* zchunk_out, float* us_per_sw
         }
     }
     // time one tolerance group exactly as a step issues it: 2G colour passes in launches of
-    // `d` (the last one partial when d does not divide 2G), the first with the fused residual
+    // `d` (the first one partial when d does not divide 2G), the first with the fused residual
     const bool use_tol = sim->p.tol > 0.0f;
     const int G = use_tol ? sim->p.check_every : std::max(1, std::min(sim->p.max_sweeps, 20));
     auto run_group = [&](int d, int rows, int zc) -> int {
         if (use_tol) SMK_CUDA(cudaMemsetAsync(sim->tune_status, 0, sizeof(StepStatus) + sizeof(unsigned), st));
-        for (int h = 0; h < 2 * G; h += d) {
-            const int nh = 2 * G - h < d ? 2 * G - h : d;
+        for (int h = 0; h < 2 * G;) {
+            const int nh = (h == 0 && (2 * G) % d != 0) ? (2 * G) % d : d;
             if (launch_sweep_tb(sim->maps, g, true, sim->P2, d, rows, nh, h & 1, zc, wacc,
                                 use_tol ? sim->tune_status : nullptr, use_tol && h == 0, 0, sim->p.tol,
                                 nullptr, 0, sim->kerr, nullptr, st) != 0)
                 return fail(SMK_ERR_CUDA, "sweep kernel configuration failed");
+            h += nh;
         }
         return SMK_OK;
     };

@@ -128,6 +128,7 @@ struct smk_sim {
     // loop (graph conditional node) instead of launches for every group up to the cap
     bool graph_loops = true;
     bool vec_stages = true;  // 4-wide forcing / rhs / subtract kernels where the layout allows
+    bool fuse_subtract = false;  // the gradient subtract inside the solve's last sweep launch
     GraphSlot graphs[2];
     cudaStream_t cap_stream = nullptr;
     cudaStream_t body_stream = nullptr;  // captures the loop body

@@ -58,6 +58,16 @@ __device__ __forceinline__ void tma_load_3d(uint32_t dst, const CUtensorMap* map
         : "memory");
 }
 
+// 4-byte asynchronous copy global -> shared (no register holds the value); completion by
+// cp_async_commit / cp_async_wait_all of the issuing thread.
+__device__ __forceinline__ void cp_async4(uint32_t dst, const void* src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+// every committed group but the most recent one has completed
+__device__ __forceinline__ void cp_async_wait_one() { asm volatile("cp.async.wait_group 1;" ::: "memory"); }
+
 // Windows along an axis of n cells, W cells wide with a T-cell halo.  A side of a window that
 // reaches the grid's first or last cell needs no halo: those cells (the boundary ring) and every
 // cell outside the grid are never updated by a sweep, so they never change, and a wrong value
