@@ -306,8 +306,8 @@ T residual_max(const Dims& d, const T* P, const T* b, const uint8_t* s) {
 //   r      = fma(-acc, P_c, b_c + nbr_sum)
 //   P_c   <- fma(omega/acc, r, P_c)           (omega/acc rounded to T once per acc value)
 // Tolerance rule (tol > 0): at every check point j = k*check_every the residual max of the
-// current state is computed; the sweeps of that group run regardless, and if the residual was
-// <= tol the solve ends after them.  The GPU kernels follow the same rule.
+// current state is computed, and if it is <= tol the solve ends there, on that state (sweeps =
+// j).  The GPU kernels follow the same rule.
 template <typename T>
 int project_pressure(const Dims& d, T* u, T* v, T* w, T* P, T* b, const uint8_t* s, int max_sweeps,
                      double omega, float tol, int check_every, int warm_start, orc_stats* st,
@@ -340,10 +340,12 @@ int project_pressure(const Dims& d, T* u, T* v, T* w, T* P, T* b, const uint8_t*
     T last_r = 0;
     const int G = check_every > 0 ? check_every : 1;
     while (sweeps < max_sweeps) {
-        bool stop_after_group = false;
         if (tol > 0.0f && sweeps % G == 0) {
             last_r = residual_max(d, P, b, s);
-            if (last_r <= (T)tol) stop_after_group = true;
+            if (last_r <= (T)tol) {
+                converged = 1;
+                break;
+            }
         }
         int group_end = (tol > 0.0f) ? std::min(max_sweeps, (sweeps / G + 1) * G) : max_sweeps;
         for (; sweeps < group_end; ++sweeps) {
@@ -384,10 +386,6 @@ int project_pressure(const Dims& d, T* u, T* v, T* w, T* P, T* b, const uint8_t*
                         }
                     }
             }
-        }
-        if (stop_after_group) {
-            converged = 1;
-            break;
         }
     }
     // gradient subtract on faces whose two cells are both fluid (P = 0 off the projectable set)

@@ -42,10 +42,32 @@ enum : uint8_t {
 struct StepStatus {
     unsigned div_bits;   // max |div u| after projection, as float bits (non-negative)
     int done;            // tolerance reached: later sweep groups are skipped
-    int done_group;      // check group that set `done`
-    int error;           // a bounded device wait gave up (the kernel returned early)
+    int done_group;      // the solve ended at the start of this check group (its residual <= tol)
+    unsigned arrivals;   // blocks of the running check launch that have added their residual;
+                         // the last one decides and resets it (check_decide)
     unsigned rmax_bits[1];  // max |residual| per check group (flexible; sized at allocation)
 };
+
+// The tolerance rule, decided at the end of the launch that records the residual of check
+// group `group`: every block calls it once after its block_max_to into rmax_bits[group] (thread
+// 0 of the block, which made that atomic); the last of `nblocks` to arrive reads the group's
+// residual and, when it is <= tol, ends the solve there (done, done_group) and, for a launch
+// that swept from one pressure buffer into the other, points *pcur back at the launch's input
+// (in_idx >= 0), so that the passes it applied are dropped.  Returns whether it ended the solve.
+__device__ __forceinline__ bool check_decide(StepStatus* status, int group, float tol, unsigned nblocks,
+                                             int* pcur, int in_idx) {
+    __threadfence();
+    const unsigned prev = atomicAdd(&status->arrivals, 1u);
+    if (prev + 1u != nblocks) return false;
+    __threadfence();
+    const float r = __uint_as_float(*(volatile unsigned*)&status->rmax_bits[group]);
+    status->arrivals = 0u;
+    if (!(r <= tol)) return false;
+    status->done = 1;
+    status->done_group = group;
+    if (pcur != nullptr && in_idx >= 0) *pcur = in_idx;
+    return true;
+}
 
 // Device-side state of the projection's FP64-checked refinement rounds.
 struct RefineStatus {

@@ -102,20 +102,16 @@ void destroy_sweep_maps(SweepMaps* m);
 // The gradient subtract fused into the last launch of a solve: u, v, w (FP32, the grid's
 // layout) move by the final pressure's gradient inside the launch that applies the last colour
 // pass, and *sub_done is set so that the separate subtract (launch_gradient_subtract with
-// skip = sub_done) does nothing.  mode 1: the launch ends the solve (fixed sweep count, or the
-// last group under the sweep cap).  Where only the device knows (the launch ends the solve when
-// the residual its tolerance group started from was within tol: the tolerance rule then stops
-// before the next group; or its group is the last one, last_group, under the sweep cap), the
-// launch is issued twice, mode 3 then mode 2: the mode-3 launch (plain kernel) works unless the
-// launch ends the solve, the mode-2 launch (fused kernel) only when it does, so the fused
-// kernel, which needs more registers, runs once per solve.
+// skip = sub_done) does nothing.  mode 1: the launch ends the solve unless the tolerance rule
+// ended it earlier (fixed sweep count, or the last launch under the sweep cap; the host knows).
+// Under the tolerance rule the solve ends on the input of a check launch, which only its end
+// decides, so the launch that ends it is known to nobody in time and the subtract stays a pass.
 struct SweepFuse {
     float* u;
     float* v;
     float* w;
     int* sub_done;
     int mode;
-    int last_group;
 };
 // Whether launch_sweep_tb can fuse the subtract into a launch of this shape (full launches of
 // the plain 2-row and 4-row kernels, not check launches).

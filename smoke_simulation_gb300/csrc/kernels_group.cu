@@ -354,20 +354,8 @@ __global__ void __launch_bounds__(GROUP_TILE) k_group_project(const GroupArgs a)
             const GroupGrid& d = a.grids[j];
             uint8_t m = gst[j] & GA_DONE;
             if (!m && d.wave == wave && s < d.max_sweeps) {
-                bool check = false;
-                if (!a.sweeps_only && d.tol > 0.0f && s % d.check_every == 0) {
-                    const int k = s / d.check_every;
-                    if (k > 0 && __uint_as_float(*(volatile unsigned*)&d.status->rmax_bits[k - 1]) <= d.tol) {
-                        m = GA_DONE;
-                        if (blockIdx.x == 0) {
-                            d.status->done = 1;
-                            d.status->done_group = k;
-                        }
-                    } else {
-                        check = true;
-                    }
-                }
-                if (!m) m = check ? (GA_SWEEP | GA_CHECK) : GA_SWEEP;
+                const bool check = !a.sweeps_only && d.tol > 0.0f && s % d.check_every == 0;
+                m = check ? (GA_SWEEP | GA_CHECK) : GA_SWEEP;
             }
             gst[j] = m;
             act |= m & GA_SWEEP;
@@ -408,6 +396,27 @@ __global__ void __launch_bounds__(GROUP_TILE) k_group_project(const GroupArgs a)
                 group_abort(a);
                 return;
             }
+            // the tolerance rule: a grid whose residual is within tolerance ends its solve here,
+            // before this group's sweeps
+            act = 0;
+            for (int j = tid; j < a.n; j += GROUP_TILE) {
+                const GroupGrid& d = a.grids[j];
+                uint8_t m = gst[j];
+                if (m & GA_CHECK) {
+                    const int k = s / d.check_every;
+                    if (__uint_as_float(*(volatile unsigned*)&d.status->rmax_bits[k]) <= d.tol) {
+                        m = GA_DONE;
+                        if (blockIdx.x == 0) {
+                            d.status->done = 1;
+                            d.status->done_group = k;
+                        }
+                    }
+                }
+                gst[j] = m;
+                act |= m & GA_SWEEP;
+            }
+            act = __syncthreads_or(act);
+            if (!act) continue;  // every checked grid is done; the next pass finds none active
         }
 
         for (int colour = 0; colour < 2; ++colour) {

@@ -103,7 +103,7 @@ __global__ void k_jacobi(Grid g, const float* __restrict__ Pin, float* __restric
 __global__ void k_resid_check(Grid g, const float* __restrict__ P, const float* __restrict__ b,
                               const uint8_t* __restrict__ flags, StepStatus* status, int group,
                               float tol) {
-    body_resid_check(g, P, b, flags, status, group, tol, blockIdx);
+    body_resid_check(g, P, b, flags, status, group, tol, blockIdx, gridDim.x * gridDim.y * gridDim.z);
 }
 
 

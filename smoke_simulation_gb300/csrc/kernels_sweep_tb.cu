@@ -188,8 +188,8 @@ __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, fl
                                            int nhalf, int colour0, int zchunk, const WAcc8& wa,
                                            StepStatus* status, int check, int group, float tol,
                                            int* __restrict__ pcur, int out_idx, int* __restrict__ kerr,
-                                           int bx, int by, int bz, int ycl_n = 1, int ycl_hy = 0,
-                                           SweepFuse fz = SweepFuse{}) {
+                                           int bx, int by, int bz, unsigned ntiles, int ycl_n = 1,
+                                           int ycl_hy = 0, SweepFuse fz = SweepFuse{}) {
     static_assert(!FUSE || (FULL && CHK == 0 && !YCLUSTER && !GLOBAL_MAPS), "fused subtract: plain full launches");
     const bool chk = CHK < 0 ? check != 0 : CHK == 1;
     using G = TBGeom<PY>;
@@ -226,24 +226,9 @@ __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, fl
     __shared__ int tma_bad;           // YCLUSTER: a TMA stage of this CTA never completed
 
     const bool first_tile = (bx | by | bz) == 0;
-    if (status != nullptr) {
-        if (*(volatile int*)&status->done) return;
-        if (chk && group > 0 && __uint_as_float(status->rmax_bits[group - 1]) <= tol) {
-            if (first_tile && threadIdx.x == 0 && threadIdx.y == 0) {
-                status->done = 1;
-                status->done_group = group;
-            }
-            return;
-        }
-    }
-    // modes 2 and 3 are the two launches of a pair of which exactly one works: the fused one when
-    // this launch ends the solve (the residual its group started from, recorded by the group's
-    // check launch, was within tol, or the group is the last under the sweep cap), the plain one
-    // otherwise
-    if ((fz.mode == 2 || fz.mode == 3) && status != nullptr &&
-        (group == fz.last_group || __uint_as_float(status->rmax_bits[group]) <= tol) != (fz.mode == 2))
-        return;
-    const bool fuse = FUSE && (fz.mode == 1 || fz.mode == 2);
+    // the solve ended at an earlier check (check_decide at the end of a check launch)
+    if (status != nullptr && *(volatile int*)&status->done) return;
+    const bool fuse = FUSE && fz.mode == 1;
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int tid = ty * TB_TX + tx;
     const bool leader = tid == 0;
@@ -628,7 +613,12 @@ __device__ __forceinline__ void sweep_tile(const TBMaps& maps, const Grid& g, fl
         }
     }
     if (FUSE && fuse) cp_async_wait_all();  // no staged copy outlives the CTA
-    if (chk) block_max_to(rmax, &status->rmax_bits[group]);
+    if (chk) {
+        // the residual of this launch's input; if it is within tolerance the solve ends on that
+        // input and this launch's passes are dropped
+        block_max_to(rmax, &status->rmax_bits[group]);
+        if (tid == 0) check_decide(status, group, tol, ntiles, pcur, 1 - out_idx);
+    }
     if (YCLUSTER) cluster_sync_all();  // no CTA leaves while a neighbour may still address it
 }
 
@@ -637,12 +627,12 @@ __global__ void __launch_bounds__(TBGeom<PY>::THREADS, 1)
 k_sweep_tb(const __grid_constant__ TBMaps maps, Grid g, float* __restrict__ Pout, int nhalf,
            int colour0, int zchunk, const __grid_constant__ WAcc8 wa, StepStatus* status, int check, int group,
            float tol, int* __restrict__ pcur, int out_idx, int* __restrict__ kerr,
-           const int* __restrict__ group_base, int pair_mode, int last_group) {
+           const int* __restrict__ group_base) {
     // inside a graph's device-side group loop the group index is relative to the loop counter
     if (group_base != nullptr) group += *group_base;
     sweep_tile<T, PY, false, false, FULL, CHK>(maps, g, Pout, nhalf, colour0, zchunk, wa, status, check, group,
                                                tol, pcur, out_idx, kerr, (int)blockIdx.x, (int)blockIdx.y,
-                                               (int)blockIdx.z, 1, 0, SweepFuse{nullptr, nullptr, nullptr, nullptr, pair_mode, last_group});
+                                               (int)blockIdx.z, gridDim.x * gridDim.y * gridDim.z);
 }
 
 // A full non-check launch that may end the solve: the gradient subtract fused (sweep_tile FUSE).
@@ -654,7 +644,7 @@ k_sweep_tb_fused(const __grid_constant__ TBMaps maps, Grid g, float* __restrict_
     if (group_base != nullptr) group += *group_base;
     sweep_tile<T, PY, false, false, true, 0, true>(maps, g, Pout, T, colour0, zchunk, wa, status, 0, group, tol, pcur,
                                                    out_idx, kerr, (int)blockIdx.x, (int)blockIdx.y, (int)blockIdx.z,
-                                                   1, 0, fz);
+                                                   gridDim.x * gridDim.y * gridDim.z, 1, 0, fz);
 }
 
 // The y-cluster form (2-row patches): runs of ycl_n CTAs along y form clusters, with a halo of
@@ -667,7 +657,8 @@ k_sweep_tb_ycl(const __grid_constant__ TBMaps maps, Grid g, float* __restrict__ 
                int ycl_n, int ycl_hy) {
     if (group_base != nullptr) group += *group_base;
     sweep_tile<T, 2, false, true>(maps, g, Pout, nhalf, colour0, zchunk, wa, status, check, group, tol, pcur,
-                                  out_idx, kerr, (int)blockIdx.x, (int)blockIdx.y, (int)blockIdx.z, ycl_n, ycl_hy);
+                                  out_idx, kerr, (int)blockIdx.x, (int)blockIdx.y, (int)blockIdx.z,
+                                  gridDim.x * gridDim.y * gridDim.z, ycl_n, ycl_hy);
 }
 
 // ---- grouped form: one blocked launch over the tiles of every grid of a batch ---------------
@@ -713,7 +704,8 @@ k_group_sweep_tb(const GroupTBGrid* __restrict__ grids, const int* __restrict__ 
     int* const kerr = d.kerr;
     const float tol = d.tol;
     sweep_tile<T, 2, true, false, FULL, CHK>(d.maps[in_a ? 0 : 1], g, Pout, nhalf, colour0, zchunk, d.wa, status,
-                                             check, group, tol, pcur, in_a ? 1 : 0, kerr, bx, by, bz);
+                                             check, group, tol, pcur, in_a ? 1 : 0, kerr, bx, by, bz,
+                                             (unsigned)(per * d.zchunks));
 }
 
 // End of one iteration of a grouped step's device-side loop over tolerance groups: advance
@@ -801,16 +793,11 @@ int launch_tb(const TBMaps& maps, const Grid& g, float* Pout, int nhalf, int col
 #define SMK_TB_LAUNCH(FULL, CHK)                                                                             \
     k_sweep_tb<T, PY, FULL, CHK><<<grid, dim3(TB_TX, G::TY), smem, st>>>(maps, g, Pout, nhalf, colour0, zchunk, \
                                                                         wa, status, check, group, tol, pcur,  \
-                                                                        out_idx, kerr, group_base, 0, -1)
-    const int mode = fuse != nullptr ? fuse->mode : 0;
+                                                                        out_idx, kerr, group_base)
     if (nhalf == T && check) SMK_TB_LAUNCH(true, 1);
-    else if (nhalf == T && (mode == 1 || mode == 2))
+    else if (nhalf == T && fuse != nullptr && fuse->mode == 1)
         k_sweep_tb_fused<T, PY><<<grid, dim3(TB_TX, G::TY), tb_smem_bytes_fused<T, PY>(), st>>>(
             maps, g, Pout, colour0, zchunk, wa, status, group, tol, pcur, out_idx, kerr, group_base, *fuse);
-    else if (nhalf == T && mode == 3)
-        k_sweep_tb<T, PY, true, 0><<<grid, dim3(TB_TX, G::TY), smem, st>>>(
-            maps, g, Pout, nhalf, colour0, zchunk, wa, status, check, group, tol, pcur, out_idx, kerr, group_base, 3,
-            fuse->last_group);
     else if (nhalf == T) SMK_TB_LAUNCH(true, 0);
     else SMK_TB_LAUNCH(false, -1);
 #undef SMK_TB_LAUNCH

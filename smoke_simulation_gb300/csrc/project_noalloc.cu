@@ -231,7 +231,7 @@ int smk_project_noalloc(float* u, float* v, float* w, const uint8_t* mask, int n
         memcpy(&stats->div_max, &hs.div_bits, 4);
         stats->sweeps = p.max_sweeps;
         if (use_tol && ngroups > 0) {
-            const int last = hs.done ? hs.done_group - 1 : ngroups - 1;
+            const int last = hs.done ? hs.done_group : ngroups - 1;
             unsigned bits = 0;
             NA_CUDA(cudaMemcpy(&bits, reinterpret_cast<const unsigned char*>(status) +
                                           offsetof(smk::StepStatus, rmax_bits) + 4 * (size_t)last,

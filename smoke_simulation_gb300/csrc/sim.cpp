@@ -348,14 +348,11 @@ int smk_sim::enqueue(float dt, cudaStream_t st) {
             // ping-ponging P <-> P2; group starts are the check launches, and a launch of fewer
             // passes comes first in its group, so that the group ends with a full launch
             int nl = 0;
-            // With smk_set_fused_subtract, the gradient subtract is fused into the group's last
-            // launch where it can end the solve (FP32 state, a group of two launches or more):
-            // one launch of the fused kernel where the host knows it ends the solve (no
-            // tolerance, or the group at the sweep cap), else a pair (the plain kernel, then the
-            // fused one; one of them works)
+            // With smk_set_fused_subtract, the gradient subtract is fused into the solve's last
+            // launch where the host knows it (FP32 state; no tolerance, or the last launch under
+            // the sweep cap, when the tolerance rule has not ended the solve before it)
             int* sub_done = reinterpret_cast<int*>(&status->rmax_bits[status_groups]);
             const bool fusable = fuse_subtract && !bf16 && p.max_sweeps > 0;
-            const int last_group = (p.max_sweeps + G - 1) / G - 1;
             bool fused_known = false;  // a launch that certainly runs ends the solve fused
             // at_cap: the group ends at the sweep cap (unrolled groups only)
             auto issue_group = [&](int grp, int s0, int s1, const int* gbase, cudaStream_t s, bool at_cap) -> int {
@@ -366,24 +363,15 @@ int smk_sim::enqueue(float dt, cudaStream_t st) {
                     const bool in_a = (nl & 1) == 0;
                     const bool chk = use_tol && h == h0;
                     const bool last = h + nh == h1;
-                    int modes[2] = {0, -1};
-                    if (fusable && last && h > h0 && sweep_tb_fusable(sweep_depth, sweep_rows, nh, chk)) {
-                        if (!use_tol || at_cap) {
-                            modes[0] = 1;
-                            fused_known = fused_known || !use_tol;
-                        } else {
-                            modes[0] = 3;
-                            modes[1] = 2;
-                        }
-                    }
-                    for (int m = 0; m < 2 && modes[m] >= 0; ++m) {
-                        const SweepFuse fz{u[now], v[now], w[now], sub_done, modes[m], last_group};
-                        if (launch_sweep_tb(maps, g, in_a, in_a ? P2 : P, sweep_depth, sweep_rows, nh, h & 1,
-                                            sweep_zchunk, wacc, use_tol ? status : nullptr, chk, grp, p.tol, pcur,
-                                            in_a ? 1 : 0, kerr, gbase, s, modes[m] ? &fz : nullptr) != 0)
-                            return fail(SMK_ERR_CUDA, "sweep kernel configuration failed");
-                        ++launches;
-                    }
+                    const bool fz_on = fusable && last && (!use_tol || at_cap) &&
+                                       sweep_tb_fusable(sweep_depth, sweep_rows, nh, chk);
+                    fused_known = fused_known || (fz_on && !use_tol);
+                    const SweepFuse fz{u[now], v[now], w[now], sub_done, 1};
+                    if (launch_sweep_tb(maps, g, in_a, in_a ? P2 : P, sweep_depth, sweep_rows, nh, h & 1, sweep_zchunk,
+                                        wacc, use_tol ? status : nullptr, chk, grp, p.tol, pcur, in_a ? 1 : 0, kerr,
+                                        gbase, s, fz_on ? &fz : nullptr) != 0)
+                        return fail(SMK_ERR_CUDA, "sweep kernel configuration failed");
+                    ++launches;
                     ++nl;
                     h += nh;
                 }
@@ -397,7 +385,9 @@ int smk_sim::enqueue(float dt, cudaStream_t st) {
             // entry, so results are identical.
             const int nlg = (2 * G + sweep_depth - 1) / sweep_depth;
             const int U = (nlg % 2 == 0) ? 1 : 2;
-            const int full = use_tol ? p.max_sweeps / G : 0;
+            // with the subtract fused, the group at the cap stays out of the loop: its last launch
+            // is then issued knowing that it ends the solve (if the tolerance rule has not)
+            const int full = use_tol ? p.max_sweeps / G - (fusable && p.max_sweeps % G == 0 ? 1 : 0) : 0;
             const int loop_groups = (capturing && graph_loops && use_tol) ? (full / U) * U : 0;
             if (loop_groups > U) {
                 SMK_CUDA(cudaMemsetAsync(gcount, 0, sizeof(int), st));
@@ -963,7 +953,7 @@ int smk_get_stats(smk_sim* sim, smk_stats* out) {
         if (hs.done) {
             out->sweeps = hs.done_group * G;
             out->converged = 1;
-            memcpy(&out->resid_max, &rmax[hs.done_group - 1], 4);
+            memcpy(&out->resid_max, &rmax[hs.done_group], 4);
         } else {
             out->sweeps = sim->last_max_sweeps;
             float r = 0;
@@ -1327,13 +1317,14 @@ int smk_autotune(smk_sim* sim, int* depth_out, int* zchunk_out, float* us_per_sw
     const bool use_tol = sim->p.tol > 0.0f;
     const int G = use_tol ? sim->p.check_every : std::max(1, std::min(sim->p.max_sweeps, 20));
     int nl = 0;
+    // tolerance -1: the check launch records its residual but never ends the timed solve
     auto run_group = [&](int d, int rows, int zc) -> int {
         if (use_tol) SMK_CUDA(cudaMemsetAsync(sim->tune_status, 0, sizeof(StepStatus) + sizeof(unsigned), st));
         for (int h = 0; h < 2 * G;) {
             const int nh = (h == 0 && (2 * G) % d != 0) ? (2 * G) % d : d;
             const bool in_a = saved.p == nullptr || (nl & 1) == 0;
             if (launch_sweep_tb(sim->maps, g, in_a, in_a ? sim->P2 : sim->P, d, rows, nh, h & 1, zc, wacc,
-                                use_tol ? sim->tune_status : nullptr, use_tol && h == 0, 0, sim->p.tol,
+                                use_tol ? sim->tune_status : nullptr, use_tol && h == 0, 0, -1.0f,
                                 nullptr, 0, sim->kerr, nullptr, st) != 0)
                 return fail(SMK_ERR_CUDA, "sweep kernel configuration failed");
             h += nh;

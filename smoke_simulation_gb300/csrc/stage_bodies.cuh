@@ -213,26 +213,21 @@ __device__ __forceinline__ void body_sweep(const Grid& g, float* P, const float*
     cell_sweep(g, P, b, flags, g.idx(x, y, z), wa.w);
 }
 
-// Residual check at the start of sweep group `group`: if the previous group's residual was
-// within tolerance the solve is over (set `done`); otherwise record max |r| for this group.
-// Contains a block barrier: every thread of the block must call it.
+// Residual check at the start of sweep group `group`: record max |r| of the current pressure;
+// the last block to finish decides (check_decide): within tolerance, the solve ends here and
+// the group's sweeps, which test `done`, do nothing.  Contains a block barrier: every thread of
+// the block must call it.  nblocks: the blocks of the launch.
 __device__ __forceinline__ void body_resid_check(const Grid& g, const float* P, const float* b,
                                                  const uint8_t* __restrict__ flags, StepStatus* status,
-                                                 int group, float tol, uint3 bid) {
+                                                 int group, float tol, uint3 bid, unsigned nblocks) {
     if (*(volatile int*)&status->done) return;
-    if (group > 0 && __uint_as_float(status->rmax_bits[group - 1]) <= tol) {
-        if (bid.x == 0 && bid.y == 0 && bid.z == 0 && threadIdx.x == 0 && threadIdx.y == 0) {
-            status->done = 1;
-            status->done_group = group;
-        }
-        return;
-    }
     const int x = 1 + (int)bid.x * SB_BX + (int)threadIdx.x;
     const int y = 1 + (int)bid.y * SB_BY + (int)threadIdx.y;
     const int z = 1 + (int)bid.z;
     float m = 0.0f;
     if (x <= g.nx - 2 && y <= g.ny - 2 && z <= g.nz - 2) m = cell_resid(g, P, b, flags, g.idx(x, y, z));
     block_max_to(__float_as_uint(m), &status->rmax_bits[group]);
+    if (threadIdx.x == 0 && threadIdx.y == 0) check_decide(status, group, tol, nblocks, nullptr, -1);
 }
 
 // u -= P(x) - P(x-1) on faces whose two cells are fluid (P is 0 off the projectable set).  The
