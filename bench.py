@@ -388,11 +388,13 @@ def main():
     # ---- roofline of the dominant kernel (the blocked sweep, per launch) ---------------------
     # algorithmic bytes per launch = cells x 13 B x (depth/2 sweeps); the launch duration is the
     # event-timed sweep phase of the measured steps divided by the launches that ran in it
-    # (the residual check is fused into the first launch of each group: no extra bytes)
+    # (the residual check is fused into the first launch of each group: no extra bytes).  A
+    # solve that the tolerance rule ends also ran the check launch whose passes it dropped (the
+    # solve ends on that launch's input): one launch more than its sweeps count
     peak, peak_kind = load_peaks()
     mean_sweeps = float(np.mean(sweeps))
     sweeps_per_launch = depth / 2.0 if depth > 0 else 0.5
-    launches_run = mean_sweeps / sweeps_per_launch
+    launches_run = mean_sweeps / sweeps_per_launch + (float(np.mean(conv)) if depth > 0 and sc.tol > 0 else 0.0)
     bytes_per_launch = sc.cells * SWEEP_BYTES_PER_CELL * sweeps_per_launch
     launch_seconds = float(np.mean(sweep_ms)) / 1e3 / launches_run
     achieved = bytes_per_launch / launch_seconds / 1e9 if launch_seconds > 0 else None
