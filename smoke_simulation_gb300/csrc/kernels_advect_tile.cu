@@ -102,7 +102,9 @@ __device__ __forceinline__ float sample_win(const float* __restrict__ f, const G
     }
     const float a100 = sx ? b100 : a000, a110 = sx ? b110 : a010, a101 = sx ? b101 : a001,
                 a111 = sx ? b111 : a011;
-    // trilinear_ref's products as packed pairs (each lane one IEEE product, the same bits)
+    // trilinear_ref's products as packed pairs (each lane one IEEE product, the same bits).  The
+    // products feed products and scalar sums only: ptxas contracts a packed product followed by a
+    // packed add into a fused multiply-add, even with -fmad=false and explicit .rn forms
     const float2 xw = make_float2(xw0, xw1);
     const float2 xy0 = __fmul2_rn(xw, make_float2(yw0, yw0)), xy1 = __fmul2_rn(xw, make_float2(yw1, yw1));
     const float2 z0v = make_float2(zw0, zw0), z1v = make_float2(zw1, zw1);
