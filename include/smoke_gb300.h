@@ -78,6 +78,16 @@ typedef struct smk_params {
                            SMK_SOLVER_JACOBI weighted Jacobi: every cell from the previous
                            iterate, P += (omega/acc) * residual, one iteration per "sweep" (use
                            omega <= 1); the refinement rounds' correction solves stay red-black. */
+    double omega_warm;  /* PRESSURE with warm_start: the over-relaxation of the solves from the
+                           (omega_warm_after + 1)-th step after the pressure history started (at
+                           creation, smk_write_state, or a switch from the REFERENCE scheme); the
+                           earlier steps use omega.  0 (default): omega throughout.  A warm-started
+                           solve corrects the last step's pressure, an error of shorter wavelength
+                           than a cold start's, which a smaller over-relaxation damps in fewer
+                           sweeps (256^3 workload at tol 1e-4: 22.6 instead of 35.3 sweeps per step
+                           with 1.75 after 2 steps).  Single grids, BRANCHES batches and STREAMS
+                           serving; GROUPED batches and ticks use omega throughout. */
+    int omega_warm_after; /* see omega_warm; default 2 */
 } smk_params;
 
 typedef struct smk_stats {

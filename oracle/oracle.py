@@ -127,6 +127,7 @@ class OracleSim:
         self.boxes, self.n_boxes = _objects(scene.boxes, 9)
         self.obstacles, self.n_obstacles = _objects(scene.obstacles, 7)
         self.last = OrcStats()
+        self.hist = 0  # steps since the pressure history started (the library's omega_warm rule)
 
     def _state(self) -> OrcState:
         st = OrcState()
@@ -148,6 +149,10 @@ class OracleSim:
         p.gravity, p.buoyancy, p.clamp_const = sc.gravity, sc.buoyancy, sc.clamp_const
         p.clamp_mode, p.scheme, p.iterations = sc.clamp_mode, self.scheme, sc.iterations
         p.omega, p.tol, p.check_every, p.warm_start = sc.omega, sc.tol, sc.check_every, sc.warm_start
+        # smk_params.omega_warm: warm-started pressure solves from step omega_warm_after on
+        ow, after = getattr(sc, "omega_warm", 0.0), getattr(sc, "omega_warm_after", 2)
+        if self.scheme == 1 and sc.warm_start and ow > 0.0 and self.hist >= after:
+            p.omega = ow
         p.spheres, p.n_spheres = _fptr(self.spheres), self.n_spheres
         p.boxes, p.n_boxes = _fptr(self.boxes), self.n_boxes
         p.obstacles, p.n_obstacles = _fptr(self.obstacles), self.n_obstacles
@@ -165,7 +170,13 @@ class OracleSim:
         fn(C.byref(st), C.byref(p), C.c_float(self.sc.dt if dt is None else dt), C.byref(out))
         self.index_now = st.index_now
         self.last = out
+        self.hist += 1
         return out
+
+    def reset_history(self):
+        """The pressure history starts over (as smk_write_state does): P = 0, omega again."""
+        self.P[...] = 0
+        self.hist = 0
 
     def run(self, steps: Optional[int] = None):
         for _ in range(self.sc.steps if steps is None else steps):

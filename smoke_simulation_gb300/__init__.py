@@ -46,7 +46,7 @@ class Params(C.Structure):
         ("omega", C.c_double), ("tol", C.c_float), ("check_every", C.c_int),
         ("warm_start", C.c_int), ("report_div", C.c_int), ("storage", C.c_int),
         ("refine", C.c_int), ("refine_sweeps", C.c_int), ("obstacle_velocity", C.c_int),
-        ("solver", C.c_int),
+        ("solver", C.c_int), ("omega_warm", C.c_double), ("omega_warm_after", C.c_int),
     ]
 
 
@@ -489,6 +489,7 @@ def params_for_scene(scene, **overrides) -> Params:
     p.refine, p.refine_sweeps = scene.refine, scene.refine_sweeps
     p.obstacle_velocity = scene.obstacle_velocity
     p.solver = scene.solver
+    p.omega_warm, p.omega_warm_after = scene.omega_warm, scene.omega_warm_after
     for k, v in overrides.items():
         setattr(p, k, v)
     return p

@@ -381,6 +381,7 @@ bool grouped_eligible(const smk_batch* b) { return grouped_eligible(b->sims.data
 void after_step(smk_sim* s) {
     s->index_now ^= 1;
     ++s->steps;
+    ++s->hist_steps;
     const bool use_tol = s->p.tol > 0.0f;
     const int G = use_tol ? s->p.check_every : (s->p.max_sweeps > 0 ? s->p.max_sweeps : 1);
     s->last_groups = s->p.max_sweeps > 0 ? (s->p.max_sweeps + G - 1) / G : 0;
@@ -501,10 +502,11 @@ int branches_step(smk_batch* b, const float* dts, float dt_all, cudaStream_t st)
     }
     if (b->exec == nullptr || sig != b->sig) {
         std::vector<int> idx0(n), steps0(n);
-        std::vector<long long> l0(n);
+        std::vector<long long> l0(n), hist0(n);
         for (int i = 0; i < n; ++i) {
             idx0[i] = b->sims[i]->index_now;
             steps0[i] = b->sims[i]->steps;
+            hist0[i] = b->sims[i]->hist_steps;
             l0[i] = b->sims[i]->launches;
         }
         SMK_CUDA(cudaStreamBeginCapture(b->origin, cudaStreamCaptureModeThreadLocal));
@@ -530,6 +532,7 @@ int branches_step(smk_batch* b, const float* dts, float dt_all, cudaStream_t st)
             b->groups[i] = s->last_groups;
             s->index_now = idx0[i];
             s->steps = steps0[i];
+            s->hist_steps = hist0[i];
             s->launches = l0[i];
         }
         if (rc != SMK_OK || ce != cudaSuccess || ee != cudaSuccess) {
@@ -552,6 +555,7 @@ int branches_step(smk_batch* b, const float* dts, float dt_all, cudaStream_t st)
         s->launches += b->branch_launches[i];
         b->launches += b->branch_launches[i];
         ++s->steps;
+        ++s->hist_steps;
         s->last_groups = b->groups[i];
         s->last_projection = s->p.projection;
         s->last_tol = s->p.tol;

@@ -52,6 +52,9 @@ int check_params(const smk_params* p) {
     if (p->refine > 0 && (p->refine_sweeps < 1 || p->refine_sweeps > 100000))
         return fail(SMK_ERR_INVALID, "refine_sweeps must be 1..100000");
     if (p->solver != SMK_SOLVER_RBSOR && p->solver != SMK_SOLVER_JACOBI) return fail(SMK_ERR_INVALID, "unknown solver");
+    if (!std::isfinite(p->omega_warm) || p->omega_warm < 0.0 || p->omega_warm >= 2.0)
+        return fail(SMK_ERR_INVALID, "omega_warm must be 0 (off) or in (0, 2)");
+    if (p->omega_warm_after < 0) return fail(SMK_ERR_INVALID, "omega_warm_after must be >= 0");
     if (p->solver == SMK_SOLVER_JACOBI && p->projection != SMK_PROJECT_PRESSURE)
         return fail(SMK_ERR_INVALID, "the Jacobi solver needs the PRESSURE projection");
     if (p->projection == SMK_PROJECT_PRESSURE && p->tol > 0 &&
@@ -312,7 +315,8 @@ int smk_sim::enqueue(float dt, cudaStream_t st) {
     } else {
         float wacc[7];
         wacc[0] = 0.0f;
-        for (int a = 1; a <= 6; ++a) wacc[a] = (float)p.omega / (float)a;
+        const double om = pressure_omega();  // omega, or omega_warm once the history is long enough
+        for (int a = 1; a <= 6; ++a) wacc[a] = (float)om / (float)a;
         if (bf16)
             launch_rhs(g, (const __nv_bfloat16*)bf(u[now]), (const __nv_bfloat16*)bf(v[now]),
                        (const __nv_bfloat16*)bf(w[now]), flags, b, P, P2, pcur, p.warm_start, st, vec_stages);
@@ -508,6 +512,7 @@ int smk_sim::enqueue(float dt, cudaStream_t st) {
     if (timed) SMK_CUDA(rec(ev[4]));
     SMK_CUDA(cudaGetLastError());
     ++steps;
+    ++hist_steps;
     last_projection = p.projection;
     last_tol = p.tol;
     last_max_sweeps = p.max_sweeps;
@@ -543,6 +548,8 @@ std::string smk_sim::graph_signature(float dt) const {
     auto put = [&sig](const void* p, size_t n) { sig.append(static_cast<const char*>(p), n); };
     put(&dt, sizeof(dt));
     put(&p, sizeof(p));
+    const double om = pressure_omega();  // the over-relaxation this step's solve uses
+    put(&om, sizeof(om));
     put(&sweep_depth, sizeof(sweep_depth));
     put(&sweep_zchunk, sizeof(sweep_zchunk));
     put(&sweep_rows, sizeof(sweep_rows));
@@ -567,12 +574,14 @@ int smk_sim::step(float dt, cudaStream_t st) {
         SMK_CUDA(cudaMemsetAsync(P2, 0, elems() * sizeof(float), st));
         SMK_CUDA(cudaMemsetAsync(pcur, 0, sizeof(int), st));
         pressure_clobbered = false;
+        hist_steps = 0;
     }
     if (!use_graphs || mask_dirty || obstacles_dirty) return enqueue(dt, st);
     GraphSlot& gs = graphs[index_now];
     std::string sig = graph_signature(dt);
     if (gs.exec == nullptr || gs.sig != sig) {
         const int idx0 = index_now, steps0 = steps;
+        const long long hist0 = hist_steps;
         const long long l0 = launches;
         SMK_CUDA(cudaStreamBeginCapture(cap_stream, cudaStreamCaptureModeThreadLocal));
         const int rc = enqueue(dt, cap_stream);
@@ -582,6 +591,7 @@ int smk_sim::step(float dt, cudaStream_t st) {
             if (graph) cudaGraphDestroy(graph);
             index_now = idx0;
             steps = steps0;
+            hist_steps = hist0;
             launches = l0;
             return rc;
         }
@@ -590,6 +600,7 @@ int smk_sim::step(float dt, cudaStream_t st) {
         gs.groups = last_groups;
         index_now = idx0;
         steps = steps0;
+        hist_steps = hist0;
         launches = l0;
         if (gs.exec) cudaGraphExecDestroy(gs.exec);
         gs.exec = nullptr;
@@ -602,6 +613,7 @@ int smk_sim::step(float dt, cudaStream_t st) {
     index_now ^= 1;
     launches += gs.launches;
     ++steps;
+    ++hist_steps;
     last_groups = gs.groups;
     last_projection = p.projection;
     last_tol = p.tol;
@@ -644,6 +656,8 @@ void smk_default_params(smk_params* p) {
     p->storage = SMK_STORAGE_F32;
     p->refine = 0;
     p->refine_sweeps = 10;
+    p->omega_warm = 0.0;
+    p->omega_warm_after = 2;
 }
 
 const char* smk_error_string(int code) {
@@ -918,6 +932,7 @@ int smk_write_state(smk_sim* sim, const smk_host_state* st) {
     SMK_CUDA(cudaMemset(sim->P2, 0, sim->elems() * sizeof(float)));
     SMK_CUDA(cudaMemset(sim->pcur, 0, sizeof(int)));
     SMK_CUDA(cudaDeviceSynchronize());
+    sim->hist_steps = 0;
     return SMK_OK;
 }
 

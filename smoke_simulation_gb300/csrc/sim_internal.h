@@ -98,6 +98,12 @@ struct smk_sim {
     // the blocked velocity sweep used P, P2, b as scratch: a PRESSURE step must restart its
     // pressure from zero (cleared in step(), outside any captured graph)
     bool pressure_clobbered = false;
+    // steps since the pressure history started (creation, smk_write_state, a pressure reset):
+    // decides between omega and omega_warm (pressure_omega)
+    long long hist_steps = 0;
+    double pressure_omega() const {
+        return (p.warm_start && p.omega_warm > 0.0 && hist_steps >= p.omega_warm_after) ? p.omega_warm : p.omega;
+    }
 
     bool timing = false;
     cudaEvent_t ev[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};

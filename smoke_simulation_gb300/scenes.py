@@ -92,6 +92,8 @@ class Scene:
     refine_sweeps: int = 10
     obstacle_velocity: int = 0                 # 1: obstacles' velocity drives the fluid
     solver: int = 0                            # pressure scheme: 0 red-black SOR, 1 Jacobi (omega <= 1)
+    omega_warm: float = 0.0                    # warm-started solves after omega_warm_after steps (0: off)
+    omega_warm_after: int = 2
 
     @property
     def cells(self) -> int:
