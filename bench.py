@@ -158,11 +158,10 @@ def dist_barrier(ws: int):
 
 def workload(n: int, warm_start: int = 1):
     """The 256^3 workload.  The headline solve warm-starts the pressure from the previous step
-    (same red-black SOR, same tolerance rule, so the same max|div| <= 1e-4 guarantee)."""
+    and over-relaxes the warm-started solves with 1.75 from the third step on (same red-black
+    SOR, same tolerance rule, so the same max|div| <= 1e-4 guarantee; scenes.large_workload)."""
     from smoke_simulation_gb300 import scenes as S
-    sc = S.config_large(n=n, steps=50)
-    sc.warm_start = warm_start
-    return sc
+    return S.large_workload(n=n, steps=50, warm_start=warm_start)
 
 
 def cpu_reference_rate(n: int, sweeps: int, steps: int, threads: int = 0):
@@ -446,6 +445,28 @@ def main():
                 "steps": args.cold_steps,
                 "note": "pressure restarted from zero every step, as the reference's projection "
                         "does; same tolerance rule; the first steps of the workload"}
+    # ---- the same warm-started solve with omega 1.9 throughout (no over-relaxation schedule) --
+    fixed = None
+    if args.cold_steps > 0 and sc.warm_start and getattr(sc, "omega_warm", 0.0) > 0.0:
+        sim.set_params(warm_start=1, omega_warm=0.0)
+        fixed_s = 0.0
+        for n in segments(args.cold_steps):
+            sim.write_state(initial)
+            fixed_s += _timed_steps(lambda: sim.step(sc.dt, sh), stream, n, torch)
+        sim.write_state(initial)
+        fixed_sweeps, fixed_conv = [], []
+        for _ in range(min(seg, args.cold_steps)):
+            sim.step(sc.dt, sh)
+            st = sim.stats()
+            fixed_sweeps.append(st.sweeps)
+            fixed_conv.append(st.converged)
+        sim.set_params(omega_warm=sc.omega_warm)
+        fixed = {"value": dist_sum(float(sc.cells * args.cold_steps), ws) / dist_max(fixed_s, ws),
+                 "ms_per_step": 1e3 * fixed_s / args.cold_steps,
+                 "mean_sweeps": float(np.mean(fixed_sweeps)), "converged_frac": float(np.mean(fixed_conv)),
+                 "steps": args.cold_steps,
+                 "note": "warm-started pressure, over-relaxation 1.9 in every step (the reference's "
+                         "constant); same tolerance rule"}
     clk = clocks.stop()
     clk["window_s"] = time.perf_counter() - t_clk0
     clk["window"] = "device-timed, e2e and zero-pressure-start steps of the plain workload"
@@ -504,7 +525,8 @@ def main():
                        "max_div_post_projection": float(np.max(divs)),
                        "max_div_measured": "after every projection of the workload's steps, in a "
                                            "separate pass (the timed steps run without the diagnostic)",
-                       "pressure_start": "warm (previous step's pressure)",
+                       "pressure_start": "warm (previous step's pressure); over-relaxation 1.9 in the "
+                                         "first 2 steps of the history, 1.75 after (smk_params.omega_warm)",
                        # the same workload with the pressure restarted from zero every step (the
                        # reference's projection): the like-for-like comparison with the
                        # reference arm; value / cold_value is what warm starting contributes
@@ -512,8 +534,14 @@ def main():
                        "cold_ms_per_step": cold["ms_per_step"] if cold else None,
                        "cold_mean_sweeps": cold["mean_sweeps"] if cold else None,
                        "warm_start_gain": (value / cold["value"]) if cold else None,
+                       # the same warm-started workload with 1.9 throughout: value / omega_fixed_value
+                       # is what the over-relaxation schedule contributes
+                       "omega_fixed_value": fixed["value"] if fixed else None,
+                       "omega_fixed_mean_sweeps": fixed["mean_sweeps"] if fixed else None,
+                       "omega_schedule_gain": (value / fixed["value"]) if fixed else None,
                        **err_keys,
-                       "cold_start_form": cold},
+                       "cold_start_form": cold,
+                       "omega_fixed_form": fixed},
             "roofline": {"bound": "hbm", "kernel": "%s (z-chunk %d)" % (kname, zchunk),
                          "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": (achieved / peak) if achieved else None, "traffic": traffic,
@@ -683,7 +711,10 @@ def run_forms(args, smk, torch):
                                      ("bf16_all_jacobi", smk.STORAGE_BF16,
                                       {"solver": smk.SOLVER_JACOBI, "omega": 1.0})):
             # FP32 pressure solve with the FP64-checked refinement (2 rounds of 10 sweeps at most)
-            sim = smk.from_scene(sc, report_div=1, storage=storage, refine=2, refine_sweeps=10, **extra)
+            # the SOR forms over-relax warm-started solves with 1.75 from the third step, as the
+            # headline workload does; the Jacobi form keeps its weight
+            sim = smk.from_scene(sc, report_div=1, storage=storage, refine=2, refine_sweeps=10,
+                                 omega_warm=0.0 if extra else 1.75, omega_warm_after=2, **extra)
             sim.autotune()
             sim.step(sc.dt, sh)  # mask upload step (direct launches)
             secs = _timed_steps(lambda: sim.step(sc.dt, sh), stream, args.forms_steps - 1, torch)
@@ -698,7 +729,8 @@ def run_forms(args, smk, torch):
         for name in ("bf16_vel", "bf16_all", "bf16_all_jacobi"):
             mixed[name]["density_rel_l2_vs_f32"] = _rel_l2(rho[name], rho["f32"])
         forms["mixed"] = {"workload": "%d^3, 2%% random solids (seed 3), one 32x8x32 emitter, dt=0.02, "
-                                      "warm-started FP32 pressure red-black SOR to max|div|<=1e-4 (checked every "
+                                      "warm-started FP32 pressure red-black SOR (over-relaxation 1.9, 1.75 from "
+                                      "the third step) to max|div|<=1e-4 (checked every "
                                       "10 sweeps), then max|div| measured with FP64 accumulation and "
                                       "corrected by up to 2 refinement rounds while above 1e-4, %d steps; bf16_vel = u,v,w in BF16 + density FP32, bf16_all = "
                                       "density too; bf16_all_jacobi = all-BF16 with the FP32 weighted-Jacobi solve (weight 1) "

@@ -204,6 +204,17 @@ def config_large(n: int = 256, steps: int = 50, max_sweeps: int = 200, tol: floa
     return sc
 
 
+def large_workload(n: int = 256, steps: int = 50, warm_start: int = 1) -> Scene:
+    """The single-large-grid workload as the benchmark solves it: config_large with the pressure
+    warm-started from the previous step and, once the history is two steps long, over-relaxed
+    with 1.75 instead of 1.9 (smk_params.omega_warm)."""
+    sc = config_large(n=n, steps=steps)
+    sc.warm_start = warm_start
+    if warm_start:
+        sc.omega_warm, sc.omega_warm_after = 1.75, 2
+    return sc
+
+
 def config_batched(count: int = 64, steps: int = 100, seed: int = 2, lo: int = 32, hi: int = 128,
                    scheme: int = 1, iterations: int = 40) -> List[Scene]:
     """Batched plain-precision grids: cube side log-uniform in [lo, hi] (seed 2), each with a

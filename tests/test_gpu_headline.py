@@ -67,8 +67,7 @@ def _within_fp32_tolerances(err):
 def test_large256_bit_exact_with_oracle_and_error_vs_fp64(gpu):
     import torch
     steps = 5
-    sc = S.config_large(n=256, steps=steps)
-    sc.warm_start = 1
+    sc = S.large_workload(n=256, steps=steps)
     tuned = smk.from_scene(sc, report_div=1)
     depth, zchunk, _ = tuned.autotune()
     fixed = smk.from_scene(sc, report_div=1)
