@@ -85,8 +85,8 @@ typedef struct smk_params {
                            solve corrects the last step's pressure, an error of shorter wavelength
                            than a cold start's, which a smaller over-relaxation damps in fewer
                            sweeps (256^3 workload at tol 1e-4: 22.6 instead of 35.3 sweeps per step
-                           with 1.75 after 2 steps).  Single grids, BRANCHES batches and STREAMS
-                           serving; GROUPED batches and ticks use omega throughout. */
+                           with 1.75 after 2 steps).  Every batch form and serving mode follows
+                           it per grid. */
     int omega_warm_after; /* see omega_warm; default 2 */
 } smk_params;
 

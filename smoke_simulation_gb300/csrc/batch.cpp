@@ -169,7 +169,8 @@ void fill_record(smk_sim* s, float dt, TableImage& t, GroupGrid& d) {
     d.lim = p.clamp_const;
     d.clamp_mode = p.clamp_mode;
     d.wacc[0] = 0.0f;
-    for (int a = 1; a <= 6; ++a) d.wacc[a] = (float)p.omega / (float)a;
+    const double om = s->pressure_omega();  // omega, or omega_warm once the history is long enough
+    for (int a = 1; a <= 6; ++a) d.wacc[a] = (float)om / (float)a;
     d.wacc[7] = 0.0f;
     d.tol = p.tol;
     d.check_every = p.check_every > 0 ? p.check_every : 1;
@@ -256,7 +257,8 @@ int build_table(smk_sim* const* sims, int n, const float* dts, float dt_all, con
             smk_sim* sm = sims[t.tb_order[i]];
             float wacc[7];
             wacc[0] = 0.0f;
-            for (int a = 1; a <= 6; ++a) wacc[a] = (float)sm->p.omega / (float)a;
+            const double om = sm->pressure_omega();
+            for (int a = 1; a <= 6; ++a) wacc[a] = (float)om / (float)a;
             t.tb_starts[i] = (int)acc;
             acc += group_tb_fill(&t.tb_recs[rb * i], sm->maps, sm->g, sm->P, sm->P2, sm->status, sm->pcur, sm->kerr,
                                  wacc, sm->p.tol, t.tb_zchunk);

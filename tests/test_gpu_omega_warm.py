@@ -90,3 +90,27 @@ def test_omega_warm_branches_batch_equals_alone(gpu):
     batch.close()
     for s in batch_sims:
         s.close()
+
+
+@pytest.mark.parametrize("blocked", [0, 37])
+def test_omega_warm_grouped_batch_equals_oracle(gpu, blocked):
+    """GROUPED batches (the cooperative colour-pass projection, and the blocked solve) rebuild a
+    member's record when its over-relaxation switches; members stay bit-exact with the oracle."""
+    scs = S.config_batched(count=4, steps=6, seed=9, lo=16, hi=36, scheme=1, iterations=120)
+    for i, sc in enumerate(scs):
+        sc.tol, sc.check_every, sc.warm_start = 2e-4, 6, 1
+        sc.omega_warm, sc.omega_warm_after = 1.75, 1 + (i % 2)
+    sims = [smk.from_scene(sc) for sc in scs]
+    oracles = [O.OracleSim(sc) for sc in scs]
+    batch = smk.Batch(sims, mode=smk.BATCH_GROUPED)
+    batch.set_blocked(blocked)
+    for k in range(5):
+        batch.step([sc.dt for sc in scs])
+        assert batch.info()[0] == smk.BATCH_GROUPED
+        for o in oracles:
+            o.step()
+    for i, (s, o) in enumerate(zip(sims, oracles)):
+        assert H.first_mismatch(s.read_state(), H.oracle_state(o)) == "", i
+    batch.close()
+    for s in sims:
+        s.close()
