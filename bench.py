@@ -408,21 +408,28 @@ def main():
     # ---- e2e through the public API with host buffers ----------------------------------------
     e2e_steps = args.e2e_steps or args.steps
     out = torch.empty(sc.cell_shape, dtype=torch.float32, pin_memory=True).numpy()
-    # warm-up calls (graph capture for this output buffer); the timed segments restart from the
-    # initial state
-    for _ in range(max(args.warmup, 1)):
-        sim.simulate(out, sc.dt)
-    e2e_dt = 0.0
-    for n in segments(e2e_steps):
-        sim.write_state(initial)
-        dist_barrier(ws)
-        t0 = time.perf_counter()
-        for _ in range(n):
-            # the step's input: the emitter positions (launch parameters); result: the density
+
+    def e2e_run(slabs):
+        # smk_simulate with the density copied out in `slabs` slabs during the advection (0: the
+        # copy after the step); warm-up calls capture the graph for this output buffer, and the
+        # timed segments restart from the initial state
+        sim.set_readback_slabs(slabs)
+        for _ in range(max(args.warmup, 1)):
             sim.simulate(out, sc.dt)
-        e2e_dt += time.perf_counter() - t0
-    e2e_dt = dist_max(e2e_dt, ws)
-    e2e_value = dist_sum(float(sc.cells * e2e_steps), ws) / e2e_dt
+        dt_sum = 0.0
+        for n in segments(e2e_steps):
+            sim.write_state(initial)
+            dist_barrier(ws)
+            t0 = time.perf_counter()
+            for _ in range(n):
+                # the step's input: the emitter positions (launch parameters); result: the density
+                sim.simulate(out, sc.dt)
+            dt_sum += time.perf_counter() - t0
+        return dist_sum(float(sc.cells * e2e_steps), ws) / dist_max(dt_sum, ws)
+
+    e2e_copy_after = e2e_run(0)
+    e2e_value = e2e_run(-1)  # the default: the slab count chosen from the grid size
+    readback_slabs = sim.readback_slabs()
 
     # ---- the same solve from a zero pressure every step (the reference's iteration) ---------
     cold = None
@@ -552,7 +559,10 @@ def main():
                                  "achieved can exceed the single-pass roofline"},
             "clocks": clk,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 16 * len(sc.spheres),
-                    "d2h_bytes_per_step": 4 * sc.cells, "api": "smk_simulate (pinned host out)"},
+                    "d2h_bytes_per_step": 4 * sc.cells,
+                    "api": "smk_simulate (pinned host out; the density copied in %d z-slabs while the "
+                           "advection computes)" % readback_slabs,
+                    "copy_after_step_value": e2e_copy_after},
             "gpu_launches": int(launches),
             "cpu_baseline": cpu,
             "forms": forms,
@@ -775,8 +785,8 @@ def run_forms(args, smk, torch):
     if args.serve_requests > 0:
         arr = SV.poisson_stream(args.serve_requests)
 
-        def serve_run(arrivals, budget, slots, **kw):
-            srv = SV.Server(budget_bytes=budget, max_active=slots)
+        def serve_run(arrivals, budget, slots, mode=SV.SERVE_STREAMS, **kw):
+            srv = SV.Server(budget_bytes=budget, max_active=slots, mode=mode)
             wall, _ = SV.drive(srv, arrivals, **kw)
             st = srv.stats()
             srv.close()
@@ -793,6 +803,13 @@ def run_forms(args, smk, torch):
         # the same kind of stream under a budget that binds: admission waits on device memory
         tight = serve_run(arr[:args.serve_tight_requests], int(args.serve_tight_gb * 1e9), 64,
                           storage=smk.STORAGE_BF16_VEL, **ow) if args.serve_tight_requests > 0 else None
+        # the grouped form (one persistent launch per stage over every active request; the solve
+        # blocked, its default) on the first requests of the stream
+        grouped = streams_head = None
+        if args.serve_tight_requests > 0:
+            head = arr[:args.serve_tight_requests]
+            grouped = serve_run(head, 120 * 10**9, 64, mode=SV.SERVE_GROUPED, storage=smk.STORAGE_BF16_VEL, **ow)
+            streams_head = serve_run(head, 120 * 10**9, 64, storage=smk.STORAGE_BF16_VEL, **ow)
         # one request at a time in plain FP32, on every 12th request of the stream (a sample that
         # spans its sizes and step counts): pressure from zero each step, and warm-started
         sample = arr[::12]
@@ -803,12 +820,17 @@ def run_forms(args, smk, torch):
                                         "u,v,w in BF16 (density FP32), warm-started pressure (over-relaxation "
                                         "1.75 from a request's third step), up to 64 "
                                         "resident (120 GB budget), each request's step on its own stream; "
-                                        "tight = the first %d requests under a %.1f GB budget; plain = every "
+                                        "tight = the first %d requests under a %.1f GB budget; grouped = "
+                                        "the same requests in the grouped form (one launch per stage over "
+                                        "every active request, blocked solve), streams_head = those requests "
+                                        "in the default form; plain = every "
                                         "12th request of the stream one at a time, FP32, pressure from zero "
                                         "each step (plain_warm: warm-started); cell-updates/s over host wall "
                                         "time; queue = submission to admission"
                                         % (args.serve_requests, args.serve_tight_requests, args.serve_tight_gb),
-                            "served": serve, "served_tight_budget": tight,
+                            "served": serve, "served_tight_budget": tight, "served_grouped": grouped,
+                            "served_streams_head": streams_head,
+                            "grouped_vs_streams": grouped["value"] / streams_head["value"] if grouped else None,
                             "plain_one_at_a_time": plain1, "plain_warm_one_at_a_time": plain_warm1,
                             "served_vs_plain": serve["value"] / plain1["value"],
                             "served_vs_plain_warm": serve["value"] / plain_warm1["value"]}

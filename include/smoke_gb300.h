@@ -153,8 +153,16 @@ int smk_clear_objects(smk_sim* sim);
  * (:774-811) without its D2H copy. */
 int smk_step(smk_sim* sim, float dt, void* stream);
 /* simulate(float*, dt) (:774-819): one step, then a blocking copy of the new density into
- * host_out (nx*ny*nz floats). */
+ * host_out (nx*ny*nz floats).  When host_out is page-locked (cudaHostAlloc, cudaHostRegister)
+ * and the density is stored in FP32, the copy overlaps the step's advection: the advection runs
+ * in z-slabs and each slab's density planes go to host_out while the next slab computes
+ * (smk_set_readback_slabs).  Otherwise the copy follows the step. */
 int smk_simulate(smk_sim* sim, float* host_out, float dt);
+/* Slabs of smk_simulate's overlapped readback: 1..64, 0 = the copy after the step, -1 (the
+ * default) = one slab per 16 MiB of density, 1 to 8 (4 at 256^3).  The result is the same for
+ * every count.  smk_get_readback_slabs gives the count this simulation uses. */
+int smk_set_readback_slabs(smk_sim* sim, int slabs);
+int smk_get_readback_slabs(const smk_sim* sim, int* slabs);
 /* Copy the current density (the buffer the last step wrote) to host or device memory,
  * stream-ordered; call smk_sync (or synchronise the stream) before reading a host copy. */
 int smk_read_density(smk_sim* sim, float* dst, int dst_on_device, void* stream);
@@ -337,8 +345,9 @@ int smk_server_set_mode(smk_server* server, int mode);
 /* smk_set_graph_loops for the requests admitted from now on (default off: with many request
  * graphs in flight at once, the loop's per-iteration cost exceeds the launches it saves). */
 int smk_server_set_graph_loops(smk_server* server, int enable);
-/* GROUPED form: the blocked solve for the ticks whose requests share a tolerance group size and
- * sweep cap (smk_batch_set_blocked; 0 = cooperative colour passes, the default). */
+/* GROUPED form: the blocked solve, with z-chunks of `zchunk` planes, for the ticks whose requests
+ * share a tolerance group size and sweep cap (smk_batch_set_blocked; default 137; 0 = cooperative
+ * colour passes for every tick). */
 int smk_server_set_blocked(smk_server* server, int zchunk);
 int smk_server_submit(smk_server* server, const smk_request_desc* request, int* id);
 int smk_server_tick(smk_server* server, int* n_active, int* n_queued);

@@ -125,6 +125,8 @@ def lib() -> C.CDLL:
         "smk_set_graph_loops": (i, [vp, i]),
         "smk_set_vector_stages": (i, [vp, i]),
         "smk_set_fused_subtract": (i, [vp, i]),
+        "smk_set_readback_slabs": (i, [vp, i]),
+        "smk_get_readback_slabs": (i, [vp, C.POINTER(i)]),
         "smk_default_render_params": (None, [C.c_void_p]),
         "smk_render": (i, [vp, C.c_void_p, vp, vp, vp]),
         "smk_batch_create": (i, [i, C.POINTER(vp), C.POINTER(vp)]),
@@ -344,6 +346,18 @@ class Simulation:
         """PRESSURE, FP32, blocked sweeps: the gradient subtract inside the solve's last sweep
         launch (default off); results are identical."""
         _check(lib().smk_set_fused_subtract(self.h, 1 if enable else 0))
+
+    def set_readback_slabs(self, slabs: int):
+        """simulate() into page-locked memory: the advection in `slabs` z-slabs, each slab's
+        density copied to the host while the next computes (-1, the default: one slab per
+        16 MiB of density, 1 to 8; 0: the copy after the step); results are identical."""
+        _check(lib().smk_set_readback_slabs(self.h, int(slabs)))
+
+    def readback_slabs(self) -> int:
+        """The slab count simulate() uses on this grid."""
+        n = C.c_int(0)
+        _check(lib().smk_get_readback_slabs(self.h, C.byref(n)))
+        return n.value
 
     def set_sweep_kernel(self, depth: int, zchunk: int = 32, rows: int = 2):
         """Blocked sweep kernel shape: `depth` colour passes per launch, z-chunks of `zchunk`

@@ -185,13 +185,20 @@ struct AdvectMaps;
 AdvectMaps* create_advect_maps(const Grid& g, const float* const* u, const float* const* v, const float* const* w,
                                int n);
 void destroy_advect_maps(AdvectMaps* m);
+// The velocity advection walks the face planes 1 .. nz - 1 in chunks of
+// advect_velocity_chunk_planes() planes (chunk c: planes 1 + c * that .. ); a launch advects the
+// chunks [c0, c1) (c1 < 0: through the last).  The density advection's launch covers cells
+// z = 1 + zz for zz in [z0, z1) (z1 < 0: through nz - 2); cell z reads the advected faces of
+// planes z and z + 1.
 template <typename To>
 int launch_advect_velocity_tile(const AdvectMaps* m, int set, const Grid& g, const float* u0, const float* v0,
                                 const float* w0, To* u1, To* v1, To* w1, const uint8_t* flags, float dt, int* kerr,
-                                cudaStream_t st);
+                                cudaStream_t st, int c0 = 0, int c1 = -1);
+int advect_velocity_chunk_planes();
+int advect_velocity_chunks(const Grid& g);
 template <typename T, typename Tv>
 void launch_advect_density(const Grid& g, const T* r0, T* r1, const Tv* u1, const Tv* v1, const Tv* w1,
-                           const uint8_t* flags, float dt, cudaStream_t st);
+                           const uint8_t* flags, float dt, cudaStream_t st, int z0 = 0, int z1 = -1);
 // BF16 storage form: the projection written in FP32 over every face, and rounded into the state.
 void launch_project_bf16(const Grid& g, __nv_bfloat16* u, __nv_bfloat16* v, __nv_bfloat16* w,
                          const float* P0, const float* P1, const int* pcur, const uint8_t* flags,

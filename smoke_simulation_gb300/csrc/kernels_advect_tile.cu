@@ -120,13 +120,13 @@ __global__ void __launch_bounds__(AT_TX * AT_TY, 4)
 k_advect_velocity_tile(const __grid_constant__ AdvMaps maps, Grid g, const float* __restrict__ u0,
                        const float* __restrict__ v0, const float* __restrict__ w0, To* __restrict__ u1,
                        To* __restrict__ v1, To* __restrict__ w1, const uint8_t* __restrict__ flags, float dt,
-                       int* kerr) {
+                       int* kerr, int cz0) {
     __shared__ alignas(128) float win[AT_SLOTS][3][AT_PSTR];
     __shared__ alignas(8) uint64_t mbar[AT_SLOTS];
     const int tx = (int)threadIdx.x, ty = (int)threadIdx.y;
     const bool leader = tx == 0 && ty == 0;
     const int xt = (int)blockIdx.x * AT_TX, yt = 1 + (int)blockIdx.y * AT_TY;
-    const int zs = 1 + (int)blockIdx.z * AT_ZC;
+    const int zs = 1 + (cz0 + (int)blockIdx.z) * AT_ZC;
     const int ze = min(zs + AT_ZC, g.nz);  // planes [zs, ze) are advected; [zs - 1, ze] are read
     const int wx0 = xt - AT_OX, wy0 = yt - 1;
 
@@ -267,22 +267,30 @@ void destroy_advect_maps(AdvectMaps* m) { delete m; }
 template <typename To>
 int launch_advect_velocity_tile(const AdvectMaps* m, int set, const Grid& g, const float* u0, const float* v0,
                                 const float* w0, To* u1, To* v1, To* w1, const uint8_t* flags, float dt, int* kerr,
-                                cudaStream_t st) {
+                                cudaStream_t st, int c0, int c1) {
     if (m == nullptr || set < 0 || set >= m->n) return -1;
     if (g.nx < 2 || g.ny < 2 || g.nz < 2) return 0;
+    const int chunks = advect_velocity_chunks(g);
+    if (c1 < 0 || c1 > chunks) c1 = chunks;
+    if (c0 < 0) c0 = 0;
+    if (c1 <= c0) return 0;
     const dim3 grid((unsigned)((g.nx + AT_TX - 1) / AT_TX), (unsigned)((g.ny - 1 + AT_TY - 1) / AT_TY),
-                    (unsigned)((g.nz - 1 + AT_ZC - 1) / AT_ZC));
+                    (unsigned)(c1 - c0));
     k_advect_velocity_tile<To><<<grid, dim3(AT_TX, AT_TY), 0, st>>>(m->set[set], g, u0, v0, w0, u1, v1, w1, flags,
-                                                                     dt, kerr);
+                                                                     dt, kerr, c0);
     return 0;
 }
 
+int advect_velocity_chunk_planes() { return AT_ZC; }
+
+int advect_velocity_chunks(const Grid& g) { return g.nz < 2 ? 0 : (g.nz - 1 + AT_ZC - 1) / AT_ZC; }
+
 template int launch_advect_velocity_tile<float>(const AdvectMaps*, int, const Grid&, const float*, const float*,
                                                 const float*, float*, float*, float*, const uint8_t*, float, int*,
-                                                cudaStream_t);
+                                                cudaStream_t, int, int);
 template int launch_advect_velocity_tile<__nv_bfloat16>(const AdvectMaps*, int, const Grid&, const float*,
                                                         const float*, const float*, __nv_bfloat16*,
                                                         __nv_bfloat16*, __nv_bfloat16*, const uint8_t*, float, int*,
-                                                        cudaStream_t);
+                                                        cudaStream_t, int, int);
 
 }  // namespace smk

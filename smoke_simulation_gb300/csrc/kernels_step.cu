@@ -164,10 +164,10 @@ template <typename T, typename Tv>
 __global__ void __launch_bounds__(BX * BY, 8) k_advect_density(Grid g, const T* __restrict__ r0, T* __restrict__ r1,
                                  const Tv* __restrict__ u, const Tv* __restrict__ v,
                                  const Tv* __restrict__ w, const uint8_t* __restrict__ flags,
-                                 float dt, int rz) {
+                                 float dt, int z0, int z1) {
     for (int k = 0; k < ADV_ZC; ++k) {
-        const int zz = (int)blockIdx.z * ADV_ZC + k;
-        if (zz >= rz) break;
+        const int zz = z0 + (int)blockIdx.z * ADV_ZC + k;
+        if (zz >= z1) break;
         body_advect_density(g, r0, r1, u, v, w, flags, dt, make_uint3(blockIdx.x, blockIdx.y, (unsigned)zz));
     }
 }
@@ -323,10 +323,13 @@ void launch_project_velocity(const Grid& g, float* u, float* v, float* w, const 
 template <typename T, typename Tv>
 void launch_advect_density(const Grid& g, const T* r0, T* r1, const Tv* u1,
                            const Tv* v1, const Tv* w1, const uint8_t* flags, float dt,
-                           cudaStream_t st) {
+                           cudaStream_t st, int z0, int z1) {
     if (g.nx < 3 || g.ny < 3 || g.nz < 3) return;
-    k_advect_density<<<grid3(g.nx - 2, g.ny - 2, (g.nz - 2 + ADV_ZC - 1) / ADV_ZC), dim3(BX, BY), 0, st>>>(
-        g, r0, r1, u1, v1, w1, flags, dt, g.nz - 2);
+    if (z1 < 0 || z1 > g.nz - 2) z1 = g.nz - 2;
+    if (z0 < 0) z0 = 0;
+    if (z1 <= z0) return;
+    k_advect_density<<<grid3(g.nx - 2, g.ny - 2, (z1 - z0 + ADV_ZC - 1) / ADV_ZC), dim3(BX, BY), 0, st>>>(
+        g, r0, r1, u1, v1, w1, flags, dt, z0, z1);
 }
 
 void launch_div_max(const Grid& g, const float* u, const float* v, const float* w,
@@ -376,14 +379,14 @@ template void launch_forcing<__nv_bfloat16, float>(const Grid&, __nv_bfloat16*, 
                                                    cudaStream_t, bool);
 template void launch_advect_density<float, float>(const Grid&, const float*, float*, const float*,
                                                   const float*, const float*, const uint8_t*, float,
-                                                  cudaStream_t);
+                                                  cudaStream_t, int, int);
 template void launch_advect_density<float, __nv_bfloat16>(const Grid&, const float*, float*,
                                                           const __nv_bfloat16*, const __nv_bfloat16*,
                                                           const __nv_bfloat16*, const uint8_t*, float,
-                                                          cudaStream_t);
+                                                          cudaStream_t, int, int);
 template void launch_advect_density<__nv_bfloat16, __nv_bfloat16>(const Grid&, const __nv_bfloat16*,
                                                                   __nv_bfloat16*, const __nv_bfloat16*,
                                                                   const __nv_bfloat16*, const __nv_bfloat16*,
-                                                                  const uint8_t*, float, cudaStream_t);
+                                                                  const uint8_t*, float, cudaStream_t, int, int);
 
 }  // namespace smk

@@ -109,7 +109,10 @@ struct smk_server {
     bool started = false;  // the form is fixed once a request was admitted
     cudaStream_t stream = nullptr;
     GroupRunner* runner = nullptr;
-    smk::GroupSchedule sched{0, 4, 0, 0};
+    // GROUPED form: the blocked solve with 137-plane z-chunks (the batch autotuner's choice on a
+    // 64-grid batch of cubes of side 32..128); ticks whose requests do not share a tolerance
+    // group size and sweep cap use the colour passes
+    smk::GroupSchedule sched{0, 4, 0, 137};
     TickRec ticks[2];
     int tick_next = 0;
 };

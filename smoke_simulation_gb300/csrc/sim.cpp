@@ -162,6 +162,9 @@ int smk_sim::alloc() {
     for (auto& e : ev) SMK_CUDA(cudaEventCreate(&e));
     SMK_CUDA(cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking));
     SMK_CUDA(cudaStreamCreateWithFlags(&body_stream, cudaStreamNonBlocking));
+    SMK_CUDA(cudaStreamCreateWithFlags(&rb_stream, cudaStreamNonBlocking));
+    SMK_CUDA(cudaEventCreateWithFlags(&rb_fork, cudaEventDisableTiming));
+    SMK_CUDA(cudaEventCreateWithFlags(&rb_join, cudaEventDisableTiming));
     if (prepare_sweep_kernels() != 0 || prepare_vsweep_kernels() != 0)
         return fail(SMK_ERR_CUDA, "sweep kernel configuration failed");
     // initializeVolume's mask: fluid except the y = 0 floor (smokeSimulation.cu:200-207)
@@ -192,6 +195,9 @@ void smk_sim::release() {
         if (gs.exec) cudaGraphExecDestroy(gs.exec);
     if (cap_stream) cudaStreamDestroy(cap_stream);
     if (body_stream) cudaStreamDestroy(body_stream);
+    if (rb_stream) cudaStreamDestroy(rb_stream);
+    if (rb_fork) cudaEventDestroy(rb_fork);
+    if (rb_join) cudaEventDestroy(rb_join);
 }
 
 int smk_sim::upload_mask(const uint8_t* host) {
@@ -488,27 +494,56 @@ int smk_sim::enqueue(float dt, cudaStream_t st) {
     }
     if (timed) SMK_CUDA(rec(ev[3]));
 
-    // a: advection (:805-810)
-    if (bf16) {
-        if (launch_advect_velocity_tile(amaps, 0, g, pu, pv, pw, bf(u[past]), bf(v[past]), bf(w[past]), flags, dt,
-                                        kerr, st) != 0)
-            return fail(SMK_ERR_CUDA, "velocity advection launch failed");
-        if (rho_bf16)
-            launch_advect_density(g, (const __nv_bfloat16*)bf(rho[now]), bf(rho[past]),
-                                  (const __nv_bfloat16*)bf(u[past]), (const __nv_bfloat16*)bf(v[past]),
-                                  (const __nv_bfloat16*)bf(w[past]), flags, dt, st);
-        else
-            launch_advect_density(g, (const float*)rho[now], rho[past], (const __nv_bfloat16*)bf(u[past]),
-                                  (const __nv_bfloat16*)bf(v[past]), (const __nv_bfloat16*)bf(w[past]),
-                                  flags, dt, st);
-    } else {
-        if (launch_advect_velocity_tile(amaps, now, g, pu, pv, pw, u[past], v[past], w[past], flags, dt, kerr, st) !=
-            0)
-            return fail(SMK_ERR_CUDA, "velocity advection launch failed");
-        launch_advect_density(g, (const float*)rho[now], rho[past], (const float*)u[past],
-                              (const float*)v[past], (const float*)w[past], flags, dt, st);
+    // a: advection (:805-810).  With a host readback (rb_host) it runs in z-slabs: slab s
+    // advects velocity chunks [c0, c1), then the density cells whose faces those chunks
+    // finished (cell z reads the faces of planes z and z + 1), and its density planes go to the
+    // host on rb_stream while the next slab computes.  Every cell's arithmetic is the same.
+    const int chunks = advect_velocity_chunks(g), chunk_planes = advect_velocity_chunk_planes();
+    const int nslab = rb_host ? std::max(1, std::min(readback_slabs(), chunks)) : 1;
+    int zz_done = 0, plane_done = 0;
+    for (int sl = 0; sl < nslab; ++sl) {
+        const bool last_slab = sl == nslab - 1;
+        const int c0 = (int)((long long)chunks * sl / nslab);
+        const int c1 = last_slab ? -1 : (int)((long long)chunks * (sl + 1) / nslab);
+        const int zz1 = last_slab ? -1 : c1 * chunk_planes - 1;  // density cells 1 .. zz1 are ready
+        if (bf16) {
+            if (launch_advect_velocity_tile(amaps, 0, g, pu, pv, pw, bf(u[past]), bf(v[past]), bf(w[past]), flags,
+                                            dt, kerr, st, c0, c1) != 0)
+                return fail(SMK_ERR_CUDA, "velocity advection launch failed");
+            if (rho_bf16)
+                launch_advect_density(g, (const __nv_bfloat16*)bf(rho[now]), bf(rho[past]),
+                                      (const __nv_bfloat16*)bf(u[past]), (const __nv_bfloat16*)bf(v[past]),
+                                      (const __nv_bfloat16*)bf(w[past]), flags, dt, st, zz_done, zz1);
+            else
+                launch_advect_density(g, (const float*)rho[now], rho[past], (const __nv_bfloat16*)bf(u[past]),
+                                      (const __nv_bfloat16*)bf(v[past]), (const __nv_bfloat16*)bf(w[past]),
+                                      flags, dt, st, zz_done, zz1);
+        } else {
+            if (launch_advect_velocity_tile(amaps, now, g, pu, pv, pw, u[past], v[past], w[past], flags, dt, kerr, st,
+                                            c0, c1) != 0)
+                return fail(SMK_ERR_CUDA, "velocity advection launch failed");
+            launch_advect_density(g, (const float*)rho[now], rho[past], (const float*)u[past],
+                                  (const float*)v[past], (const float*)w[past], flags, dt, st, zz_done, zz1);
+        }
+        launches += 2;
+        if (rb_host) {
+            // planes [plane_done, p1) of the density are final: the boundary planes z = 0 and
+            // z = nz - 1 are not written by the advection
+            const int p1 = last_slab ? g.nz : zz1 + 1;
+            SMK_CUDA(cudaEventRecord(rb_fork, st));
+            SMK_CUDA(cudaStreamWaitEvent(rb_stream, rb_fork, 0));
+            auto m = copy3d(rb_host + (size_t)plane_done * g.nx * g.ny, (size_t)g.nx * 4, g.ny,
+                            rho[past] + (size_t)plane_done * g.XY, (size_t)g.X * 4, g.ny + 1, (size_t)g.nx * 4, g.ny,
+                            p1 - plane_done, cudaMemcpyDeviceToHost);
+            SMK_CUDA(cudaMemcpy3DAsync(&m, rb_stream));
+            plane_done = p1;
+        }
+        zz_done = zz1;
     }
-    launches += 2;
+    if (rb_host) {
+        SMK_CUDA(cudaEventRecord(rb_join, rb_stream));
+        SMK_CUDA(cudaStreamWaitEvent(st, rb_join, 0));
+    }
     if (timed) SMK_CUDA(rec(ev[4]));
     SMK_CUDA(cudaGetLastError());
     ++steps;
@@ -557,6 +592,9 @@ std::string smk_sim::graph_signature(float dt) const {
     put(&vsweep_zchunk, sizeof(vsweep_zchunk));
     const char t = timing ? 1 : 0;
     put(&t, 1);
+    put(&rb_host, sizeof(rb_host));  // the host readback's copies are nodes of the graph
+    const int nrb = rb_host ? readback_slabs() : 0;
+    put(&nrb, sizeof(nrb));
     for (const Object& o : objects) put(&o, sizeof(o));
     return sig;
 }
@@ -852,15 +890,51 @@ int smk_sync(smk_sim* sim, void* stream) {
     return check_kernel_error(sim);
 }
 
+// Both ends of [p, p + bytes) lie in page-locked (registered or cudaHostAlloc) host memory.
+static bool pinned_host_range(const void* p, size_t bytes) {
+    const char* ends[2] = {static_cast<const char*>(p), static_cast<const char*>(p) + bytes - 1};
+    for (const char* q : ends) {
+        cudaPointerAttributes a{};
+        if (cudaPointerGetAttributes(&a, q) != cudaSuccess) {
+            cudaGetLastError();
+            return false;
+        }
+        if (a.type != cudaMemoryTypeHost) return false;
+    }
+    return true;
+}
+
 int smk_simulate(smk_sim* sim, float* host_out, float dt) {
     if (!sim || !host_out) return fail(SMK_ERR_INVALID, "null argument");
     DeviceGuard dg(sim->device);
-    int rc = sim->step(dt, (cudaStream_t)0);
-    if (rc) return rc;
-    rc = smk_read_density(sim, host_out, 0, nullptr);
-    if (rc) return rc;
+    const size_t bytes = (size_t)sim->g.nx * sim->g.ny * sim->g.nz * sizeof(float);
+    if (sim->readback_slabs() > 0 && !sim->rho_bf16 && pinned_host_range(host_out, bytes)) {
+        // the density is copied out slab by slab inside the step (smk_set_readback_slabs)
+        sim->rb_host = host_out;
+        const int rc = sim->step(dt, (cudaStream_t)0);
+        sim->rb_host = nullptr;
+        if (rc) return rc;
+    } else {
+        int rc = sim->step(dt, (cudaStream_t)0);
+        if (rc) return rc;
+        rc = smk_read_density(sim, host_out, 0, nullptr);
+        if (rc) return rc;
+    }
     SMK_CUDA(cudaStreamSynchronize((cudaStream_t)0));
     return check_kernel_error(sim);
+}
+
+int smk_set_readback_slabs(smk_sim* sim, int slabs) {
+    if (!sim) return fail(SMK_ERR_INVALID, "sim is null");
+    if (slabs < -1 || slabs > 64) return fail(SMK_ERR_INVALID, "slabs must be in -1..64");
+    sim->rb_slabs = slabs;
+    return SMK_OK;
+}
+
+int smk_get_readback_slabs(const smk_sim* sim, int* slabs) {
+    if (!sim || !slabs) return fail(SMK_ERR_INVALID, "null argument");
+    *slabs = sim->readback_slabs();
+    return SMK_OK;
 }
 
 static int state_copy(smk_sim* sim, const smk_host_state* st, bool to_device) {

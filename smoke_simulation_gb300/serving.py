@@ -99,7 +99,7 @@ class Server:
         _srv_check(_bind().smk_server_set_graph_loops(self.h, 1 if enable else 0))
 
     def set_blocked(self, zchunk: int):
-        """GROUPED form: blocked solve with z-chunks of `zchunk` planes (0: colour passes)."""
+        """GROUPED form: blocked solve with z-chunks of `zchunk` planes (default 137; 0: colour passes)."""
         _srv_check(_bind().smk_server_set_blocked(self.h, int(zchunk)))
 
     def submit(self, scene, steps: Optional[int] = None, params: Optional[Params] = None,

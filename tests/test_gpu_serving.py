@@ -26,13 +26,15 @@ def _alone(sc, steps):
     return rho
 
 
-@pytest.mark.parametrize("mode,blocked", [(SV.SERVE_STREAMS, 0), (SV.SERVE_GROUPED, 0), (SV.SERVE_GROUPED, 17)])
+@pytest.mark.parametrize("mode,blocked", [(SV.SERVE_STREAMS, None), (SV.SERVE_GROUPED, None),
+                                          (SV.SERVE_GROUPED, 0), (SV.SERVE_GROUPED, 17)])
 def test_results_same_alone_and_in_the_mix(gpu, mode, blocked):
     """Each request's result is the same alone and in the mix, in both serving forms, the
-    grouped one with the colour-pass or the blocked solve."""
+    grouped one with its default (the blocked solve, 137-plane z-chunks), the colour passes (0)
+    and 17-plane z-chunks."""
     reqs = _requests()
     srv = SV.Server(budget_bytes=10**10, max_active=3, mode=mode)  # 3 slots: later requests queue
-    if blocked:
+    if blocked is not None:
         srv.set_blocked(blocked)
     ids = [srv.submit(sc, steps) for sc, steps in reqs]
     seen_queue = False
