@@ -284,6 +284,7 @@ def main():
                     help="timed steps of the zero-pressure-start form (0: skip)")
     ap.add_argument("--forms-steps", type=int, default=10, help="timed steps of the batched/mixed forms")
     ap.add_argument("--mixed-n", type=int, default=512, help="mixed-precision grid side (0: skip)")
+    ap.add_argument("--mixed-steps", type=int, default=20, help="steps of the mixed-precision form")
     ap.add_argument("--serve-requests", type=int, default=200, help="serving stream length (0: skip)")
     ap.add_argument("--serve-tight-requests", type=int, default=60,
                     help="requests of the serving run under a binding memory budget (0: skip)")
@@ -714,8 +715,9 @@ def run_forms(args, smk, torch):
 
     # ---- mixed precision at 512^3 -------------------------------------------------------------
     if args.mixed_n > 0:
-        sc = S.config_mixed(args.mixed_n, steps=args.forms_steps)
+        sc = S.config_mixed(args.mixed_n, steps=args.mixed_steps)
         sc.warm_start = 1
+        msteps = max(2, args.mixed_steps)
         mixed = {}
         rho = {}
         for name, storage, extra in (("f32", smk.STORAGE_F32, {}), ("bf16_vel", smk.STORAGE_BF16_VEL, {}),
@@ -726,29 +728,42 @@ def run_forms(args, smk, torch):
             # FP32 pressure solve with the FP64-checked refinement (2 rounds of 10 sweeps at most)
             # the SOR forms over-relax warm-started solves with 1.75 from the third step, as the
             # headline workload does; the Jacobi form keeps its weight
-            sim = smk.from_scene(sc, report_div=1, storage=storage, refine=2, refine_sweeps=10,
-                                 omega_warm=0.0 if extra else 1.75, omega_warm_after=2, **extra)
+            kw = dict(report_div=1, storage=storage, refine=2, refine_sweeps=10,
+                      omega_warm=0.0 if extra else 1.75, omega_warm_after=2, **extra)
+            sim = smk.from_scene(sc, **kw)
             sim.autotune()
             sim.step(sc.dt, sh)  # mask upload step (direct launches)
-            secs = _timed_steps(lambda: sim.step(sc.dt, sh), stream, args.forms_steps - 1, torch)
+            secs = _timed_steps(lambda: sim.step(sc.dt, sh), stream, msteps - 1, torch)
             st = sim.stats()
-            mixed[name] = {"value": float(sc.cells) * (args.forms_steps - 1) / secs,
-                           "ms_per_step": 1e3 * secs / (args.forms_steps - 1), "sweeps_last": st.sweeps,
+            mixed[name] = {"value": float(sc.cells) * (msteps - 1) / secs,
+                           "ms_per_step": 1e3 * secs / (msteps - 1), "sweeps_last": st.sweeps,
                            "converged_last": st.converged,
                            "max_div_post_projection": st.div_max, "max_div_fp64": st.div64_max,
                            "refine_rounds_last": st.refine_rounds}
             rho[name] = sim.read_density()
             sim.close()
+            if not extra:
+                # the same steps again, untimed, for their sweep counts (the runs are deterministic)
+                sim = smk.from_scene(sc, **kw)
+                sim.autotune()
+                sweeps = []
+                for _ in range(msteps):
+                    sim.step(sc.dt, sh)
+                    sweeps.append(sim.stats().sweeps)
+                sim.close()
+                mixed[name]["mean_sweeps"] = float(np.mean(sweeps[1:]))
         for name in ("bf16_vel", "bf16_all", "bf16_all_jacobi"):
             mixed[name]["density_rel_l2_vs_f32"] = _rel_l2(rho[name], rho["f32"])
         forms["mixed"] = {"workload": "%d^3, 2%% random solids (seed 3), one 32x8x32 emitter, dt=0.02, "
                                       "warm-started FP32 pressure red-black SOR (over-relaxation 1.9, 1.75 from "
                                       "the third step) to max|div|<=1e-4 (checked every "
-                                      "10 sweeps), then max|div| measured with FP64 accumulation and "
-                                      "corrected by up to 2 refinement rounds while above 1e-4, %d steps; bf16_vel = u,v,w in BF16 + density FP32, bf16_all = "
+                                      "6 sweeps), then max|div| measured with FP64 accumulation and "
+                                      "corrected by up to 2 refinement rounds while above 1e-4, %d steps (the "
+                                      "first, a mask upload, untimed); bf16_vel = u,v,w in BF16 + density FP32, bf16_all = "
                                       "density too; bf16_all_jacobi = all-BF16 with the FP32 weighted-Jacobi solve (weight 1) "
-                                      "and the same refinement; errors vs the FP64 oracle: tests/test_gpu_headline.py (512^3, 2 steps)"
-                                      % (args.mixed_n, args.forms_steps),
+                                      "and the same refinement; mean_sweeps over the timed steps; errors vs the FP64 "
+                                      "oracle: tests/test_gpu_headline.py (512^3, 2 steps)"
+                                      % (args.mixed_n, msteps),
                           "cells": float(sc.cells), **mixed}
 
     # ---- headless rendering: the reference application's frame ---------------------------------

@@ -104,7 +104,7 @@ def test_large256_bit_exact_with_oracle_and_error_vs_fp64(gpu):
 
 def test_mixed512_forms_error_vs_fp64(gpu):
     """The 512^3 mixed-precision form of the benchmark (2% random solids, one 32x8x32 emitter,
-    dt 0.02, warm-started FP32 pressure SOR to 1e-4 checked every 10 sweeps, FP64-checked
+    dt 0.02, warm-started FP32 pressure SOR to 1e-4 checked every 6 sweeps, FP64-checked
     refinement of up to 2 rounds of 10 sweeps): FP32 storage bit for bit with the FP32
     restatement, and every storage form's density and velocities against the FP64 oracle."""
     import torch
