@@ -444,6 +444,10 @@ int smk_barrier_timeout_report(int* ctas_left, int* ctas);
  * n values: scaled[i] = float(double(x[i]) * omega) and quotient[i] = x[i] / d[i] (d in 1..6) as
  * the kernel computes them without the FP64 pipe (either output may be NULL). */
 int smk_test_exact_arith(const float* x, const int* d, int n, double omega, float* scaled, float* quotient);
+/* Testing: the blocked velocity sweep's per-cell p_t = float(double(x / d) * omega), d = 1..6,
+ * through its branch-free common path and its out-of-line path for rare operands (host
+ * instance). */
+int smk_test_exact_cell(const float* x, const int* d, int n, double omega, float* pt);
 
 #ifdef __cplusplus
 }

@@ -103,8 +103,9 @@ __device__ __forceinline__ CellCoef make_coef(int e) {
 __device__ __forceinline__ float cell_pt(unsigned f, const CellCoef& c, float uc, float ux, float vc, float vy,
                                          float wc, float wz, const OmegaSplit& os, double omega) {
     const float div = -uc + ux + -vc + vy + -wc + wz;
-    const float q = div_small(-div, c.a.x, c.a.y);
-    const float pt = omega_scale(q, os, omega);
+    bool rare;
+    float pt = div_scale_fast(-div, c.a.x, c.a.y, os, rare);
+    if (rare) pt = div_scale_full(-div, c.a.x, c.a.y, os.mo_hi, os.mo_lo, os.eo, os.sign, os.emin, os.emax, omega);
     return (f & F_PROJ) ? pt : 0.0f;
 }
 
@@ -502,6 +503,20 @@ extern "C" int smk_test_exact_arith(const float* x, const int* d, int n, double 
             const int k = d[i] < 1 ? 1 : (d[i] > 6 ? 6 : d[i]);
             quotient[i] = smk::div_small(x[i], (float)k, 1.0f / (float)k);
         }
+    }
+    return 0;
+}
+
+extern "C" int smk_test_exact_cell(const float* x, const int* d, int n, double omega, float* pt) {
+    if (!x || !d || !pt || n < 0) return 1;
+    const smk::OmegaSplit os = smk::omega_split(omega);
+    for (int i = 0; i < n; ++i) {
+        const int k = d[i] < 1 ? 1 : (d[i] > 6 ? 6 : d[i]);
+        const float df = (float)k, r = 1.0f / (float)k;
+        bool rare = false;
+        float v = smk::div_scale_fast(x[i], df, r, os, rare);
+        if (rare) v = smk::div_scale_full(x[i], df, r, os.mo_hi, os.mo_lo, os.eo, os.sign, os.emin, os.emax, omega);
+        pt[i] = v;
     }
     return 0;
 }
