@@ -128,6 +128,10 @@ class OracleSim:
         self.obstacles, self.n_obstacles = _objects(scene.obstacles, 7)
         self.last = OrcStats()
         self.hist = 0  # steps since the pressure history started (the library's omega_warm rule)
+        self.nsteps = 0
+        # smk_params.warm_extrapolate: the last pressure as saved by the previous step's rhs pass
+        self.Ph = None
+        self.ph_step = -2
 
     def _state(self) -> OrcState:
         st = OrcState()
@@ -161,8 +165,26 @@ class OracleSim:
         p.solver = getattr(sc, "solver", 0)
         return p
 
+    def _warm_extrapolate(self):
+        """The library's extrapolated warm start (body_rhs with a pressure history,
+        csrc/stage_bodies.cuh): the last pressure Pl is saved for the next step, and once two
+        solves of the history exist and the previous step saved its Pl, the solve starts from
+        Pl + a * (Pl - Ph) in the field's precision (a = the float factor; the restatement's rhs
+        then zeroes the cells that are not projectable, as the library's does)."""
+        sc = self.sc
+        ea = float(np.float32(getattr(sc, "warm_extrapolate", 0.0)))
+        if not (self.scheme == 1 and sc.warm_start and ea > 0.0):
+            return
+        pl = self.P.copy()
+        if self.hist >= 2 and self.Ph is not None and self.ph_step == self.nsteps - 1:
+            a = self.dtype.type(ea)
+            self.P[...] = pl + a * (pl - self.Ph)
+        self.Ph = pl
+        self.ph_step = self.nsteps
+
     def step(self, dt: Optional[float] = None) -> OrcStats:
         lib = restatement()
+        self._warm_extrapolate()
         st = self._state()
         p = self._params()
         out = OrcStats()
@@ -171,6 +193,7 @@ class OracleSim:
         self.index_now = st.index_now
         self.last = out
         self.hist += 1
+        self.nsteps += 1
         return out
 
     def reset_history(self):

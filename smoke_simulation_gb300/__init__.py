@@ -47,6 +47,7 @@ class Params(C.Structure):
         ("warm_start", C.c_int), ("report_div", C.c_int), ("storage", C.c_int),
         ("refine", C.c_int), ("refine_sweeps", C.c_int), ("obstacle_velocity", C.c_int),
         ("solver", C.c_int), ("omega_warm", C.c_double), ("omega_warm_after", C.c_int),
+        ("warm_extrapolate", C.c_float),
     ]
 
 
@@ -504,6 +505,7 @@ def params_for_scene(scene, **overrides) -> Params:
     p.obstacle_velocity = scene.obstacle_velocity
     p.solver = scene.solver
     p.omega_warm, p.omega_warm_after = scene.omega_warm, scene.omega_warm_after
+    p.warm_extrapolate = scene.warm_extrapolate
     for k, v in overrides.items():
         setattr(p, k, v)
     return p

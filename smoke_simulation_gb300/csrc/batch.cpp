@@ -369,11 +369,13 @@ int launch_config(const GroupSchedule& sched, const TableImage& t, GroupLaunch& 
     return SMK_OK;
 }
 
+// The grouped kernels run the PRESSURE projection's red-black solve from the last pressure: no
+// refinement, moving-boundary velocities, Jacobi solver or extrapolated warm start.
 bool grouped_eligible(smk_sim* const* sims, int n) {
     if (n > MAX_GROUPED) return false;
     for (int i = 0; i < n; ++i)
         if (sims[i]->p.projection != SMK_PROJECT_PRESSURE || sims[i]->p.refine > 0 || sims[i]->p.obstacle_velocity ||
-            sims[i]->p.solver != SMK_SOLVER_RBSOR)
+            sims[i]->p.solver != SMK_SOLVER_RBSOR || sims[i]->p.warm_extrapolate > 0.0f)
             return false;
     return true;
 }
@@ -616,6 +618,8 @@ void group_runner_destroy(GroupRunner* r) {
     }
     delete r;
 }
+
+bool group_runner_eligible(smk_sim* sim) { return grouped_eligible(&sim, 1); }
 
 int group_runner_step(GroupRunner* r, smk_sim* const* sims, const float* dts, int n,
                       const GroupSchedule& sched, cudaStream_t st, int* kernels) {

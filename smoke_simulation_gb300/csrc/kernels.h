@@ -21,7 +21,7 @@ void launch_fill_smoke(const Grid& g, T* rho0, T* rho1, const SphereObj* sp, int
 bool sphere_bounds(const Grid& g, const SphereObj* sp, int ns, int a0[3], int a1[3]);
 void launch_fill_obstacles(const Grid& g, uint8_t* s, const ObstacleObj* ob, int no, cudaStream_t st);
 // Neighbour flags from the mask; zeroes the pressure where a cell is not projectable.
-void launch_build_flags(const Grid& g, const uint8_t* s, uint8_t* flags, float* P, cudaStream_t st);
+void launch_build_flags(const Grid& g, const uint8_t* s, uint8_t* flags, cudaStream_t st);
 
 // Moving-obstacle boundary (smk_params.obstacle_velocity): faces touching a cell of `last`
 // take its velocity.
@@ -40,8 +40,11 @@ void launch_project_velocity(const Grid& g, float* u, float* v, float* w, const 
 
 // Stage c/d (pressure scheme).
 template <typename T>
+// Ph (may be NULL): the pressure history of smk_params.warm_extrapolate (body_rhs), alpha its
+// extrapolation factor for this step (0: start from the last pressure, still saving it).
 void launch_rhs(const Grid& g, const T* u, const T* v, const T* w, const uint8_t* flags,
-                float* b, float* P, const float* P2, const int* pcur, int warm, cudaStream_t st, bool vec = true);
+                float* b, float* P, const float* P2, const int* pcur, int warm, cudaStream_t st, bool vec = true,
+                float* Ph = nullptr, float alpha = 0.0f);
 // One weighted Jacobi iteration Pin -> Pout (see k_jacobi); *pcur = out_idx when it runs.
 void launch_jacobi(const Grid& g, const float* Pin, float* Pout, const float* b, const uint8_t* flags,
                    const float* wacc7, const StepStatus* status, int* pcur, int out_idx, cudaStream_t st);

@@ -31,8 +31,8 @@ template <typename T>
 __global__ void k_rhs(Grid g, const T* __restrict__ u, const T* __restrict__ v,
                       const T* __restrict__ w, const uint8_t* __restrict__ flags,
                       float* __restrict__ b, float* __restrict__ P, const float* __restrict__ P2,
-                      const int* __restrict__ pcur, int warm) {
-    body_rhs(g, u, v, w, flags, b, P, P2, pcur, warm, blockIdx);
+                      const int* __restrict__ pcur, int warm, float* __restrict__ Ph, float alpha) {
+    body_rhs(g, u, v, w, flags, b, P, P2, pcur, warm, blockIdx, Ph, alpha);
 }
 
 // rhs with four consecutive x per thread (vector loads and stores; body_rhs_x4).
@@ -41,9 +41,9 @@ __global__ void __launch_bounds__(256) k_rhs_x4(Grid g, const T* __restrict__ u,
                                                 const T* __restrict__ w, const uint8_t* __restrict__ flags,
                                                 float* __restrict__ b, float* __restrict__ P,
                                                 const float* __restrict__ P2, const int* __restrict__ pcur,
-                                                int warm) {
+                                                int warm, float* __restrict__ Ph, float alpha) {
     body_rhs_x4(g, u, v, w, flags, b, P, P2, pcur, warm, 4 * ((int)blockIdx.x * 32 + (int)threadIdx.x),
-                (int)blockIdx.y * 8 + (int)threadIdx.y, (int)blockIdx.z);
+                (int)blockIdx.y * 8 + (int)threadIdx.y, (int)blockIdx.z, Ph, alpha);
 }
 
 // FP32 gradient subtract with four consecutive x per thread (body_gradient_subtract_x4).
@@ -111,20 +111,21 @@ __global__ void k_resid_check(Grid g, const float* __restrict__ P, const float* 
 
 template <typename T>
 void launch_rhs(const Grid& g, const T* u, const T* v, const T* w, const uint8_t* flags,
-                float* b, float* P, const float* P2, const int* pcur, int warm, cudaStream_t st, bool vec) {
-    if (vec && vec4_layout_of<T>(g, {u, v, w}, {b, P, P2}, flags)) {
+                float* b, float* P, const float* P2, const int* pcur, int warm, cudaStream_t st, bool vec,
+                float* Ph, float alpha) {
+    if (vec && vec4_layout_of<T>(g, {u, v, w}, {b, P, P2, Ph}, flags)) {
         const int groups = (g.nx + 3) / 4;
         k_rhs_x4<T><<<dim3((unsigned)((groups + 31) / 32), (unsigned)((g.ny + 7) / 8), (unsigned)g.nz), dim3(32, 8),
-                      0, st>>>(g, u, v, w, flags, b, P, P2, pcur, warm);
+                      0, st>>>(g, u, v, w, flags, b, P, P2, pcur, warm, Ph, alpha);
         return;
     }
-    k_rhs<<<grid3(g.nx, g.ny, g.nz), dim3(BX, BY), 0, st>>>(g, u, v, w, flags, b, P, P2, pcur, warm);
+    k_rhs<<<grid3(g.nx, g.ny, g.nz), dim3(BX, BY), 0, st>>>(g, u, v, w, flags, b, P, P2, pcur, warm, Ph, alpha);
 }
 template void launch_rhs<float>(const Grid&, const float*, const float*, const float*, const uint8_t*, float*,
-                                float*, const float*, const int*, int, cudaStream_t, bool);
+                                float*, const float*, const int*, int, cudaStream_t, bool, float*, float);
 template void launch_rhs<__nv_bfloat16>(const Grid&, const __nv_bfloat16*, const __nv_bfloat16*,
                                         const __nv_bfloat16*, const uint8_t*, float*, float*, const float*,
-                                        const int*, int, cudaStream_t, bool);
+                                        const int*, int, cudaStream_t, bool, float*, float);
 
 void launch_sweep(const Grid& g, float* P, const float* b, const uint8_t* flags, int colour,
                   const float* wacc7, const StepStatus* status, cudaStream_t st) {

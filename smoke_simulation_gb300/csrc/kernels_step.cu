@@ -86,8 +86,10 @@ __global__ void k_fill_obstacles(Grid g, uint8_t* __restrict__ s, ObstacleList L
     if (val != 2) s[g.idx(x, y, z)] = val;
 }
 
-__global__ void k_build_flags(Grid g, const uint8_t* __restrict__ s, uint8_t* __restrict__ flags,
-                              float* __restrict__ P) {
+// The pressure is left alone: the rhs pass zeroes it on the cells that are not projectable before
+// a solve reads it, so the last solution keeps its values until then (the warm start's history
+// saves it as the solve left it).
+__global__ void k_build_flags(Grid g, const uint8_t* __restrict__ s, uint8_t* __restrict__ flags) {
     int x = blockIdx.x * BX + threadIdx.x;
     int y = blockIdx.y * BY + threadIdx.y;
     int z = blockIdx.z;
@@ -103,7 +105,6 @@ __global__ void k_build_flags(Grid g, const uint8_t* __restrict__ s, uint8_t* __
     bool interior = x >= 1 && y >= 1 && z >= 1 && x <= g.nx - 2 && y <= g.ny - 2 && z <= g.nz - 2;
     if (interior && (f & F_SELF) && (f & F_NBRS)) f |= F_PROJ;
     flags[i] = (uint8_t)f;
-    if (!(f & F_PROJ) && P) P[i] = 0.0f;
 }
 
 // ---- b: integrate (smokeSimulation.cu:315-329) + velocityConfinement (:331-352) ------------
@@ -291,8 +292,8 @@ template void launch_obstacle_velocity<float>(const Grid&, float*, float*, float
 template void launch_obstacle_velocity<__nv_bfloat16>(const Grid&, __nv_bfloat16*, __nv_bfloat16*, __nv_bfloat16*,
                                                       const ObstacleObj&, cudaStream_t);
 
-void launch_build_flags(const Grid& g, const uint8_t* s, uint8_t* flags, float* P, cudaStream_t st) {
-    k_build_flags<<<grid3(g.nx, g.ny, g.nz), dim3(BX, BY), 0, st>>>(g, s, flags, P);
+void launch_build_flags(const Grid& g, const uint8_t* s, uint8_t* flags, cudaStream_t st) {
+    k_build_flags<<<grid3(g.nx, g.ny, g.nz), dim3(BX, BY), 0, st>>>(g, s, flags);
 }
 
 template <typename Tv, typename T>

@@ -531,15 +531,16 @@ static int tick_grouped(smk_server* s) {
         }
     }
     s->peak_queued = std::max(s->peak_queued, (int)s->queue.size());
-    // (3) one grouped step over every active request with steps left (requests on the
-    // reference projection, which the grouped kernels do not run, step on their own)
+    // (3) one grouped step over every active request with steps left (requests whose
+    // parameters the grouped kernels do not run, such as the reference projection, step on
+    // their own)
     std::vector<smk_sim*> grouped;
     std::vector<float> dts;
     std::vector<Request*> members, single;
     for (Request* r : s->active) {
         if (r->steps_issued >= r->steps || r->cancel) continue;
         members.push_back(r);
-        if (r->params.projection == SMK_PROJECT_PRESSURE) {
+        if (group_runner_eligible(r->sim)) {
             grouped.push_back(r->sim);
             dts.push_back(r->dt);
         } else {

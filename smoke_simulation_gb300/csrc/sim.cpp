@@ -55,6 +55,8 @@ int check_params(const smk_params* p) {
     if (!std::isfinite(p->omega_warm) || p->omega_warm < 0.0 || p->omega_warm >= 2.0)
         return fail(SMK_ERR_INVALID, "omega_warm must be 0 (off) or in (0, 2)");
     if (p->omega_warm_after < 0) return fail(SMK_ERR_INVALID, "omega_warm_after must be >= 0");
+    if (!std::isfinite(p->warm_extrapolate) || p->warm_extrapolate < 0.0f || p->warm_extrapolate > 1.0f)
+        return fail(SMK_ERR_INVALID, "warm_extrapolate must be in 0..1");
     if (p->solver == SMK_SOLVER_JACOBI && p->projection != SMK_PROJECT_PRESSURE)
         return fail(SMK_ERR_INVALID, "the Jacobi solver needs the PRESSURE projection");
     if (p->projection == SMK_PROJECT_PRESSURE && p->tol > 0 &&
@@ -97,6 +99,15 @@ static std::atomic<int> g_inject_alloc_failures{0};
 
 // ---- smk_sim --------------------------------------------------------------------------------
 
+int smk_sim::enable_pressure_history() {
+    if (!Ph) {
+        SMK_CUDA(cudaMalloc((void**)&Ph, elems() * sizeof(float)));
+        SMK_CUDA(cudaMemset(Ph, 0, elems() * sizeof(float)));
+    }
+    ph_from = steps;  // saved from the next step on
+    return SMK_OK;
+}
+
 int smk_sim::alloc() {
     const size_t n = elems();
     bf16 = p.storage == SMK_STORAGE_BF16 || p.storage == SMK_STORAGE_BF16_VEL;
@@ -117,6 +128,10 @@ int smk_sim::alloc() {
     for (float** f : fl) {
         SMK_CUDA(cudaMalloc((void**)f, n * sizeof(float)));
         SMK_CUDA(cudaMemset(*f, 0, n * sizeof(float)));
+    }
+    if (p.warm_extrapolate > 0.0f) {
+        const int rc = enable_pressure_history();
+        if (rc) return rc;
     }
     if (bf16) {
         // FP32 projected velocity (what advection consumes); scratch for conversions between steps
@@ -175,7 +190,7 @@ int smk_sim::alloc() {
 }
 
 void smk_sim::release() {
-    float* fl[] = {rho[0], rho[1], u[0], u[1], v[0], v[1], w[0], w[1], P, P2, b, proj[0], proj[1], proj[2]};
+    float* fl[] = {rho[0], rho[1], u[0], u[1], v[0], v[1], w[0], w[1], P, P2, b, proj[0], proj[1], proj[2], Ph};
     for (float* f : fl)
         if (f) cudaFree(f);
     if (pcur) cudaFree(pcur);
@@ -250,7 +265,7 @@ int smk_sim::enqueue(float dt, cudaStream_t st) {
     }
     obstacles_dirty = false;
     if (mask_dirty) {
-        launch_build_flags(g, s, flags, P, st);
+        launch_build_flags(g, s, flags, st);
         ++launches;
         mask_dirty = false;
     }
@@ -323,12 +338,17 @@ int smk_sim::enqueue(float dt, cudaStream_t st) {
         wacc[0] = 0.0f;
         const double om = pressure_omega();  // omega, or omega_warm once the history is long enough
         for (int a = 1; a <= 6; ++a) wacc[a] = (float)om / (float)a;
+        // the extrapolated warm start (smk_params.warm_extrapolate): the rhs pass saves the last
+        // pressure into Ph and starts the solve from its extrapolation
+        float* ph = keeps_history() ? Ph : nullptr;
+        const float alpha = extrapolation();
         if (bf16)
             launch_rhs(g, (const __nv_bfloat16*)bf(u[now]), (const __nv_bfloat16*)bf(v[now]),
-                       (const __nv_bfloat16*)bf(w[now]), flags, b, P, P2, pcur, p.warm_start, st, vec_stages);
+                       (const __nv_bfloat16*)bf(w[now]), flags, b, P, P2, pcur, p.warm_start, st, vec_stages, ph,
+                       alpha);
         else
             launch_rhs(g, (const float*)u[now], (const float*)v[now], (const float*)w[now], flags, b, P, P2,
-                       pcur, p.warm_start, st, vec_stages);
+                       pcur, p.warm_start, st, vec_stages, ph, alpha);
         ++launches;
         const bool use_tol = p.tol > 0.0f;
         const int G = use_tol ? p.check_every : (p.max_sweeps > 0 ? p.max_sweeps : 1);
@@ -568,7 +588,7 @@ int smk_sim::prepare_mask(cudaStream_t st) {
     }
     obstacles_dirty = false;
     if (mask_dirty) {
-        launch_build_flags(g, s, flags, P, st);
+        launch_build_flags(g, s, flags, st);
         ++n;
         mask_dirty = false;
     }
@@ -585,6 +605,10 @@ std::string smk_sim::graph_signature(float dt) const {
     put(&p, sizeof(p));
     const double om = pressure_omega();  // the over-relaxation this step's solve uses
     put(&om, sizeof(om));
+    const float ea = extrapolation();  // and its warm start's extrapolation (a launch parameter)
+    const char kh = keeps_history() ? 1 : 0;
+    put(&ea, sizeof(ea));
+    put(&kh, 1);
     put(&sweep_depth, sizeof(sweep_depth));
     put(&sweep_zchunk, sizeof(sweep_zchunk));
     put(&sweep_rows, sizeof(sweep_rows));
@@ -696,6 +720,7 @@ void smk_default_params(smk_params* p) {
     p->refine_sweeps = 10;
     p->omega_warm = 0.0;
     p->omega_warm_after = 2;
+    p->warm_extrapolate = 0.0f;
 }
 
 const char* smk_error_string(int code) {
@@ -759,7 +784,13 @@ int smk_set_params(smk_sim* sim, const smk_params* params) {
     if (rc) return rc;
     if (params->storage != sim->p.storage)
         return fail(SMK_ERR_INVALID, "the storage precision is fixed when the simulation is created");
+    const bool was = sim->p.warm_extrapolate > 0.0f;
     sim->p = *params;
+    if (params->warm_extrapolate > 0.0f && !was) {
+        DeviceGuard dg(sim->device);
+        rc = sim->enable_pressure_history();
+        if (rc) return rc;
+    }
     return SMK_OK;
 }
 

@@ -104,6 +104,18 @@ struct smk_sim {
     double pressure_omega() const {
         return (p.warm_start && p.omega_warm > 0.0 && hist_steps >= p.omega_warm_after) ? p.omega_warm : p.omega;
     }
+    // smk_params.warm_extrapolate: Ph holds the pressure the previous step's solve started from
+    // (the solution of the step before it), saved by every rhs pass from step ph_from on; a solve
+    // extrapolates once two solves of the history exist and Ph was saved by the previous step
+    float* Ph = nullptr;
+    int ph_from = 0;
+    int enable_pressure_history();
+    bool keeps_history() const {
+        return p.projection == SMK_PROJECT_PRESSURE && p.warm_start && p.warm_extrapolate > 0.0f && Ph != nullptr;
+    }
+    float extrapolation() const {
+        return (keeps_history() && hist_steps >= 2 && steps > ph_from) ? p.warm_extrapolate : 0.0f;
+    }
 
     bool timing = false;
     cudaEvent_t ev[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
@@ -171,6 +183,9 @@ int check_kernel_error(smk_sim* sim);
 namespace smk { struct GroupSchedule; }
 struct GroupRunner;
 GroupRunner* group_runner_create();
+// The simulation can be a member of a grouped step (its parameters are ones the grouped
+// kernels run).
+bool group_runner_eligible(smk_sim* sim);
 void group_runner_destroy(GroupRunner* r);
 // One grouped step of `n` simulations (dts[i] each) on `st` with direct launches; the
 // per-step tables come from a ring of device buffers recycled once their step completed.

@@ -148,10 +148,17 @@ __device__ __forceinline__ void body_forcing(const Grid& g, Tv* __restrict__ u, 
 
 // b = -div(u*) on projectable cells; P = 0 off them (and everywhere on a cold start); on a warm
 // start whose previous solve ended in the second buffer (*pcur == 1) P is taken from there.
+// With a pressure history Ph (smk_params.warm_extrapolate): Ph takes the last pressure Pl of
+// every cell, and a projectable cell starts from Pl + alpha * (Pl - Ph_before) (alpha = 0: Pl).
+__device__ __forceinline__ float warm_extrapolated(float pl, float ph, float alpha) {
+    return alpha != 0.0f ? __fadd_rn(pl, __fmul_rn(alpha, __fsub_rn(pl, ph))) : pl;
+}
+
 template <typename T>
 __device__ __forceinline__ void body_rhs(const Grid& g, const T* u, const T* v, const T* w,
                                          const uint8_t* __restrict__ flags, float* b, float* P,
-                                         const float* P2, const int* pcur, int warm, uint3 bid) {
+                                         const float* P2, const int* pcur, int warm, uint3 bid,
+                                         float* Ph = nullptr, float alpha = 0.0f) {
     const int x = (int)bid.x * SB_BX + (int)threadIdx.x;
     const int y = (int)bid.y * SB_BY + (int)threadIdx.y;
     const int z = (int)bid.z;
@@ -165,8 +172,16 @@ __device__ __forceinline__ void body_rhs(const Grid& g, const T* u, const T* v, 
     const float div = -u0 + u1 + -v0 + v1 + -w0 + w1;
     const bool proj = (f & F_PROJ) != 0;
     b[i] = proj ? -div : 0.0f;
+    const bool from2 = pcur != nullptr && P2 != nullptr && *pcur == 1;
+    if (Ph != nullptr) {
+        const float pl = warm ? (from2 ? P2[i] : P[i]) : 0.0f;
+        const float ph = Ph[i];
+        Ph[i] = pl;
+        P[i] = proj ? warm_extrapolated(pl, ph, alpha) : 0.0f;
+        return;
+    }
     if (!proj || !warm) P[i] = 0.0f;
-    else if (pcur != nullptr && P2 != nullptr && *pcur == 1) P[i] = P2[i];
+    else if (from2) P[i] = P2[i];
 }
 
 // One cell of a colour pass:  r = fma(-acc, P_c, b_c + (((P_x-+P_x+)+(P_y-+P_y+))+(P_z-+P_z+)));
@@ -305,7 +320,8 @@ __device__ __forceinline__ void body_forcing_x4(const Grid& g, Tv* u, Tv* v, Tv*
 template <typename T>
 __device__ __forceinline__ void body_rhs_x4(const Grid& g, const T* u, const T* v, const T* w,
                                             const uint8_t* flags, float* b, float* P, const float* P2,
-                                            const int* pcur, int warm, int x0, int y, int z) {
+                                            const int* pcur, int warm, int x0, int y, int z,
+                                            float* Ph = nullptr, float alpha = 0.0f) {
     if (x0 >= g.nx || y >= g.ny || z >= g.nz) return;
     const int i = g.idx(x0, y, z);
     const bool from2 = warm && pcur != nullptr && P2 != nullptr && *pcur == 1;
@@ -325,6 +341,16 @@ __device__ __forceinline__ void body_rhs_x4(const Grid& g, const T* u, const T* 
         const float d3 = -u0.w + u4 + -v0.w + v1.w + -w0.w + w1.w;
         *reinterpret_cast<float4*>(b + i) =
             make_float4(p0 ? -d0 : 0.0f, p1 ? -d1 : 0.0f, p2 ? -d2 : 0.0f, p3 ? -d3 : 0.0f);
+        if (Ph != nullptr) {
+            const float4 pl = warm ? *reinterpret_cast<const float4*>((from2 ? P2 : P) + i)
+                                   : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            const float4 ph = *reinterpret_cast<const float4*>(Ph + i);
+            *reinterpret_cast<float4*>(Ph + i) = pl;
+            *reinterpret_cast<float4*>(P + i) = make_float4(
+                p0 ? warm_extrapolated(pl.x, ph.x, alpha) : 0.0f, p1 ? warm_extrapolated(pl.y, ph.y, alpha) : 0.0f,
+                p2 ? warm_extrapolated(pl.z, ph.z, alpha) : 0.0f, p3 ? warm_extrapolated(pl.w, ph.w, alpha) : 0.0f);
+            return;
+        }
         if (!warm) {
             *reinterpret_cast<float4*>(P + i) = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         } else if (from2) {
@@ -344,6 +370,13 @@ __device__ __forceinline__ void body_rhs_x4(const Grid& g, const T* u, const T* 
         const float div = -ldv(u, k) + ldv(u, k + 1) + -ldv(v, k) + ldv(v, k + g.X) + -ldv(w, k) + ldv(w, k + g.XY);
         const bool proj = (flags[k] & F_PROJ) != 0;
         b[k] = proj ? -div : 0.0f;
+        if (Ph != nullptr) {
+            const float pl = warm ? (from2 ? P2[k] : P[k]) : 0.0f;
+            const float ph = Ph[k];
+            Ph[k] = pl;
+            P[k] = proj ? warm_extrapolated(pl, ph, alpha) : 0.0f;
+            continue;
+        }
         if (!proj || !warm) P[k] = 0.0f;
         else if (from2) P[k] = P2[k];
     }
