@@ -641,8 +641,10 @@ def run_forms(args, smk, torch):
     scs = S.config_batched(count=64, steps=args.forms_steps)
     for sc in scs:
         sc.tol, sc.check_every, sc.iterations, sc.warm_start = 1e-4, 6, 200, 1
-        # warm-started solves over-relaxed with 1.75 from the third step, as in the headline
+        # warm-started solves over-relaxed with 1.75 from the third step and started from the
+        # extrapolated pressure, as in the headline
         sc.omega_warm, sc.omega_warm_after = 1.75, 2
+        sc.warm_extrapolate = 0.5
     cells = float(sum(sc.cells for sc in scs))
     batched = {}
     dens = {}
@@ -700,8 +702,8 @@ def run_forms(args, smk, torch):
     for s in sims:
         s.close()
     forms["batched"] = {"workload": "64 grids, cube side log-uniform 32..128 (seed 2), sphere solid + box "
-                                    "emitter each, dt=0.05, warm-started pressure (over-relaxation 1.9, 1.75 "
-                                    "from the third step) to max|div|<=1e-4; "
+                                    "emitter each, dt=0.05, warm-started pressure (extrapolated by 0.5, "
+                                    "over-relaxation 1.9, 1.75 from the third step) to max|div|<=1e-4; "
                                     "one persistent launch per stage over all grids (grouped form; the "
                                     "solve as cooperative colour passes or blocked launches over every "
                                     "grid's tiles, whichever the autotuner finds faster), CUDA-graph "
@@ -842,8 +844,9 @@ def run_forms(args, smk, torch):
                     "peak_active": st.peak_active, "peak_queued": st.peak_queued,
                     "peak_gb": st.peak_bytes / 1e9, "budget_gb": budget / 1e9}
 
-        # warm-started solves over-relaxed with 1.75 from each request's third step
-        ow = dict(omega_warm=1.75, omega_warm_after=2)
+        # warm-started solves over-relaxed with 1.75 from each request's third step and started
+        # from the extrapolated pressure
+        ow = dict(omega_warm=1.75, omega_warm_after=2, warm_extrapolate=0.5)
         serve = serve_run(arr, 120 * 10**9, 64, storage=smk.STORAGE_BF16_VEL, **ow)
         # the same kind of stream under a budget that binds: admission waits on device memory
         tight = serve_run(arr[:args.serve_tight_requests], int(args.serve_tight_gb * 1e9), 64,
@@ -862,8 +865,8 @@ def run_forms(args, smk, torch):
         plain_warm1 = serve_run(sample, 120 * 10**9, 1, **ow)
         forms["serving"] = {"workload": "%d requests, Poisson 200/s (seed 4), cube side log-uniform 48..192, "
                                         "50..500 steps, sphere solid + box emitter, tol 1e-4; served with "
-                                        "u,v,w in BF16 (density FP32), warm-started pressure (over-relaxation "
-                                        "1.75 from a request's third step), up to 64 "
+                                        "u,v,w in BF16 (density FP32), warm-started pressure (extrapolated by "
+                                        "0.5, over-relaxation 1.75 from a request's third step), up to 64 "
                                         "resident (120 GB budget), each request's step on its own stream; "
                                         "tight = the first %d requests under a %.1f GB budget; grouped = "
                                         "the same requests in the grouped form (one launch per stage over "

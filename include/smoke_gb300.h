@@ -94,9 +94,8 @@ typedef struct smk_params {
                              the last pressure).  Keeps one more pressure array.  256^3 workload
                              at tol 1e-4: 20.4 instead of 23.1 sweeps per step over the first 20
                              steps with a = 0.5; a = 0.75 and 1 let the solve error grow and are
-                             not stable.  Single-grid steps, BRANCHES batches and STREAMS
-                             serving; a member with it leaves a batch's GROUPED form (the grouped
-                             kernels start from the last pressure). */
+                             not stable.  Every batch form and serving mode follows it per
+                             grid. */
 } smk_params;
 
 typedef struct smk_stats {

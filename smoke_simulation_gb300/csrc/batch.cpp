@@ -156,6 +156,8 @@ void fill_record(smk_sim* s, float dt, TableImage& t, GroupGrid& d) {
     d.b = s->b;
     d.P2 = s->P2;
     d.pcur = s->pcur;
+    d.Ph = s->keeps_history() ? s->Ph : nullptr;  // smk_params.warm_extrapolate
+    d.extrap = s->extrapolation();
     d.flags = s->flags;
     d.status = s->status;
     const bool use_tol = p.tol > 0.0f;
@@ -181,10 +183,10 @@ void fill_record(smk_sim* s, float dt, TableImage& t, GroupGrid& d) {
     if (!s->vec_stages)
         d.vec4 = 0;
     else if (d.kind == GK_F32)
-        d.vec4 = vec4_layout(s->g, {d.u_now, d.v_now, d.w_now, d.rho_now, d.P, d.P2, d.b}, d.flags);
+        d.vec4 = vec4_layout(s->g, {d.u_now, d.v_now, d.w_now, d.rho_now, d.P, d.P2, d.b, d.Ph}, d.flags);
     else
         d.vec4 = vec4_layout_of<h>(s->g, {(const h*)d.u_now, (const h*)d.v_now, (const h*)d.w_now},
-                                   {d.P, d.P2, d.b, d.pu, d.pv, d.pw}, d.flags) &&
+                                   {d.P, d.P2, d.b, d.pu, d.pv, d.pw, d.Ph}, d.flags) &&
                  (d.kind == GK_BF16 ? vec4_layout_of<h>(s->g, {(const h*)d.rho_now}, {}, d.flags)
                                     : vec4_layout(s->g, {d.rho_now}, d.flags));
 
@@ -369,13 +371,13 @@ int launch_config(const GroupSchedule& sched, const TableImage& t, GroupLaunch& 
     return SMK_OK;
 }
 
-// The grouped kernels run the PRESSURE projection's red-black solve from the last pressure: no
-// refinement, moving-boundary velocities, Jacobi solver or extrapolated warm start.
+// The grouped kernels run the PRESSURE projection's red-black solve: no refinement,
+// moving-boundary velocities or Jacobi solver.
 bool grouped_eligible(smk_sim* const* sims, int n) {
     if (n > MAX_GROUPED) return false;
     for (int i = 0; i < n; ++i)
         if (sims[i]->p.projection != SMK_PROJECT_PRESSURE || sims[i]->p.refine > 0 || sims[i]->p.obstacle_velocity ||
-            sims[i]->p.solver != SMK_SOLVER_RBSOR || sims[i]->p.warm_extrapolate > 0.0f)
+            sims[i]->p.solver != SMK_SOLVER_RBSOR)
             return false;
     return true;
 }

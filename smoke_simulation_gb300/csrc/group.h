@@ -57,6 +57,8 @@ struct GroupGrid {
     float* b;
     const float* P2;  // second pressure buffer: a warm start reads it when *pcur == 1
     int* pcur;
+    float* Ph;        // pressure history of the extrapolated warm start (NULL: none)
+    float extrap;     // its factor this step (0: start from the last pressure)
     const uint8_t* flags;
     StepStatus* status;
     int status_words;  // words of *status the step zeroes (header + residual groups)

@@ -318,21 +318,21 @@ __global__ void __launch_bounds__(GROUP_TILE) k_group_project(const GroupArgs a)
                 x4_coords(local, gx, ry, y0, z0, x, y, z);
                 if (d.kind == GK_F32)
                     body_rhs_x4<float>(gg, (const float*)d.u_now, (const float*)d.v_now, (const float*)d.w_now,
-                                       d.flags, d.b, d.P, d.P2, d.pcur, d.warm, x, y, z);
+                                       d.flags, d.b, d.P, d.P2, d.pcur, d.warm, x, y, z, d.Ph, d.extrap);
                 else
                     body_rhs_x4<__nv_bfloat16>(gg, (const __nv_bfloat16*)d.u_now, (const __nv_bfloat16*)d.v_now,
                                                (const __nv_bfloat16*)d.w_now, d.flags, d.b, d.P, d.P2, d.pcur,
-                                               d.warm, x, y, z);
+                                               d.warm, x, y, z, d.Ph, d.extrap);
                 return;
             }
             const uint3 bid = tile_bid(local, d.g.nx, d.g.ny);
             if (d.kind == GK_F32)
                 body_rhs<float>(gg, (const float*)d.u_now, (const float*)d.v_now, (const float*)d.w_now, d.flags,
-                                d.b, d.P, d.P2, d.pcur, d.warm, bid);
+                                d.b, d.P, d.P2, d.pcur, d.warm, bid, d.Ph, d.extrap);
             else
                 body_rhs<__nv_bfloat16>(gg, (const __nv_bfloat16*)d.u_now, (const __nv_bfloat16*)d.v_now,
                                         (const __nv_bfloat16*)d.w_now, d.flags, d.b, d.P, d.P2, d.pcur, d.warm,
-                                        bid);
+                                        bid, d.Ph, d.extrap);
         });
         if (!group_barrier(a, target)) {
             group_abort(a);

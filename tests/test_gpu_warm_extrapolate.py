@@ -7,8 +7,8 @@ OracleSim).  These tests hold every field of both buffers, the sweep counts and 
 it bit for bit: for the blocked kernels, the one-colour-pass kernel and the Jacobi solver, in
 graph replay with and without the device-side group loop and as direct launches, across a state
 write (which restarts the history), when the option is switched on between steps, with an
-obstacle moving every step, for members of a BRANCHES batch, and for a batch or serving form that
-groups its members (an extrapolating member steps on its own).
+obstacle moving every step, for members of BRANCHES and GROUPED batches (the cooperative
+colour passes and the blocked solve), and in the GROUPED serving form.
 """
 import numpy as np
 import pytest
@@ -128,31 +128,36 @@ def test_extrapolated_warm_start_moving_obstacle(gpu, graphs):
     sim.close()
 
 
-def test_extrapolated_warm_start_in_batches(gpu):
-    """A BRANCHES batch steps each member as alone; a batch asked for the default form with an
-    extrapolating member runs as branches (the grouped kernels start from the last pressure)."""
+@pytest.mark.parametrize("mode,blocked", [(smk.BATCH_BRANCHES, 0), (smk.BATCH_GROUPED, 0),
+                                          (smk.BATCH_GROUPED, 37)])
+def test_extrapolated_warm_start_in_batches(gpu, mode, blocked):
+    """BRANCHES and GROUPED batches (the cooperative colour passes and the blocked solve) step
+    each member as the oracle does alone: members with different factors, one without."""
     scs = [_scene(), S.small_scene(30, 34, 28, steps=6, seed=31, scheme=1, iterations=150, tol=2e-4,
-                                   check_every=6, warm_start=1)]
+                                   check_every=6, warm_start=1),
+           S.small_scene(24, 20, 26, steps=6, seed=33, scheme=1, iterations=150, tol=2e-4, check_every=6,
+                         warm_start=1)]
     scs[1].warm_extrapolate = 0.35
-    for mode in (smk.BATCH_BRANCHES, None):
-        sims = [smk.from_scene(sc) for sc in scs]
-        oracles = [O.OracleSim(sc) for sc in scs]
-        batch = smk.Batch(sims) if mode is None else smk.Batch(sims, mode=mode)
-        for _ in range(5):
-            batch.step([sc.dt for sc in scs])
-            assert batch.info()[0] == smk.BATCH_BRANCHES
-            for o in oracles:
-                o.step()
-        for s, o in zip(sims, oracles):
-            assert H.first_mismatch(s.read_state(), H.oracle_state(o)) == ""
-        batch.close()
-        for s in sims:
-            s.close()
+    sims = [smk.from_scene(sc) for sc in scs]
+    oracles = [O.OracleSim(sc) for sc in scs]
+    batch = smk.Batch(sims, mode=mode)
+    if blocked:
+        batch.set_blocked(blocked)
+    for _ in range(5):
+        batch.step([sc.dt for sc in scs])
+        assert batch.info()[0] == mode
+        for o in oracles:
+            o.step()
+    for i, (s, o) in enumerate(zip(sims, oracles)):
+        assert H.first_mismatch(s.read_state(), H.oracle_state(o)) == "", i
+    batch.close()
+    for s in sims:
+        s.close()
 
 
-def test_grouped_serving_steps_an_extrapolating_request_on_its_own(gpu):
-    """In the GROUPED serving form a request with the extrapolated warm start steps on its own
-    (the others stay grouped); every result equals the request alone."""
+def test_grouped_serving_with_an_extrapolating_request(gpu):
+    """In the GROUPED serving form a request with the extrapolated warm start is stepped in the
+    grouped ticks with the others; every result equals the request alone."""
     arr = SV.poisson_stream(4, rate=1e6, seed=21, lo=12, hi=40, steps_lo=3, steps_hi=9)
     reqs = [(a.scene, a.steps) for a in arr]
     reqs[1][0].warm_extrapolate = 0.5
