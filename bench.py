@@ -760,6 +760,8 @@ def run_forms(args, smk, torch):
             # FP32 pressure solve with the FP64-checked refinement (2 rounds of 10 sweeps at most)
             # the SOR forms over-relax warm-started solves with 1.75 from the third step, as the
             # headline workload does; the Jacobi form keeps its weight
+            # (started from the last pressure: the extrapolated start helps the FP32 form, 10.21
+            # against 10.08 G, and costs the BF16 forms, 9.84 / 9.90 against 10.03 / 10.09 G)
             kw = dict(report_div=1, storage=storage, refine=2, refine_sweeps=10,
                       omega_warm=0.0 if extra else 1.75, omega_warm_after=2, **extra)
             sim = smk.from_scene(sc, **kw)
@@ -787,8 +789,9 @@ def run_forms(args, smk, torch):
         for name in ("bf16_vel", "bf16_all", "bf16_all_jacobi"):
             mixed[name]["density_rel_l2_vs_f32"] = _rel_l2(rho[name], rho["f32"])
         forms["mixed"] = {"workload": "%d^3, 2%% random solids (seed 3), one 32x8x32 emitter, dt=0.02, "
-                                      "warm-started FP32 pressure red-black SOR (over-relaxation 1.9, 1.75 from "
-                                      "the third step) to max|div|<=1e-4 (checked every "
+                                      "warm-started FP32 pressure red-black SOR (from the last pressure, "
+                                      "over-relaxation 1.9, 1.75 from the third step) to max|div|<=1e-4 "
+                                      "(checked every "
                                       "6 sweeps), then max|div| measured with FP64 accumulation and "
                                       "corrected by up to 2 refinement rounds while above 1e-4, %d steps (the "
                                       "first, a mask upload, untimed); bf16_vel = u,v,w in BF16 + density FP32, bf16_all = "

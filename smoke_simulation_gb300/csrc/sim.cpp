@@ -144,6 +144,8 @@ int smk_sim::alloc() {
     SMK_CUDA(cudaMalloc((void**)&pcur, 4 * sizeof(int)));
     SMK_CUDA(cudaMemset(pcur, 0, 4 * sizeof(int)));
     kerr = pcur + 1;
+    SMK_CUDA(cudaHostAlloc((void**)&kerr_host, sizeof(int), cudaHostAllocDefault));
+    *kerr_host = 0;
     gcount = pcur + 2;
     SMK_CUDA(cudaMalloc((void**)&loop_launches, sizeof(unsigned long long)));
     SMK_CUDA(cudaMemset(loop_launches, 0, sizeof(unsigned long long)));
@@ -194,6 +196,7 @@ void smk_sim::release() {
     for (float* f : fl)
         if (f) cudaFree(f);
     if (pcur) cudaFree(pcur);
+    if (kerr_host) cudaFreeHost(kerr_host);
     if (loop_launches) cudaFree(loop_launches);
     if (refine) cudaFree(refine);
     if (render_scratch) cudaFree(render_scratch);
@@ -951,8 +954,10 @@ int smk_simulate(smk_sim* sim, float* host_out, float dt) {
         rc = smk_read_density(sim, host_out, 0, nullptr);
         if (rc) return rc;
     }
+    // the error word travels with the step's copies: one synchronisation for both
+    SMK_CUDA(cudaMemcpyAsync(sim->kerr_host, sim->kerr, sizeof(int), cudaMemcpyDeviceToHost, (cudaStream_t)0));
     SMK_CUDA(cudaStreamSynchronize((cudaStream_t)0));
-    return check_kernel_error(sim);
+    return *sim->kerr_host ? check_kernel_error(sim) : SMK_OK;
 }
 
 int smk_set_readback_slabs(smk_sim* sim, int slabs) {

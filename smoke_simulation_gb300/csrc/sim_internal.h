@@ -66,6 +66,7 @@ struct smk_sim {
     float* b = nullptr;
     int* pcur = nullptr;  // device: which pressure buffer the last executed sweep wrote
     int* kerr = nullptr;  // device: a bounded wait in a kernel gave up (sticky until read)
+    int* kerr_host = nullptr;  // page-locked: *kerr as copied at the end of an smk_simulate step
     int* gcount = nullptr;  // device: tolerance groups done by a graph's device-side group loop
     unsigned long long* loop_launches = nullptr;  // device: kernels launched by those loops
     smk::RefineStatus* refine = nullptr;          // device: FP64-checked refinement rounds
