@@ -244,3 +244,39 @@ def test_jacobi_reaches_the_sor_solution():
             x, y = getattr(a, k)[j], getattr(b, k)[j]
             assert H.rel_l2(x, y) < 1e-5, (k, j, H.rel_l2(x, y))
     assert min(out[1][1]) > max(out[0][1])
+
+
+def _extrap_scene(a):
+    sc = S.small_scene(24, 22, 26, steps=6, seed=19, scheme=1, iterations=120, tol=1e-4, check_every=3,
+                       warm_start=1)
+    sc.warm_extrapolate = a
+    return sc
+
+
+def test_warm_extrapolate_rule():
+    """The extrapolated warm start as the library applies it (body_rhs with a pressure history):
+    the first two steps of a history start from the last pressure (identical to a = 0), the third
+    starts from P + a (P - P_before) computed in float32, and a history switched on between
+    steps is saved by the next step and used one step later."""
+    plain = O.OracleSim(_extrap_scene(0.0))
+    ext = O.OracleSim(_extrap_scene(0.5))
+    for k in range(2):
+        plain.step()
+        ext.step()
+        assert np.array_equal(plain.P, ext.P) and H.first_mismatch(H.oracle_state(plain), H.oracle_state(ext)) == ""
+    # the start of step 3, restated from the two saved solutions
+    p1 = ext.P.copy()
+    p0 = ext.Ph.copy()
+    want = p1 + np.float32(0.5) * (p1 - p0)
+    ext._warm_extrapolate()
+    assert np.array_equal(ext.P, want) and not np.array_equal(want, p1)
+    # switched on after two plain steps: step 3 saves, step 4 extrapolates
+    late = O.OracleSim(_extrap_scene(0.0))
+    ref = O.OracleSim(_extrap_scene(0.0))
+    for k in range(4):
+        if k == 2:
+            late.sc.warm_extrapolate = 0.5
+        late.step()
+        ref.step()
+        same = H.first_mismatch(H.oracle_state(late), H.oracle_state(ref)) == ""
+        assert same == (k < 3), k
