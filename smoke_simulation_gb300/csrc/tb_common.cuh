@@ -104,7 +104,7 @@ __host__ __device__ inline void sweep_window(int n, int W, int T, int k, int& st
 
 // Host: a 3-D tiled TMA tensor map over one field of grid g (X x (ny+1) x (nz+1) elements, 4-byte
 // floats or bytes), boxes of BOX_F (BOX_U8) x rows x 1; false when the base is null or not
-// 16-byte aligned or the driver refuses the map.  Defined in kernels_sweep_tb.cu.
+// 16-byte aligned or cuTensorMapEncodeTiled refuses the map.  Defined in kernels_sweep_tb.cu.
 bool encode_3d(CUtensorMap* m, const void* base, bool is_u8, const Grid& g, int rows);
 // The same with a box box_w elements wide (box_w x element size a multiple of 16 bytes).
 bool encode_3d_box(CUtensorMap* m, const void* base, bool is_u8, const Grid& g, int box_w, int rows);
